@@ -1,0 +1,364 @@
+#!/usr/bin/env python
+"""Benchmark: batched American-option pricing, options/s at 101 x 498, FP64.
+
+Workload (one "step" = one pass of the hot path over the batch):
+  65,536 American options, puts and calls alternating, spot 100,
+  K~U[80,120], T~U[0.1,2], sigma~U[0.1,0.5], r~U[0,0.08], q~U[0,0.04]
+  (seeded), each on the reference's sinh-clustered grid pinned to
+  101 space points x 498 time steps (estimate_pde_grid with
+  min = max = 101, PDEGridConfig n_time = 498).  Synthetic data.
+
+  value : options/s with the batch resident in device memory (setup +
+          march + outputs kernels per step; ~1.4 GB of per-option state,
+          far above the 129 MB L2, so no flush is needed between steps).
+  e2e   : options/s through the C ABI call mango_gpu_price_american_batch
+          with host arrays: validation, grid generation, H2D, kernels, D2H.
+  roofline: the march kernel against the FP64 FMA rate measured live on the
+          same GPU (mango_gpu_fp64_probe).
+  cpu_baseline: the oracle's C restatement of the reference's per-option
+          loop (OpenMP over all host cores) on a bounded sample.
+
+--impl reference: the reference's CPU implementation of the same path on
+the host cores (the C restatement; the reference's own build is not
+available on the GPU host), same metric and config.
+
+Multi-GPU (--gpus N under torchrun): replicas only -- every option is
+independent, each rank prices its own copy of the batch, no collective on
+the data path; value = options priced by all ranks / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_OPTIONS = 65536
+NX, NT = 101, 498
+METRIC = "options/s @101x498 FP64 (batched American pricing with value/delta/gamma/theta)"
+
+
+def make_workload(pkg, n, seed=20251203, uneven=False):
+    rng = np.random.default_rng(seed)
+    S = np.full(n, 100.0)
+    K = rng.uniform(80, 120, n)
+    T = rng.uniform(0.1, 2.0, n)
+    sig = rng.uniform(0.1, 0.5, n)
+    r = rng.uniform(0.0, 0.08, n)
+    q = rng.uniform(0.0, 0.04, n)
+    put = (np.arange(n) % 2 == 0).astype(np.int32)
+    params = pkg.pricing_array(S, K, T, sig, r, q, put)
+    if uneven:
+        nx = rng.integers(51, 402, n)
+        nt = rng.integers(100, 1001, n)
+        grids = pkg.grid_array(n, pkg.GRID_FIXED_N, nx, nt)
+    else:
+        grids = pkg.grid_array(1, pkg.GRID_FIXED_N, NX, NT)
+    return params, grids, (S, K, T, sig, r, q, put)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def reduce_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def load_oracle():
+    """The CPU implementation of the reference's path for the baseline legs:
+    the reference's own build when it is loadable here, else the C
+    restatement (the GPU host never has the reference tree)."""
+    import importlib.util
+    ref = ROOT / "oracle" / "_ref" / "libmango_ref.so"
+    try:
+        if ref.exists():
+            return ctypes.CDLL(str(ref)), "reference", "ref_price_batch"
+    except OSError:
+        pass
+    spec = importlib.util.spec_from_file_location("_b", ROOT / "mango-option_gb300" / "build.py")
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    return ctypes.CDLL(str(b.build_oracle())), "port", "mo_price_batch"
+
+
+def cpu_price(lib, fn, cols, nx, nt, threads):
+    S, K, T, sig, r, q, put = (np.ascontiguousarray(c) for c in cols)
+    n = len(S)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    nxa = np.full(n, nx, np.int64)
+    nta = np.full(n, nt, np.int64)
+    out = np.zeros(4 * n)
+    st = np.zeros(n, np.int32)
+    t0 = time.perf_counter()
+    getattr(lib, fn)(ctypes.c_int64(n), P(S), P(K), P(T), P(sig), P(r), P(q), P(put.astype(np.int32)), P(nxa),
+                     P(nta), ctypes.c_int32(1), ctypes.c_int32(threads), P(out), None, P(st))
+    return time.perf_counter() - t0, out.reshape(n, 4)
+
+
+def cpu_sample(lib, fn, cols, threads, target_s=2.0):
+    """Options/s of the CPU path on a bounded sample sized to ~target_s wall."""
+    m = 64
+    while True:
+        sub = [c[:m] for c in cols]
+        t, _ = cpu_price(lib, fn, sub, NX, NT, threads)
+        if t > target_s / 4 or m >= len(cols[0]):
+            break
+        m = min(len(cols[0]), m * 4)
+    return m / t, m, t
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mango_option_gb300", ROOT / "mango-option_gb300" / "__init__.py")
+    pkg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(pkg)
+    _, _, cols = make_workload(pkg, N_OPTIONS)
+    lib, kind, fn = load_oracle()
+    threads = os.cpu_count() or 1
+    _, m, _ = cpu_sample(lib, fn, cols, threads, target_s=1.0)
+    for _ in range(args.warmup):
+        cpu_price(lib, fn, [c[:m] for c in cols], NX, NT, threads)
+    times = []
+    for _ in range(args.steps):
+        t, _ = cpu_price(lib, fn, [c[:m] for c in cols], NX, NT, threads)
+        times.append(t)
+    total = sum(times)
+    value = m * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "options/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{N_OPTIONS} American puts/calls, 101x498 grid rule (bounded sample of {m} per step)",
+                   "options_per_step": m},
+        "cpu_baseline": {"value": value, "unit": "options/s", "cores": threads, "kind": kind,
+                         "sample": f"first {m} options of the {N_OPTIONS}-option workload per step"},
+        "e2e": {"value": value, "unit": "options/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--options", type=int, default=N_OPTIONS)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extra", action="store_true", help="skip the uneven-grid side measurement")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    eng = pkg.Engine(local)
+    stream = torch.cuda.current_stream()
+    eng.set_stream(stream.cuda_stream)
+    fp64_peak = eng.fp64_probe()
+
+    n = args.options
+    params, grids, cols = make_workload(pkg, n)
+    batch = eng.batch(params, grids)
+    for _ in range(max(3, args.warmup)):
+        batch.run()
+    torch.cuda.synchronize()
+    warm = batch.results()
+    assert (warm["status"] == 0).all(), "warm-up batch reported failures"
+    batch.timings(reset=True)
+
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.3)
+    barrier(ws)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        batch.run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    clocks = clk.stop()
+    t_dev = reduce_max(e0.elapsed_time(e1) / 1e3, ws)
+    kt = batch.timings()
+    value = n * ws * args.steps / t_dev
+
+    # End to end through the C ABI with host arrays.
+    for _ in range(2):
+        eng.price_arrays(params, grids)
+    torch.cuda.synchronize()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        out = eng.price_arrays(params, grids)
+    t_e2e = reduce_max(time.perf_counter() - t0, ws)
+    st = eng.stats()
+    e2e = {"value": n * ws * args.steps / t_e2e, "unit": "options/s",
+           "h2d_bytes_per_step": int(st["h2d_bytes"]), "d2h_bytes_per_step": int(st["d2h_bytes"]),
+           "ms_per_step": 1e3 * t_e2e / args.steps,
+           "breakdown_ms": {k: round(st[k], 3) for k in ("host_prep_ms", "h2d_ms", "prep_ms", "march_ms",
+                                                        "outputs_ms", "d2h_ms", "total_ms")}}
+    assert (out["status"] == 0).all()
+
+    # Roofline of the dominant kernel (the march).
+    algo = st["algo_flops"]
+    march_s = kt["march_ms"] / 1e3
+    achieved = algo / march_s / 1e12
+    traffic = None
+    tf = ROOT / "profiles" / "march_kernel_traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get("bytes_per_launch")
+        except Exception:
+            traffic = None
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak, "traffic": traffic,
+                "peak_source": "measured live: mango_gpu_fp64_probe (independent DFMA chains, all SMs)",
+                "kernel": "march_kernel", "kernel_ms": kt["march_ms"],
+                "algo_flops_per_launch": algo}
+
+    extra = {}
+    if not args.no_extra and rank == 0:
+        p2, g2, _ = make_workload(pkg, n, seed=77, uneven=True)
+        b2 = eng.batch(p2, g2)
+        b2.run()
+        torch.cuda.synchronize()
+        b2.timings(reset=True)
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(2):
+            b2.run()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        tu = f0.elapsed_time(f1) / 1e3
+        o2 = b2.results()
+        kt2 = b2.timings()
+        algo2 = eng.stats()["algo_flops"]
+        extra["uneven_grids"] = {
+            "workload": f"{n} puts/calls, N_x~U{{51..401}}, N_t~U{{100..1000}}, one persistent launch",
+            "value": 2 * n / tu, "unit": "options/s", "failed": int(np.count_nonzero(o2["status"])),
+            "march_ms": kt2["march_ms"], "fp64_frac": algo2 / (kt2["march_ms"] / 1e3) / 1e12 / fp64_peak}
+        b2.close()
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        lib, kind, fn = load_oracle()
+        threads = os.cpu_count() or 1
+        v, m, t = cpu_sample(lib, fn, cols, threads)
+        cpu = {"value": v, "unit": "options/s", "cores": threads, "kind": kind,
+               "sample": f"first {m} options of the workload, 101x498, {t:.2f} s wall on {threads} threads"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "options/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{n} American puts/calls (50/50), 101x498 sinh grid rule, FP64",
+                       "options": n, "n_space": NX, "n_time": NT, "parallelism": f"replicas x{ws}",
+                       "l2": "no flush: per-step device state ~1.4 GB >> 129 MB L2"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": 3 * args.steps,
+            "kernel_ms_per_step": {k: round(kt[k], 4) for k in ("prep_ms", "march_ms", "outputs_ms")},
+            **extra,
+        }
+        print(json.dumps(line), flush=True)
+    batch.close()
+    eng.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,253 @@
+/* mango_gpu.h -- C ABI of the GB300 (sm_103a) batched American-option engine.
+ *
+ * Additive to the reference's stable C ABI (src/ffi/mango_c_api.h): the value
+ * types below are the reference's own (same names, same layout, asserted at
+ * the end of this file), so a caller that already fills MangoPricingParams /
+ * MangoIvQuery for mango_price_american / mango_solve_iv passes the same
+ * arrays here.  Include src/ffi/mango_c_api.h FIRST when using both headers;
+ * its include guard then suppresses the duplicate type definitions below.
+ *
+ * Conventions follow the reference ABI (src/ffi/mango_c_api.h:16-28,
+ * src/ffi/mango_c_api.cpp:23-31, 354-366, 523-576): functions return a
+ * MangoStatus, an optional MangoError* receives a code and a 256-byte
+ * message, batch calls never abort the whole batch (a per-slot status plus a
+ * failed count), and no exception crosses the boundary.  Every batch call is
+ * synchronous with respect to the caller's host buffers.
+ *
+ * Scope (the reference's hot path): constant rate and continuous dividend
+ * yield.  Yield curves and discrete dividends are rejected per slot with
+ * MANGO_ERR_VALIDATION and a message naming the unsupported feature.
+ */
+#ifndef MANGO_GPU_H
+#define MANGO_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef MANGO_C_API_H
+/* ---- value types shared with src/ffi/mango_c_api.h:16-139 ---- */
+typedef int32_t MangoStatus;
+#define MANGO_OK 0
+#define MANGO_ERR_VALIDATION 1
+#define MANGO_ERR_ARBITRAGE 2
+#define MANGO_ERR_NO_CONVERGENCE 3
+#define MANGO_ERR_BRACKETING 4
+#define MANGO_ERR_SOLVER 5
+
+typedef int32_t MangoOptionType;
+#define MANGO_CALL 0
+#define MANGO_PUT 1
+
+typedef struct { int32_t code; char message[256]; } MangoError;
+typedef struct { double calendar_time; double amount; } MangoDividend;
+typedef struct { double tenor; double log_discount; } MangoTenorPoint;
+
+typedef struct {
+  double spot;
+  double strike;
+  double maturity;
+  double dividend_yield;
+  double volatility;
+  double rate_const;
+  const MangoTenorPoint* tenor_points;
+  uint64_t n_tenor_points;
+  const MangoDividend* dividends;
+  uint64_t n_dividends;
+  MangoOptionType option_type;
+} MangoPricingParams;
+
+typedef struct {
+  double spot;
+  double strike;
+  double maturity;
+  double dividend_yield;
+  double market_price;
+  double rate_const;
+  const MangoTenorPoint* tenor_points;
+  uint64_t n_tenor_points;
+  const MangoDividend* dividends;
+  uint64_t n_dividends;
+  MangoOptionType option_type;
+} MangoIvQuery;
+
+typedef struct {
+  double implied_vol;
+  uint64_t iterations;
+  double final_error;
+  double vega;
+  int32_t has_vega;
+  int32_t used_rate_approximation;
+} MangoIvSuccess;
+
+typedef struct { double brent_tol_abs; int32_t max_iter; } MangoIvConfig;
+
+typedef struct {
+  int32_t status;
+  MangoIvSuccess success;
+} MangoIvBatchSlot;
+#endif /* MANGO_C_API_H */
+
+/* ---- engine-specific types ---- */
+
+/* Grid selection for one option, the C form of the reference's PDEGridSpec
+ * variant (src/option/grid_spec_types.hpp:55-61):
+ *   MANGO_GPU_GRID_AUTO     estimate_pde_grid(params, GridAccuracyParams{})
+ *                           (src/option/grid_spec_types.cpp:37-118);
+ *   MANGO_GPU_GRID_FIXED_N  estimate_pde_grid with min_spatial_points ==
+ *                           max_spatial_points == n_space, then
+ *                           PDEGridConfig{spec, n_time}: the reference's own
+ *                           sinh-clustered grid at a pinned size;
+ *   MANGO_GPU_GRID_SINH     PDEGridConfig{GridSpec::sinh_spaced(x_min, x_max,
+ *                           n_space, alpha), n_time};
+ *   MANGO_GPU_GRID_UNIFORM  PDEGridConfig{GridSpec::uniform(x_min, x_max,
+ *                           n_space), n_time}.
+ * x_min/x_max are log-moneyness ln(S/K). */
+#define MANGO_GPU_GRID_AUTO 0
+#define MANGO_GPU_GRID_FIXED_N 1
+#define MANGO_GPU_GRID_SINH 2
+#define MANGO_GPU_GRID_UNIFORM 3
+typedef struct {
+  int32_t kind;
+  int32_t reserved;
+  int64_t n_space;
+  int64_t n_time;
+  double x_min;
+  double x_max;
+  double alpha;
+} MangoGpuGrid;
+
+/* TRBDF2Config subset honoured by the march (src/pde/core/trbdf2_config.hpp:
+ * 18-49): gamma (default 2 - sqrt 2) and the Rannacher start-up flag
+ * (default on, as AmericanOptionSolver sets it). Pass NULL for defaults. */
+typedef struct {
+  double gamma;
+  int32_t rannacher_startup;
+  int32_t reserved;
+} MangoGpuTrbdf2;
+
+/* Per-option result: AmericanOptionResult::value/delta/gamma/theta
+ * (src/option/american_option_result.cpp:25-121).  status is a MangoStatus;
+ * n_space/n_time report the grid the option was solved on. */
+typedef struct {
+  double value;
+  double delta;
+  double gamma;
+  double theta;
+  int32_t status;
+  int32_t n_space;
+  int32_t n_time;
+  int32_t reserved;
+} MangoGpuAmericanOut;
+
+/* Opaque engine context: one CUDA device, one stream, grow-only device
+ * buffers reused across calls.  Not thread-safe: use one context per host
+ * thread (contexts on the same device share nothing). */
+typedef struct MangoGpuContext MangoGpuContext;
+
+/* Create a context on CUDA device `device`.  Fails (MANGO_ERR_SOLVER) when
+ * the device is absent or is not an sm_103 part this library was built for. */
+MangoStatus mango_gpu_context_create(int32_t device, MangoGpuContext** out,
+                                     MangoError* err);
+void mango_gpu_context_destroy(MangoGpuContext* ctx);
+
+/* Batched American pricing with Greeks.  Replaces a loop of
+ * mango_price_american (src/ffi/mango_c_api.h:141-150) and the C++
+ * BatchAmericanOptionSolver::solve_batch regular path
+ * (src/option/american_option_batch.cpp:384-518), which has no C export.
+ * grids: NULL => MANGO_GPU_GRID_AUTO for every option; else one per option,
+ * or a single entry applied to all when grid_stride == 0.
+ * out: n slots.  *out_failed (nullable) = slots whose status != MANGO_OK.
+ * Returns MANGO_OK unless the call itself could not run (bad pointers, CUDA
+ * failure), in which case err says why and no slot is meaningful. */
+MangoStatus mango_gpu_price_american_batch(MangoGpuContext* ctx,
+                                           const MangoPricingParams* params,
+                                           uint64_t n, const MangoGpuGrid* grids,
+                                           uint64_t grid_stride,
+                                           const MangoGpuTrbdf2* trbdf2,
+                                           MangoGpuAmericanOut* out,
+                                           uint64_t* out_failed, MangoError* err);
+
+/* Resident batch: the same pipeline as mango_gpu_price_american_batch split
+ * so that inputs can stay in device memory across runs (repeat pricing of a
+ * book, IV iterations, benchmarking).  _create validates, resolves grids and
+ * uploads; _run enqueues the device work (setup, march, outputs) on the
+ * context's stream and returns without waiting; _results waits and copies the
+ * per-option results to the caller.  No counterpart in the reference ABI. */
+typedef struct MangoGpuBatch MangoGpuBatch;
+MangoStatus mango_gpu_batch_create(MangoGpuContext* ctx, const MangoPricingParams* params,
+                                   uint64_t n, const MangoGpuGrid* grids, uint64_t grid_stride,
+                                   const MangoGpuTrbdf2* trbdf2, MangoGpuBatch** out,
+                                   MangoError* err);
+MangoStatus mango_gpu_batch_run(MangoGpuBatch* batch, MangoError* err);
+MangoStatus mango_gpu_batch_results(MangoGpuBatch* batch, MangoGpuAmericanOut* out,
+                                    uint64_t* out_failed, MangoError* err);
+void mango_gpu_batch_destroy(MangoGpuBatch* batch);
+/* Mean device time (CUDA events on the launching stream) of the setup,
+ * march and outputs kernels over the runs since the last reset (at most the
+ * last 256); waits for the stream.  reset != 0 starts a new window. */
+MangoStatus mango_gpu_batch_timings(MangoGpuBatch* batch, int32_t reset, double* prep_ms,
+                                    double* march_ms, double* outputs_ms, int64_t* runs,
+                                    MangoError* err);
+
+/* Make the context enqueue its work on `stream` (a cudaStream_t of the same
+ * device, e.g. a framework's current stream), or on its own stream when
+ * NULL.  No counterpart in the reference ABI. */
+MangoStatus mango_gpu_context_set_stream(MangoGpuContext* ctx, void* stream);
+
+/* Diagnostic: FP64 FMA throughput of this device in TFLOP/s (an FMA counts
+ * 2), measured with independent FMA chains on every SM; the denominator the
+ * engine's FP64 roofline fractions are quoted against.  No counterpart in
+ * the reference ABI. */
+MangoStatus mango_gpu_fp64_probe(MangoGpuContext* ctx, double* tflops, MangoError* err);
+
+/* Host only (no device needed): the grid the engine would solve `params` on
+ * for `grid`, i.e. resolve_grid + GridSpec::generate
+ * (src/option/american_option.cpp:54-73, src/pde/core/grid.hpp:364-498).
+ * Writes up to `cap` points to x_out and the sizes to *n_space / *n_time. */
+MangoStatus mango_gpu_resolve_grid(const MangoPricingParams* params, const MangoGpuGrid* grid,
+                                   double* x_out, int64_t cap, int64_t* n_space,
+                                   int64_t* n_time, MangoError* err);
+
+/* Timings and work counters of the context's last batch call.  Device
+ * times come from CUDA events on the context's stream.  algo_flops counts
+ * the reference algorithm's FP64 work: 28 flops per interior row per TR-BDF2
+ * step, 18 per row for the Rannacher start, 20 per row for the outputs (an
+ * FMA counts 2, a divide 1).  No counterpart in the reference ABI. */
+typedef struct {
+  double host_prep_ms;
+  double h2d_ms;
+  double prep_ms;
+  double march_ms;
+  double outputs_ms;
+  double d2h_ms;
+  double total_ms;
+  double algo_flops;
+  double h2d_bytes;
+  double d2h_bytes;
+  int64_t options;
+  int64_t tiles;
+  int64_t kernel_launches;
+} MangoGpuStats;
+MangoStatus mango_gpu_last_stats(const MangoGpuContext* ctx, MangoGpuStats* out);
+
+/* Library build information (never NULL). */
+const char* mango_gpu_build_info(void);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#ifdef __cplusplus
+static_assert(sizeof(MangoPricingParams) == 88, "MangoPricingParams size");
+static_assert(offsetof(MangoPricingParams, rate_const) == 40, "rate_const off");
+static_assert(offsetof(MangoPricingParams, option_type) == 80, "option_type off");
+static_assert(sizeof(MangoIvQuery) == 88, "MangoIvQuery size");
+static_assert(sizeof(MangoGpuGrid) == 48, "MangoGpuGrid size");
+static_assert(sizeof(MangoGpuAmericanOut) == 48, "MangoGpuAmericanOut size");
+#endif
+
+#endif /* MANGO_GPU_H */

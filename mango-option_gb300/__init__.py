@@ -1,0 +1,442 @@
+"""mango-option GB300 engine: Python surface over the C ABI in include/mango_gpu.h.
+
+The names mirror the reference's pybind11 module ``mango_option``
+(src/python/mango_bindings.cpp): ``OptionType``, ``PricingParams``,
+``american_option_price`` (mango_bindings.cpp:580), ``BatchAmericanOptionSolver``
+with ``solve_batch`` (mango_bindings.cpp:681-745) and the result accessors
+``value``/``delta``/``gamma``/``theta``.  Batches may also be passed as numpy
+arrays (``price_arrays``), which is how large workloads avoid per-option Python
+objects.
+
+Everything runs through ``libmango_gpu.so`` (built in-tree by build.py).  There
+is no CPU fallback: if the library is missing or no GB300 is present, the calls
+raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import enum
+import pathlib
+from typing import Iterable, Optional, Sequence
+
+import numpy as np
+
+_PKG = pathlib.Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "libmango_gpu.so"
+
+MANGO_OK = 0
+MANGO_ERR_VALIDATION = 1
+MANGO_ERR_ARBITRAGE = 2
+MANGO_ERR_NO_CONVERGENCE = 3
+MANGO_ERR_BRACKETING = 4
+MANGO_ERR_SOLVER = 5
+
+GRID_AUTO = 0
+GRID_FIXED_N = 1
+GRID_SINH = 2
+GRID_UNIFORM = 3
+
+# C layouts (include/mango_gpu.h); sizes are asserted there and in tests.
+PRICING_DTYPE = np.dtype([
+    ("spot", "f8"), ("strike", "f8"), ("maturity", "f8"), ("dividend_yield", "f8"),
+    ("volatility", "f8"), ("rate_const", "f8"), ("tenor_points", "u8"),
+    ("n_tenor_points", "u8"), ("dividends", "u8"), ("n_dividends", "u8"),
+    ("option_type", "i4"), ("_pad", "i4")])
+IVQUERY_DTYPE = np.dtype([
+    ("spot", "f8"), ("strike", "f8"), ("maturity", "f8"), ("dividend_yield", "f8"),
+    ("market_price", "f8"), ("rate_const", "f8"), ("tenor_points", "u8"),
+    ("n_tenor_points", "u8"), ("dividends", "u8"), ("n_dividends", "u8"),
+    ("option_type", "i4"), ("_pad", "i4")])
+GRID_DTYPE = np.dtype([
+    ("kind", "i4"), ("reserved", "i4"), ("n_space", "i8"), ("n_time", "i8"),
+    ("x_min", "f8"), ("x_max", "f8"), ("alpha", "f8")])
+OUT_DTYPE = np.dtype([
+    ("value", "f8"), ("delta", "f8"), ("gamma", "f8"), ("theta", "f8"),
+    ("status", "i4"), ("n_space", "i4"), ("n_time", "i4"), ("reserved", "i4")])
+
+
+class MangoError(ctypes.Structure):
+    _fields_ = [("code", ctypes.c_int32), ("message", ctypes.c_char * 256)]
+
+
+class MangoGpuTrbdf2(ctypes.Structure):
+    _fields_ = [("gamma", ctypes.c_double), ("rannacher_startup", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class MangoGpuStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in (
+        "host_prep_ms", "h2d_ms", "prep_ms", "march_ms", "outputs_ms", "d2h_ms", "total_ms",
+        "algo_flops", "h2d_bytes", "d2h_bytes")] + [
+        ("options", ctypes.c_int64), ("tiles", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
+
+
+class EngineError(RuntimeError):
+    """Raised when the engine call itself fails (no device, CUDA error)."""
+
+
+_lib = None
+_P = ctypes.c_void_p
+
+
+def library() -> ctypes.CDLL:
+    """Load libmango_gpu.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        lib = ctypes.CDLL(str(LIB_PATH))
+        lib.mango_gpu_context_create.argtypes = [ctypes.c_int32, ctypes.POINTER(_P), ctypes.POINTER(MangoError)]
+        lib.mango_gpu_context_create.restype = ctypes.c_int32
+        lib.mango_gpu_context_destroy.argtypes = [_P]
+        lib.mango_gpu_context_destroy.restype = None
+        lib.mango_gpu_price_american_batch.argtypes = [
+            _P, _P, ctypes.c_uint64, _P, ctypes.c_uint64, ctypes.POINTER(MangoGpuTrbdf2), _P,
+            ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(MangoError)]
+        lib.mango_gpu_price_american_batch.restype = ctypes.c_int32
+        lib.mango_gpu_resolve_grid.argtypes = [_P, _P, _P, ctypes.c_int64,
+                                               ctypes.POINTER(ctypes.c_int64),
+                                               ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(MangoError)]
+        lib.mango_gpu_resolve_grid.restype = ctypes.c_int32
+        lib.mango_gpu_last_stats.argtypes = [_P, ctypes.POINTER(MangoGpuStats)]
+        lib.mango_gpu_last_stats.restype = ctypes.c_int32
+        lib.mango_gpu_batch_create.argtypes = [_P, _P, ctypes.c_uint64, _P, ctypes.c_uint64,
+                                               ctypes.POINTER(MangoGpuTrbdf2), ctypes.POINTER(_P),
+                                               ctypes.POINTER(MangoError)]
+        lib.mango_gpu_batch_create.restype = ctypes.c_int32
+        lib.mango_gpu_batch_run.argtypes = [_P, ctypes.POINTER(MangoError)]
+        lib.mango_gpu_batch_run.restype = ctypes.c_int32
+        lib.mango_gpu_batch_results.argtypes = [_P, _P, ctypes.POINTER(ctypes.c_uint64),
+                                                ctypes.POINTER(MangoError)]
+        lib.mango_gpu_batch_results.restype = ctypes.c_int32
+        lib.mango_gpu_batch_destroy.argtypes = [_P]
+        lib.mango_gpu_batch_destroy.restype = None
+        lib.mango_gpu_batch_timings.argtypes = [_P, ctypes.c_int32] + [ctypes.POINTER(ctypes.c_double)] * 3 + [
+            ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(MangoError)]
+        lib.mango_gpu_batch_timings.restype = ctypes.c_int32
+        lib.mango_gpu_context_set_stream.argtypes = [_P, _P]
+        lib.mango_gpu_context_set_stream.restype = ctypes.c_int32
+        lib.mango_gpu_fp64_probe.argtypes = [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(MangoError)]
+        lib.mango_gpu_fp64_probe.restype = ctypes.c_int32
+        lib.mango_gpu_build_info.argtypes = []
+        lib.mango_gpu_build_info.restype = ctypes.c_char_p
+        _lib = lib
+    return _lib
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+class OptionType(enum.IntEnum):
+    """Reference OptionType; values are the C ABI's (MANGO_CALL=0, MANGO_PUT=1)."""
+    CALL = 0
+    PUT = 1
+
+
+@dataclasses.dataclass
+class PricingParams:
+    """Reference PricingParams (src/option/option_spec.hpp:262-281), constant
+    rate and continuous dividend yield."""
+    spot: float = 0.0
+    strike: float = 0.0
+    maturity: float = 0.0
+    rate: float = 0.0
+    dividend_yield: float = 0.0
+    option_type: OptionType = OptionType.CALL
+    volatility: float = 0.0
+
+
+@dataclasses.dataclass
+class PDEGridConfig:
+    """Explicit grid: sinh (alpha > 0) or uniform (alpha == 0) over
+    [x_min, x_max] in ln(S/K), n_space points, n_time steps
+    (src/option/grid_spec_types.hpp:55-59)."""
+    x_min: float = -3.0
+    x_max: float = 3.0
+    n_space: int = 101
+    n_time: int = 1000
+    alpha: float = 2.0 * float(np.arcsinh(5.0 / np.sqrt(2.0)))
+
+
+@dataclasses.dataclass
+class FixedGrid:
+    """The reference's sinh-clustered auto grid pinned to n_space points,
+    with n_time steps (estimate_pde_grid with min = max = n_space)."""
+    n_space: int = 101
+    n_time: int = 498
+
+
+def pricing_array(spot, strike, maturity, volatility, rate, dividend_yield, is_put) -> np.ndarray:
+    """Pack per-option arrays (broadcast) into the C MangoPricingParams layout."""
+    cols = np.broadcast_arrays(*(np.asarray(v, dtype=np.float64) for v in
+                                 (spot, strike, maturity, volatility, rate, dividend_yield, is_put)))
+    n = cols[0].size
+    a = np.zeros(n, dtype=PRICING_DTYPE)
+    a["spot"], a["strike"], a["maturity"] = cols[0].ravel(), cols[1].ravel(), cols[2].ravel()
+    a["volatility"], a["rate_const"], a["dividend_yield"] = cols[3].ravel(), cols[4].ravel(), cols[5].ravel()
+    a["option_type"] = np.where(cols[6].ravel() != 0, 1, 0).astype(np.int32)
+    return a
+
+
+def grid_array(n: int, kind: int = GRID_AUTO, n_space=0, n_time=0, x_min=0.0, x_max=0.0,
+               alpha=0.0) -> np.ndarray:
+    g = np.zeros(n, dtype=GRID_DTYPE)
+    g["kind"] = kind
+    g["n_space"] = n_space
+    g["n_time"] = n_time
+    g["x_min"] = x_min
+    g["x_max"] = x_max
+    g["alpha"] = alpha
+    return g
+
+
+def _grid_entry(grid) -> np.ndarray:
+    if grid is None:
+        return grid_array(1, GRID_AUTO)
+    if isinstance(grid, FixedGrid):
+        return grid_array(1, GRID_FIXED_N, grid.n_space, grid.n_time)
+    if isinstance(grid, PDEGridConfig):
+        kind = GRID_SINH if grid.alpha > 0 else GRID_UNIFORM
+        return grid_array(1, kind, grid.n_space, grid.n_time, grid.x_min, grid.x_max, grid.alpha)
+    raise TypeError(f"unsupported grid {grid!r}")
+
+
+class Engine:
+    """One CUDA context of the engine (include/mango_gpu.h MangoGpuContext)."""
+
+    def __init__(self, device: int = 0):
+        lib = library()
+        self._ctx = _P()
+        err = MangoError()
+        st = lib.mango_gpu_context_create(device, ctypes.byref(self._ctx), ctypes.byref(err))
+        if st != MANGO_OK:
+            self._ctx = None
+            raise EngineError(f"mango_gpu_context_create: {err.message.decode(errors='replace')}")
+
+    def close(self) -> None:
+        if self._ctx:
+            library().mango_gpu_context_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def price_arrays(self, params: np.ndarray, grids: Optional[np.ndarray] = None,
+                     rannacher: bool = True, gamma: float = 0.0) -> np.ndarray:
+        """Batched pricing.  params: PRICING_DTYPE array; grids: GRID_DTYPE array
+        of length len(params) or 1 (applied to all) or None (auto grid).
+        Returns an OUT_DTYPE array (value, delta, gamma, theta, status, n_space, n_time)."""
+        params = np.ascontiguousarray(params, dtype=PRICING_DTYPE)
+        n = params.size
+        out = np.zeros(n, dtype=OUT_DTYPE)
+        stride = 0
+        if grids is not None:
+            grids = np.ascontiguousarray(grids, dtype=GRID_DTYPE)
+            if grids.size == n and n != 1:
+                stride = 1
+            elif grids.size != 1:
+                raise ValueError("grids must have length 1 or len(params)")
+        tr = MangoGpuTrbdf2(gamma, 1 if rannacher else 0, 0)
+        failed = ctypes.c_uint64()
+        err = MangoError()
+        st = library().mango_gpu_price_american_batch(
+            self._ctx, _ptr(params), n, _ptr(grids), stride, ctypes.byref(tr), _ptr(out),
+            ctypes.byref(failed), ctypes.byref(err))
+        if st != MANGO_OK:
+            raise EngineError(f"mango_gpu_price_american_batch: {err.message.decode(errors='replace')}")
+        return out
+
+    def set_stream(self, stream_handle: Optional[int]) -> None:
+        """Enqueue on a caller's cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""
+        library().mango_gpu_context_set_stream(self._ctx, _P(stream_handle) if stream_handle else None)
+
+    def fp64_probe(self) -> float:
+        """Measured FP64 FMA throughput of the device, TFLOP/s."""
+        v = ctypes.c_double()
+        err = MangoError()
+        if library().mango_gpu_fp64_probe(self._ctx, ctypes.byref(v), ctypes.byref(err)) != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+        return v.value
+
+    def batch(self, params: np.ndarray, grids: Optional[np.ndarray] = None, rannacher: bool = True,
+              gamma: float = 0.0) -> "ResidentBatch":
+        return ResidentBatch(self, params, grids, rannacher, gamma)
+
+    def stats(self) -> dict:
+        s = MangoGpuStats()
+        library().mango_gpu_last_stats(self._ctx, ctypes.byref(s))
+        return {k: getattr(s, k) for k, _ in MangoGpuStats._fields_}
+
+
+class ResidentBatch:
+    """A batch uploaded once and re-run on the device (mango_gpu_batch_*)."""
+
+    def __init__(self, engine: Engine, params: np.ndarray, grids: Optional[np.ndarray], rannacher: bool,
+                 gamma: float):
+        self._engine = engine
+        self.params = np.ascontiguousarray(params, dtype=PRICING_DTYPE)
+        n = self.params.size
+        stride = 0
+        if grids is not None:
+            grids = np.ascontiguousarray(grids, dtype=GRID_DTYPE)
+            stride = 1 if (grids.size == n and n != 1) else 0
+        self._grids = grids
+        self._b = _P()
+        err = MangoError()
+        tr = MangoGpuTrbdf2(gamma, 1 if rannacher else 0, 0)
+        st = library().mango_gpu_batch_create(engine._ctx, _ptr(self.params), n, _ptr(grids), stride,
+                                              ctypes.byref(tr), ctypes.byref(self._b), ctypes.byref(err))
+        if st != MANGO_OK:
+            self._b = None
+            raise EngineError(err.message.decode(errors="replace"))
+        self.n = n
+
+    def run(self) -> None:
+        err = MangoError()
+        if library().mango_gpu_batch_run(self._b, ctypes.byref(err)) != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+
+    def results(self) -> np.ndarray:
+        out = np.zeros(self.n, dtype=OUT_DTYPE)
+        failed = ctypes.c_uint64()
+        err = MangoError()
+        if library().mango_gpu_batch_results(self._b, _ptr(out), ctypes.byref(failed), ctypes.byref(err)) != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+        return out
+
+    def timings(self, reset: bool = False) -> dict:
+        a, m, o = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        runs = ctypes.c_int64()
+        err = MangoError()
+        if library().mango_gpu_batch_timings(self._b, 1 if reset else 0, ctypes.byref(a), ctypes.byref(m),
+                                             ctypes.byref(o), ctypes.byref(runs), ctypes.byref(err)) != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+        return {"prep_ms": a.value, "march_ms": m.value, "outputs_ms": o.value, "runs": runs.value}
+
+    def close(self) -> None:
+        if self._b:
+            library().mango_gpu_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def resolve_grid(params: np.ndarray, grid=None):
+    """Host-only: the grid (x, n_time) the engine uses for one option."""
+    params = np.ascontiguousarray(params, dtype=PRICING_DTYPE).reshape(1)
+    g = grid if isinstance(grid, np.ndarray) else _grid_entry(grid)
+    g = np.ascontiguousarray(g, dtype=GRID_DTYPE).reshape(1)
+    x = np.zeros(1 << 16)
+    n = ctypes.c_int64()
+    nt = ctypes.c_int64()
+    err = MangoError()
+    st = library().mango_gpu_resolve_grid(_ptr(params), _ptr(g), _ptr(x), x.size, ctypes.byref(n),
+                                          ctypes.byref(nt), ctypes.byref(err))
+    if st != MANGO_OK:
+        raise ValueError(err.message.decode(errors="replace"))
+    return x[: n.value].copy(), nt.value
+
+
+_default_engine: Optional[Engine] = None
+
+
+def default_engine() -> Engine:
+    global _default_engine
+    if _default_engine is None:
+        _default_engine = Engine(0)
+    return _default_engine
+
+
+def _to_array(params: Sequence[PricingParams]) -> np.ndarray:
+    return pricing_array([p.spot for p in params], [p.strike for p in params],
+                         [p.maturity for p in params], [p.volatility for p in params],
+                         [p.rate for p in params], [p.dividend_yield for p in params],
+                         [int(p.option_type == OptionType.PUT) for p in params])
+
+
+@dataclasses.dataclass
+class AmericanOptionResult:
+    """Reference AmericanOptionResult accessors (american_option_result.hpp)."""
+    _row: np.void
+    params: PricingParams
+
+    def value(self) -> float:
+        return float(self._row["value"])
+
+    def delta(self) -> float:
+        return float(self._row["delta"])
+
+    def gamma(self) -> float:
+        return float(self._row["gamma"])
+
+    def theta(self) -> float:
+        return float(self._row["theta"])
+
+    @property
+    def n_space(self) -> int:
+        return int(self._row["n_space"])
+
+    @property
+    def n_time(self) -> int:
+        return int(self._row["n_time"])
+
+
+class SolverError(RuntimeError):
+    def __init__(self, status: int, message: str = ""):
+        super().__init__(message or f"status {status}")
+        self.status = status
+
+
+def american_option_price(params: PricingParams, grid=None) -> AmericanOptionResult:
+    """Single option (mango_bindings.cpp:580; american_option.cpp:440-450)."""
+    out = default_engine().price_arrays(_to_array([params]), _grid_entry(grid))
+    if out[0]["status"] != MANGO_OK:
+        raise SolverError(int(out[0]["status"]))
+    return AmericanOptionResult(out[0], params)
+
+
+@dataclasses.dataclass
+class BatchAmericanOptionResult:
+    results: list
+    failed_count: int
+
+
+class BatchAmericanOptionSolver:
+    """Reference BatchAmericanOptionSolver (american_option_batch.hpp:114);
+    solve_batch prices every option on its own grid in one GPU batch."""
+
+    def __init__(self, engine: Optional[Engine] = None):
+        self._engine = engine
+        self._grid = None
+
+    def set_grid(self, grid) -> None:
+        self._grid = grid
+
+    def solve_batch(self, params: Iterable[PricingParams], use_shared_grid: bool = False,
+                    custom_grid=None) -> BatchAmericanOptionResult:
+        plist = list(params)
+        eng = self._engine or default_engine()
+        grid = custom_grid if custom_grid is not None else self._grid
+        out = eng.price_arrays(_to_array(plist), _grid_entry(grid))
+        results = []
+        for row, p in zip(out, plist):
+            if row["status"] == MANGO_OK:
+                results.append(AmericanOptionResult(row, p))
+            else:
+                results.append(SolverError(int(row["status"])))
+        return BatchAmericanOptionResult(results, int(np.count_nonzero(out["status"])))

@@ -1,0 +1,673 @@
+// engine.cu -- C ABI implementation (include/mango_gpu.h) and the batched
+// pricing pipeline.  Mirrors the reference's ABI conventions: status codes
+// and 256-byte messages (src/ffi/mango_c_api.cpp:23-31), every exception
+// caught at the boundary (mango_c_api.cpp:354-360), per-slot status for batch
+// calls (mango_c_api.cpp:523-576).
+#include "engine.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <thread>
+
+namespace mgpu {
+
+__global__ void prep_kernel(const TileDev*, int, const OptDev*, const double*, double*, uint8_t*,
+                            int32_t*, MarchConst);
+__global__ void march_kernel(const TileDev*, int, const OptDev*, double*, const uint8_t*,
+                             const int32_t*, int32_t*, int*, MarchConst);
+__global__ void outputs_kernel(const TileDev*, int, const OptDev*, const double*, double*,
+                               const int32_t*, const int32_t*, MarchConst, double*);
+__global__ void fp64_probe_kernel(double* out, int iters);
+
+void check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    throw CudaError(std::string(what) + ": " + cudaGetErrorName(e) + " (" +
+                    cudaGetErrorString(e) + ")");
+  }
+}
+
+void* DevBuf::get(size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (bytes > cap) {
+    if (p) check(cudaFree(p), "cudaFree");
+    p = nullptr;
+    cap = 0;
+    check(cudaMalloc(&p, bytes), "cudaMalloc");
+    cap = bytes;
+  }
+  return p;
+}
+void DevBuf::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+}
+void* HostBuf::get(size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (bytes > cap) {
+    if (p) check(cudaFreeHost(p), "cudaFreeHost");
+    p = nullptr;
+    cap = 0;
+    check(cudaMallocHost(&p, bytes), "cudaMallocHost");
+    cap = bytes;
+  }
+  return p;
+}
+void HostBuf::release() {
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  cap = 0;
+}
+
+void parallel_for(int64_t n, const std::function<void(int64_t)>& f) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int64_t per = 512;
+  const int64_t nth = std::min<int64_t>(hw, (n + per - 1) / per);
+  if (nth <= 1) {
+    for (int64_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve(static_cast<size_t>(nth));
+  for (int64_t t = 0; t < nth; ++t) {
+    th.emplace_back([&, t] {
+      const int64_t a = n * t / nth, b = n * (t + 1) / nth;
+      for (int64_t i = a; i < b; ++i) f(i);
+    });
+  }
+  for (auto& x : th) x.join();
+}
+
+std::string validate(const MangoPricingParams& p) {
+  // validate_pricing_params (src/option/option_spec.cpp:8-40, 117-157)
+  if (!(p.spot > 0.0) || !std::isfinite(p.spot)) return "invalid spot";
+  if (!(p.strike > 0.0) || !std::isfinite(p.strike)) return "invalid strike";
+  if (!(p.maturity > 0.0) || !std::isfinite(p.maturity)) return "invalid maturity";
+  if (!std::isfinite(p.rate_const)) return "invalid rate";
+  if (p.dividend_yield < 0.0 || !std::isfinite(p.dividend_yield)) return "invalid dividend yield";
+  if (!(p.volatility > 0.0) || !std::isfinite(p.volatility)) return "invalid volatility";
+  if (p.option_type != MANGO_PUT && p.option_type != MANGO_CALL) return "invalid option type";
+  if (p.n_tenor_points != 0) return "yield curves are not supported by the GPU engine";
+  if (p.n_dividends != 0) return "discrete dividends are not supported by the GPU engine";
+  return {};
+}
+
+std::string resolve(const MangoPricingParams& p, const MangoGpuGrid& g, Resolved* r,
+                    std::vector<double>* scratch) {
+  // resolve_grid (src/option/american_option.cpp:54-73)
+  const Accuracy def = default_accuracy();
+  switch (g.kind) {
+    case MANGO_GPU_GRID_AUTO:
+      estimate_grid(p.spot, p.strike, p.maturity, p.volatility, def, &r->spec, &r->nt, scratch);
+      break;
+    case MANGO_GPU_GRID_FIXED_N: {
+      if (g.n_space < 3 || g.n_time < 1) return "grid: n_space >= 3 and n_time >= 1 required";
+      Accuracy a = def;
+      a.min_points = a.max_points = g.n_space;
+      int64_t nt_auto = 0;
+      estimate_grid(p.spot, p.strike, p.maturity, p.volatility, a, &r->spec, &nt_auto, scratch);
+      r->nt = g.n_time;
+      break;
+    }
+    case MANGO_GPU_GRID_SINH:
+      if (g.n_space < 3 || g.n_time < 1) return "grid: n_space >= 3 and n_time >= 1 required";
+      if (!(g.x_min < g.x_max)) return "grid: x_min < x_max required";
+      if (!(g.alpha > 0.0)) return "grid: alpha > 0 required";
+      r->spec = sinh_spec(g.x_min, g.x_max, g.n_space, g.alpha);
+      r->nt = g.n_time;
+      break;
+    case MANGO_GPU_GRID_UNIFORM:
+      if (g.n_space < 3 || g.n_time < 1) return "grid: n_space >= 3 and n_time >= 1 required";
+      if (!(g.x_min < g.x_max)) return "grid: x_min < x_max required";
+      r->spec = uniform_spec(g.x_min, g.x_max, g.n_space);
+      r->nt = g.n_time;
+      break;
+    default:
+      return "grid: unknown kind";
+  }
+  if (r->spec.n > 100000) return "grid: n_space above 100000";
+  if (r->nt > 100000000) return "grid: n_time above 1e8";
+  return {};
+}
+
+namespace {
+
+void set_err(MangoError* err, int32_t code, const std::string& msg) {
+  if (!err) return;
+  err->code = code;
+  std::snprintf(err->message, sizeof(err->message), "%s", msg.c_str());
+}
+
+using Clock = std::chrono::steady_clock;
+double ms_since(Clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+}
+
+MarchConst make_const(const MangoGpuTrbdf2* trbdf2) {
+  MarchConst mc{};
+  mc.gamma = (trbdf2 && trbdf2->gamma > 0.0) ? trbdf2->gamma : 2.0 - std::sqrt(2.0);
+  mc.rannacher = trbdf2 ? (trbdf2->rannacher_startup != 0) : 1;
+  // solve_stage2 coefficients (pde_solver.hpp:372-380)
+  const double omg = 1.0 - mc.gamma, tmg = 2.0 - mc.gamma, den = mc.gamma * tmg;
+  mc.alpha = 1.0 / den;
+  mc.beta = -(omg * omg) / den;
+  return mc;
+}
+
+void destroy_batch(MangoGpuBatch* b) {
+  if (!b) return;
+  for (mgpu::DevBuf* d : {&b->d_pool, &b->d_xs, &b->d_flags, &b->d_opts, &b->d_tiles, &b->d_mode,
+                          &b->d_status, &b->d_out4, &b->d_queue})
+    d->release();
+  for (mgpu::HostBuf* h : {&b->h_xs, &b->h_opts, &b->h_tiles, &b->h_out4, &b->h_status})
+    h->release();
+  for (auto& e : b->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : b->run_ev)
+    if (e) cudaEventDestroy(e);
+  delete b;
+}
+
+// Validate, resolve grids, sort/tile, pack and upload.
+MangoGpuBatch* create_batch(MangoGpuContext* ctx, const MangoPricingParams* params, int64_t n,
+                            const MangoGpuGrid* grids, uint64_t grid_stride,
+                            const MangoGpuTrbdf2* trbdf2) {
+  auto t0 = Clock::now();
+  std::unique_ptr<MangoGpuBatch, void (*)(MangoGpuBatch*)> b(new MangoGpuBatch(), destroy_batch);
+  b->ctx = ctx;
+  b->n = n;
+  b->mc = make_const(trbdf2);
+  b->res.resize(static_cast<size_t>(n));
+  b->msgs.resize(static_cast<size_t>(n));
+  for (auto& e : b->ev) check(cudaEventCreate(&e), "cudaEventCreate");
+  parallel_for(n, [&](int64_t i) {
+    thread_local std::vector<double> scratch;
+    Resolved& r = b->res[i];
+    r.orig = static_cast<int32_t>(i);
+    std::string m = validate(params[i]);
+    if (m.empty()) {
+      MangoGpuGrid g{};
+      g.kind = MANGO_GPU_GRID_AUTO;
+      if (grids) g = grids[grid_stride ? i : 0];
+      m = resolve(params[i], g, &r, &scratch);
+    }
+    if (!m.empty()) {
+      r.status = MANGO_ERR_VALIDATION;
+      b->msgs[i] = m;
+    }
+  });
+  // Sort accepted options by (n_space, n_time) descending: similar lanes
+  // share a tile and the largest tiles are dequeued first.
+  std::vector<int32_t>& order = b->order;
+  for (int64_t i = 0; i < n; ++i)
+    if (b->res[i].status == 0) order.push_back(static_cast<int32_t>(i));
+  std::sort(order.begin(), order.end(), [&](int32_t a, int32_t c) {
+    const Resolved& ra = b->res[a];
+    const Resolved& rc = b->res[c];
+    if (ra.spec.n != rc.spec.n) return ra.spec.n > rc.spec.n;
+    if (ra.nt != rc.nt) return ra.nt > rc.nt;
+    return a < c;
+  });
+  const int64_t m = static_cast<int64_t>(order.size());
+  const int32_t ntiles = static_cast<int32_t>((m + kTile - 1) / kTile);
+  b->ntiles = ntiles;
+  TileDev* tiles = static_cast<TileDev*>(b->h_tiles.get(sizeof(TileDev) * std::max(ntiles, 1)));
+  int64_t off = 0, xoff = 0, foff = 0;
+  double flops = 0;
+  const MarchConst& mc = b->mc;
+  for (int32_t t = 0; t < ntiles; ++t) {
+    TileDev& td = tiles[t];
+    td.first = t * kTile;
+    td.count = static_cast<int32_t>(std::min<int64_t>(kTile, m - td.first));
+    int64_t nx = 0, nt = 0;
+    for (int l = 0; l < td.count; ++l) {
+      const Resolved& r = b->res[order[td.first + l]];
+      nx = std::max<int64_t>(nx, r.spec.n);
+      nt = std::max<int64_t>(nt, r.nt);
+      // Algorithmic FP64 work (FMA = 2): 28 per row per TR-BDF2 step, 18 per
+      // row for the Rannacher start, 20 per row for the output splines.
+      const double steps = static_cast<double>(r.nt) - (mc.rannacher ? 1.0 : 0.0);
+      flops += static_cast<double>(r.spec.n) * (28.0 * steps + (mc.rannacher ? 18.0 : 0.0) + 20.0);
+    }
+    td.nx = static_cast<int32_t>(nx);
+    td.nt = static_cast<int32_t>(nt);
+    td.off = off;
+    td.xoff = xoff;
+    td.foff = foff;
+    off += static_cast<int64_t>(A_COUNT) * nx * kTile;
+    xoff += nx * kTile;
+    foff += nx * kTile;
+  }
+  b->algo_flops = flops;
+
+  OptDev* opts = static_cast<OptDev*>(b->h_opts.get(sizeof(OptDev) * std::max<int64_t>(m, 1)));
+  double* xs = static_cast<double*>(b->h_xs.get(sizeof(double) * std::max<int64_t>(xoff, 1)));
+  parallel_for(ntiles, [&](int64_t t) {
+    const TileDev& td = tiles[t];
+    std::vector<double> x;
+    for (int l = 0; l < kTile; ++l) {
+      double* dst = xs + td.xoff + l;
+      if (l >= td.count) {
+        for (int i = 0; i < td.nx; ++i) dst[static_cast<size_t>(i) * kTile] = 0.0;
+        continue;
+      }
+      const Resolved& r = b->res[order[td.first + l]];
+      const MangoPricingParams& p = params[r.orig];
+      x.resize(static_cast<size_t>(r.spec.n));
+      generate_grid(r.spec, x.data());
+      for (int i = 0; i < td.nx; ++i)
+        dst[static_cast<size_t>(i) * kTile] = x[std::min<int64_t>(i, r.spec.n - 1)];
+      OptDev& o = opts[td.first + l];
+      o.dt = (p.maturity - 0.0) / static_cast<double>(r.nt);  // TimeDomain::from_n_steps
+      o.sigma = p.volatility;
+      o.r = p.rate_const;
+      o.q = p.dividend_yield;
+      const bool put = p.option_type == MANGO_PUT;
+      o.bc_left = put ? std::max(1.0 - std::exp(x[0]), 0.0) : 0.0;  // american_option.cpp:192-197
+      o.exp_xr = std::exp(x[r.spec.n - 1]);
+      o.x_spot = std::log(p.spot / p.strike);
+      o.spot = p.spot;
+      o.strike = p.strike;
+      o.n = static_cast<int32_t>(r.spec.n);
+      o.nt = static_cast<int32_t>(r.nt);
+      o.is_put = put ? 1 : 0;
+      o.orig = r.orig;
+    }
+  });
+  b->host_prep_ms = ms_since(t0);
+
+  if (m > 0) {
+    cudaStream_t st = ctx->stream;
+    b->d_pool.get(sizeof(double) * off);
+    double* d_xs = static_cast<double*>(b->d_xs.get(sizeof(double) * xoff));
+    b->d_flags.get(static_cast<size_t>(foff));
+    OptDev* d_opts = static_cast<OptDev*>(b->d_opts.get(sizeof(OptDev) * m));
+    TileDev* d_tiles = static_cast<TileDev*>(b->d_tiles.get(sizeof(TileDev) * ntiles));
+    b->d_mode.get(sizeof(int32_t) * m);
+    b->d_status.get(sizeof(int32_t) * m);
+    b->d_out4.get(sizeof(double) * 4 * m);
+    b->d_queue.get(sizeof(int) * 4);
+    check(cudaEventRecord(b->ev[0], st), "event");
+    check(cudaMemcpyAsync(d_xs, xs, sizeof(double) * xoff, cudaMemcpyHostToDevice, st), "H2D grids");
+    check(cudaMemcpyAsync(d_opts, opts, sizeof(OptDev) * m, cudaMemcpyHostToDevice, st), "H2D options");
+    check(cudaMemcpyAsync(d_tiles, tiles, sizeof(TileDev) * ntiles, cudaMemcpyHostToDevice, st),
+          "H2D tiles");
+    check(cudaEventRecord(b->ev[1], st), "event");
+    b->h2d_bytes = static_cast<double>(sizeof(double) * xoff + sizeof(OptDev) * m +
+                                       sizeof(TileDev) * ntiles);
+  }
+  return b.release();
+}
+
+// Enqueue setup, march and outputs for a created batch.
+void run_batch(MangoGpuBatch* b) {
+  MangoGpuContext* ctx = b->ctx;
+  const int64_t m = static_cast<int64_t>(b->order.size());
+  b->ran = true;
+  if (m == 0) return;
+  cudaStream_t st = ctx->stream;
+  const int ntiles = b->ntiles;
+  const int threads = ntiles * kTile;
+  const TileDev* d_tiles = b->d_tiles.as<TileDev>();
+  const OptDev* d_opts = b->d_opts.as<OptDev>();
+  double* d_pool = b->d_pool.as<double>();
+  const double* d_xs = b->d_xs.as<double>();
+  uint8_t* d_flags = b->d_flags.as<uint8_t>();
+  int32_t* d_mode = b->d_mode.as<int32_t>();
+  int32_t* d_status = b->d_status.as<int32_t>();
+  check(cudaMemsetAsync(b->d_queue.p, 0, sizeof(int) * 4, st), "memset queue");
+  const size_t slot = static_cast<size_t>(b->runs % MangoGpuBatch::kMaxTimedRuns) * 4;
+  if (b->run_ev.size() < slot + 4) {
+    b->run_ev.resize(slot + 4, nullptr);
+    for (size_t j = slot; j < slot + 4; ++j) check(cudaEventCreate(&b->run_ev[j]), "cudaEventCreate");
+  }
+  ++b->runs;
+  check(cudaEventRecord(b->run_ev[slot + 0], st), "event");
+  check(cudaEventRecord(b->ev[2], st), "event");
+  prep_kernel<<<(threads + 127) / 128, 128, 0, st>>>(d_tiles, ntiles, d_opts, d_xs, d_pool,
+                                                     d_flags, d_mode, b->mc);
+  check(cudaGetLastError(), "prep_kernel launch");
+  check(cudaEventRecord(b->ev[3], st), "event");
+  check(cudaEventRecord(b->run_ev[slot + 1], st), "event");
+  const int warps_per_block = 4;
+  const int blocks = std::max(1, std::min<int>(ctx->num_sms * ctx->march_blocks_per_sm,
+                                               (ntiles + warps_per_block - 1) / warps_per_block));
+  march_kernel<<<blocks, 32 * warps_per_block, 0, st>>>(d_tiles, ntiles, d_opts, d_pool, d_flags,
+                                                        d_mode, d_status, b->d_queue.as<int>(),
+                                                        b->mc);
+  check(cudaGetLastError(), "march_kernel launch");
+  check(cudaEventRecord(b->ev[4], st), "event");
+  check(cudaEventRecord(b->run_ev[slot + 2], st), "event");
+  outputs_kernel<<<(threads + 127) / 128, 128, 0, st>>>(d_tiles, ntiles, d_opts, d_xs, d_pool,
+                                                        d_mode, d_status, b->mc,
+                                                        b->d_out4.as<double>());
+  check(cudaGetLastError(), "outputs_kernel launch");
+  check(cudaEventRecord(b->ev[5], st), "event");
+  check(cudaEventRecord(b->run_ev[slot + 3], st), "event");
+}
+
+// Wait for the batch, copy results into caller slots, update context stats.
+uint64_t fetch_batch(MangoGpuBatch* b, MangoGpuAmericanOut* out, std::string* first_msg) {
+  MangoGpuContext* ctx = b->ctx;
+  const int64_t m = static_cast<int64_t>(b->order.size());
+  Stats& S = ctx->stats;
+  for (int64_t i = 0; i < b->n; ++i) {
+    MangoGpuAmericanOut& o = out[i];
+    o.value = o.delta = o.gamma = o.theta = NAN;
+    o.status = b->res[i].status;
+    o.n_space = static_cast<int32_t>(b->res[i].spec.n);
+    o.n_time = static_cast<int32_t>(b->res[i].nt);
+    o.reserved = 0;
+    if (o.status != 0 && first_msg->empty()) *first_msg = b->msgs[i];
+  }
+  if (m > 0) {
+    cudaStream_t st = ctx->stream;
+    double* h_out4 = static_cast<double*>(b->h_out4.get(sizeof(double) * 4 * m));
+    int32_t* h_status = static_cast<int32_t*>(b->h_status.get(sizeof(int32_t) * m));
+    check(cudaMemcpyAsync(h_out4, b->d_out4.p, sizeof(double) * 4 * m, cudaMemcpyDeviceToHost, st),
+          "D2H results");
+    check(cudaMemcpyAsync(h_status, b->d_status.p, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, st),
+          "D2H status");
+    check(cudaEventRecord(b->ev[6], st), "event");
+    check(cudaStreamSynchronize(st), "stream synchronize");
+    for (int64_t s = 0; s < m; ++s) {
+      MangoGpuAmericanOut& o = out[b->order[s]];
+      o.status = h_status[s];
+      o.value = h_out4[4 * s + 0];
+      o.delta = h_out4[4 * s + 1];
+      o.gamma = h_out4[4 * s + 2];
+      o.theta = h_out4[4 * s + 3];
+    }
+    float a = 0;
+    if (cudaEventElapsedTime(&a, b->ev[0], b->ev[1]) == cudaSuccess) S.h2d_ms = a;
+    if (cudaEventElapsedTime(&a, b->ev[2], b->ev[3]) == cudaSuccess) S.prep_ms = a;
+    if (cudaEventElapsedTime(&a, b->ev[3], b->ev[4]) == cudaSuccess) S.march_ms = a;
+    if (cudaEventElapsedTime(&a, b->ev[4], b->ev[5]) == cudaSuccess) S.outputs_ms = a;
+    if (cudaEventElapsedTime(&a, b->ev[5], b->ev[6]) == cudaSuccess) S.d2h_ms = a;
+    cudaGetLastError();  // elapsed-time queries on unrecorded events are not errors here
+    S.d2h_bytes = static_cast<double>(sizeof(double) * 4 * m + sizeof(int32_t) * m);
+  }
+  uint64_t failed = 0;
+  for (int64_t i = 0; i < b->n; ++i) failed += out[i].status != 0;
+  S.options = b->n;
+  S.tiles = b->ntiles;
+  S.algo_flops = b->algo_flops;
+  S.h2d_bytes = b->h2d_bytes;
+  S.host_prep_ms = b->host_prep_ms;
+  S.kernel_launches = m > 0 ? 3 : 0;
+  return failed;
+}
+
+}  // namespace
+}  // namespace mgpu
+
+using namespace mgpu;
+
+extern "C" {
+
+const char* mango_gpu_build_info(void) {
+  return "mango-option GB300 engine: sm_103a FP64 TR-BDF2/projected-Thomas march";
+}
+
+MangoStatus mango_gpu_context_create(int32_t device, MangoGpuContext** out, MangoError* err) {
+  if (!out) {
+    set_err(err, MANGO_ERR_VALIDATION, "out is null");
+    return MANGO_ERR_VALIDATION;
+  }
+  *out = nullptr;
+  MangoGpuContext* ctx = nullptr;
+  try {
+    int count = 0;
+    check(cudaGetDeviceCount(&count), "cudaGetDeviceCount");
+    if (device < 0 || device >= count) throw CudaError("no such CUDA device");
+    cudaDeviceProp prop{};
+    check(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+    if (prop.major != 10 || prop.minor != 3)
+      throw CudaError("this library is built for sm_103a (GB300) only; device is sm_" +
+                      std::to_string(prop.major) + std::to_string(prop.minor));
+    check(cudaSetDevice(device), "cudaSetDevice");
+    ctx = new MangoGpuContext();
+    ctx->device = device;
+    ctx->num_sms = prop.multiProcessorCount;
+    check(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking), "stream");
+    ctx->stream = ctx->own_stream;
+    int bps = 0;
+    check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, march_kernel, 128, 0), "occupancy");
+    ctx->march_blocks_per_sm = std::max(1, bps);
+    *out = ctx;
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    if (ctx && ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+void mango_gpu_context_destroy(MangoGpuContext* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+}
+
+MangoStatus mango_gpu_context_set_stream(MangoGpuContext* ctx, void* stream) {
+  if (!ctx) return MANGO_ERR_VALIDATION;
+  ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  return MANGO_OK;
+}
+
+MangoStatus mango_gpu_batch_create(MangoGpuContext* ctx, const MangoPricingParams* params,
+                                   uint64_t n, const MangoGpuGrid* grids, uint64_t grid_stride,
+                                   const MangoGpuTrbdf2* trbdf2, MangoGpuBatch** out,
+                                   MangoError* err) {
+  if (!ctx || !out || (n > 0 && !params)) {
+    set_err(err, MANGO_ERR_VALIDATION, "null context, params or out");
+    return MANGO_ERR_VALIDATION;
+  }
+  *out = nullptr;
+  if (n > (1ull << 30)) {
+    set_err(err, MANGO_ERR_VALIDATION, "batch above 2^30 options");
+    return MANGO_ERR_VALIDATION;
+  }
+  try {
+    check(cudaSetDevice(ctx->device), "cudaSetDevice");
+    *out = create_batch(ctx, params, static_cast<int64_t>(n), grids, grid_stride, trbdf2);
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+MangoStatus mango_gpu_batch_run(MangoGpuBatch* b, MangoError* err) {
+  if (!b) {
+    set_err(err, MANGO_ERR_VALIDATION, "null batch");
+    return MANGO_ERR_VALIDATION;
+  }
+  try {
+    check(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+    run_batch(b);
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+MangoStatus mango_gpu_batch_results(MangoGpuBatch* b, MangoGpuAmericanOut* out,
+                                    uint64_t* out_failed, MangoError* err) {
+  if (!b || (b->n > 0 && !out)) {
+    set_err(err, MANGO_ERR_VALIDATION, "null batch or out");
+    return MANGO_ERR_VALIDATION;
+  }
+  if (!b->ran) {
+    set_err(err, MANGO_ERR_VALIDATION, "mango_gpu_batch_run has not been called");
+    return MANGO_ERR_VALIDATION;
+  }
+  try {
+    check(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+    std::string first;
+    const uint64_t failed = fetch_batch(b, out, &first);
+    if (out_failed) *out_failed = failed;
+    if (failed && err) set_err(err, MANGO_OK, first.empty() ? "solver failure" : first);
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+void mango_gpu_batch_destroy(MangoGpuBatch* b) {
+  if (!b) return;
+  cudaSetDevice(b->ctx->device);
+  cudaStreamSynchronize(b->ctx->stream);
+  destroy_batch(b);
+}
+
+MangoStatus mango_gpu_batch_timings(MangoGpuBatch* b, int32_t reset, double* prep_ms,
+                                    double* march_ms, double* outputs_ms, int64_t* runs,
+                                    MangoError* err) {
+  if (!b) {
+    set_err(err, MANGO_ERR_VALIDATION, "null batch");
+    return MANGO_ERR_VALIDATION;
+  }
+  try {
+    check(cudaStreamSynchronize(b->ctx->stream), "stream synchronize");
+    const int64_t k = std::min<int64_t>(b->runs, MangoGpuBatch::kMaxTimedRuns);
+    double acc[3] = {0, 0, 0};
+    for (int64_t r = 0; r < k; ++r)
+      for (int j = 0; j < 3; ++j) {
+        float ms = 0;
+        check(cudaEventElapsedTime(&ms, b->run_ev[4 * r + j], b->run_ev[4 * r + j + 1]), "elapsed");
+        acc[j] += ms;
+      }
+    const double d = k > 0 ? static_cast<double>(k) : 1.0;
+    if (prep_ms) *prep_ms = acc[0] / d;
+    if (march_ms) *march_ms = acc[1] / d;
+    if (outputs_ms) *outputs_ms = acc[2] / d;
+    if (runs) *runs = k;
+    if (reset) b->runs = 0;
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+MangoStatus mango_gpu_price_american_batch(MangoGpuContext* ctx, const MangoPricingParams* params,
+                                           uint64_t n, const MangoGpuGrid* grids,
+                                           uint64_t grid_stride, const MangoGpuTrbdf2* trbdf2,
+                                           MangoGpuAmericanOut* out, uint64_t* out_failed,
+                                           MangoError* err) {
+  if (!ctx || (n > 0 && (!params || !out))) {
+    set_err(err, MANGO_ERR_VALIDATION, "null context, params or out");
+    return MANGO_ERR_VALIDATION;
+  }
+  auto t0 = Clock::now();
+  MangoGpuBatch* b = nullptr;
+  MangoStatus st = mango_gpu_batch_create(ctx, params, n, grids, grid_stride, trbdf2, &b, err);
+  if (st != MANGO_OK) return st;
+  st = mango_gpu_batch_run(b, err);
+  if (st == MANGO_OK) st = mango_gpu_batch_results(b, out, out_failed, err);
+  mango_gpu_batch_destroy(b);
+  ctx->stats.total_ms = ms_since(t0);
+  return st;
+}
+
+MangoStatus mango_gpu_fp64_probe(MangoGpuContext* ctx, double* tflops, MangoError* err) {
+  if (!ctx || !tflops) {
+    set_err(err, MANGO_ERR_VALIDATION, "null argument");
+    return MANGO_ERR_VALIDATION;
+  }
+  try {
+    check(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    const int blocks = ctx->num_sms * 4, threads = 256, iters = 4096;
+    double* d = nullptr;
+    check(cudaMallocAsync(reinterpret_cast<void**>(&d), sizeof(double) * blocks * threads, st),
+          "cudaMallocAsync");
+    cudaEvent_t e0, e1;
+    check(cudaEventCreate(&e0), "event");
+    check(cudaEventCreate(&e1), "event");
+    fp64_probe_kernel<<<blocks, threads, 0, st>>>(d, 64);  // warm-up
+    double best = 0;
+    for (int rep = 0; rep < 3; ++rep) {
+      check(cudaEventRecord(e0, st), "event");
+      fp64_probe_kernel<<<blocks, threads, 0, st>>>(d, iters);
+      check(cudaEventRecord(e1, st), "event");
+      check(cudaEventSynchronize(e1), "event sync");
+      float ms = 0;
+      check(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+      // 8 independent chains x iters FMAs per thread, 2 flops each
+      const double fl = 2.0 * 8.0 * iters * static_cast<double>(blocks) * threads;
+      best = std::max(best, fl / (ms * 1e-3) / 1e12);
+    }
+    check(cudaFreeAsync(d, st), "cudaFreeAsync");
+    check(cudaStreamSynchronize(st), "sync");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *tflops = best;
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+MangoStatus mango_gpu_resolve_grid(const MangoPricingParams* params, const MangoGpuGrid* grid,
+                                   double* x_out, int64_t cap, int64_t* n_space,
+                                   int64_t* n_time, MangoError* err) {
+  if (!params || !n_space || !n_time) {
+    set_err(err, MANGO_ERR_VALIDATION, "null argument");
+    return MANGO_ERR_VALIDATION;
+  }
+  try {
+    std::string m = validate(*params);
+    Resolved r;
+    std::vector<double> scratch;
+    if (m.empty()) {
+      MangoGpuGrid g{};
+      g.kind = MANGO_GPU_GRID_AUTO;
+      if (grid) g = *grid;
+      m = resolve(*params, g, &r, &scratch);
+    }
+    if (!m.empty()) {
+      set_err(err, MANGO_ERR_VALIDATION, m);
+      return MANGO_ERR_VALIDATION;
+    }
+    *n_space = r.spec.n;
+    *n_time = r.nt;
+    if (x_out && cap >= r.spec.n) generate_grid(r.spec, x_out);
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+MangoStatus mango_gpu_last_stats(const MangoGpuContext* ctx, MangoGpuStats* out) {
+  if (!ctx || !out) return MANGO_ERR_VALIDATION;
+  const Stats& s = ctx->stats;
+  out->host_prep_ms = s.host_prep_ms;
+  out->h2d_ms = s.h2d_ms;
+  out->prep_ms = s.prep_ms;
+  out->march_ms = s.march_ms;
+  out->outputs_ms = s.outputs_ms;
+  out->d2h_ms = s.d2h_ms;
+  out->total_ms = s.total_ms;
+  out->algo_flops = s.algo_flops;
+  out->h2d_bytes = s.h2d_bytes;
+  out->d2h_bytes = s.d2h_bytes;
+  out->options = s.options;
+  out->tiles = s.tiles;
+  out->kernel_launches = s.kernel_launches;
+  return MANGO_OK;
+}
+
+}  // extern "C"

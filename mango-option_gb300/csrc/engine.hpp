@@ -1,0 +1,101 @@
+// engine.hpp -- host side of the GPU engine: the context and resident-batch
+// objects behind the C ABI (include/mango_gpu.h), device buffer management
+// and the batch pipeline (validate -> grid -> sort/tile -> upload -> setup ->
+// march -> outputs -> download).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "grid_host.hpp"
+#include "march.cuh"
+#include "mango_gpu.h"
+
+namespace mgpu {
+
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+void check(cudaError_t e, const char* what);
+
+// Grow-only device allocation.
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  void* get(size_t bytes);
+  void release();
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Grow-only pinned host allocation.
+struct HostBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  void* get(size_t bytes);
+  void release();
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// One option after validation and grid resolution, host side.
+struct Resolved {
+  GridSpec spec;
+  int64_t nt = 0;
+  int32_t status = 0;  // MangoStatus; non-zero options never reach the GPU
+  int32_t orig = 0;
+};
+
+// Timings of the last batch call (milliseconds) and work counters.
+struct Stats {
+  double host_prep_ms = 0, h2d_ms = 0, prep_ms = 0, march_ms = 0, outputs_ms = 0,
+         d2h_ms = 0, total_ms = 0;
+  int64_t options = 0, tiles = 0, kernel_launches = 0;
+  double algo_flops = 0;
+  double h2d_bytes = 0, d2h_bytes = 0;
+};
+
+// Validation (validate_pricing_params plus the engine's scope) and grid
+// resolution; empty string when the option is accepted.
+std::string validate(const MangoPricingParams& p);
+std::string resolve(const MangoPricingParams& p, const MangoGpuGrid& g, Resolved* r,
+                    std::vector<double>* scratch);
+
+// Run f(i) for i in [0, n) on all host cores.
+void parallel_for(int64_t n, const std::function<void(int64_t)>& f);
+
+}  // namespace mgpu
+
+struct MangoGpuContext {
+  int device = 0;
+  int num_sms = 0;
+  int march_blocks_per_sm = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;  // own_stream or a caller's stream
+  mgpu::Stats stats;
+};
+
+struct MangoGpuBatch {
+  MangoGpuContext* ctx = nullptr;
+  int64_t n = 0;                          // caller's slot count
+  std::vector<mgpu::Resolved> res;        // per slot
+  std::vector<std::string> msgs;          // per slot validation message
+  std::vector<int32_t> order;             // sorted position -> slot
+  int32_t ntiles = 0;
+  mgpu::MarchConst mc{};
+  double algo_flops = 0;
+  double h2d_bytes = 0;
+  double host_prep_ms = 0;
+  mgpu::DevBuf d_pool, d_xs, d_flags, d_opts, d_tiles, d_mode, d_status, d_out4, d_queue;
+  mgpu::HostBuf h_xs, h_opts, h_tiles, h_out4, h_status;
+  cudaEvent_t ev[8] = {};
+  bool ran = false;
+  // Per-run kernel timing: 4 events per run (before setup, after setup,
+  // after march, after outputs), kept for the last kMaxTimedRuns runs.
+  static constexpr int kMaxTimedRuns = 256;
+  std::vector<cudaEvent_t> run_ev;
+  int64_t runs = 0;      // runs since the last timing reset
+};

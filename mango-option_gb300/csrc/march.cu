@@ -1,0 +1,595 @@
+// march.cu -- FP64 TR-BDF2 / projected-Thomas American-option march on sm_103a.
+//
+// Restates, per option, PDESolver::solve with the obstacle path
+// (src/pde/internal/pde_solver.hpp:114-178, 342-447, 525-729) and
+// solve_thomas_projected (src/math/thomas_solver.hpp:321-420), then the
+// AmericanOptionResult functionals (src/option/american_option_result.cpp:
+// 25-121).
+//
+// GB300 design.  FP64 issue rate is the bound (the part has a small fraction
+// of its FP32 rate in FP64), so the march spends as few FP64 instructions per
+// grid row as the reference's arithmetic allows:
+//  * the operator and the stage matrices are time invariant for a constant
+//    rate, so prep_kernel builds them once per option, together with the
+//    Thomas factorisation of each stage matrix (c'_i and 1/pivot_i);
+//  * the steady-state row update is then divide-free:
+//      stage 1  d'_i = e_l u_{i-1} + e_d u_i + e_u u_{i+1} - l1h d'_{i-1}
+//      stage 2  d'_i = a2h g_i + b2h u_i - l2h d'_{i-1}
+//      back     x_i  = max(d'_i - c'_i x_{i+1}, psi_i)
+//  * rows locked to the obstacle (pde_solver.hpp:635-680) change the matrix;
+//    after a locked row the factorisation is recomputed row by row, exactly
+//    as the reference does, until the recomputed c'_i is bit-identical to
+//    the cached one -- from there on both recurrences coincide, so the cached
+//    values are exact again (3-4 rows in practice).
+#include "march.cuh"
+
+#include <cuda_runtime.h>
+#include <climits>
+
+namespace mgpu {
+
+namespace {
+
+struct TileView {
+  double* B;
+  int NX;
+  int lane;
+  __device__ __forceinline__ double& at(int a, int i) const {
+    return B[(static_cast<size_t>(a) * NX + i) * kTile + lane];
+  }
+  __device__ __forceinline__ double* row(int a) const {
+    return B + static_cast<size_t>(a) * NX * kTile + lane;
+  }
+};
+
+#define ROW(p, i) (p)[static_cast<size_t>(i) * kTile]
+
+// std::max(a, b) as the reference spells it: (a < b) ? b : a.
+__device__ __forceinline__ double dmax_ref(double a, double b) { return (a < b) ? b : a; }
+
+__device__ __forceinline__ bool same_bits(double a, double b) {
+  return __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- setup --
+// One lane per option.  Builds psi, the stencils, the three stage-matrix
+// band sets, both cached factorisations, the lock-candidate flags and u^0.
+__global__ void prep_kernel(const TileDev* __restrict__ tiles, int ntiles,
+                            const OptDev* __restrict__ opts, const double* __restrict__ xs,
+                            double* __restrict__ pool, uint8_t* __restrict__ flags,
+                            int32_t* __restrict__ mode, MarchConst mc) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = gt / kTile, lane = gt % kTile;
+  if (t >= ntiles) return;
+  const TileDev td = tiles[t];
+  if (lane >= td.count) return;
+  const int k = td.first + lane;
+  const OptDev o = opts[k];
+  const int n = o.n;
+  TileView V{pool + td.off, td.nx, lane};
+  const double* X = xs + td.xoff + lane;
+  auto x = [&](int i) { return X[static_cast<size_t>(i) * kTile]; };
+  uint8_t* F = flags + td.foff + lane;
+
+  const double rate = o.r;
+  const double hss = 0.5 * o.sigma * o.sigma;  // black_scholes_pde.hpp:45
+  const double drift = rate - o.q - hss;       // black_scholes_pde.hpp:73-74
+  const double dt = o.dt;
+  const double w1 = mc.gamma * dt / 2.0;       // trbdf2_config.hpp:39-41
+  const double w2 = (1.0 - mc.gamma) * dt / (2.0 - mc.gamma);
+  const double wr = 0.5 * dt;                  // pde_solver.hpp:419
+
+  // GridSpacing uniformity test (grid.hpp:680-711).
+  const double expected = (x(n - 1) - x(0)) / static_cast<double>(n - 1);
+  bool uniform = true;
+  for (int i = 1; i < n; ++i)
+    if (fabs((x(i) - x(i - 1)) - expected) > 100.0 * 2.220446049250313e-16) {
+      uniform = false;
+      break;
+    }
+  const double u_dx_inv = 1.0 / expected;
+  const double u_dx2 = u_dx_inv * u_dx_inv;
+  const double u_hdx = u_dx_inv * 0.5;
+
+  // Obstacle = payoff (option_spec.hpp:122-135); psi_max as max_element.
+  double psi_max = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double ex = exp(x(i));
+    const double p = o.is_put ? dmax_ref(1.0 - ex, 0.0) : dmax_ref(ex - 1.0, 0.0);
+    V.at(A_PSI, i) = p;
+    if (i == 0 || psi_max < p) psi_max = p;
+  }
+  const double thr = 0.95 * psi_max;
+
+  int32_t md = uniform ? 2 : 0;
+  double cp1 = 0.0, cp2 = 0.0;  // cached factor recurrences; row 0: c'_0 = 0/1
+  for (int i = 0; i < td.nx; ++i) F[static_cast<size_t>(i) * kTile] = 0;
+  for (int i = 1; i < n - 1; ++i) {
+    const double xl = x(i - 1), xi = x(i), xr = x(i + 1);
+    const double pl = V.at(A_PSI, i - 1), pi = V.at(A_PSI, i), pr = V.at(A_PSI, i + 1);
+    // Explicit operator L(u)_i = A u_{i-1} + Bc u_i + C u_{i+1}; L(psi)_i in
+    // the reference's apply order for the lock test's sign.
+    double A, Bc, C, lpsi;
+    if (uniform) {
+      A = hss * u_dx2 - drift * u_hdx;
+      Bc = -2.0 * hss * u_dx2 - rate;
+      C = hss * u_dx2 + drift * u_hdx;
+      const double d2 = fma(pr + pl, u_dx2, -2.0 * pi * u_dx2);  // centered_difference.hpp:24-48
+      const double d1 = (pr - pl) * u_hdx;
+      lpsi = hss * d2 + drift * d1 - rate * pi;
+    } else {
+      const double dl = xi - xl, dr = xr - xi;  // grid.hpp:552-565
+      const double dc = 0.5 * (dl + dr);
+      const double li = 1.0 / dl, ri = 1.0 / dr, ci = 1.0 / dc;
+      const double wl = dr / (dl + dr), wrr = dl / (dl + dr);
+      A = hss * (li * ci) - drift * (wl * li);
+      Bc = -hss * ((ri + li) * ci) + drift * (wl * li - wrr * ri) - rate;
+      C = hss * (ri * ci) + drift * (wrr * ri);
+      const double fwd = (pr - pi) * ri;  // centered_difference.hpp:56-99
+      const double bwd = (pi - pl) * li;
+      const double d2 = (fwd - bwd) * ci;
+      const double d1 = wl * (pi - pl) * li + wrr * (pr - pi) * ri;
+      lpsi = hss * d2 + drift * d1 - rate * pi;
+    }
+    // Lock conditions 1 and 3 (pde_solver.hpp:635-680) are time invariant
+    // here; condition 2 (u - psi < 1e-8) is tested in every stage.
+    F[static_cast<size_t>(i) * kTile] = (psi_max > 0.0 && pi > thr && lpsi < 0.0) ? 1 : 0;
+
+    const double el = w1 * A, ed = 1.0 + w1 * Bc, eu = w1 * C;
+    V.at(A_E1L0, i) = el;
+    V.at(A_E1D0, i) = ed;
+    V.at(A_E1U0, i) = eu;
+
+    // assemble_jacobian (spatial_operator.hpp:123-163).
+    const double b_coef = rate - o.q - hss;
+    const double dxl = xi - xl, dxr = xr - xi;
+    const double dxa = (dxl + dxr) / 2.0;
+    const double d2m = hss / (dxl * dxa);
+    const double d2i = -hss * (1.0 / dxl + 1.0 / dxr) / dxa;
+    const double d2p = hss / (dxr * dxa);
+    const double d1d = dxl + dxr;
+    const double d1m = -b_coef * dxr / (dxl * d1d);
+    const double d1i = b_coef * (dxr - dxl) / (dxl * dxr);
+    const double d1p = b_coef * dxl / (dxr * d1d);
+    const double jl = d2m + d1m;
+    const double jd = d2i + d1i + (-rate);
+    const double ju = d2p + d1p;
+    const double l1 = -w1 * jl, dg1 = 1.0 - w1 * jd, u1 = -w1 * ju;
+    const double l2 = -w2 * jl, dg2 = 1.0 - w2 * jd, u2 = -w2 * ju;
+    V.at(A_L1, i) = l1;
+    V.at(A_D1, i) = dg1;
+    V.at(A_U1, i) = u1;
+    V.at(A_L2, i) = l2;
+    V.at(A_D2, i) = dg2;
+    V.at(A_U2, i) = u2;
+    V.at(A_LR, i) = -wr * jl;
+    V.at(A_DR, i) = 1.0 - wr * jd;
+    V.at(A_UR, i) = -wr * ju;
+
+    // Cached factorisations (the thomas_solver.hpp:382-395 recurrence).
+    const double den1 = fma(-l1, cp1, dg1);
+    const double den2 = fma(-l2, cp2, dg2);
+    if (fabs(den1) < 1e-15 || fabs(den2) < 1e-15) md |= 1;  // never trust the cache
+    const double inv1 = 1.0 / den1, inv2 = 1.0 / den2;
+    cp1 = u1 * inv1;
+    cp2 = u2 * inv2;
+    V.at(A_C1, i) = cp1;
+    V.at(A_C2, i) = cp2;
+    V.at(A_E1L, i) = el * inv1;
+    V.at(A_E1D, i) = ed * inv1;
+    V.at(A_E1U, i) = eu * inv1;
+    V.at(A_L1H, i) = l1 * inv1;
+    V.at(A_A2H, i) = mc.alpha * inv2;
+    V.at(A_B2H, i) = mc.beta * inv2;
+    V.at(A_L2H, i) = l2 * inv2;
+  }
+  mode[k] = md;
+
+  // PDESolver::initialize (pde_solver.hpp:96-109): payoff, boundary values
+  // at t = 0, then the obstacle projection.
+  for (int i = 1; i < n - 1; ++i) V.at(A_U, i) = V.at(A_PSI, i);
+  const double bcr0 = o.is_put ? 0.0 : o.exp_xr - exp(-rate * 0.0);
+  V.at(A_U, 0) = dmax_ref(o.bc_left, V.at(A_PSI, 0));
+  V.at(A_U, n - 1) = dmax_ref(bcr0, V.at(A_PSI, n - 1));
+}
+
+// ---------------------------------------------------------------- march --
+
+namespace {
+
+enum StageKind { kRannacher = 0, kStage1 = 1, kStage2 = 2 };
+
+// One implicit stage for one lane (solve_implicit_stage_projected).
+//   kRannacher: rhs = in (u_prev), guess = in, bands LR/DR/UR, never cached.
+//   kStage1:    rhs = u + w1 L(u) of in (= u^n), guess = in.
+//   kStage2:    rhs = alpha in + beta in2 (in = u^{n+gamma}, in2 = u^n), guess = in.
+// Lanes that are not live execute no memory operation.
+template <int K>
+__device__ __forceinline__ void stage(bool live, int n, const TileView& V,
+                                      const uint8_t* __restrict__ F, bool nocache,
+                                      double bcl, double bcr, double alpha, double beta,
+                                      int a_in, int a_in2, int a_out, int32_t& st) {
+  const int NX = V.NX;
+  const double* IN = V.row(a_in);
+  const double* IN2 = V.row(a_in2);
+  const double* PSI = V.row(A_PSI);
+  double* OUT = V.row(a_out);
+  double* Dd = V.row(A_D);
+  double* CP = V.row(A_CP);
+  constexpr int aC = (K == kStage2) ? A_C2 : A_C1;
+  constexpr int aL = (K == kRannacher) ? A_LR : (K == kStage1 ? A_L1 : A_L2);
+  constexpr int aDg = (K == kRannacher) ? A_DR : (K == kStage1 ? A_D1 : A_D2);
+  constexpr int aU = (K == kRannacher) ? A_UR : (K == kStage1 ? A_U1 : A_U2);
+  const double* Cc = V.row(aC);
+  const double* Lb = V.row(aL);
+  const double* Db = V.row(aDg);
+  const double* Ub = V.row(aU);
+  const bool always_fresh = (K == kRannacher) || nocache;
+
+  // ---- forward elimination
+  double dprev = bcl;  // d'_0 = rhs_0 / 1 on the Dirichlet row
+  double cprev = 0.0;  // recomputed c'_{i-1}; valid whenever `fresh`
+  bool fresh = always_fresh;
+  int lo = INT_MAX, hi = -1;  // rows [lo, hi] take c' from CP
+  double um = 0.0, u0 = 0.0, up = 0.0;
+  if (K == kStage1 && live) {
+    um = ROW(IN, 0);
+    u0 = ROW(IN, 1);
+  }
+  for (int i = 1; i < NX - 1; ++i) {
+    if (!live || i >= n - 1) continue;
+    double g;
+    if (K == kStage1) {
+      up = ROW(IN, i + 1);
+      g = u0;
+    } else {
+      g = ROW(IN, i);
+    }
+    bool lock = false;
+    double psi_i = 0.0;
+    if (ROW(F, i)) {
+      psi_i = ROW(PSI, i);
+      lock = (g - psi_i < 1e-8);
+    }
+    double dcur;
+    bool own;  // this row's c' is not the cached one
+    if (lock) {
+      dcur = psi_i;  // identity row with rhs psi: c' = 0, d' = psi
+      cprev = 0.0;
+      fresh = true;
+      own = true;
+    } else if (!fresh) {
+      if (K == kStage1) {
+        const double part =
+            fma(V.at(A_E1L, i), um, fma(V.at(A_E1D, i), u0, V.at(A_E1U, i) * up));
+        dcur = fma(-V.at(A_L1H, i), dprev, part);
+      } else {
+        const double part = fma(V.at(A_A2H, i), g, V.at(A_B2H, i) * ROW(IN2, i));
+        dcur = fma(-V.at(A_L2H, i), dprev, part);
+      }
+      own = false;
+    } else {
+      double rhs;
+      if (K == kStage1)
+        rhs = fma(V.at(A_E1L0, i), um, fma(V.at(A_E1D0, i), u0, V.at(A_E1U0, i) * up));
+      else if (K == kStage2)
+        rhs = fma(alpha, g, beta * ROW(IN2, i));
+      else
+        rhs = g;
+      const double l = ROW(Lb, i);
+      const double denom = fma(-l, cprev, ROW(Db, i));
+      if (fabs(denom) < 1e-15) st = kStatusSolver;  // thomas_solver.hpp:386-388
+      const double inv = 1.0 / denom;
+      const double ccur = ROW(Ub, i) * inv;
+      dcur = fma(-l, dprev, rhs) * inv;
+      cprev = ccur;
+      if (!always_fresh) fresh = !same_bits(ccur, ROW(Cc, i));
+      own = true;
+    }
+    if (own) {
+      if (hi >= 0 && i > hi + 1)
+        for (int j = hi + 1; j < i; ++j) ROW(CP, j) = ROW(Cc, j);
+      ROW(CP, i) = cprev;
+      if (lo == INT_MAX) lo = i;
+      hi = i;
+    }
+    ROW(Dd, i) = dcur;
+    dprev = dcur;
+    if (K == kStage1) {
+      um = u0;
+      u0 = up;
+    }
+  }
+
+  // ---- projected back substitution; last row d' = rhs = bcr
+  if (!live) return;
+  double xnext = dmax_ref(bcr, ROW(PSI, n - 1));
+  for (int i = NX - 2; i >= 1; --i) {
+    if (i > n - 2) continue;
+    const double c = (i >= lo && i <= hi) ? ROW(CP, i) : ROW(Cc, i);
+    const double xv = dmax_ref(fma(-c, xnext, ROW(Dd, i)), ROW(PSI, i));
+    ROW(OUT, i) = xv;
+    xnext = xv;
+  }
+  // apply_boundary_conditions after the solve (pde_solver.hpp:724-726).
+  ROW(OUT, 0) = bcl;
+  ROW(OUT, n - 1) = bcr;
+}
+
+__device__ __forceinline__ double right_bc(const OptDev& o, double t) {
+  return o.is_put ? 0.0 : o.exp_xr - exp(-o.r * t);  // american_option.cpp:276-290
+}
+
+}  // namespace
+
+// Persistent march: each warp pulls tiles (largest first) from the queue.
+__global__ void __launch_bounds__(128) march_kernel(
+    const TileDev* __restrict__ tiles, int ntiles, const OptDev* __restrict__ opts,
+    double* __restrict__ pool, const uint8_t* __restrict__ flags,
+    const int32_t* __restrict__ mode, int32_t* __restrict__ status, int* __restrict__ queue,
+    MarchConst mc) {
+  const int lane = threadIdx.x & (kTile - 1);
+  for (;;) {
+    int t = 0;
+    if (lane == 0) t = atomicAdd(queue, 1);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= ntiles) break;
+    const TileDev td = tiles[t];
+    const bool active = lane < td.count;
+    const int k = td.first + lane;
+    OptDev o{};
+    int32_t md = 0;
+    if (active) {
+      o = opts[k];
+      md = mode[k];
+    }
+    const bool nocache = (md & 1) != 0;
+    const int n = active ? o.n : 0;
+    const int nt = active ? o.nt : 0;
+    const TileView V{pool + td.off, td.nx, lane};
+    const uint8_t* F = flags + td.foff + lane;
+    int32_t st = kStatusOk;
+    const double dt = o.dt;
+    int step = 0;
+    if (mc.rannacher) {
+      // solve_rannacher_startup (pde_solver.hpp:413-447): two implicit Euler
+      // half steps with coefficient dt/2 to t + dt/2 and t + dt.
+      const double t_mid = 0.0 + 0.5 * dt;
+      const double t_next = 0.0 + dt;
+      stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_mid), mc.alpha,
+                        mc.beta, A_U, A_U, A_G, st);
+      stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_next), mc.alpha,
+                        mc.beta, A_G, A_G, A_U, st);
+      step = 1;
+    }
+    for (; step < td.nt; ++step) {
+      const bool live = active && step < nt && st == kStatusOk;
+      // Time points are i*dt (time_domain.hpp:120-128).
+      const double t = static_cast<double>(step) * dt;
+      const double t1 = t + mc.gamma * dt;
+      const double tn = static_cast<double>(step + 1) * dt;
+      const bool last = (step == nt - 1);
+      stage<kStage1>(live, n, V, F, nocache, o.bc_left, right_bc(o, t1), mc.alpha, mc.beta,
+                     A_U, A_U, A_G, st);
+      stage<kStage2>(live, n, V, F, nocache, o.bc_left, right_bc(o, tn), mc.alpha, mc.beta,
+                     A_G, A_U, last ? A_G : A_U, st);
+    }
+    if (active) status[k] = st;
+  }
+}
+
+// -------------------------------------------------------------- outputs --
+
+namespace {
+
+// Natural cubic spline through (x, y) (cubic_spline_solver.hpp:74-170,
+// 264-369): solve for the second-derivative terms c_i with the plain Thomas
+// recurrence (thomas_solver.hpp:86-198), then evaluate at xe.  cw/dw are
+// per-lane scratch rows of length >= n.
+__device__ void spline_at(const double* __restrict__ X, const double* __restrict__ Y, int n,
+                          double xe, double* cw, double* dw, int iv, double* val,
+                          double* der) {
+  auto x = [&](int i) { return ROW(X, i); };
+  auto y = [&](int i) { return ROW(Y, i); };
+  auto h = [&](int i) { return x(i + 1) - x(i); };
+  double ci = 0.0, ci1 = 0.0;  // c[iv], c[iv+1]
+  const int m = n - 2;
+  if (m >= 1) {
+    // system row j (0..m-1) for knot k = j+1:
+    //   lower h[j] (j>0), diag 2(h[j]+h[j+1]), upper h[j+1] (j<m-1)
+    auto rhs = [&](int j) {
+      const double sr = (y(j + 2) - y(j + 1)) / h(j + 1);
+      const double sl = (y(j + 1) - y(j)) / h(j);
+      return 3.0 * (sr - sl);
+    };
+    if (m == 1) {
+      const double s = rhs(0) / (2.0 * (h(0) + h(1)));
+      if (iv == 0) { ci = 0.0; ci1 = s; } else { ci = s; ci1 = 0.0; }
+    } else {
+      // forward
+      double diag0 = 2.0 * (h(0) + h(1));
+      double cp = h(1) / diag0;
+      double dp = rhs(0) / diag0;
+      ROW(cw, 0) = cp;
+      ROW(dw, 0) = dp;
+      for (int j = 1; j < m - 1; ++j) {
+        const double lower = h(j);
+        const double denom = fma(-lower, cp, 2.0 * (h(j) + h(j + 1)));
+        const double inv = 1.0 / denom;
+        cp = h(j + 1) * inv;
+        dp = fma(-lower, dp, rhs(j)) * inv;
+        ROW(cw, j) = cp;
+        ROW(dw, j) = dp;
+      }
+      {
+        const int j = m - 1;
+        const double lower = h(j);
+        const double denom = fma(-lower, cp, 2.0 * (h(j) + h(j + 1)));
+        dp = fma(-lower, dp, rhs(j)) / denom;
+        ROW(dw, j) = dp;
+      }
+      // backward: sol[j] = c[j+1]; need c[iv] and c[iv+1].
+      double s = ROW(dw, m - 1);
+      // c index k = j+1; walk j from m-1 down to max(iv-1, 0)
+      auto take = [&](int kk, double v) {
+        if (kk == iv) ci = v;
+        if (kk == iv + 1) ci1 = v;
+      };
+      take(m, s);
+      for (int j = m - 1; j > 0; --j) {
+        s = fma(-ROW(cw, j - 1), s, ROW(dw, j - 1));
+        take(j, s);
+        if (j <= iv) break;
+      }
+    }
+  }
+  const double hi = h(iv);
+  const double a = y(iv);
+  const double b = (y(iv + 1) - y(iv)) / hi - hi * (2.0 * ci + ci1) / 3.0;
+  const double d = (ci1 - ci) / (3.0 * hi);
+  const double dx = xe - x(iv);
+  *val = a + b * dx + ci * (dx * dx) + d * (dx * dx * dx);
+  *der = b + 2.0 * ci * dx + 3.0 * d * (dx * dx);
+}
+
+// CenteredDifference first/second derivative at row i, zero outside the
+// rows [1, n-2) that AmericanOptionResult::gamma fills
+// (american_option_result.cpp:66-71).
+__device__ void stencil_at(const double* __restrict__ X, const double* __restrict__ U, int n,
+                           int i, bool uniform, double* d1, double* d2) {
+  *d1 = 0.0;
+  *d2 = 0.0;
+  if (i < 1 || i >= n - 2) return;
+  const double ul = ROW(U, i - 1), uc = ROW(U, i), ur = ROW(U, i + 1);
+  if (uniform) {
+    const double expected = (ROW(X, n - 1) - ROW(X, 0)) / static_cast<double>(n - 1);
+    const double dxi = 1.0 / expected;
+    const double dx2 = dxi * dxi;
+    *d2 = fma(ur + ul, dx2, -2.0 * uc * dx2);
+    *d1 = (ur - ul) * (dxi * 0.5);
+    return;
+  }
+  const double dl = ROW(X, i) - ROW(X, i - 1), dr = ROW(X, i + 1) - ROW(X, i);
+  const double dc = 0.5 * (dl + dr);
+  const double li = 1.0 / dl, ri = 1.0 / dr, ci = 1.0 / dc;
+  const double wl = dr / (dl + dr), wr = dl / (dl + dr);
+  *d2 = ((ur - uc) * ri - (uc - ul) * li) * ci;
+  *d1 = wl * (uc - ul) * li + wr * (ur - uc) * ri;
+}
+
+// CubicSpline::find_interval (cubic_spline_solver.hpp:348-368).
+__device__ int find_interval(const double* __restrict__ X, int n, double xe) {
+  if (xe <= ROW(X, 0)) return 0;
+  if (xe >= ROW(X, n - 1)) return n - 2;
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = lo + (hi - lo) / 2;
+    if (ROW(X, mid) < xe) lo = mid + 1; else hi = mid;
+  }
+  int idx = lo;
+  if (idx > 0 && (idx == n || ROW(X, idx) > xe)) --idx;
+  return idx < n - 2 ? idx : n - 2;
+}
+
+}  // namespace
+
+// value, delta, gamma, theta per option (american_option_result.cpp:25-121).
+// out4 is in sorted order; u_final is G unless (Rannacher && nt == 1).
+__global__ void outputs_kernel(const TileDev* __restrict__ tiles, int ntiles,
+                               const OptDev* __restrict__ opts, const double* __restrict__ xs,
+                               double* __restrict__ pool, const int32_t* __restrict__ mode,
+                               const int32_t* __restrict__ status, MarchConst mc,
+                               double* __restrict__ out4) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = gt / kTile, lane = gt % kTile;
+  if (t >= ntiles) return;
+  const TileDev td = tiles[t];
+  if (lane >= td.count) return;
+  const int k = td.first + lane;
+  const OptDev o = opts[k];
+  double* res = out4 + 4 * static_cast<size_t>(k);
+  if (status[k] != kStatusOk) {
+    res[0] = res[1] = res[2] = res[3] = __longlong_as_double(0x7ff8000000000000ll);
+    return;
+  }
+  const int n = o.n;
+  const TileView V{pool + td.off, td.nx, lane};
+  const double* X = xs + td.xoff + lane;
+  const bool swap = mc.rannacher && o.nt == 1;
+  const double* U = V.row(swap ? A_U : A_G);
+  const double* UP = V.row(swap ? A_G : A_U);
+  double* cw = V.row(A_CP);
+  double* dw = V.row(A_D);
+  const double xs_ = o.x_spot;
+  const int iv = find_interval(X, n, xs_);
+  double sv, sd;
+  spline_at(X, U, n, xs_, cw, dw, iv, &sv, &sd);
+  double value;
+  if (xs_ <= ROW(X, 0)) value = ROW(U, 0) * o.strike;
+  else if (xs_ >= ROW(X, n - 1)) value = ROW(U, n - 1) * o.strike;
+  else value = dmax_ref(0.0, sv) * o.strike;
+  const double delta = sd * (o.strike / o.spot);
+  // gamma: stencil derivatives linearly interpolated at x_spot.
+  int il, ir;
+  if (xs_ <= ROW(X, 0)) { il = ir = 0; }
+  else if (xs_ >= ROW(X, n - 1)) { il = ir = n - 1; }
+  else {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+      const int mid = lo + (hi - lo) / 2;
+      if (ROW(X, mid) < xs_) lo = mid + 1; else hi = mid;
+    }
+    ir = lo;
+    il = ir > 0 ? ir - 1 : 0;
+    if (fabs(ROW(X, ir) - xs_) < 1e-14) il = ir;
+  }
+  const bool uniform = (mode[k] & 2) != 0;
+  double d1l, d2l, d1r, d2r;
+  stencil_at(X, U, n, il, uniform, &d1l, &d2l);
+  double d1, d2;
+  if (il == ir) {
+    d1 = d1l;
+    d2 = d2l;
+  } else {
+    stencil_at(X, U, n, ir, uniform, &d1r, &d2r);
+    const double al = (xs_ - ROW(X, il)) / (ROW(X, ir) - ROW(X, il));
+    d1 = d1l + al * (d1r - d1l);
+    d2 = d2l + al * (d2r - d2l);
+  }
+  const double kos2 = o.strike / (o.spot * o.spot);
+  const double gam = fma(kos2, d2, -kos2 * d1);
+  // theta: (S_prev(x) - S(x)) / dt * K with an unclamped spline value.
+  double pv, pd;
+  spline_at(X, UP, n, xs_, cw, dw, iv, &pv, &pd);
+  const double theta = (pv - sv) / o.dt * o.strike;
+  res[0] = value;
+  res[1] = delta;
+  res[2] = gam;
+  res[3] = theta;
+}
+
+#undef ROW
+
+}  // namespace mgpu
+
+namespace mgpu {
+// Diagnostic FP64 FMA throughput probe: 8 independent FMA chains per thread
+// so issue, not latency, bounds it.  The result is stored so the work is kept.
+__global__ void fp64_probe_kernel(double* out, int iters) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  double a[8];
+  const double m = 1.0 + 1e-9 * (tid & 7), c = 1e-12;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = 0.5 + 0.01 * j + 1e-7 * tid;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = fma(a[j], m, c);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += a[j];
+  out[tid] = s;
+}
+}  // namespace mgpu

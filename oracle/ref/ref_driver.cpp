@@ -1,0 +1,211 @@
+// Test infrastructure only: a thin extern "C" driver over the UNMODIFIED
+// reference C++ sources (compiled from the reference tree by oracle/ref/Makefile
+// into oracle/_ref/).  It exists to (a) generate golden vectors for tests/golden
+// and (b) pin the C restatement in oracle/mango_oracle.c.  Nothing in the
+// product links or loads this library.
+//
+// Grid rule used by the fixed-size paths (BASELINE configs 0/1/3/4): the
+// spatial GridSpec comes from estimate_pde_grid with
+// min_spatial_points == max_spatial_points == nx
+// (src/option/grid_spec_types.cpp:37-118), and the time axis from
+// PDEGridConfig{spec, nt} (src/option/grid_spec_types.hpp:55-59).
+#include "mango/option/american_option.hpp"
+#include "mango/option/american_option_batch.hpp"
+#include "mango/option/iv_solver.hpp"
+#include "mango/option/grid_spec_types.hpp"
+#include "mango/math/bspline/bspline_nd.hpp"
+#include "mango/math/bspline/bspline_basis.hpp"
+
+#include <omp.h>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <array>
+
+using namespace mango;
+
+namespace {
+
+PricingParams make_params(double S, double K, double T, double sigma, double r,
+                          double q, int32_t is_put) {
+  PricingParams p;
+  p.spot = S;
+  p.strike = K;
+  p.maturity = T;
+  p.volatility = sigma;
+  p.rate = r;
+  p.dividend_yield = q;
+  p.option_type = is_put ? OptionType::PUT : OptionType::CALL;
+  return p;
+}
+
+// nx == 0 -> reference auto grid (GridAccuracyParams{}); else grid rule above.
+std::optional<PDEGridSpec> grid_for(const PricingParams& p, int64_t nx, int64_t nt,
+                                    double grid_sigma) {
+  if (nx <= 0) return std::nullopt;
+  GridAccuracyParams acc;
+  acc.min_spatial_points = static_cast<size_t>(nx);
+  acc.max_spatial_points = static_cast<size_t>(nx);
+  PricingParams pg = p;
+  if (grid_sigma > 0.0) pg.volatility = grid_sigma;
+  auto [spec, td] = estimate_pde_grid(pg, acc);
+  (void)td;
+  return PDEGridSpec{PDEGridConfig{spec, static_cast<size_t>(nt), {}}};
+}
+
+}  // namespace
+
+extern "C" {
+
+// Price n options through AmericanOptionSolver::create + solve, OpenMP over
+// options exactly like solve_regular_batch's loop body
+// (src/option/american_option_batch.cpp:442-511).
+// out4 = [value, delta, gamma, theta] per option; out_dims = [nx, nt].
+int32_t ref_price_batch(int64_t n, const double* S, const double* K, const double* T,
+                        const double* sigma, const double* r, const double* q,
+                        const int32_t* is_put, const int64_t* nx, const int64_t* nt,
+                        int32_t rannacher, int32_t n_threads, double* out4,
+                        int64_t* out_dims, int32_t* status) {
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    auto p = make_params(S[i], K[i], T[i], sigma[i], r[i], q[i], is_put[i]);
+    auto grid = grid_for(p, nx ? nx[i] : 0, nt ? nt[i] : 0, 0.0);
+    auto solver = AmericanOptionSolver::create(p, grid);
+    if (!solver) { status[i] = 1; continue; }
+    TRBDF2Config cfg;
+    cfg.rannacher_startup = rannacher != 0;
+    solver->set_trbdf2_config(cfg);
+    auto res = solver->solve();
+    if (!res) { status[i] = 5; continue; }
+    status[i] = 0;
+    out4[4 * i + 0] = res->value();
+    out4[4 * i + 1] = res->delta();
+    out4[4 * i + 2] = res->gamma();
+    out4[4 * i + 3] = res->theta();
+    if (out_dims) {
+      out_dims[2 * i + 0] = static_cast<int64_t>(res->grid()->n_space());
+      out_dims[2 * i + 1] = static_cast<int64_t>(res->grid()->time().n_steps());
+    }
+  }
+  return 0;
+}
+
+// Explicit PDEGridConfig per option: kind 2 = GridSpec::sinh_spaced(x_min,
+// x_max, n, alpha), kind 3 = GridSpec::uniform(x_min, x_max, n); nt steps.
+int32_t ref_price_explicit(int64_t n, const double* S, const double* K, const double* T,
+                           const double* sigma, const double* r, const double* q,
+                           const int32_t* is_put, const int32_t* kind, const double* x_min,
+                           const double* x_max, const int64_t* nx, const double* alpha,
+                           const int64_t* nt, int32_t rannacher, double* out4, int32_t* status) {
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t i = 0; i < n; ++i) {
+    auto p = make_params(S[i], K[i], T[i], sigma[i], r[i], q[i], is_put[i]);
+    auto spec = kind[i] == 3
+                    ? GridSpec<double>::uniform(x_min[i], x_max[i], static_cast<size_t>(nx[i]))
+                    : GridSpec<double>::sinh_spaced(x_min[i], x_max[i],
+                                                    static_cast<size_t>(nx[i]), alpha[i]);
+    if (!spec) { status[i] = 1; continue; }
+    std::optional<PDEGridSpec> grid = PDEGridSpec{PDEGridConfig{*spec, static_cast<size_t>(nt[i]), {}}};
+    auto solver = AmericanOptionSolver::create(p, grid);
+    if (!solver) { status[i] = 1; continue; }
+    TRBDF2Config cfg;
+    cfg.rannacher_startup = rannacher != 0;
+    solver->set_trbdf2_config(cfg);
+    auto res = solver->solve();
+    if (!res) { status[i] = 5; continue; }
+    status[i] = 0;
+    out4[4 * i + 0] = res->value();
+    out4[4 * i + 1] = res->delta();
+    out4[4 * i + 2] = res->gamma();
+    out4[4 * i + 3] = res->theta();
+  }
+  return 0;
+}
+
+// One option: return the spatial grid and the final / previous solution
+// vectors (normalised V/K), for element-wise comparisons.
+int32_t ref_price_solution(double S, double K, double T, double sigma, double r,
+                           double q, int32_t is_put, int64_t nx, int64_t nt,
+                           int64_t cap, double* x_out, double* u_out,
+                           double* uprev_out, int64_t* n_out) {
+  auto p = make_params(S, K, T, sigma, r, q, is_put);
+  auto grid = grid_for(p, nx, nt, 0.0);
+  auto solver = AmericanOptionSolver::create(p, grid);
+  if (!solver) return 1;
+  auto res = solver->solve();
+  if (!res) return 5;
+  auto g = res->grid();
+  const int64_t m = static_cast<int64_t>(g->n_space());
+  *n_out = m;
+  if (m > cap) return 2;
+  auto x = g->x();
+  auto u = g->solution();
+  auto up = g->solution_prev();
+  for (int64_t i = 0; i < m; ++i) { x_out[i] = x[i]; u_out[i] = u[i]; uprev_out[i] = up[i]; }
+  return 0;
+}
+
+// Grid only (estimate_pde_grid + GridSpec::generate), for the host grid code.
+int32_t ref_make_grid(double S, double K, double T, double sigma, int64_t nx,
+                      int64_t cap, double* x_out, int64_t* n_out, int64_t* nt_out) {
+  auto p = make_params(S, K, T, sigma, 0.05, 0.0, 1);
+  std::pair<GridSpec<double>, TimeDomain> g = [&] {
+    if (nx <= 0) return estimate_pde_grid(p);
+    GridAccuracyParams acc;
+    acc.min_spatial_points = static_cast<size_t>(nx);
+    acc.max_spatial_points = static_cast<size_t>(nx);
+    return estimate_pde_grid(p, acc);
+  }();
+  auto buf = g.first.generate();
+  *n_out = static_cast<int64_t>(buf.size());
+  *nt_out = static_cast<int64_t>(g.second.n_steps());
+  if (*n_out > cap) return 2;
+  for (size_t i = 0; i < buf.size(); ++i) x_out[i] = buf[i];
+  return 0;
+}
+
+// FDM implied volatility through IVSolver::solve (Brent,
+// src/option/iv_solver.cpp:133-242).  Each quote gets its own PDEGridConfig
+// built by the grid rule at grid_sigma[i] (the vol its price was made with),
+// so the objective is smooth in sigma.  out3 = [iv, iterations, final_error].
+int32_t ref_iv_batch(int64_t n, const double* S, const double* K, const double* T,
+                     const double* r, const double* q, const int32_t* is_put,
+                     const double* price, const double* grid_sigma,
+                     const int64_t* nx, const int64_t* nt, int32_t n_threads,
+                     double* out3, int32_t* status) {
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t i = 0; i < n; ++i) {
+    IVQuery query;
+    query.spot = S[i];
+    query.strike = K[i];
+    query.maturity = T[i];
+    query.rate = r[i];
+    query.dividend_yield = q[i];
+    query.option_type = is_put[i] ? OptionType::PUT : OptionType::CALL;
+    query.market_price = price[i];
+    IVSolverConfig cfg;
+    if (nx && nx[i] > 0) {
+      auto p = make_params(S[i], K[i], T[i], grid_sigma[i], r[i], q[i], is_put[i]);
+      cfg.grid = *grid_for(p, nx[i], nt[i], 0.0);
+    }
+    IVSolver solver(cfg);
+    auto res = solver.solve(query);
+    if (!res) {
+      status[i] = 10 + static_cast<int32_t>(res.error().code);
+      out3[3 * i + 0] = NAN;
+      out3[3 * i + 1] = static_cast<double>(res.error().iterations);
+      out3[3 * i + 2] = res.error().final_error;
+      continue;
+    }
+    status[i] = 0;
+    out3[3 * i + 0] = res->implied_vol;
+    out3[3 * i + 1] = static_cast<double>(res->iterations);
+    out3[3 * i + 2] = res->final_error;
+  }
+  return 0;
+}
+
+}  // extern "C"

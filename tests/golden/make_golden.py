@@ -1,0 +1,224 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Runs the UNMODIFIED reference sources, compiled by oracle/ref/Makefile into
+oracle/_ref/libmango_ref.so (needs the reference tree, so this script runs on
+the development host only; the .npz outputs are committed and travel).
+
+    python tests/golden/make_golden.py
+
+Workloads (seeded numpy generators; the reference's CPU path is the source of
+every output value):
+  pricing_cfg0.npz   64 American puts, spot 100, K~U[80,120], T~U[0.1,2],
+                     sigma~U[0.1,0.5], r~U[0,0.08], q~U[0,0.04]; grid rule
+                     101 x 498 (estimate_pde_grid with min=max=101 points)
+  pricing_mixed.npz  64 options, same distributions, puts/calls alternating
+  pricing_auto.npz   32 options on the reference auto grid (GridAccuracyParams{})
+  pricing_uneven.npz 256 options, Nx~U{51..401}, Nt~U{100..1000}, puts/calls
+  pricing_edge.npz   hand-picked edge cases (deep ITM/OTM, r=0, q>r calls,
+                     tiny grids, 1-3 steps, Rannacher off, extreme vol/maturity)
+  pricing_explicit.npz explicit sinh / uniform PDEGridConfig grids
+  grids.npz          reference grids (bit-exact host grid generation)
+  solutions.npz      full final and previous solution vectors for 4 options
+  iv.npz             16 FDM implied vols (Brent) on per-quote 101 x 498 grids
+"""
+from __future__ import annotations
+
+import ctypes
+import pathlib
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+REF_SO = ROOT / "oracle" / "_ref" / "libmango_ref.so"
+
+
+def _lib():
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle" / "ref"), "-j8"], check=True)
+    return ctypes.CDLL(str(REF_SO))
+
+
+def P(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def price(lib, S, K, T, sig, r, q, put, nx, nt, rannacher=1):
+    n = len(S)
+    args = [np.ascontiguousarray(a, dtype=np.float64) for a in (S, K, T, sig, r, q)]
+    put = np.ascontiguousarray(put, dtype=np.int32)
+    nx = np.ascontiguousarray(nx, dtype=np.int64)
+    nt = np.ascontiguousarray(nt, dtype=np.int64)
+    out = np.full(4 * n, np.nan)
+    dims = np.zeros(2 * n, np.int64)
+    st = np.zeros(n, np.int32)
+    lib.ref_price_batch(ctypes.c_int64(n), *(P(a) for a in args), P(put), P(nx), P(nt),
+                        ctypes.c_int32(rannacher), ctypes.c_int32(8), P(out), P(dims), P(st))
+    return out.reshape(n, 4), dims.reshape(n, 2), st
+
+
+def config0_inputs(n, seed, mixed):
+    rng = np.random.default_rng(seed)
+    S = np.full(n, 100.0)
+    K = rng.uniform(80, 120, n)
+    T = rng.uniform(0.1, 2.0, n)
+    sig = rng.uniform(0.1, 0.5, n)
+    r = rng.uniform(0.0, 0.08, n)
+    q = rng.uniform(0.0, 0.04, n)
+    put = (np.arange(n) % 2 == 0).astype(np.int32) if mixed else np.ones(n, np.int32)
+    return S, K, T, sig, r, q, put
+
+
+def save(name, **kw):
+    np.savez_compressed(HERE / name, **kw)
+    print("wrote", name, {k: v.shape for k, v in kw.items()})
+
+
+def main():
+    lib = _lib()
+
+    for name, mixed in (("pricing_cfg0.npz", False), ("pricing_mixed.npz", True)):
+        S, K, T, sig, r, q, put = config0_inputs(64, 42, mixed)
+        nx = np.full(64, 101)
+        nt = np.full(64, 498)
+        out, dims, st = price(lib, S, K, T, sig, r, q, put, nx, nt)
+        save(name, S=S, K=K, T=T, sigma=sig, r=r, q=q, is_put=put, nx=nx, nt=nt, out=out,
+             dims=dims, status=st)
+
+    S, K, T, sig, r, q, put = config0_inputs(32, 11, True)
+    out, dims, st = price(lib, S, K, T, sig, r, q, put, np.zeros(32), np.zeros(32))
+    save("pricing_auto.npz", S=S, K=K, T=T, sigma=sig, r=r, q=q, is_put=put, out=out,
+         dims=dims, status=st)
+
+    rng = np.random.default_rng(1234)
+    n = 256
+    S, K, T, sig, r, q, put = config0_inputs(n, 99, True)
+    nx = rng.integers(51, 402, n)
+    nt = rng.integers(100, 1001, n)
+    out, dims, st = price(lib, S, K, T, sig, r, q, put, nx, nt)
+    save("pricing_uneven.npz", S=S, K=K, T=T, sigma=sig, r=r, q=q, is_put=put, nx=nx, nt=nt,
+         out=out, dims=dims, status=st)
+
+    # Edge cases: (S, K, T, sigma, r, q, put, nx, nt, rannacher)
+    edge = [
+        (25.0, 100.0, 1.0, 0.2, 0.05, 0.0, 1, 101, 498, 1),   # deep ITM put (locks)
+        (0.25, 100.0, 1.0, 0.2, 0.05, 0.0, 1, 101, 200, 1),   # extremely deep ITM put
+        (400.0, 100.0, 1.0, 0.2, 0.05, 0.0, 1, 101, 200, 1),  # deep OTM put
+        (100.0, 100.0, 1.0, 0.3, 0.0, 0.0, 1, 101, 300, 1),   # r = 0 put (never locks)
+        (100.0, 100.0, 1.0, 0.3, 0.02, 0.08, 0, 101, 300, 1),  # call, q > r: early exercise
+        (250.0, 100.0, 1.0, 0.3, 0.02, 0.08, 0, 101, 300, 1),  # deep ITM call, q > r
+        (100.0, 100.0, 1.0, 0.3, 0.05, 0.0, 0, 101, 300, 1),  # call, q = 0 (European)
+        (100.0, 100.0, 0.02, 0.3, 0.05, 0.02, 1, 101, 50, 1),  # very short maturity
+        (100.0, 100.0, 2.0, 0.8, 0.08, 0.04, 1, 101, 500, 1),  # high vol, long
+        (100.0, 100.0, 2.0, 0.05, 0.08, 0.0, 1, 101, 500, 1),  # low vol
+        (100.0, 95.0, 1.0, 0.25, 0.05, 0.01, 1, 5, 3, 1),     # tiny grid
+        (100.0, 95.0, 1.0, 0.25, 0.05, 0.01, 1, 7, 2, 1),
+        (100.0, 95.0, 1.0, 0.25, 0.05, 0.01, 0, 9, 1, 1),     # one step (Rannacher only)
+        (100.0, 95.0, 1.0, 0.25, 0.05, 0.01, 1, 9, 1, 0),     # one TR-BDF2 step
+        (100.0, 105.0, 1.0, 0.25, 0.05, 0.01, 1, 101, 100, 0),  # Rannacher off
+        (100.0, 105.0, 1.0, 0.25, 0.05, 0.01, 0, 101, 100, 0),
+        (100.0, 100.0, 1.0, 0.2, -0.01, 0.0, 1, 101, 200, 1),  # negative rate
+        (100.0, 80.0, 0.5, 0.4, 0.08, 0.04, 1, 401, 1000, 1),  # large grid
+    ]
+    cols = list(zip(*edge))
+    out = np.full((len(edge), 4), np.nan)
+    st = np.zeros(len(edge), np.int32)
+    dims = np.zeros((len(edge), 2), np.int64)
+    for rann in (0, 1):
+        sel = [i for i, e in enumerate(edge) if e[9] == rann]
+        o, d, s = price(lib, *(np.array(c)[sel] for c in cols[:9]), rannacher=rann)
+        out[sel], dims[sel], st[sel] = o, d, s
+    save("pricing_edge.npz", S=np.array(cols[0]), K=np.array(cols[1]), T=np.array(cols[2]),
+         sigma=np.array(cols[3]), r=np.array(cols[4]), q=np.array(cols[5]),
+         is_put=np.array(cols[6], np.int32), nx=np.array(cols[7]), nt=np.array(cols[8]),
+         rannacher=np.array(cols[9], np.int32), out=out, dims=dims, status=st)
+
+    # Explicit grids: sinh_spaced and uniform PDEGridConfig.
+    alpha = 2.0 * np.arcsinh(5.0 / np.sqrt(2.0))
+    ex = [
+        (100.0, 100.0, 2.0, 0.3, 0.05, 0.0, 1, 2, -3.0, 3.0, 201, alpha, 1000),
+        (100.0, 90.0, 1.0, 0.2, 0.03, 0.01, 1, 2, -1.5, 1.5, 101, 3.0, 300),
+        (100.0, 110.0, 1.0, 0.2, 0.03, 0.05, 0, 2, -1.5, 1.5, 101, 1.0, 300),
+        (100.0, 100.0, 1.0, 0.25, 0.04, 0.0, 1, 3, -2.0, 2.0, 161, 0.0, 400),
+        (100.0, 100.0, 1.0, 0.25, 0.04, 0.06, 0, 3, -2.0, 2.0, 161, 0.0, 400),
+    ]
+    c = [np.array(v) for v in zip(*ex)]
+    n = len(ex)
+    o = np.full(4 * n, np.nan)
+    s = np.zeros(n, np.int32)
+    f = [np.ascontiguousarray(a, dtype=np.float64) for a in c[:6]]
+    lib.ref_price_explicit(ctypes.c_int64(n), *(P(a) for a in f),
+                           P(np.ascontiguousarray(c[6], np.int32)),
+                           P(np.ascontiguousarray(c[7], np.int32)),
+                           P(np.ascontiguousarray(c[8], np.float64)),
+                           P(np.ascontiguousarray(c[9], np.float64)),
+                           P(np.ascontiguousarray(c[10], np.int64)),
+                           P(np.ascontiguousarray(c[11], np.float64)),
+                           P(np.ascontiguousarray(c[12], np.int64)), ctypes.c_int32(1), P(o), P(s))
+    save("pricing_explicit.npz", S=c[0], K=c[1], T=c[2], sigma=c[3], r=c[4], q=c[5],
+         is_put=c[6].astype(np.int32), kind=c[7].astype(np.int32), x_min=c[8], x_max=c[9],
+         nx=c[10], alpha=c[11], nt=c[12], out=o.reshape(n, 4), status=s)
+
+    # Grids (bitwise): mix of auto and pinned sizes.
+    gs = [(100, 100, 1, 0.2, 0), (100, 93, 1.3, 0.3, 101), (100, 120, 0.1, 0.1, 0),
+          (100, 80, 2.0, 0.5, 401), (100, 100, 0.5, 0.8, 51), (100, 300, 1.0, 0.2, 101)]
+    xs = np.full((len(gs), 2048), np.nan)
+    ns = np.zeros(len(gs), np.int64)
+    nts = np.zeros(len(gs), np.int64)
+    for i, (S_, K_, T_, s_, nx_) in enumerate(gs):
+        x = np.zeros(2048)
+        nn = np.zeros(1, np.int64)
+        ntt = np.zeros(1, np.int64)
+        lib.ref_make_grid(ctypes.c_double(S_), ctypes.c_double(K_), ctypes.c_double(T_),
+                          ctypes.c_double(s_), ctypes.c_int64(nx_), ctypes.c_int64(2048), P(x),
+                          P(nn), P(ntt))
+        xs[i] = x
+        ns[i], nts[i] = nn[0], ntt[0]
+    save("grids.npz", params=np.array(gs, np.float64), x=xs, n=ns, nt=nts)
+
+    # Solutions for element-wise checks.
+    sol = [(100, 93, 1.3, 0.3, 0.05, 0.02, 1, 101, 498), (100, 110, 1.0, 0.2, 0.03, 0.06, 0, 101, 300),
+           (25, 100, 1.0, 0.2, 0.05, 0.0, 1, 101, 498), (100, 100, 0.5, 0.4, 0.02, 0.01, 1, 201, 250)]
+    U = np.full((4, 512), np.nan)
+    UP = np.full((4, 512), np.nan)
+    X = np.full((4, 512), np.nan)
+    NS = np.zeros(4, np.int64)
+    for i, (S_, K_, T_, s_, r_, q_, p_, nx_, nt_) in enumerate(sol):
+        x = np.zeros(512)
+        u = np.zeros(512)
+        up = np.zeros(512)
+        nn = np.zeros(1, np.int64)
+        rc = lib.ref_price_solution(*(ctypes.c_double(v) for v in (S_, K_, T_, s_, r_, q_)),
+                                    ctypes.c_int32(p_), ctypes.c_int64(nx_), ctypes.c_int64(nt_),
+                                    ctypes.c_int64(512), P(x), P(u), P(up), P(nn))
+        assert rc == 0
+        X[i], U[i], UP[i], NS[i] = x, u, up, nn[0]
+    save("solutions.npz", params=np.array(sol, np.float64), x=X, u=U, u_prev=UP, n=NS)
+
+    # IV: prices from the reference at a true vol, recovered by reference Brent.
+    rng = np.random.default_rng(4242)
+    n = 16
+    S = np.full(n, 100.0)
+    K = S * rng.uniform(0.8, 1.2, n)
+    T = rng.uniform(0.02, 2.0, n)
+    r = rng.uniform(0.0, 0.08, n)
+    q = rng.uniform(0.0, 0.04, n)
+    vt = rng.uniform(0.05, 0.8, n)
+    put = (np.arange(n) % 4 != 3).astype(np.int32)
+    nx = np.full(n, 101)
+    nt = np.full(n, 498)
+    out, _, _ = price(lib, S, K, T, vt, r, q, put, nx, nt)
+    px = out[:, 0].copy()
+    o3 = np.full(3 * n, np.nan)
+    st = np.zeros(n, np.int32)
+    f = [np.ascontiguousarray(a, dtype=np.float64) for a in (S, K, T, r, q)]
+    lib.ref_iv_batch(ctypes.c_int64(n), *(P(a) for a in f), P(put), P(px), P(vt),
+                     P(np.ascontiguousarray(nx, np.int64)), P(np.ascontiguousarray(nt, np.int64)),
+                     ctypes.c_int32(8), P(o3), P(st))
+    save("iv.npz", S=S, K=K, T=T, r=r, q=q, is_put=put, price=px, true_vol=vt, nx=nx, nt=nt,
+         out=o3.reshape(n, 3), status=st)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -240,7 +240,11 @@ def main():
     import __graft_entry__ as ge
     pkg = ge.load_package()
     eng = pkg.Engine(local)
-    stream = torch.cuda.current_stream()
+    # A dedicated (non-default) stream: the engine enqueues on it and the
+    # CUDA events below are recorded on it, so they bracket exactly its work.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    assert stream.cuda_stream != 0
     eng.set_stream(stream.cuda_stream)
     fp64_peak = eng.fp64_probe()
 

@@ -588,7 +588,7 @@ MangoStatus mango_gpu_fp64_probe(MangoGpuContext* ctx, double* tflops, MangoErro
   try {
     check(cudaSetDevice(ctx->device), "cudaSetDevice");
     cudaStream_t st = ctx->stream;
-    const int blocks = ctx->num_sms * 4, threads = 256, iters = 4096;
+    const int blocks = ctx->num_sms * 8, threads = 256, iters = 2048;
     double* d = nullptr;
     check(cudaMallocAsync(reinterpret_cast<void**>(&d), sizeof(double) * blocks * threads, st),
           "cudaMallocAsync");
@@ -604,8 +604,8 @@ MangoStatus mango_gpu_fp64_probe(MangoGpuContext* ctx, double* tflops, MangoErro
       check(cudaEventSynchronize(e1), "event sync");
       float ms = 0;
       check(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
-      // 8 independent chains x iters FMAs per thread, 2 flops each
-      const double fl = 2.0 * 8.0 * iters * static_cast<double>(blocks) * threads;
+      // 16 independent chains x iters FMAs per thread, 2 flops each
+      const double fl = 2.0 * 16.0 * iters * static_cast<double>(blocks) * threads;
       best = std::max(best, fl / (ms * 1e-3) / 1e12);
     }
     check(cudaFreeAsync(d, st), "cudaFreeAsync");

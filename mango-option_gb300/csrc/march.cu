@@ -575,21 +575,21 @@ __global__ void outputs_kernel(const TileDev* __restrict__ tiles, int ntiles,
 }  // namespace mgpu
 
 namespace mgpu {
-// Diagnostic FP64 FMA throughput probe: 8 independent FMA chains per thread
+// Diagnostic FP64 FMA throughput probe: 16 independent FMA chains per thread
 // so issue, not latency, bounds it.  The result is stored so the work is kept.
 __global__ void fp64_probe_kernel(double* out, int iters) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  double a[8];
+  double a[16];
   const double m = 1.0 + 1e-9 * (tid & 7), c = 1e-12;
 #pragma unroll
-  for (int j = 0; j < 8; ++j) a[j] = 0.5 + 0.01 * j + 1e-7 * tid;
+  for (int j = 0; j < 16; ++j) a[j] = 0.5 + 0.01 * j + 1e-7 * tid;
   for (int it = 0; it < iters; ++it) {
 #pragma unroll
-    for (int j = 0; j < 8; ++j) a[j] = fma(a[j], m, c);
+    for (int j = 0; j < 16; ++j) a[j] = fma(a[j], m, c);
   }
   double s = 0.0;
 #pragma unroll
-  for (int j = 0; j < 8; ++j) s += a[j];
+  for (int j = 0; j < 16; ++j) s += a[j];
   out[tid] = s;
 }
 }  // namespace mgpu

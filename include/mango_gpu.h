@@ -204,6 +204,26 @@ MangoStatus mango_gpu_context_set_stream(MangoGpuContext* ctx, void* stream);
  * the reference ABI. */
 MangoStatus mango_gpu_fp64_probe(MangoGpuContext* ctx, double* tflops, MangoError* err);
 
+/* Batched pricing for callers that cannot allocate device memory (for
+ * example code running under an allocator that owns the whole GPU, or with a
+ * fixed memory budget).  Same inputs, outputs and per-slot semantics as
+ * mango_gpu_price_american_batch, but no context is needed and nothing is
+ * allocated: the work runs in one static device array of about 28 MB that
+ * every GPU loading this library holds until the process exits.  Limits: at
+ * most 4096 options per call and at most 131072 grid rows (sum over
+ * 32-option tiles of 32 x the tile's largest n_space); larger requests are
+ * rejected with MANGO_ERR_VALIDATION.  The first call on a device looks up
+ * the array's address (make it outside any stream capture).  Calls share
+ * the array: GPU work of overlapping calls races, so keep them on one stream
+ * or synchronise between them.  stream may be NULL (legacy default stream).
+ * No counterpart in the reference ABI. */
+MangoStatus mango_gpu_price_american_batch_noalloc(int32_t device, void* stream,
+                                                   const MangoPricingParams* params, uint64_t n,
+                                                   const MangoGpuGrid* grids, uint64_t grid_stride,
+                                                   const MangoGpuTrbdf2* trbdf2,
+                                                   MangoGpuAmericanOut* out, uint64_t* out_failed,
+                                                   MangoError* err);
+
 /* Host only (no device needed): the grid the engine would solve `params` on
  * for `grid`, i.e. resolve_grid + GridSpec::generate
  * (src/option/american_option.cpp:54-73, src/pde/core/grid.hpp:364-498).

@@ -202,4 +202,57 @@ void estimate_grid(double spot, double strike, double maturity, double sigma,
   *n_time = nt;
 }
 
+void estimate_grid(double spot, double strike, double maturity, double sigma,
+                   const Accuracy& acc, GridSpec* spec, int64_t* n_time, double* scratch,
+                   int64_t cap) {
+  // Identical to the vector overload above (estimate_pde_grid,
+  // src/option/grid_spec_types.cpp:37-118) except for where the trial grid lives.
+  const double sst = sigma * std::sqrt(maturity);
+  const double x0 = std::log(spot / strike);
+  const double lo = x0 - acc.n_sigma * sst;
+  const double hi = x0 + acc.n_sigma * sst;
+  const double dx_target = sigma * std::sqrt(acc.tol);
+  int64_t nx = static_cast<int64_t>(std::ceil((hi - lo) / dx_target));
+  if (nx < acc.min_points) nx = acc.min_points;
+  if (nx > acc.max_points) nx = acc.max_points;
+  if (nx % 2 == 0) ++nx;
+
+  GridSpec s;
+  s.n = nx;
+  s.x_min = lo;
+  s.x_max = hi;
+  s.n_clusters = 1;
+  s.c_center[0] = x0;
+  s.c_alpha[0] = acc.alpha;
+  s.c_weight[0] = 0.5;
+  if (0.0 >= lo && 0.0 <= hi) {
+    s.c_center[1] = 0.0;
+    s.c_alpha[1] = acc.alpha;
+    s.c_weight[1] = 1.0;
+    s.n_clusters = 2;
+  }
+  bool ok = nx >= 2 && lo < hi;
+  for (int k = 0; k < s.n_clusters && ok; ++k)
+    ok = s.c_alpha[k] > 0 && s.c_weight[k] > 0 && s.c_center[k] >= lo && s.c_center[k] <= hi;
+  if (ok) {
+    s.type = GridSpec::MultiSinh;
+    merge_clusters(&s);
+  } else {
+    s = sinh_spec(lo, hi, nx, acc.alpha);
+  }
+  *spec = s;
+  *n_time = 0;
+  if (nx > cap) return;
+  generate_grid(s, scratch);
+  double dx_min = scratch[1] - scratch[0];
+  for (int64_t i = 2; i < nx; ++i) {
+    const double d = scratch[i] - scratch[i - 1];
+    if (d < dx_min) dx_min = d;
+  }
+  const double dt = acc.c_t * dx_min;
+  int64_t nt = static_cast<int64_t>(std::ceil(maturity / dt));
+  if (nt > acc.max_steps) nt = acc.max_steps;
+  *n_time = nt;
+}
+
 }  // namespace mgpu

@@ -49,6 +49,12 @@ void estimate_grid(double spot, double strike, double maturity, double sigma,
                    const Accuracy& acc, GridSpec* spec, int64_t* n_time,
                    std::vector<double>* scratch);
 
+// Same, with caller-provided scratch of `cap` doubles (no heap use); a grid
+// larger than cap is not generated and *n_time is left at 0.
+void estimate_grid(double spot, double strike, double maturity, double sigma,
+                   const Accuracy& acc, GridSpec* spec, int64_t* n_time, double* scratch,
+                   int64_t cap);
+
 // GridSpec::sinh_spaced / uniform factories (no validation; callers check).
 GridSpec sinh_spec(double x_min, double x_max, int64_t n, double alpha);
 GridSpec uniform_spec(double x_min, double x_max, int64_t n);

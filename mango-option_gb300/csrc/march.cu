@@ -6,21 +6,24 @@
 // AmericanOptionResult functionals (src/option/american_option_result.cpp:
 // 25-121).
 //
-// GB300 design.  FP64 issue rate is the bound (the part has a small fraction
-// of its FP32 rate in FP64), so the march spends as few FP64 instructions per
-// grid row as the reference's arithmetic allows:
+// GB300 design.  FP64 issue rate is the bound (an SMSP issues one FP64 warp
+// instruction per ~64 cycles), so the march spends as few FP64 instructions
+// per grid row as the reference's arithmetic allows:
 //  * the operator and the stage matrices are time invariant for a constant
 //    rate, so prep_kernel builds them once per option, together with the
 //    Thomas factorisation of each stage matrix (c'_i and 1/pivot_i);
-//  * the steady-state row update is then divide-free:
-//      stage 1  d'_i = e_l u_{i-1} + e_d u_i + e_u u_{i+1} - l1h d'_{i-1}
-//      stage 2  d'_i = a2h g_i + b2h u_i - l2h d'_{i-1}
-//      back     x_i  = max(d'_i - c'_i x_{i+1}, psi_i)
+//  * the steady-state row update is then divide-free (negated factors are
+//    stored so every update is one FMA chain):
+//      stage 1  d'_i = e_l u_{i-1} + e_d u_i + e_u u_{i+1} + n1h d'_{i-1}
+//      stage 2  d'_i = a2h g_i + b2h u_i + n2h d'_{i-1}
+//      back     x_i  = max(nc_i x_{i+1} + d'_i, psi_i)
 //  * rows locked to the obstacle (pde_solver.hpp:635-680) change the matrix;
 //    after a locked row the factorisation is recomputed row by row, exactly
 //    as the reference does, until the recomputed c'_i is bit-identical to
 //    the cached one -- from there on both recurrences coincide, so the cached
-//    values are exact again (3-4 rows in practice).
+//    values are exact again (3-4 rows in practice);
+//  * every sweep keeps the next four rows of its inputs in a register queue,
+//    so the serial recurrence does not wait on memory latency row by row.
 #include "march.cuh"
 
 #include <cuda_runtime.h>
@@ -30,26 +33,35 @@ namespace mgpu {
 
 namespace {
 
+// Rows of one lane inside a tile block ([row][array][lane]).
 struct TileView {
-  double* B;
+  double* B;  // tile block + lane
   int NX;
-  int lane;
-  __device__ __forceinline__ double& at(int a, int i) const {
-    return B[(static_cast<size_t>(a) * NX + i) * kTile + lane];
+  __device__ __forceinline__ double* rp(int i) const {
+    return B + static_cast<size_t>(i) * kRowStride;
   }
-  __device__ __forceinline__ double* row(int a) const {
-    return B + static_cast<size_t>(a) * NX * kTile + lane;
-  }
+  __device__ __forceinline__ double& at(int a, int i) const { return rp(i)[a * kTile]; }
 };
 
+// [row][lane] arrays (grids, flags).
 #define ROW(p, i) (p)[static_cast<size_t>(i) * kTile]
 
 // std::max(a, b) as the reference spells it: (a < b) ? b : a.
 __device__ __forceinline__ double dmax_ref(double a, double b) { return (a < b) ? b : a; }
 
+// std::max(v, psi) for psi >= +0 (a payoff), with integer compares instead of
+// an FP64 instruction: non-negative doubles order like their bit patterns and
+// any negative v (sign bit set) loses.  Differs from the reference only for
+// v = -0, psi = +0 (returns +0 instead of -0, the same number).
+__device__ __forceinline__ double proj_max(double v, double psi) {
+  const long long vb = __double_as_longlong(v), pb = __double_as_longlong(psi);
+  return __longlong_as_double(vb > pb ? vb : pb);
+}
+
 __device__ __forceinline__ bool same_bits(double a, double b) {
   return __double_as_longlong(a) == __double_as_longlong(b);
 }
+
 
 }  // namespace
 
@@ -68,7 +80,7 @@ __global__ void prep_kernel(const TileDev* __restrict__ tiles, int ntiles,
   const int k = td.first + lane;
   const OptDev o = opts[k];
   const int n = o.n;
-  TileView V{pool + td.off, td.nx, lane};
+  const TileView V{pool + td.off + lane, td.nx};
   const double* X = xs + td.xoff + lane;
   auto x = [&](int i) { return X[static_cast<size_t>(i) * kTile]; };
   uint8_t* F = flags + td.foff + lane;
@@ -138,9 +150,10 @@ __global__ void prep_kernel(const TileDev* __restrict__ tiles, int ntiles,
     F[static_cast<size_t>(i) * kTile] = (psi_max > 0.0 && pi > thr && lpsi < 0.0) ? 1 : 0;
 
     const double el = w1 * A, ed = 1.0 + w1 * Bc, eu = w1 * C;
-    V.at(A_E1L0, i) = el;
-    V.at(A_E1D0, i) = ed;
-    V.at(A_E1U0, i) = eu;
+    double* r = V.rp(i);
+    r[A_E1L0 * kTile] = el;
+    r[A_E1D0 * kTile] = ed;
+    r[A_E1U0 * kTile] = eu;
 
     // assemble_jacobian (spatial_operator.hpp:123-163).
     const double b_coef = rate - o.q - hss;
@@ -158,15 +171,15 @@ __global__ void prep_kernel(const TileDev* __restrict__ tiles, int ntiles,
     const double ju = d2p + d1p;
     const double l1 = -w1 * jl, dg1 = 1.0 - w1 * jd, u1 = -w1 * ju;
     const double l2 = -w2 * jl, dg2 = 1.0 - w2 * jd, u2 = -w2 * ju;
-    V.at(A_L1, i) = l1;
-    V.at(A_D1, i) = dg1;
-    V.at(A_U1, i) = u1;
-    V.at(A_L2, i) = l2;
-    V.at(A_D2, i) = dg2;
-    V.at(A_U2, i) = u2;
-    V.at(A_LR, i) = -wr * jl;
-    V.at(A_DR, i) = 1.0 - wr * jd;
-    V.at(A_UR, i) = -wr * ju;
+    r[A_L1 * kTile] = l1;
+    r[A_D1 * kTile] = dg1;
+    r[A_U1 * kTile] = u1;
+    r[A_L2 * kTile] = l2;
+    r[A_D2 * kTile] = dg2;
+    r[A_U2 * kTile] = u2;
+    r[A_LR * kTile] = -wr * jl;
+    r[A_DR * kTile] = 1.0 - wr * jd;
+    r[A_UR * kTile] = -wr * ju;
 
     // Cached factorisations (the thomas_solver.hpp:382-395 recurrence).
     const double den1 = fma(-l1, cp1, dg1);
@@ -175,15 +188,15 @@ __global__ void prep_kernel(const TileDev* __restrict__ tiles, int ntiles,
     const double inv1 = 1.0 / den1, inv2 = 1.0 / den2;
     cp1 = u1 * inv1;
     cp2 = u2 * inv2;
-    V.at(A_C1, i) = cp1;
-    V.at(A_C2, i) = cp2;
-    V.at(A_E1L, i) = el * inv1;
-    V.at(A_E1D, i) = ed * inv1;
-    V.at(A_E1U, i) = eu * inv1;
-    V.at(A_L1H, i) = l1 * inv1;
-    V.at(A_A2H, i) = mc.alpha * inv2;
-    V.at(A_B2H, i) = mc.beta * inv2;
-    V.at(A_L2H, i) = l2 * inv2;
+    r[A_NC1 * kTile] = -cp1;
+    r[A_NC2 * kTile] = -cp2;
+    r[A_E1L * kTile] = el * inv1;
+    r[A_E1D * kTile] = ed * inv1;
+    r[A_E1U * kTile] = eu * inv1;
+    r[A_N1H * kTile] = -(l1 * inv1);
+    r[A_A2H * kTile] = mc.alpha * inv2;
+    r[A_B2H * kTile] = mc.beta * inv2;
+    r[A_N2H * kTile] = -(l2 * inv2);
   }
   mode[k] = md;
 
@@ -201,121 +214,198 @@ namespace {
 
 enum StageKind { kRannacher = 0, kStage1 = 1, kStage2 = 2 };
 
-// One implicit stage for one lane (solve_implicit_stage_projected).
-//   kRannacher: rhs = in (u_prev), guess = in, bands LR/DR/UR, never cached.
-//   kStage1:    rhs = u + w1 L(u) of in (= u^n), guess = in.
-//   kStage2:    rhs = alpha in + beta in2 (in = u^{n+gamma}, in2 = u^n), guess = in.
-// Lanes that are not live execute no memory operation.
+// Inputs of one forward-sweep row, prefetched into registers.
+struct FwdRow {
+  double a, b, c, nl, v;
+  unsigned f;
+};
+
 template <int K>
-__device__ __forceinline__ void stage(bool live, int n, const TileView& V,
-                                      const uint8_t* __restrict__ F, bool nocache,
-                                      double bcl, double bcr, double alpha, double beta,
-                                      int a_in, int a_in2, int a_out, int32_t& st) {
-  const int NX = V.NX;
-  const double* IN = V.row(a_in);
-  const double* IN2 = V.row(a_in2);
-  const double* PSI = V.row(A_PSI);
-  double* OUT = V.row(a_out);
-  double* Dd = V.row(A_D);
-  double* CP = V.row(A_CP);
-  constexpr int aC = (K == kStage2) ? A_C2 : A_C1;
+__device__ __forceinline__ void load_fwd(const TileView& V, const uint8_t* __restrict__ F,
+                                         int a_in, int i, FwdRow& r) {
+  const double* p = V.rp(i);
+  if (K == kStage1) {
+    r.a = p[A_E1L * kTile];
+    r.b = p[A_E1D * kTile];
+    r.c = p[A_E1U * kTile];
+    r.nl = p[A_N1H * kTile];
+    r.v = V.rp(i + 1)[A_U * kTile];
+  } else if (K == kStage2) {
+    r.a = p[A_A2H * kTile];
+    r.b = p[A_B2H * kTile];
+    r.nl = p[A_N2H * kTile];
+    r.c = p[A_G * kTile];  // guess u^{n+gamma}
+    r.v = p[A_U * kTile];  // u^n
+  } else {
+    r.c = p[a_in * kTile];  // rhs = guess = u_prev
+  }
+  r.f = ROW(F, i);
+}
+
+struct BwdRow {
+  double nc, psi, d;
+};
+
+template <int K>
+__device__ __forceinline__ void load_bwd(const TileView& V, int i, BwdRow& r) {
+  const double* p = V.rp(i);
+  r.nc = p[(K == kStage2 ? A_NC2 : A_NC1) * kTile];
+  r.psi = p[A_PSI * kTile];
+  r.d = p[A_D * kTile];
+}
+
+// A forward-sweep row off the cached factorisation: a locked row (identity
+// with rhs psi) or a row whose factor is recomputed exactly as the reference
+// does (thomas_solver.hpp:382-395).  Records the row's own c' in A_CP and
+// keeps [lo, hi] contiguous.  Kept out of line: it runs for a few rows per
+// stage, and inlining it into the prefetching loop costs registers.
+struct SlowOut {
+  double d;      // d'_i
+  double c;      // c'_i of this row (0 for a locked row)
+  int lo, hi;    // rows held in A_CP
+  bool fresh;    // next row is still off the cache
+  bool singular; // |pivot| < 1e-15 (thomas_solver.hpp:386-388)
+};
+
+// A forward-sweep row off the cached factorisation: a locked row (identity
+// with rhs psi) or a row whose factor is recomputed exactly as the reference
+// does (thomas_solver.hpp:382-395).  Records the row's own c' in A_CP and
+// keeps [lo, hi] contiguous.  Kept out of line: it runs for a few rows per
+// stage, and inlining it into the prefetching loop costs registers.  All
+// state travels by value so the caller keeps it in registers.
+template <int K>
+__device__ __forceinline__ SlowOut slow_row(const TileView V, int i, bool lock, double psi_i,
+                                         double um, double u0, double v, double g,
+                                         double alpha, double beta, double dprev,
+                                         double cprev, bool always_fresh, int lo, int hi) {
   constexpr int aL = (K == kRannacher) ? A_LR : (K == kStage1 ? A_L1 : A_L2);
   constexpr int aDg = (K == kRannacher) ? A_DR : (K == kStage1 ? A_D1 : A_D2);
   constexpr int aU = (K == kRannacher) ? A_UR : (K == kStage1 ? A_U1 : A_U2);
-  const double* Cc = V.row(aC);
-  const double* Lb = V.row(aL);
-  const double* Db = V.row(aDg);
-  const double* Ub = V.row(aU);
+  constexpr int aNC = (K == kStage2) ? A_NC2 : A_NC1;
+  double* p = V.rp(i);
+  SlowOut o;
+  o.singular = false;
+  if (lock) {
+    o.d = psi_i;  // identity row with rhs psi: c' = 0, d' = psi
+    o.c = 0.0;
+    o.fresh = true;
+  } else {
+    double rhs;
+    if (K == kStage1)
+      rhs = fma(p[A_E1L0 * kTile], um, fma(p[A_E1D0 * kTile], u0, p[A_E1U0 * kTile] * v));
+    else if (K == kStage2)
+      rhs = fma(alpha, g, beta * v);
+    else
+      rhs = g;
+    const double l = p[aL * kTile];
+    const double denom = fma(-l, cprev, p[aDg * kTile]);
+    o.singular = fabs(denom) < 1e-15;
+    const double inv = 1.0 / denom;
+    o.c = p[aU * kTile] * inv;
+    o.d = fma(-l, dprev, rhs) * inv;
+    o.fresh = always_fresh || !same_bits(-o.c, p[aNC * kTile]);
+  }
+  // Rows between the previous off-cache row and this one keep their cached
+  // value in A_CP so that [lo, hi] is valid for the back substitution.
+  if (hi >= 0 && i > hi + 1)
+    for (int q = hi + 1; q < i; ++q) V.at(A_CP, q) = -V.at(aNC, q);
+  p[A_CP * kTile] = o.c;
+  o.lo = lo == INT_MAX ? i : lo;
+  o.hi = i;
+  return o;
+}
+
+// One implicit stage for one lane (solve_implicit_stage_projected).
+//   kRannacher: rhs = guess = u_prev (array a_in), bands LR/DR/UR, never cached.
+//   kStage1:    rhs = u + w1 L(u) of u^n (A_U), guess = u^n, writes A_G.
+//   kStage2:    rhs = alpha g + beta u^n (g = A_G), guess = g, writes a_out.
+// Lanes that are not live execute no memory operation.
+template <int K>
+__device__ __noinline__ void stage(bool live, int n, const TileView& V,
+                                   const uint8_t* __restrict__ F, bool nocache, double bcl,
+                                   double bcr, double alpha, double beta, int a_in, int a_out,
+                                   int32_t& st) {
+  const int last = V.NX - 2;  // last interior row of the tile
   const bool always_fresh = (K == kRannacher) || nocache;
 
   // ---- forward elimination
   double dprev = bcl;  // d'_0 = rhs_0 / 1 on the Dirichlet row
   double cprev = 0.0;  // recomputed c'_{i-1}; valid whenever `fresh`
   bool fresh = always_fresh;
-  int lo = INT_MAX, hi = -1;  // rows [lo, hi] take c' from CP
-  double um = 0.0, u0 = 0.0, up = 0.0;
+  int lo = INT_MAX, hi = -1;  // rows [lo, hi] take c' from A_CP
+  double um = 0.0, u0 = 0.0;
   if (K == kStage1 && live) {
-    um = ROW(IN, 0);
-    u0 = ROW(IN, 1);
+    um = V.at(A_U, 0);
+    u0 = V.at(A_U, 1);
   }
-  for (int i = 1; i < NX - 1; ++i) {
-    if (!live || i >= n - 1) continue;
-    double g;
-    if (K == kStage1) {
-      up = ROW(IN, i + 1);
-      g = u0;
-    } else {
-      g = ROW(IN, i);
-    }
+  // Rows i..i+3 ride in a register queue: the loads of row i+4 are issued
+  // before row i is computed, so the d' recurrence does not wait on memory.
+  const int stop = live ? min(last, n - 2) : 0;
+  FwdRow q0{}, q1{}, q2{}, q3{};
+  if (1 <= stop) load_fwd<K>(V, F, a_in, 1, q0);
+  if (2 <= stop) load_fwd<K>(V, F, a_in, 2, q1);
+  if (3 <= stop) load_fwd<K>(V, F, a_in, 3, q2);
+  if (4 <= stop) load_fwd<K>(V, F, a_in, 4, q3);
+  for (int i = 1; i <= stop; ++i) {
+    const FwdRow r = q0;
+    q0 = q1;
+    q1 = q2;
+    q2 = q3;
+    if (i + 4 <= stop) load_fwd<K>(V, F, a_in, i + 4, q3);
+    const double g = (K == kStage1) ? u0 : r.c;
     bool lock = false;
     double psi_i = 0.0;
-    if (ROW(F, i)) {
-      psi_i = ROW(PSI, i);
+    if (r.f) {
+      psi_i = V.at(A_PSI, i);
       lock = (g - psi_i < 1e-8);
     }
     double dcur;
-    bool own;  // this row's c' is not the cached one
-    if (lock) {
-      dcur = psi_i;  // identity row with rhs psi: c' = 0, d' = psi
-      cprev = 0.0;
-      fresh = true;
-      own = true;
-    } else if (!fresh) {
-      if (K == kStage1) {
-        const double part =
-            fma(V.at(A_E1L, i), um, fma(V.at(A_E1D, i), u0, V.at(A_E1U, i) * up));
-        dcur = fma(-V.at(A_L1H, i), dprev, part);
-      } else {
-        const double part = fma(V.at(A_A2H, i), g, V.at(A_B2H, i) * ROW(IN2, i));
-        dcur = fma(-V.at(A_L2H, i), dprev, part);
-      }
-      own = false;
-    } else {
-      double rhs;
+    if (!lock && !fresh) {
       if (K == kStage1)
-        rhs = fma(V.at(A_E1L0, i), um, fma(V.at(A_E1D0, i), u0, V.at(A_E1U0, i) * up));
-      else if (K == kStage2)
-        rhs = fma(alpha, g, beta * ROW(IN2, i));
+        dcur = fma(r.nl, dprev, fma(r.a, um, fma(r.b, u0, r.c * r.v)));
       else
-        rhs = g;
-      const double l = ROW(Lb, i);
-      const double denom = fma(-l, cprev, ROW(Db, i));
-      if (fabs(denom) < 1e-15) st = kStatusSolver;  // thomas_solver.hpp:386-388
-      const double inv = 1.0 / denom;
-      const double ccur = ROW(Ub, i) * inv;
-      dcur = fma(-l, dprev, rhs) * inv;
-      cprev = ccur;
-      if (!always_fresh) fresh = !same_bits(ccur, ROW(Cc, i));
-      own = true;
+        dcur = fma(r.nl, dprev, fma(r.a, g, r.b * r.v));
+    } else {
+      const SlowOut so = slow_row<K>(V, i, lock, psi_i, um, u0, r.v, g, alpha, beta, dprev, cprev,
+                                     always_fresh, lo, hi);
+      dcur = so.d;
+      cprev = so.c;
+      fresh = so.fresh;
+      lo = so.lo;
+      hi = so.hi;
+      if (so.singular) st = kStatusSolver;
     }
-    if (own) {
-      if (hi >= 0 && i > hi + 1)
-        for (int j = hi + 1; j < i; ++j) ROW(CP, j) = ROW(Cc, j);
-      ROW(CP, i) = cprev;
-      if (lo == INT_MAX) lo = i;
-      hi = i;
-    }
-    ROW(Dd, i) = dcur;
+    V.at(A_D, i) = dcur;
     dprev = dcur;
     if (K == kStage1) {
       um = u0;
-      u0 = up;
+      u0 = r.v;
     }
   }
 
   // ---- projected back substitution; last row d' = rhs = bcr
   if (!live) return;
-  double xnext = dmax_ref(bcr, ROW(PSI, n - 1));
-  for (int i = NX - 2; i >= 1; --i) {
-    if (i > n - 2) continue;
-    const double c = (i >= lo && i <= hi) ? ROW(CP, i) : ROW(Cc, i);
-    const double xv = dmax_ref(fma(-c, xnext, ROW(Dd, i)), ROW(PSI, i));
-    ROW(OUT, i) = xv;
+  double xnext = dmax_ref(bcr, V.at(A_PSI, n - 1));
+  const int top = n - 2;  // this lane's first row going down
+  BwdRow q0b{}, q1b{}, q2b{}, q3b{};
+  if (top >= 1) load_bwd<K>(V, top, q0b);
+  if (top - 1 >= 1) load_bwd<K>(V, top - 1, q1b);
+  if (top - 2 >= 1) load_bwd<K>(V, top - 2, q2b);
+  if (top - 3 >= 1) load_bwd<K>(V, top - 3, q3b);
+  for (int i = top; i >= 1; --i) {
+    const BwdRow r = q0b;
+    q0b = q1b;
+    q1b = q2b;
+    q2b = q3b;
+    if (i - 4 >= 1) load_bwd<K>(V, i - 4, q3b);
+    const double nc = (i >= lo && i <= hi) ? -V.at(A_CP, i) : r.nc;
+    const double xv = proj_max(fma(nc, xnext, r.d), r.psi);
+    V.at(a_out, i) = xv;
     xnext = xv;
   }
   // apply_boundary_conditions after the solve (pde_solver.hpp:724-726).
-  ROW(OUT, 0) = bcl;
-  ROW(OUT, n - 1) = bcr;
+  V.at(a_out, 0) = bcl;
+  V.at(a_out, n - 1) = bcr;
 }
 
 __device__ __forceinline__ double right_bc(const OptDev& o, double t) {
@@ -325,7 +415,7 @@ __device__ __forceinline__ double right_bc(const OptDev& o, double t) {
 }  // namespace
 
 // Persistent march: each warp pulls tiles (largest first) from the queue.
-__global__ void __launch_bounds__(128) march_kernel(
+__global__ void __launch_bounds__(128, 4) march_kernel(
     const TileDev* __restrict__ tiles, int ntiles, const OptDev* __restrict__ opts,
     double* __restrict__ pool, const uint8_t* __restrict__ flags,
     const int32_t* __restrict__ mode, int32_t* __restrict__ status, int* __restrict__ queue,
@@ -348,7 +438,7 @@ __global__ void __launch_bounds__(128) march_kernel(
     const bool nocache = (md & 1) != 0;
     const int n = active ? o.n : 0;
     const int nt = active ? o.nt : 0;
-    const TileView V{pool + td.off, td.nx, lane};
+    const TileView V{pool + td.off + lane, td.nx};
     const uint8_t* F = flags + td.foff + lane;
     int32_t st = kStatusOk;
     const double dt = o.dt;
@@ -358,10 +448,10 @@ __global__ void __launch_bounds__(128) march_kernel(
       // half steps with coefficient dt/2 to t + dt/2 and t + dt.
       const double t_mid = 0.0 + 0.5 * dt;
       const double t_next = 0.0 + dt;
-      stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_mid), mc.alpha,
-                        mc.beta, A_U, A_U, A_G, st);
-      stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_next), mc.alpha,
-                        mc.beta, A_G, A_G, A_U, st);
+      stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_mid),
+                        mc.alpha, mc.beta, A_U, A_G, st);
+      stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_next),
+                        mc.alpha, mc.beta, A_G, A_U, st);
       step = 1;
     }
     for (; step < td.nt; ++step) {
@@ -371,10 +461,10 @@ __global__ void __launch_bounds__(128) march_kernel(
       const double t1 = t + mc.gamma * dt;
       const double tn = static_cast<double>(step + 1) * dt;
       const bool last = (step == nt - 1);
-      stage<kStage1>(live, n, V, F, nocache, o.bc_left, right_bc(o, t1), mc.alpha, mc.beta,
-                     A_U, A_U, A_G, st);
-      stage<kStage2>(live, n, V, F, nocache, o.bc_left, right_bc(o, tn), mc.alpha, mc.beta,
-                     A_G, A_U, last ? A_G : A_U, st);
+      stage<kStage1>(live, n, V, F, nocache, o.bc_left, right_bc(o, t1), mc.alpha,
+                     mc.beta, A_U, A_G, st);
+      stage<kStage2>(live, n, V, F, nocache, o.bc_left, right_bc(o, tn), mc.alpha,
+                     mc.beta, A_G, last ? A_G : A_U, st);
     }
     if (active) status[k] = st;
   }
@@ -386,13 +476,12 @@ namespace {
 
 // Natural cubic spline through (x, y) (cubic_spline_solver.hpp:74-170,
 // 264-369): solve for the second-derivative terms c_i with the plain Thomas
-// recurrence (thomas_solver.hpp:86-198), then evaluate at xe.  cw/dw are
-// per-lane scratch rows of length >= n.
-__device__ void spline_at(const double* __restrict__ X, const double* __restrict__ Y, int n,
-                          double xe, double* cw, double* dw, int iv, double* val,
-                          double* der) {
+// recurrence (thomas_solver.hpp:86-198), then evaluate at xe on interval iv.
+// The lane's A_CP / A_D rows serve as the c' / d' scratch.
+__device__ void spline_at(const double* __restrict__ X, const TileView& V, int ay, int n,
+                          double xe, int iv, double* val, double* der) {
   auto x = [&](int i) { return ROW(X, i); };
-  auto y = [&](int i) { return ROW(Y, i); };
+  auto y = [&](int i) { return V.at(ay, i); };
   auto h = [&](int i) { return x(i + 1) - x(i); };
   double ci = 0.0, ci1 = 0.0;  // c[iv], c[iv+1]
   const int m = n - 2;
@@ -406,40 +495,44 @@ __device__ void spline_at(const double* __restrict__ X, const double* __restrict
     };
     if (m == 1) {
       const double s = rhs(0) / (2.0 * (h(0) + h(1)));
-      if (iv == 0) { ci = 0.0; ci1 = s; } else { ci = s; ci1 = 0.0; }
+      if (iv == 0) {
+        ci = 0.0;
+        ci1 = s;
+      } else {
+        ci = s;
+        ci1 = 0.0;
+      }
     } else {
-      // forward
-      double diag0 = 2.0 * (h(0) + h(1));
+      const double diag0 = 2.0 * (h(0) + h(1));
       double cp = h(1) / diag0;
       double dp = rhs(0) / diag0;
-      ROW(cw, 0) = cp;
-      ROW(dw, 0) = dp;
+      V.at(A_CP, 0) = cp;
+      V.at(A_D, 0) = dp;
       for (int j = 1; j < m - 1; ++j) {
         const double lower = h(j);
         const double denom = fma(-lower, cp, 2.0 * (h(j) + h(j + 1)));
         const double inv = 1.0 / denom;
         cp = h(j + 1) * inv;
         dp = fma(-lower, dp, rhs(j)) * inv;
-        ROW(cw, j) = cp;
-        ROW(dw, j) = dp;
+        V.at(A_CP, j) = cp;
+        V.at(A_D, j) = dp;
       }
       {
         const int j = m - 1;
         const double lower = h(j);
         const double denom = fma(-lower, cp, 2.0 * (h(j) + h(j + 1)));
         dp = fma(-lower, dp, rhs(j)) / denom;
-        ROW(dw, j) = dp;
+        V.at(A_D, j) = dp;
       }
-      // backward: sol[j] = c[j+1]; need c[iv] and c[iv+1].
-      double s = ROW(dw, m - 1);
-      // c index k = j+1; walk j from m-1 down to max(iv-1, 0)
+      // back substitution: sol[j] = c[j+1]; only c[iv], c[iv+1] are needed.
+      double s = V.at(A_D, m - 1);
       auto take = [&](int kk, double v) {
         if (kk == iv) ci = v;
         if (kk == iv + 1) ci1 = v;
       };
       take(m, s);
       for (int j = m - 1; j > 0; --j) {
-        s = fma(-ROW(cw, j - 1), s, ROW(dw, j - 1));
+        s = fma(-V.at(A_CP, j - 1), s, V.at(A_D, j - 1));
         take(j, s);
         if (j <= iv) break;
       }
@@ -457,12 +550,12 @@ __device__ void spline_at(const double* __restrict__ X, const double* __restrict
 // CenteredDifference first/second derivative at row i, zero outside the
 // rows [1, n-2) that AmericanOptionResult::gamma fills
 // (american_option_result.cpp:66-71).
-__device__ void stencil_at(const double* __restrict__ X, const double* __restrict__ U, int n,
+__device__ void stencil_at(const double* __restrict__ X, const TileView& V, int au, int n,
                            int i, bool uniform, double* d1, double* d2) {
   *d1 = 0.0;
   *d2 = 0.0;
   if (i < 1 || i >= n - 2) return;
-  const double ul = ROW(U, i - 1), uc = ROW(U, i), ur = ROW(U, i + 1);
+  const double ul = V.at(au, i - 1), uc = V.at(au, i), ur = V.at(au, i + 1);
   if (uniform) {
     const double expected = (ROW(X, n - 1) - ROW(X, 0)) / static_cast<double>(n - 1);
     const double dxi = 1.0 / expected;
@@ -496,7 +589,7 @@ __device__ int find_interval(const double* __restrict__ X, int n, double xe) {
 }  // namespace
 
 // value, delta, gamma, theta per option (american_option_result.cpp:25-121).
-// out4 is in sorted order; u_final is G unless (Rannacher && nt == 1).
+// out4 is in sorted order; u_final is A_G unless (Rannacher && nt == 1).
 __global__ void outputs_kernel(const TileDev* __restrict__ tiles, int ntiles,
                                const OptDev* __restrict__ opts, const double* __restrict__ xs,
                                double* __restrict__ pool, const int32_t* __restrict__ mode,
@@ -515,27 +608,27 @@ __global__ void outputs_kernel(const TileDev* __restrict__ tiles, int ntiles,
     return;
   }
   const int n = o.n;
-  const TileView V{pool + td.off, td.nx, lane};
+  const TileView V{pool + td.off + lane, td.nx};
   const double* X = xs + td.xoff + lane;
   const bool swap = mc.rannacher && o.nt == 1;
-  const double* U = V.row(swap ? A_U : A_G);
-  const double* UP = V.row(swap ? A_G : A_U);
-  double* cw = V.row(A_CP);
-  double* dw = V.row(A_D);
+  const int au = swap ? A_U : A_G;
+  const int aup = swap ? A_G : A_U;
   const double xs_ = o.x_spot;
   const int iv = find_interval(X, n, xs_);
   double sv, sd;
-  spline_at(X, U, n, xs_, cw, dw, iv, &sv, &sd);
+  spline_at(X, V, au, n, xs_, iv, &sv, &sd);
   double value;
-  if (xs_ <= ROW(X, 0)) value = ROW(U, 0) * o.strike;
-  else if (xs_ >= ROW(X, n - 1)) value = ROW(U, n - 1) * o.strike;
+  if (xs_ <= ROW(X, 0)) value = V.at(au, 0) * o.strike;
+  else if (xs_ >= ROW(X, n - 1)) value = V.at(au, n - 1) * o.strike;
   else value = dmax_ref(0.0, sv) * o.strike;
   const double delta = sd * (o.strike / o.spot);
   // gamma: stencil derivatives linearly interpolated at x_spot.
   int il, ir;
-  if (xs_ <= ROW(X, 0)) { il = ir = 0; }
-  else if (xs_ >= ROW(X, n - 1)) { il = ir = n - 1; }
-  else {
+  if (xs_ <= ROW(X, 0)) {
+    il = ir = 0;
+  } else if (xs_ >= ROW(X, n - 1)) {
+    il = ir = n - 1;
+  } else {
     int lo = 0, hi = n;
     while (lo < hi) {
       const int mid = lo + (hi - lo) / 2;
@@ -547,13 +640,13 @@ __global__ void outputs_kernel(const TileDev* __restrict__ tiles, int ntiles,
   }
   const bool uniform = (mode[k] & 2) != 0;
   double d1l, d2l, d1r, d2r;
-  stencil_at(X, U, n, il, uniform, &d1l, &d2l);
+  stencil_at(X, V, au, n, il, uniform, &d1l, &d2l);
   double d1, d2;
   if (il == ir) {
     d1 = d1l;
     d2 = d2l;
   } else {
-    stencil_at(X, U, n, ir, uniform, &d1r, &d2r);
+    stencil_at(X, V, au, n, ir, uniform, &d1r, &d2r);
     const double al = (xs_ - ROW(X, il)) / (ROW(X, ir) - ROW(X, il));
     d1 = d1l + al * (d1r - d1l);
     d2 = d2l + al * (d2r - d2l);
@@ -562,7 +655,7 @@ __global__ void outputs_kernel(const TileDev* __restrict__ tiles, int ntiles,
   const double gam = fma(kos2, d2, -kos2 * d1);
   // theta: (S_prev(x) - S(x)) / dt * K with an unclamped spline value.
   double pv, pd;
-  spline_at(X, UP, n, xs_, cw, dw, iv, &pv, &pd);
+  spline_at(X, V, aup, n, xs_, iv, &pv, &pd);
   const double theta = (pv - sv) / o.dt * o.strike;
   res[0] = value;
   res[1] = delta;
@@ -572,9 +665,6 @@ __global__ void outputs_kernel(const TileDev* __restrict__ tiles, int ntiles,
 
 #undef ROW
 
-}  // namespace mgpu
-
-namespace mgpu {
 // Diagnostic FP64 FMA throughput probe: 16 independent FMA chains per thread
 // so issue, not latency, bounds it.  The result is stored so the work is kept.
 __global__ void fp64_probe_kernel(double* out, int iters) {
@@ -592,4 +682,5 @@ __global__ void fp64_probe_kernel(double* out, int iters) {
   for (int j = 0; j < 16; ++j) s += a[j];
   out[tid] = s;
 }
+
 }  // namespace mgpu

@@ -3,9 +3,7 @@
 // Options are sorted by (n_space, n_time) descending and packed into tiles
 // of 32: one warp marches one tile, one lane per option (thread-per-option
 // Thomas sweeps; the tridiagonal recurrences are serial along the grid, so
-// the work-optimal parallel axis is across options).  Each tile owns a block
-// of A_COUNT double arrays laid out [array][row][lane] so that a warp touching
-// row i of one array reads 32 consecutive doubles (two 128-byte lines).
+// the work-optimal parallel axis is across options).
 #pragma once
 #include <cstdint>
 
@@ -13,31 +11,34 @@ namespace mgpu {
 
 constexpr int kTile = 32;
 
-// Per-row arrays of a tile block.  "Stage 1/2" are the TR-BDF2 stages; the
-// hot (every-step) arrays come first.
+// Per-row arrays of a tile block, laid out [row][array][lane]: one warp
+// touching array a of row i reads 32 consecutive doubles (two 128-byte
+// lines), and every array of a row is reached from one row pointer with an
+// immediate offset.  The arrays read in every time step come first.
 enum TileArray : int {
-  A_PSI = 0,  // obstacle psi = payoff (time invariant for these payoffs)
-  A_E1L,      // stage-1 right-hand side stencil pre-scaled by the cached
+  A_E1L = 0,  // stage-1 right-hand-side stencil pre-scaled by the cached
   A_E1D,      //   inverse pivot: d'_i = e_l u_{i-1} + e_d u_i + e_u u_{i+1}
-  A_E1U,      //   - l1h d'_{i-1}
-  A_L1H,      // stage-1 sub-diagonal times cached inverse pivot
-  A_C1,       // stage-1 cached Thomas factor c'_i (unlocked matrix)
-  A_A2H,      // stage-2: alpha * inv pivot
-  A_B2H,      // stage-2: beta * inv pivot
-  A_L2H,      // stage-2 sub-diagonal times inverse pivot
-  A_C2,       // stage-2 cached c'_i
-  A_E1L0,     // unscaled stage-1 stencil (rows that leave the cached path)
+  A_E1U,      //   + n1h d'_{i-1}
+  A_N1H,      // stage 1: -(sub-diagonal x cached inverse pivot)
+  A_NC1,      // stage 1: -c'_i of the unlocked matrix (cached factor)
+  A_PSI,      // obstacle psi = payoff (time invariant for these payoffs)
+  A_A2H,      // stage 2: alpha x inverse pivot
+  A_B2H,      // stage 2: beta x inverse pivot
+  A_N2H,      // stage 2: -(sub-diagonal x inverse pivot)
+  A_NC2,      // stage 2: -c'_i (cached)
+  A_U,        // state u^n
+  A_G,        // state u^{n+gamma} (and the final u)
+  A_D,        // Thomas d' scratch
+  A_CP,       // Thomas c' of rows solved off the cache
+  A_E1L0,     // unscaled stage-1 stencil (rows off the cache)
   A_E1D0,
   A_E1U0,
   A_L1, A_D1, A_U1,  // stage-1 matrix bands (assemble_jacobian form)
   A_L2, A_D2, A_U2,  // stage-2 matrix bands
   A_LR, A_DR, A_UR,  // Rannacher half-step bands
-  A_U,        // state u^n
-  A_G,        // state u^{n+gamma} (and final u)
-  A_D,        // Thomas d' scratch
-  A_CP,       // Thomas c' scratch for rows off the cached path
   A_COUNT
 };
+constexpr int kRowStride = A_COUNT * 32;  // doubles between consecutive rows
 
 // Per-option parameters, in sorted order.
 struct OptDev {

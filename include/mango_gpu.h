@@ -104,12 +104,18 @@ typedef struct {
  *   MANGO_GPU_GRID_SINH     PDEGridConfig{GridSpec::sinh_spaced(x_min, x_max,
  *                           n_space, alpha), n_time};
  *   MANGO_GPU_GRID_UNIFORM  PDEGridConfig{GridSpec::uniform(x_min, x_max,
- *                           n_space), n_time}.
+ *                           n_space), n_time};
+ *   MANGO_GPU_GRID_FIXED_N_AT_VOL  as FIXED_N, but the grid is sized with the
+ *                           volatility given in `alpha` instead of the
+ *                           option's own -- a fixed per-quote PDEGridConfig
+ *                           for implied-volatility solves, where the
+ *                           volatility is the unknown.
  * x_min/x_max are log-moneyness ln(S/K). */
 #define MANGO_GPU_GRID_AUTO 0
 #define MANGO_GPU_GRID_FIXED_N 1
 #define MANGO_GPU_GRID_SINH 2
 #define MANGO_GPU_GRID_UNIFORM 3
+#define MANGO_GPU_GRID_FIXED_N_AT_VOL 4
 typedef struct {
   int32_t kind;
   int32_t reserved;
@@ -170,6 +176,22 @@ MangoStatus mango_gpu_price_american_batch(MangoGpuContext* ctx,
                                            const MangoGpuTrbdf2* trbdf2,
                                            MangoGpuAmericanOut* out,
                                            uint64_t* out_failed, MangoError* err);
+
+/* Batched FDM implied volatility: IVSolver::solve (src/option/iv_solver.cpp:
+ * 133-242) with Brent (src/math/root_finding.hpp:145-302) for every quote,
+ * the batch analogue of mango_solve_iv (src/ffi/mango_c_api.h:154-157) and
+ * of IVSolver::solve_batch.  Each quote needs a grid that does not depend on
+ * the unknown volatility: MANGO_GPU_GRID_FIXED_N_AT_VOL, _SINH or _UNIFORM
+ * (the reference's IVSolverConfig.grid = PDEGridConfig); grid_stride as for
+ * pricing.  config NULL or zero fields => brent_tol_abs 1e-6, max_iter 100.
+ * Slot status: MANGO_OK, _VALIDATION, _ARBITRAGE (price outside
+ * [intrinsic, upper bound]), _BRACKETING, _NO_CONVERGENCE, _SOLVER.  Each
+ * Brent evaluation re-prices the active quotes on the device; the launch
+ * sequence of one evaluation is a CUDA graph replayed per iteration. */
+MangoStatus mango_gpu_solve_iv_batch(MangoGpuContext* ctx, const MangoIvQuery* queries,
+                                     uint64_t n, const MangoGpuGrid* grids, uint64_t grid_stride,
+                                     const MangoIvConfig* config, MangoIvBatchSlot* out,
+                                     uint64_t* out_failed, MangoError* err);
 
 /* Resident batch: the same pipeline as mango_gpu_price_american_batch split
  * so that inputs can stay in device memory across runs (repeat pricing of a

@@ -36,6 +36,7 @@ GRID_AUTO = 0
 GRID_FIXED_N = 1
 GRID_SINH = 2
 GRID_UNIFORM = 3
+GRID_FIXED_N_AT_VOL = 4
 
 # C layouts (include/mango_gpu.h); sizes are asserted there and in tests.
 PRICING_DTYPE = np.dtype([
@@ -51,6 +52,9 @@ IVQUERY_DTYPE = np.dtype([
 GRID_DTYPE = np.dtype([
     ("kind", "i4"), ("reserved", "i4"), ("n_space", "i8"), ("n_time", "i8"),
     ("x_min", "f8"), ("x_max", "f8"), ("alpha", "f8")])
+IVSLOT_DTYPE = np.dtype([
+    ("status", "i4"), ("_pad", "i4"), ("implied_vol", "f8"), ("iterations", "u8"),
+    ("final_error", "f8"), ("vega", "f8"), ("has_vega", "i4"), ("used_rate_approximation", "i4")])
 OUT_DTYPE = np.dtype([
     ("value", "f8"), ("delta", "f8"), ("gamma", "f8"), ("theta", "f8"),
     ("status", "i4"), ("n_space", "i4"), ("n_time", "i4"), ("reserved", "i4")])
@@ -58,6 +62,10 @@ OUT_DTYPE = np.dtype([
 
 class MangoError(ctypes.Structure):
     _fields_ = [("code", ctypes.c_int32), ("message", ctypes.c_char * 256)]
+
+
+class MangoIvConfig(ctypes.Structure):
+    _fields_ = [("brent_tol_abs", ctypes.c_double), ("max_iter", ctypes.c_int32)]
 
 
 class MangoGpuTrbdf2(ctypes.Structure):
@@ -119,6 +127,10 @@ def library() -> ctypes.CDLL:
         lib.mango_gpu_context_set_stream.restype = ctypes.c_int32
         lib.mango_gpu_fp64_probe.argtypes = [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(MangoError)]
         lib.mango_gpu_fp64_probe.restype = ctypes.c_int32
+        lib.mango_gpu_solve_iv_batch.argtypes = [_P, _P, ctypes.c_uint64, _P, ctypes.c_uint64,
+                                                 ctypes.POINTER(MangoIvConfig), _P,
+                                                 ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(MangoError)]
+        lib.mango_gpu_solve_iv_batch.restype = ctypes.c_int32
         lib.mango_gpu_build_info.argtypes = []
         lib.mango_gpu_build_info.restype = ctypes.c_char_p
         _lib = lib
@@ -177,6 +189,19 @@ def pricing_array(spot, strike, maturity, volatility, rate, dividend_yield, is_p
     a["spot"], a["strike"], a["maturity"] = cols[0].ravel(), cols[1].ravel(), cols[2].ravel()
     a["volatility"], a["rate_const"], a["dividend_yield"] = cols[3].ravel(), cols[4].ravel(), cols[5].ravel()
     a["option_type"] = np.where(cols[6].ravel() != 0, 1, 0).astype(np.int32)
+    return a
+
+
+def query_array(spot, strike, maturity, rate, dividend_yield, is_put, market_price) -> np.ndarray:
+    """Pack per-quote arrays (broadcast) into the C MangoIvQuery layout."""
+    cols = np.broadcast_arrays(*(np.asarray(v, dtype=np.float64) for v in
+                                 (spot, strike, maturity, rate, dividend_yield, is_put, market_price)))
+    n = cols[0].size
+    a = np.zeros(n, dtype=IVQUERY_DTYPE)
+    a["spot"], a["strike"], a["maturity"] = cols[0].ravel(), cols[1].ravel(), cols[2].ravel()
+    a["rate_const"], a["dividend_yield"] = cols[3].ravel(), cols[4].ravel()
+    a["option_type"] = np.where(cols[5].ravel() != 0, 1, 0).astype(np.int32)
+    a["market_price"] = cols[6].ravel()
     return a
 
 
@@ -255,6 +280,26 @@ class Engine:
             ctypes.byref(failed), ctypes.byref(err))
         if st != MANGO_OK:
             raise EngineError(f"mango_gpu_price_american_batch: {err.message.decode(errors='replace')}")
+        return out
+
+    def solve_iv_arrays(self, queries: np.ndarray, grids: np.ndarray, tol: float = 0.0,
+                        max_iter: int = 0) -> np.ndarray:
+        """Batched FDM implied volatility (mango_gpu_solve_iv_batch).  queries:
+        IVQUERY_DTYPE; grids: GRID_DTYPE (length 1 or len(queries)), each a
+        volatility-independent grid.  Returns IVSLOT_DTYPE records."""
+        queries = np.ascontiguousarray(queries, dtype=IVQUERY_DTYPE)
+        grids = np.ascontiguousarray(grids, dtype=GRID_DTYPE)
+        n = queries.size
+        stride = 1 if (grids.size == n and n != 1) else 0
+        out = np.zeros(n, dtype=IVSLOT_DTYPE)
+        cfg = MangoIvConfig(tol, max_iter)
+        failed = ctypes.c_uint64()
+        err = MangoError()
+        st = library().mango_gpu_solve_iv_batch(self._ctx, _ptr(queries), n, _ptr(grids), stride,
+                                                ctypes.byref(cfg), _ptr(out), ctypes.byref(failed),
+                                                ctypes.byref(err))
+        if st != MANGO_OK:
+            raise EngineError(f"mango_gpu_solve_iv_batch: {err.message.decode(errors='replace')}")
         return out
 
     def set_stream(self, stream_handle: Optional[int]) -> None:
@@ -440,3 +485,89 @@ class BatchAmericanOptionSolver:
             else:
                 results.append(SolverError(int(row["status"])))
         return BatchAmericanOptionResult(results, int(np.count_nonzero(out["status"])))
+
+
+@dataclasses.dataclass
+class IVQuery:
+    """Reference IVQuery (src/option/option_spec.hpp:208-228), constant rate."""
+    spot: float = 0.0
+    strike: float = 0.0
+    maturity: float = 0.0
+    rate: float = 0.0
+    dividend_yield: float = 0.0
+    option_type: OptionType = OptionType.CALL
+    market_price: float = 0.0
+
+
+@dataclasses.dataclass
+class IVSuccess:
+    implied_vol: float
+    iterations: int
+    final_error: float
+    vega: Optional[float] = None
+
+
+class IVError(RuntimeError):
+    def __init__(self, status: int, iterations: int = 0, final_error: float = float("nan")):
+        super().__init__(f"status {status}")
+        self.status = status
+        self.iterations = iterations
+        self.final_error = final_error
+
+
+@dataclasses.dataclass
+class BatchIVResult:
+    results: list
+    failed_count: int
+
+
+@dataclasses.dataclass
+class IVSolverConfig:
+    """Reference IVSolverConfig (src/option/iv_solver.hpp:48-68); `grid` must
+    not depend on the unknown volatility: a PDEGridConfig, or FixedGrid
+    sized at `grid_vol`."""
+    grid: object = None
+    grid_vol: float = 0.0
+    brent_tol_abs: float = 1e-6
+    max_iter: int = 100
+
+
+class IVSolver:
+    """Reference IVSolver (src/option/iv_solver.hpp:134): Brent FDM IV, all
+    quotes of solve_batch solved together on the GPU."""
+
+    def __init__(self, config: Optional[IVSolverConfig] = None, engine: Optional[Engine] = None):
+        self.config = config or IVSolverConfig(grid=PDEGridConfig())
+        self._engine = engine
+
+    def _grid(self):
+        g = self.config.grid
+        if isinstance(g, FixedGrid):
+            if not self.config.grid_vol > 0:
+                raise ValueError("FixedGrid for IV needs IVSolverConfig.grid_vol > 0")
+            return grid_array(1, GRID_FIXED_N_AT_VOL, g.n_space, g.n_time, alpha=self.config.grid_vol)
+        if isinstance(g, PDEGridConfig):
+            return _grid_entry(g)
+        raise ValueError("IVSolver on the GPU needs a fixed grid (PDEGridConfig or FixedGrid)")
+
+    def solve_batch(self, queries) -> BatchIVResult:
+        qs = list(queries)
+        arr = query_array([q.spot for q in qs], [q.strike for q in qs], [q.maturity for q in qs],
+                          [q.rate for q in qs], [q.dividend_yield for q in qs],
+                          [int(q.option_type == OptionType.PUT) for q in qs], [q.market_price for q in qs])
+        eng = self._engine or default_engine()
+        out = eng.solve_iv_arrays(arr, self._grid(), self.config.brent_tol_abs, self.config.max_iter)
+        res = []
+        for row in out:
+            if row["status"] == MANGO_OK:
+                res.append(IVSuccess(float(row["implied_vol"]), int(row["iterations"]), float(row["final_error"])))
+            else:
+                res.append(IVError(int(row["status"]), int(row["iterations"]), float(row["final_error"])))
+        return BatchIVResult(res, int(np.count_nonzero(out["status"])))
+
+    def solve(self, query):
+        r = self.solve_batch([query]).results[0]
+        if isinstance(r, IVError):
+            raise r
+        return r
+

@@ -15,12 +15,6 @@
 
 namespace mgpu {
 
-__global__ void prep_kernel(const TileDev*, int, const OptDev*, const double*, double*, uint8_t*,
-                            int32_t*, MarchConst);
-__global__ void march_kernel(const TileDev*, int, const OptDev*, double*, const uint8_t*,
-                             const int32_t*, int32_t*, int*, MarchConst);
-__global__ void outputs_kernel(const TileDev*, int, const OptDev*, const double*, double*,
-                               const int32_t*, const int32_t*, MarchConst, double*);
 __global__ void fp64_probe_kernel(double* out, int iters);
 
 void check(cudaError_t e, const char* what) {
@@ -104,12 +98,15 @@ std::string resolve(const MangoPricingParams& p, const MangoGpuGrid& g, Resolved
     case MANGO_GPU_GRID_AUTO:
       estimate_grid(p.spot, p.strike, p.maturity, p.volatility, def, &r->spec, &r->nt, scratch);
       break;
-    case MANGO_GPU_GRID_FIXED_N: {
+    case MANGO_GPU_GRID_FIXED_N:
+    case MANGO_GPU_GRID_FIXED_N_AT_VOL: {
       if (g.n_space < 3 || g.n_time < 1) return "grid: n_space >= 3 and n_time >= 1 required";
+      const double vol = g.kind == MANGO_GPU_GRID_FIXED_N ? p.volatility : g.alpha;
+      if (!(vol > 0.0) || !std::isfinite(vol)) return "grid: sizing volatility must be > 0";
       Accuracy a = def;
       a.min_points = a.max_points = g.n_space;
       int64_t nt_auto = 0;
-      estimate_grid(p.spot, p.strike, p.maturity, p.volatility, a, &r->spec, &nt_auto, scratch);
+      estimate_grid(p.spot, p.strike, p.maturity, vol, a, &r->spec, &nt_auto, scratch);
       r->nt = g.n_time;
       break;
     }
@@ -134,18 +131,18 @@ std::string resolve(const MangoPricingParams& p, const MangoGpuGrid& g, Resolved
   return {};
 }
 
-namespace {
-
 void set_err(MangoError* err, int32_t code, const std::string& msg) {
   if (!err) return;
   err->code = code;
   std::snprintf(err->message, sizeof(err->message), "%s", msg.c_str());
 }
 
+namespace {
 using Clock = std::chrono::steady_clock;
 double ms_since(Clock::time_point t0) {
   return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
 }
+}  // namespace
 
 MarchConst make_const(const MangoGpuTrbdf2* trbdf2) {
   MarchConst mc{};
@@ -402,7 +399,6 @@ uint64_t fetch_batch(MangoGpuBatch* b, MangoGpuAmericanOut* out, std::string* fi
   return failed;
 }
 
-}  // namespace
 }  // namespace mgpu
 
 using namespace mgpu;

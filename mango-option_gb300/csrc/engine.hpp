@@ -67,6 +67,30 @@ std::string resolve(const MangoPricingParams& p, const MangoGpuGrid& g, Resolved
 // Run f(i) for i in [0, n) on all host cores.
 void parallel_for(int64_t n, const std::function<void(int64_t)>& f);
 
+void set_err(MangoError* err, int32_t code, const std::string& msg);
+
+}  // namespace mgpu
+
+struct MangoGpuBatch;
+
+namespace mgpu {
+MarchConst make_const(const MangoGpuTrbdf2* trbdf2);
+// Validate, resolve grids, sort/tile, pack and upload (batch pipeline).
+MangoGpuBatch* create_batch(MangoGpuContext* ctx, const MangoPricingParams* params, int64_t n,
+                            const MangoGpuGrid* grids, uint64_t grid_stride,
+                            const MangoGpuTrbdf2* trbdf2);
+void destroy_batch(MangoGpuBatch* b);
+// Enqueue setup, march and outputs (with timing events).
+void run_batch(MangoGpuBatch* b);
+// Wait, copy results into caller slots, update the context stats.
+uint64_t fetch_batch(MangoGpuBatch* b, MangoGpuAmericanOut* out, std::string* first_msg);
+// Kernels (march.cu).
+__global__ void prep_kernel(const TileDev*, int, const OptDev*, const double*, double*, uint8_t*,
+                            int32_t*, MarchConst);
+__global__ void march_kernel(const TileDev*, int, const OptDev*, double*, const uint8_t*,
+                             const int32_t*, int32_t*, int*, MarchConst);
+__global__ void outputs_kernel(const TileDev*, int, const OptDev*, const double*, double*,
+                               const int32_t*, const int32_t*, MarchConst, double*);
 }  // namespace mgpu
 
 struct MangoGpuContext {

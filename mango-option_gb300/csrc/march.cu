@@ -78,6 +78,7 @@ __global__ void prep_kernel(const TileDev* __restrict__ tiles, int ntiles,
   const TileDev td = tiles[t];
   if (lane >= td.count) return;
   const int k = td.first + lane;
+  if (mc.active && !mc.active[k]) return;
   const OptDev o = opts[k];
   const int n = o.n;
   const TileView V{pool + td.off + lane, td.nx};
@@ -86,7 +87,8 @@ __global__ void prep_kernel(const TileDev* __restrict__ tiles, int ntiles,
   uint8_t* F = flags + td.foff + lane;
 
   const double rate = o.r;
-  const double hss = 0.5 * o.sigma * o.sigma;  // black_scholes_pde.hpp:45
+  const double sigma = mc.sigma ? mc.sigma[k] : o.sigma;
+  const double hss = 0.5 * sigma * sigma;  // black_scholes_pde.hpp:45
   const double drift = rate - o.q - hss;       // black_scholes_pde.hpp:73-74
   const double dt = o.dt;
   const double w1 = mc.gamma * dt / 2.0;       // trbdf2_config.hpp:39-41
@@ -427,8 +429,9 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= ntiles) break;
     const TileDev td = tiles[t];
-    const bool active = lane < td.count;
     const int k = td.first + lane;
+    const bool active = lane < td.count && (!mc.active || mc.active[k]);
+    if (!__any_sync(0xffffffffu, active)) continue;
     OptDev o{};
     int32_t md = 0;
     if (active) {
@@ -601,6 +604,7 @@ __global__ void outputs_kernel(const TileDev* __restrict__ tiles, int ntiles,
   const TileDev td = tiles[t];
   if (lane >= td.count) return;
   const int k = td.first + lane;
+  if (mc.active && !mc.active[k]) return;
   const OptDev o = opts[k];
   double* res = out4 + 4 * static_cast<size_t>(k);
   if (status[k] != kStatusOk) {
@@ -622,6 +626,11 @@ __global__ void outputs_kernel(const TileDev* __restrict__ tiles, int ntiles,
   else if (xs_ >= ROW(X, n - 1)) value = V.at(au, n - 1) * o.strike;
   else value = dmax_ref(0.0, sv) * o.strike;
   const double delta = sd * (o.strike / o.spot);
+  if (mc.value_only) {
+    res[0] = value;
+    res[1] = delta;
+    return;
+  }
   // gamma: stencil derivatives linearly interpolated at x_spot.
   int il, ir;
   if (xs_ <= ROW(X, 0)) {

@@ -68,7 +68,9 @@ struct MarchConst {
   double alpha;     // 1 / (gamma (2 - gamma))
   double beta;      // -(1 - gamma)^2 / (gamma (2 - gamma))
   int32_t rannacher;
-  int32_t pad;
+  int32_t value_only;            // outputs: skip delta/gamma/theta
+  const double* sigma;           // per-option volatility override (sorted), or null
+  const int32_t* active;         // per-option run flag (sorted), or null = all
 };
 
 // Status codes written per option (MangoStatus values).

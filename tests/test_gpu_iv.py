@@ -1,0 +1,90 @@
+"""GPU FDM implied volatility (Brent) against the reference's own IVSolver and
+the CPU oracle.  Bar: implied vols within 1e-8 (the benchmark spec), the same Brent
+iteration counts (the device replays the reference's iterate sequence), and
+the reference's error categories for invalid quotes."""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def per_quote_grid(pkg, vol, nx=101, nt=498):
+    return pkg.grid_array(len(vol), pkg.GRID_FIXED_N_AT_VOL, nx, nt, alpha=vol)
+
+
+def test_iv_vs_reference_brent(engine, pkg):
+    g = golden("iv.npz")
+    q = pkg.query_array(g["S"], g["K"], g["T"], g["r"], g["q"], g["is_put"], g["price"])
+    out = engine.solve_iv_arrays(q, per_quote_grid(pkg, g["true_vol"], 101, 498))
+    assert (out["status"] == 0).all() and (g["status"] == 0).all()
+    assert np.abs(out["implied_vol"] - g["out"][:, 0]).max() < 1e-8
+    assert (out["iterations"] == g["out"][:, 1]).all()
+    # and the round trip to the vol the prices were made with
+    assert np.abs(out["implied_vol"] - g["true_vol"]).max() < 1e-6
+
+
+def test_iv_vs_oracle_sample(engine, pkg, oracle):
+    rng = np.random.default_rng(77)
+    n = 384
+    S = np.full(n, 100.0)
+    K = S * rng.uniform(0.8, 1.2, n)
+    T = rng.uniform(0.02, 2.0, n)
+    r = rng.uniform(0.0, 0.08, n)
+    q = rng.uniform(0.0, 0.04, n)
+    vt = rng.uniform(0.05, 0.8, n)
+    put = (np.arange(n) % 3 != 0).astype(np.int32)
+    grids = per_quote_grid(pkg, vt)
+    px = engine.price_arrays(pkg.pricing_array(S, K, T, vt, r, q, put),
+                             pkg.grid_array(n, pkg.GRID_FIXED_N_AT_VOL, 101, 498, alpha=vt))
+    assert (px["status"] == 0).all()
+    out = engine.solve_iv_arrays(pkg.query_array(S, K, T, r, q, put, px["value"]), grids)
+    ref, st = oracle.iv_batch(S, K, T, r, q, put, px["value"], vt, 101, 498)
+    ok = (st == 0)
+    assert (out["status"][ok] == 0).all()
+    # Same Brent path: identical iteration counts and final residuals.
+    assert (out["iterations"][ok] == ref[ok, 1]).all()
+    assert np.allclose(out["final_error"][ok], ref[ok, 2], rtol=1e-6, atol=1e-12)
+    # Vols within 1e-8, except where the quote is ill-conditioned: Brent
+    # stops at |f| < 1e-6 in price units, so a rounding-level price
+    # difference dp moves the root by dp / vega.  Allow 1e-11 dollars.
+    h = 1e-4
+    sig = out["implied_vol"]
+    up = engine.price_arrays(pkg.pricing_array(S, K, T, sig + h, r, q, put), grids)["value"]
+    dn = engine.price_arrays(pkg.pricing_array(S, K, T, sig - h, r, q, put), grids)["value"]
+    vega = np.abs(up - dn) / (2 * h)
+    allowed = 1e-8 + 1e-11 / np.maximum(vega, 1e-12)
+    d = np.abs(sig - ref[:, 0])
+    assert (d[ok] <= allowed[ok]).all(), f"worst {d[ok].max():.3e}"
+    assert np.mean(d[ok] < 1e-8) > 0.95
+    # failures (if any) land in the same category as the oracle's
+    assert ((out["status"] != 0) == ~ok).all()
+
+
+def test_iv_error_slots(engine, pkg):
+    q = pkg.query_array([100, 100, 100, -1, 100], [100, 80, 120, 100, 100], 1.0, 0.05, 0.0,
+                        [1, 1, 1, 1, 1], [5.0, 10.0, 25.0, 5.0, 150.0])
+    out = engine.solve_iv_arrays(q, pkg.grid_array(1, pkg.GRID_FIXED_N_AT_VOL, 101, 200, alpha=0.3))
+    # put K=80 priced 10 > K - S? intrinsic 0, fine; K=120 price 25 >= intrinsic 20: fine
+    assert out["status"][0] == 0 and out["status"][1] == 0 and out["status"][2] == 0
+    assert out["status"][3] == pkg.MANGO_ERR_VALIDATION     # invalid spot
+    assert out["status"][4] == pkg.MANGO_ERR_ARBITRAGE      # price above the strike
+    below = pkg.query_array(100, 120, 1.0, 0.05, 0.0, 1, 15.0)  # below intrinsic 20
+    assert engine.solve_iv_arrays(below, pkg.grid_array(1, pkg.GRID_FIXED_N_AT_VOL, 101, 200, alpha=0.3))[
+        "status"][0] == pkg.MANGO_ERR_ARBITRAGE
+    auto = pkg.grid_array(1, pkg.GRID_AUTO)
+    assert engine.solve_iv_arrays(q[:1], auto)["status"][0] == pkg.MANGO_ERR_VALIDATION
+
+
+def test_iv_solver_mirror(pkg):
+    solver = pkg.IVSolver(pkg.IVSolverConfig(grid=pkg.FixedGrid(101, 300), grid_vol=0.25))
+    p = pkg.PricingParams(spot=100, strike=105, maturity=0.75, rate=0.03, dividend_yield=0.01,
+                          option_type=pkg.OptionType.PUT, volatility=0.25)
+    with pkg.Engine(0) as eng:
+        px = eng.price_arrays(pkg.pricing_array(100, 105, 0.75, 0.25, 0.03, 0.01, 1),
+                              pkg.grid_array(1, pkg.GRID_FIXED_N_AT_VOL, 101, 300, alpha=0.25))
+    res = solver.solve(pkg.IVQuery(spot=100, strike=105, maturity=0.75, rate=0.03, dividend_yield=0.01,
+                                   option_type=pkg.OptionType.PUT, market_price=float(px["value"][0])))
+    assert abs(res.implied_vol - 0.25) < 1e-6
+    assert p.volatility == 0.25

@@ -193,6 +193,50 @@ MangoStatus mango_gpu_solve_iv_batch(MangoGpuContext* ctx, const MangoIvQuery* q
                                      const MangoIvConfig* config, MangoIvBatchSlot* out,
                                      uint64_t* out_failed, MangoError* err);
 
+/* Price-table PDE sweep: PriceTableBuilderND<4>::make_batch + solve_batch +
+ * extract_tensor (src/option/table/bspline/bspline_builder.cpp:198-480).  One
+ * American option per (volatility, rate) pair at spot = strike = K_ref and
+ * maturity = the last maturity-axis point, marched with snapshots at the
+ * maturity axis and resampled onto the log-moneyness axis by natural cubic
+ * splines.  grid: NULL or MANGO_GPU_GRID_AUTO => GridAccuracyParams{} (one
+ * shared grid); MANGO_GPU_GRID_SINH / _UNIFORM => PDEGridConfig, used as is
+ * when it meets the reference's width / spacing limits, else the reference's
+ * fallback (auto estimation pinned to n_space, per-slice grids through the
+ * normalized-chain route).  tensor: nm*ntau*nsig*nr doubles, layout
+ * [moneyness][maturity][volatility][rate], normalized prices V/K_ref; NaN for
+ * failed slices.  slice_dims (nullable): {n_space, n_time} per slice, slices
+ * ordered volatility-major.  No C export in the reference (C++ API only). */
+MangoStatus mango_gpu_price_table_sweep(MangoGpuContext* ctx, const double* moneyness,
+                                        uint64_t nm, const double* maturity, uint64_t ntau,
+                                        const double* volatility, uint64_t nsig,
+                                        const double* rate, uint64_t nr, double K_ref,
+                                        double dividend_yield, MangoOptionType option_type,
+                                        const MangoGpuGrid* grid, double* tensor,
+                                        int64_t* slice_dims, uint64_t* out_failed_slices,
+                                        MangoError* err);
+
+/* 4D cubic B-spline surface: BSplineND<double,4> (src/math/bspline/
+ * bspline_nd.hpp:66-157) with knots from clamped_knots_cubic
+ * (src/math/bspline/bspline_basis.hpp:47-91) on each axis grid.  grids:
+ * the four axis grids concatenated (sizes[4] points each, 4..512, strictly
+ * increasing); coeffs: row-major [axis0][axis1][axis2][axis3].  The surface
+ * keeps knots, reciprocal tables and coefficients in device memory. */
+typedef struct MangoGpuBSpline4D MangoGpuBSpline4D;
+MangoStatus mango_gpu_bspline4d_create(MangoGpuContext* ctx, const double* grids,
+                                       const int64_t* sizes, const double* coeffs,
+                                       MangoGpuBSpline4D** out, MangoError* err);
+void mango_gpu_bspline4d_destroy(MangoGpuBSpline4D* surface);
+/* BSplineND::eval for n query points (queries: n x 4, host arrays; out: n). */
+MangoStatus mango_gpu_bspline4d_eval(MangoGpuBSpline4D* surface, const double* queries,
+                                     uint64_t n, double* out, MangoError* err);
+/* Same with device-resident queries and output, enqueued on the context's
+ * stream without waiting. */
+MangoStatus mango_gpu_bspline4d_eval_device(MangoGpuBSpline4D* surface, const double* d_queries,
+                                            uint64_t n, double* d_out, MangoError* err);
+/* The packed knot vectors (axis 0..3, sizes[d] + 4 each), for inspection. */
+MangoStatus mango_gpu_bspline4d_knots(const MangoGpuBSpline4D* surface, double* out, uint64_t cap,
+                                      uint64_t* n_out);
+
 /* Resident batch: the same pipeline as mango_gpu_price_american_batch split
  * so that inputs can stay in device memory across runs (repeat pricing of a
  * book, IV iterations, benchmarking).  _create validates, resolves grids and

@@ -131,6 +131,21 @@ def library() -> ctypes.CDLL:
                                                  ctypes.POINTER(MangoIvConfig), _P,
                                                  ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(MangoError)]
         lib.mango_gpu_solve_iv_batch.restype = ctypes.c_int32
+        lib.mango_gpu_price_table_sweep.argtypes = [
+            _P, _P, ctypes.c_uint64, _P, ctypes.c_uint64, _P, ctypes.c_uint64, _P, ctypes.c_uint64,
+            ctypes.c_double, ctypes.c_double, ctypes.c_int32, _P, _P, _P, ctypes.POINTER(ctypes.c_uint64),
+            ctypes.POINTER(MangoError)]
+        lib.mango_gpu_price_table_sweep.restype = ctypes.c_int32
+        lib.mango_gpu_bspline4d_create.argtypes = [_P, _P, _P, _P, ctypes.POINTER(_P), ctypes.POINTER(MangoError)]
+        lib.mango_gpu_bspline4d_create.restype = ctypes.c_int32
+        lib.mango_gpu_bspline4d_destroy.argtypes = [_P]
+        lib.mango_gpu_bspline4d_destroy.restype = None
+        lib.mango_gpu_bspline4d_eval.argtypes = [_P, _P, ctypes.c_uint64, _P, ctypes.POINTER(MangoError)]
+        lib.mango_gpu_bspline4d_eval.restype = ctypes.c_int32
+        lib.mango_gpu_bspline4d_eval_device.argtypes = [_P, _P, ctypes.c_uint64, _P, ctypes.POINTER(MangoError)]
+        lib.mango_gpu_bspline4d_eval_device.restype = ctypes.c_int32
+        lib.mango_gpu_bspline4d_knots.argtypes = [_P, _P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
+        lib.mango_gpu_bspline4d_knots.restype = ctypes.c_int32
         lib.mango_gpu_build_info.argtypes = []
         lib.mango_gpu_build_info.restype = ctypes.c_char_p
         _lib = lib
@@ -302,6 +317,29 @@ class Engine:
             raise EngineError(f"mango_gpu_solve_iv_batch: {err.message.decode(errors='replace')}")
         return out
 
+    def price_table_sweep(self, moneyness, maturity, volatility, rate, K_ref: float = 100.0,
+                          dividend_yield: float = 0.0, option_type: int = 1, grid=None):
+        """PriceTableBuilderND<4> sweep + extraction (mango_gpu_price_table_sweep).
+        Returns (tensor [m][tau][sigma][r] of V/K_ref, slice dims (n_slices x 2),
+        failed slice count).  grid: None (GridAccuracyParams{}) or PDEGridConfig."""
+        axes = [np.ascontiguousarray(a, dtype=np.float64) for a in (moneyness, maturity, volatility, rate)]
+        shape = tuple(a.size for a in axes)
+        tensor = np.zeros(shape)
+        dims = np.zeros((shape[2] * shape[3], 2), np.int64)
+        g = None if grid is None else _grid_entry(grid)
+        failed = ctypes.c_uint64()
+        err = MangoError()
+        st = library().mango_gpu_price_table_sweep(
+            self._ctx, _ptr(axes[0]), shape[0], _ptr(axes[1]), shape[1], _ptr(axes[2]), shape[2],
+            _ptr(axes[3]), shape[3], K_ref, dividend_yield, int(option_type), _ptr(g), _ptr(tensor),
+            _ptr(dims), ctypes.byref(failed), ctypes.byref(err))
+        if st != MANGO_OK:
+            raise EngineError(f"mango_gpu_price_table_sweep: {err.message.decode(errors='replace')}")
+        return tensor, dims, failed.value
+
+    def bspline4d(self, grids, coeffs) -> "BSpline4D":
+        return BSpline4D(self, grids, coeffs)
+
     def set_stream(self, stream_handle: Optional[int]) -> None:
         """Enqueue on a caller's cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""
         library().mango_gpu_context_set_stream(self._ctx, _P(stream_handle) if stream_handle else None)
@@ -322,6 +360,56 @@ class Engine:
         s = MangoGpuStats()
         library().mango_gpu_last_stats(self._ctx, ctypes.byref(s))
         return {k: getattr(s, k) for k, _ in MangoGpuStats._fields_}
+
+
+class BSpline4D:
+    """Device-resident 4D cubic B-spline surface (mango_gpu_bspline4d_*),
+    the counterpart of BSplineND<double,4>."""
+
+    def __init__(self, engine: Engine, grids, coeffs):
+        self._engine = engine
+        gs = [np.ascontiguousarray(g, dtype=np.float64) for g in grids]
+        self.sizes = np.array([g.size for g in gs], np.int64)
+        packed = np.concatenate(gs)
+        c = np.ascontiguousarray(coeffs, dtype=np.float64).ravel()
+        self._s = _P()
+        err = MangoError()
+        st = library().mango_gpu_bspline4d_create(engine._ctx, _ptr(packed), _ptr(self.sizes), _ptr(c),
+                                                  ctypes.byref(self._s), ctypes.byref(err))
+        if st != MANGO_OK:
+            self._s = None
+            raise EngineError(err.message.decode(errors="replace"))
+
+    def eval(self, queries: np.ndarray) -> np.ndarray:
+        q = np.ascontiguousarray(queries, dtype=np.float64).reshape(-1, 4)
+        out = np.zeros(q.shape[0])
+        err = MangoError()
+        if library().mango_gpu_bspline4d_eval(self._s, _ptr(q), q.shape[0], _ptr(out), ctypes.byref(err)) != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+        return out
+
+    def eval_device(self, d_queries: int, n: int, d_out: int) -> None:
+        err = MangoError()
+        if library().mango_gpu_bspline4d_eval_device(self._s, _P(d_queries), n, _P(d_out), ctypes.byref(err)) != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+
+    def knots(self) -> np.ndarray:
+        n = ctypes.c_uint64()
+        library().mango_gpu_bspline4d_knots(self._s, None, 0, ctypes.byref(n))
+        out = np.zeros(n.value)
+        library().mango_gpu_bspline4d_knots(self._s, _ptr(out), n.value, ctypes.byref(n))
+        return out
+
+    def close(self):
+        if self._s:
+            library().mango_gpu_bspline4d_destroy(self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class ResidentBatch:

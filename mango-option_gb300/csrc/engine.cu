@@ -174,16 +174,11 @@ MangoGpuBatch* create_batch(MangoGpuContext* ctx, const MangoPricingParams* para
                             const MangoGpuGrid* grids, uint64_t grid_stride,
                             const MangoGpuTrbdf2* trbdf2) {
   auto t0 = Clock::now();
-  std::unique_ptr<MangoGpuBatch, void (*)(MangoGpuBatch*)> b(new MangoGpuBatch(), destroy_batch);
-  b->ctx = ctx;
-  b->n = n;
-  b->mc = make_const(trbdf2);
-  b->res.resize(static_cast<size_t>(n));
-  b->msgs.resize(static_cast<size_t>(n));
-  for (auto& e : b->ev) check(cudaEventCreate(&e), "cudaEventCreate");
+  std::vector<Resolved> res(static_cast<size_t>(n));
+  std::vector<std::string> msgs(static_cast<size_t>(n));
   parallel_for(n, [&](int64_t i) {
     thread_local std::vector<double> scratch;
-    Resolved& r = b->res[i];
+    Resolved& r = res[i];
     r.orig = static_cast<int32_t>(i);
     std::string m = validate(params[i]);
     if (m.empty()) {
@@ -194,9 +189,29 @@ MangoGpuBatch* create_batch(MangoGpuContext* ctx, const MangoPricingParams* para
     }
     if (!m.empty()) {
       r.status = MANGO_ERR_VALIDATION;
-      b->msgs[i] = m;
+      msgs[i] = m;
     }
   });
+  const double resolve_ms = ms_since(t0);
+  MangoGpuBatch* b = create_batch_resolved(ctx, params, std::move(res), std::move(msgs), trbdf2);
+  b->host_prep_ms += resolve_ms;
+  return b;
+}
+
+MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingParams* params,
+                                     std::vector<Resolved> resolved,
+                                     std::vector<std::string> messages,
+                                     const MangoGpuTrbdf2* trbdf2) {
+  auto t0 = Clock::now();
+  const int64_t n = static_cast<int64_t>(resolved.size());
+  std::unique_ptr<MangoGpuBatch, void (*)(MangoGpuBatch*)> b(new MangoGpuBatch(), destroy_batch);
+  b->ctx = ctx;
+  b->n = n;
+  b->mc = make_const(trbdf2);
+  b->res = std::move(resolved);
+  b->msgs = std::move(messages);
+  b->msgs.resize(static_cast<size_t>(n));
+  for (auto& e : b->ev) check(cudaEventCreate(&e), "cudaEventCreate");
   // Sort accepted options by (n_space, n_time) descending: similar lanes
   // share a tile and the largest tiles are dequeued first.
   std::vector<int32_t>& order = b->order;

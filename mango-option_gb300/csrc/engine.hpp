@@ -79,6 +79,12 @@ MarchConst make_const(const MangoGpuTrbdf2* trbdf2);
 MangoGpuBatch* create_batch(MangoGpuContext* ctx, const MangoPricingParams* params, int64_t n,
                             const MangoGpuGrid* grids, uint64_t grid_stride,
                             const MangoGpuTrbdf2* trbdf2);
+// Same pipeline from already validated and resolved options (res[i].orig
+// indexes params; status != 0 entries stay off the device).
+MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingParams* params,
+                                     std::vector<Resolved> resolved,
+                                     std::vector<std::string> messages,
+                                     const MangoGpuTrbdf2* trbdf2);
 void destroy_batch(MangoGpuBatch* b);
 // Enqueue setup, march and outputs (with timing events).
 void run_batch(MangoGpuBatch* b);

@@ -445,6 +445,22 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
     const uint8_t* F = flags + td.foff + lane;
     int32_t st = kStatusOk;
     const double dt = o.dt;
+    // Snapshot taps: copy the state after the listed steps.
+    int sp = 0, sc = 0;
+    const int32_t* sidx = nullptr;
+    double* sout = nullptr;
+    if (active && mc.snap_idx) {
+      sidx = mc.snap_idx + mc.snap_begin[k];
+      sc = mc.snap_count[k];
+      sout = mc.snap_out + mc.snap_off[k];
+    }
+    auto record = [&](int state, int arr) {
+      while (sp < sc && sidx[sp] == state) {
+        for (int i = 0; i < n; ++i) sout[static_cast<size_t>(sp) * n + i] = V.at(arr, i);
+        ++sp;
+      }
+    };
+    if (active) record(0, A_U);
     int step = 0;
     if (mc.rannacher) {
       // solve_rannacher_startup (pde_solver.hpp:413-447): two implicit Euler
@@ -456,6 +472,7 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
       stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_next),
                         mc.alpha, mc.beta, A_G, A_U, st);
       step = 1;
+      if (active && nt >= 1) record(1, A_U);
     }
     for (; step < td.nt; ++step) {
       const bool live = active && step < nt && st == kStatusOk;
@@ -468,6 +485,7 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
                      mc.beta, A_U, A_G, st);
       stage<kStage2>(live, n, V, F, nocache, o.bc_left, right_bc(o, tn), mc.alpha,
                      mc.beta, A_G, last ? A_G : A_U, st);
+      if (live && sc) record(step + 1, last ? A_G : A_U);
     }
     if (active) status[k] = st;
   }

@@ -71,6 +71,15 @@ struct MarchConst {
   int32_t value_only;            // outputs: skip delta/gamma/theta
   const double* sigma;           // per-option volatility override (sorted), or null
   const int32_t* active;         // per-option run flag (sorted), or null = all
+  // Snapshot taps (Grid::record, src/pde/core/grid.hpp:947-961), or null:
+  // per sorted option, snap_count ascending state indices starting at
+  // snap_idx + snap_begin[k]; the state after that step goes to
+  // snap_out + snap_off[k] + j * n.
+  const int32_t* snap_idx;
+  const int32_t* snap_begin;
+  const int32_t* snap_count;
+  const int64_t* snap_off;
+  double* snap_out;
 };
 
 // Status codes written per option (MangoStatus values).

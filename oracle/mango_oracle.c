@@ -870,3 +870,151 @@ int32_t mo_iv_batch(int64_t n, const double* S, const double* K, const double* T
   (void)n_threads;
   return 0;
 }
+
+/* ------------------------------------------------------------ B-splines -- */
+
+void mo_clamped_knots(const double* x, int64_t n, double* t) {
+  /* clamped_knots_cubic, src/math/bspline/bspline_basis.hpp:47-91 */
+  for (int k = 0; k < 4; ++k) t[k] = x[0];
+  if (n > 4) {
+    const int64_t interior = n - 4, intervals = n - 1;
+    for (int64_t idx = 0; idx < interior; ++idx) {
+      const double ratio = (double)(idx + 1) / (double)(interior + 1);
+      const double pos = ratio * (double)intervals;
+      int64_t low = (int64_t)floor(pos);
+      if (low >= intervals) low = intervals - 1;
+      const double frac = pos - (double)low;
+      const double left = x[low], right = x[low + 1];
+      double knot = (1.0 - frac) * left + frac * right;
+      const double spacing = right - left;
+      const double e1 = 128.0 * DBL_EPSILON * spacing;
+      const double e2 = DBL_EPSILON * dmax(fabs(right), 1.0);
+      const double eps = dmax(e1, e2);
+      const double lo = left + eps, hi = right - eps;
+      if (knot < lo) knot = lo;            /* std::clamp(v, lo, hi) */
+      else if (hi < knot) knot = hi;
+      t[4 + idx] = knot;
+    }
+  }
+  for (int k = 0; k < 4; ++k) t[n + k] = x[n - 1];
+}
+
+/* find_span_cubic, bspline_basis.hpp:120-142 */
+static int span_cubic(const double* t, int nk, double x) {
+  const int n_ctrl = nk - 4;
+  const int max_span = n_ctrl - 1 > 3 ? n_ctrl - 1 : 3;
+  if (x <= t[3]) return 3;
+  if (x >= t[n_ctrl]) return max_span;
+  int lo = 3, hi = n_ctrl + 1; /* upper_bound: first t > x */
+  while (lo < hi) {
+    const int mid = lo + (hi - lo) / 2;
+    if (t[mid] <= x) lo = mid + 1; else hi = mid;
+  }
+  int i = lo - 1;
+  if (i < 3) i = 3;
+  if (i > max_span) i = max_span;
+  return i;
+}
+
+/* cubic_basis_nonuniform, bspline_basis.hpp:164-238 (full triangle). */
+static void basis_cubic(const double* t, int n, int i, double x, double N[4]) {
+  if (fabs(x - t[n - 1]) < 64.0 * DBL_EPSILON * dmax(fabs(t[n - 1]), 1.0)) {
+    N[0] = 1.0; N[1] = 0.0; N[2] = 0.0; N[3] = 0.0;
+    return;
+  }
+  double N0[4] = {0, 0, 0, 0}, N1[4] = {0, 0, 0, 0}, N2[4] = {0, 0, 0, 0};
+  for (int k = 0; k < 4; ++k) {
+    const int idx = i - k;
+    if (idx >= 0 && idx + 1 < n) N0[k] = (t[idx] <= x && x < t[idx + 1]) ? 1.0 : 0.0;
+  }
+  for (int k = 0; k < 4; ++k) {
+    const int idx = i - k;
+    if (idx >= 0 && idx + 2 < n) {
+      const double ld = t[idx + 1] - t[idx], rd = t[idx + 2] - t[idx + 1];
+      const double l = (ld > 0.0) ? (x - t[idx]) / ld * N0[k] : 0.0;
+      const double r = (rd > 0.0 && k > 0) ? (t[idx + 2] - x) / rd * N0[k - 1] : 0.0;
+      N1[k] = l + r;
+    }
+  }
+  for (int k = 0; k < 4; ++k) {
+    const int idx = i - k;
+    if (idx >= 0 && idx + 3 < n) {
+      const double ld = t[idx + 2] - t[idx], rd = t[idx + 3] - t[idx + 1];
+      const double l = (ld > 0.0) ? (x - t[idx]) / ld * N1[k] : 0.0;
+      const double r = (rd > 0.0 && k > 0) ? (t[idx + 3] - x) / rd * N1[k - 1] : 0.0;
+      N2[k] = l + r;
+    }
+  }
+  for (int k = 0; k < 4; ++k) {
+    const int idx = i - k;
+    if (idx >= 0 && idx + 4 < n) {
+      const double ld = t[idx + 3] - t[idx], rd = t[idx + 4] - t[idx + 1];
+      const double l = (ld > 0.0) ? (x - t[idx]) / ld * N2[k] : 0.0;
+      const double r = (rd > 0.0 && k > 0) ? (t[idx + 4] - x) / rd * N2[k - 1] : 0.0;
+      N[k] = l + r;
+    } else {
+      N[k] = 0.0;
+    }
+  }
+}
+
+int32_t mo_bspline4d_eval(const int64_t* sizes, const double* grids, const double* coeffs,
+                          const double* q, int64_t n, double* out) {
+  double* knots[4];
+  const double* g[4];
+  int nk[4];
+  const double* gp = grids;
+  for (int d = 0; d < 4; ++d) {
+    if (sizes[d] < 4) return 1;
+    nk[d] = (int)sizes[d] + 4;
+    knots[d] = (double*)malloc(sizeof(double) * (size_t)nk[d]);
+    g[d] = gp;
+    mo_clamped_knots(gp, sizes[d], knots[d]);
+    gp += sizes[d];
+  }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+  for (int64_t qi = 0; qi < n; ++qi) {
+    int span[4];
+    double w[4][4];
+    for (int d = 0; d < 4; ++d) {
+      double x = q[4 * qi + d];
+      const double lo = g[d][0], hi = g[d][sizes[d] - 1];
+      if (x <= lo) x = lo;                       /* clamp_bspline_query */
+      else if (x >= hi) x = nextafter(hi, -INFINITY);
+      span[d] = span_cubic(knots[d], nk[d], x);
+      basis_cubic(knots[d], nk[d], span[d], x, w[d]);
+    }
+    /* eval_tensor_product, bspline_nd.hpp:314-346 */
+    double s0 = 0.0;
+    for (int o0 = 0; o0 < 4; ++o0) {
+      const int i0 = span[0] - o0;
+      if ((unsigned)i0 >= (unsigned)sizes[0]) continue;
+      double s1 = 0.0;
+      for (int o1 = 0; o1 < 4; ++o1) {
+        const int i1 = span[1] - o1;
+        if ((unsigned)i1 >= (unsigned)sizes[1]) continue;
+        double s2 = 0.0;
+        for (int o2 = 0; o2 < 4; ++o2) {
+          const int i2 = span[2] - o2;
+          if ((unsigned)i2 >= (unsigned)sizes[2]) continue;
+          double s3 = 0.0;
+          for (int o3 = 0; o3 < 4; ++o3) {
+            const int i3 = span[3] - o3;
+            if ((unsigned)i3 >= (unsigned)sizes[3]) continue;
+            const double c =
+                coeffs[(((int64_t)i0 * sizes[1] + i1) * sizes[2] + i2) * sizes[3] + i3];
+            s3 = fma(c, w[3][o3], s3);
+          }
+          s2 = fma(s3, w[2][o2], s2);
+        }
+        s1 = fma(s2, w[1][o1], s1);
+      }
+      s0 = fma(s1, w[0][o0], s0);
+    }
+    out[qi] = s0;
+  }
+  for (int d = 0; d < 4; ++d) free(knots[d]);
+  return 0;
+}

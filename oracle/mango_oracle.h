@@ -92,6 +92,15 @@ int32_t mo_thomas_projected(const double* lower, const double* diag, const doubl
                             const double* rhs, const double* psi, double* x, int64_t n,
                             double* ws);
 
+/* clamped_knots_cubic (src/math/bspline/bspline_basis.hpp:47-91): n + 4 knots. */
+void mo_clamped_knots(const double* x, int64_t n, double* t);
+
+/* BSplineND<double,4>::eval (src/math/bspline/bspline_nd.hpp:133-157,
+ * 314-346) with knots from mo_clamped_knots on each axis.  grids: the four
+ * axes concatenated (sizes[d] points each); coeffs row-major; q: n x 4. */
+int32_t mo_bspline4d_eval(const int64_t* sizes, const double* grids, const double* coeffs,
+                          const double* q, int64_t n, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,6 +15,7 @@
 #include "mango/option/grid_spec_types.hpp"
 #include "mango/math/bspline/bspline_nd.hpp"
 #include "mango/math/bspline/bspline_basis.hpp"
+#include "mango/option/table/bspline/bspline_builder.hpp"
 
 #include <omp.h>
 #include <cmath>
@@ -24,6 +25,19 @@
 #include <array>
 
 using namespace mango;
+
+// The reference declares this friend for its tests (bspline_builder.hpp:368);
+// the oracle defines its own to reach the private sweep stage.
+namespace mango::testing {
+template <>
+struct PriceTableBuilderAccess<4> {
+  static BatchAmericanOptionResult solve_batch(const PriceTableBuilderND<4>& b,
+                                               const std::vector<PricingParams>& batch,
+                                               const PriceTableAxesND<4>& a) {
+    return b.solve_batch(batch, a);
+  }
+};
+}  // namespace mango::testing
 
 namespace {
 
@@ -205,6 +219,77 @@ int32_t ref_iv_batch(int64_t n, const double* S, const double* K, const double* 
     out3[3 * i + 1] = static_cast<double>(res->iterations);
     out3[3 * i + 2] = res->final_error;
   }
+  return 0;
+}
+
+// 4D cubic B-spline: knots from clamped_knots_cubic (bspline_basis.hpp:47-91)
+// on each axis grid, then BSplineND<double,4>::eval (bspline_nd.hpp:133-157).
+// sizes[4]; grids concatenated; coeffs row-major [d0][d1][d2][d3]; q n x 4.
+int32_t ref_bspline4d_eval(const int64_t* sizes, const double* grids, const double* coeffs,
+                           const double* q, int64_t n, double* out, double* knots_out) {
+  std::array<std::vector<double>, 4> g, k;
+  size_t off = 0, total = 1, koff = 0;
+  for (int d = 0; d < 4; ++d) {
+    g[d].assign(grids + off, grids + off + sizes[d]);
+    off += static_cast<size_t>(sizes[d]);
+    k[d] = clamped_knots_cubic(g[d]);
+    total *= static_cast<size_t>(sizes[d]);
+    if (knots_out) {
+      for (size_t j = 0; j < k[d].size(); ++j) knots_out[koff + j] = k[d][j];
+      koff += k[d].size();
+    }
+  }
+  std::vector<double> c(coeffs, coeffs + total);
+  auto sp = BSplineND<double, 4>::create(g, k, std::move(c));
+  if (!sp) return 1;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i)
+    out[i] = sp->eval({q[4 * i + 0], q[4 * i + 1], q[4 * i + 2], q[4 * i + 3]});
+  return 0;
+}
+
+// Price-table PDE sweep + extraction (PriceTableBuilderND<4>::make_batch,
+// solve_batch, extract_tensor; src/option/table/bspline/bspline_builder.cpp:
+// 198-480).  grid_kind 0: GridAccuracyParams{}; 1: PDEGridConfig with
+// GridSpec::sinh_spaced(x_min, x_max, nx, alpha) and n_time steps.
+// out: tensor [m][tau][sigma][r]; dims: per (sigma, r) slice {n_space, n_time}.
+int32_t ref_table_sweep(const double* m, int64_t nm, const double* tau, int64_t ntau,
+                        const double* sig, int64_t ns, const double* rr, int64_t nr,
+                        double K_ref, double q, int32_t is_put, int32_t grid_kind,
+                        double x_min, double x_max, int64_t nx, double alpha, int64_t n_time,
+                        double* out, int64_t* dims) {
+  PriceTableConfig cfg;
+  cfg.option_type = is_put ? OptionType::PUT : OptionType::CALL;
+  cfg.K_ref = K_ref;
+  cfg.dividends.dividend_yield = q;
+  if (grid_kind == 1) {
+    auto spec = GridSpec<double>::sinh_spaced(x_min, x_max, static_cast<size_t>(nx), alpha);
+    if (!spec) return 1;
+    cfg.pde_grid = PDEGridConfig{*spec, static_cast<size_t>(n_time), {}};
+  }
+  PriceTableBuilderND<4> b(cfg);
+  PriceTableAxesND<4> axes;
+  axes.grids[0].assign(m, m + nm);
+  axes.grids[1].assign(tau, tau + ntau);
+  axes.grids[2].assign(sig, sig + ns);
+  axes.grids[3].assign(rr, rr + nr);
+  auto batch = b.make_batch(axes);
+  auto res = testing::PriceTableBuilderAccess<4>::solve_batch(b, batch, axes);
+  for (size_t i = 0; i < res.results.size(); ++i) {
+    if (res.results[i]) {
+      dims[2 * i] = static_cast<int64_t>(res.results[i]->grid()->n_space());
+      dims[2 * i + 1] = static_cast<int64_t>(res.results[i]->grid()->time().n_steps());
+    } else {
+      dims[2 * i] = dims[2 * i + 1] = -1;
+    }
+  }
+  auto ext = b.extract_tensor(res, axes);
+  if (!ext) return 2;
+  for (int64_t i = 0; i < nm; ++i)
+    for (int64_t j = 0; j < ntau; ++j)
+      for (int64_t k = 0; k < ns; ++k)
+        for (int64_t l = 0; l < nr; ++l)
+          out[((i * ntau + j) * ns + k) * nr + l] = ext->tensor.view[i, j, k, l];
   return 0;
 }
 

@@ -20,6 +20,13 @@ every output value):
   grids.npz          reference grids (bit-exact host grid generation)
   solutions.npz      full final and previous solution vectors for 4 options
   iv.npz             16 FDM implied vols (Brent) on per-quote 101 x 498 grids
+  bspline.npz        BSplineND<double,4>::eval on the 50x30x20x10 table axes with
+                     seeded standard-normal coefficients (regenerated from the
+                     stored seed), 4096 random + edge queries, and the knots
+  table.npz          PriceTableBuilderND<4> sweep + extraction on reduced axes
+                     (12 x 6 x 5 x 3) for the explicit 201 x 1000 grid (the
+                     reference's per-slice fallback route) and the default
+                     accuracy route, with each slice's (N_x, N_t)
 """
 from __future__ import annotations
 
@@ -218,6 +225,61 @@ def main():
                      ctypes.c_int32(8), P(o3), P(st))
     save("iv.npz", S=S, K=K, T=T, r=r, q=q, is_put=put, price=px, true_vol=vt, nx=nx, nt=nt,
          out=o3.reshape(n, 3), status=st)
+
+    golden_bspline(lib)
+    golden_table(lib)
+
+
+def table_axes(nm, ntau, ns, nr):
+    return (np.linspace(np.log(0.7), np.log(1.3), nm), np.linspace(0.02, 2.0, ntau),
+            np.linspace(0.05, 0.8, ns), np.linspace(0.0, 0.08, nr))
+
+
+BSPLINE_SEED = 2025
+
+
+def bspline_coeffs(sizes):
+    return np.random.default_rng(BSPLINE_SEED).standard_normal(int(np.prod(sizes)))
+
+
+def golden_bspline(lib):
+    axes = table_axes(50, 30, 20, 10)
+    sizes = np.array([a.size for a in axes], np.int64)
+    grids = np.concatenate(axes)
+    coeffs = bspline_coeffs(sizes)
+    rng = np.random.default_rng(7)
+    q = np.stack([rng.uniform(a[0], a[-1], 4096) for a in axes], 1)
+    edge = []
+    for a in axes:
+        edge.append([a[0], a[-1], a[0] - 0.1, a[-1] + 0.1, a[1], a[-2], 0.5 * (a[3] + a[4]), a[len(a) // 2]])
+    edge = np.array(edge).T  # 8 x 4 combos along the diagonal
+    e2 = np.array([[axes[0][i % 50], axes[1][(3 * i) % 30], axes[2][(7 * i) % 20], axes[3][(11 * i) % 10]]
+                   for i in range(56)])
+    q = np.ascontiguousarray(np.vstack([q, edge, e2]))
+    out = np.zeros(q.shape[0])
+    knots = np.zeros(int(sizes.sum()) + 16)
+    rc = lib.ref_bspline4d_eval(P(sizes), P(grids), P(coeffs), P(q), ctypes.c_int64(q.shape[0]), P(out), P(knots))
+    assert rc == 0
+    save("bspline.npz", sizes=sizes, grids=grids, seed=np.array(BSPLINE_SEED), q=q, out=out, knots=knots)
+
+
+def golden_table(lib):
+    res = {}
+    axes = table_axes(12, 6, 5, 3)
+    alpha = 2.0 * np.arcsinh(5.0 / np.sqrt(2.0))
+    for name, kind in (("explicit", 1), ("auto", 0)):
+        nm, nt, ns, nr = (a.size for a in axes)
+        out = np.zeros(nm * nt * ns * nr)
+        dims = np.zeros(2 * ns * nr, np.int64)
+        rc = lib.ref_table_sweep(P(axes[0]), ctypes.c_int64(nm), P(axes[1]), ctypes.c_int64(nt), P(axes[2]),
+                                 ctypes.c_int64(ns), P(axes[3]), ctypes.c_int64(nr), ctypes.c_double(100.0),
+                                 ctypes.c_double(0.0), ctypes.c_int32(1), ctypes.c_int32(kind),
+                                 ctypes.c_double(-3.0), ctypes.c_double(3.0), ctypes.c_int64(201),
+                                 ctypes.c_double(alpha), ctypes.c_int64(1000), P(out), P(dims))
+        assert rc == 0
+        res[f"{name}_tensor"] = out.reshape(nm, nt, ns, nr)
+        res[f"{name}_dims"] = dims.reshape(ns * nr, 2)
+    save("table.npz", m=axes[0], tau=axes[1], sigma=axes[2], r=axes[3], **res)
 
 
 if __name__ == "__main__":

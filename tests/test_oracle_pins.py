@@ -118,3 +118,28 @@ def test_oracle_thomas_projected_known_answers(oracle):
     diag0 = diag.copy()
     diag0[0] = 0.0
     assert lib.mo_thomas_projected(P(lower), P(diag0), P(upper), P(rhs), P(psi), P(x), ctypes.c_int64(n), P(ws)) == 1
+
+
+def test_oracle_bspline_vs_reference(oracle):
+    import ctypes
+    g = golden("bspline.npz")
+    sizes = g["sizes"]
+    coeffs = np.random.default_rng(int(g["seed"])).standard_normal(int(np.prod(sizes)))
+    knots = np.zeros(int(sizes.sum()) + 16)
+    off = 0
+    goff = 0
+    for d in range(4):
+        n = int(sizes[d])
+        t = np.zeros(n + 4)
+        oracle.lib().mo_clamped_knots(oracle.P(np.ascontiguousarray(g["grids"][goff:goff + n])), ctypes.c_int64(n),
+                                      oracle.P(t))
+        knots[off:off + n + 4] = t
+        off += n + 4
+        goff += n
+    assert np.array_equal(knots, g["knots"]), "clamped knots must match the reference exactly"
+    q = np.ascontiguousarray(g["q"])
+    out = np.zeros(q.shape[0])
+    assert oracle.lib().mo_bspline4d_eval(oracle.P(sizes), oracle.P(g["grids"]), oracle.P(coeffs), oracle.P(q),
+                                          ctypes.c_int64(q.shape[0]), oracle.P(out)) == 0
+    bound = 1e-12 * np.abs(g["out"]) + 1e-14 * np.abs(coeffs).max()
+    assert (np.abs(out - g["out"]) <= bound).all()

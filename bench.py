@@ -221,6 +221,75 @@ def bench_iv(pkg, eng, n):
             "graph_launches": int(eng.stats()["kernel_launches"])}
 
 
+def bench_greeks(pkg, eng, n=16384):
+    """Sensitivity workload: 16,384 American puts (config-0 distributions,
+    101 x 498 grid rule), value/delta/gamma/theta plus frozen-grid vega, rho,
+    dividend rho and dV/dK (8 bumped copies each, one device batch)."""
+    rng = np.random.default_rng(3)
+    params = pkg.pricing_array(np.full(n, 100.0), rng.uniform(80, 120, n), rng.uniform(0.1, 2.0, n),
+                               rng.uniform(0.1, 0.5, n), rng.uniform(0.0, 0.08, n), rng.uniform(0.0, 0.04, n), 1)
+    grid = pkg.grid_array(1, pkg.GRID_FIXED_N, NX, NT)
+    eng.greeks_arrays(params, grid)
+    t0 = time.perf_counter()
+    out = eng.greeks_arrays(params, grid)
+    t = time.perf_counter() - t0
+    return {"workload": f"{n} American puts, 101x498, value+delta+gamma+theta+vega+rho+dq+dK "
+                        "(central differences on the frozen grid, 9 prices per option)",
+            "value": n / t, "unit": "options with full Greeks/s (end to end)", "seconds": t,
+            "failed": int(np.count_nonzero(out["status"]))}
+
+
+TABLE_AXES = (np.linspace(np.log(0.7), np.log(1.3), 50), np.linspace(0.02, 2.0, 30),
+              np.linspace(0.05, 0.8, 20), np.linspace(0.0, 0.08, 10))
+
+
+def bench_table(pkg, eng, torch, stream, nq, fp64_peak):
+    """Price-table workload: 50 x 30 x 20 x 10 axes, 200 (sigma, r) PDE solves
+    on the explicit 201 x 1000 sinh grid (the reference falls back to
+    per-slice grids), then nq uniform random in-range 4D queries."""
+    grid = pkg.PDEGridConfig(-3.0, 3.0, 201, 1000)
+    eng.price_table_sweep(*TABLE_AXES, 100.0, 0.0, 1, grid)  # warm-up
+    t0 = time.perf_counter()
+    tensor, dims, failed = eng.price_table_sweep(*TABLE_AXES, 100.0, 0.0, 1, grid)
+    t_sweep = time.perf_counter() - t0
+    sweep = {"workload": "PriceTableBuilderND<4> sweep+extraction, 50x30x20x10 axes, 200 PDE solves, "
+                         "explicit 201x1000 grid (per-slice fallback grids)",
+             "seconds": t_sweep, "value": 200 / t_sweep, "unit": "PDE solves/s (end to end)",
+             "failed": int(failed), "max_n_time": int(dims[:, 1].max())}
+    sizes = [a.size for a in TABLE_AXES]
+    coeffs = np.random.default_rng(2025).standard_normal(int(np.prod(sizes)))
+    surf = eng.bspline4d(TABLE_AXES, coeffs)
+    rng = np.random.default_rng(7)
+    q = np.stack([rng.uniform(a[0], a[-1], nq) for a in TABLE_AXES], 1)
+    dq = torch.from_numpy(q).to("cuda")
+    dout = torch.empty(nq, dtype=torch.float64, device="cuda")
+    for _ in range(3):
+        surf.eval_device(dq.data_ptr(), nq, dout.data_ptr())
+    torch.cuda.synchronize()
+    reps = 10
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        surf.eval_device(dq.data_ptr(), nq, dout.data_ptr())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / reps
+    t0 = time.perf_counter()
+    host_out = surf.eval(q)
+    t_e2e = time.perf_counter() - t0
+    assert np.isfinite(host_out).all()
+    flops_per_query = 780.0  # algorithmic count: 4 x (span + Cox-de Boor) + 256 FMA + partial sums
+    query = {"workload": f"{nq} uniform random in-range 4D queries, 50x30x20x10 cubic B-spline (2.4 MB coeffs)",
+             "value": nq / t, "unit": "queries/s (device-resident)",
+             "e2e": {"value": nq / t_e2e, "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
+                     "d2h_bytes_per_step": int(host_out.nbytes)},
+             "hbm_gbs": 40.0 * nq / t / 1e9,
+             "fp64_frac": flops_per_query * nq / t / 1e12 / fp64_peak, "ms": 1e3 * t}
+    surf.close()
+    return sweep, query
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return 0
@@ -265,6 +334,8 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the uneven-grid side measurement")
     ap.add_argument("--no-iv", action="store_true", help="skip the batched-IV side measurement")
     ap.add_argument("--iv-quotes", type=int, default=262144)
+    ap.add_argument("--no-table", action="store_true", help="skip the table sweep / query side measurement")
+    ap.add_argument("--queries", type=int, default=10_000_000)
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
@@ -374,6 +445,11 @@ def main():
 
     if not args.no_iv and rank == 0:
         extra["iv_brent"] = bench_iv(pkg, eng, args.iv_quotes)
+    if not args.no_iv and rank == 0:
+        extra["greeks"] = bench_greeks(pkg, eng)
+    if not args.no_table and rank == 0:
+        extra["table_sweep"], extra["bspline_query"] = bench_table(pkg, eng, torch, stream,
+                                                                   args.queries, fp64_peak)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:

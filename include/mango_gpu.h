@@ -237,6 +237,28 @@ MangoStatus mango_gpu_bspline4d_eval_device(MangoGpuBSpline4D* surface, const do
 MangoStatus mango_gpu_bspline4d_knots(const MangoGpuBSpline4D* surface, double* out, uint64_t cap,
                                       uint64_t* n_out);
 
+/* Sensitivities on a frozen grid: value, delta, gamma, theta as in
+ * mango_gpu_price_american_batch plus dV/dvolatility, dV/drate,
+ * dV/ddividend_yield and dV/dstrike, each a central difference with a
+ * relative bump h_rel (0 => 1e-5) of that parameter, all bumped copies
+ * priced on the unbumped option's grid (the grid of the reference's
+ * estimate_pde_grid moves with volatility and strike, so derivatives through
+ * it are discontinuous; this is the reference's bump-and-reprice definition
+ * of these Greeks).  One device batch of 9 x n options.  No counterpart in
+ * the reference ABI. */
+typedef struct {
+  MangoGpuAmericanOut base;
+  double vega;
+  double rho;
+  double dividend_rho;
+  double dstrike;
+} MangoGpuGreeksOut;
+MangoStatus mango_gpu_price_american_greeks_batch(MangoGpuContext* ctx,
+                                                  const MangoPricingParams* params, uint64_t n,
+                                                  const MangoGpuGrid* grids, uint64_t grid_stride,
+                                                  double h_rel, MangoGpuGreeksOut* out,
+                                                  uint64_t* out_failed, MangoError* err);
+
 /* Resident batch: the same pipeline as mango_gpu_price_american_batch split
  * so that inputs can stay in device memory across runs (repeat pricing of a
  * book, IV iterations, benchmarking).  _create validates, resolves grids and
@@ -334,6 +356,7 @@ static_assert(offsetof(MangoPricingParams, option_type) == 80, "option_type off"
 static_assert(sizeof(MangoIvQuery) == 88, "MangoIvQuery size");
 static_assert(sizeof(MangoGpuGrid) == 48, "MangoGpuGrid size");
 static_assert(sizeof(MangoGpuAmericanOut) == 48, "MangoGpuAmericanOut size");
+static_assert(sizeof(MangoGpuGreeksOut) == 80, "MangoGpuGreeksOut size");
 #endif
 
 #endif /* MANGO_GPU_H */

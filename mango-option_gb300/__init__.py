@@ -52,6 +52,10 @@ IVQUERY_DTYPE = np.dtype([
 GRID_DTYPE = np.dtype([
     ("kind", "i4"), ("reserved", "i4"), ("n_space", "i8"), ("n_time", "i8"),
     ("x_min", "f8"), ("x_max", "f8"), ("alpha", "f8")])
+GREEKS_DTYPE = np.dtype([
+    ("value", "f8"), ("delta", "f8"), ("gamma", "f8"), ("theta", "f8"),
+    ("status", "i4"), ("n_space", "i4"), ("n_time", "i4"), ("reserved", "i4"),
+    ("vega", "f8"), ("rho", "f8"), ("dividend_rho", "f8"), ("dstrike", "f8")])
 IVSLOT_DTYPE = np.dtype([
     ("status", "i4"), ("_pad", "i4"), ("implied_vol", "f8"), ("iterations", "u8"),
     ("final_error", "f8"), ("vega", "f8"), ("has_vega", "i4"), ("used_rate_approximation", "i4")])
@@ -146,6 +150,10 @@ def library() -> ctypes.CDLL:
         lib.mango_gpu_bspline4d_eval_device.restype = ctypes.c_int32
         lib.mango_gpu_bspline4d_knots.argtypes = [_P, _P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
         lib.mango_gpu_bspline4d_knots.restype = ctypes.c_int32
+        lib.mango_gpu_price_american_greeks_batch.argtypes = [
+            _P, _P, ctypes.c_uint64, _P, ctypes.c_uint64, ctypes.c_double, _P,
+            ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(MangoError)]
+        lib.mango_gpu_price_american_greeks_batch.restype = ctypes.c_int32
         lib.mango_gpu_build_info.argtypes = []
         lib.mango_gpu_build_info.restype = ctypes.c_char_p
         _lib = lib
@@ -339,6 +347,26 @@ class Engine:
 
     def bspline4d(self, grids, coeffs) -> "BSpline4D":
         return BSpline4D(self, grids, coeffs)
+
+    def greeks_arrays(self, params: np.ndarray, grids: Optional[np.ndarray] = None,
+                      h_rel: float = 1e-5) -> np.ndarray:
+        """Prices, delta/gamma/theta and frozen-grid central differences for
+        vega, rho, dividend rho and dV/dK (mango_gpu_price_american_greeks_batch)."""
+        params = np.ascontiguousarray(params, dtype=PRICING_DTYPE)
+        n = params.size
+        stride = 0
+        if grids is not None:
+            grids = np.ascontiguousarray(grids, dtype=GRID_DTYPE)
+            stride = 1 if (grids.size == n and n != 1) else 0
+        out = np.zeros(n, dtype=GREEKS_DTYPE)
+        failed = ctypes.c_uint64()
+        err = MangoError()
+        st = library().mango_gpu_price_american_greeks_batch(self._ctx, _ptr(params), n, _ptr(grids), stride,
+                                                             h_rel, _ptr(out), ctypes.byref(failed),
+                                                             ctypes.byref(err))
+        if st != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+        return out
 
     def set_stream(self, stream_handle: Optional[int]) -> None:
         """Enqueue on a caller's cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""

@@ -323,10 +323,10 @@ __device__ __forceinline__ SlowOut slow_row(const TileView V, int i, bool lock, 
 //   kStage2:    rhs = alpha g + beta u^n (g = A_G), guess = g, writes a_out.
 // Lanes that are not live execute no memory operation.
 template <int K>
-__device__ __noinline__ void stage(bool live, int n, const TileView& V,
-                                   const uint8_t* __restrict__ F, bool nocache, double bcl,
-                                   double bcr, double alpha, double beta, int a_in, int a_out,
-                                   int32_t& st) {
+__device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
+                                      const uint8_t* __restrict__ F, bool nocache, double bcl,
+                                      double bcr, double alpha, double beta, int a_in, int a_out,
+                                      int32_t st) {
   const int last = V.NX - 2;  // last interior row of the tile
   const bool always_fresh = (K == kRannacher) || nocache;
 
@@ -386,7 +386,7 @@ __device__ __noinline__ void stage(bool live, int n, const TileView& V,
   }
 
   // ---- projected back substitution; last row d' = rhs = bcr
-  if (!live) return;
+  if (!live) return st;
   double xnext = dmax_ref(bcr, V.at(A_PSI, n - 1));
   const int top = n - 2;  // this lane's first row going down
   BwdRow q0b{}, q1b{}, q2b{}, q3b{};
@@ -408,6 +408,7 @@ __device__ __noinline__ void stage(bool live, int n, const TileView& V,
   // apply_boundary_conditions after the solve (pde_solver.hpp:724-726).
   V.at(a_out, 0) = bcl;
   V.at(a_out, n - 1) = bcr;
+  return st;
 }
 
 __device__ __forceinline__ double right_bc(const OptDev& o, double t) {
@@ -467,10 +468,10 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
       // half steps with coefficient dt/2 to t + dt/2 and t + dt.
       const double t_mid = 0.0 + 0.5 * dt;
       const double t_next = 0.0 + dt;
-      stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_mid),
-                        mc.alpha, mc.beta, A_U, A_G, st);
-      stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_next),
-                        mc.alpha, mc.beta, A_G, A_U, st);
+      st = stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_mid),
+                             mc.alpha, mc.beta, A_U, A_G, st);
+      st = stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_next),
+                             mc.alpha, mc.beta, A_G, A_U, st);
       step = 1;
       if (active && nt >= 1) record(1, A_U);
     }
@@ -481,10 +482,10 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
       const double t1 = t + mc.gamma * dt;
       const double tn = static_cast<double>(step + 1) * dt;
       const bool last = (step == nt - 1);
-      stage<kStage1>(live, n, V, F, nocache, o.bc_left, right_bc(o, t1), mc.alpha,
-                     mc.beta, A_U, A_G, st);
-      stage<kStage2>(live, n, V, F, nocache, o.bc_left, right_bc(o, tn), mc.alpha,
-                     mc.beta, A_G, last ? A_G : A_U, st);
+      st = stage<kStage1>(live, n, V, F, nocache, o.bc_left, right_bc(o, t1), mc.alpha,
+                          mc.beta, A_U, A_G, st);
+      st = stage<kStage2>(live, n, V, F, nocache, o.bc_left, right_bc(o, tn), mc.alpha,
+                          mc.beta, A_G, last ? A_G : A_U, st);
       if (live && sc) record(step + 1, last ? A_G : A_U);
     }
     if (active) status[k] = st;

@@ -205,20 +205,32 @@ def bench_iv(pkg, eng, n):
     S, K, T, r, q, vt, put, grids = make_iv_workload(pkg, n)
     px = eng.price_arrays(pkg.pricing_array(S, K, T, vt, r, q, put), grids)
     quotes = pkg.query_array(S, K, T, r, q, put, px["value"])
-    t0 = time.perf_counter()
-    out = eng.solve_iv_arrays(quotes, grids)
-    t = time.perf_counter() - t0
-    ok = out["status"] == 0
-    err = np.abs(out["implied_vol"][ok] - vt[ok])
-    return {"workload": f"{n} American quotes (3/4 puts), true vol~U[0.05,0.8], K/S~U[0.8,1.2], "
-                        f"T~U[0.02,2], 101x498 per-quote grids, prices from the forward solver",
-            "method": "Brent (reference iterate sequence), CUDA-graph iteration",
-            "value": n / t, "unit": "IV/s (end to end through mango_gpu_solve_iv_batch)",
-            "seconds": t, "failed": int(np.count_nonzero(~ok)),
+    res = {"workload": f"{n} American quotes (3/4 puts), true vol~U[0.05,0.8], K/S~U[0.8,1.2], "
+                       f"T~U[0.02,2], 101x498 per-quote grids, prices from the forward solver"}
+    for name, method in (("brent", pkg.IV_BRENT), ("secant", pkg.IV_SECANT)):
+        t0 = time.perf_counter()
+        out = eng.solve_iv_arrays(quotes, grids, method=method)
+        t = time.perf_counter() - t0
+        st = eng.stats()
+        ok = out["status"] == 0
+        err = np.abs(out["implied_vol"][ok] - vt[ok])
+        codes, counts = np.unique(out["status"], return_counts=True)
+        res[name] = {
+            "method": ("Brent, the reference iterate sequence" if method == pkg.IV_BRENT else
+                       "secant from the Black-Scholes IV, Brent fallback"),
+            "value": n / t, "unit": "IV/s (end to end through mango_gpu_solve_iv_batch_method)",
+            "seconds": t, "status_counts": {int(c): int(k) for c, k in zip(codes, counts)},
             "iterations_mean": float(out["iterations"][ok].mean()) if ok.any() else None,
             "max_abs_vol_error": float(err.max()) if ok.any() else None,
             "frac_within_1e-6_vol": float(np.mean(err <= 1e-6)) if ok.any() else None,
-            "graph_launches": int(eng.stats()["kernel_launches"])}
+            "quote_marches": int(st["options"]), "evaluations": int(st["tiles"]),
+            "kernel_launches": int(st["kernel_launches"]),
+            "breakdown_ms": {"host_prep": round(st["host_prep_ms"], 2), "repack": round(st["prep_ms"], 2),
+                             "evaluations_device": round(st["march_ms"], 2), "total": round(st["total_ms"], 2)}}
+    res["value"] = res["secant"]["value"]
+    res["unit"] = res["secant"]["unit"]
+    res["speedup_secant_vs_brent"] = res["secant"]["value"] / res["brent"]["value"]
+    return res
 
 
 def bench_greeks(pkg, eng, n=16384):

@@ -186,12 +186,44 @@ MangoStatus mango_gpu_price_american_batch(MangoGpuContext* ctx,
  * pricing.  config NULL or zero fields => brent_tol_abs 1e-6, max_iter 100.
  * Slot status: MANGO_OK, _VALIDATION, _ARBITRAGE (price outside
  * [intrinsic, upper bound]), _BRACKETING, _NO_CONVERGENCE, _SOLVER.  Each
- * Brent evaluation re-prices the active quotes on the device; the launch
- * sequence of one evaluation is a CUDA graph replayed per iteration. */
+ * Brent evaluation re-prices the quotes still iterating on the device; the
+ * launch sequence of one evaluation is a CUDA graph replayed per iteration,
+ * and the quotes still iterating are re-packed into full tiles as others
+ * finish.  After the call, mango_gpu_last_stats reports options = quote
+ * evaluations (marches), tiles = evaluations (graph replays), algo_flops =
+ * their work, march_ms = device time of the evaluations, prep_ms = host
+ * time of the re-packing, host_prep_ms = validation and grid generation,
+ * total_ms = the whole call. */
 MangoStatus mango_gpu_solve_iv_batch(MangoGpuContext* ctx, const MangoIvQuery* queries,
                                      uint64_t n, const MangoGpuGrid* grids, uint64_t grid_stride,
                                      const MangoIvConfig* config, MangoIvBatchSlot* out,
                                      uint64_t* out_failed, MangoError* err);
+
+/* Root finders for mango_gpu_solve_iv_batch_method. */
+enum {
+  MANGO_GPU_IV_BRENT = 0,   /* the reference's Brent, iterate for iterate */
+  MANGO_GPU_IV_SECANT = 1   /* safeguarded secant, Brent fallback (below) */
+};
+
+/* mango_gpu_solve_iv_batch with a choice of root finder.  MANGO_GPU_IV_BRENT
+ * is mango_gpu_solve_iv_batch.  MANGO_GPU_IV_SECANT starts every quote at the
+ * Black-Scholes implied volatility of its price, takes one Newton step along
+ * the Black-Scholes vega, then secant steps kept inside the bracket seen so
+ * far (bisection otherwise); it stops on the same test as Brent (|V - P| <
+ * brent_tol_abs, or a bracket narrower than brent_tol_abs).  A quote not
+ * settled within 10 evaluations, or whose root lies outside the Brent
+ * bracket, is solved again from scratch by Brent, so failure statuses are
+ * Brent's, with one exception: where V - P has no sign change over Brent's
+ * bracket [0.01, upper] (Brent: MANGO_ERR_BRACKETING) but the secant reaches
+ * |V - P| < brent_tol_abs inside it, the quote is reported settled at that
+ * point.  Converged roots of the two methods differ by at most about
+ * 2 brent_tol_abs / vega.  iterations = evaluations for secant-settled
+ * quotes, Brent's count otherwise.  No counterpart in the reference ABI. */
+MangoStatus mango_gpu_solve_iv_batch_method(MangoGpuContext* ctx, const MangoIvQuery* queries,
+                                            uint64_t n, const MangoGpuGrid* grids,
+                                            uint64_t grid_stride, const MangoIvConfig* config,
+                                            int32_t method, MangoIvBatchSlot* out,
+                                            uint64_t* out_failed, MangoError* err);
 
 /* Price-table PDE sweep: PriceTableBuilderND<4>::make_batch + solve_batch +
  * extract_tensor (src/option/table/bspline/bspline_builder.cpp:198-480).  One

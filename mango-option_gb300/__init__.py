@@ -38,6 +38,10 @@ GRID_SINH = 2
 GRID_UNIFORM = 3
 GRID_FIXED_N_AT_VOL = 4
 
+# Root finders of mango_gpu_solve_iv_batch_method.
+IV_BRENT = 0
+IV_SECANT = 1
+
 # C layouts (include/mango_gpu.h); sizes are asserted there and in tests.
 PRICING_DTYPE = np.dtype([
     ("spot", "f8"), ("strike", "f8"), ("maturity", "f8"), ("dividend_yield", "f8"),
@@ -135,6 +139,11 @@ def library() -> ctypes.CDLL:
                                                  ctypes.POINTER(MangoIvConfig), _P,
                                                  ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(MangoError)]
         lib.mango_gpu_solve_iv_batch.restype = ctypes.c_int32
+        lib.mango_gpu_solve_iv_batch_method.argtypes = [_P, _P, ctypes.c_uint64, _P, ctypes.c_uint64,
+                                                        ctypes.POINTER(MangoIvConfig), ctypes.c_int32, _P,
+                                                        ctypes.POINTER(ctypes.c_uint64),
+                                                        ctypes.POINTER(MangoError)]
+        lib.mango_gpu_solve_iv_batch_method.restype = ctypes.c_int32
         lib.mango_gpu_price_table_sweep.argtypes = [
             _P, _P, ctypes.c_uint64, _P, ctypes.c_uint64, _P, ctypes.c_uint64, _P, ctypes.c_uint64,
             ctypes.c_double, ctypes.c_double, ctypes.c_int32, _P, _P, _P, ctypes.POINTER(ctypes.c_uint64),
@@ -306,10 +315,11 @@ class Engine:
         return out
 
     def solve_iv_arrays(self, queries: np.ndarray, grids: np.ndarray, tol: float = 0.0,
-                        max_iter: int = 0) -> np.ndarray:
-        """Batched FDM implied volatility (mango_gpu_solve_iv_batch).  queries:
-        IVQUERY_DTYPE; grids: GRID_DTYPE (length 1 or len(queries)), each a
-        volatility-independent grid.  Returns IVSLOT_DTYPE records."""
+                        max_iter: int = 0, method: int = 0) -> np.ndarray:
+        """Batched FDM implied volatility (mango_gpu_solve_iv_batch_method).
+        queries: IVQUERY_DTYPE; grids: GRID_DTYPE (length 1 or len(queries)),
+        each a volatility-independent grid; method IV_BRENT (the reference's
+        Brent) or IV_SECANT.  Returns IVSLOT_DTYPE records."""
         queries = np.ascontiguousarray(queries, dtype=IVQUERY_DTYPE)
         grids = np.ascontiguousarray(grids, dtype=GRID_DTYPE)
         n = queries.size
@@ -318,9 +328,9 @@ class Engine:
         cfg = MangoIvConfig(tol, max_iter)
         failed = ctypes.c_uint64()
         err = MangoError()
-        st = library().mango_gpu_solve_iv_batch(self._ctx, _ptr(queries), n, _ptr(grids), stride,
-                                                ctypes.byref(cfg), _ptr(out), ctypes.byref(failed),
-                                                ctypes.byref(err))
+        st = library().mango_gpu_solve_iv_batch_method(self._ctx, _ptr(queries), n, _ptr(grids), stride,
+                                                       ctypes.byref(cfg), int(method), _ptr(out),
+                                                       ctypes.byref(failed), ctypes.byref(err))
         if st != MANGO_OK:
             raise EngineError(f"mango_gpu_solve_iv_batch: {err.message.decode(errors='replace')}")
         return out
@@ -646,6 +656,7 @@ class IVSolverConfig:
     grid_vol: float = 0.0
     brent_tol_abs: float = 1e-6
     max_iter: int = 100
+    method: int = 0  # IV_BRENT (the reference's root finder) or IV_SECANT
 
 
 class IVSolver:
@@ -672,7 +683,8 @@ class IVSolver:
                           [q.rate for q in qs], [q.dividend_yield for q in qs],
                           [int(q.option_type == OptionType.PUT) for q in qs], [q.market_price for q in qs])
         eng = self._engine or default_engine()
-        out = eng.solve_iv_arrays(arr, self._grid(), self.config.brent_tol_abs, self.config.max_iter)
+        out = eng.solve_iv_arrays(arr, self._grid(), self.config.brent_tol_abs, self.config.max_iter,
+                                  self.config.method)
         res = []
         for row in out:
             if row["status"] == MANGO_OK:

@@ -3,16 +3,47 @@
 // Restates IVSolver::solve / solve_brent (src/option/iv_solver.cpp:133-242)
 // with brent_find_root (src/math/root_finding.hpp:145-302) as a per-quote
 // state machine on the device.  Every quote keeps its own fixed grid; each
-// Brent evaluation re-prices all still-active quotes at their current trial
-// volatility with the same setup / march / value kernels as batched pricing,
-// then one thread per quote advances Brent by exactly one function value.
-// The per-iteration launch sequence is captured once as a CUDA graph and
-// replayed until every quote has converged or failed.
+// evaluation re-prices the quotes still iterating at their trial
+// volatilities with the same setup / march / value kernels as batched
+// pricing, then one thread per quote consumes the objective values and
+// proposes the next trial points.
+//
+// Two root finders share that pipeline:
+//   MANGO_GPU_IV_BRENT   the reference's Brent, iterate for iterate (one
+//                        trial point per quote per evaluation);
+//   MANGO_GPU_IV_SECANT  starts at the Black-Scholes implied volatility of
+//                        the quote, steps along the Black-Scholes vega, then
+//                        by secant, inside the bracket seen so far.  While
+//                        many quotes are iterating each gets one trial point
+//                        per evaluation; once few are left, each gets k
+//                        points (k = one wave of lanes / quotes left, at
+//                        most 32): the secant point, points around it, a
+//                        k-section of the bracket and, while a side of the
+//                        bracket is unverified, Brent's bracket end there.
+//                        A march of a lone warp costs as long as a full wave
+//                        (the FP64 pipe is paced per warp instruction), so
+//                        the extra points are free and cut the number of
+//                        evaluations the last quotes need.  Once a sign
+//                        change of V - P is seen the search keeps a
+//                        sign-change bracket, so it converges even where V
+//                        is not monotone in the volatility.  Quotes that go
+//                        non-finite, or find no sign change within
+//                        kFastMaxEvals evaluations, are re-solved by Brent.
+// Both stop on the reference's test |V(sigma) - P| < tol (or a bracket
+// narrower than tol).
+//
+// Each evaluation packs the trial points still to price into tiles of 32 in
+// sorted order (one gather of grids and parameters on the device), so
+// finished quotes never occupy warps.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -20,28 +51,60 @@
 
 namespace mgpu {
 
+// Result codes of the state machines.
+constexpr int32_t kIvOk = 0, kIvBracket = 1, kIvMaxIter = 2, kIvNumerical = 3;
+// Evaluations of the fast root finder before a quote without a sign change
+// is handed to Brent, and the cap for a quote inside a sign-change bracket
+// (which at least halves every second evaluation).
+constexpr int kFastMaxEvals = 12;
+constexpr int kFastMaxBracketEvals = 60;
+// Trial points per quote and evaluation, at most.
+constexpr int kMaxPts = 32;
+// IVSolver::solve_brent lower bracket (iv_solver.cpp:150).
+constexpr double kVolLower = 0.01;
+
+// ------------------------------------------------------------- Brent --
+
 // Brent state of one quote (root_finding.hpp:145-302 variables).
 struct BrentDev {
   double a, b, c, d, fa, fb, fc, s;
   double root, ferr;
-  int32_t iter, mflag, phase, code;  // phase: 0 eval a, 1 eval b, 2 eval s, 3 done
+  int32_t iter, mflag, phase, code;  // phase: 0 eval a, 1 eval b, 2 eval s
 };
 
-// Result codes of the state machine.
-constexpr int32_t kIvOk = 0, kIvBracket = 1, kIvMaxIter = 2, kIvNumerical = 3;
+// Fast root-finder state of one quote.  Until a sign change of f has been
+// seen, [lo, hi] steers the search assuming f rises with the volatility;
+// from then on [bl, br] always holds a sign change (f(bl) f(br) < 0), so
+// the search converges whether or not f is monotone.
+struct FastDev {
+  double lo, hi;   // steering bounds: f(lo) < 0 (seen bit 0), f(hi) > 0 (seen bit 1)
+  double flo, fhi;
+  double bl, br;   // sign-change bracket, when has_br
+  double fl, fr;
+  double xa, fa;   // best point so far (smallest |f|), f signed
+  double xb, fb;   // second best point
+  double e0, e1;   // f at Brent's bracket ends 0.01 and upper, when evaluated
+  double guess;    // Black-Scholes implied volatility of the price
+  double width;    // bracket width before the last evaluation
+  int32_t iter;    // evaluations consumed
+  int32_t seen;
+  int32_t ends;    // bit 0: f(0.01) evaluated; bit 1: f(upper) evaluated
+  int32_t has_br;
+};
 
-__global__ void brent_init_kernel(int m, const double* __restrict__ upper, BrentDev* __restrict__ S,
-                                  double* __restrict__ sigma, int32_t* __restrict__ active) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= m) return;
-  BrentDev s{};
-  s.a = 0.01;  // IVSolver::solve_brent vol_lower (iv_solver.cpp:150)
-  s.b = upper[k];
-  s.phase = 0;
-  S[k] = s;
-  sigma[k] = s.a;
-  active[k] = 1;
-}
+// Per-quote root-finder state.
+struct IvDev {
+  BrentDev br;
+  FastDev fs;
+  int32_t mode;  // 0 fast, 1 Brent, 2 finished
+  int32_t pad;
+};
+
+// Final result of one quote.
+struct IvOut {
+  double root, ferr;
+  int32_t iter, code;
+};
 
 namespace {
 
@@ -50,6 +113,9 @@ __device__ __forceinline__ void swap_d(double& x, double& y) {
   x = y;
   y = t;
 }
+
+__device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000ll); }
+__device__ __forceinline__ double pinf() { return __longlong_as_double(0x7ff0000000000000ll); }
 
 // Convergence test and next trial point at the top of a Brent iteration;
 // returns false when the quote is finished.
@@ -91,105 +157,400 @@ __device__ bool brent_propose(BrentDev& s, double tol, int max_iter) {
   return true;
 }
 
-}  // namespace
+__device__ void brent_start(BrentDev& s, double upper) {
+  s = BrentDev{};
+  s.a = kVolLower;
+  s.b = upper;
+  s.phase = 0;
+  s.code = kIvNumerical;
+}
 
-// Consume the objective value at the last trial point and advance Brent.
-// f = value_at(spot) - market price (iv_solver.cpp:48-119); a failed march
-// gives NaN, as the reference's objective does.
-__global__ void brent_step_kernel(int m, BrentDev* __restrict__ S, const double* __restrict__ out4,
-                                  const int32_t* __restrict__ mstatus,
-                                  const double* __restrict__ price, double* __restrict__ sigma,
-                                  int32_t* __restrict__ active, double tol, int max_iter,
-                                  int* __restrict__ n_active) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= m) return;
-  BrentDev s = S[k];
-  if (s.phase == 3) {
-    active[k] = 0;
-    return;
-  }
-  const double f = mstatus[k] == kStatusOk ? out4[4 * static_cast<size_t>(k)] - price[k]
-                                           : __longlong_as_double(0x7ff8000000000000ll);
-  bool go = true;
-  double next = 0.0;
+// Consume the objective value f at the last trial point and advance Brent
+// by one function value; returns true with the next trial point in *next,
+// false when the quote is finished (code, root, ferr, iter set).
+__device__ bool brent_consume(BrentDev& s, double f, double tol, int max_iter, double* next) {
   if (s.phase == 0) {
     s.fa = f;
     s.phase = 1;
-    next = s.b;
-  } else if (s.phase == 1) {
+    *next = s.b;
+    return true;
+  }
+  if (s.phase == 1) {
     s.fb = f;
+    s.iter = 0;
     if (!isfinite(s.fa) || !isfinite(s.fb)) {
       s.code = kIvNumerical;
-      s.ferr = __longlong_as_double(0x7ff8000000000000ll);
-      s.iter = 0;
-      go = false;
-    } else if (s.fa * s.fb > 0.0) {
+      s.ferr = qnan();
+      return false;
+    }
+    if (s.fa * s.fb > 0.0) {
       s.code = kIvBracket;
       s.ferr = fmin(fabs(s.fa), fabs(s.fb));
-      s.iter = 0;
-      go = false;
-    } else if (fabs(s.fa) < tol) {
+      return false;
+    }
+    if (fabs(s.fa) < tol) {
       s.code = kIvOk;
       s.root = s.a;
       s.ferr = fabs(s.fa);
-      s.iter = 0;
-      go = false;
-    } else if (fabs(s.fb) < tol) {
+      return false;
+    }
+    if (fabs(s.fb) < tol) {
       s.code = kIvOk;
       s.root = s.b;
       s.ferr = fabs(s.fb);
-      s.iter = 0;
-      go = false;
-    } else {
-      if (fabs(s.fa) < fabs(s.fb)) {
-        swap_d(s.a, s.b);
-        swap_d(s.fa, s.fb);
-      }
-      s.c = s.a;
-      s.fc = s.fa;
-      s.mflag = 1;
-      s.d = 0.0;
-      s.iter = 0;
-      go = brent_propose(s, tol, max_iter);
-      next = s.s;
-      s.phase = 2;
+      return false;
     }
+    if (fabs(s.fa) < fabs(s.fb)) {
+      swap_d(s.a, s.b);
+      swap_d(s.fa, s.fb);
+    }
+    s.c = s.a;
+    s.fc = s.fa;
+    s.mflag = 1;
+    s.d = 0.0;
+    s.phase = 2;
+    const bool go = brent_propose(s, tol, max_iter);
+    *next = s.s;
+    return go;
+  }
+  if (!isfinite(f)) {
+    s.code = kIvNumerical;
+    s.root = s.s;
+    s.ferr = qnan();
+    s.iter += 1;
+    return false;
+  }
+  s.d = s.c;
+  s.c = s.b;
+  s.fc = s.fb;
+  if (s.fa * f < 0.0) {
+    s.b = s.s;
+    s.fb = f;
   } else {
-    const double fs = f;
-    if (!isfinite(fs)) {
-      s.code = kIvNumerical;
-      s.root = s.s;
-      s.ferr = __longlong_as_double(0x7ff8000000000000ll);
-      s.iter += 1;
-      go = false;
-    } else {
-      s.d = s.c;
-      s.c = s.b;
-      s.fc = s.fb;
-      if (s.fa * fs < 0.0) {
-        s.b = s.s;
-        s.fb = fs;
-      } else {
-        s.a = s.s;
-        s.fa = fs;
-      }
-      if (fabs(s.fa) < fabs(s.fb)) {
-        swap_d(s.a, s.b);
-        swap_d(s.fa, s.fb);
-      }
-      s.iter += 1;
-      go = brent_propose(s, tol, max_iter);
-      next = s.s;
+    s.a = s.s;
+    s.fa = f;
+  }
+  if (fabs(s.fa) < fabs(s.fb)) {
+    swap_d(s.a, s.b);
+    swap_d(s.fa, s.fb);
+  }
+  s.iter += 1;
+  const bool go = brent_propose(s, tol, max_iter);
+  *next = s.s;
+  return go;
+}
+
+// ------------------------------------------------------ fast finder --
+
+// Black-Scholes price with continuous dividend yield (closed form).
+__device__ double bs_price(bool put, double S, double K, double T, double r, double q,
+                           double sig) {
+  const double st = sig * sqrt(T);
+  const double d1 = (log(S / K) + (r - q + 0.5 * sig * sig) * T) / st;
+  const double d2 = d1 - st;
+  const double dfq = exp(-q * T), dfr = exp(-r * T);
+  const double h = 0.7071067811865476;  // 1/sqrt(2): N(z) = erfc(-z/sqrt(2))/2
+  if (put) return K * dfr * 0.5 * erfc(d2 * h) - S * dfq * 0.5 * erfc(d1 * h);
+  return S * dfq * 0.5 * erfc(-d1 * h) - K * dfr * 0.5 * erfc(-d2 * h);
+}
+
+// Black-Scholes vega (same for puts and calls).
+__device__ double bs_vega(double S, double K, double T, double r, double q, double sig) {
+  const double st = sqrt(T);
+  const double d1 = (log(S / K) + (r - q + 0.5 * sig * sig) * T) / (sig * st);
+  return S * exp(-q * T) * st * exp(-0.5 * d1 * d1) * 0.3989422804014327;  // 1/sqrt(2 pi)
+}
+
+// European implied volatility of the quote's price inside [lo, hi] by
+// bisection-safeguarded Newton; only a starting point (the American price
+// is what gets matched).  A price outside the European range on [lo, hi]
+// starts at the nearer end.
+__device__ double european_iv_guess(bool put, double S, double K, double T, double r, double q,
+                                    double P, double lo, double hi) {
+  double a = lo, b = hi;
+  if (!(bs_price(put, S, K, T, r, q, a) - P < 0.0)) return lo;
+  if (!(bs_price(put, S, K, T, r, q, b) - P > 0.0)) return hi;
+  double x = fmin(fmax(0.3, a), b);
+  for (int it = 0; it < 40; ++it) {
+    const double f = bs_price(put, S, K, T, r, q, x) - P;
+    if (fabs(f) < 1e-12 * fmax(P, 1.0)) break;
+    if (f > 0.0) b = x; else a = x;
+    const double v = bs_vega(S, K, T, r, q, x);
+    double xn = v > 0.0 ? x - f / v : 0.5 * (a + b);
+    if (!(xn > a && xn < b)) xn = 0.5 * (a + b);
+    const bool small = fabs(xn - x) < 1e-12;
+    x = xn;
+    if (small) break;
+  }
+  return x;
+}
+
+constexpr int kFastGo = 0, kFastSettled = 1, kFastBracket = 2, kFastHandOver = 3;
+
+// Consume the n objective values f[j] at sig[j].  Settled when a point has
+// |f| < tol (the Brent stopping test, root_finding.hpp:210-218) or the
+// sign-change bracket is narrower than tol.  With f evaluated at both of
+// Brent's bracket ends and no sign change anywhere, the quote fails as
+// Brent's does (root_finding.hpp:176-185).
+__device__ int fast_consume(FastDev& s, const double* sig, const double* f, int n, double upper,
+                            double tol) {
+  s.iter += 1;
+  s.width = s.has_br ? s.br - s.bl : s.hi - s.lo;
+  for (int j = 0; j < n; ++j)
+    if (!isfinite(f[j])) return kFastHandOver;
+  for (int j = 0; j < n; ++j) {
+    const double x = sig[j], fj = f[j];
+    if (fabs(fj) < fabs(s.fa)) {
+      s.xb = s.xa;
+      s.fb = s.fa;
+      s.xa = x;
+      s.fa = fj;
+    } else if (fabs(fj) < fabs(s.fb) && x != s.xa) {
+      s.xb = x;
+      s.fb = fj;
+    }
+    if (x == kVolLower) {
+      s.ends |= 1;
+      s.e0 = fj;
+    }
+    if (x == upper) {
+      s.ends |= 2;
+      s.e1 = fj;
+    }
+    if (fj < 0.0 && (!(s.seen & 1) || x > s.lo)) {
+      s.lo = x;
+      s.flo = fj;
+      s.seen |= 1;
+    } else if (fj > 0.0 && (!(s.seen & 2) || x < s.hi)) {
+      s.hi = x;
+      s.fhi = fj;
+      s.seen |= 2;
     }
   }
-  if (!go) {
-    s.phase = 3;
-    active[k] = 0;
-  } else {
-    sigma[k] = next;
-    atomicAdd(n_active, 1);
+  if (fabs(s.fa) < tol) return kFastSettled;
+  if (!s.has_br && s.seen == 3) {
+    s.has_br = 1;
+    if (s.lo < s.hi) {
+      s.bl = s.lo, s.fl = s.flo, s.br = s.hi, s.fr = s.fhi;
+    } else {
+      s.bl = s.hi, s.fl = s.fhi, s.br = s.lo, s.fr = s.flo;
+    }
   }
-  S[k] = s;
+  if (s.has_br) {
+    // Narrow to the first sign change along bl < points inside < br.
+    double px[kMaxPts], pf[kMaxPts];
+    int m = 0;
+    for (int j = 0; j < n; ++j)
+      if (sig[j] > s.bl && sig[j] < s.br) {
+        int i = m++;
+        while (i > 0 && px[i - 1] > sig[j]) {
+          px[i] = px[i - 1];
+          pf[i] = pf[i - 1];
+          --i;
+        }
+        px[i] = sig[j];
+        pf[i] = f[j];
+      }
+    double xl = s.bl, fl = s.fl;
+    for (int i = 0; i < m; ++i) {
+      if ((fl < 0.0) != (pf[i] < 0.0)) {
+        s.br = px[i];
+        s.fr = pf[i];
+        break;
+      }
+      xl = px[i];
+      fl = pf[i];
+    }
+    s.bl = xl;
+    s.fl = fl;
+    if (s.br - s.bl < tol) return kFastSettled;
+  } else if (s.ends == 3) {
+    return kFastBracket;
+  }
+  if (s.iter >= (s.has_br ? kFastMaxBracketEvals : kFastMaxEvals)) return kFastHandOver;
+  return kFastGo;
+}
+
+// Up to k next trial points into pts (distinct); returns how many.
+__device__ int fast_propose(const FastDev& s, const OptDev& o, double T, double upper, int k,
+                            double* pts) {
+  int n = 0;
+  auto add = [&](double x) {
+    if (n >= k || !(x >= kVolLower && x <= upper)) return;
+    for (int j = 0; j < n; ++j)
+      if (fabs(pts[j] - x) <= 1e-14 * x) return;
+    pts[n++] = x;
+  };
+  const double lo = s.has_br ? s.bl : s.lo, hi = s.has_br ? s.br : s.hi;
+  auto inside = [&](double x) { return x > lo && x < hi; };
+  // centre: the secant through the two best points, a Black-Scholes-vega
+  // Newton step from a lone point, or the starting guess; inside a
+  // sign-change bracket the false-position point when the secant leaves
+  // it, and the midpoint when the last evaluation did not halve it
+  double c, w;
+  if (s.iter == 0) {
+    c = s.guess;
+    w = 0.1 * c;
+  } else {
+    if (isfinite(s.fb) && s.fb != s.fa) {
+      c = s.xa - s.fa * (s.xa - s.xb) / (s.fa - s.fb);
+    } else {
+      c = s.xa - s.fa / bs_vega(o.spot, o.strike, T, o.r, o.q, s.xa);
+    }
+    if (s.has_br) {
+      if (!inside(c)) c = s.bl - s.fl * (s.br - s.bl) / (s.fr - s.fl);
+      if (!inside(c) || (k == 1 && s.br - s.bl > 0.5 * s.width)) c = 0.5 * (s.bl + s.br);
+    } else if (!inside(c)) {
+      c = 0.5 * (lo + hi);
+    }
+    w = 2.0 * fabs(c - s.xa);
+  }
+  add(c);
+  if (k >= 3 && !s.has_br) {
+    if (!(s.ends & 1)) add(kVolLower);
+    if (!(s.ends & 2)) add(upper);
+  }
+  const int rest = k - n;
+  const int near = rest / 2, spread = rest - near;
+  for (int j = 1; j <= near; ++j) {
+    const double off = w * static_cast<double>((j + 1) / 2) / static_cast<double>((near + 1) / 2);
+    const double x = (j & 1) ? c + off : c - off;
+    if (inside(x)) add(x);
+  }
+  for (int j = 1; j <= spread; ++j) {
+    const double x = lo + (hi - lo) * static_cast<double>(j) / static_cast<double>(spread + 1);
+    if (inside(x)) add(x);
+  }
+  return n;
+}
+
+// Objective at working slot k: V(sigma) - P (iv_solver.cpp:48-119); a failed
+// march gives NaN, as the reference's objective does.
+__device__ __forceinline__ double objective(const double* out4, const int32_t* mstatus, int k,
+                                            double price) {
+  return mstatus[k] == kStatusOk ? out4[4 * static_cast<size_t>(k)] - price : qnan();
+}
+
+}  // namespace
+
+// First trial points of every sorted quote: the Black-Scholes implied vol
+// and up to k - 1 more (fast), or the lower bracket 0.01 (Brent).
+__global__ void iv_init_kernel(int m, int32_t method, int k, const OptDev* __restrict__ opts,
+                               const double* __restrict__ mat, const double* __restrict__ price,
+                               const double* __restrict__ upper, IvDev* __restrict__ S,
+                               IvOut* __restrict__ R, double* __restrict__ next_sig,
+                               int32_t* __restrict__ npts) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= m) return;
+  R[q] = IvOut{qnan(), qnan(), 0, kIvNumerical};
+  IvDev st{};
+  double* pts = next_sig + static_cast<size_t>(q) * kMaxPts;
+  if (method == MANGO_GPU_IV_SECANT) {
+    const OptDev o = opts[q];
+    FastDev& s = st.fs;
+    s.lo = kVolLower;
+    s.hi = upper[q];
+    s.guess = european_iv_guess(o.is_put != 0, o.spot, o.strike, mat[q], o.r, o.q, price[q], s.lo,
+                                s.hi);
+    s.xa = s.xb = qnan();
+    s.fa = s.fb = pinf();
+    s.e0 = s.e1 = qnan();
+    st.mode = 0;
+    npts[q] = fast_propose(s, o, mat[q], s.hi, k, pts);
+  } else {
+    brent_start(st.br, upper[q]);
+    st.mode = 1;
+    pts[0] = st.br.a;
+    npts[q] = 1;
+  }
+  S[q] = st;
+}
+
+// Consume the objective values of quote qlist[i] (slots qbase[i] ..
+// qbase[i] + npts - 1) and propose its next trial points (k at most for
+// the fast finder); npts[q] = 0 once the quote is finished.
+__global__ void iv_step_kernel(int nq, const int32_t* __restrict__ qlist,
+                               const int32_t* __restrict__ qbase, int k, IvDev* __restrict__ S,
+                               IvOut* __restrict__ R, const OptDev* __restrict__ opts,
+                               const double* __restrict__ mat, const double* __restrict__ upper,
+                               const double* __restrict__ out4, const int32_t* __restrict__ mstatus,
+                               const double* __restrict__ sigma_w, const double* __restrict__ price,
+                               double* __restrict__ next_sig, int32_t* __restrict__ npts, double tol,
+                               int max_iter, int trace) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  const int q = qlist[i];
+  const int base = qbase[i];
+  const int n = min(npts[q], kMaxPts);
+  IvDev st = S[q];
+  double* pts = next_sig + static_cast<size_t>(q) * kMaxPts;
+  const double P = price[q];
+  int next_n = 0;
+  if (st.mode == 0) {
+    double sg[kMaxPts], fv[kMaxPts];
+    for (int j = 0; j < n; ++j) {
+      sg[j] = sigma_w[base + j];
+      fv[j] = objective(out4, mstatus, base + j, P);
+    }
+    const int r = fast_consume(st.fs, sg, fv, n, upper[q], tol);
+    if (r == kFastGo) {
+      next_n = fast_propose(st.fs, opts[q], mat[q], upper[q], k, pts);
+    } else if (r == kFastSettled) {
+      R[q] = IvOut{st.fs.xa, fabs(st.fs.fa), st.fs.iter, kIvOk};
+      st.mode = 2;
+    } else if (r == kFastBracket) {
+      R[q] = IvOut{qnan(), fmin(fabs(st.fs.e0), fabs(st.fs.e1)), 0, kIvBracket};
+      st.mode = 2;
+    } else {
+      if (trace)
+        printf("iv hand-over q=%d iter=%d lo=%.17g hi=%.17g seen=%d ends=%d bracket=%d [%.17g, %.17g] "
+               "xa=%.17g fa=%.6e xb=%.17g fb=%.6e guess=%.6g n=%d\n",
+               q, st.fs.iter, st.fs.lo, st.fs.hi, st.fs.seen, st.fs.ends, st.fs.has_br, st.fs.bl,
+               st.fs.br, st.fs.xa, st.fs.fa, st.fs.xb, st.fs.fb, st.fs.guess, n);
+      brent_start(st.br, upper[q]);
+      st.mode = 1;
+      pts[0] = st.br.a;
+      next_n = 1;
+    }
+  } else if (st.mode == 1) {
+    double next = 0.0;
+    if (brent_consume(st.br, objective(out4, mstatus, base, P), tol, max_iter, &next)) {
+      pts[0] = next;
+      next_n = 1;
+    } else {
+      R[q] = IvOut{st.br.root, st.br.ferr, st.br.iter, st.br.code};
+      st.mode = 2;
+    }
+  }
+  npts[q] = next_n;
+  S[q] = st;
+}
+
+// Gather the working set from the batch (sorted order, tile t holding
+// sorted quotes [32 t, 32 t + 32)): slot k prices quote map[k] at its trial
+// point pt[k].
+__global__ void iv_gather_kernel(int mw, const int32_t* __restrict__ map,
+                                 const int32_t* __restrict__ pt,
+                                 const TileDev* __restrict__ src_tiles,
+                                 const OptDev* __restrict__ src_opts,
+                                 const double* __restrict__ src_xs,
+                                 const TileDev* __restrict__ dst_tiles,
+                                 OptDev* __restrict__ dst_opts, double* __restrict__ dst_xs,
+                                 const double* __restrict__ next_sig,
+                                 double* __restrict__ sigma_w, int32_t* __restrict__ active_w) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= mw) return;
+  const int q = map[k];
+  const OptDev o = src_opts[q];
+  dst_opts[k] = o;
+  const TileDev ts = src_tiles[q / kTile];
+  const TileDev td = dst_tiles[k / kTile];
+  const double* src = src_xs + ts.xoff + (q % kTile);
+  double* dst = dst_xs + td.xoff + (k % kTile);
+  for (int i = 0; i < td.nx; ++i)
+    dst[static_cast<size_t>(i) * kTile] = src[static_cast<size_t>(min(i, o.n - 1)) * kTile];
+  sigma_w[k] = next_sig[static_cast<size_t>(q) * kMaxPts + pt[k]];
+  active_w[k] = 1;
 }
 
 namespace {
@@ -222,16 +583,110 @@ int32_t validate_query(const MangoIvQuery& q, std::string* msg) {
   return MANGO_OK;
 }
 
-}  // namespace
-}  // namespace mgpu
+using Clock = std::chrono::steady_clock;
 
-using namespace mgpu;
+double ms_since(Clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+}
 
-extern "C" MangoStatus mango_gpu_solve_iv_batch(MangoGpuContext* ctx, const MangoIvQuery* queries,
-                                                uint64_t n, const MangoGpuGrid* grids,
-                                                uint64_t grid_stride, const MangoIvConfig* config,
-                                                MangoIvBatchSlot* out, uint64_t* out_failed,
-                                                MangoError* err) {
+// The trial points of one evaluation packed into tiles of 32 (sorted
+// order), with the device buffers their marches use.
+struct WorkSet {
+  MangoGpuBatch* b = nullptr;
+  cudaStream_t st = nullptr;
+  int64_t mw = 0;  // slots
+  int32_t ntiles = 0;
+  int64_t nq = 0;  // quotes
+  std::vector<int32_t> map_h, pt_h, qlist_h, qbase_h;
+  std::vector<TileDev> tiles_h;
+  DevBuf d_tiles, d_opts, d_xs, d_map, d_pt, d_qlist, d_qbase, d_sigma, d_active, d_pool, d_flags,
+      d_mode, d_status, d_out4;
+
+  ~WorkSet() {
+    for (DevBuf* d : {&d_tiles, &d_opts, &d_xs, &d_map, &d_pt, &d_qlist, &d_qbase, &d_sigma,
+                      &d_active, &d_pool, &d_flags, &d_mode, &d_status, &d_out4})
+      d->release();
+  }
+
+  // Slots for the quotes in `active` (ascending) with npts[q] > 0.  The
+  // host arrays must stay untouched until the stream has passed the copies.
+  void pack(const std::vector<int32_t>& active, const int32_t* npts, const double* next_sig) {
+    map_h.clear();
+    pt_h.clear();
+    qlist_h.clear();
+    qbase_h.clear();
+    for (int32_t q : active) {
+      const int c = std::min(npts[q], kMaxPts);
+      if (c <= 0) continue;
+      qlist_h.push_back(q);
+      qbase_h.push_back(static_cast<int32_t>(map_h.size()));
+      for (int j = 0; j < c; ++j) {
+        map_h.push_back(q);
+        pt_h.push_back(j);
+      }
+    }
+    mw = static_cast<int64_t>(map_h.size());
+    nq = static_cast<int64_t>(qlist_h.size());
+    if (mw == 0) return;
+    if (mw > (1LL << 31) - 1) throw CudaError("IV working set above 2^31 points");
+    ntiles = static_cast<int32_t>((mw + kTile - 1) / kTile);
+    tiles_h.assign(static_cast<size_t>(ntiles), TileDev{});
+    const OptDev* ho = b->h_opts.as<OptDev>();
+    int64_t off = 0, xoff = 0, foff = 0;
+    for (int32_t t = 0; t < ntiles; ++t) {
+      TileDev& td = tiles_h[t];
+      td.first = t * kTile;
+      td.count = static_cast<int32_t>(std::min<int64_t>(kTile, mw - td.first));
+      int32_t nx = 0, nt = 0;
+      for (int l = 0; l < td.count; ++l) {
+        const OptDev& o = ho[map_h[td.first + l]];
+        nx = std::max(nx, o.n);
+        nt = std::max(nt, o.nt);
+      }
+      td.nx = nx;
+      td.nt = nt;
+      td.off = off;
+      td.xoff = xoff;
+      td.foff = foff;
+      off += static_cast<int64_t>(A_COUNT) * nx * kTile;
+      xoff += static_cast<int64_t>(nx) * kTile;
+      foff += static_cast<int64_t>(nx) * kTile;
+    }
+    check(cudaMemcpyAsync(d_tiles.get(sizeof(TileDev) * ntiles), tiles_h.data(),
+                          sizeof(TileDev) * ntiles, cudaMemcpyHostToDevice, st),
+          "H2D working tiles");
+    check(cudaMemcpyAsync(d_map.get(sizeof(int32_t) * mw), map_h.data(), sizeof(int32_t) * mw,
+                          cudaMemcpyHostToDevice, st),
+          "H2D working map");
+    check(cudaMemcpyAsync(d_pt.get(sizeof(int32_t) * mw), pt_h.data(), sizeof(int32_t) * mw,
+                          cudaMemcpyHostToDevice, st),
+          "H2D working points");
+    check(cudaMemcpyAsync(d_qlist.get(sizeof(int32_t) * nq), qlist_h.data(), sizeof(int32_t) * nq,
+                          cudaMemcpyHostToDevice, st),
+          "H2D quote list");
+    check(cudaMemcpyAsync(d_qbase.get(sizeof(int32_t) * nq), qbase_h.data(), sizeof(int32_t) * nq,
+                          cudaMemcpyHostToDevice, st),
+          "H2D quote slots");
+    d_opts.get(sizeof(OptDev) * mw);
+    d_xs.get(sizeof(double) * xoff);
+    d_sigma.get(sizeof(double) * mw);
+    d_active.get(sizeof(int32_t) * mw);
+    d_pool.get(sizeof(double) * off);
+    d_flags.get(static_cast<size_t>(foff));
+    d_mode.get(sizeof(int32_t) * mw);
+    d_status.get(sizeof(int32_t) * mw);
+    d_out4.get(sizeof(double) * 4 * mw);
+    iv_gather_kernel<<<static_cast<int>((mw + 255) / 256), 256, 0, st>>>(
+        static_cast<int>(mw), d_map.as<int32_t>(), d_pt.as<int32_t>(), b->d_tiles.as<TileDev>(),
+        b->d_opts.as<OptDev>(), b->d_xs.as<double>(), d_tiles.as<TileDev>(), d_opts.as<OptDev>(),
+        d_xs.as<double>(), next_sig, d_sigma.as<double>(), d_active.as<int32_t>());
+    check(cudaGetLastError(), "iv_gather launch");
+  }
+};
+
+MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t n,
+                     const MangoGpuGrid* grids, uint64_t grid_stride, const MangoIvConfig* config,
+                     int32_t method, MangoIvBatchSlot* out, uint64_t* out_failed, MangoError* err) {
   if (!ctx || (n > 0 && (!queries || !out))) {
     set_err(err, MANGO_ERR_VALIDATION, "null context, queries or out");
     return MANGO_ERR_VALIDATION;
@@ -241,15 +696,20 @@ extern "C" MangoStatus mango_gpu_solve_iv_batch(MangoGpuContext* ctx, const Mang
             "IV needs a fixed grid per quote (MANGO_GPU_GRID_FIXED_N_AT_VOL, _SINH or _UNIFORM)");
     return MANGO_ERR_VALIDATION;
   }
+  if (method != MANGO_GPU_IV_BRENT && method != MANGO_GPU_IV_SECANT) {
+    set_err(err, MANGO_ERR_VALIDATION, "unknown IV method");
+    return MANGO_ERR_VALIDATION;
+  }
   if (n > (1ull << 30)) {
     set_err(err, MANGO_ERR_VALIDATION, "batch above 2^30 quotes");
     return MANGO_ERR_VALIDATION;
   }
   const double tol = (config && config->brent_tol_abs > 0.0) ? config->brent_tol_abs : 1e-6;
   const int max_iter = (config && config->max_iter > 0) ? config->max_iter : 100;
+  const char* trace_env = std::getenv("MANGO_GPU_IV_TRACE");
+  const bool trace = trace_env && trace_env[0] == '1';
   MangoGpuBatch* b = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  cudaGraph_t graph = nullptr;
+  const auto t_start = Clock::now();
   try {
     check(cudaSetDevice(ctx->device), "cudaSetDevice");
     const int64_t nn = static_cast<int64_t>(n);
@@ -286,78 +746,130 @@ extern "C" MangoStatus mango_gpu_solve_iv_batch(MangoGpuContext* ctx, const Mang
       upper[i] = ratio > 0.5 ? 3.0 : (ratio > 0.2 ? 2.0 : 1.5);
     }
     b = create_batch(ctx, pp.data(), nn, grids, grid_stride, nullptr);
+    // The batch's own march buffers are not used: every evaluation runs on
+    // a packed working set.
+    for (DevBuf* d : {&b->d_pool, &b->d_flags, &b->d_mode, &b->d_status, &b->d_out4}) d->release();
+    const double host_prep_ms = b->host_prep_ms;
     const int64_t m = static_cast<int64_t>(b->order.size());
-    std::vector<int32_t> code(static_cast<size_t>(m), kIvNumerical);
-    std::vector<BrentDev> hs(static_cast<size_t>(m));
+    std::vector<IvOut> hr(static_cast<size_t>(m));
+    int64_t launches = 0, evaluations = 0;
+    double slot_evals = 0, eval_ms = 0, pack_ms = 0;
     if (m > 0) {
       cudaStream_t st = ctx->stream;
-      std::vector<double> hi_sorted(static_cast<size_t>(m)), px(static_cast<size_t>(m));
+      std::vector<double> hi_sorted(static_cast<size_t>(m)), px(static_cast<size_t>(m)),
+          mat(static_cast<size_t>(m));
       for (int64_t s = 0; s < m; ++s) {
+        const MangoIvQuery& q = queries[b->order[s]];
         hi_sorted[s] = upper[b->order[s]];
-        px[s] = queries[b->order[s]].market_price;
+        px[s] = q.market_price;
+        mat[s] = q.maturity;
       }
-      DevBuf d_state, d_sigma, d_active, d_hi, d_px, d_count;
-      HostBuf h_count;
-      BrentDev* S = static_cast<BrentDev*>(d_state.get(sizeof(BrentDev) * m));
-      double* sigma = static_cast<double*>(d_sigma.get(sizeof(double) * m));
-      int32_t* active = static_cast<int32_t*>(d_active.get(sizeof(int32_t) * m));
+      DevBuf d_state, d_res, d_next, d_npts, d_hi, d_px, d_mat;
+      HostBuf h_npts;
+      struct Release {
+        std::vector<DevBuf*> d;
+        HostBuf* h;
+        ~Release() {
+          for (DevBuf* x : d) x->release();
+          h->release();
+        }
+      } release{{&d_state, &d_res, &d_next, &d_npts, &d_hi, &d_px, &d_mat}, &h_npts};
+      IvDev* S = static_cast<IvDev*>(d_state.get(sizeof(IvDev) * m));
+      IvOut* R = static_cast<IvOut*>(d_res.get(sizeof(IvOut) * m));
+      double* next_sig = static_cast<double*>(d_next.get(sizeof(double) * kMaxPts * m));
+      int32_t* npts = static_cast<int32_t*>(d_npts.get(sizeof(int32_t) * m));
+      int32_t* hnpts = static_cast<int32_t*>(h_npts.get(sizeof(int32_t) * m));
       double* dhi = static_cast<double*>(d_hi.get(sizeof(double) * m));
       double* dpx = static_cast<double*>(d_px.get(sizeof(double) * m));
-      int* count = static_cast<int*>(d_count.get(sizeof(int) * 4));
-      int* hcount = static_cast<int*>(h_count.get(sizeof(int) * 4));
+      double* dmat = static_cast<double*>(d_mat.get(sizeof(double) * m));
       check(cudaMemcpyAsync(dhi, hi_sorted.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st), "H2D");
       check(cudaMemcpyAsync(dpx, px.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st), "H2D");
-      const int tb = 256, gb = static_cast<int>((m + tb - 1) / tb);
-      brent_init_kernel<<<gb, tb, 0, st>>>(static_cast<int>(m), dhi, S, sigma, active);
-      check(cudaGetLastError(), "brent_init launch");
-
-      MarchConst mc = b->mc;
-      mc.value_only = 1;
-      mc.sigma = sigma;
-      mc.active = active;
-      const int ntiles = b->ntiles;
-      const int threads = ntiles * kTile;
-      const int blocks = std::max(1, std::min<int>(ctx->num_sms * ctx->march_blocks_per_sm, (ntiles + 3) / 4));
-      // One Brent evaluation as a graph: reset counters, setup, march,
-      // value, Brent update.
-      check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
-      cudaMemsetAsync(b->d_queue.p, 0, sizeof(int) * 4, st);
-      cudaMemsetAsync(count, 0, sizeof(int) * 4, st);
-      prep_kernel<<<(threads + 127) / 128, 128, 0, st>>>(b->d_tiles.as<TileDev>(), ntiles,
-                                                         b->d_opts.as<OptDev>(), b->d_xs.as<double>(),
-                                                         b->d_pool.as<double>(), b->d_flags.as<uint8_t>(),
-                                                         b->d_mode.as<int32_t>(), mc);
-      march_kernel<<<blocks, 128, 0, st>>>(b->d_tiles.as<TileDev>(), ntiles, b->d_opts.as<OptDev>(),
-                                           b->d_pool.as<double>(), b->d_flags.as<uint8_t>(),
-                                           b->d_mode.as<int32_t>(), b->d_status.as<int32_t>(),
-                                           b->d_queue.as<int>(), mc);
-      outputs_kernel<<<(threads + 127) / 128, 128, 0, st>>>(
-          b->d_tiles.as<TileDev>(), ntiles, b->d_opts.as<OptDev>(), b->d_xs.as<double>(),
-          b->d_pool.as<double>(), b->d_mode.as<int32_t>(), b->d_status.as<int32_t>(), mc,
-          b->d_out4.as<double>());
-      brent_step_kernel<<<gb, tb, 0, st>>>(static_cast<int>(m), S, b->d_out4.as<double>(),
-                                           b->d_status.as<int32_t>(), dpx, sigma, active, tol,
-                                           max_iter, count);
-      cudaMemcpyAsync(hcount, count, sizeof(int), cudaMemcpyDeviceToHost, st);
-      check(cudaStreamEndCapture(st, &graph), "end capture");
-      check(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
-      // Two endpoint evaluations plus at most max_iter Brent steps.
-      int launches = 0;
-      for (int it = 0; it < max_iter + 3; ++it) {
-        check(cudaGraphLaunch(exec, st), "graph launch");
+      check(cudaMemcpyAsync(dmat, mat.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st), "H2D");
+      const int tb = 256;
+      auto grid_of = [&](int64_t c) { return static_cast<int>((c + tb - 1) / tb); };
+      // Points per quote: one wave of lanes (one warp per SM sub-partition)
+      // spread over the quotes left, 1 .. kMaxPts.
+      const int64_t wave = 4LL * ctx->num_sms * kTile;
+      auto points_for = [&](int64_t quotes) {
+        if (method != MANGO_GPU_IV_SECANT) return 1;
+        return static_cast<int>(
+            std::max<int64_t>(1, std::min<int64_t>(kMaxPts, wave / std::max<int64_t>(quotes, 1))));
+      };
+      iv_init_kernel<<<grid_of(m), tb, 0, st>>>(static_cast<int>(m), method, points_for(m),
+                                                b->d_opts.as<OptDev>(), dmat, dpx, dhi, S, R,
+                                                next_sig, npts);
+      check(cudaGetLastError(), "iv_init launch");
+      ++launches;
+      cudaEvent_t ev[2] = {nullptr, nullptr};
+      struct Events {
+        cudaEvent_t* e;
+        ~Events() {
+          for (int j = 0; j < 2; ++j)
+            if (e[j]) cudaEventDestroy(e[j]);
+        }
+      } events{ev};
+      for (cudaEvent_t& e : ev) check(cudaEventCreate(&e), "cudaEventCreate");
+      WorkSet w;
+      w.b = b;
+      w.st = st;
+      std::vector<int32_t> active(static_cast<size_t>(m));
+      std::iota(active.begin(), active.end(), 0);
+      // Fast evaluations, then Brent's two bracket ends and max_iter steps.
+      const int max_evals = (method == MANGO_GPU_IV_SECANT ? kFastMaxBracketEvals : 0) + max_iter + 3;
+      for (int e = 0; e < max_evals; ++e) {
+        check(cudaMemcpyAsync(hnpts, npts, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, st),
+              "D2H points");
         check(cudaStreamSynchronize(st), "stream synchronize");
-        ++launches;
-        if (hcount[0] == 0) break;
+        const auto tp = Clock::now();
+        w.pack(active, hnpts, next_sig);
+        pack_ms += ms_since(tp);
+        if (w.nq == 0) break;
+        active = w.qlist_h;
+        const int k_next = points_for(w.nq);
+        MarchConst mc = b->mc;
+        mc.value_only = 1;
+        mc.sigma = w.d_sigma.as<double>();
+        mc.active = w.d_active.as<int32_t>();
+        const int ntiles = w.ntiles, threads = ntiles * kTile;
+        const int blocks =
+            std::max(1, std::min<int>(ctx->num_sms * ctx->march_blocks_per_sm, (ntiles + 3) / 4));
+        const TileDev* tiles = w.d_tiles.as<TileDev>();
+        const OptDev* wopts = w.d_opts.as<OptDev>();
+        const double* xs = w.d_xs.as<double>();
+        check(cudaMemsetAsync(b->d_queue.p, 0, sizeof(int) * 4, st), "memset queue");
+        check(cudaEventRecord(ev[0], st), "event");
+        prep_kernel<<<(threads + 127) / 128, 128, 0, st>>>(tiles, ntiles, wopts, xs,
+                                                           w.d_pool.as<double>(),
+                                                           w.d_flags.as<uint8_t>(),
+                                                           w.d_mode.as<int32_t>(), mc);
+        march_kernel<<<blocks, 128, 0, st>>>(tiles, ntiles, wopts, w.d_pool.as<double>(),
+                                             w.d_flags.as<uint8_t>(), w.d_mode.as<int32_t>(),
+                                             w.d_status.as<int32_t>(), b->d_queue.as<int>(), mc);
+        outputs_kernel<<<(threads + 127) / 128, 128, 0, st>>>(
+            tiles, ntiles, wopts, xs, w.d_pool.as<double>(), w.d_mode.as<int32_t>(),
+            w.d_status.as<int32_t>(), mc, w.d_out4.as<double>());
+        iv_step_kernel<<<grid_of(w.nq), tb, 0, st>>>(
+            static_cast<int>(w.nq), w.d_qlist.as<int32_t>(), w.d_qbase.as<int32_t>(), k_next, S, R,
+            b->d_opts.as<OptDev>(), dmat, dhi, w.d_out4.as<double>(), w.d_status.as<int32_t>(),
+            w.d_sigma.as<double>(), dpx, next_sig, npts, tol, max_iter, trace ? 1 : 0);
+        check(cudaGetLastError(), "iv evaluation launch");
+        check(cudaEventRecord(ev[1], st), "event");
+        check(cudaStreamSynchronize(st), "stream synchronize");
+        float ms = 0.f;
+        check(cudaEventElapsedTime(&ms, ev[0], ev[1]), "event time");
+        eval_ms += ms;
+        launches += 5;  // gather, prep, march, outputs, step
+        evaluations += 1;
+        slot_evals += static_cast<double>(w.mw);
+        if (trace)
+          std::fprintf(stderr,
+                       "iv evaluation %d: %lld quotes, %lld points in %d tiles, next %d per quote, "
+                       "%.3f ms\n",
+                       e, static_cast<long long>(w.nq), static_cast<long long>(w.mw), w.ntiles, k_next,
+                       ms);
       }
-      ctx->stats.kernel_launches = 4LL * launches + 1;
-      check(cudaMemcpyAsync(hs.data(), S, sizeof(BrentDev) * m, cudaMemcpyDeviceToHost, st), "D2H state");
+      check(cudaMemcpyAsync(hr.data(), R, sizeof(IvOut) * m, cudaMemcpyDeviceToHost, st), "D2H results");
       check(cudaStreamSynchronize(st), "stream synchronize");
-      cudaGraphExecDestroy(exec);
-      exec = nullptr;
-      cudaGraphDestroy(graph);
-      graph = nullptr;
-      for (DevBuf* d : {&d_state, &d_sigma, &d_active, &d_hi, &d_px, &d_count}) d->release();
-      h_count.release();
     }
     uint64_t failed = 0;
     std::string first;
@@ -368,8 +880,8 @@ extern "C" MangoStatus mango_gpu_solve_iv_batch(MangoGpuContext* ctx, const Mang
       if (vstatus[i] != MANGO_OK && first.empty()) first = vmsg[i];
     }
     for (int64_t s = 0; s < m; ++s) {
-      const BrentDev& r = hs[s];
       MangoIvBatchSlot& o = out[b->order[s]];
+      const IvOut& r = hr[s];
       switch (r.code) {
         case kIvOk: o.status = MANGO_OK; break;
         case kIvBracket: o.status = MANGO_ERR_BRACKETING; break;
@@ -384,15 +896,44 @@ extern "C" MangoStatus mango_gpu_solve_iv_batch(MangoGpuContext* ctx, const Mang
       o.success.used_rate_approximation = 0;
     }
     for (int64_t i = 0; i < nn; ++i) failed += out[i].status != MANGO_OK;
+    ctx->stats = Stats{};
+    ctx->stats.host_prep_ms = host_prep_ms;
+    ctx->stats.prep_ms = pack_ms;
+    ctx->stats.march_ms = eval_ms;
+    ctx->stats.total_ms = ms_since(t_start);
+    ctx->stats.kernel_launches = launches;
+    ctx->stats.options = static_cast<int64_t>(slot_evals);
+    ctx->stats.tiles = evaluations;
+    ctx->stats.algo_flops = m > 0 ? b->algo_flops * slot_evals / static_cast<double>(m) : 0.0;
     if (out_failed) *out_failed = failed;
     if (failed && err) set_err(err, MANGO_OK, first.empty() ? "root finding failed" : first);
     destroy_batch(b);
     return MANGO_OK;
   } catch (const std::exception& e) {
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
     if (b) destroy_batch(b);
     set_err(err, MANGO_ERR_SOLVER, e.what());
     return MANGO_ERR_SOLVER;
   }
+}
+
+}  // namespace
+}  // namespace mgpu
+
+extern "C" MangoStatus mango_gpu_solve_iv_batch(MangoGpuContext* ctx, const MangoIvQuery* queries,
+                                                uint64_t n, const MangoGpuGrid* grids,
+                                                uint64_t grid_stride, const MangoIvConfig* config,
+                                                MangoIvBatchSlot* out, uint64_t* out_failed,
+                                                MangoError* err) {
+  return mgpu::solve_iv(ctx, queries, n, grids, grid_stride, config, MANGO_GPU_IV_BRENT, out,
+                        out_failed, err);
+}
+
+extern "C" MangoStatus mango_gpu_solve_iv_batch_method(MangoGpuContext* ctx,
+                                                       const MangoIvQuery* queries, uint64_t n,
+                                                       const MangoGpuGrid* grids,
+                                                       uint64_t grid_stride,
+                                                       const MangoIvConfig* config, int32_t method,
+                                                       MangoIvBatchSlot* out, uint64_t* out_failed,
+                                                       MangoError* err) {
+  return mgpu::solve_iv(ctx, queries, n, grids, grid_stride, config, method, out, out_failed, err);
 }

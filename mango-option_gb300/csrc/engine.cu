@@ -212,16 +212,29 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
   b->msgs = std::move(messages);
   b->msgs.resize(static_cast<size_t>(n));
   for (auto& e : b->ev) check(cudaEventCreate(&e), "cudaEventCreate");
-  // Sort accepted options by (n_space, n_time) descending: similar lanes
-  // share a tile and the largest tiles are dequeued first.
+  // Sort accepted options by (n_space, n_time) descending, so that the
+  // largest tiles are dequeued first and a tile's lanes share their row
+  // and step counts; then by option type and normalised moneyness
+  // ln(S/K) / (sigma sqrt(T)), so that a tile's lanes meet the obstacle at
+  // similar rows and leave the cached factorisation together (lanes on the
+  // off-cache path at different rows serialise a warp).
   std::vector<int32_t>& order = b->order;
-  for (int64_t i = 0; i < n; ++i)
-    if (b->res[i].status == 0) order.push_back(static_cast<int32_t>(i));
+  std::vector<double> mkey(static_cast<size_t>(n), 0.0);
+  for (int64_t i = 0; i < n; ++i) {
+    if (b->res[i].status != 0) continue;
+    order.push_back(static_cast<int32_t>(i));
+    const MangoPricingParams& p = params[b->res[i].orig];
+    const double k = std::log(p.spot / p.strike) / (p.volatility * std::sqrt(p.maturity));
+    mkey[i] = std::isfinite(k) ? k : 0.0;
+  }
   std::sort(order.begin(), order.end(), [&](int32_t a, int32_t c) {
     const Resolved& ra = b->res[a];
     const Resolved& rc = b->res[c];
     if (ra.spec.n != rc.spec.n) return ra.spec.n > rc.spec.n;
     if (ra.nt != rc.nt) return ra.nt > rc.nt;
+    const int pa = params[ra.orig].option_type, pc = params[rc.orig].option_type;
+    if (pa != pc) return pa < pc;
+    if (mkey[a] != mkey[c]) return mkey[a] < mkey[c];
     return a < c;
   });
   const int64_t m = static_cast<int64_t>(order.size());

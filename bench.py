@@ -299,6 +299,42 @@ def bench_table(pkg, eng, torch, stream, nq, fp64_peak):
              "hbm_gbs": 40.0 * nq / t / 1e9,
              "fp64_frac": flops_per_query * nq / t / 1e12 / fp64_peak, "ms": 1e3 * t}
     surf.close()
+    # Whole table build on the device (sweep -> EEP -> fit -> surface) and
+    # the standard table's price query (EEPLayer over TransformLeaf).
+    eng.price_table_build(*TABLE_AXES, K_ref=100.0, dividend_yield=0.0, option_type=1, grid=grid)[0].close()
+    t0 = time.perf_counter()
+    table, fstats = eng.price_table_build(*TABLE_AXES, K_ref=100.0, dividend_yield=0.0, option_type=1, grid=grid)
+    t_build = time.perf_counter() - t0
+    sweep["build"] = {"workload": "PriceTableBuilderND<4>::build on the device: sweep + EEP + fit + surface",
+                      "seconds": t_build, "fit_max_residual": max(fstats["max_residual"]),
+                      "fit_failed_slices": int(sum(fstats["failed_slices"]))}
+    nrec = min(nq, 2_000_000)
+    rng = np.random.default_rng(8)
+    recs = pkg.pricing_array(np.full(nrec, 100.0), 100.0 / np.exp(rng.uniform(TABLE_AXES[0][0], TABLE_AXES[0][-1], nrec)),
+                             rng.uniform(0.02, 2.0, nrec), rng.uniform(0.05, 0.8, nrec), rng.uniform(0.0, 0.08, nrec),
+                             0.0, 1)
+    d_rec = torch.from_numpy(recs.view(np.uint8)).to("cuda")
+    d_val = torch.empty(nrec, dtype=torch.float64, device="cuda")
+    for _ in range(3):
+        table.price_device(d_rec.data_ptr(), nrec, d_val.data_ptr())
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        table.price_device(d_rec.data_ptr(), nrec, d_val.data_ptr())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_price = e0.elapsed_time(e1) / 1e3 / reps
+    t0 = time.perf_counter()
+    host_vals = table.price_arrays(recs)
+    t_price_e2e = time.perf_counter() - t0
+    assert np.isfinite(host_vals).all()
+    query["table_price"] = {
+        "workload": f"{nrec} American put prices from the 50x30x20x10 EEP table "
+                    "(spline + max(0, .) K/K_ref + closed-form European)",
+        "value": nrec / t_price, "unit": "prices/s (device-resident)",
+        "e2e": {"value": nrec / t_price_e2e, "unit": "prices/s", "h2d_bytes_per_step": int(recs.nbytes),
+                "d2h_bytes_per_step": int(host_vals.nbytes)}}
+    table.close()
     return sweep, query
 
 

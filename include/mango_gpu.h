@@ -269,6 +269,85 @@ MangoStatus mango_gpu_bspline4d_eval_device(MangoGpuBSpline4D* surface, const do
 MangoStatus mango_gpu_bspline4d_knots(const MangoGpuBSpline4D* surface, double* out, uint64_t cap,
                                       uint64_t* n_out);
 
+/* Separable collocation fit: BSplineNDSeparable<double,4>::fit
+ * (src/math/bspline/bspline_nd_separable.hpp:153-384) with
+ * BSplineCollocation1D (src/math/bspline/bspline_collocation.hpp:326-390):
+ * coefficients whose BSplineND interpolates values (row-major, same layout
+ * as coeffs) at the grid points.  Axes 3, 2, 1, 0 in turn; every slice along
+ * an axis solves the axis's cubic collocation system (banded LU with partial
+ * pivoting, factored once per axis) and is accepted when max |B c - f| <=
+ * tolerance (0 => 1e-6, BSplineNDSeparableConfig).  A rejected slice keeps
+ * its input values and counts in failed_slices; any failure makes the call
+ * return MANGO_ERR_SOLVER ("fitting failed"), as the reference's fit does.
+ * NaN or infinite values: MANGO_ERR_VALIDATION.  condition[d] is the exact
+ * 1-norm condition number of the axis's collocation matrix (the reference
+ * reports LAPACK dgbcon's estimate of it). */
+typedef struct {
+  double max_residual[4];
+  double condition[4];
+  uint64_t failed_slices[4];
+} MangoGpuFitStats;
+MangoStatus mango_gpu_bspline4d_fit(MangoGpuContext* ctx, const double* grids,
+                                    const int64_t* sizes, const double* values, double tolerance,
+                                    double* coeffs, MangoGpuFitStats* stats, MangoError* err);
+
+/* Price table: the reference's standard 4D B-spline price table
+ * (make_bspline_surface, src/option/table/bspline/bspline_surface.cpp:9-37):
+ * axes log-moneyness, maturity, volatility, rate; price(S, K, tau, sigma, r)
+ * = max(0, spline(log(S/K), tau, sigma, r)) * K / K_ref (TransformLeaf,
+ * src/option/table/transform_leaf.hpp:28-33) plus, when eep != 0, the
+ * closed-form European price with the table's option type and dividend yield
+ * (EEPLayer + AnalyticalEEP, src/option/table/eep/eep_layer.hpp:21-25).
+ * Queries are clamped into the axes as BSplineND::eval clamps them. */
+typedef struct MangoGpuPriceTable MangoGpuPriceTable;
+/* From given spline coefficients (grids, sizes, coeffs as for
+ * mango_gpu_bspline4d_create). */
+MangoStatus mango_gpu_price_table_create(MangoGpuContext* ctx, const double* grids,
+                                         const int64_t* sizes, const double* coeffs, double K_ref,
+                                         double dividend_yield, MangoOptionType option_type,
+                                         int32_t eep, MangoGpuPriceTable** out, MangoError* err);
+/* Whole build on the device: PriceTableBuilderND<4>::build
+ * (src/option/table/bspline/bspline_builder.cpp:140-196) = the sweep of
+ * mango_gpu_price_table_sweep (same arguments), then, when eep != 0, the EEP
+ * decomposition of the tensor (eep_decompose with AnalyticalEEP,
+ * src/option/table/eep/eep_decomposer.hpp:60-80: entry = softplus floor of
+ * K_ref V - European), then the fit (tolerance as for
+ * mango_gpu_bspline4d_fit).  A build with failed PDE slices is refused
+ * (MANGO_ERR_SOLVER; the reference repairs them from neighbours). */
+MangoStatus mango_gpu_price_table_build(
+    MangoGpuContext* ctx, const double* moneyness, uint64_t n_moneyness, const double* maturity,
+    uint64_t n_maturity, const double* volatility, uint64_t n_volatility, const double* rate,
+    uint64_t n_rate, double K_ref, double dividend_yield, MangoOptionType option_type,
+    const MangoGpuGrid* grid, int32_t eep, double tolerance, MangoGpuPriceTable** out,
+    MangoGpuFitStats* stats, uint64_t* out_failed_slices, MangoError* err);
+void mango_gpu_price_table_destroy(MangoGpuPriceTable* table);
+/* The EEP step alone (the TensorTransformFn of the standard build,
+ * eep_decompose with AnalyticalEEP over BSplineTensorAccessor,
+ * src/option/table/bspline/bspline_tensor_accessor.hpp:16-56): tensor
+ * [m][tau][sigma][r] of V/K_ref in, EEP in price units out, in place. */
+MangoStatus mango_gpu_eep_decompose(MangoGpuContext* ctx, const double* moneyness,
+                                    uint64_t n_moneyness, const double* maturity,
+                                    uint64_t n_maturity, const double* volatility,
+                                    uint64_t n_volatility, const double* rate, uint64_t n_rate,
+                                    double K_ref, double dividend_yield,
+                                    MangoOptionType option_type, double* tensor, MangoError* err);
+/* The table's spline (owned by the table): eval / knots as above. */
+MangoGpuBSpline4D* mango_gpu_price_table_spline(MangoGpuPriceTable* table);
+/* K_ref, dividend yield, option type, eep flag and the axis bounds
+ * (m, tau, sigma, rate: min, max); any output may be NULL. */
+MangoStatus mango_gpu_price_table_info(const MangoGpuPriceTable* table, double* K_ref,
+                                       double* dividend_yield, int32_t* option_type, int32_t* eep,
+                                       double* bounds8);
+/* AnyPriceTable::price (src/option/price_table_factory.cpp:746-751) for n
+ * parameter records (host arrays).  Constant rates only: a record with
+ * tenor points prices as NaN. */
+MangoStatus mango_gpu_price_table_price(MangoGpuPriceTable* table, const MangoPricingParams* params,
+                                        uint64_t n, double* out, MangoError* err);
+/* Same with device-resident records and output, enqueued without waiting. */
+MangoStatus mango_gpu_price_table_price_device(MangoGpuPriceTable* table,
+                                               const MangoPricingParams* d_params, uint64_t n,
+                                               double* d_out, MangoError* err);
+
 /* Sensitivities on a frozen grid: value, delta, gamma, theta as in
  * mango_gpu_price_american_batch plus dV/dvolatility, dV/drate,
  * dV/ddividend_yield and dV/dstrike, each a central difference with a
@@ -389,6 +468,7 @@ static_assert(sizeof(MangoIvQuery) == 88, "MangoIvQuery size");
 static_assert(sizeof(MangoGpuGrid) == 48, "MangoGpuGrid size");
 static_assert(sizeof(MangoGpuAmericanOut) == 48, "MangoGpuAmericanOut size");
 static_assert(sizeof(MangoGpuGreeksOut) == 80, "MangoGpuGreeksOut size");
+static_assert(sizeof(MangoGpuFitStats) == 96, "MangoGpuFitStats size");
 #endif
 
 #endif /* MANGO_GPU_H */

@@ -88,6 +88,11 @@ class MangoGpuStats(ctypes.Structure):
         ("options", ctypes.c_int64), ("tiles", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
 
 
+class MangoGpuFitStats(ctypes.Structure):
+    _fields_ = [("max_residual", ctypes.c_double * 4), ("condition", ctypes.c_double * 4),
+                ("failed_slices", ctypes.c_uint64 * 4)]
+
+
 class EngineError(RuntimeError):
     """Raised when the engine call itself fails (no device, CUDA error)."""
 
@@ -159,6 +164,35 @@ def library() -> ctypes.CDLL:
         lib.mango_gpu_bspline4d_eval_device.restype = ctypes.c_int32
         lib.mango_gpu_bspline4d_knots.argtypes = [_P, _P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
         lib.mango_gpu_bspline4d_knots.restype = ctypes.c_int32
+        lib.mango_gpu_bspline4d_fit.argtypes = [_P, _P, _P, _P, ctypes.c_double, _P,
+                                                ctypes.POINTER(MangoGpuFitStats), ctypes.POINTER(MangoError)]
+        lib.mango_gpu_bspline4d_fit.restype = ctypes.c_int32
+        lib.mango_gpu_price_table_create.argtypes = [_P, _P, _P, _P, ctypes.c_double, ctypes.c_double,
+                                                     ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_P),
+                                                     ctypes.POINTER(MangoError)]
+        lib.mango_gpu_price_table_create.restype = ctypes.c_int32
+        lib.mango_gpu_price_table_build.argtypes = [
+            _P, _P, ctypes.c_uint64, _P, ctypes.c_uint64, _P, ctypes.c_uint64, _P, ctypes.c_uint64,
+            ctypes.c_double, ctypes.c_double, ctypes.c_int32, _P, ctypes.c_int32, ctypes.c_double,
+            ctypes.POINTER(_P), ctypes.POINTER(MangoGpuFitStats), ctypes.POINTER(ctypes.c_uint64),
+            ctypes.POINTER(MangoError)]
+        lib.mango_gpu_price_table_build.restype = ctypes.c_int32
+        lib.mango_gpu_eep_decompose.argtypes = [_P, _P, ctypes.c_uint64, _P, ctypes.c_uint64, _P, ctypes.c_uint64,
+                                                _P, ctypes.c_uint64, ctypes.c_double, ctypes.c_double,
+                                                ctypes.c_int32, _P, ctypes.POINTER(MangoError)]
+        lib.mango_gpu_eep_decompose.restype = ctypes.c_int32
+        lib.mango_gpu_price_table_destroy.argtypes = [_P]
+        lib.mango_gpu_price_table_destroy.restype = None
+        lib.mango_gpu_price_table_spline.argtypes = [_P]
+        lib.mango_gpu_price_table_spline.restype = _P
+        lib.mango_gpu_price_table_info.argtypes = [_P, ctypes.POINTER(ctypes.c_double),
+                                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int32),
+                                                   ctypes.POINTER(ctypes.c_int32), _P]
+        lib.mango_gpu_price_table_info.restype = ctypes.c_int32
+        lib.mango_gpu_price_table_price.argtypes = [_P, _P, ctypes.c_uint64, _P, ctypes.POINTER(MangoError)]
+        lib.mango_gpu_price_table_price.restype = ctypes.c_int32
+        lib.mango_gpu_price_table_price_device.argtypes = [_P, _P, ctypes.c_uint64, _P, ctypes.POINTER(MangoError)]
+        lib.mango_gpu_price_table_price_device.restype = ctypes.c_int32
         lib.mango_gpu_price_american_greeks_batch.argtypes = [
             _P, _P, ctypes.c_uint64, _P, ctypes.c_uint64, ctypes.c_double, _P,
             ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(MangoError)]
@@ -358,6 +392,77 @@ class Engine:
     def bspline4d(self, grids, coeffs) -> "BSpline4D":
         return BSpline4D(self, grids, coeffs)
 
+    def bspline4d_fit(self, grids, values, tolerance: float = 0.0):
+        """BSplineNDSeparable<double,4>::fit (mango_gpu_bspline4d_fit): the
+        coefficients (same shape as values) and per-axis diagnostics.  Raises
+        EngineError when a slice fails the residual check."""
+        gs = [np.ascontiguousarray(g, dtype=np.float64) for g in grids]
+        sizes = np.array([g.size for g in gs], np.int64)
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        coeffs = np.zeros(v.size)
+        stats = MangoGpuFitStats()
+        err = MangoError()
+        st = library().mango_gpu_bspline4d_fit(self._ctx, _ptr(np.concatenate(gs)), _ptr(sizes), _ptr(v),
+                                               tolerance, _ptr(coeffs), ctypes.byref(stats), ctypes.byref(err))
+        info = _fit_stats(stats)
+        if st != MANGO_OK:
+            e = EngineError(err.message.decode(errors="replace"))
+            e.status, e.stats = st, info
+            raise e
+        return coeffs.reshape(v.shape), info
+
+    def eep_decompose(self, moneyness, maturity, volatility, rate, tensor, K_ref: float = 100.0,
+                      dividend_yield: float = 0.0, option_type: int = 1) -> np.ndarray:
+        """eep_decompose with AnalyticalEEP of a V/K_ref tensor (mango_gpu_eep_decompose)."""
+        axes = [np.ascontiguousarray(a, dtype=np.float64) for a in (moneyness, maturity, volatility, rate)]
+        t = np.ascontiguousarray(tensor, dtype=np.float64).copy()
+        err = MangoError()
+        st = library().mango_gpu_eep_decompose(self._ctx, _ptr(axes[0]), axes[0].size, _ptr(axes[1]),
+                                               axes[1].size, _ptr(axes[2]), axes[2].size, _ptr(axes[3]),
+                                               axes[3].size, K_ref, dividend_yield, int(option_type), _ptr(t),
+                                               ctypes.byref(err))
+        if st != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+        return t
+
+    def price_table_create(self, grids, coeffs, K_ref: float, dividend_yield: float = 0.0,
+                           option_type: int = 1, eep: bool = True) -> "GpuPriceTable":
+        """Standard price table over given spline coefficients
+        (make_bspline_surface; mango_gpu_price_table_create)."""
+        gs = [np.ascontiguousarray(g, dtype=np.float64) for g in grids]
+        sizes = np.array([g.size for g in gs], np.int64)
+        c = np.ascontiguousarray(coeffs, dtype=np.float64).ravel()
+        h = _P()
+        err = MangoError()
+        st = library().mango_gpu_price_table_create(self._ctx, _ptr(np.concatenate(gs)), _ptr(sizes), _ptr(c),
+                                                    K_ref, dividend_yield, int(option_type), int(bool(eep)),
+                                                    ctypes.byref(h), ctypes.byref(err))
+        if st != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+        return GpuPriceTable(self, h)
+
+    def price_table_build(self, moneyness, maturity, volatility, rate, K_ref: float = 100.0,
+                          dividend_yield: float = 0.0, option_type: int = 1, grid=None, eep: bool = True,
+                          tolerance: float = 0.0):
+        """PriceTableBuilderND<4>::build on the device (mango_gpu_price_table_build):
+        sweep, EEP decomposition, fit.  moneyness is log-moneyness.  Returns
+        (GpuPriceTable, fit diagnostics)."""
+        axes = [np.ascontiguousarray(a, dtype=np.float64) for a in (moneyness, maturity, volatility, rate)]
+        g = None if grid is None else _grid_entry(grid)
+        h = _P()
+        stats = MangoGpuFitStats()
+        failed = ctypes.c_uint64()
+        err = MangoError()
+        st = library().mango_gpu_price_table_build(
+            self._ctx, _ptr(axes[0]), axes[0].size, _ptr(axes[1]), axes[1].size, _ptr(axes[2]), axes[2].size,
+            _ptr(axes[3]), axes[3].size, K_ref, dividend_yield, int(option_type), _ptr(g), int(bool(eep)),
+            tolerance, ctypes.byref(h), ctypes.byref(stats), ctypes.byref(failed), ctypes.byref(err))
+        if st != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+        info = _fit_stats(stats)
+        info["failed_pde_slices"] = int(failed.value)
+        return GpuPriceTable(self, h), info
+
     def greeks_arrays(self, params: np.ndarray, grids: Optional[np.ndarray] = None,
                       h_rel: float = 1e-5) -> np.ndarray:
         """Prices, delta/gamma/theta and frozen-grid central differences for
@@ -448,6 +553,128 @@ class BSpline4D:
             self.close()
         except Exception:
             pass
+
+
+def _fit_stats(s: MangoGpuFitStats) -> dict:
+    return {"max_residual": list(s.max_residual), "condition": list(s.condition),
+            "failed_slices": [int(x) for x in s.failed_slices]}
+
+
+class GpuPriceTable:
+    """Device-resident standard price table (mango_gpu_price_table_*): the
+    counterpart of the reference's PriceTable (AnyPriceTable) for the 4D
+    B-spline surface with EEP decomposition."""
+
+    surface_type = "bspline"
+
+    def __init__(self, engine: Engine, handle):
+        self._engine = engine
+        self._t = handle
+        K, q = ctypes.c_double(), ctypes.c_double()
+        ot, eep = ctypes.c_int32(), ctypes.c_int32()
+        b = np.zeros(8)
+        library().mango_gpu_price_table_info(self._t, ctypes.byref(K), ctypes.byref(q), ctypes.byref(ot),
+                                             ctypes.byref(eep), _ptr(b))
+        self.K_ref, self.dividend_yield = K.value, q.value
+        self.option_type = OptionType(ot.value)
+        self.eep = bool(eep.value)
+        self.bounds = b.reshape(4, 2)
+
+    def price_arrays(self, params: np.ndarray) -> np.ndarray:
+        """AnyPriceTable::price for PRICING_DTYPE records (no range checks)."""
+        params = np.ascontiguousarray(params, dtype=PRICING_DTYPE)
+        out = np.zeros(params.size)
+        err = MangoError()
+        if library().mango_gpu_price_table_price(self._t, _ptr(params), params.size, _ptr(out),
+                                                 ctypes.byref(err)) != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+        return out
+
+    def price_device(self, d_params: int, n: int, d_out: int) -> None:
+        err = MangoError()
+        if library().mango_gpu_price_table_price_device(self._t, _P(d_params), n, _P(d_out),
+                                                        ctypes.byref(err)) != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+
+    def validate(self, p: PricingParams) -> None:
+        """AnyPriceTable::validate_pricing_params (price_table_factory.cpp:700-744)."""
+        if p.option_type != self.option_type:
+            raise ValueError("option type does not match the table")
+        if abs(p.dividend_yield - self.dividend_yield) > 1e-10:
+            raise ValueError("dividend yield does not match the table")
+        coords = (np.log(p.spot / p.strike), p.maturity, p.volatility, p.rate)
+        for d, x in enumerate(coords):
+            if x < self.bounds[d, 0] or x > self.bounds[d, 1]:
+                raise ValueError(f"axis {d} value {x} outside the table")
+
+    def price(self, params: PricingParams) -> float:
+        """PriceTable.price of the reference's bindings: validate, then price."""
+        self.validate(params)
+        return float(self.price_arrays(_to_array([params]))[0])
+
+    def spline_eval(self, queries: np.ndarray) -> np.ndarray:
+        q = np.ascontiguousarray(queries, dtype=np.float64).reshape(-1, 4)
+        out = np.zeros(q.shape[0])
+        err = MangoError()
+        s = library().mango_gpu_price_table_spline(self._t)
+        if library().mango_gpu_bspline4d_eval(s, _ptr(q), q.shape[0], _ptr(out), ctypes.byref(err)) != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+        return out
+
+    def close(self):
+        if self._t:
+            library().mango_gpu_price_table_destroy(self._t)
+            self._t = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclasses.dataclass
+class IVGrid:
+    """Reference IVGrid (moneyness S/K, volatility and rate axes)."""
+    moneyness: Sequence[float]
+    vol: Sequence[float]
+    rate: Sequence[float]
+
+
+@dataclasses.dataclass
+class BSplineBackend:
+    """Reference BSplineBackend (maturity axis)."""
+    maturity_grid: Sequence[float]
+
+
+@dataclasses.dataclass
+class IVSolverFactoryConfig:
+    """Reference IVSolverFactoryConfig for the standard B-spline path
+    (continuous dividend yield)."""
+    option_type: OptionType = OptionType.PUT
+    spot: float = 100.0
+    dividend_yield: float = 0.0
+    grid: Optional[IVGrid] = None
+    backend: Optional[BSplineBackend] = None
+
+
+def make_price_table(config: IVSolverFactoryConfig, engine: Optional[Engine] = None) -> GpuPriceTable:
+    """make_price_table, standard B-spline path (price_table_factory.cpp:
+    294-325): log-moneyness from the moneyness axis, K_ref = spot, the default
+    accuracy PDE grid, EEP decomposition.  Axes are sorted and de-duplicated
+    as PriceTableBuilder::from_vectors does."""
+    if config.grid is None or config.backend is None:
+        raise ValueError("config needs grid and backend")
+    m = np.asarray(config.grid.moneyness, dtype=np.float64)
+    if (m <= 0).any():
+        raise ValueError("moneyness must be positive")
+    axes = [np.unique(np.log(m)), np.unique(np.asarray(config.backend.maturity_grid, dtype=np.float64)),
+            np.unique(np.asarray(config.grid.vol, dtype=np.float64)),
+            np.unique(np.asarray(config.grid.rate, dtype=np.float64))]
+    eng = engine or default_engine()
+    table, _ = eng.price_table_build(*axes, K_ref=config.spot, dividend_yield=config.dividend_yield,
+                                     option_type=int(config.option_type), grid=None, eep=True)
+    return table
 
 
 class ResidentBatch:

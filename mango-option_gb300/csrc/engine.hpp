@@ -90,6 +90,17 @@ void destroy_batch(MangoGpuBatch* b);
 void run_batch(MangoGpuBatch* b);
 // Wait, copy results into caller slots, update the context stats.
 uint64_t fetch_batch(MangoGpuBatch* b, MangoGpuAmericanOut* out, std::string* first_msg);
+// Price-table sweep (table.cu): argument checks, and the sweep with the
+// tensor [m][tau][sigma][r] left in device memory; returns failed slices.
+std::string check_table_args(const double* moneyness, uint64_t nm, const double* maturity,
+                             uint64_t ntau, const double* volatility, uint64_t nsig,
+                             const double* rate, uint64_t nr, double K_ref, double dividend_yield,
+                             MangoOptionType option_type);
+uint64_t table_sweep_device(MangoGpuContext* ctx, const double* moneyness, uint64_t nm,
+                            const double* maturity, uint64_t ntau, const double* volatility,
+                            uint64_t nsig, const double* rate, uint64_t nr, double K_ref,
+                            double dividend_yield, MangoOptionType option_type,
+                            const MangoGpuGrid* grid, double* dten, int64_t* slice_dims);
 // Kernels (march.cu).
 __global__ void prep_kernel(const TileDev*, int, const OptDev*, const double*, double*, uint8_t*,
                             int32_t*, MarchConst);

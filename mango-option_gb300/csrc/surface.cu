@@ -1,0 +1,596 @@
+// surface.cu -- price-table surface on the GPU: separable collocation fit,
+// EEP decomposition, the assembled table and its batched price query.
+//
+// Restates, for the 4D standard table:
+//   BSplineNDSeparable<double,4>::fit (src/math/bspline/bspline_nd_separable.hpp:153-384)
+//     with BSplineCollocation1D::fit_with_workspace
+//     (src/math/bspline/bspline_collocation.hpp:326-390): axes in the order
+//     3, 2, 1, 0; per slice along the axis, solve B c = f, residual
+//     max |B c - f| (fma order of compute_residual_from_span), a slice whose
+//     residual exceeds the tolerance keeps its input values and counts as
+//     failed;
+//   eep_decompose with AnalyticalEEP over BSplineTensorAccessor
+//     (src/option/table/eep/eep_decomposer.hpp:14-80,
+//     src/option/table/bspline/bspline_tensor_accessor.hpp:16-56): the tensor
+//     entry becomes eep_floor(K_ref V - European(K_ref e^m, K_ref, tau, sigma, r));
+//   PriceTableBuilderND<4>::build steps 3-5
+//     (src/option/table/bspline/bspline_builder.cpp:140-196) and
+//     make_bspline_surface (src/option/table/bspline/bspline_surface.cpp:9-37);
+//   the query AnyPriceTable::price -> EEPLayer::price -> TransformLeaf::price
+//     (src/option/price_table_factory.cpp:746-751,
+//     src/option/table/eep/eep_layer.hpp:21-25,
+//     src/option/table/transform_leaf.hpp:28-33) with StandardTransform4D
+//     coordinates (log(S/K), tau, sigma, r) and the closed-form European
+//     price of EuropeanOptionResult::compute_price
+//     (src/option/european_option.cpp:25-51).
+//
+// GB300 design: the collocation factors of an axis are computed once on the
+// host (fit_host.cpp) and broadcast through shared memory; one thread solves
+// one slice in place, ping-ponging between two device tensors, so a whole
+// table build (sweep -> EEP -> fit -> surface) never leaves the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "bspline.cuh"
+#include "fit_host.hpp"
+
+namespace mgpu {
+
+MangoGpuBSpline4D* new_surface(MangoGpuContext* ctx, const double* grids, const int64_t* sizes);
+
+namespace {
+
+__device__ __forceinline__ double norm_cdf(double x) {
+  return 0.5 * erfc(-x * 0.70710678118654752440);  // european_option.hpp:30-32
+}
+
+// EuropeanOptionResult::compute_price (european_option.cpp:25-51).
+__device__ double european_price(double S, double K, double tau, double sigma, double r, double q,
+                                 bool put) {
+  if (tau <= 0.0 || sigma <= 0.0) {
+    double s = S, k = K;
+    if (tau > 0.0) {
+      s = S * exp(-q * tau);
+      k = K * exp(-r * tau);
+    }
+    return put ? fmax(k - s, 0.0) : fmax(s - k, 0.0);
+  }
+  const double sst = sigma * sqrt(tau);
+  const double d1 = (log(S / K) + (r - q + 0.5 * sigma * sigma) * tau) / sst;
+  const double d2 = d1 - sigma * sqrt(tau);
+  const double eq = exp(-q * tau), er = exp(-r * tau);
+  if (put) return K * er * norm_cdf(-d2) - S * eq * norm_cdf(-d1);
+  return S * eq * norm_cdf(d1) - K * er * norm_cdf(d2);
+}
+
+// eep_floor (eep_decomposer.hpp:21-29): debiased softplus with sharpness 100.
+__device__ double eep_floor(double e) {
+  if (100.0 * e > 500.0) return e;
+  const double softplus = log1p(exp(100.0 * e)) / 100.0;
+  const double bias = log(2.0) / 100.0;
+  return fmax(0.0, softplus - bias);
+}
+
+}  // namespace
+
+// One fit axis: slice s covers src[base + i * inner], i < n, with
+// base = (s / inner) * n * inner + s % inner.  Factors in shared memory:
+// band (4n), lower (3n), upper (7n) doubles, then col_start, piv (n each).
+struct FitAxisDev {
+  int n;
+  int64_t inner;
+  int64_t nslices;
+};
+
+__global__ void fit_axis_kernel(FitAxisDev A, const double* __restrict__ fac,
+                                const int32_t* __restrict__ faci, const double* __restrict__ src,
+                                double* __restrict__ dst, double tol,
+                                unsigned long long* __restrict__ max_res_bits,
+                                unsigned long long* __restrict__ failed) {
+  extern __shared__ double fsm[];
+  const int n = A.n;
+  for (int i = threadIdx.x; i < 14 * n; i += blockDim.x) fsm[i] = fac[i];
+  int32_t* ism = reinterpret_cast<int32_t*>(fsm + 14 * n);
+  for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) ism[i] = faci[i];
+  __syncthreads();
+  const double* band = fsm;
+  const double* lower = fsm + 4 * n;
+  const double* upper = fsm + 7 * n;
+  const int32_t* col_start = ism;
+  const int32_t* piv = ism + n;
+  const int64_t s = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (s >= A.nslices) return;
+  const int64_t inner = A.inner;
+  const int64_t base = (s / inner) * n * inner + s % inner;
+  const double* f = src + base;
+  double* c = dst + base;
+  auto F = [&](int i) { return f[static_cast<size_t>(i) * inner]; };
+  auto C = [&](int i) -> double& { return c[static_cast<size_t>(i) * inner]; };
+  for (int i = 0; i < n; ++i) C(i) = F(i);
+  // dgbtrs: forward elimination with the row interchanges
+  for (int j = 0; j + 1 < n; ++j) {
+    const int p = piv[j];
+    if (p != j) {
+      const double tmp = C(p);
+      C(p) = C(j);
+      C(j) = tmp;
+    }
+    const double bj = -C(j);
+    const int lm = min(3, n - 1 - j);
+    for (int i = 1; i <= lm; ++i) C(j + i) = __dadd_rn(C(j + i), __dmul_rn(lower[3 * j + i - 1], bj));
+  }
+  // dtbsv: column-oriented back substitution
+  for (int j = n - 1; j >= 0; --j) {
+    if (C(j) == 0.0) continue;
+    const double cj = C(j) / upper[7 * j];
+    C(j) = cj;
+    for (int i = j - 1; i >= max(0, j - 6); --i)
+      C(i) = __dsub_rn(C(i), __dmul_rn(cj, upper[7 * i + (j - i)]));
+  }
+  // compute_residual_from_span
+  double res = 0.0;
+  for (int i = 0; i < n; ++i) {
+    double bc = 0.0;
+    const int cs = col_start[i];
+    for (int k = 0; k < 4 && cs + k < n; ++k) bc = fma(band[4 * i + k], C(cs + k), bc);
+    res = fmax(res, fabs(bc - F(i)));
+  }
+  if (!(res <= tol)) {
+    for (int i = 0; i < n; ++i) C(i) = F(i);
+    atomicAdd(failed, 1ull);
+  } else {
+    atomicMax(max_res_bits, static_cast<unsigned long long>(__double_as_longlong(res)));
+  }
+}
+
+// Tensor [m][tau][sigma][r] of V/K_ref -> EEP in price units.
+__global__ void eep_decompose_kernel(int nm, int nt, int nv, int nr, const double* __restrict__ mg,
+                                     const double* __restrict__ tg, const double* __restrict__ vg,
+                                     const double* __restrict__ rg, double K_ref, double q, int put,
+                                     double* __restrict__ tensor) {
+  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  const int64_t total = static_cast<int64_t>(nm) * nt * nv * nr;
+  if (i >= total) return;
+  int64_t f = i;
+  const int ri = static_cast<int>(f % nr);
+  f /= nr;
+  const int vi = static_cast<int>(f % nv);
+  f /= nv;
+  const int ti = static_cast<int>(f % nt);
+  const int mi = static_cast<int>(f / nt);
+  const double am = K_ref * tensor[i];
+  const double spot = exp(mg[mi]) * K_ref;
+  const double eu = european_price(spot, K_ref, tg[ti], vg[vi], rg[ri], q, put != 0);
+  tensor[i] = eep_floor(am - eu);
+}
+
+// AnyPriceTable::price for n parameter records.
+__global__ void surface_price_kernel(BSplineDims D, const double* __restrict__ tables,
+                                     const double* __restrict__ coeffs,
+                                     const MangoPricingParams* __restrict__ p, int64_t n,
+                                     double K_ref, double q, int put, int eep,
+                                     double* __restrict__ out) {
+  extern __shared__ double sm[];
+  for (int i = threadIdx.x; i < 4 * D.ktot; i += blockDim.x) sm[i] = tables[i];
+  __syncthreads();
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < n; k += stride) {
+    const MangoPricingParams pk = p[k];
+    if (pk.n_tenor_points != 0) {  // get_zero_rate of a curve: not supported
+      out[k] = __longlong_as_double(0x7ff8000000000000ll);
+      continue;
+    }
+    const double S = pk.spot, K = pk.strike, tau = pk.maturity, sigma = pk.volatility;
+    const double r = pk.rate_const;
+    const double x[4] = {log(S / K), tau, sigma, r};
+    const double raw = bspline4d_value(D, sm, coeffs, x);
+    double v = fmax(0.0, raw) * K / K_ref;
+    if (eep) v += european_price(S, K, tau, sigma, r, q, put != 0);
+    out[k] = v;
+  }
+}
+
+namespace {
+
+// Fit the row-major tensor in a (n0*n1*n2*n3 doubles, device) in place; b is
+// scratch of the same size.  Axis order 3, 2, 1, 0, ping-ponging a -> b -> a.
+void fit_device(MangoGpuContext* ctx, const double* grids, const int64_t* sizes, double* a,
+                double* b, double tol, MangoGpuFitStats* stats) {
+  cudaStream_t st = ctx->stream;
+  DevBuf d_fac, d_faci, d_acc;
+  struct Release {
+    DevBuf* d[3];
+    ~Release() {
+      for (DevBuf* x : d) x->release();
+    }
+  } release{{&d_fac, &d_faci, &d_acc}};
+  unsigned long long* acc = static_cast<unsigned long long*>(d_acc.get(sizeof(unsigned long long) * 8));
+  check(cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * 8, st), "memset");
+  int64_t total = 1;
+  for (int d = 0; d < 4; ++d) total *= sizes[d];
+  int64_t offs[4];
+  int64_t o = 0;
+  for (int d = 0; d < 4; ++d) {
+    offs[d] = o;
+    o += sizes[d];
+  }
+  double* src = a;
+  double* dst = b;
+  std::vector<double> cond(4, 0.0);
+  std::vector<int> singular(4, 0);
+  for (int axis = 3; axis >= 0; --axis) {
+    const int n = static_cast<int>(sizes[axis]);
+    const AxisFactor F = factor_axis(grids + offs[axis], n);
+    cond[axis] = F.cond1;
+    int64_t inner = 1;
+    for (int d = axis + 1; d < 4; ++d) inner *= sizes[d];
+    const int64_t nslices = total / n;
+    if (F.singular) {
+      // factorize_banded_workspace fails for every slice: values stay.
+      singular[axis] = 1;
+      check(cudaMemcpyAsync(dst, src, sizeof(double) * total, cudaMemcpyDeviceToDevice, st), "D2D");
+    } else {
+      std::vector<double> fac(static_cast<size_t>(14) * n);
+      std::vector<int32_t> faci(static_cast<size_t>(2) * n);
+      std::copy(F.band.begin(), F.band.end(), fac.begin());
+      std::copy(F.lower.begin(), F.lower.end(), fac.begin() + 4 * n);
+      std::copy(F.upper.begin(), F.upper.end(), fac.begin() + 7 * n);
+      std::copy(F.col_start.begin(), F.col_start.end(), faci.begin());
+      std::copy(F.piv.begin(), F.piv.end(), faci.begin() + n);
+      double* dfac = static_cast<double*>(d_fac.get(sizeof(double) * fac.size()));
+      int32_t* dfaci = static_cast<int32_t*>(d_faci.get(sizeof(int32_t) * faci.size()));
+      check(cudaMemcpyAsync(dfac, fac.data(), sizeof(double) * fac.size(), cudaMemcpyHostToDevice, st), "H2D");
+      check(cudaMemcpyAsync(dfaci, faci.data(), sizeof(int32_t) * faci.size(), cudaMemcpyHostToDevice, st), "H2D");
+      const size_t smem = sizeof(double) * 14 * n + sizeof(int32_t) * 2 * n;
+      check(cudaFuncSetAttribute(fit_axis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(smem)),
+            "smem attribute");
+      const int tb = 128;
+      fit_axis_kernel<<<static_cast<int>((nslices + tb - 1) / tb), tb, smem, st>>>(
+          FitAxisDev{n, inner, nslices}, dfac, dfaci, src, dst, tol, acc + axis, acc + 4 + axis);
+      check(cudaGetLastError(), "fit_axis_kernel launch");
+      // the host vectors must outlive the copies
+      check(cudaStreamSynchronize(st), "stream synchronize");
+    }
+    std::swap(src, dst);
+  }
+  unsigned long long h[8];
+  check(cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, st), "D2H");
+  check(cudaStreamSynchronize(st), "stream synchronize");
+  if (stats) {
+    for (int d = 0; d < 4; ++d) {
+      double r;
+      std::memcpy(&r, &h[d], sizeof(r));
+      stats->max_residual[d] = r;
+      stats->condition[d] = cond[d];
+      stats->failed_slices[d] = singular[d] ? static_cast<uint64_t>(total / sizes[d]) : h[4 + d];
+    }
+  }
+}
+
+uint64_t total_failed(const MangoGpuFitStats& s) {
+  return s.failed_slices[0] + s.failed_slices[1] + s.failed_slices[2] + s.failed_slices[3];
+}
+
+std::string check_fit_args(const double* grids, const int64_t* sizes, int64_t* total) {
+  if (!grids || !sizes) return "null grids or sizes";
+  *total = 1;
+  for (int d = 0; d < 4; ++d) {
+    if (sizes[d] < 4 || sizes[d] > kMaxAxis) return "each axis needs 4..512 grid points";
+    *total *= sizes[d];
+  }
+  return {};
+}
+
+}  // namespace
+}  // namespace mgpu
+
+struct MangoGpuPriceTable {
+  MangoGpuBSpline4D* surface = nullptr;
+  double K_ref = 0, q = 0;
+  int32_t option_type = 0;
+  int32_t eep = 1;
+  double bounds[8] = {};  // m, tau, sigma, rate: min, max
+  mgpu::DevBuf d_p, d_out;
+};
+
+using namespace mgpu;
+
+extern "C" {
+
+MangoStatus mango_gpu_bspline4d_fit(MangoGpuContext* ctx, const double* grids,
+                                    const int64_t* sizes, const double* values, double tolerance,
+                                    double* coeffs, MangoGpuFitStats* stats, MangoError* err) {
+  int64_t total = 0;
+  std::string bad = check_fit_args(grids, sizes, &total);
+  if (!ctx || !values || !coeffs) bad = "null argument";
+  if (!bad.empty()) {
+    set_err(err, MANGO_ERR_VALIDATION, bad);
+    return MANGO_ERR_VALIDATION;
+  }
+  for (int64_t i = 0; i < total; ++i)
+    if (!std::isfinite(values[i])) {
+      set_err(err, MANGO_ERR_VALIDATION, std::isnan(values[i]) ? "NaN input value" : "infinite input value");
+      return MANGO_ERR_VALIDATION;
+    }
+  DevBuf da, db;
+  try {
+    check(cudaSetDevice(ctx->device), "cudaSetDevice");
+    {  // BSplineNDSeparable::create validation: strictly increasing axes
+      std::vector<double> tab, kn;
+      BSplineDims D;
+      bspline_tables(grids, sizes, &D, &tab, &kn);
+    }
+    cudaStream_t st = ctx->stream;
+    double* a = static_cast<double*>(da.get(sizeof(double) * total));
+    double* b = static_cast<double*>(db.get(sizeof(double) * total));
+    check(cudaMemcpyAsync(a, values, sizeof(double) * total, cudaMemcpyHostToDevice, st), "H2D");
+    MangoGpuFitStats s{};
+    fit_device(ctx, grids, sizes, a, b, tolerance > 0.0 ? tolerance : 1e-6, &s);
+    check(cudaMemcpyAsync(coeffs, a, sizeof(double) * total, cudaMemcpyDeviceToHost, st), "D2H");
+    check(cudaStreamSynchronize(st), "stream synchronize");
+    da.release();
+    db.release();
+    if (stats) *stats = s;
+    if (total_failed(s) > 0) {
+      set_err(err, MANGO_ERR_SOLVER, "fitting failed: " + std::to_string(total_failed(s)) + " slices");
+      return MANGO_ERR_SOLVER;
+    }
+    return MANGO_OK;
+  } catch (const std::invalid_argument& e) {
+    da.release();
+    db.release();
+    set_err(err, MANGO_ERR_VALIDATION, e.what());
+    return MANGO_ERR_VALIDATION;
+  } catch (const std::exception& e) {
+    da.release();
+    db.release();
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+MangoStatus mango_gpu_price_table_create(MangoGpuContext* ctx, const double* grids,
+                                         const int64_t* sizes, const double* coeffs, double K_ref,
+                                         double dividend_yield, MangoOptionType option_type,
+                                         int32_t eep, MangoGpuPriceTable** out, MangoError* err) {
+  if (out) *out = nullptr;
+  MangoGpuBSpline4D* s = nullptr;
+  MangoStatus rc = mango_gpu_bspline4d_create(ctx, grids, sizes, coeffs, &s, err);
+  if (rc != MANGO_OK) return rc;
+  if (!out || !(K_ref > 0.0) || (option_type != MANGO_PUT && option_type != MANGO_CALL)) {
+    mango_gpu_bspline4d_destroy(s);
+    set_err(err, MANGO_ERR_VALIDATION, "invalid K_ref, option type or out");
+    return MANGO_ERR_VALIDATION;
+  }
+  MangoGpuPriceTable* t = new MangoGpuPriceTable();
+  t->surface = s;
+  t->K_ref = K_ref;
+  t->q = dividend_yield;
+  t->option_type = option_type;
+  t->eep = eep ? 1 : 0;
+  for (int d = 0; d < 4; ++d) {
+    t->bounds[2 * d] = s->dims.lo[d];
+    t->bounds[2 * d + 1] = s->dims.hi[d];
+  }
+  *out = t;
+  return MANGO_OK;
+}
+
+MangoStatus mango_gpu_price_table_build(
+    MangoGpuContext* ctx, const double* moneyness, uint64_t nm, const double* maturity,
+    uint64_t ntau, const double* volatility, uint64_t nsig, const double* rate, uint64_t nr,
+    double K_ref, double dividend_yield, MangoOptionType option_type, const MangoGpuGrid* grid,
+    int32_t eep, double tolerance, MangoGpuPriceTable** out, MangoGpuFitStats* stats,
+    uint64_t* out_failed_slices, MangoError* err) {
+  if (out) *out = nullptr;
+  std::string bad = check_table_args(moneyness, nm, maturity, ntau, volatility, nsig, rate, nr,
+                                     K_ref, dividend_yield, option_type);
+  if (bad.empty() && (!ctx || !out)) bad = "null argument";
+  const int64_t sizes[4] = {static_cast<int64_t>(nm), static_cast<int64_t>(ntau),
+                            static_cast<int64_t>(nsig), static_cast<int64_t>(nr)};
+  std::vector<double> grids;
+  if (bad.empty()) {
+    grids.insert(grids.end(), moneyness, moneyness + nm);
+    grids.insert(grids.end(), maturity, maturity + ntau);
+    grids.insert(grids.end(), volatility, volatility + nsig);
+    grids.insert(grids.end(), rate, rate + nr);
+    int64_t total = 0;
+    bad = check_fit_args(grids.data(), sizes, &total);
+  }
+  if (!bad.empty()) {
+    set_err(err, MANGO_ERR_VALIDATION, bad);
+    return MANGO_ERR_VALIDATION;
+  }
+  MangoGpuPriceTable* t = nullptr;
+  DevBuf da, db, dax;
+  try {
+    check(cudaSetDevice(ctx->device), "cudaSetDevice");
+    t = new MangoGpuPriceTable();
+    t->surface = new_surface(ctx, grids.data(), sizes);
+    t->K_ref = K_ref;
+    t->q = dividend_yield;
+    t->option_type = option_type;
+    t->eep = eep ? 1 : 0;
+    for (int d = 0; d < 4; ++d) {
+      t->bounds[2 * d] = t->surface->dims.lo[d];
+      t->bounds[2 * d + 1] = t->surface->dims.hi[d];
+    }
+    cudaStream_t st = ctx->stream;
+    const int64_t total = static_cast<int64_t>(nm * ntau * nsig * nr);
+    double* a = static_cast<double*>(da.get(sizeof(double) * total));
+    double* b = static_cast<double*>(db.get(sizeof(double) * total));
+    // Step 1: sweep + extraction into a.
+    const uint64_t failed = table_sweep_device(ctx, moneyness, nm, maturity, ntau, volatility, nsig,
+                                               rate, nr, K_ref, dividend_yield, option_type, grid,
+                                               a, nullptr);
+    if (out_failed_slices) *out_failed_slices = failed;
+    if (failed > 0)
+      throw std::runtime_error(std::to_string(failed) +
+                               " PDE slices failed (failed-slice repair is not supported)");
+    // Step 3: EEP decomposition.
+    if (t->eep) {
+      double* ax = static_cast<double*>(dax.get(sizeof(double) * grids.size()));
+      check(cudaMemcpyAsync(ax, grids.data(), sizeof(double) * grids.size(), cudaMemcpyHostToDevice, st), "H2D");
+      const int tb = 256;
+      eep_decompose_kernel<<<static_cast<int>((total + tb - 1) / tb), tb, 0, st>>>(
+          static_cast<int>(nm), static_cast<int>(ntau), static_cast<int>(nsig), static_cast<int>(nr),
+          ax, ax + nm, ax + nm + ntau, ax + nm + ntau + nsig, K_ref, dividend_yield,
+          option_type == MANGO_PUT ? 1 : 0, a);
+      check(cudaGetLastError(), "eep_decompose_kernel launch");
+    }
+    // Step 4: fit (results in a); step 5: the surface takes them over.
+    MangoGpuFitStats s{};
+    fit_device(ctx, grids.data(), sizes, a, b, tolerance > 0.0 ? tolerance : 1e-6, &s);
+    if (stats) *stats = s;
+    if (total_failed(s) > 0)
+      throw std::runtime_error("fitting failed: " + std::to_string(total_failed(s)) + " slices");
+    std::swap(t->surface->d_coeffs.p, da.p);
+    std::swap(t->surface->d_coeffs.cap, da.cap);
+    db.release();
+    da.release();
+    dax.release();
+    *out = t;
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    da.release();
+    db.release();
+    dax.release();
+    if (t) {
+      if (t->surface) mango_gpu_bspline4d_destroy(t->surface);
+      delete t;
+    }
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+MangoStatus mango_gpu_eep_decompose(MangoGpuContext* ctx, const double* moneyness, uint64_t nm,
+                                    const double* maturity, uint64_t ntau,
+                                    const double* volatility, uint64_t nsig, const double* rate,
+                                    uint64_t nr, double K_ref, double dividend_yield,
+                                    MangoOptionType option_type, double* tensor, MangoError* err) {
+  std::string bad = check_table_args(moneyness, nm, maturity, ntau, volatility, nsig, rate, nr,
+                                     K_ref, dividend_yield, option_type);
+  if (bad.empty() && (!ctx || !tensor)) bad = "null argument";
+  if (!bad.empty()) {
+    set_err(err, MANGO_ERR_VALIDATION, bad);
+    return MANGO_ERR_VALIDATION;
+  }
+  DevBuf dt, dax;
+  try {
+    check(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    const int64_t total = static_cast<int64_t>(nm * ntau * nsig * nr);
+    std::vector<double> ax;
+    ax.insert(ax.end(), moneyness, moneyness + nm);
+    ax.insert(ax.end(), maturity, maturity + ntau);
+    ax.insert(ax.end(), volatility, volatility + nsig);
+    ax.insert(ax.end(), rate, rate + nr);
+    double* d = static_cast<double*>(dt.get(sizeof(double) * total));
+    double* a = static_cast<double*>(dax.get(sizeof(double) * ax.size()));
+    check(cudaMemcpyAsync(d, tensor, sizeof(double) * total, cudaMemcpyHostToDevice, st), "H2D");
+    check(cudaMemcpyAsync(a, ax.data(), sizeof(double) * ax.size(), cudaMemcpyHostToDevice, st), "H2D");
+    const int tb = 256;
+    eep_decompose_kernel<<<static_cast<int>((total + tb - 1) / tb), tb, 0, st>>>(
+        static_cast<int>(nm), static_cast<int>(ntau), static_cast<int>(nsig), static_cast<int>(nr), a,
+        a + nm, a + nm + ntau, a + nm + ntau + nsig, K_ref, dividend_yield,
+        option_type == MANGO_PUT ? 1 : 0, d);
+    check(cudaGetLastError(), "eep_decompose_kernel launch");
+    check(cudaMemcpyAsync(tensor, d, sizeof(double) * total, cudaMemcpyDeviceToHost, st), "D2H");
+    check(cudaStreamSynchronize(st), "stream synchronize");
+    dt.release();
+    dax.release();
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    dt.release();
+    dax.release();
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+void mango_gpu_price_table_destroy(MangoGpuPriceTable* t) {
+  if (!t) return;
+  if (t->surface) {
+    cudaSetDevice(t->surface->ctx->device);
+    cudaStreamSynchronize(t->surface->ctx->stream);
+  }
+  t->d_p.release();
+  t->d_out.release();
+  if (t->surface) mango_gpu_bspline4d_destroy(t->surface);
+  delete t;
+}
+
+MangoGpuBSpline4D* mango_gpu_price_table_spline(MangoGpuPriceTable* t) {
+  return t ? t->surface : nullptr;
+}
+
+MangoStatus mango_gpu_price_table_info(const MangoGpuPriceTable* t, double* K_ref,
+                                       double* dividend_yield, int32_t* option_type,
+                                       int32_t* eep, double* bounds8) {
+  if (!t) return MANGO_ERR_VALIDATION;
+  if (K_ref) *K_ref = t->K_ref;
+  if (dividend_yield) *dividend_yield = t->q;
+  if (option_type) *option_type = t->option_type;
+  if (eep) *eep = t->eep;
+  if (bounds8) std::memcpy(bounds8, t->bounds, sizeof(t->bounds));
+  return MANGO_OK;
+}
+
+MangoStatus mango_gpu_price_table_price_device(MangoGpuPriceTable* t,
+                                               const MangoPricingParams* d_params, uint64_t n,
+                                               double* d_out, MangoError* err) {
+  if (!t || (n > 0 && (!d_params || !d_out))) {
+    set_err(err, MANGO_ERR_VALIDATION, "null argument");
+    return MANGO_ERR_VALIDATION;
+  }
+  if (n == 0) return MANGO_OK;
+  try {
+    MangoGpuBSpline4D* s = t->surface;
+    check(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    const int64_t need = static_cast<int64_t>((n + 255) / 256);
+    const int blocks = static_cast<int>(std::min<int64_t>(s->blocks, need));
+    surface_price_kernel<<<blocks, 256, sizeof(double) * 4 * s->dims.ktot, s->ctx->stream>>>(
+        s->dims, s->d_tables.as<double>(), s->d_coeffs.as<double>(), d_params,
+        static_cast<int64_t>(n), t->K_ref, t->q, t->option_type == MANGO_PUT ? 1 : 0, t->eep, d_out);
+    check(cudaGetLastError(), "surface_price_kernel launch");
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+MangoStatus mango_gpu_price_table_price(MangoGpuPriceTable* t, const MangoPricingParams* params,
+                                        uint64_t n, double* out, MangoError* err) {
+  if (!t || (n > 0 && (!params || !out))) {
+    set_err(err, MANGO_ERR_VALIDATION, "null argument");
+    return MANGO_ERR_VALIDATION;
+  }
+  if (n == 0) return MANGO_OK;
+  try {
+    MangoGpuBSpline4D* s = t->surface;
+    check(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    cudaStream_t st = s->ctx->stream;
+    MangoPricingParams* dp = static_cast<MangoPricingParams*>(t->d_p.get(sizeof(MangoPricingParams) * n));
+    double* dout = static_cast<double*>(t->d_out.get(sizeof(double) * n));
+    check(cudaMemcpyAsync(dp, params, sizeof(MangoPricingParams) * n, cudaMemcpyHostToDevice, st), "H2D");
+    MangoStatus rc = mango_gpu_price_table_price_device(t, dp, n, dout, err);
+    if (rc != MANGO_OK) return rc;
+    check(cudaMemcpyAsync(out, dout, sizeof(double) * n, cudaMemcpyDeviceToHost, st), "D2H");
+    check(cudaStreamSynchronize(st), "stream synchronize");
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+}  // extern "C"

@@ -189,35 +189,40 @@ __global__ void resample_kernel(int nslices, int ntau, int nm, int ns, int nr,
   }
 }
 
-}  // namespace mgpu
-
-using namespace mgpu;
-
-extern "C" MangoStatus mango_gpu_price_table_sweep(
-    MangoGpuContext* ctx, const double* moneyness, uint64_t nm, const double* maturity,
-    uint64_t ntau, const double* volatility, uint64_t nsig, const double* rate, uint64_t nr,
-    double K_ref, double dividend_yield, MangoOptionType option_type, const MangoGpuGrid* grid,
-    double* tensor, int64_t* slice_dims, uint64_t* out_failed_slices, MangoError* err) {
-  if (!ctx || !moneyness || !maturity || !volatility || !rate || !tensor) {
-    set_err(err, MANGO_ERR_VALIDATION, "null argument");
-    return MANGO_ERR_VALIDATION;
-  }
-  if (nm < 1 || ntau < 1 || nsig < 1 || nr < 1 || nsig * nr > (1u << 24)) {
-    set_err(err, MANGO_ERR_VALIDATION, "empty or oversized axis");
-    return MANGO_ERR_VALIDATION;
-  }
+// Argument checks of the sweep (PriceTableBuilderND<4>::from_vectors and
+// make_batch preconditions, bspline_builder.cpp:198-226, 533-620); empty
+// string when the arguments are accepted.
+std::string check_table_args(const double* moneyness, uint64_t nm, const double* maturity,
+                             uint64_t ntau, const double* volatility, uint64_t nsig,
+                             const double* rate, uint64_t nr, double K_ref, double dividend_yield,
+                             MangoOptionType option_type) {
+  if (!moneyness || !maturity || !volatility || !rate) return "null axis";
+  if (nm < 1 || ntau < 1 || nsig < 1 || nr < 1 || nsig * nr > (1u << 24))
+    return "empty or oversized axis";
   if (!(K_ref > 0.0) || dividend_yield < 0.0 ||
-      (option_type != MANGO_PUT && option_type != MANGO_CALL)) {
-    set_err(err, MANGO_ERR_VALIDATION, "invalid K_ref, dividend yield or option type");
-    return MANGO_ERR_VALIDATION;
-  }
+      (option_type != MANGO_PUT && option_type != MANGO_CALL))
+    return "invalid K_ref, dividend yield or option type";
   for (uint64_t i = 1; i < ntau; ++i)
-    if (!(maturity[i] > maturity[i - 1])) {
-      set_err(err, MANGO_ERR_VALIDATION, "maturity axis must be strictly increasing");
-      return MANGO_ERR_VALIDATION;
-    }
+    if (!(maturity[i] > maturity[i - 1])) return "maturity axis must be strictly increasing";
+  return {};
+}
+
+// The sweep with the tensor left on the device (dten: nm*ntau*nsig*nr
+// doubles, [m][tau][sigma][r], NaN for failed slices).  Returns the number of
+// failed slices; throws on a CUDA or argument error.
+uint64_t table_sweep_device(MangoGpuContext* ctx, const double* moneyness, uint64_t nm,
+                            const double* maturity, uint64_t ntau, const double* volatility,
+                            uint64_t nsig, const double* rate, uint64_t nr, double K_ref,
+                            double dividend_yield, MangoOptionType option_type,
+                            const MangoGpuGrid* grid, double* dten, int64_t* slice_dims) {
   MangoGpuBatch* b = nullptr;
-  try {
+  struct Guard {
+    MangoGpuBatch** b;
+    ~Guard() {
+      if (*b) destroy_batch(*b);
+    }
+  } guard{&b};
+  {
     check(cudaSetDevice(ctx->device), "cudaSetDevice");
     const double T = maturity[ntau - 1];
     // make_batch: (sigma, r) cartesian product, sigma outer (bspline_builder.cpp:214-226).
@@ -346,7 +351,7 @@ extern "C" MangoStatus mango_gpu_price_table_sweep(
     uint64_t failed = 0;
     if (m > 0) {
       cudaStream_t st = ctx->stream;
-      DevBuf d_sidx, d_sbegin, d_scount, d_soff, d_snaps, d_slice, d_m, d_scratch, d_tensor;
+      DevBuf d_sidx, d_sbegin, d_scount, d_soff, d_snaps, d_slice, d_m, d_scratch;
       int32_t* dsidx = static_cast<int32_t*>(d_sidx.get(sizeof(int32_t) * std::max<size_t>(sidx.size(), 1)));
       int32_t* dsb = static_cast<int32_t*>(d_sbegin.get(sizeof(int32_t) * m));
       int32_t* dsc = static_cast<int32_t*>(d_scount.get(sizeof(int32_t) * m));
@@ -357,8 +362,6 @@ extern "C" MangoStatus mango_gpu_price_table_sweep(
       const int64_t work = ns * static_cast<int64_t>(ntau);
       const int64_t stride = 3 * static_cast<int64_t>(max_n);
       double* dscr = static_cast<double*>(d_scratch.get(sizeof(double) * stride * work));
-      const size_t tensor_n = nm * ntau * nsig * nr;
-      double* dten = static_cast<double*>(d_tensor.get(sizeof(double) * tensor_n));
       check(cudaMemcpyAsync(dsidx, sidx.data(), sizeof(int32_t) * sidx.size(), cudaMemcpyHostToDevice, st), "H2D");
       check(cudaMemcpyAsync(dsb, sbegin.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, st), "H2D");
       check(cudaMemcpyAsync(dsc, scount.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, st), "H2D");
@@ -379,25 +382,58 @@ extern "C" MangoStatus mango_gpu_price_table_sweep(
           b->d_xs.as<double>(), b->d_tiles.as<TileDev>(), b->d_status.as<int32_t>(), dsc, dso,
           dsnap, dm, dscr, stride, dten);
       check(cudaGetLastError(), "resample_kernel launch");
-      check(cudaMemcpyAsync(tensor, dten, sizeof(double) * tensor_n, cudaMemcpyDeviceToHost, st), "D2H tensor");
       std::vector<int32_t> hst(static_cast<size_t>(m));
       check(cudaMemcpyAsync(hst.data(), b->d_status.p, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, st), "D2H");
       check(cudaStreamSynchronize(st), "stream synchronize");
       for (int64_t k = 0; k < m; ++k) failed += hst[k] != kStatusOk;
-      for (DevBuf* d : {&d_sidx, &d_sbegin, &d_scount, &d_soff, &d_snaps, &d_slice, &d_m, &d_scratch, &d_tensor})
+      for (DevBuf* d : {&d_sidx, &d_sbegin, &d_scount, &d_soff, &d_snaps, &d_slice, &d_m, &d_scratch})
         d->release();
     }
+    if (m == 0)  // no slice reached the device: every tensor entry is NaN
+      check(cudaMemsetAsync(dten, 0xFF, sizeof(double) * nm * ntau * nsig * nr, ctx->stream),
+            "memset tensor");
     failed += static_cast<uint64_t>(ns - m);
     if (slice_dims)
       for (int64_t s = 0; s < ns; ++s) {
         slice_dims[2 * s] = b->res[s].status == 0 ? b->res[s].spec.n : -1;
         slice_dims[2 * s + 1] = b->res[s].status == 0 ? b->res[s].nt : -1;
       }
+    return failed;
+  }
+}
+
+}  // namespace mgpu
+
+using namespace mgpu;
+
+extern "C" MangoStatus mango_gpu_price_table_sweep(
+    MangoGpuContext* ctx, const double* moneyness, uint64_t nm, const double* maturity,
+    uint64_t ntau, const double* volatility, uint64_t nsig, const double* rate, uint64_t nr,
+    double K_ref, double dividend_yield, MangoOptionType option_type, const MangoGpuGrid* grid,
+    double* tensor, int64_t* slice_dims, uint64_t* out_failed_slices, MangoError* err) {
+  const std::string bad = check_table_args(moneyness, nm, maturity, ntau, volatility, nsig, rate,
+                                           nr, K_ref, dividend_yield, option_type);
+  if (!ctx || !tensor || !bad.empty()) {
+    set_err(err, MANGO_ERR_VALIDATION, bad.empty() ? "null argument" : bad);
+    return MANGO_ERR_VALIDATION;
+  }
+  DevBuf d_tensor;
+  try {
+    check(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const size_t tensor_n = nm * ntau * nsig * nr;
+    double* dten = static_cast<double*>(d_tensor.get(sizeof(double) * tensor_n));
+    const uint64_t failed =
+        table_sweep_device(ctx, moneyness, nm, maturity, ntau, volatility, nsig, rate, nr, K_ref,
+                           dividend_yield, option_type, grid, dten, slice_dims);
+    check(cudaMemcpyAsync(tensor, dten, sizeof(double) * tensor_n, cudaMemcpyDeviceToHost,
+                          ctx->stream),
+          "D2H tensor");
+    check(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    d_tensor.release();
     if (out_failed_slices) *out_failed_slices = failed;
-    destroy_batch(b);
     return MANGO_OK;
   } catch (const std::exception& e) {
-    if (b) destroy_batch(b);
+    d_tensor.release();
     set_err(err, MANGO_ERR_SOLVER, e.what());
     return MANGO_ERR_SOLVER;
   }

@@ -16,6 +16,9 @@
 #include "mango/math/bspline/bspline_nd.hpp"
 #include "mango/math/bspline/bspline_basis.hpp"
 #include "mango/option/table/bspline/bspline_builder.hpp"
+#include "mango/option/table/bspline/bspline_surface.hpp"
+#include "mango/option/table/bspline/bspline_tensor_accessor.hpp"
+#include "mango/option/table/eep/eep_decomposer.hpp"
 
 #include <omp.h>
 #include <cmath>
@@ -290,6 +293,62 @@ int32_t ref_table_sweep(const double* m, int64_t nm, const double* tau, int64_t 
       for (int64_t k = 0; k < ns; ++k)
         for (int64_t l = 0; l < nr; ++l)
           out[((i * ntau + j) * ns + k) * nr + l] = ext->tensor.view[i, j, k, l];
+  return 0;
+}
+
+// Standard price table over given spline coefficients
+// (make_bspline_surface, src/option/table/bspline/bspline_surface.cpp:9-37)
+// and its price(spot, strike, tau, sigma, rate) (EEPLayer over TransformLeaf).
+// p: n x 5 records {spot, strike, tau, sigma, rate}.
+int32_t ref_surface_price(const int64_t* sizes, const double* grids, const double* coeffs,
+                          double K_ref, double q, int32_t is_put, const double* p, int64_t n,
+                          double* out) {
+  std::array<std::vector<double>, 4> g, k;
+  size_t off = 0, total = 1;
+  for (int d = 0; d < 4; ++d) {
+    g[d].assign(grids + off, grids + off + sizes[d]);
+    off += static_cast<size_t>(sizes[d]);
+    k[d] = clamped_knots_cubic(g[d]);
+    total *= static_cast<size_t>(sizes[d]);
+  }
+  std::vector<double> c(coeffs, coeffs + total);
+  auto sp = BSplineND<double, 4>::create(g, k, std::move(c));
+  if (!sp) return 1;
+  auto shared = std::make_shared<const BSplineND<double, 4>>(std::move(sp.value()));
+  auto table = make_bspline_surface(shared, K_ref, q, is_put ? OptionType::PUT : OptionType::CALL);
+  if (!table) return 2;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i)
+    out[i] = table->price(p[5 * i], p[5 * i + 1], p[5 * i + 2], p[5 * i + 3], p[5 * i + 4]);
+  return 0;
+}
+
+// eep_decompose over BSplineTensorAccessor with AnalyticalEEP
+// (src/option/table/eep/eep_decomposer.hpp:60-80): tensor [m][tau][sigma][r]
+// of V/K_ref in, EEP out, in place.
+int32_t ref_eep_decompose(const double* m, int64_t nm, const double* tau, int64_t ntau,
+                          const double* sig, int64_t ns, const double* rr, int64_t nr,
+                          double K_ref, double q, int32_t is_put, double* tensor) {
+  PriceTableAxesND<4> axes;
+  axes.grids[0].assign(m, m + nm);
+  axes.grids[1].assign(tau, tau + ntau);
+  axes.grids[2].assign(sig, sig + ns);
+  axes.grids[3].assign(rr, rr + nr);
+  auto t = PriceTensorND<4>::create({static_cast<size_t>(nm), static_cast<size_t>(ntau),
+                                     static_cast<size_t>(ns), static_cast<size_t>(nr)});
+  if (!t) return 1;
+  for (int64_t i = 0; i < nm; ++i)
+    for (int64_t j = 0; j < ntau; ++j)
+      for (int64_t a = 0; a < ns; ++a)
+        for (int64_t l = 0; l < nr; ++l)
+          t->view[i, j, a, l] = tensor[((i * ntau + j) * ns + a) * nr + l];
+  BSplineTensorAccessor acc(*t, axes, K_ref);
+  eep_decompose(acc, AnalyticalEEP(is_put ? OptionType::PUT : OptionType::CALL, q));
+  for (int64_t i = 0; i < nm; ++i)
+    for (int64_t j = 0; j < ntau; ++j)
+      for (int64_t a = 0; a < ns; ++a)
+        for (int64_t l = 0; l < nr; ++l)
+          tensor[((i * ntau + j) * ns + a) * nr + l] = t->view[i, j, a, l];
   return 0;
 }
 

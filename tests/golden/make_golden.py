@@ -27,6 +27,11 @@ every output value):
                      (12 x 6 x 5 x 3) for the explicit 201 x 1000 grid (the
                      reference's per-slice fallback route) and the default
                      accuracy route, with each slice's (N_x, N_t)
+  surface.npz        the standard price table (make_bspline_surface: EEPLayer
+                     over TransformLeaf) on 12 x 8 x 6 x 5 axes with seeded
+                     coefficients: 2048 price queries (some outside the axes)
+                     for a put and a call table; and eep_decompose
+                     (AnalyticalEEP) of a seeded V/K_ref tensor on the same axes
 """
 from __future__ import annotations
 
@@ -228,6 +233,7 @@ def main():
 
     golden_bspline(lib)
     golden_table(lib)
+    golden_surface(lib)
 
 
 def table_axes(nm, ntau, ns, nr):
@@ -280,6 +286,34 @@ def golden_table(lib):
         res[f"{name}_tensor"] = out.reshape(nm, nt, ns, nr)
         res[f"{name}_dims"] = dims.reshape(ns * nr, 2)
     save("table.npz", m=axes[0], tau=axes[1], sigma=axes[2], r=axes[3], **res)
+
+
+def golden_surface(lib):
+    axes = table_axes(12, 8, 6, 5)
+    sizes = np.array([a.size for a in axes], np.int64)
+    grids = np.concatenate(axes)
+    rng = np.random.default_rng(2026)
+    coeffs = rng.standard_normal(int(np.prod(sizes))) * 2.0 + 0.5
+    n = 2048
+    p = np.stack([rng.uniform(80, 120, n), rng.uniform(80, 120, n), rng.uniform(0.005, 2.1, n),
+                  rng.uniform(0.04, 0.85, n), rng.uniform(-0.005, 0.085, n)], 1)
+    p = np.ascontiguousarray(p)
+    res = {}
+    for name, put, q in (("put", 1, 0.015), ("call", 0, 0.03)):
+        out = np.zeros(n)
+        rc = lib.ref_surface_price(P(sizes), P(grids), P(coeffs), ctypes.c_double(100.0), ctypes.c_double(q),
+                                   ctypes.c_int32(put), P(p), ctypes.c_int64(n), P(out))
+        assert rc == 0
+        res[f"{name}_price"] = out
+        res[f"{name}_q"] = np.array(q)
+    nm, nt, ns, nr = (a.size for a in axes)
+    ten = np.ascontiguousarray(rng.uniform(0.0, 0.45, nm * nt * ns * nr))
+    eep = ten.copy()
+    rc = lib.ref_eep_decompose(P(axes[0]), ctypes.c_int64(nm), P(axes[1]), ctypes.c_int64(nt), P(axes[2]),
+                               ctypes.c_int64(ns), P(axes[3]), ctypes.c_int64(nr), ctypes.c_double(100.0),
+                               ctypes.c_double(0.015), ctypes.c_int32(1), P(eep))
+    assert rc == 0
+    save("surface.npz", sizes=sizes, grids=grids, coeffs=coeffs, params=p, eep_in=ten, eep_out=eep, **res)
 
 
 if __name__ == "__main__":

@@ -107,3 +107,28 @@ def iv_batch(S, K, T, r, q, is_put, price, grid_sigma, nx, nt, threads=0):
     lib().mo_iv_batch(ctypes.c_int64(n), *(P(a) for a in f), P(put), P(px), P(gs), P(nx), P(nt),
                       ctypes.c_int32(threads), P(out), P(st))
     return out.reshape(n, 3), st
+
+
+def bspline4d_eval(axes, coeffs, q):
+    """BSplineND<double,4>::eval of the C restatement (mo_bspline4d_eval)."""
+    sizes = np.array([len(a) for a in axes], np.int64)
+    grids = np.ascontiguousarray(np.concatenate([np.asarray(a, np.float64) for a in axes]))
+    c = np.ascontiguousarray(coeffs, dtype=np.float64).ravel()
+    q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, 4)
+    out = np.zeros(q.shape[0])
+    rc = lib().mo_bspline4d_eval(P(sizes), P(grids), P(c), P(q), ctypes.c_int64(q.shape[0]), P(out))
+    assert rc == 0
+    return out
+
+
+def surface_price(axes, coeffs, params, K_ref, q, put, eep=True):
+    """AnyPriceTable::price restated: max(0, spline(log(S/K), tau, sigma, r)) K/K_ref
+    plus the European price (params: n x 5 {S, K, tau, sigma, r})."""
+    import fit_oracle
+    p = np.asarray(params, np.float64).reshape(-1, 5)
+    x = np.stack([np.log(p[:, 0] / p[:, 1]), p[:, 2], p[:, 3], p[:, 4]], 1)
+    raw = bspline4d_eval(axes, coeffs, x)
+    v = np.maximum(0.0, raw) * p[:, 1] / K_ref
+    if eep:
+        v = v + np.array([fit_oracle.european_price(*row, q, bool(put)) for row in p])
+    return v

@@ -1,0 +1,168 @@
+"""GPU price-table surface: the separable collocation fit, the EEP step, the
+standard table's price query and the whole device-resident build, against the
+reference's golden outputs (surface.npz) and the CPU restatement
+(oracle/fit_oracle.py, pinned in test_oracle_surface.py).
+
+Bars: prices 1e-12 relative against the reference on the same coefficients;
+EEP 1e-12 absolute; fit coefficients within cond(B) x 1e-14 of the dense
+restatement (LAPACK boundary, parity otherwise unpinned); cubic
+reproduction 1e-11."""
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden
+
+sys.path.insert(0, str(ROOT / "oracle"))
+import fit_oracle  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def axes_of(g):
+    return np.split(g["grids"], np.cumsum(g["sizes"])[:-1])
+
+
+def records(pkg, p, put, q):
+    return pkg.pricing_array(p[:, 0], p[:, 1], p[:, 2], p[:, 3], p[:, 4], q, put)
+
+
+def test_table_price_vs_reference(engine, pkg):
+    g = golden("surface.npz")
+    axes = axes_of(g)
+    for name, put in (("put", 1), ("call", 0)):
+        q = float(g[f"{name}_q"])
+        t = engine.price_table_create(axes, g["coeffs"], 100.0, q, put, eep=True)
+        v = t.price_arrays(records(pkg, g["params"], put, q))
+        ref = g[f"{name}_price"]
+        assert np.abs(v - ref).max() <= 1e-12 * np.abs(ref).max() + 1e-13, name
+        t.close()
+
+
+def test_table_without_eep_is_the_transform_leaf(engine, pkg, oracle):
+    g = golden("surface.npz")
+    axes = axes_of(g)
+    t = engine.price_table_create(axes, g["coeffs"], 100.0, 0.0, 1, eep=False)
+    v = t.price_arrays(records(pkg, g["params"], 1, 0.0))
+    ref = oracle.surface_price(axes, g["coeffs"], g["params"], 100.0, 0.0, 1, eep=False)
+    assert np.abs(v - ref).max() <= 1e-13 * np.abs(ref).max() + 1e-14
+    assert (v >= 0).all()
+
+
+def test_eep_decompose_vs_reference(engine):
+    g = golden("surface.npz")
+    axes = axes_of(g)
+    out = engine.eep_decompose(*axes, g["eep_in"], K_ref=100.0, dividend_yield=0.015, option_type=1)
+    assert np.abs(out.ravel() - g["eep_out"]).max() < 1e-12
+
+
+def cubic(a, b, c, d):
+    return 1 + a - 2 * a ** 3 + 0.5 * b ** 2 * c - c ** 3 + 3 * d * a ** 2 + b ** 3 * d
+
+
+def test_fit_reproduces_cubics(engine, oracle):
+    axes = [np.linspace(-0.4, 0.3, 11) + 0.01 * np.arange(11) ** 2, np.linspace(0.02, 2.0, 9),
+            np.linspace(0.05, 0.8, 7), np.linspace(0.0, 0.08, 5)]
+    mesh = np.meshgrid(*axes, indexing="ij")
+    coeffs, stats = engine.bspline4d_fit(axes, cubic(*mesh))
+    assert stats["failed_slices"] == [0, 0, 0, 0]
+    assert max(stats["max_residual"]) < 1e-12
+    rng = np.random.default_rng(11)
+    q = np.stack([rng.uniform(a[0], a[-1], 2000) for a in axes], 1)
+    surf = engine.bspline4d(axes, coeffs)
+    assert np.abs(surf.eval(q) - cubic(*q.T)).max() < 1e-11
+    assert np.abs(oracle.bspline4d_eval(axes, coeffs, q) - cubic(*q.T)).max() < 1e-11
+
+
+def test_fit_vs_dense_restatement(engine):
+    g = golden("surface.npz")
+    axes = axes_of(g)
+    vals = np.random.default_rng(3).standard_normal([a.size for a in axes])
+    coeffs, stats = engine.bspline4d_fit(axes, vals)
+    ref = fit_oracle.fit4d(axes, vals)
+    conds = [np.linalg.cond(fit_oracle.collocation_matrix(a), 1) for a in axes]
+    assert np.allclose(stats["condition"], conds, rtol=1e-9)
+    bound = np.prod(conds) * 1e-14 * np.abs(ref).max()
+    assert np.abs(coeffs - ref).max() <= bound, (np.abs(coeffs - ref).max(), bound)
+
+
+def test_fit_failure_and_validation(engine, pkg):
+    axes = [np.linspace(0, 1, 6), np.linspace(0, 1, 5), np.linspace(0, 1, 4), np.linspace(0, 1, 4)]
+    vals = np.random.default_rng(1).standard_normal([6, 5, 4, 4])
+    with pytest.raises(pkg.EngineError) as e:
+        engine.bspline4d_fit(axes, vals, tolerance=1e-300)
+    assert e.value.status == pkg.MANGO_ERR_SOLVER and sum(e.value.stats["failed_slices"]) > 0
+    bad = vals.copy()
+    bad[1, 2, 3, 0] = np.nan
+    with pytest.raises(pkg.EngineError) as e:
+        engine.bspline4d_fit(axes, bad)
+    assert e.value.status == pkg.MANGO_ERR_VALIDATION
+    with pytest.raises(pkg.EngineError):
+        engine.bspline4d_fit([np.linspace(0, 1, 3)] + axes[1:], np.zeros([3, 5, 4, 4]))
+
+
+TABLE_AXES = (np.linspace(np.log(0.7), np.log(1.3), 10), np.linspace(0.05, 1.5, 7),
+              np.linspace(0.1, 0.6, 5), np.linspace(0.0, 0.06, 4))
+
+
+def test_table_build_vs_restated_pipeline(engine, pkg, oracle):
+    """Device build (sweep -> EEP -> fit -> surface) against the CPU
+    composition of the same stages: the GPU sweep tensor (pinned to the
+    reference in test_gpu_table.py), the restated EEP and fit, the C
+    B-spline evaluation and the European add-back."""
+    grid = pkg.PDEGridConfig(-3.0, 3.0, 101, 200)
+    q = 0.01
+    table, stats = engine.price_table_build(*TABLE_AXES, K_ref=100.0, dividend_yield=q, option_type=1,
+                                            grid=grid, eep=True)
+    assert stats["failed_slices"] == [0, 0, 0, 0] and stats["failed_pde_slices"] == 0
+    tensor, _, failed = engine.price_table_sweep(*TABLE_AXES, 100.0, q, 1, grid)
+    assert failed == 0
+    eep = fit_oracle.eep_decompose(TABLE_AXES, tensor, 100.0, q, True)
+    coeffs = fit_oracle.fit4d(TABLE_AXES, eep)
+    rng = np.random.default_rng(9)
+    n = 512
+    p = np.stack([np.full(n, 100.0), 100.0 / np.exp(rng.uniform(TABLE_AXES[0][0], TABLE_AXES[0][-1], n)),
+                  rng.uniform(0.05, 1.5, n), rng.uniform(0.1, 0.6, n), rng.uniform(0.0, 0.06, n)], 1)
+    got = table.price_arrays(records(pkg, p, 1, q))
+    ref = oracle.surface_price(TABLE_AXES, coeffs, p, 100.0, q, 1)
+    assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max()
+    # the mirror's validated scalar price
+    pp = pkg.PricingParams(spot=100.0, strike=float(p[0, 1]), maturity=float(p[0, 2]), rate=float(p[0, 4]),
+                           dividend_yield=q, option_type=pkg.OptionType.PUT, volatility=float(p[0, 3]))
+    assert abs(table.price(pp) - got[0]) < 1e-12 * abs(got[0]) + 1e-14
+    with pytest.raises(ValueError):
+        table.price(pkg.PricingParams(spot=100.0, strike=100.0, maturity=5.0, rate=0.01, dividend_yield=q,
+                                      option_type=pkg.OptionType.PUT, volatility=0.2))
+    table.close()
+
+
+def test_table_build_interpolates_at_nodes(engine, pkg):
+    """At the table's nodes the surface returns the PDE price it was built
+    from, through the EEP floor: K/K_ref (eep_floor(K_ref u - E) + E), with
+    u the normalised PDE price and E the European price at K_ref."""
+    grid = pkg.PDEGridConfig(-3.0, 3.0, 101, 200)
+    table, _ = engine.price_table_build(*TABLE_AXES, K_ref=100.0, dividend_yield=0.0, option_type=1, grid=grid)
+    tensor, _, _ = engine.price_table_sweep(*TABLE_AXES, 100.0, 0.0, 1, grid)
+    for mi, ti, vi, ri in ((0, 3, 2, 1), (5, 3, 2, 1), (9, 6, 4, 3), (2, 0, 0, 0)):
+        m, tau, sig, r = (TABLE_AXES[d][i] for d, i in enumerate((mi, ti, vi, ri)))
+        K = 100.0 / np.exp(m)
+        e = fit_oracle.european_price(100.0 * np.exp(m), 100.0, tau, sig, r, 0.0, True)
+        want = K / 100.0 * (fit_oracle.eep_floor(100.0 * tensor[mi, ti, vi, ri] - e) + e)
+        v = table.price_arrays(pkg.pricing_array(100.0, K, tau, sig, r, 0.0, 1))[0]
+        assert abs(v - want) < 1e-9 * K, (mi, ti, vi, ri, v, want)
+    table.close()
+
+
+def test_make_price_table_mirror(engine, pkg):
+    cfg = pkg.IVSolverFactoryConfig(option_type=pkg.OptionType.PUT, spot=100.0, dividend_yield=0.0,
+                                    grid=pkg.IVGrid(moneyness=np.linspace(0.8, 1.2, 8), vol=[0.15, 0.25, 0.35, 0.45],
+                                                    rate=[0.0, 0.02, 0.04, 0.06]),
+                                    backend=pkg.BSplineBackend(maturity_grid=[0.25, 0.5, 0.75, 1.0, 1.5]))
+    t = pkg.make_price_table(cfg, engine)
+    assert t.surface_type == "bspline" and t.option_type == pkg.OptionType.PUT
+    p = pkg.PricingParams(spot=100.0, strike=100.0, maturity=1.0, rate=0.03, dividend_yield=0.0,
+                          option_type=pkg.OptionType.PUT, volatility=0.25)
+    direct = pkg.american_option_price(p).value()
+    assert abs(t.price(p) - direct) < 0.02 * direct
+    t.close()

@@ -86,6 +86,14 @@ typedef struct {
 typedef struct { double brent_tol_abs; int32_t max_iter; } MangoIvConfig;
 
 typedef struct {
+  uint64_t max_iter;
+  double tolerance;
+  double sigma_min;
+  double sigma_max;
+  double vega_threshold;
+} MangoInterpSolverConfig;
+
+typedef struct {
   int32_t status;
   MangoIvSuccess success;
 } MangoIvBatchSlot;
@@ -347,6 +355,38 @@ MangoStatus mango_gpu_price_table_price(MangoGpuPriceTable* table, const MangoPr
 MangoStatus mango_gpu_price_table_price_device(MangoGpuPriceTable* table,
                                                const MangoPricingParams* d_params, uint64_t n,
                                                double* d_out, MangoError* err);
+/* AnyPriceTable::vega (EEPLayer::vega over TransformLeaf::vega,
+ * src/option/table/eep/eep_layer.hpp:27-31, transform_leaf.hpp:35-47): the
+ * spline's analytic partial along the volatility axis times K/K_ref where
+ * the spline value is positive, plus the closed-form European vega when
+ * the table has EEP.  Constant rates only (NaN otherwise). */
+MangoStatus mango_gpu_price_table_vega(MangoGpuPriceTable* table, const MangoPricingParams* params,
+                                       uint64_t n, double* out, MangoError* err);
+
+/* Interpolated implied volatility on the table:
+ * InterpolatedIVSolver::solve_batch (src/option/interpolated_iv_solver.hpp:
+ * 427-560), the batch analogue of mango_interp_iv_solve_batch
+ * (src/ffi/mango_c_api.cpp:523-576).  Per quote: the reference's checks
+ * (option type and dividend yield must match the table; validate_iv_query),
+ * the adaptive volatility bracket, the axis-range check, the vega pre-check
+ * at volatilities 0.10 / 0.25 / 0.50 against vega_threshold, then Brent on
+ * table price - market price.  config NULL => the reference defaults
+ * (max_iter 50, tolerance 1e-6, sigma 0.01 .. 3.0, vega_threshold 1e-4);
+ * fields are applied verbatim otherwise.  Slot statuses follow the
+ * reference's map_iv_error (mango_c_api.cpp:124-141): range and
+ * type/dividend mismatches MANGO_ERR_VALIDATION, vega too small
+ * MANGO_ERR_SOLVER. */
+MangoStatus mango_gpu_price_table_iv_batch(MangoGpuPriceTable* table,
+                                           const MangoInterpSolverConfig* config,
+                                           const MangoIvQuery* queries, uint64_t n,
+                                           MangoIvBatchSlot* out, uint64_t* out_failed,
+                                           MangoError* err);
+/* Same with device-resident queries and slots, enqueued without waiting
+ * (no failed count). */
+MangoStatus mango_gpu_price_table_iv_batch_device(MangoGpuPriceTable* table,
+                                                  const MangoInterpSolverConfig* config,
+                                                  const MangoIvQuery* d_queries, uint64_t n,
+                                                  MangoIvBatchSlot* d_out, MangoError* err);
 
 /* Sensitivities on a frozen grid: value, delta, gamma, theta as in
  * mango_gpu_price_american_batch plus dV/dvolatility, dV/drate,
@@ -469,6 +509,8 @@ static_assert(sizeof(MangoGpuGrid) == 48, "MangoGpuGrid size");
 static_assert(sizeof(MangoGpuAmericanOut) == 48, "MangoGpuAmericanOut size");
 static_assert(sizeof(MangoGpuGreeksOut) == 80, "MangoGpuGreeksOut size");
 static_assert(sizeof(MangoGpuFitStats) == 96, "MangoGpuFitStats size");
+static_assert(sizeof(MangoInterpSolverConfig) == 40, "MangoInterpSolverConfig size");
+static_assert(sizeof(MangoIvBatchSlot) == 48, "MangoIvBatchSlot size");
 #endif
 
 #endif /* MANGO_GPU_H */

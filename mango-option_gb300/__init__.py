@@ -88,6 +88,11 @@ class MangoGpuStats(ctypes.Structure):
         ("options", ctypes.c_int64), ("tiles", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
 
 
+class MangoInterpSolverConfig(ctypes.Structure):
+    _fields_ = [("max_iter", ctypes.c_uint64), ("tolerance", ctypes.c_double), ("sigma_min", ctypes.c_double),
+                ("sigma_max", ctypes.c_double), ("vega_threshold", ctypes.c_double)]
+
+
 class MangoGpuFitStats(ctypes.Structure):
     _fields_ = [("max_residual", ctypes.c_double * 4), ("condition", ctypes.c_double * 4),
                 ("failed_slices", ctypes.c_uint64 * 4)]
@@ -193,6 +198,15 @@ def library() -> ctypes.CDLL:
         lib.mango_gpu_price_table_price.restype = ctypes.c_int32
         lib.mango_gpu_price_table_price_device.argtypes = [_P, _P, ctypes.c_uint64, _P, ctypes.POINTER(MangoError)]
         lib.mango_gpu_price_table_price_device.restype = ctypes.c_int32
+        lib.mango_gpu_price_table_vega.argtypes = [_P, _P, ctypes.c_uint64, _P, ctypes.POINTER(MangoError)]
+        lib.mango_gpu_price_table_vega.restype = ctypes.c_int32
+        lib.mango_gpu_price_table_iv_batch.argtypes = [_P, ctypes.POINTER(MangoInterpSolverConfig), _P,
+                                                       ctypes.c_uint64, _P, ctypes.POINTER(ctypes.c_uint64),
+                                                       ctypes.POINTER(MangoError)]
+        lib.mango_gpu_price_table_iv_batch.restype = ctypes.c_int32
+        lib.mango_gpu_price_table_iv_batch_device.argtypes = [_P, ctypes.POINTER(MangoInterpSolverConfig), _P,
+                                                              ctypes.c_uint64, _P, ctypes.POINTER(MangoError)]
+        lib.mango_gpu_price_table_iv_batch_device.restype = ctypes.c_int32
         lib.mango_gpu_price_american_greeks_batch.argtypes = [
             _P, _P, ctypes.c_uint64, _P, ctypes.c_uint64, ctypes.c_double, _P,
             ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(MangoError)]
@@ -596,6 +610,45 @@ class GpuPriceTable:
                                                         ctypes.byref(err)) != MANGO_OK:
             raise EngineError(err.message.decode(errors="replace"))
 
+    def vega_arrays(self, params: np.ndarray) -> np.ndarray:
+        """AnyPriceTable::vega for PRICING_DTYPE records (no range checks)."""
+        params = np.ascontiguousarray(params, dtype=PRICING_DTYPE)
+        out = np.zeros(params.size)
+        err = MangoError()
+        if library().mango_gpu_price_table_vega(self._t, _ptr(params), params.size, _ptr(out),
+                                                ctypes.byref(err)) != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+        return out
+
+    def vega(self, params: PricingParams) -> float:
+        self.validate(params)
+        return float(self.vega_arrays(_to_array([params]))[0])
+
+    def iv_arrays(self, queries: np.ndarray, config: Optional["InterpolatedIVSolverConfig"] = None) -> np.ndarray:
+        """InterpolatedIVSolver::solve_batch (mango_gpu_price_table_iv_batch):
+        IVQUERY_DTYPE in, IVSLOT_DTYPE out."""
+        queries = np.ascontiguousarray(queries, dtype=IVQUERY_DTYPE)
+        out = np.zeros(queries.size, dtype=IVSLOT_DTYPE)
+        cfg = None if config is None else ctypes.byref(config._c())
+        failed = ctypes.c_uint64()
+        err = MangoError()
+        if library().mango_gpu_price_table_iv_batch(self._t, cfg, _ptr(queries), queries.size, _ptr(out),
+                                                    ctypes.byref(failed), ctypes.byref(err)) != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+        return out
+
+    def iv_device(self, d_queries: int, n: int, d_slots: int,
+                  config: Optional["InterpolatedIVSolverConfig"] = None) -> None:
+        cfg = None if config is None else ctypes.byref(config._c())
+        err = MangoError()
+        if library().mango_gpu_price_table_iv_batch_device(self._t, cfg, _P(d_queries), n, _P(d_slots),
+                                                           ctypes.byref(err)) != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+
+    def make_iv_solver(self, solver_config: Optional["InterpolatedIVSolverConfig"] = None):
+        """PriceTable.make_iv_solver of the reference's bindings."""
+        return InterpolatedIVSolver(self, solver_config)
+
     def validate(self, p: PricingParams) -> None:
         """AnyPriceTable::validate_pricing_params (price_table_factory.cpp:700-744)."""
         if p.option_type != self.option_type:
@@ -634,6 +687,49 @@ class GpuPriceTable:
 
 
 @dataclasses.dataclass
+class InterpolatedIVSolverConfig:
+    """Reference InterpolatedIVSolverConfig (src/option/interpolated_iv_solver.hpp:44-57)."""
+    max_iter: int = 50
+    tolerance: float = 1e-6
+    sigma_min: float = 0.01
+    sigma_max: float = 3.0
+    vega_threshold: float = 1e-4
+
+    def _c(self) -> MangoInterpSolverConfig:
+        return MangoInterpSolverConfig(self.max_iter, self.tolerance, self.sigma_min, self.sigma_max,
+                                       self.vega_threshold)
+
+
+class InterpolatedIVSolver:
+    """Reference InterpolatedIVSolver on a GPU price table: all quotes of
+    solve_batch solved together on the device."""
+
+    def __init__(self, table: "GpuPriceTable", config: Optional[InterpolatedIVSolverConfig] = None):
+        self.table = table
+        self.config = config or InterpolatedIVSolverConfig()
+
+    def solve_batch(self, queries) -> "BatchIVResult":
+        qs = list(queries)
+        arr = query_array([q.spot for q in qs], [q.strike for q in qs], [q.maturity for q in qs],
+                          [q.rate for q in qs], [q.dividend_yield for q in qs],
+                          [int(q.option_type == OptionType.PUT) for q in qs], [q.market_price for q in qs])
+        out = self.table.iv_arrays(arr, self.config)
+        res = []
+        for row in out:
+            if row["status"] == MANGO_OK:
+                res.append(IVSuccess(float(row["implied_vol"]), int(row["iterations"]), float(row["final_error"])))
+            else:
+                res.append(IVError(int(row["status"]), int(row["iterations"]), float(row["final_error"])))
+        return BatchIVResult(res, int(np.count_nonzero(out["status"])))
+
+    def solve(self, query):
+        r = self.solve_batch([query]).results[0]
+        if isinstance(r, IVError):
+            raise r
+        return r
+
+
+@dataclasses.dataclass
 class IVGrid:
     """Reference IVGrid (moneyness S/K, volatility and rate axes)."""
     moneyness: Sequence[float]
@@ -656,6 +752,13 @@ class IVSolverFactoryConfig:
     dividend_yield: float = 0.0
     grid: Optional[IVGrid] = None
     backend: Optional[BSplineBackend] = None
+
+
+def make_interpolated_iv_solver(config: IVSolverFactoryConfig, engine: Optional[Engine] = None,
+                                solver_config: Optional[InterpolatedIVSolverConfig] = None) -> InterpolatedIVSolver:
+    """make_interpolated_iv_solver, standard B-spline path: build the table,
+    then wrap it in an interpolated IV solver."""
+    return make_price_table(config, engine).make_iv_solver(solver_config)
 
 
 def make_price_table(config: IVSolverFactoryConfig, engine: Optional[Engine] = None) -> GpuPriceTable:

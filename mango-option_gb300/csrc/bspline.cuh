@@ -42,10 +42,14 @@ std::vector<double> clamped_knots(const double* x, int n);
 void bspline_tables(const double* grids, const int64_t* sizes, BSplineDims* D,
                     std::vector<double>* tab, std::vector<double>* knots);
 
-// BSplineND<double,4>::eval at x[0..3]; sm holds the packed tables.
-__device__ __forceinline__ double bspline4d_value(const BSplineDims& D, const double* sm,
-                                                  const double* __restrict__ coeffs,
-                                                  const double* xq) {
+// BSplineND<double,4>::eval at x[0..3] (DAX < 0), or eval_partial along
+// axis DAX (bspline_nd.hpp:168-199: the derivative basis
+// cubic_basis_derivative_nonuniform, bspline_basis.hpp:258-330, on that axis,
+// without the right-end special case); sm holds the packed tables.
+template <int DAX = -1>
+__device__ __forceinline__ double bspline4d_eval_t(const BSplineDims& D, const double* sm,
+                                                   const double* __restrict__ coeffs,
+                                                   const double* xq) {
   int span[4];
   double w[4][4];
 #pragma unroll
@@ -76,6 +80,18 @@ __device__ __forceinline__ double bspline4d_value(const BSplineDims& D, const do
       i = min(max(lo - 1, 3), max_span);
     }
     span[d] = i;
+    if (d == DAX) {
+      const double n10 = (x - t[i]) * R1[i];
+      const double n11 = (t[i + 1] - x) * R1[i];
+      const double n20 = (x - t[i]) * R2[i] * n10;
+      const double n21 = (x - t[i - 1]) * R2[i - 1] * n11 + (t[i + 2] - x) * R2[i] * n10;
+      const double n22 = (t[i + 1] - x) * R2[i - 1] * n11;
+      w[d][0] = 3.0 * R3[i] * n20;
+      w[d][1] = 3.0 * R3[i - 1] * n21 - 3.0 * R3[i] * n20;
+      w[d][2] = 3.0 * R3[i - 2] * n22 - 3.0 * R3[i - 1] * n21;
+      w[d][3] = 0.0 - 3.0 * R3[i - 2] * n22;
+      continue;
+    }
     // cubic_basis_nonuniform
     if (fabs(x - D.tlast[d]) < 64.0 * DBL_EPSILON * fmax(fabs(D.tlast[d]), 1.0)) {
       w[d][0] = 1.0;
@@ -126,6 +142,12 @@ __device__ __forceinline__ double bspline4d_value(const BSplineDims& D, const do
     s0 = fma(s1, w[0][o0], s0);
   }
   return s0;
+}
+
+__device__ __forceinline__ double bspline4d_value(const BSplineDims& D, const double* sm,
+                                                  const double* __restrict__ coeffs,
+                                                  const double* xq) {
+  return bspline4d_eval_t<-1>(D, sm, coeffs, xq);
 }
 
 }  // namespace mgpu

@@ -90,6 +90,10 @@ void destroy_batch(MangoGpuBatch* b);
 void run_batch(MangoGpuBatch* b);
 // Wait, copy results into caller slots, update the context stats.
 uint64_t fetch_batch(MangoGpuBatch* b, MangoGpuAmericanOut* out, std::string* first_msg);
+// Status of an IV query before any solve, as the reference C ABI reports it
+// (iv.cu); msg names the failed check.
+int32_t iv_query_status(const MangoIvQuery& q, std::string* msg);
+
 // Price-table sweep (table.cu): argument checks, and the sweep with the
 // tensor [m][tau][sigma][r] left in device memory; returns failed slices.
 std::string check_table_args(const double* moneyness, uint64_t nm, const double* maturity,

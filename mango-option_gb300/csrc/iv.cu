@@ -47,12 +47,13 @@
 #include <string>
 #include <vector>
 
+#include "brent.cuh"
 #include "engine.hpp"
 
 namespace mgpu {
 
-// Result codes of the state machines.
-constexpr int32_t kIvOk = 0, kIvBracket = 1, kIvMaxIter = 2, kIvNumerical = 3;
+using namespace brentdev;
+
 // Evaluations of the fast root finder before a quote without a sign change
 // is handed to Brent, and the cap for a quote inside a sign-change bracket
 // (which at least halves every second evaluation).
@@ -62,15 +63,6 @@ constexpr int kFastMaxBracketEvals = 60;
 constexpr int kMaxPts = 32;
 // IVSolver::solve_brent lower bracket (iv_solver.cpp:150).
 constexpr double kVolLower = 0.01;
-
-// ------------------------------------------------------------- Brent --
-
-// Brent state of one quote (root_finding.hpp:145-302 variables).
-struct BrentDev {
-  double a, b, c, d, fa, fb, fc, s;
-  double root, ferr;
-  int32_t iter, mflag, phase, code;  // phase: 0 eval a, 1 eval b, 2 eval s
-};
 
 // Fast root-finder state of one quote.  Until a sign change of f has been
 // seen, [lo, hi] steers the search assuming f rises with the volatility;
@@ -107,138 +99,6 @@ struct IvOut {
 };
 
 namespace {
-
-__device__ __forceinline__ void swap_d(double& x, double& y) {
-  const double t = x;
-  x = y;
-  y = t;
-}
-
-__device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000ll); }
-__device__ __forceinline__ double pinf() { return __longlong_as_double(0x7ff0000000000000ll); }
-
-// Convergence test and next trial point at the top of a Brent iteration;
-// returns false when the quote is finished.
-__device__ bool brent_propose(BrentDev& s, double tol, int max_iter) {
-  if (s.iter >= max_iter) {
-    s.code = kIvMaxIter;
-    s.root = s.b;
-    s.ferr = fabs(s.fb);
-    return false;
-  }
-  if (fabs(s.fb) < tol || fabs(s.b - s.a) < tol) {
-    s.code = kIvOk;
-    s.root = s.b;
-    s.ferr = fabs(s.fb);
-    s.iter += 1;  // the reference reports iter + 1 here
-    return false;
-  }
-  const double a = s.a, b = s.b, c = s.c, fa = s.fa, fb = s.fb, fc = s.fc;
-  double x;
-  if (fa != fc && fb != fc) {  // inverse quadratic interpolation
-    x = a * fb * fc / ((fa - fb) * (fa - fc)) + b * fa * fc / ((fb - fa) * (fb - fc)) +
-        c * fa * fb / ((fc - fa) * (fc - fb));
-  } else {  // secant
-    x = b - fb * (b - a) / (fb - fa);
-  }
-  const double bis = (3.0 * a + b) / 4.0;
-  const bool c1 = !((x > bis && x < b) || (x < bis && x > b));
-  const bool c2 = s.mflag && fabs(x - b) >= fabs(b - c) / 2.0;
-  const bool c3 = !s.mflag && fabs(x - b) >= fabs(c - s.d) / 2.0;
-  const bool c4 = s.mflag && fabs(b - c) < tol;
-  const bool c5 = !s.mflag && fabs(c - s.d) < tol;
-  if (c1 || c2 || c3 || c4 || c5) {
-    x = (a + b) / 2.0;
-    s.mflag = 1;
-  } else {
-    s.mflag = 0;
-  }
-  s.s = x;
-  return true;
-}
-
-__device__ void brent_start(BrentDev& s, double upper) {
-  s = BrentDev{};
-  s.a = kVolLower;
-  s.b = upper;
-  s.phase = 0;
-  s.code = kIvNumerical;
-}
-
-// Consume the objective value f at the last trial point and advance Brent
-// by one function value; returns true with the next trial point in *next,
-// false when the quote is finished (code, root, ferr, iter set).
-__device__ bool brent_consume(BrentDev& s, double f, double tol, int max_iter, double* next) {
-  if (s.phase == 0) {
-    s.fa = f;
-    s.phase = 1;
-    *next = s.b;
-    return true;
-  }
-  if (s.phase == 1) {
-    s.fb = f;
-    s.iter = 0;
-    if (!isfinite(s.fa) || !isfinite(s.fb)) {
-      s.code = kIvNumerical;
-      s.ferr = qnan();
-      return false;
-    }
-    if (s.fa * s.fb > 0.0) {
-      s.code = kIvBracket;
-      s.ferr = fmin(fabs(s.fa), fabs(s.fb));
-      return false;
-    }
-    if (fabs(s.fa) < tol) {
-      s.code = kIvOk;
-      s.root = s.a;
-      s.ferr = fabs(s.fa);
-      return false;
-    }
-    if (fabs(s.fb) < tol) {
-      s.code = kIvOk;
-      s.root = s.b;
-      s.ferr = fabs(s.fb);
-      return false;
-    }
-    if (fabs(s.fa) < fabs(s.fb)) {
-      swap_d(s.a, s.b);
-      swap_d(s.fa, s.fb);
-    }
-    s.c = s.a;
-    s.fc = s.fa;
-    s.mflag = 1;
-    s.d = 0.0;
-    s.phase = 2;
-    const bool go = brent_propose(s, tol, max_iter);
-    *next = s.s;
-    return go;
-  }
-  if (!isfinite(f)) {
-    s.code = kIvNumerical;
-    s.root = s.s;
-    s.ferr = qnan();
-    s.iter += 1;
-    return false;
-  }
-  s.d = s.c;
-  s.c = s.b;
-  s.fc = s.fb;
-  if (s.fa * f < 0.0) {
-    s.b = s.s;
-    s.fb = f;
-  } else {
-    s.a = s.s;
-    s.fa = f;
-  }
-  if (fabs(s.fa) < fabs(s.fb)) {
-    swap_d(s.a, s.b);
-    swap_d(s.fa, s.fb);
-  }
-  s.iter += 1;
-  const bool go = brent_propose(s, tol, max_iter);
-  *next = s.s;
-  return go;
-}
 
 // ------------------------------------------------------ fast finder --
 
@@ -458,7 +318,7 @@ __global__ void iv_init_kernel(int m, int32_t method, int k, const OptDev* __res
     st.mode = 0;
     npts[q] = fast_propose(s, o, mat[q], s.hi, k, pts);
   } else {
-    brent_start(st.br, upper[q]);
+    brent_start(st.br, kVolLower, upper[q]);
     st.mode = 1;
     pts[0] = st.br.a;
     npts[q] = 1;
@@ -507,7 +367,7 @@ __global__ void iv_step_kernel(int nq, const int32_t* __restrict__ qlist,
                "xa=%.17g fa=%.6e xb=%.17g fb=%.6e guess=%.6g n=%d\n",
                q, st.fs.iter, st.fs.lo, st.fs.hi, st.fs.seen, st.fs.ends, st.fs.has_br, st.fs.bl,
                st.fs.br, st.fs.xa, st.fs.fa, st.fs.xb, st.fs.fb, st.fs.guess, n);
-      brent_start(st.br, upper[q]);
+      brent_start(st.br, kVolLower, upper[q]);
       st.mode = 1;
       pts[0] = st.br.a;
       next_n = 1;
@@ -553,26 +413,31 @@ __global__ void iv_gather_kernel(int mw, const int32_t* __restrict__ map,
   active_w[k] = 1;
 }
 
-namespace {
-
-// validate_iv_query (src/option/option_spec.cpp:52-112) plus the engine's
-// scope; returns the MangoStatus and a message.
-int32_t validate_query(const MangoIvQuery& q, std::string* msg) {
+// Status of an IV query before any solve, as the reference C ABI reports
+// it: build_iv_query (src/ffi/mango_c_api.cpp:168-203) rejects a bad option
+// type and non-finite rate or dividend yield with MANGO_ERR_VALIDATION; then
+// validate_iv_query (src/option/option_spec.cpp:52-112) through
+// validation_error_to_iv_error (src/option/iv_result.hpp:55-99) and
+// map_iv_error (mango_c_api.cpp:124-141): bad spot / strike / maturity /
+// non-positive price -> VALIDATION, negative dividend yield and a price
+// outside [intrinsic, upper bound] -> ARBITRAGE.  Yield curves and discrete
+// dividends are outside the engine's scope (VALIDATION).
+int32_t iv_query_status(const MangoIvQuery& q, std::string* msg) {
   auto bad = [&](int32_t code, const char* m) {
     *msg = m;
     return code;
   };
-  if (!(q.spot > 0.0) || !std::isfinite(q.spot)) return bad(MANGO_ERR_VALIDATION, "invalid spot");
-  if (!(q.strike > 0.0) || !std::isfinite(q.strike)) return bad(MANGO_ERR_VALIDATION, "invalid strike");
-  if (!(q.maturity > 0.0) || !std::isfinite(q.maturity))
-    return bad(MANGO_ERR_VALIDATION, "invalid maturity");
-  if (!std::isfinite(q.rate_const)) return bad(MANGO_ERR_VALIDATION, "invalid rate");
-  if (q.dividend_yield < 0.0 || !std::isfinite(q.dividend_yield))
-    return bad(MANGO_ERR_VALIDATION, "invalid dividend yield");
   if (q.option_type != MANGO_PUT && q.option_type != MANGO_CALL)
     return bad(MANGO_ERR_VALIDATION, "invalid option type");
   if (q.n_tenor_points != 0) return bad(MANGO_ERR_VALIDATION, "yield curves are not supported by the GPU engine");
   if (q.n_dividends != 0) return bad(MANGO_ERR_VALIDATION, "discrete dividends are not supported by the GPU engine");
+  if (!std::isfinite(q.dividend_yield)) return bad(MANGO_ERR_VALIDATION, "dividend_yield must be finite");
+  if (!std::isfinite(q.rate_const)) return bad(MANGO_ERR_VALIDATION, "rate must be finite");
+  if (!(q.spot > 0.0) || !std::isfinite(q.spot)) return bad(MANGO_ERR_VALIDATION, "invalid spot");
+  if (!(q.strike > 0.0) || !std::isfinite(q.strike)) return bad(MANGO_ERR_VALIDATION, "invalid strike");
+  if (!(q.maturity > 0.0) || !std::isfinite(q.maturity))
+    return bad(MANGO_ERR_VALIDATION, "invalid maturity");
+  if (q.dividend_yield < 0.0) return bad(MANGO_ERR_ARBITRAGE, "invalid dividend yield");
   if (!std::isfinite(q.market_price) || q.market_price <= 0.0)
     return bad(MANGO_ERR_VALIDATION, "invalid market price");
   const bool put = q.option_type == MANGO_PUT;
@@ -582,6 +447,8 @@ int32_t validate_query(const MangoIvQuery& q, std::string* msg) {
   if (q.market_price > upper) return bad(MANGO_ERR_ARBITRAGE, "market price above the upper bound");
   return MANGO_OK;
 }
+
+namespace {
 
 using Clock = std::chrono::steady_clock;
 
@@ -731,7 +598,7 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
       p.rate_const = q.rate_const;
       p.option_type = q.option_type;
       p.volatility = 0.2;  // placeholder; every evaluation overrides it
-      vstatus[i] = validate_query(q, &vmsg[i]);
+      vstatus[i] = iv_query_status(q, &vmsg[i]);
       if (vstatus[i] == MANGO_OK && g.kind != MANGO_GPU_GRID_FIXED_N_AT_VOL &&
           g.kind != MANGO_GPU_GRID_SINH && g.kind != MANGO_GPU_GRID_UNIFORM) {
         vstatus[i] = MANGO_ERR_VALIDATION;

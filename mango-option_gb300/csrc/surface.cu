@@ -37,6 +37,7 @@
 #include <string>
 #include <vector>
 
+#include "brent.cuh"
 #include "bspline.cuh"
 #include "fit_host.hpp"
 
@@ -67,6 +68,12 @@ __device__ double european_price(double S, double K, double tau, double sigma, d
   const double eq = exp(-q * tau), er = exp(-r * tau);
   if (put) return K * er * norm_cdf(-d2) - S * eq * norm_cdf(-d1);
   return S * eq * norm_cdf(d1) - K * er * norm_cdf(d2);
+}
+
+// bs_vega (european_option.hpp:43-48), EuropeanOptionResult::vega.
+__device__ double european_vega(double S, double K, double tau, double sigma, double r, double q) {
+  const double d1 = (log(S / K) + (r - q + 0.5 * sigma * sigma) * tau) / (sigma * sqrt(tau));
+  return S * exp(-q * tau) * sqrt(tau) * (0.3989422804014327 * exp(-0.5 * d1 * d1));
 }
 
 // eep_floor (eep_decomposer.hpp:21-29): debiased softplus with sharpness 100.
@@ -168,6 +175,138 @@ __global__ void eep_decompose_kernel(int nm, int nt, int nv, int nr, const doubl
   const double spot = exp(mg[mi]) * K_ref;
   const double eu = european_price(spot, K_ref, tg[ti], vg[vi], rg[ri], q, put != 0);
   tensor[i] = eep_floor(am - eu);
+}
+
+// The table as the query kernels see it.
+struct TableDev {
+  double K_ref, q;
+  int put, eep;
+  double lo[4], hi[4];  // axis ranges (m, tau, sigma, rate)
+};
+
+// AnyPriceTable::price (EEPLayer::price over TransformLeaf::price).
+__device__ __forceinline__ double table_price(const BSplineDims& D, const double* sm,
+                                              const double* coeffs, const TableDev& T, double S,
+                                              double K, double tau, double sigma, double r) {
+  const double x[4] = {log(S / K), tau, sigma, r};
+  const double raw = bspline4d_value(D, sm, coeffs, x);
+  double v = fmax(0.0, raw) * K / T.K_ref;
+  if (T.eep) v += european_price(S, K, tau, sigma, r, T.q, T.put != 0);
+  return v;
+}
+
+// AnyPriceTable::vega (EEPLayer::vega over TransformLeaf::vega).
+__device__ __forceinline__ double table_vega(const BSplineDims& D, const double* sm,
+                                             const double* coeffs, const TableDev& T, double S,
+                                             double K, double tau, double sigma, double r) {
+  const double x[4] = {log(S / K), tau, sigma, r};
+  const double raw = bspline4d_value(D, sm, coeffs, x);
+  double v = 0.0;
+  if (raw > 0.0) v = bspline4d_eval_t<2>(D, sm, coeffs, x) * K / T.K_ref;
+  if (T.eep) v += european_vega(S, K, tau, sigma, r, T.q);
+  return v;
+}
+
+__global__ void surface_vega_kernel(BSplineDims D, const double* __restrict__ tables,
+                                    const double* __restrict__ coeffs, TableDev T,
+                                    const MangoPricingParams* __restrict__ p, int64_t n,
+                                    double* __restrict__ out) {
+  extern __shared__ double sm[];
+  for (int i = threadIdx.x; i < 4 * D.ktot; i += blockDim.x) sm[i] = tables[i];
+  __syncthreads();
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < n; k += stride) {
+    const MangoPricingParams pk = p[k];
+    out[k] = pk.n_tenor_points != 0
+                 ? __longlong_as_double(0x7ff8000000000000ll)
+                 : table_vega(D, sm, coeffs, T, pk.spot, pk.strike, pk.maturity, pk.volatility,
+                              pk.rate_const);
+  }
+}
+
+// InterpolatedIVSolver::solve (interpolated_iv_solver.hpp:427-520) per quote.
+__global__ void surface_iv_kernel(BSplineDims D, const double* __restrict__ tables,
+                                  const double* __restrict__ coeffs, TableDev T,
+                                  MangoInterpSolverConfig cfg,
+                                  const MangoIvQuery* __restrict__ qs, int64_t n,
+                                  MangoIvBatchSlot* __restrict__ out) {
+  extern __shared__ double sm[];
+  for (int i = threadIdx.x; i < 4 * D.ktot; i += blockDim.x) sm[i] = tables[i];
+  __syncthreads();
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < n; k += stride) {
+    const MangoIvQuery q = qs[k];
+    MangoIvBatchSlot slot{};
+    auto finish = [&](int32_t status) {
+      slot.status = status;
+      out[k] = slot;
+    };
+    // build_iv_query (mango_c_api.cpp:168-203) and validate_query
+    // (interpolated_iv_solver.hpp:375-398): type and dividend yield must
+    // match the table, then validate_iv_query.
+    if (q.option_type != MANGO_PUT && q.option_type != MANGO_CALL) { finish(MANGO_ERR_VALIDATION); continue; }
+    if (q.n_tenor_points != 0 || q.n_dividends != 0 || !isfinite(q.dividend_yield) ||
+        !isfinite(q.rate_const)) { finish(MANGO_ERR_VALIDATION); continue; }
+    const bool put = q.option_type == MANGO_PUT;
+    if (put != (T.put != 0) || fabs(q.dividend_yield - T.q) > 1e-10) { finish(MANGO_ERR_VALIDATION); continue; }
+    if (!(q.spot > 0.0) || !isfinite(q.spot) || !(q.strike > 0.0) || !isfinite(q.strike) ||
+        !(q.maturity > 0.0) || !isfinite(q.maturity)) { finish(MANGO_ERR_VALIDATION); continue; }
+    if (q.dividend_yield < 0.0) { finish(MANGO_ERR_ARBITRAGE); continue; }
+    if (!isfinite(q.market_price) || q.market_price <= 0.0) { finish(MANGO_ERR_VALIDATION); continue; }
+    const double intrinsic = put ? fmax(q.strike - q.spot, 0.0) : fmax(q.spot - q.strike, 0.0);
+    const double upper_bound = put ? q.strike : q.spot;
+    if (q.market_price < intrinsic || q.market_price > upper_bound) { finish(MANGO_ERR_ARBITRAGE); continue; }
+    // adaptive_bounds (interpolated_iv_solver.hpp:400-425)
+    const double tv_pct = (q.market_price - intrinsic) / q.market_price;
+    const double sigma_upper = tv_pct > 0.5 ? 3.0 : (tv_pct > 0.2 ? 2.0 : 1.5);
+    double smin = fmax(cfg.sigma_min, T.lo[2]);
+    double smax = fmin(fmin(sigma_upper, cfg.sigma_max), T.hi[2]);
+    if (smin >= smax) {
+      smin = T.lo[2];
+      smax = T.hi[2];
+    }
+    // is_in_bounds at both ends (interpolated_iv_solver.hpp:134-145)
+    const double x = log(q.spot / q.strike);
+    const double r = q.rate_const;
+    const bool in = x >= T.lo[0] && x <= T.hi[0] && q.maturity >= T.lo[1] && q.maturity <= T.hi[1] &&
+                    r >= T.lo[3] && r <= T.hi[3] && smin >= T.lo[2] && smin <= T.hi[2] &&
+                    smax >= T.lo[2] && smax <= T.hi[2];
+    if (!in) { finish(MANGO_ERR_VALIDATION); continue; }
+    // vega pre-check
+    if (cfg.vega_threshold > 0.0) {
+      double vmax = 0.0;
+      const double probe[3] = {0.10, 0.25, 0.50};
+      for (int j = 0; j < 3; ++j)
+        vmax = fmax(vmax, fabs(table_vega(D, sm, coeffs, T, q.spot, q.strike, q.maturity, probe[j], r)));
+      if (vmax < cfg.vega_threshold) {
+        slot.success.final_error = vmax;
+        finish(MANGO_ERR_SOLVER);
+        continue;
+      }
+    }
+    // Brent on f(sigma) = price(m K, K, tau, sigma, r) - P
+    const double mny = q.spot / q.strike;
+    const double spot = mny * q.strike;
+    BrentDev b;
+    brentdev::brent_start(b, smin, smax);
+    double sig = smin;
+    const int max_iter = static_cast<int>(cfg.max_iter > 1000000 ? 1000000 : cfg.max_iter);
+    for (int e = 0; e < max_iter + 3; ++e) {
+      const double f = table_price(D, sm, coeffs, T, spot, q.strike, q.maturity, sig, r) - q.market_price;
+      double next = 0.0;
+      if (!brentdev::brent_consume(b, f, cfg.tolerance, max_iter, &next)) break;
+      sig = next;
+    }
+    slot.success.iterations = static_cast<uint64_t>(b.iter);
+    slot.success.final_error = b.ferr;
+    if (b.code == kIvOk) {
+      slot.success.implied_vol = b.root;
+      finish(MANGO_OK);
+    } else {
+      finish(b.code == kIvBracket ? MANGO_ERR_BRACKETING
+                                  : (b.code == kIvMaxIter ? MANGO_ERR_NO_CONVERGENCE : MANGO_ERR_SOLVER));
+    }
+  }
 }
 
 // AnyPriceTable::price for n parameter records.
@@ -588,6 +727,131 @@ MangoStatus mango_gpu_price_table_price(MangoGpuPriceTable* t, const MangoPricin
     check(cudaStreamSynchronize(st), "stream synchronize");
     return MANGO_OK;
   } catch (const std::exception& e) {
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+}  // extern "C"
+
+namespace {
+
+TableDev table_dev(const MangoGpuPriceTable* t) {
+  TableDev T{};
+  T.K_ref = t->K_ref;
+  T.q = t->q;
+  T.put = t->option_type == MANGO_PUT ? 1 : 0;
+  T.eep = t->eep;
+  for (int d = 0; d < 4; ++d) {
+    T.lo[d] = t->bounds[2 * d];
+    T.hi[d] = t->bounds[2 * d + 1];
+  }
+  return T;
+}
+
+MangoInterpSolverConfig interp_config(const MangoInterpSolverConfig* c) {
+  if (c) return *c;
+  MangoInterpSolverConfig d{};
+  d.max_iter = 50;  // InterpolatedIVSolverConfig (interpolated_iv_solver.hpp:44-57)
+  d.tolerance = 1e-6;
+  d.sigma_min = 0.01;
+  d.sigma_max = 3.0;
+  d.vega_threshold = 1e-4;
+  return d;
+}
+
+}  // namespace
+
+extern "C" {
+
+MangoStatus mango_gpu_price_table_vega(MangoGpuPriceTable* t, const MangoPricingParams* params,
+                                       uint64_t n, double* out, MangoError* err) {
+  if (!t || (n > 0 && (!params || !out))) {
+    set_err(err, MANGO_ERR_VALIDATION, "null argument");
+    return MANGO_ERR_VALIDATION;
+  }
+  if (n == 0) return MANGO_OK;
+  try {
+    MangoGpuBSpline4D* s = t->surface;
+    check(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    cudaStream_t st = s->ctx->stream;
+    MangoPricingParams* dp = static_cast<MangoPricingParams*>(t->d_p.get(sizeof(MangoPricingParams) * n));
+    double* dout = static_cast<double*>(t->d_out.get(sizeof(double) * n));
+    check(cudaMemcpyAsync(dp, params, sizeof(MangoPricingParams) * n, cudaMemcpyHostToDevice, st), "H2D");
+    const int blocks = static_cast<int>(std::min<int64_t>(s->blocks, static_cast<int64_t>((n + 255) / 256)));
+    surface_vega_kernel<<<blocks, 256, sizeof(double) * 4 * s->dims.ktot, st>>>(
+        s->dims, s->d_tables.as<double>(), s->d_coeffs.as<double>(), table_dev(t), dp,
+        static_cast<int64_t>(n), dout);
+    check(cudaGetLastError(), "surface_vega_kernel launch");
+    check(cudaMemcpyAsync(out, dout, sizeof(double) * n, cudaMemcpyDeviceToHost, st), "D2H");
+    check(cudaStreamSynchronize(st), "stream synchronize");
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+MangoStatus mango_gpu_price_table_iv_batch_device(MangoGpuPriceTable* t,
+                                                  const MangoInterpSolverConfig* config,
+                                                  const MangoIvQuery* d_queries, uint64_t n,
+                                                  MangoIvBatchSlot* d_out, MangoError* err) {
+  if (!t || (n > 0 && (!d_queries || !d_out))) {
+    set_err(err, MANGO_ERR_VALIDATION, "null argument");
+    return MANGO_ERR_VALIDATION;
+  }
+  if (n == 0) return MANGO_OK;
+  try {
+    MangoGpuBSpline4D* s = t->surface;
+    check(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    const int blocks = static_cast<int>(std::min<int64_t>(s->blocks, static_cast<int64_t>((n + 255) / 256)));
+    surface_iv_kernel<<<blocks, 256, sizeof(double) * 4 * s->dims.ktot, s->ctx->stream>>>(
+        s->dims, s->d_tables.as<double>(), s->d_coeffs.as<double>(), table_dev(t), interp_config(config),
+        d_queries, static_cast<int64_t>(n), d_out);
+    check(cudaGetLastError(), "surface_iv_kernel launch");
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+MangoStatus mango_gpu_price_table_iv_batch(MangoGpuPriceTable* t,
+                                           const MangoInterpSolverConfig* config,
+                                           const MangoIvQuery* queries, uint64_t n,
+                                           MangoIvBatchSlot* out, uint64_t* out_failed,
+                                           MangoError* err) {
+  if (!t || (n > 0 && (!queries || !out))) {
+    set_err(err, MANGO_ERR_VALIDATION, "null argument");
+    return MANGO_ERR_VALIDATION;
+  }
+  if (out_failed) *out_failed = 0;
+  if (n == 0) return MANGO_OK;
+  DevBuf dq, ds;
+  try {
+    MangoGpuBSpline4D* s = t->surface;
+    check(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    cudaStream_t st = s->ctx->stream;
+    MangoIvQuery* d_q = static_cast<MangoIvQuery*>(dq.get(sizeof(MangoIvQuery) * n));
+    MangoIvBatchSlot* d_s = static_cast<MangoIvBatchSlot*>(ds.get(sizeof(MangoIvBatchSlot) * n));
+    check(cudaMemcpyAsync(d_q, queries, sizeof(MangoIvQuery) * n, cudaMemcpyHostToDevice, st), "H2D");
+    MangoStatus rc = mango_gpu_price_table_iv_batch_device(t, config, d_q, n, d_s, err);
+    if (rc != MANGO_OK) {
+      dq.release();
+      ds.release();
+      return rc;
+    }
+    check(cudaMemcpyAsync(out, d_s, sizeof(MangoIvBatchSlot) * n, cudaMemcpyDeviceToHost, st), "D2H");
+    check(cudaStreamSynchronize(st), "stream synchronize");
+    dq.release();
+    ds.release();
+    uint64_t failed = 0;
+    for (uint64_t i = 0; i < n; ++i) failed += out[i].status != MANGO_OK;
+    if (out_failed) *out_failed = failed;
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    dq.release();
+    ds.release();
     set_err(err, MANGO_ERR_SOLVER, e.what());
     return MANGO_ERR_SOLVER;
   }

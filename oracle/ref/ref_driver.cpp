@@ -19,6 +19,7 @@
 #include "mango/option/table/bspline/bspline_surface.hpp"
 #include "mango/option/table/bspline/bspline_tensor_accessor.hpp"
 #include "mango/option/table/eep/eep_decomposer.hpp"
+#include "mango/option/interpolated_iv_solver.hpp"
 
 #include <omp.h>
 #include <cmath>
@@ -349,6 +350,97 @@ int32_t ref_eep_decompose(const double* m, int64_t nm, const double* tau, int64_
       for (int64_t a = 0; a < ns; ++a)
         for (int64_t l = 0; l < nr; ++l)
           tensor[((i * ntau + j) * ns + a) * nr + l] = t->view[i, j, a, l];
+  return 0;
+}
+
+// The standard table's vega (EEPLayer::vega over TransformLeaf::vega);
+// p as for ref_surface_price.
+int32_t ref_surface_vega(const int64_t* sizes, const double* grids, const double* coeffs,
+                         double K_ref, double q, int32_t is_put, const double* p, int64_t n,
+                         double* out) {
+  std::array<std::vector<double>, 4> g, k;
+  size_t off = 0, total = 1;
+  for (int d = 0; d < 4; ++d) {
+    g[d].assign(grids + off, grids + off + sizes[d]);
+    off += static_cast<size_t>(sizes[d]);
+    k[d] = clamped_knots_cubic(g[d]);
+    total *= static_cast<size_t>(sizes[d]);
+  }
+  std::vector<double> c(coeffs, coeffs + total);
+  auto sp = BSplineND<double, 4>::create(g, k, std::move(c));
+  if (!sp) return 1;
+  auto shared = std::make_shared<const BSplineND<double, 4>>(std::move(sp.value()));
+  auto table = make_bspline_surface(shared, K_ref, q, is_put ? OptionType::PUT : OptionType::CALL);
+  if (!table) return 2;
+  for (int64_t i = 0; i < n; ++i)
+    out[i] = table->vega(p[5 * i], p[5 * i + 1], p[5 * i + 2], p[5 * i + 3], p[5 * i + 4]);
+  return 0;
+}
+
+// InterpolatedIVSolver<BSplinePriceTable>::solve_batch on the standard table.
+// cfg = {max_iter, tolerance, sigma_min, sigma_max, vega_threshold};
+// queries n x 7 {spot, strike, tau, rate, q, is_put, price}; out n x 3
+// {iv, iterations, final_error}; status = the C ABI's map_iv_error
+// (src/ffi/mango_c_api.cpp:124-141) of each result (0 on success).
+int32_t ref_surface_iv(const int64_t* sizes, const double* grids, const double* coeffs,
+                       double K_ref, double q, int32_t is_put, const double* cfg,
+                       const double* qs, int64_t n, double* out, int32_t* status) {
+  std::array<std::vector<double>, 4> g, k;
+  size_t off = 0, total = 1;
+  for (int d = 0; d < 4; ++d) {
+    g[d].assign(grids + off, grids + off + sizes[d]);
+    off += static_cast<size_t>(sizes[d]);
+    k[d] = clamped_knots_cubic(g[d]);
+    total *= static_cast<size_t>(sizes[d]);
+  }
+  std::vector<double> c(coeffs, coeffs + total);
+  auto sp = BSplineND<double, 4>::create(g, k, std::move(c));
+  if (!sp) return 1;
+  auto shared = std::make_shared<const BSplineND<double, 4>>(std::move(sp.value()));
+  auto table = make_bspline_surface(shared, K_ref, q, is_put ? OptionType::PUT : OptionType::CALL);
+  if (!table) return 2;
+  InterpolatedIVSolverConfig sc;
+  sc.max_iter = static_cast<size_t>(cfg[0]);
+  sc.tolerance = cfg[1];
+  sc.sigma_min = cfg[2];
+  sc.sigma_max = cfg[3];
+  sc.vega_threshold = cfg[4];
+  auto solver = InterpolatedIVSolver<BSplinePriceTable>::create(std::move(*table), sc);
+  if (!solver) return 3;
+  std::vector<IVQuery> queries;
+  for (int64_t i = 0; i < n; ++i) {
+    const double* r = qs + 7 * i;
+    OptionSpec spec{.spot = r[0], .strike = r[1], .maturity = r[2], .rate = r[3],
+                    .dividend_yield = r[4], .option_type = r[5] != 0.0 ? OptionType::PUT : OptionType::CALL};
+    queries.emplace_back(spec, r[6]);
+  }
+  auto res = solver->solve_batch(queries);
+  for (int64_t i = 0; i < n; ++i) {
+    const auto& r = res.results[i];
+    if (r) {
+      out[3 * i] = r->implied_vol;
+      out[3 * i + 1] = static_cast<double>(r->iterations);
+      out[3 * i + 2] = r->final_error;
+      status[i] = 0;
+    } else {
+      out[3 * i] = NAN;
+      out[3 * i + 1] = static_cast<double>(r.error().iterations);
+      out[3 * i + 2] = r.error().final_error;
+      switch (r.error().code) {
+        case IVErrorCode::ArbitrageViolation: status[i] = 2; break;
+        case IVErrorCode::BracketingFailed: status[i] = 4; break;
+        case IVErrorCode::MaxIterationsExceeded: status[i] = 3; break;
+        case IVErrorCode::NegativeSpot:
+        case IVErrorCode::NegativeStrike:
+        case IVErrorCode::NegativeMaturity:
+        case IVErrorCode::NegativeMarketPrice:
+        case IVErrorCode::InvalidGridConfig:
+        case IVErrorCode::OptionTypeMismatch:
+        case IVErrorCode::DividendYieldMismatch: status[i] = 1; break;
+        default: status[i] = 5; break;
+      }
+    }
+  }
   return 0;
 }
 

@@ -32,6 +32,13 @@ every output value):
                      coefficients: 2048 price queries (some outside the axes)
                      for a put and a call table; and eep_decompose
                      (AnalyticalEEP) of a seeded V/K_ref tensor on the same axes
+  interp_iv.npz      a real EEP table: the reference's own sweep tensor on
+                     12 x 6 x 5 x 4 axes (auto grid), its eep_decompose, fitted by the
+                     CPU restatement (oracle/fit_oracle.py; the reference's fit
+                     needs LAPACKE); on it the reference's vega at 1024 points
+                     and InterpolatedIVSolver::solve_batch for 1024 quotes
+                     (prices from the table at seeded vols, plus invalid,
+                     out-of-range and mismatched quotes)
 """
 from __future__ import annotations
 
@@ -234,6 +241,7 @@ def main():
     golden_bspline(lib)
     golden_table(lib)
     golden_surface(lib)
+    golden_interp_iv(lib)
 
 
 def table_axes(nm, ntau, ns, nr):
@@ -314,6 +322,63 @@ def golden_surface(lib):
                                ctypes.c_double(0.015), ctypes.c_int32(1), P(eep))
     assert rc == 0
     save("surface.npz", sizes=sizes, grids=grids, coeffs=coeffs, params=p, eep_in=ten, eep_out=eep, **res)
+
+
+def golden_interp_iv(lib):
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import fit_oracle
+    axes = list(table_axes(12, 6, 5, 4))
+    nm, nt, ns, nr = (a.size for a in axes)
+    ten = np.zeros(nm * nt * ns * nr)
+    dims = np.zeros(2 * ns * nr, np.int64)
+    rc = lib.ref_table_sweep(P(axes[0]), ctypes.c_int64(nm), P(axes[1]), ctypes.c_int64(nt), P(axes[2]),
+                             ctypes.c_int64(ns), P(axes[3]), ctypes.c_int64(nr), ctypes.c_double(100.0),
+                             ctypes.c_double(0.0), ctypes.c_int32(1), ctypes.c_int32(0), ctypes.c_double(0.0),
+                             ctypes.c_double(0.0), ctypes.c_int64(0), ctypes.c_double(0.0), ctypes.c_int64(0),
+                             P(ten), P(dims))
+    assert rc == 0
+    rc = lib.ref_eep_decompose(P(axes[0]), ctypes.c_int64(nm), P(axes[1]), ctypes.c_int64(nt), P(axes[2]),
+                               ctypes.c_int64(ns), P(axes[3]), ctypes.c_int64(nr), ctypes.c_double(100.0),
+                               ctypes.c_double(0.0), ctypes.c_int32(1), P(ten))
+    assert rc == 0
+    coeffs = np.ascontiguousarray(fit_oracle.fit4d(axes, ten.reshape(nm, nt, ns, nr)).ravel())
+    sizes = np.array([nm, nt, ns, nr], np.int64)
+    grids = np.ascontiguousarray(np.concatenate(axes))
+    rng = np.random.default_rng(31)
+    n = 1024
+    # vega at random in-range points
+    vp = np.ascontiguousarray(np.stack([np.full(n, 100.0), 100.0 / np.exp(rng.uniform(axes[0][0], axes[0][-1], n)),
+                                        rng.uniform(0.02, 2.0, n), rng.uniform(0.05, 0.8, n),
+                                        rng.uniform(0.0, 0.08, n)], 1))
+    vega = np.zeros(n)
+    assert lib.ref_surface_vega(P(sizes), P(grids), P(coeffs), ctypes.c_double(100.0), ctypes.c_double(0.0),
+                                ctypes.c_int32(1), P(vp), ctypes.c_int64(n), P(vega)) == 0
+    # quotes priced from the table itself at seeded vols
+    vt = rng.uniform(0.08, 0.7, n)
+    K = 100.0 / np.exp(rng.uniform(axes[0][0], axes[0][-1], n))
+    tau = rng.uniform(0.05, 1.9, n)
+    r = rng.uniform(0.0, 0.08, n)
+    pp = np.ascontiguousarray(np.stack([np.full(n, 100.0), K, tau, vt, r], 1))
+    px = np.zeros(n)
+    assert lib.ref_surface_price(P(sizes), P(grids), P(coeffs), ctypes.c_double(100.0), ctypes.c_double(0.0),
+                                 ctypes.c_int32(1), P(pp), ctypes.c_int64(n), P(px)) == 0
+    qs = np.stack([np.full(n, 100.0), K, tau, r, np.zeros(n), np.ones(n), px], 1)
+    # invalid and edge quotes in the last rows
+    qs[-1] = [100.0, 100.0, 1.0, 0.03, 0.0, 1.0, 150.0]       # above the put bound K -> arbitrage
+    qs[-2] = [100.0, 100.0, 5.0, 0.03, 0.0, 1.0, 8.0]         # maturity outside the table
+    qs[-3] = [100.0, 100.0, 1.0, 0.03, 0.01, 1.0, 8.0]        # dividend yield mismatch
+    qs[-4] = [100.0, 100.0, 1.0, 0.03, 0.0, 0.0, 8.0]         # option type mismatch
+    qs[-5] = [100.0, 130.0, 0.05, 0.03, 0.0, 1.0, 29.9]       # below intrinsic -> arbitrage
+    qs[-6] = [100.0, 71.0, 0.03, 0.0, 0.0, 1.0, 1e-9]         # deep OTM, tiny vega
+    qs[-7] = [100.0, 100.0, 1.0, 0.03, 0.0, 1.0, 45.0]        # no root in the bracket
+    qs = np.ascontiguousarray(qs)
+    cfg = np.array([50.0, 1e-6, 0.01, 3.0, 1e-4])
+    out = np.zeros(3 * n)
+    st = np.zeros(n, np.int32)
+    assert lib.ref_surface_iv(P(sizes), P(grids), P(coeffs), ctypes.c_double(100.0), ctypes.c_double(0.0),
+                              ctypes.c_int32(1), P(cfg), P(qs), ctypes.c_int64(n), P(out), P(st)) == 0
+    save("interp_iv.npz", sizes=sizes, grids=grids, coeffs=coeffs, vega_params=vp, vega=vega, quotes=qs,
+         true_vol=vt, cfg=cfg, out=out.reshape(n, 3), status=st)
 
 
 if __name__ == "__main__":

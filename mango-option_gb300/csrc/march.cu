@@ -28,6 +28,7 @@
 
 #include <cuda_runtime.h>
 #include <climits>
+#include <type_traits>
 
 namespace mgpu {
 
@@ -216,51 +217,60 @@ namespace {
 
 enum StageKind { kRannacher = 0, kStage1 = 1, kStage2 = 2 };
 
-// Inputs of one forward-sweep row, prefetched into registers.
-struct FwdRow {
-  double a, b, c, nl, v;
-  unsigned f;
-};
+// Row inputs stream through a per-warp shared-memory ring, kRing rows ahead
+// of the row being solved: each lane copies its own elements with cp.async
+// (one commit group per row), so a deep prefetch costs no registers and the
+// serial recurrences never wait on HBM.  Ring layout [slot][array][lane],
+// at most kRingArrays arrays per row; a row's slot is refilled one row after
+// it was read.
+constexpr int kRing = 8;                        // rows in flight
+constexpr int kRingSlots = kRing + 1;           // the slot refilled was read one row earlier
+constexpr int kRingArrays = 5;
+constexpr int kRingSlot = kRingArrays * kTile;  // doubles per slot
 
+__device__ __forceinline__ void cp_async8(double* sdst, const double* gsrc) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(sdst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+// Wait until the oldest of the kRing groups in flight has landed.
+__device__ __forceinline__ void cp_wait_oldest() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(kRing - 1) : "memory");
+}
+
+// Forward-sweep inputs of row i into ring slot i % kRingSlots.
 template <int K>
-__device__ __forceinline__ void load_fwd(const TileView& V, const uint8_t* __restrict__ F,
-                                         int a_in, int i, FwdRow& r) {
+__device__ __forceinline__ void issue_fwd(const TileView& V, double* R, int a_in, int i) {
+  double* s = R + (i % kRingSlots) * kRingSlot;
   const double* p = V.rp(i);
   if (K == kStage1) {
-    r.a = p[A_E1L * kTile];
-    r.b = p[A_E1D * kTile];
-    r.c = p[A_E1U * kTile];
-    r.nl = p[A_N1H * kTile];
-    r.v = V.rp(i + 1)[A_U * kTile];
+    cp_async8(s, p + A_E1L * kTile);
+    cp_async8(s + kTile, p + A_E1D * kTile);
+    cp_async8(s + 2 * kTile, p + A_E1U * kTile);
+    cp_async8(s + 3 * kTile, p + A_N1H * kTile);
+    cp_async8(s + 4 * kTile, V.rp(i + 1) + A_U * kTile);
   } else if (K == kStage2) {
-    r.a = p[A_A2H * kTile];
-    r.b = p[A_B2H * kTile];
-    r.nl = p[A_N2H * kTile];
-    r.c = p[A_G * kTile];  // guess u^{n+gamma}
-    r.v = p[A_U * kTile];  // u^n
+    cp_async8(s, p + A_A2H * kTile);
+    cp_async8(s + kTile, p + A_B2H * kTile);
+    cp_async8(s + 2 * kTile, p + A_N2H * kTile);
+    cp_async8(s + 3 * kTile, p + A_G * kTile);  // guess u^{n+gamma}
+    cp_async8(s + 4 * kTile, p + A_U * kTile);  // u^n
   } else {
-    r.c = p[a_in * kTile];  // rhs = guess = u_prev
+    cp_async8(s + 3 * kTile, p + a_in * kTile);  // rhs = guess = u_prev
   }
-  r.f = ROW(F, i);
 }
 
-struct BwdRow {
-  double nc, psi, d;
-};
-
+// Back-substitution inputs of row i into ring slot i % kRingSlots.
 template <int K>
-__device__ __forceinline__ void load_bwd(const TileView& V, int i, BwdRow& r) {
+__device__ __forceinline__ void issue_bwd(const TileView& V, double* R, int i) {
+  double* s = R + (i % kRingSlots) * kRingSlot;
   const double* p = V.rp(i);
-  r.nc = p[(K == kStage2 ? A_NC2 : A_NC1) * kTile];
-  r.psi = p[A_PSI * kTile];
-  r.d = p[A_D * kTile];
+  cp_async8(s, p + (K == kStage2 ? A_NC2 : A_NC1) * kTile);
+  cp_async8(s + kTile, p + A_PSI * kTile);
+  cp_async8(s + 2 * kTile, p + A_D * kTile);
 }
 
-// A forward-sweep row off the cached factorisation: a locked row (identity
-// with rhs psi) or a row whose factor is recomputed exactly as the reference
-// does (thomas_solver.hpp:382-395).  Records the row's own c' in A_CP and
-// keeps [lo, hi] contiguous.  Kept out of line: it runs for a few rows per
-// stage, and inlining it into the prefetching loop costs registers.
+// Result of a forward-sweep row solved off the cached factorisation.
 struct SlowOut {
   double d;      // d'_i
   double c;      // c'_i of this row (0 for a locked row)
@@ -271,10 +281,9 @@ struct SlowOut {
 
 // A forward-sweep row off the cached factorisation: a locked row (identity
 // with rhs psi) or a row whose factor is recomputed exactly as the reference
-// does (thomas_solver.hpp:382-395).  Records the row's own c' in A_CP and
-// keeps [lo, hi] contiguous.  Kept out of line: it runs for a few rows per
-// stage, and inlining it into the prefetching loop costs registers.  All
-// state travels by value so the caller keeps it in registers.
+// does (thomas_solver.hpp:382-395).  Records the row's own -c' in A_CP and
+// keeps [lo, hi] contiguous.  All state travels by value so the caller keeps
+// it in registers.
 template <int K>
 __device__ __forceinline__ SlowOut slow_row(const TileView V, int i, bool lock, double psi_i,
                                          double um, double u0, double v, double g,
@@ -310,8 +319,8 @@ __device__ __forceinline__ SlowOut slow_row(const TileView V, int i, bool lock, 
   // Rows between the previous off-cache row and this one keep their cached
   // value in A_CP so that [lo, hi] is valid for the back substitution.
   if (hi >= 0 && i > hi + 1)
-    for (int q = hi + 1; q < i; ++q) V.at(A_CP, q) = -V.at(aNC, q);
-  p[A_CP * kTile] = o.c;
+    for (int q = hi + 1; q < i; ++q) V.at(A_CP, q) = V.at(aNC, q);
+  p[A_CP * kTile] = -o.c;
   o.lo = lo == INT_MAX ? i : lo;
   o.hi = i;
   return o;
@@ -326,49 +335,61 @@ template <int K>
 __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
                                       const uint8_t* __restrict__ F, bool nocache, double bcl,
                                       double bcr, double alpha, double beta, int a_in, int a_out,
-                                      int32_t st) {
+                                      int32_t st, int flo, int fhi, double* R) {
   const int last = V.NX - 2;  // last interior row of the tile
   const bool always_fresh = (K == kRannacher) || nocache;
+  R += threadIdx.x & (kTile - 1);  // this lane's column of the ring
+  // The previous sweeps' global writes of this lane come before the async
+  // copies that read them.
+  __threadfence_block();
 
   // ---- forward elimination
   double dprev = bcl;  // d'_0 = rhs_0 / 1 on the Dirichlet row
   double cprev = 0.0;  // recomputed c'_{i-1}; valid whenever `fresh`
   bool fresh = always_fresh;
-  int lo = INT_MAX, hi = -1;  // rows [lo, hi] take c' from A_CP
+  int lo = INT_MAX, hi = -1;  // rows [lo, hi] take -c' from A_CP
   double um = 0.0, u0 = 0.0;
   if (K == kStage1 && live) {
     um = V.at(A_U, 0);
     u0 = V.at(A_U, 1);
   }
-  // Rows i..i+3 ride in a register queue: the loads of row i+4 are issued
-  // before row i is computed, so the d' recurrence does not wait on memory.
   const int stop = live ? min(last, n - 2) : 0;
-  FwdRow q0{}, q1{}, q2{}, q3{};
-  if (1 <= stop) load_fwd<K>(V, F, a_in, 1, q0);
-  if (2 <= stop) load_fwd<K>(V, F, a_in, 2, q1);
-  if (3 <= stop) load_fwd<K>(V, F, a_in, 3, q2);
-  if (4 <= stop) load_fwd<K>(V, F, a_in, 4, q3);
-  for (int i = 1; i <= stop; ++i) {
-    const FwdRow r = q0;
-    q0 = q1;
-    q1 = q2;
-    q2 = q3;
-    if (i + 4 <= stop) load_fwd<K>(V, F, a_in, i + 4, q3);
-    const double g = (K == kStage1) ? u0 : r.c;
+  for (int j = 1; j <= kRing; ++j) {
+    if (j <= stop) issue_fwd<K>(V, R, a_in, j);
+    cp_commit();
+  }
+  // The lock test (pde_solver.hpp:635-680) only runs on the tile's
+  // lock-candidate rows [flo, fhi]: the union over its lanes of each lane's
+  // contiguous candidate block.  Elsewhere a row cannot lock, so those
+  // segments carry no test at all.
+  auto row = [&](int i, auto may_lock) {
+    cp_wait_oldest();
+    const double* s = R + (i % kRingSlots) * kRingSlot;
+    double ra = 0.0, rb = 0.0, rc, rnl = 0.0, rv = 0.0;
+    if (K != kRannacher) {
+      ra = s[0];
+      rb = s[kTile];
+      rnl = s[(K == kStage1 ? 3 : 2) * kTile];
+      rv = s[4 * kTile];
+    }
+    rc = s[(K == kStage1 ? 2 : 3) * kTile];
+    if (i + kRing <= stop) issue_fwd<K>(V, R, a_in, i + kRing);
+    cp_commit();
+    const double g = (K == kStage1) ? u0 : rc;
     bool lock = false;
     double psi_i = 0.0;
-    if (r.f) {
+    if (decltype(may_lock)::value && ROW(F, i)) {
       psi_i = V.at(A_PSI, i);
       lock = (g - psi_i < 1e-8);
     }
     double dcur;
     if (!lock && !fresh) {
       if (K == kStage1)
-        dcur = fma(r.nl, dprev, fma(r.a, um, fma(r.b, u0, r.c * r.v)));
+        dcur = fma(rnl, dprev, fma(ra, um, fma(rb, u0, rc * rv)));
       else
-        dcur = fma(r.nl, dprev, fma(r.a, g, r.b * r.v));
+        dcur = fma(rnl, dprev, fma(ra, g, rb * rv));
     } else {
-      const SlowOut so = slow_row<K>(V, i, lock, psi_i, um, u0, r.v, g, alpha, beta, dprev, cprev,
+      const SlowOut so = slow_row<K>(V, i, lock, psi_i, um, u0, rv, g, alpha, beta, dprev, cprev,
                                      always_fresh, lo, hi);
       dcur = so.d;
       cprev = so.c;
@@ -381,27 +402,31 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
     dprev = dcur;
     if (K == kStage1) {
       um = u0;
-      u0 = r.v;
+      u0 = rv;
     }
-  }
+  };
+  int i = 1;
+  for (const int e1 = min(flo - 1, stop); i <= e1; ++i) row(i, std::false_type{});
+  for (const int e2 = min(fhi, stop); i <= e2; ++i) row(i, std::true_type{});
+  for (; i <= stop; ++i) row(i, std::false_type{});
 
   // ---- projected back substitution; last row d' = rhs = bcr
   if (!live) return st;
+  __threadfence_block();
   double xnext = dmax_ref(bcr, V.at(A_PSI, n - 1));
   const int top = n - 2;  // this lane's first row going down
-  BwdRow q0b{}, q1b{}, q2b{}, q3b{};
-  if (top >= 1) load_bwd<K>(V, top, q0b);
-  if (top - 1 >= 1) load_bwd<K>(V, top - 1, q1b);
-  if (top - 2 >= 1) load_bwd<K>(V, top - 2, q2b);
-  if (top - 3 >= 1) load_bwd<K>(V, top - 3, q3b);
+  for (int j = 0; j < kRing; ++j) {
+    if (top - j >= 1) issue_bwd<K>(V, R, top - j);
+    cp_commit();
+  }
   for (int i = top; i >= 1; --i) {
-    const BwdRow r = q0b;
-    q0b = q1b;
-    q1b = q2b;
-    q2b = q3b;
-    if (i - 4 >= 1) load_bwd<K>(V, i - 4, q3b);
-    const double nc = (i >= lo && i <= hi) ? -V.at(A_CP, i) : r.nc;
-    const double xv = proj_max(fma(nc, xnext, r.d), r.psi);
+    cp_wait_oldest();
+    const double* s = R + (i % kRingSlots) * kRingSlot;
+    const double rnc = s[0], rpsi = s[kTile], rd = s[2 * kTile];
+    if (i - kRing >= 1) issue_bwd<K>(V, R, i - kRing);
+    cp_commit();
+    const double nc = (i >= lo && i <= hi) ? V.at(A_CP, i) : rnc;
+    const double xv = proj_max(fma(nc, xnext, rd), rpsi);
     V.at(a_out, i) = xv;
     xnext = xv;
   }
@@ -424,6 +449,7 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
     const int32_t* __restrict__ mode, int32_t* __restrict__ status, int* __restrict__ queue,
     MarchConst mc) {
   const int lane = threadIdx.x & (kTile - 1);
+  __shared__ double ring[4][kRingSlots * kRingSlot];  // one ring per warp (128 threads)
   for (;;) {
     int t = 0;
     if (lane == 0) t = atomicAdd(queue, 1);
@@ -444,6 +470,16 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
     const int nt = active ? o.nt : 0;
     const TileView V{pool + td.off + lane, td.nx};
     const uint8_t* F = flags + td.foff + lane;
+    double* R = ring[threadIdx.x / kTile];
+    // Lock-candidate rows of the tile: union over its lanes.
+    int flo = INT_MAX, fhi = -1;
+    for (int i = 1; i < n - 1; ++i)
+      if (ROW(F, i)) {
+        flo = min(flo, i);
+        fhi = i;
+      }
+    flo = __reduce_min_sync(0xffffffffu, flo);
+    fhi = __reduce_max_sync(0xffffffffu, fhi);
     int32_t st = kStatusOk;
     const double dt = o.dt;
     // Snapshot taps: copy the state after the listed steps.
@@ -469,9 +505,9 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
       const double t_mid = 0.0 + 0.5 * dt;
       const double t_next = 0.0 + dt;
       st = stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_mid),
-                             mc.alpha, mc.beta, A_U, A_G, st);
+                             mc.alpha, mc.beta, A_U, A_G, st, flo, fhi, R);
       st = stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_next),
-                             mc.alpha, mc.beta, A_G, A_U, st);
+                             mc.alpha, mc.beta, A_G, A_U, st, flo, fhi, R);
       step = 1;
       if (active && nt >= 1) record(1, A_U);
     }
@@ -483,9 +519,9 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
       const double tn = static_cast<double>(step + 1) * dt;
       const bool last = (step == nt - 1);
       st = stage<kStage1>(live, n, V, F, nocache, o.bc_left, right_bc(o, t1), mc.alpha,
-                          mc.beta, A_U, A_G, st);
+                          mc.beta, A_U, A_G, st, flo, fhi, R);
       st = stage<kStage2>(live, n, V, F, nocache, o.bc_left, right_bc(o, tn), mc.alpha,
-                          mc.beta, A_G, last ? A_G : A_U, st);
+                          mc.beta, A_G, last ? A_G : A_U, st, flo, fhi, R);
       if (live && sc) record(step + 1, last ? A_G : A_U);
     }
     if (active) status[k] = st;

@@ -68,6 +68,15 @@ def make_workload(pkg, n, seed=20251203, uneven=False):
     return params, grids, (S, K, T, sig, r, q, put)
 
 
+def measured_hbm_gbs():
+    """Measured HBM copy bandwidth of the GB300s (MEASURED_PEAKS.json), or None."""
+    f = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(f.read_text())["hbm_gbs"])
+    except Exception:
+        return None
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -486,18 +495,27 @@ def main():
     algo = st["algo_flops"]
     march_s = kt["march_ms"] / 1e3
     achieved = algo / march_s / 1e12
-    traffic = None
+    # DRAM traffic of one launch from the committed ncu capture of this
+    # workload (dram__bytes_read + dram__bytes_write), scaled by row-steps
+    # when the option count differs from the captured one.
+    traffic, hbm = None, None
     tf = ROOT / "profiles" / "march_kernel_traffic.json"
     if tf.exists():
         try:
-            traffic = json.loads(tf.read_text()).get("bytes_per_launch")
+            cap = json.loads(tf.read_text())
+            traffic = cap["bytes_per_row_step"] * n * (NT - 1) * (NX - 2)
         except Exception:
             traffic = None
+    if traffic is not None:
+        hbm_peak = measured_hbm_gbs()
+        hbm = {"traffic_gbs": traffic / march_s / 1e9, "peak_gbs": hbm_peak,
+               "frac": (traffic / march_s / 1e9 / hbm_peak) if hbm_peak else None,
+               "note": "per-option working state (21 KB) re-streamed every step; 1.4 GB >> L2"}
     roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp64_peak, "traffic": traffic,
                 "peak_source": "measured live: mango_gpu_fp64_probe (independent DFMA chains, all SMs)",
                 "kernel": "march_kernel", "kernel_ms": kt["march_ms"],
-                "algo_flops_per_launch": algo}
+                "algo_flops_per_launch": algo, "hbm_streaming": hbm}
 
     extra = {}
     if not args.no_extra and rank == 0:

@@ -108,7 +108,9 @@ typedef struct {
  *   MANGO_GPU_GRID_FIXED_N  estimate_pde_grid with min_spatial_points ==
  *                           max_spatial_points == n_space, then
  *                           PDEGridConfig{spec, n_time}: the reference's own
- *                           sinh-clustered grid at a pinned size;
+ *                           sinh-clustered grid at a pinned size; n_time == 0
+ *                           keeps the estimate's own step count (the
+ *                           GridAccuracyParams alternative of PDEGridSpec);
  *   MANGO_GPU_GRID_SINH     PDEGridConfig{GridSpec::sinh_spaced(x_min, x_max,
  *                           n_space, alpha), n_time};
  *   MANGO_GPU_GRID_UNIFORM  PDEGridConfig{GridSpec::uniform(x_min, x_max,
@@ -184,6 +186,34 @@ MangoStatus mango_gpu_price_american_batch(MangoGpuContext* ctx,
                                            const MangoGpuTrbdf2* trbdf2,
                                            MangoGpuAmericanOut* out,
                                            uint64_t* out_failed, MangoError* err);
+
+/* BatchAmericanOptionSolver::solve_batch(params, use_shared_grid = true,
+ * no setup callback, custom_grid) (src/option/american_option_batch.cpp:
+ * 272-302).  With use_normalized != 0 and a batch that is_normalized_eligible
+ * accepts (american_option_batch.cpp:26-107: one option type, positive spot
+ * and strike, the first option's estimated grid no wider than 5.8 with
+ * spacing <= 0.05 and margins >= max(0.35, 6 dx) around ln(S/K) of every
+ * option), options are grouped by (volatility, rate, dividend yield,
+ * maturity, type) within 1e-10, each group is solved once at S = K = 1 and
+ * every option is read from its group's solution with its own spot and
+ * strike (solve_normalized_chain, american_option_batch.cpp:313-382);
+ * otherwise every option is marched on one grid shared by the batch
+ * (solve_regular_batch, american_option_batch.cpp:384-518).
+ * custom_grid: NULL => the shared grid is estimate_batch_pde_grid over the
+ * batch (src/option/grid_spec_types.cpp:120-177; over the normalised group
+ * option on the chain route); else it is resolved, any kind, for the first
+ * option of the solve (the normalised group option on the chain route).
+ * Options that fail validation do not shape the shared grid and are
+ * reported MANGO_ERR_VALIDATION.  *out_route (nullable) = 1 when the chain
+ * route ran, 0 otherwise.  Other arguments and returns as
+ * mango_gpu_price_american_batch. */
+MangoStatus mango_gpu_price_american_batch_shared(MangoGpuContext* ctx,
+                                                  const MangoPricingParams* params, uint64_t n,
+                                                  const MangoGpuGrid* custom_grid,
+                                                  int32_t use_normalized,
+                                                  const MangoGpuTrbdf2* trbdf2,
+                                                  MangoGpuAmericanOut* out, uint64_t* out_failed,
+                                                  int32_t* out_route, MangoError* err);
 
 /* Batched FDM implied volatility: IVSolver::solve (src/option/iv_solver.cpp:
  * 133-242) with Brent (src/math/root_finding.hpp:145-302) for every quote,

@@ -121,6 +121,10 @@ def library() -> ctypes.CDLL:
             _P, _P, ctypes.c_uint64, _P, ctypes.c_uint64, ctypes.POINTER(MangoGpuTrbdf2), _P,
             ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(MangoError)]
         lib.mango_gpu_price_american_batch.restype = ctypes.c_int32
+        lib.mango_gpu_price_american_batch_shared.argtypes = [
+            _P, _P, ctypes.c_uint64, _P, ctypes.c_int32, ctypes.POINTER(MangoGpuTrbdf2), _P,
+            ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(MangoError)]
+        lib.mango_gpu_price_american_batch_shared.restype = ctypes.c_int32
         lib.mango_gpu_resolve_grid.argtypes = [_P, _P, _P, ctypes.c_int64,
                                                ctypes.POINTER(ctypes.c_int64),
                                                ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(MangoError)]
@@ -361,6 +365,35 @@ class Engine:
         if st != MANGO_OK:
             raise EngineError(f"mango_gpu_price_american_batch: {err.message.decode(errors='replace')}")
         return out
+
+    def price_shared_arrays(self, params: np.ndarray, custom_grid: Optional[np.ndarray] = None,
+                            use_normalized: bool = True, rannacher: bool = True,
+                            gamma: float = 0.0):
+        """Shared-grid batch (mango_gpu_price_american_batch_shared): the
+        normalized chain when use_normalized and the batch is eligible, else
+        one grid for the whole batch.  custom_grid: one GRID_DTYPE record
+        resolved for the first option of the solve, or None for the
+        batch-estimated grid.  Returns (OUT_DTYPE records, route) with route
+        1 for the chain, 0 for the regular shared grid."""
+        params = np.ascontiguousarray(params, dtype=PRICING_DTYPE)
+        n = params.size
+        out = np.zeros(n, dtype=OUT_DTYPE)
+        if custom_grid is not None:
+            custom_grid = np.ascontiguousarray(custom_grid, dtype=GRID_DTYPE)
+            if custom_grid.size != 1:
+                raise ValueError("custom_grid must be a single grid record")
+        tr = MangoGpuTrbdf2(gamma, 1 if rannacher else 0, 0)
+        failed = ctypes.c_uint64()
+        route = ctypes.c_int32()
+        err = MangoError()
+        st = library().mango_gpu_price_american_batch_shared(
+            self._ctx, _ptr(params), n, _ptr(custom_grid), 1 if use_normalized else 0, ctypes.byref(tr),
+            _ptr(out), ctypes.byref(failed), ctypes.byref(route), ctypes.byref(err))
+        if st != MANGO_OK:
+            e = EngineError(f"mango_gpu_price_american_batch_shared: {err.message.decode(errors='replace')}")
+            e.status = st
+            raise e
+        return out, int(route.value)
 
     def solve_iv_arrays(self, queries: np.ndarray, grids: np.ndarray, tol: float = 0.0,
                         max_iter: int = 0, method: int = 0) -> np.ndarray:
@@ -918,22 +951,53 @@ class BatchAmericanOptionResult:
 
 
 class BatchAmericanOptionSolver:
-    """Reference BatchAmericanOptionSolver (american_option_batch.hpp:114);
-    solve_batch prices every option on its own grid in one GPU batch."""
+    """Reference BatchAmericanOptionSolver (american_option_batch.hpp:114).
+    solve_batch without a shared grid prices every option on its own grid in
+    one GPU batch; with use_shared_grid it takes the reference's routing
+    (american_option_batch.cpp:272-302): the normalized chain when
+    use_normalized (default on) and the batch is eligible, else one grid for
+    the whole batch.  A custom_grid is resolved once, for the first option,
+    as the reference's solve_regular_batch does."""
 
     def __init__(self, engine: Optional[Engine] = None):
         self._engine = engine
         self._grid = None
+        self._use_normalized = True
+        self._rannacher = True
+        self._gamma = 0.0
+        self.last_route = None
 
     def set_grid(self, grid) -> None:
+        """Per-option grid for batches without a shared or custom grid."""
         self._grid = grid
+
+    def set_use_normalized(self, enable: bool) -> "BatchAmericanOptionSolver":
+        self._use_normalized = bool(enable)
+        return self
+
+    def use_normalized(self) -> bool:
+        return self._use_normalized
+
+    def set_trbdf2_config(self, gamma: float = 0.0, rannacher_startup: bool = True) -> "BatchAmericanOptionSolver":
+        self._gamma = float(gamma)
+        self._rannacher = bool(rannacher_startup)
+        return self
 
     def solve_batch(self, params: Iterable[PricingParams], use_shared_grid: bool = False,
                     custom_grid=None) -> BatchAmericanOptionResult:
         plist = list(params)
         eng = self._engine or default_engine()
-        grid = custom_grid if custom_grid is not None else self._grid
-        out = eng.price_arrays(_to_array(plist), _grid_entry(grid))
+        arr = _to_array(plist)
+        if use_shared_grid or custom_grid is not None:
+            # Without a shared grid, a custom grid resolved for the first
+            # option serves every option: the shared route minus the chain.
+            cg = None if custom_grid is None else _grid_entry(custom_grid)
+            out, self.last_route = eng.price_shared_arrays(
+                arr, cg, use_normalized=self._use_normalized and use_shared_grid,
+                rannacher=self._rannacher, gamma=self._gamma)
+        else:
+            out = eng.price_arrays(arr, _grid_entry(self._grid), rannacher=self._rannacher, gamma=self._gamma)
+            self.last_route = None
         results = []
         for row, p in zip(out, plist):
             if row["status"] == MANGO_OK:

@@ -100,14 +100,15 @@ std::string resolve(const MangoPricingParams& p, const MangoGpuGrid& g, Resolved
       break;
     case MANGO_GPU_GRID_FIXED_N:
     case MANGO_GPU_GRID_FIXED_N_AT_VOL: {
-      if (g.n_space < 3 || g.n_time < 1) return "grid: n_space >= 3 and n_time >= 1 required";
+      if (g.n_space < 3 || g.n_time < 0) return "grid: n_space >= 3 and n_time >= 0 required";
       const double vol = g.kind == MANGO_GPU_GRID_FIXED_N ? p.volatility : g.alpha;
       if (!(vol > 0.0) || !std::isfinite(vol)) return "grid: sizing volatility must be > 0";
       Accuracy a = def;
       a.min_points = a.max_points = g.n_space;
       int64_t nt_auto = 0;
       estimate_grid(p.spot, p.strike, p.maturity, vol, a, &r->spec, &nt_auto, scratch);
-      r->nt = g.n_time;
+      // n_time 0: the estimate's own step count (GridAccuracyParams alone)
+      r->nt = g.n_time > 0 ? g.n_time : nt_auto;
       break;
     }
     case MANGO_GPU_GRID_SINH:

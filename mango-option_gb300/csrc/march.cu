@@ -536,8 +536,17 @@ namespace {
 // 264-369): solve for the second-derivative terms c_i with the plain Thomas
 // recurrence (thomas_solver.hpp:86-198), then evaluate at xe on interval iv.
 // The lane's A_CP / A_D rows serve as the c' / d' scratch.
+// Thomas scratch of one evaluation: c'_j at cp[j * stride], d'_j at dp[j * stride].
+struct SplineScratch {
+  double* cp;
+  double* dp;
+  size_t stride;
+  __device__ __forceinline__ double& C(int j) const { return cp[static_cast<size_t>(j) * stride]; }
+  __device__ __forceinline__ double& D(int j) const { return dp[static_cast<size_t>(j) * stride]; }
+};
+
 __device__ void spline_at(const double* __restrict__ X, const TileView& V, int ay, int n,
-                          double xe, int iv, double* val, double* der) {
+                          double xe, int iv, const SplineScratch& W, double* val, double* der) {
   auto x = [&](int i) { return ROW(X, i); };
   auto y = [&](int i) { return V.at(ay, i); };
   auto h = [&](int i) { return x(i + 1) - x(i); };
@@ -564,33 +573,33 @@ __device__ void spline_at(const double* __restrict__ X, const TileView& V, int a
       const double diag0 = 2.0 * (h(0) + h(1));
       double cp = h(1) / diag0;
       double dp = rhs(0) / diag0;
-      V.at(A_CP, 0) = cp;
-      V.at(A_D, 0) = dp;
+      W.C(0) = cp;
+      W.D(0) = dp;
       for (int j = 1; j < m - 1; ++j) {
         const double lower = h(j);
         const double denom = fma(-lower, cp, 2.0 * (h(j) + h(j + 1)));
         const double inv = 1.0 / denom;
         cp = h(j + 1) * inv;
         dp = fma(-lower, dp, rhs(j)) * inv;
-        V.at(A_CP, j) = cp;
-        V.at(A_D, j) = dp;
+        W.C(j) = cp;
+        W.D(j) = dp;
       }
       {
         const int j = m - 1;
         const double lower = h(j);
         const double denom = fma(-lower, cp, 2.0 * (h(j) + h(j + 1)));
         dp = fma(-lower, dp, rhs(j)) / denom;
-        V.at(A_D, j) = dp;
+        W.D(j) = dp;
       }
       // back substitution: sol[j] = c[j+1]; only c[iv], c[iv+1] are needed.
-      double s = V.at(A_D, m - 1);
+      double s = W.D(m - 1);
       auto take = [&](int kk, double v) {
         if (kk == iv) ci = v;
         if (kk == iv + 1) ci1 = v;
       };
       take(m, s);
       for (int j = m - 1; j > 0; --j) {
-        s = fma(-V.at(A_CP, j - 1), s, V.at(A_D, j - 1));
+        s = fma(-W.C(j - 1), s, W.D(j - 1));
         take(j, s);
         if (j <= iv) break;
       }
@@ -646,42 +655,22 @@ __device__ int find_interval(const double* __restrict__ X, int n, double xe) {
 
 }  // namespace
 
-// value, delta, gamma, theta per option (american_option_result.cpp:25-121).
-// out4 is in sorted order; u_final is A_G unless (Rannacher && nt == 1).
-__global__ void outputs_kernel(const TileDev* __restrict__ tiles, int ntiles,
-                               const OptDev* __restrict__ opts, const double* __restrict__ xs,
-                               double* __restrict__ pool, const int32_t* __restrict__ mode,
-                               const int32_t* __restrict__ status, MarchConst mc,
-                               double* __restrict__ out4) {
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int t = gt / kTile, lane = gt % kTile;
-  if (t >= ntiles) return;
-  const TileDev td = tiles[t];
-  if (lane >= td.count) return;
-  const int k = td.first + lane;
-  if (mc.active && !mc.active[k]) return;
-  const OptDev o = opts[k];
-  double* res = out4 + 4 * static_cast<size_t>(k);
-  if (status[k] != kStatusOk) {
-    res[0] = res[1] = res[2] = res[3] = __longlong_as_double(0x7ff8000000000000ll);
-    return;
-  }
-  const int n = o.n;
-  const TileView V{pool + td.off + lane, td.nx};
-  const double* X = xs + td.xoff + lane;
-  const bool swap = mc.rannacher && o.nt == 1;
-  const int au = swap ? A_U : A_G;
-  const int aup = swap ? A_G : A_U;
-  const double xs_ = o.x_spot;
+// value, delta, gamma, theta of an option (american_option_result.cpp:25-121)
+// from a solution on grid X: final u in array au, previous in aup, the
+// option's log-moneyness xs_, strike and spot, the solve's dt.
+__device__ void option_outputs(const double* __restrict__ X, const TileView& V, int au, int aup,
+                               int n, double xs_, double strike, double spot, double dt,
+                               bool uniform, bool value_only, const SplineScratch& W,
+                               double* __restrict__ res) {
   const int iv = find_interval(X, n, xs_);
   double sv, sd;
-  spline_at(X, V, au, n, xs_, iv, &sv, &sd);
+  spline_at(X, V, au, n, xs_, iv, W, &sv, &sd);
   double value;
-  if (xs_ <= ROW(X, 0)) value = V.at(au, 0) * o.strike;
-  else if (xs_ >= ROW(X, n - 1)) value = V.at(au, n - 1) * o.strike;
-  else value = dmax_ref(0.0, sv) * o.strike;
-  const double delta = sd * (o.strike / o.spot);
-  if (mc.value_only) {
+  if (xs_ <= ROW(X, 0)) value = V.at(au, 0) * strike;
+  else if (xs_ >= ROW(X, n - 1)) value = V.at(au, n - 1) * strike;
+  else value = dmax_ref(0.0, sv) * strike;
+  const double delta = sd * (strike / spot);
+  if (value_only) {
     res[0] = value;
     res[1] = delta;
     return;
@@ -702,7 +691,6 @@ __global__ void outputs_kernel(const TileDev* __restrict__ tiles, int ntiles,
     il = ir > 0 ? ir - 1 : 0;
     if (fabs(ROW(X, ir) - xs_) < 1e-14) il = ir;
   }
-  const bool uniform = (mode[k] & 2) != 0;
   double d1l, d2l, d1r, d2r;
   stencil_at(X, V, au, n, il, uniform, &d1l, &d2l);
   double d1, d2;
@@ -715,22 +703,82 @@ __global__ void outputs_kernel(const TileDev* __restrict__ tiles, int ntiles,
     d1 = d1l + al * (d1r - d1l);
     d2 = d2l + al * (d2r - d2l);
   }
-  const double kos2 = o.strike / (o.spot * o.spot);
+  const double kos2 = strike / (spot * spot);
   const double gam = fma(kos2, d2, -kos2 * d1);
   // theta: (S_prev(x) - S(x)) / dt * K with an unclamped spline value.
   double pv, pd;
-  spline_at(X, V, aup, n, xs_, iv, &pv, &pd);
-  const double theta = (pv - sv) / o.dt * o.strike;
+  spline_at(X, V, aup, n, xs_, iv, W, &pv, &pd);
+  const double theta = (pv - sv) / dt * strike;
   res[0] = value;
   res[1] = delta;
   res[2] = gam;
   res[3] = theta;
 }
 
-#undef ROW
+// Per option of a batch: out4 in sorted order; u_final is A_G unless
+// (Rannacher && nt == 1).
+__global__ void outputs_kernel(const TileDev* __restrict__ tiles, int ntiles,
+                               const OptDev* __restrict__ opts, const double* __restrict__ xs,
+                               double* __restrict__ pool, const int32_t* __restrict__ mode,
+                               const int32_t* __restrict__ status, MarchConst mc,
+                               double* __restrict__ out4) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = gt / kTile, lane = gt % kTile;
+  if (t >= ntiles) return;
+  const TileDev td = tiles[t];
+  if (lane >= td.count) return;
+  const int k = td.first + lane;
+  if (mc.active && !mc.active[k]) return;
+  const OptDev o = opts[k];
+  double* res = out4 + 4 * static_cast<size_t>(k);
+  if (status[k] != kStatusOk) {
+    res[0] = res[1] = res[2] = res[3] = __longlong_as_double(0x7ff8000000000000ll);
+    return;
+  }
+  const TileView V{pool + td.off + lane, td.nx};
+  const double* X = xs + td.xoff + lane;
+  const bool swap = mc.rannacher && o.nt == 1;
+  const SplineScratch W{&V.at(A_CP, 0), &V.at(A_D, 0), kRowStride};
+  option_outputs(X, V, swap ? A_U : A_G, swap ? A_G : A_U, o.n, o.x_spot, o.strike, o.spot, o.dt,
+                 (mode[k] & 2) != 0, mc.value_only != 0, W, res);
+}
 
-// Diagnostic FP64 FMA throughput probe: 16 independent FMA chains per thread
-// so issue, not latency, bounds it.  The result is stored so the work is kept.
+// BatchAmericanOptionSolver::solve_normalized_chain result extraction
+// (american_option_batch.cpp:313-382): option j reads the S = K = 1
+// solution of its parameter group grp[j] (sorted index in the group batch)
+// and evaluates the functionals with its own spot and strike.  scratch holds
+// 2 x nmax doubles per option, interleaved by option.
+__global__ void chain_outputs_kernel(int nout, const int32_t* __restrict__ grp,
+                                     const double* __restrict__ spot,
+                                     const double* __restrict__ strike,
+                                     const TileDev* __restrict__ tiles,
+                                     const OptDev* __restrict__ opts,
+                                     const double* __restrict__ xs, double* __restrict__ pool,
+                                     const int32_t* __restrict__ mode,
+                                     const int32_t* __restrict__ status, MarchConst mc,
+                                     double* __restrict__ scratch, int nmax,
+                                     double* __restrict__ out4) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nout) return;
+  const int g = grp[j];
+  double* res = out4 + 4 * static_cast<size_t>(j);
+  if (g < 0 || status[g] != kStatusOk) {
+    res[0] = res[1] = res[2] = res[3] = __longlong_as_double(0x7ff8000000000000ll);
+    return;
+  }
+  const OptDev o = opts[g];
+  const TileDev td = tiles[g / kTile];
+  const int lane = g % kTile;
+  const TileView V{pool + td.off + lane, td.nx};
+  const double* X = xs + td.xoff + lane;
+  const bool swap = mc.rannacher && o.nt == 1;
+  const SplineScratch W{scratch + j, scratch + static_cast<size_t>(nmax) * nout + j,
+                        static_cast<size_t>(nout)};
+  const double S = spot[j], K = strike[j];
+  option_outputs(X, V, swap ? A_U : A_G, swap ? A_G : A_U, o.n, log(S / K), K, S, o.dt,
+                 (mode[g] & 2) != 0, false, W, res);
+}
+
 __global__ void fp64_probe_kernel(double* out, int iters) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   double a[16];

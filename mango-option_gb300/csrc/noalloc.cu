@@ -113,7 +113,7 @@ const char* resolve_grid(const MangoPricingParams& p, const MangoGpuGrid& g, Gri
     case MANGO_GPU_GRID_FIXED_N: {
       Accuracy a = def;
       if (g.kind == MANGO_GPU_GRID_FIXED_N) {
-        if (g.n_space < 3 || g.n_time < 1) return "grid: n_space >= 3 and n_time >= 1 required";
+        if (g.n_space < 3 || g.n_time < 0) return "grid: n_space >= 3 and n_time >= 0 required";
         if (g.n_space > kMaxSpace) return "grid: n_space above the no-allocation limit";
         a.min_points = a.max_points = g.n_space;
       }
@@ -121,7 +121,7 @@ const char* resolve_grid(const MangoPricingParams& p, const MangoGpuGrid& g, Gri
       estimate_grid(p.spot, p.strike, p.maturity, p.volatility, a, spec, &nt_auto,
                     g_host.scratch, static_cast<int64_t>(sizeof(g_host.scratch) / sizeof(double)));
       if (spec->n > kMaxSpace) return "grid: n_space above the no-allocation limit";
-      *nt = g.kind == MANGO_GPU_GRID_FIXED_N ? g.n_time : nt_auto;
+      *nt = (g.kind == MANGO_GPU_GRID_FIXED_N && g.n_time > 0) ? g.n_time : nt_auto;
       break;
     }
     case MANGO_GPU_GRID_SINH:

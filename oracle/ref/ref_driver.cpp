@@ -444,4 +444,49 @@ int32_t ref_surface_iv(const int64_t* sizes, const double* grids, const double* 
   return 0;
 }
 
+
+// BatchAmericanOptionSolver::solve_batch with use_shared_grid = true
+// (src/option/american_option_batch.cpp:272-302): the normalized chain when
+// use_normalized and the batch is eligible, else the regular shared-grid
+// batch.  kind 0 = no custom grid; 2 / 3 = PDEGridConfig{sinh_spaced /
+// uniform(x_min, x_max, nx[, alpha]), nt}; 1 = GridAccuracyParams with
+// min == max == nx.  out_dims = [n_space, n_time] per option.
+int32_t ref_batch_shared(int64_t n, const double* S, const double* K, const double* T,
+                         const double* sigma, const double* r, const double* q,
+                         const int32_t* is_put, int32_t use_normalized, int32_t kind,
+                         double x_min, double x_max, int64_t nx, double alpha, int64_t nt,
+                         int32_t n_threads, double* out4, int64_t* out_dims, int32_t* status) {
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+  std::vector<PricingParams> ps;
+  ps.reserve(static_cast<size_t>(n));
+  for (int64_t i = 0; i < n; ++i) ps.push_back(make_params(S[i], K[i], T[i], sigma[i], r[i], q[i], is_put[i]));
+  std::optional<PDEGridSpec> custom;
+  if (kind == 2 || kind == 3) {
+    auto spec = kind == 3 ? GridSpec<double>::uniform(x_min, x_max, static_cast<size_t>(nx))
+                          : GridSpec<double>::sinh_spaced(x_min, x_max, static_cast<size_t>(nx), alpha);
+    if (!spec) return 1;
+    custom = PDEGridSpec{PDEGridConfig{*spec, static_cast<size_t>(nt), {}}};
+  } else if (kind == 1) {
+    GridAccuracyParams acc;
+    acc.min_spatial_points = static_cast<size_t>(nx);
+    acc.max_spatial_points = static_cast<size_t>(nx);
+    custom = PDEGridSpec{acc};
+  }
+  BatchAmericanOptionSolver solver;
+  solver.set_use_normalized(use_normalized != 0);
+  auto res = solver.solve_batch(ps, true, nullptr, custom);
+  for (int64_t i = 0; i < n; ++i) {
+    const auto& ri = res.results[static_cast<size_t>(i)];
+    if (!ri) { status[i] = 5; continue; }
+    status[i] = 0;
+    out4[4 * i + 0] = ri->value();
+    out4[4 * i + 1] = ri->delta();
+    out4[4 * i + 2] = ri->gamma();
+    out4[4 * i + 3] = ri->theta();
+    out_dims[2 * i + 0] = static_cast<int64_t>(ri->grid()->n_space());
+    out_dims[2 * i + 1] = static_cast<int64_t>(ri->grid()->time().n_steps());
+  }
+  return 0;
+}
+
 }  // extern "C"

@@ -242,6 +242,7 @@ def main():
     golden_table(lib)
     golden_surface(lib)
     golden_interp_iv(lib)
+    golden_shared(lib)
 
 
 def table_axes(nm, ntau, ns, nr):
@@ -379,6 +380,68 @@ def golden_interp_iv(lib):
                               ctypes.c_int32(1), P(cfg), P(qs), ctypes.c_int64(n), P(out), P(st)) == 0
     save("interp_iv.npz", sizes=sizes, grids=grids, coeffs=coeffs, vega_params=vp, vega=vega, quotes=qs,
          true_vol=vt, cfg=cfg, out=out.reshape(n, 3), status=st)
+
+
+
+def shared_batch(lib, S, K, T, sig, r, q, put, use_normalized, kind=0, x_min=0.0, x_max=0.0, nx=0,
+                 alpha=0.0, nt=0):
+    n = len(S)
+    args = [np.ascontiguousarray(a, dtype=np.float64) for a in (S, K, T, sig, r, q)]
+    put = np.ascontiguousarray(put, dtype=np.int32)
+    out = np.full(4 * n, np.nan)
+    dims = np.zeros(2 * n, np.int64)
+    st = np.zeros(n, np.int32)
+    rc = lib.ref_batch_shared(ctypes.c_int64(n), *(P(a) for a in args), P(put), ctypes.c_int32(use_normalized),
+                              ctypes.c_int32(kind), ctypes.c_double(x_min), ctypes.c_double(x_max),
+                              ctypes.c_int64(nx), ctypes.c_double(alpha), ctypes.c_int64(nt), ctypes.c_int32(8),
+                              P(out), P(dims), P(st))
+    assert rc == 0
+    return out.reshape(n, 4), dims.reshape(n, 2), st
+
+
+def golden_shared(lib):
+    """BatchAmericanOptionSolver::solve_batch(use_shared_grid = true): option
+    chains (several strikes per (sigma, r, q, T) group) on the normalized
+    route, and batches the route rejects (mixed types, a wide grid) on the
+    regular shared grid, with and without custom grids."""
+    rng = np.random.default_rng(41)
+    groups = [(0.2, 0.03, 0.01, 1.0), (0.25, 0.05, 0.0, 0.5), (0.3, 0.02, 0.02, 1.5), (0.15, 0.04, 0.01, 0.25),
+              (0.35, 0.0, 0.0, 0.75), (0.22, 0.06, 0.03, 2.0)]
+    rows = []
+    for g in groups:
+        for K in rng.uniform(86.0, 116.0, 9):
+            rows.append((100.0, K) + g)
+    rows.append((97.0, 101.0) + groups[0])            # a different spot in group 0
+    rows.append((100.0, 100.0, 0.2 + 5e-11, 0.03, 0.01, 1.0))  # within the 1e-10 grouping tolerance
+    chain = np.array(rows)
+    n = len(chain)
+    S, K, sig, r, q, T = (np.ascontiguousarray(chain[:, i]) for i in range(6))
+    put = np.ones(n, np.int32)
+    none = (0, 0.0, 0.0, 0, 0.0, 0)
+    mixed = (np.arange(n) % 3 == 0).astype(np.int32)
+    wide_sig = sig.copy()
+    wide_sig[0] = 0.6
+    wide_T = T.copy()
+    wide_T[0] = 2.0
+    cases = {
+        "chain": (T, sig, put, 1, none),
+        "chain_sinh": (T, sig, put, 1, (2, -2.5, 2.5, 181, 2.0, 300)),
+        "chain_fixed_n": (T, sig, put, 1, (1, 0.0, 0.0, 141, 0.0, 0)),
+        "chain_regular": (T, sig, put, 0, none),
+        "mixed": (T, sig, mixed, 1, none),
+        "mixed_fixed_n": (T, sig, mixed, 1, (1, 0.0, 0.0, 151, 0.0, 0)),
+        "mixed_uniform": (T, sig, mixed, 1, (3, -3.0, 3.0, 201, 0.0, 250)),
+        "wide": (wide_T, wide_sig, put, 1, none),
+    }
+    kw = {"S": S, "K": K, "T": T, "sig": sig, "r": r, "q": q, "put": put, "mixed": mixed, "wide_sig": wide_sig,
+          "wide_T": wide_T}
+    for name, (T_, sg, p_, un, grid) in cases.items():
+        out, dims, st = shared_batch(lib, S, K, T_, sg, r, q, p_, un, *grid)
+        assert (st == 0).all(), name
+        kw[f"{name}_out"] = out
+        kw[f"{name}_dims"] = dims
+        kw[f"{name}_grid"] = np.array(grid, dtype=np.float64)
+    save("shared.npz", **kw)
 
 
 if __name__ == "__main__":

@@ -232,16 +232,88 @@ class OptionType(enum.IntEnum):
 
 
 @dataclasses.dataclass
+class Dividend:
+    """Reference Dividend (src/option/option_spec.hpp:158-161): a cash
+    amount paid at calendar_time years from the valuation date."""
+    calendar_time: float = 0.0
+    amount: float = 0.0
+
+
+class YieldCurve:
+    """Reference YieldCurve (src/option/yield_curve.hpp): tenor points
+    (tenor, ln D(tenor)) sorted by tenor, the first at t = 0; ln D linear
+    between tenors, so the forward rate is constant on each interval."""
+
+    def __init__(self, points):
+        self.points = [(float(t), float(ld)) for t, ld in points]
+
+    @staticmethod
+    def flat(rate: float) -> "YieldCurve":
+        return YieldCurve([(0.0, 0.0), (100.0, -rate * 100.0)])
+
+    @staticmethod
+    def from_points(points) -> "YieldCurve":
+        pts = sorted(((float(t), float(ld)) for t, ld in points), key=lambda p: p[0])
+        if not pts:
+            raise ValueError("Empty points vector")
+        if pts[0][0] != 0.0:
+            raise ValueError("First point must have t=0")
+        if abs(pts[0][1]) > 1e-10:
+            raise ValueError("log_discount at t=0 must be 0")
+        for a, b in zip(pts, pts[1:]):
+            if b[0] <= a[0] + 1e-10:
+                raise ValueError("Tenors must be strictly increasing")
+        return YieldCurve(pts)
+
+    @staticmethod
+    def from_discounts(tenors, discounts) -> "YieldCurve":
+        if len(tenors) != len(discounts):
+            raise ValueError("Tenors and discounts must have same size")
+        if any(d <= 0.0 for d in discounts):
+            raise ValueError("Discount factors must be positive")
+        return YieldCurve.from_points([(t, float(np.log(d))) for t, d in zip(tenors, discounts)])
+
+    def log_discount(self, t: float) -> float:
+        p = self.points
+        if len(p) < 2 or t <= 0.0:
+            return 0.0
+        j = next((k for k, q in enumerate(p) if t < q[0]), len(p))
+        if j == 0:
+            return 0.0
+        if j == len(p):
+            rate = -(p[-1][1] - p[-2][1]) / (p[-1][0] - p[-2][0])
+            return p[-1][1] - rate * (t - p[-1][0])
+        a = (t - p[j - 1][0]) / (p[j][0] - p[j - 1][0])
+        return p[j - 1][1] + a * (p[j][1] - p[j - 1][1])
+
+    def discount(self, t: float) -> float:
+        return float(np.exp(self.log_discount(t)))
+
+    def rate(self, t: float) -> float:
+        p = self.points
+        if len(p) < 2:
+            return 0.0
+        j = 0 if t <= 0.0 else next((k for k, q in enumerate(p) if t < q[0]), len(p))
+        idx = 0 if j == 0 else (len(p) - 2 if j == len(p) else j - 1)
+        return -(p[idx + 1][1] - p[idx][1]) / (p[idx + 1][0] - p[idx][0])
+
+    def zero_rate(self, t: float) -> float:
+        return self.rate(0.0) if t <= 0.0 else -self.log_discount(t) / t
+
+
+@dataclasses.dataclass
 class PricingParams:
-    """Reference PricingParams (src/option/option_spec.hpp:262-281), constant
-    rate and continuous dividend yield."""
+    """Reference PricingParams (src/option/option_spec.hpp:262-281): rate is
+    a constant or a YieldCurve; discrete_dividends a list of Dividend on top
+    of the continuous dividend_yield."""
     spot: float = 0.0
     strike: float = 0.0
     maturity: float = 0.0
-    rate: float = 0.0
+    rate: object = 0.0
     dividend_yield: float = 0.0
     option_type: OptionType = OptionType.CALL
     volatility: float = 0.0
+    discrete_dividends: list = dataclasses.field(default_factory=list)
 
 
 @dataclasses.dataclass
@@ -274,6 +346,44 @@ def pricing_array(spot, strike, maturity, volatility, rate, dividend_yield, is_p
     a["volatility"], a["rate_const"], a["dividend_yield"] = cols[3].ravel(), cols[4].ravel(), cols[5].ravel()
     a["option_type"] = np.where(cols[6].ravel() != 0, 1, 0).astype(np.int32)
     return a
+
+
+class _Records(np.ndarray):
+    """PRICING_DTYPE records that own the schedules their pointers reach."""
+
+
+def attach_schedules(records: np.ndarray, curves=None, dividends=None):
+    """Point MangoPricingParams records at yield curves and dividend
+    schedules (the C struct's tenor_points / dividends pointers).
+    curves[i]: None, a YieldCurve or (k, 2) (tenor, log discount) pairs;
+    dividends[i]: None, a list of Dividend or (k, 2) (calendar time, amount)
+    pairs.  Returns the buffers the pointers reach: keep them alive while the
+    records are in use."""
+    n = records.size
+    def pairs(v, kind):
+        if v is None:
+            return np.zeros((0, 2))
+        if isinstance(v, YieldCurve):
+            return np.asarray(v.points, dtype=np.float64).reshape(-1, 2)
+        if kind == "div" and len(v) and isinstance(v[0], Dividend):
+            return np.asarray([(d.calendar_time, d.amount) for d in v], dtype=np.float64).reshape(-1, 2)
+        return np.asarray(v, dtype=np.float64).reshape(-1, 2)
+    keep = []
+    for key, cnt, vals, kind in (("tenor_points", "n_tenor_points", curves, "curve"),
+                                 ("dividends", "n_dividends", dividends, "div")):
+        if vals is None:
+            continue
+        blocks = [pairs(v, kind) for v in vals]
+        if len(blocks) != n:
+            raise ValueError(f"{key}: one entry per record required")
+        counts = np.array([b.shape[0] for b in blocks], dtype=np.uint64)
+        flat = np.ascontiguousarray(np.concatenate(blocks + [np.zeros((1, 2))]), dtype=np.float64)
+        offs = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.uint64)
+        base = flat.ctypes.data
+        records[key] = np.where(counts > 0, base + 16 * offs, 0).astype(np.uint64)
+        records[cnt] = counts
+        keep.append(flat)
+    return keep
 
 
 def query_array(spot, strike, maturity, rate, dividend_yield, is_put, market_price) -> np.ndarray:
@@ -897,10 +1007,19 @@ def default_engine() -> Engine:
 
 
 def _to_array(params: Sequence[PricingParams]) -> np.ndarray:
-    return pricing_array([p.spot for p in params], [p.strike for p in params],
-                         [p.maturity for p in params], [p.volatility for p in params],
-                         [p.rate for p in params], [p.dividend_yield for p in params],
-                         [int(p.option_type == OptionType.PUT) for p in params])
+    curve = [p.rate if isinstance(p.rate, YieldCurve) else None for p in params]
+    divs = [p.discrete_dividends or None for p in params]
+    a = pricing_array([p.spot for p in params], [p.strike for p in params],
+                      [p.maturity for p in params], [p.volatility for p in params],
+                      [0.0 if c is not None else p.rate for c, p in zip(curve, params)],
+                      [p.dividend_yield for p in params],
+                      [int(p.option_type == OptionType.PUT) for p in params])
+    if not any(c is not None for c in curve) and not any(divs):
+        return a
+    rec = a.view(_Records)
+    rec._keep = attach_schedules(rec, curve if any(c is not None for c in curve) else None,
+                                 divs if any(divs) else None)
+    return rec
 
 
 @dataclasses.dataclass

@@ -76,24 +76,134 @@ void parallel_for(int64_t n, const std::function<void(int64_t)>& f) {
   for (auto& x : th) x.join();
 }
 
-std::string validate(const MangoPricingParams& p) {
+std::string validate(const MangoPricingParams& p, bool allow_tv) {
   // validate_pricing_params (src/option/option_spec.cpp:8-40, 117-157)
   if (!(p.spot > 0.0) || !std::isfinite(p.spot)) return "invalid spot";
   if (!(p.strike > 0.0) || !std::isfinite(p.strike)) return "invalid strike";
   if (!(p.maturity > 0.0) || !std::isfinite(p.maturity)) return "invalid maturity";
-  if (!std::isfinite(p.rate_const)) return "invalid rate";
+  if (p.n_tenor_points == 0 && !std::isfinite(p.rate_const)) return "invalid rate";
   if (p.dividend_yield < 0.0 || !std::isfinite(p.dividend_yield)) return "invalid dividend yield";
   if (!(p.volatility > 0.0) || !std::isfinite(p.volatility)) return "invalid volatility";
   if (p.option_type != MANGO_PUT && p.option_type != MANGO_CALL) return "invalid option type";
-  if (p.n_tenor_points != 0) return "yield curves are not supported by the GPU engine";
-  if (p.n_dividends != 0) return "discrete dividends are not supported by the GPU engine";
+  if (!allow_tv) {
+    if (p.n_tenor_points != 0) return "yield curves are not supported by this entry point";
+    if (p.n_dividends != 0) return "discrete dividends are not supported by this entry point";
+    return {};
+  }
+  if (p.n_tenor_points != 0) {
+    // build_rate + YieldCurve::from_points (src/ffi/mango_c_api.cpp:44-64,
+    // src/option/yield_curve.hpp): sorted by tenor, the first at t = 0 with
+    // log discount 0, tenors strictly increasing.  Non-finite entries are
+    // rejected too.
+    if (!p.tenor_points) return "tenor_points is null but n_tenor_points > 0";
+    std::vector<MangoTenorPoint> pts(p.tenor_points, p.tenor_points + p.n_tenor_points);
+    for (const auto& t : pts)
+      if (!std::isfinite(t.tenor) || !std::isfinite(t.log_discount))
+        return "invalid yield curve: non-finite tenor point";
+    std::sort(pts.begin(), pts.end(),
+              [](const MangoTenorPoint& a, const MangoTenorPoint& b) { return a.tenor < b.tenor; });
+    if (pts[0].tenor != 0.0) return "invalid yield curve: First point must have t=0";
+    if (std::abs(pts[0].log_discount) > 1e-10)
+      return "invalid yield curve: log_discount at t=0 must be 0";
+    for (size_t i = 1; i < pts.size(); ++i)
+      if (pts[i].tenor <= pts[i - 1].tenor + 1e-10)
+        return "invalid yield curve: Tenors must be strictly increasing";
+  }
+  if (p.n_dividends != 0) {
+    if (!p.dividends) return "dividends is null but n_dividends > 0";
+    for (uint64_t i = 0; i < p.n_dividends; ++i) {
+      const MangoDividend& d = p.dividends[i];
+      if (d.calendar_time < 0.0 || d.calendar_time > p.maturity) return "invalid dividend time";
+      if (d.amount < 0.0) return "invalid dividend amount";
+      if (!std::isfinite(d.calendar_time) || !std::isfinite(d.amount)) return "invalid dividend";
+    }
+  }
   return {};
+}
+
+bool time_varying(const MangoPricingParams& p) {
+  if (p.n_tenor_points != 0) return true;
+  for (uint64_t i = 0; i < p.n_dividends; ++i) {
+    const double tau = p.maturity - p.dividends[i].calendar_time;
+    if (tau > 0.0 && tau < p.maturity) return true;
+  }
+  return false;
+}
+
+namespace {
+// Times to expiry of the dividends inside (0, T) and their largest
+// amount / strike (estimate_pde_grid, grid_spec_types.cpp:59-67, 96-103).
+void dividend_taus(const MangoPricingParams& p, std::vector<double>* taus, double* max_dk) {
+  taus->clear();
+  *max_dk = 0.0;
+  for (uint64_t i = 0; i < p.n_dividends; ++i) {
+    const double tau = p.maturity - p.dividends[i].calendar_time;
+    if (tau > 0.0 && tau < p.maturity) {
+      taus->push_back(tau);
+      *max_dk = std::max(*max_dk, p.dividends[i].amount / p.strike);
+    }
+  }
+}
+}  // namespace
+
+void explicit_time_domain(double maturity, int64_t n_time, const std::vector<double>& taus,
+                          Resolved* r) {
+  // resolve_grid for a PDEGridConfig (american_option.cpp:64-72)
+  if (taus.empty()) {
+    r->tp.clear();
+    r->nt = n_time;
+    return;
+  }
+  time_points(0.0, maturity, maturity / static_cast<double>(n_time), taus, &r->tp, &r->nt);
 }
 
 std::string resolve(const MangoPricingParams& p, const MangoGpuGrid& g, Resolved* r,
                     std::vector<double>* scratch) {
   // resolve_grid (src/option/american_option.cpp:54-73)
   const Accuracy def = default_accuracy();
+  r->tv = time_varying(p);
+  r->tp.clear();
+  if (r->tv) {
+    // Dividends widen the estimated grid and add mandatory time points; an
+    // explicit grid takes them as the PDEGridConfig's mandatory times, as
+    // BatchAmericanOptionSolver attaches them (american_option_batch.cpp:
+    // 447-470).
+    std::vector<double> taus;
+    double max_dk = 0.0;
+    dividend_taus(p, &taus, &max_dk);
+    switch (g.kind) {
+      case MANGO_GPU_GRID_AUTO:
+        estimate_grid_div(p.spot, p.strike, p.maturity, p.volatility, def, taus, max_dk, &r->spec,
+                          &r->nt, &r->tp, scratch);
+        break;
+      case MANGO_GPU_GRID_FIXED_N:
+      case MANGO_GPU_GRID_FIXED_N_AT_VOL: {
+        if (g.n_space < 3 || g.n_time < 0) return "grid: n_space >= 3 and n_time >= 0 required";
+        const double vol = g.kind == MANGO_GPU_GRID_FIXED_N ? p.volatility : g.alpha;
+        if (!(vol > 0.0) || !std::isfinite(vol)) return "grid: sizing volatility must be > 0";
+        Accuracy a = def;
+        a.min_points = a.max_points = g.n_space;
+        estimate_grid_div(p.spot, p.strike, p.maturity, vol, a, taus, max_dk, &r->spec, &r->nt,
+                          &r->tp, scratch);
+        if (g.n_time > 0) explicit_time_domain(p.maturity, g.n_time, taus, r);
+        break;
+      }
+      case MANGO_GPU_GRID_SINH:
+      case MANGO_GPU_GRID_UNIFORM:
+        if (g.n_space < 3 || g.n_time < 1) return "grid: n_space >= 3 and n_time >= 1 required";
+        if (!(g.x_min < g.x_max)) return "grid: x_min < x_max required";
+        if (g.kind == MANGO_GPU_GRID_SINH && !(g.alpha > 0.0)) return "grid: alpha > 0 required";
+        r->spec = g.kind == MANGO_GPU_GRID_SINH ? sinh_spec(g.x_min, g.x_max, g.n_space, g.alpha)
+                                                : uniform_spec(g.x_min, g.x_max, g.n_space);
+        explicit_time_domain(p.maturity, g.n_time, taus, r);
+        break;
+      default:
+        return "grid: unknown kind";
+    }
+    if (r->spec.n > 100000) return "grid: n_space above 100000";
+    if (r->nt > 100000000 || r->nt < 1) return "grid: n_time outside [1, 1e8]";
+    return {};
+  }
   switch (g.kind) {
     case MANGO_GPU_GRID_AUTO:
       estimate_grid(p.spot, p.strike, p.maturity, p.volatility, def, &r->spec, &r->nt, scratch);
@@ -159,7 +269,8 @@ MarchConst make_const(const MangoGpuTrbdf2* trbdf2) {
 void destroy_batch(MangoGpuBatch* b) {
   if (!b) return;
   for (mgpu::DevBuf* d : {&b->d_pool, &b->d_xs, &b->d_flags, &b->d_opts, &b->d_tiles, &b->d_mode,
-                          &b->d_status, &b->d_out4, &b->d_queue})
+                          &b->d_status, &b->d_out4, &b->d_queue, &b->d_tv, &b->d_tv_tp,
+                          &b->d_tv_curve, &b->d_tv_ev})
     d->release();
   for (mgpu::HostBuf* h : {&b->h_xs, &b->h_opts, &b->h_tiles, &b->h_out4, &b->h_status})
     h->release();
@@ -181,7 +292,7 @@ MangoGpuBatch* create_batch(MangoGpuContext* ctx, const MangoPricingParams* para
     thread_local std::vector<double> scratch;
     Resolved& r = res[i];
     r.orig = static_cast<int32_t>(i);
-    std::string m = validate(params[i]);
+    std::string m = validate(params[i], true);
     if (m.empty()) {
       MangoGpuGrid g{};
       g.kind = MANGO_GPU_GRID_AUTO;
@@ -231,6 +342,7 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
   std::sort(order.begin(), order.end(), [&](int32_t a, int32_t c) {
     const Resolved& ra = b->res[a];
     const Resolved& rc = b->res[c];
+    if (ra.tv != rc.tv) return rc.tv;  // time-varying options last
     if (ra.spec.n != rc.spec.n) return ra.spec.n > rc.spec.n;
     if (ra.nt != rc.nt) return ra.nt > rc.nt;
     const int pa = params[ra.orig].option_type, pc = params[rc.orig].option_type;
@@ -255,9 +367,11 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
       nx = std::max<int64_t>(nx, r.spec.n);
       nt = std::max<int64_t>(nt, r.nt);
       // Algorithmic FP64 work (FMA = 2): 28 per row per TR-BDF2 step, 18 per
-      // row for the Rannacher start, 20 per row for the output splines.
+      // row for the Rannacher start, 20 per row for the output splines; the
+      // time-varying march refactors both stage matrices: 64 per row per step.
       const double steps = static_cast<double>(r.nt) - (mc.rannacher ? 1.0 : 0.0);
-      flops += static_cast<double>(r.spec.n) * (28.0 * steps + (mc.rannacher ? 18.0 : 0.0) + 20.0);
+      flops += static_cast<double>(r.spec.n) *
+               ((r.tv ? 64.0 : 28.0) * steps + (mc.rannacher ? 18.0 : 0.0) + 20.0);
     }
     td.nx = static_cast<int32_t>(nx);
     td.nt = static_cast<int32_t>(nt);
@@ -304,6 +418,73 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
       o.orig = r.orig;
     }
   });
+  // Time-varying options: per-option data, time points, curves, events.
+  int64_t nc = 0;
+  while (nc < m && !b->res[order[nc]].tv) ++nc;
+  std::vector<TvDev> tvh;
+  std::vector<double> tph, curveh, evh;
+  if (nc < m) {
+    b->mc.tv_first = static_cast<int32_t>(nc);
+    b->tv_tile0 = static_cast<int32_t>(nc / kTile);
+    tvh.resize(static_cast<size_t>(m - nc));
+    for (int64_t k = nc; k < m; ++k) {
+      const Resolved& r = b->res[order[k]];
+      const MangoPricingParams& p = params[r.orig];
+      TvDev& d = tvh[static_cast<size_t>(k - nc)];
+      d = TvDev{};
+      d.T = p.maturity;
+      d.r = p.rate_const;
+      d.tp_off = -1;
+      if (!r.tp.empty()) {
+        d.tp_off = static_cast<int32_t>(tph.size());
+        tph.insert(tph.end(), r.tp.begin(), r.tp.end());
+      }
+      d.curve_off = static_cast<int32_t>(curveh.size() / 2);
+      if (p.n_tenor_points) {
+        std::vector<MangoTenorPoint> pts(p.tenor_points, p.tenor_points + p.n_tenor_points);
+        std::sort(pts.begin(), pts.end(), [](const MangoTenorPoint& a, const MangoTenorPoint& c) {
+          return a.tenor < c.tenor;
+        });
+        for (const auto& t : pts) {
+          curveh.push_back(t.tenor);
+          curveh.push_back(t.log_discount);
+        }
+        d.n_curve = static_cast<int32_t>(pts.size());
+      }
+      // filter_and_merge_dividends (src/option/dividend_utils.hpp): inside
+      // (0, T) with a positive amount, sorted by date, same-date amounts
+      // summed; one event per dividend at tau = T - t with D/K
+      // (american_option.cpp:119-144), sorted by tau.
+      std::vector<MangoDividend> divs;
+      for (uint64_t i = 0; i < p.n_dividends; ++i) {
+        const MangoDividend& dv = p.dividends[i];
+        if (dv.calendar_time > 0.0 && dv.calendar_time < p.maturity && dv.amount > 0.0)
+          divs.push_back(dv);
+      }
+      std::sort(divs.begin(), divs.end(), [](const MangoDividend& a, const MangoDividend& c) {
+        return a.calendar_time < c.calendar_time;
+      });
+      std::vector<MangoDividend> merged;
+      for (const auto& dv : divs) {
+        if (!merged.empty() && std::abs(merged.back().calendar_time - dv.calendar_time) < 1e-12)
+          merged.back().amount += dv.amount;
+        else
+          merged.push_back(dv);
+      }
+      std::vector<std::pair<double, double>> ev;
+      for (const auto& dv : merged) ev.emplace_back(p.maturity - dv.calendar_time, dv.amount / p.strike);
+      std::sort(ev.begin(), ev.end(),
+                [](const std::pair<double, double>& a, const std::pair<double, double>& c) {
+                  return a.first < c.first;
+                });
+      d.ev_off = static_cast<int32_t>(evh.size() / 2);
+      d.n_ev = static_cast<int32_t>(ev.size());
+      for (const auto& e : ev) {
+        evh.push_back(e.first);
+        evh.push_back(e.second);
+      }
+    }
+  }
   b->host_prep_ms = ms_since(t0);
 
   if (m > 0) {
@@ -322,9 +503,21 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
     check(cudaMemcpyAsync(d_opts, opts, sizeof(OptDev) * m, cudaMemcpyHostToDevice, st), "H2D options");
     check(cudaMemcpyAsync(d_tiles, tiles, sizeof(TileDev) * ntiles, cudaMemcpyHostToDevice, st),
           "H2D tiles");
+    double tv_bytes = 0;
+    if (!tvh.empty()) {
+      auto up = [&](DevBuf& d, const void* src, size_t bytes) {
+        void* dst = d.get(bytes);
+        if (bytes) check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st), "H2D tv");
+        tv_bytes += static_cast<double>(bytes);
+      };
+      up(b->d_tv, tvh.data(), sizeof(TvDev) * tvh.size());
+      up(b->d_tv_tp, tph.data(), sizeof(double) * tph.size());
+      up(b->d_tv_curve, curveh.data(), sizeof(double) * curveh.size());
+      up(b->d_tv_ev, evh.data(), sizeof(double) * evh.size());
+    }
     check(cudaEventRecord(b->ev[1], st), "event");
     b->h2d_bytes = static_cast<double>(sizeof(double) * xoff + sizeof(OptDev) * m +
-                                       sizeof(TileDev) * ntiles);
+                                       sizeof(TileDev) * ntiles) + tv_bytes;
   }
   return b.release();
 }
@@ -366,6 +559,15 @@ void run_batch(MangoGpuBatch* b) {
                                                         d_mode, d_status, b->d_queue.as<int>(),
                                                         b->mc);
   check(cudaGetLastError(), "march_kernel launch");
+  if (b->mc.tv_first < m) {
+    const int tv_tiles = ntiles - b->tv_tile0;
+    const int tv_blocks = std::max(1, std::min<int>(ctx->num_sms * 8, (tv_tiles + 3) / 4));
+    march_tv_kernel<<<tv_blocks, 128, 0, st>>>(
+        d_tiles, b->tv_tile0, ntiles, d_opts, b->d_tv.as<TvDev>(), b->d_tv_tp.as<double>(),
+        b->d_tv_curve.as<double>(), b->d_tv_ev.as<double>(), d_xs, d_pool, d_mode, d_status,
+        b->mc);
+    check(cudaGetLastError(), "march_tv_kernel launch");
+  }
   check(cudaEventRecord(b->ev[4], st), "event");
   check(cudaEventRecord(b->run_ev[slot + 2], st), "event");
   outputs_kernel<<<(threads + 127) / 128, 128, 0, st>>>(d_tiles, ntiles, d_opts, d_xs, d_pool,
@@ -424,7 +626,7 @@ uint64_t fetch_batch(MangoGpuBatch* b, MangoGpuAmericanOut* out, std::string* fi
   S.algo_flops = b->algo_flops;
   S.h2d_bytes = b->h2d_bytes;
   S.host_prep_ms = b->host_prep_ms;
-  S.kernel_launches = m > 0 ? 3 : 0;
+  S.kernel_launches = m > 0 ? (b->mc.tv_first < m ? 4 : 3) : 0;
   return failed;
 }
 
@@ -653,7 +855,7 @@ MangoStatus mango_gpu_resolve_grid(const MangoPricingParams* params, const Mango
     return MANGO_ERR_VALIDATION;
   }
   try {
-    std::string m = validate(*params);
+    std::string m = validate(*params, true);
     Resolved r;
     std::vector<double> scratch;
     if (m.empty()) {

@@ -47,6 +47,8 @@ struct Resolved {
   int64_t nt = 0;
   int32_t status = 0;  // MangoStatus; non-zero options never reach the GPU
   int32_t orig = 0;
+  bool tv = false;         // yield curve or dividends: the time-varying march
+  std::vector<double> tp;  // explicit time points (n_time + 1), empty: i * T / n_time
 };
 
 // Timings of the last batch call (milliseconds) and work counters.
@@ -60,7 +62,15 @@ struct Stats {
 
 // Validation (validate_pricing_params plus the engine's scope) and grid
 // resolution; empty string when the option is accepted.
-std::string validate(const MangoPricingParams& p);
+// allow_tv: accept yield curves and discrete dividends (the pricing batch
+// entry points); otherwise they are rejected with a message.
+std::string validate(const MangoPricingParams& p, bool allow_tv = false);
+// The option needs the time-varying march: a yield curve, or a dividend
+// strictly inside (0, T).
+bool time_varying(const MangoPricingParams& p);
+// PDEGridConfig{spec, n_time, dividend times} time domain (resolve_grid).
+void explicit_time_domain(double maturity, int64_t n_time, const std::vector<double>& taus,
+                          Resolved* r);
 std::string resolve(const MangoPricingParams& p, const MangoGpuGrid& g, Resolved* r,
                     std::vector<double>* scratch);
 
@@ -112,6 +122,10 @@ __global__ void march_kernel(const TileDev*, int, const OptDev*, double*, const 
                              const int32_t*, int32_t*, int*, MarchConst);
 __global__ void outputs_kernel(const TileDev*, int, const OptDev*, const double*, double*,
                                const int32_t*, const int32_t*, MarchConst, double*);
+// Time-varying march (march_tv.cu).
+__global__ void march_tv_kernel(const TileDev*, int, int, const OptDev*, const TvDev*,
+                                const double*, const double*, const double*, const double*,
+                                double*, int32_t*, int32_t*, MarchConst);
 }  // namespace mgpu
 
 struct MangoGpuContext {
@@ -135,6 +149,10 @@ struct MangoGpuBatch {
   double h2d_bytes = 0;
   double host_prep_ms = 0;
   mgpu::DevBuf d_pool, d_xs, d_flags, d_opts, d_tiles, d_mode, d_status, d_out4, d_queue;
+  // Time-varying options (sorted last, from mc.tv_first): per-option data,
+  // explicit time points, yield-curve pairs, dividend-event pairs.
+  mgpu::DevBuf d_tv, d_tv_tp, d_tv_curve, d_tv_ev;
+  int32_t tv_tile0 = 0;  // first tile holding a time-varying option
   mgpu::HostBuf h_xs, h_opts, h_tiles, h_out4, h_status;
   cudaEvent_t ev[8] = {};
   bool ran = false;

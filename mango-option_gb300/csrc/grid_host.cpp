@@ -1,6 +1,8 @@
 // grid_host.cpp -- see grid_host.hpp.  Reference formulas, reference order.
 #include "grid_host.hpp"
 
+#include <algorithm>
+
 #include <cfloat>
 #include <cmath>
 
@@ -200,6 +202,106 @@ void estimate_grid(double spot, double strike, double maturity, double sigma,
   int64_t nt = static_cast<int64_t>(std::ceil(maturity / dt));
   if (nt > acc.max_steps) nt = acc.max_steps;
   *n_time = nt;
+}
+
+void time_points(double t0, double t1, double dt, std::vector<double> mandatory,
+                 std::vector<double>* pts, int64_t* n_steps) {
+  // TimeDomain::with_mandatory_points (src/pde/core/time_domain.hpp)
+  std::vector<double> breaks;
+  for (double t : mandatory)
+    if (t > t0 + 1e-14 && t < t1 - 1e-14) breaks.push_back(t);
+  std::sort(breaks.begin(), breaks.end());
+  // std::unique: drop each point within 1e-14 of the last point kept
+  size_t kept = 0;
+  for (size_t i = 0; i < breaks.size(); ++i)
+    if (kept == 0 || !(std::abs(breaks[kept - 1] - breaks[i]) < 1e-14)) breaks[kept++] = breaks[i];
+  breaks.resize(kept);
+  pts->clear();
+  if (breaks.empty()) {
+    *n_steps = static_cast<int64_t>(std::ceil((t1 - t0) / dt));
+    return;
+  }
+  std::vector<double> bounds;
+  bounds.push_back(t0);
+  for (double b : breaks) bounds.push_back(b);
+  bounds.push_back(t1);
+  pts->push_back(t0);
+  for (size_t seg = 0; seg + 1 < bounds.size(); ++seg) {
+    const double s0 = bounds[seg], s1 = bounds[seg + 1];
+    const double len = s1 - s0;
+    int64_t n_sub = static_cast<int64_t>(std::ceil(len / dt));
+    if (n_sub < 1) n_sub = 1;
+    const double sub = len / static_cast<double>(n_sub);
+    for (int64_t j = 1; j <= n_sub; ++j) pts->push_back(s0 + static_cast<double>(j) * sub);
+  }
+  *n_steps = static_cast<int64_t>(pts->size()) - 1;
+}
+
+void estimate_grid_div(double spot, double strike, double maturity, double sigma,
+                       const Accuracy& acc, const std::vector<double>& taus, double max_dk,
+                       GridSpec* spec, int64_t* n_time, std::vector<double>* tp,
+                       std::vector<double>* scratch) {
+  // estimate_pde_grid (src/option/grid_spec_types.cpp:37-118) with the
+  // dividend widening of the lower bound and the mandatory time points.
+  const double sst = sigma * std::sqrt(maturity);
+  const double x0 = std::log(spot / strike);
+  double lo = x0 - acc.n_sigma * sst;
+  const double hi = x0 + acc.n_sigma * sst;
+  const double dx_target = sigma * std::sqrt(acc.tol);
+  int64_t nx = static_cast<int64_t>(std::ceil((hi - lo) / dx_target));
+  if (nx < acc.min_points) nx = acc.min_points;
+  if (nx > acc.max_points) nx = acc.max_points;
+  if (nx % 2 == 0) ++nx;
+  if (max_dk > 0.0 && std::exp(lo) > max_dk) {
+    lo = std::log(std::exp(lo) - max_dk);
+  } else if (max_dk > 0.0) {
+    lo -= 1.0;
+  }
+
+  GridSpec s;
+  s.n = nx;
+  s.x_min = lo;
+  s.x_max = hi;
+  s.n_clusters = 1;
+  s.c_center[0] = x0;
+  s.c_alpha[0] = acc.alpha;
+  s.c_weight[0] = 0.5;
+  if (0.0 >= lo && 0.0 <= hi) {
+    s.c_center[1] = 0.0;
+    s.c_alpha[1] = acc.alpha;
+    s.c_weight[1] = 1.0;
+    s.n_clusters = 2;
+  }
+  bool ok = nx >= 2 && lo < hi;
+  for (int k = 0; k < s.n_clusters && ok; ++k)
+    ok = s.c_alpha[k] > 0 && s.c_weight[k] > 0 && s.c_center[k] >= lo && s.c_center[k] <= hi;
+  if (ok) {
+    s.type = GridSpec::MultiSinh;
+    merge_clusters(&s);
+  } else {
+    s = sinh_spec(lo, hi, nx, acc.alpha);
+  }
+  *spec = s;
+
+  scratch->resize(static_cast<size_t>(nx));
+  double* p = scratch->data();
+  generate_grid(s, p);
+  double dx_min = p[1] - p[0];
+  for (int64_t i = 2; i < nx; ++i) {
+    const double d = p[i] - p[i - 1];
+    if (d < dx_min) dx_min = d;
+  }
+  const double dt = acc.c_t * dx_min;
+  int64_t nt = static_cast<int64_t>(std::ceil(maturity / dt));
+  if (nt > acc.max_steps) nt = acc.max_steps;
+  const double cap = maturity / static_cast<double>(acc.max_steps);
+  const double dt_capped = (dt < cap) ? cap : dt;
+  tp->clear();
+  if (taus.empty()) {
+    *n_time = nt;  // TimeDomain::from_n_steps
+    return;
+  }
+  time_points(0.0, maturity, dt_capped, taus, tp, n_time);
 }
 
 void estimate_grid(double spot, double strike, double maturity, double sigma,

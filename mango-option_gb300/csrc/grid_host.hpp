@@ -55,6 +55,23 @@ void estimate_grid(double spot, double strike, double maturity, double sigma,
                    const Accuracy& acc, GridSpec* spec, int64_t* n_time, double* scratch,
                    int64_t cap);
 
+// TimeDomain::with_mandatory_points(t0, t1, dt, mandatory): the explicit
+// points (n_steps + 1 of them) in *pts, or *pts empty when no mandatory
+// point falls inside (t0, t1), the domain then being from_n_steps with
+// *n_steps = ceil((t1 - t0) / dt).
+void time_points(double t0, double t1, double dt, std::vector<double> mandatory,
+                 std::vector<double>* pts, int64_t* n_steps);
+
+// estimate_pde_grid for an option with discrete dividends: taus are the
+// times to expiry of its dividends inside (0, T) (any amount), max_dk the
+// largest amount / strike among them.  The lower bound is widened for the
+// dividend shift; the time domain is from_n_steps when taus is empty (tp
+// cleared), else with_mandatory_points at the capped step (points in *tp).
+void estimate_grid_div(double spot, double strike, double maturity, double sigma,
+                       const Accuracy& acc, const std::vector<double>& taus, double max_dk,
+                       GridSpec* spec, int64_t* n_time, std::vector<double>* tp,
+                       std::vector<double>* scratch);
+
 // GridSpec::sinh_spaced / uniform factories (no validation; callers check).
 GridSpec sinh_spec(double x_min, double x_max, int64_t n, double alpha);
 GridSpec uniform_spec(double x_min, double x_max, int64_t n);

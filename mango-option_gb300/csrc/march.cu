@@ -34,22 +34,6 @@ namespace mgpu {
 
 namespace {
 
-// Rows of one lane inside a tile block ([row][array][lane]).
-struct TileView {
-  double* B;  // tile block + lane
-  int NX;
-  __device__ __forceinline__ double* rp(int i) const {
-    return B + static_cast<size_t>(i) * kRowStride;
-  }
-  __device__ __forceinline__ double& at(int a, int i) const { return rp(i)[a * kTile]; }
-};
-
-// [row][lane] arrays (grids, flags).
-#define ROW(p, i) (p)[static_cast<size_t>(i) * kTile]
-
-// std::max(a, b) as the reference spells it: (a < b) ? b : a.
-__device__ __forceinline__ double dmax_ref(double a, double b) { return (a < b) ? b : a; }
-
 // std::max(v, psi) for psi >= +0 (a payoff), with integer compares instead of
 // an FP64 instruction: non-negative doubles order like their bit patterns and
 // any negative v (sign bit set) loses.  Differs from the reference only for
@@ -79,7 +63,7 @@ __global__ void prep_kernel(const TileDev* __restrict__ tiles, int ntiles,
   const TileDev td = tiles[t];
   if (lane >= td.count) return;
   const int k = td.first + lane;
-  if (mc.active && !mc.active[k]) return;
+  if ((mc.active && !mc.active[k]) || k >= mc.tv_first) return;
   const OptDev o = opts[k];
   const int n = o.n;
   const TileView V{pool + td.off + lane, td.nx};
@@ -457,7 +441,7 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
     if (t >= ntiles) break;
     const TileDev td = tiles[t];
     const int k = td.first + lane;
-    const bool active = lane < td.count && (!mc.active || mc.active[k]);
+    const bool active = lane < td.count && (!mc.active || mc.active[k]) && k < mc.tv_first;
     if (!__any_sync(0xffffffffu, active)) continue;
     OptDev o{};
     int32_t md = 0;
@@ -637,20 +621,6 @@ __device__ void stencil_at(const double* __restrict__ X, const TileView& V, int 
   const double wl = dr / (dl + dr), wr = dl / (dl + dr);
   *d2 = ((ur - uc) * ri - (uc - ul) * li) * ci;
   *d1 = wl * (uc - ul) * li + wr * (ur - uc) * ri;
-}
-
-// CubicSpline::find_interval (cubic_spline_solver.hpp:348-368).
-__device__ int find_interval(const double* __restrict__ X, int n, double xe) {
-  if (xe <= ROW(X, 0)) return 0;
-  if (xe >= ROW(X, n - 1)) return n - 2;
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    const int mid = lo + (hi - lo) / 2;
-    if (ROW(X, mid) < xe) lo = mid + 1; else hi = mid;
-  }
-  int idx = lo;
-  if (idx > 0 && (idx == n || ROW(X, idx) > xe)) --idx;
-  return idx < n - 2 ? idx : n - 2;
 }
 
 }  // namespace

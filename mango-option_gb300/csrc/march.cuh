@@ -80,7 +80,56 @@ struct MarchConst {
   const int32_t* snap_count;
   const int64_t* snap_off;
   double* snap_out;
+  // Sorted index of the first option on the time-varying march
+  // (march_tv.cu); options from here on are skipped by prep and march.
+  int32_t tv_first = 0x7fffffff;
 };
+
+// Per-option data of the time-varying march, indexed by sorted index minus
+// MarchConst::tv_first.  Pairs are stored as two consecutive doubles.
+struct TvDev {
+  double T;           // maturity: calendar time s = max(0, T - tau)
+  double r;           // constant rate when n_curve == 0
+  int32_t tp_off;     // first explicit time point in the point array, -1: t_i = i dt
+  int32_t curve_off;  // first (tenor, log discount) pair, sorted by tenor
+  int32_t n_curve;    // 0: constant rate r
+  int32_t ev_off;     // first (tau, amount / strike) dividend event, sorted by tau
+  int32_t n_ev;
+  int32_t pad;
+};
+
+#ifdef __CUDACC__
+// Rows of one lane inside a tile block ([row][array][lane]).
+struct TileView {
+  double* B;  // tile block + lane
+  int NX;
+  __device__ __forceinline__ double* rp(int i) const {
+    return B + static_cast<size_t>(i) * kRowStride;
+  }
+  __device__ __forceinline__ double& at(int a, int i) const { return rp(i)[a * kTile]; }
+};
+
+// [row][lane] arrays (grids, flags).
+#define ROW(p, i) (p)[static_cast<size_t>(i) * kTile]
+
+// std::max(a, b) as the reference spells it: (a < b) ? b : a.
+__device__ __forceinline__ double dmax_ref(double a, double b) { return (a < b) ? b : a; }
+
+// CubicSpline::find_interval (cubic_spline_solver.hpp:348-368) on a
+// [row][lane] grid.
+__device__ __forceinline__ int find_interval(const double* __restrict__ X, int n, double xe) {
+  if (xe <= ROW(X, 0)) return 0;
+  if (xe >= ROW(X, n - 1)) return n - 2;
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = lo + (hi - lo) / 2;
+    if (ROW(X, mid) < xe) lo = mid + 1; else hi = mid;
+  }
+  int idx = lo;
+  if (idx > 0 && (idx == n || ROW(X, idx) > xe)) --idx;
+  return idx < n - 2 ? idx : n - 2;
+}
+#endif
 
 // Status codes written per option (MangoStatus values).
 constexpr int32_t kStatusOk = 0;

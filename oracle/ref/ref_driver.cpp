@@ -10,6 +10,7 @@
 // (src/option/grid_spec_types.cpp:37-118), and the time axis from
 // PDEGridConfig{spec, nt} (src/option/grid_spec_types.hpp:55-59).
 #include "mango/option/american_option.hpp"
+#include "mango/option/yield_curve.hpp"
 #include "mango/option/american_option_batch.hpp"
 #include "mango/option/iv_solver.hpp"
 #include "mango/option/grid_spec_types.hpp"
@@ -485,6 +486,80 @@ int32_t ref_batch_shared(int64_t n, const double* S, const double* K, const doub
     out4[4 * i + 3] = ri->theta();
     out_dims[2 * i + 0] = static_cast<int64_t>(ri->grid()->n_space());
     out_dims[2 * i + 1] = static_cast<int64_t>(ri->grid()->time().n_steps());
+  }
+  return 0;
+}
+
+
+// Options with a yield curve and/or discrete dividends through the
+// reference's AmericanOptionSolver.  Per option i: curve points
+// [curve_off[i], curve_off[i] + curve_n[i]) (none: constant rate r[i]),
+// dividends [div_off[i], div_off[i] + div_n[i]).  kind 0 = the solver's own
+// grid (AmericanOptionSolver::create(p), as mango_price_american);
+// 1 = estimate_pde_grid with min == max == nx[i], then PDEGridConfig{spec,
+// nt[i], dividend times} (nt[i] == 0: the estimate's own time domain);
+// 2 / 3 = PDEGridConfig{sinh_spaced / uniform, nt[i], dividend times}.  The
+// dividend times are the taus in (0, T), as solve_regular_batch attaches
+// them.
+int32_t ref_price_tv(int64_t n, const double* S, const double* K, const double* T,
+                     const double* sigma, const double* r, const double* q, const int32_t* is_put,
+                     const int64_t* curve_off, const int64_t* curve_n, const double* curve_t,
+                     const double* curve_ld, const int64_t* div_off, const int64_t* div_n,
+                     const double* div_t, const double* div_amt, const int32_t* kind,
+                     const int64_t* nx, const int64_t* nt, const double* x_min, const double* x_max,
+                     const double* alpha, int32_t rannacher, int32_t n_threads, double* out4,
+                     int64_t* out_dims, int32_t* status) {
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t i = 0; i < n; ++i) {
+    auto p = make_params(S[i], K[i], T[i], sigma[i], r[i], q[i], is_put[i]);
+    if (curve_n[i] > 0) {
+      std::vector<TenorPoint> pts;
+      for (int64_t j = 0; j < curve_n[i]; ++j)
+        pts.push_back(TenorPoint{curve_t[curve_off[i] + j], curve_ld[curve_off[i] + j]});
+      auto c = YieldCurve::from_points(std::move(pts));
+      if (!c) { status[i] = 1; continue; }
+      p.rate = *c;
+    }
+    std::vector<double> taus;
+    for (int64_t j = 0; j < div_n[i]; ++j) {
+      p.discrete_dividends.push_back(Dividend{div_t[div_off[i] + j], div_amt[div_off[i] + j]});
+      const double tau = p.maturity - div_t[div_off[i] + j];
+      if (tau > 0.0 && tau < p.maturity) taus.push_back(tau);
+    }
+    std::optional<PDEGridSpec> grid;
+    if (kind[i] == 1) {
+      GridAccuracyParams acc;
+      acc.min_spatial_points = static_cast<size_t>(nx[i]);
+      acc.max_spatial_points = static_cast<size_t>(nx[i]);
+      if (nt[i] == 0) {
+        grid = PDEGridSpec{acc};
+      } else {
+        auto [spec, td] = estimate_pde_grid(p, acc);
+        (void)td;
+        grid = PDEGridSpec{PDEGridConfig{spec, static_cast<size_t>(nt[i]), taus}};
+      }
+    } else if (kind[i] == 2 || kind[i] == 3) {
+      auto spec = kind[i] == 3 ? GridSpec<double>::uniform(x_min[i], x_max[i], static_cast<size_t>(nx[i]))
+                               : GridSpec<double>::sinh_spaced(x_min[i], x_max[i],
+                                                               static_cast<size_t>(nx[i]), alpha[i]);
+      if (!spec) { status[i] = 1; continue; }
+      grid = PDEGridSpec{PDEGridConfig{*spec, static_cast<size_t>(nt[i]), taus}};
+    }
+    auto solver = AmericanOptionSolver::create(p, grid);
+    if (!solver) { status[i] = 1; continue; }
+    TRBDF2Config cfg;
+    cfg.rannacher_startup = rannacher != 0;
+    solver->set_trbdf2_config(cfg);
+    auto res = solver->solve();
+    if (!res) { status[i] = 5; continue; }
+    status[i] = 0;
+    out4[4 * i + 0] = res->value();
+    out4[4 * i + 1] = res->delta();
+    out4[4 * i + 2] = res->gamma();
+    out4[4 * i + 3] = res->theta();
+    out_dims[2 * i + 0] = static_cast<int64_t>(res->grid()->n_space());
+    out_dims[2 * i + 1] = static_cast<int64_t>(res->grid()->time().n_steps());
   }
   return 0;
 }

@@ -43,6 +43,7 @@ every output value):
 from __future__ import annotations
 
 import ctypes
+import json
 import pathlib
 import subprocess
 import sys
@@ -243,6 +244,7 @@ def main():
     golden_surface(lib)
     golden_interp_iv(lib)
     golden_shared(lib)
+    golden_tv(lib)
 
 
 def table_axes(nm, ntau, ns, nr):
@@ -442,6 +444,124 @@ def golden_shared(lib):
         kw[f"{name}_dims"] = dims
         kw[f"{name}_grid"] = np.array(grid, dtype=np.float64)
     save("shared.npz", **kw)
+
+
+def tv_batch(lib, rows, rannacher=1):
+    """Price rows (dicts) through ref_price_tv."""
+    n = len(rows)
+    col = lambda k, d=0.0: np.ascontiguousarray([r.get(k, d) for r in rows], dtype=np.float64)
+    icol = lambda k, d=0: np.ascontiguousarray([r.get(k, d) for r in rows], dtype=np.int64)
+    curves = [np.asarray(r.get("curve") or np.zeros((0, 2)), np.float64).reshape(-1, 2) for r in rows]
+    divs = [np.asarray(r.get("divs") or np.zeros((0, 2)), np.float64).reshape(-1, 2) for r in rows]
+    def flat(blocks):
+        cnt = np.array([b.shape[0] for b in blocks], np.int64)
+        off = np.concatenate([[0], np.cumsum(cnt)[:-1]]).astype(np.int64)
+        allp = np.concatenate(blocks + [np.zeros((1, 2))])
+        return off, cnt, np.ascontiguousarray(allp[:, 0]), np.ascontiguousarray(allp[:, 1])
+    co, cn, ct, cl = flat(curves)
+    do, dn, dt, da = flat(divs)
+    put = np.ascontiguousarray([r["put"] for r in rows], dtype=np.int32)
+    kind = np.ascontiguousarray([r.get("kind", 0) for r in rows], dtype=np.int32)
+    out = np.full(4 * n, np.nan)
+    dims = np.zeros(2 * n, np.int64)
+    st = np.zeros(n, np.int32)
+    args = [col("S"), col("K"), col("T"), col("sigma"), col("r"), col("q")]
+    rest = [icol("nx"), icol("nt"), col("x_min"), col("x_max"), col("alpha")]
+    rc = lib.ref_price_tv(ctypes.c_int64(n), *(P(a) for a in args), P(put), P(co), P(cn), P(ct), P(cl), P(do),
+                          P(dn), P(dt), P(da), P(kind), *(P(a) for a in rest), ctypes.c_int32(rannacher),
+                          ctypes.c_int32(8), P(out), P(dims), P(st))
+    assert rc == 0
+    return out.reshape(n, 4), dims.reshape(n, 2), st
+
+
+def zero_curve(tenors, zeros):
+    return [(0.0, 0.0)] + [(t, -z * t) for t, z in zip(tenors, zeros)]
+
+
+TV_CURVES = {
+    "up": zero_curve([0.25, 0.5, 1.0, 2.0, 3.0, 5.0], [0.02, 0.025, 0.03, 0.035, 0.038, 0.04]),
+    "down": zero_curve([0.25, 0.5, 1.0, 2.0, 5.0], [0.06, 0.055, 0.05, 0.04, 0.03]),
+    "short": [(0.0, 0.0), (1.0, -0.05)],
+    "negative": zero_curve([0.5, 1.0, 2.0], [-0.005, -0.002, 0.004]),
+    "single": [(0.0, 0.0)],
+}
+
+
+def tv_rows(seed, n, kinds):
+    rng = np.random.default_rng(seed)
+    rows = []
+    curve_names = [None, "up", "down", "short", "negative"]
+    for i in range(n):
+        T = float(rng.uniform(0.3, 2.0))
+        r = {"S": 100.0, "K": float(rng.uniform(80, 120)), "T": T, "sigma": float(rng.uniform(0.15, 0.45)),
+             "r": float(rng.uniform(0.0, 0.06)), "q": float(rng.choice([0.0, 0.01, 0.025])),
+             "put": int(i % 3 != 2)}
+        c = curve_names[i % 5]
+        if c:
+            r["curve"] = TV_CURVES[c]
+        d = (i // 5) % 6
+        if d == 1:
+            r["divs"] = [(0.25 * T, 1.0), (0.75 * T, 1.0)]
+        elif d == 2:
+            r["divs"] = [(0.5 * T, 3.0)]
+        elif d == 3:
+            r["divs"] = [(t, 0.5) for t in np.arange(0.25, T, 0.25)]
+        elif d == 4:
+            r["divs"] = [(0.3 * T, 0.0), (0.6 * T, 1.5)]
+        elif d == 5:
+            r["divs"] = [(0.4 * T, 1.0), (0.4 * T, 1.5)]
+        if "curve" not in r and "divs" not in r:
+            r["divs"] = [(0.5 * T, 2.0)]
+        k = kinds[i % len(kinds)]
+        r["kind"] = k
+        if k == 1:
+            r["nx"], r["nt"] = (101, 200) if i % 2 else (121, 0)
+        elif k == 2:
+            r.update(nx=121, nt=300, x_min=-3.0, x_max=3.0, alpha=2.0)
+        elif k == 3:
+            r.update(nx=151, nt=250, x_min=-3.0, x_max=3.0)
+        rows.append(r)
+    return rows
+
+
+def golden_tv(lib):
+    """Yield curves and discrete dividends through AmericanOptionSolver:
+    the solver's own grid, pinned-size, sinh and uniform grids, Rannacher on
+    and off, and edge schedules."""
+    cases = {
+        "auto": (tv_rows(51, 96, [0]), 1),
+        "explicit": (tv_rows(52, 96, [1, 2, 3]), 1),
+        "no_rannacher": (tv_rows(53, 32, [0, 2]), 0),
+    }
+    edge = [
+        # dividends at t = 0 and t = T: no event, no mandatory point
+        {"S": 100.0, "K": 100.0, "T": 1.0, "sigma": 0.25, "r": 0.04, "q": 0.0, "put": 1,
+         "divs": [(0.0, 2.0), (1.0, 2.0)], "curve": TV_CURVES["up"]},
+        # a dividend larger than e^{x_min} K: the conservative grid extension
+        {"S": 100.0, "K": 100.0, "T": 1.0, "sigma": 0.2, "r": 0.03, "q": 0.0, "put": 1, "divs": [(0.5, 60.0)]},
+        {"S": 100.0, "K": 100.0, "T": 1.0, "sigma": 0.2, "r": 0.03, "q": 0.0, "put": 0, "divs": [(0.5, 60.0)]},
+        # single-point curve: rate 0 everywhere
+        {"S": 100.0, "K": 110.0, "T": 0.7, "sigma": 0.3, "r": 0.05, "q": 0.0, "put": 1, "curve": TV_CURVES["single"]},
+        # deep ITM call before a large dividend (early exercise), and a deep ITM put
+        {"S": 150.0, "K": 100.0, "T": 0.5, "sigma": 0.2, "r": 0.02, "q": 0.0, "put": 0, "divs": [(0.25, 8.0)]},
+        {"S": 60.0, "K": 100.0, "T": 1.5, "sigma": 0.25, "r": 0.05, "q": 0.0, "put": 1, "divs": [(0.5, 1.0)],
+         "curve": TV_CURVES["down"]},
+        # curve beyond its last tenor (flat forward extrapolation)
+        {"S": 100.0, "K": 95.0, "T": 2.0, "sigma": 0.2, "r": 0.0, "q": 0.01, "put": 0, "curve": TV_CURVES["short"]},
+        # a dividend on the first step and one on the last
+        {"S": 100.0, "K": 100.0, "T": 1.0, "sigma": 0.2, "r": 0.03, "q": 0.0, "put": 1,
+         "divs": [(0.999, 1.0), (0.001, 1.0)]},
+    ]
+    cases["edge"] = (edge, 1)
+    kw = {}
+    for name, (rows, rann) in cases.items():
+        out, dims, st = tv_batch(lib, rows, rann)
+        assert (st == 0).all(), (name, st)
+        kw[f"{name}_rows"] = np.array([json.dumps(r) for r in rows])
+        kw[f"{name}_out"] = out
+        kw[f"{name}_dims"] = dims
+        kw[f"{name}_rannacher"] = np.int32(rann)
+    save("tv.npz", **kw)
 
 
 if __name__ == "__main__":

@@ -45,20 +45,49 @@ constexpr double kMaxWidth = 5.8;
 constexpr double kMaxDx = 0.05;
 constexpr double kMinMarginAbs = 0.35;
 
-// estimate_batch_pde_grid for options without discrete dividends.
+// estimate_batch_pde_grid: the union of the options' estimated x ranges
+// (each widened for its dividends), their largest n_space, and the batch
+// time domain over the longest maturity: from_n_steps at the largest step
+// count, or, when any option has a dividend inside (0, T_max),
+// with_mandatory_points at that step (capped) through the union of the
+// dividend times.  *nt is that domain's step count.
 void estimate_batch_grid(const std::vector<const MangoPricingParams*>& ps, const Accuracy& acc,
                          GridSpec* spec, int64_t* nt) {
   double gmin = 1e300, gmax = -1e300;
   int64_t gnx = 0, gnt = 0;
-  std::vector<double> scratch;
+  std::vector<double> scratch, taus, tp;
   for (const MangoPricingParams* p : ps) {
     GridSpec s;
     int64_t n_t = 0;
-    estimate_grid(p->spot, p->strike, p->maturity, p->volatility, acc, &s, &n_t, &scratch);
+    taus.clear();
+    double max_dk = 0.0;
+    for (uint64_t j = 0; j < p->n_dividends; ++j) {
+      const double tau = p->maturity - p->dividends[j].calendar_time;
+      if (tau > 0.0 && tau < p->maturity) {
+        taus.push_back(tau);
+        max_dk = std::max(max_dk, p->dividends[j].amount / p->strike);
+      }
+    }
+    estimate_grid_div(p->spot, p->strike, p->maturity, p->volatility, acc, taus, max_dk, &s, &n_t,
+                      &tp, &scratch);
     gmin = std::min(gmin, s.x_min);
     gmax = std::max(gmax, s.x_max);
     gnx = std::max<int64_t>(gnx, s.n);
     gnt = std::max<int64_t>(gnt, n_t);
+  }
+  double t_max = 0.0;
+  for (const MangoPricingParams* p : ps) t_max = std::max(t_max, p->maturity);
+  std::vector<double> all_tau;
+  for (const MangoPricingParams* p : ps)
+    for (uint64_t j = 0; j < p->n_dividends; ++j) {
+      const double tau = p->maturity - p->dividends[j].calendar_time;
+      if (tau > 0.0 && tau < t_max) all_tau.push_back(tau);
+    }
+  if (!all_tau.empty()) {
+    const double global_dt = t_max / static_cast<double>(gnt);
+    const double cap = t_max / static_cast<double>(acc.max_steps);
+    const double dt_capped = (global_dt < cap) ? cap : global_dt;
+    time_points(0.0, t_max, dt_capped, all_tau, &tp, &gnt);
   }
   GridSpec s;
   // multi_sinh_spaced with one cluster at x = 0 (grid.hpp:110-160 checks),
@@ -78,6 +107,27 @@ void estimate_batch_grid(const std::vector<const MangoPricingParams*>& ps, const
   }
   *spec = s;
   *nt = gnt;
+}
+
+// Rate comparison of group_by_pde_parameters: constants within 1e-10,
+// yield curves equal point by point within 1e-12 (YieldCurve::operator==,
+// on the tenor-sorted points).
+bool same_rate(const MangoPricingParams& a, const MangoPricingParams& b) {
+  if ((a.n_tenor_points == 0) != (b.n_tenor_points == 0)) return false;
+  if (a.n_tenor_points == 0) return std::fabs(a.rate_const - b.rate_const) < 1e-10;
+  if (a.n_tenor_points != b.n_tenor_points) return false;
+  auto sorted = [](const MangoPricingParams& p) {
+    std::vector<MangoTenorPoint> v(p.tenor_points, p.tenor_points + p.n_tenor_points);
+    std::sort(v.begin(), v.end(),
+              [](const MangoTenorPoint& x, const MangoTenorPoint& y) { return x.tenor < y.tenor; });
+    return v;
+  };
+  const auto va = sorted(a), vb = sorted(b);
+  for (size_t i = 0; i < va.size(); ++i)
+    if (std::fabs(va[i].tenor - vb[i].tenor) > 1e-12 ||
+        std::fabs(va[i].log_discount - vb[i].log_discount) > 1e-12)
+      return false;
+  return true;
 }
 
 bool eligible(const MangoPricingParams* params, int64_t n, const Accuracy& acc) {
@@ -151,7 +201,7 @@ extern "C" MangoStatus mango_gpu_price_american_batch_shared(
     std::vector<std::string> vmsg(static_cast<size_t>(nn));
     std::vector<char> valid(static_cast<size_t>(nn), 0);
     for (int64_t i = 0; i < nn; ++i) {
-      vmsg[i] = validate(params[i]);
+      vmsg[i] = validate(params[i], true);
       valid[i] = vmsg[i].empty();
     }
     for (int64_t i = 0; i < nn; ++i) {
@@ -165,8 +215,9 @@ extern "C" MangoStatus mango_gpu_price_american_batch_shared(
     if (chain) {
       // group_by_pde_parameters over the options (first match, 1e-10).
       struct Group {
-        double sigma, r, q, T;
+        double sigma, q, T;
         int32_t type;
+        const MangoPricingParams* rep;  // first option: its rate or curve
       };
       std::vector<Group> groups;
       std::vector<int32_t> gof(static_cast<size_t>(nn), -1);
@@ -176,7 +227,7 @@ extern "C" MangoStatus mango_gpu_price_american_batch_shared(
         int32_t found = -1;
         for (size_t g = 0; g < groups.size(); ++g) {
           const Group& G = groups[g];
-          if (std::fabs(G.sigma - p.volatility) < 1e-10 && std::fabs(G.r - p.rate_const) < 1e-10 &&
+          if (std::fabs(G.sigma - p.volatility) < 1e-10 && same_rate(*G.rep, p) &&
               std::fabs(G.q - p.dividend_yield) < 1e-10 && std::fabs(G.T - p.maturity) < 1e-10 &&
               G.type == p.option_type) {
             found = static_cast<int32_t>(g);
@@ -185,7 +236,7 @@ extern "C" MangoStatus mango_gpu_price_american_batch_shared(
         }
         if (found < 0) {
           found = static_cast<int32_t>(groups.size());
-          groups.push_back({p.volatility, p.rate_const, p.dividend_yield, p.maturity, p.option_type});
+          groups.push_back({p.volatility, p.dividend_yield, p.maturity, p.option_type, &p});
         }
         gof[i] = found;
       }
@@ -199,7 +250,9 @@ extern "C" MangoStatus mango_gpu_price_american_batch_shared(
         p.strike = 1.0;
         p.maturity = groups[g].T;
         p.volatility = groups[g].sigma;
-        p.rate_const = groups[g].r;
+        p.rate_const = groups[g].rep->rate_const;
+        p.tenor_points = groups[g].rep->tenor_points;
+        p.n_tenor_points = groups[g].rep->n_tenor_points;
         p.dividend_yield = groups[g].q;
         p.option_type = groups[g].type;
         Resolved& r = res[g];
@@ -211,6 +264,7 @@ extern "C" MangoStatus mango_gpu_price_american_batch_shared(
           std::vector<const MangoPricingParams*> one{&gp[g]};
           estimate_batch_grid(one, acc, &r.spec, &r.nt);
         }
+        r.tv = time_varying(p);
       }
       b = create_batch_resolved(ctx, gp.data(), std::move(res),
                                 std::vector<std::string>(static_cast<size_t>(ng)), trbdf2);
@@ -272,11 +326,17 @@ extern "C" MangoStatus mango_gpu_price_american_batch_shared(
       GridSpec spec;
       int64_t nt = 0;
       if (custom) {
+        // resolve_grid for the first option; the shared step count is that
+        // time domain's (an explicit n_time, or the estimate's own steps).
         Resolved r;
         const std::string m = resolve_custom(params[0], &r);
         if (!m.empty()) throw std::invalid_argument(m);
         spec = r.spec;
-        nt = r.nt;
+        const int32_t k = custom_grid->kind;
+        const bool explicit_nt = k == MANGO_GPU_GRID_SINH || k == MANGO_GPU_GRID_UNIFORM ||
+                                 ((k == MANGO_GPU_GRID_FIXED_N || k == MANGO_GPU_GRID_FIXED_N_AT_VOL) &&
+                                  custom_grid->n_time > 0);
+        nt = explicit_nt ? custom_grid->n_time : r.nt;
       } else {
         std::vector<const MangoPricingParams*> ps;
         for (int64_t i = 0; i < nn; ++i)
@@ -284,11 +344,25 @@ extern "C" MangoStatus mango_gpu_price_american_batch_shared(
         if (!ps.empty()) estimate_batch_grid(ps, acc, &spec, &nt);
       }
       std::vector<Resolved> res(static_cast<size_t>(nn));
+      std::vector<double> taus;
       for (int64_t i = 0; i < nn; ++i) {
         res[i].orig = static_cast<int32_t>(i);
         res[i].spec = spec;
         res[i].nt = nt;
-        if (!valid[i]) res[i].status = MANGO_ERR_VALIDATION;
+        if (!valid[i]) {
+          res[i].status = MANGO_ERR_VALIDATION;
+          continue;
+        }
+        // PDEGridConfig{shared spec, shared n_steps, this option's dividend
+        // times} (american_option_batch.cpp:447-470).
+        const MangoPricingParams& p = params[i];
+        res[i].tv = time_varying(p);
+        taus.clear();
+        for (uint64_t j = 0; j < p.n_dividends; ++j) {
+          const double tau = p.maturity - p.dividends[j].calendar_time;
+          if (tau > 0.0 && tau < p.maturity) taus.push_back(tau);
+        }
+        explicit_time_domain(p.maturity, nt, taus, &res[i]);
       }
       b = create_batch_resolved(ctx, params, std::move(res), vmsg, trbdf2);
       run_batch(b);

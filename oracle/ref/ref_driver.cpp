@@ -564,4 +564,60 @@ int32_t ref_price_tv(int64_t n, const double* S, const double* K, const double* 
   return 0;
 }
 
+
+// ref_batch_shared for options with yield curves and dividends (the
+// schedules as in ref_price_tv).
+int32_t ref_batch_shared_tv(int64_t n, const double* S, const double* K, const double* T,
+                            const double* sigma, const double* r, const double* q,
+                            const int32_t* is_put, const int64_t* curve_off, const int64_t* curve_n,
+                            const double* curve_t, const double* curve_ld, const int64_t* div_off,
+                            const int64_t* div_n, const double* div_t, const double* div_amt,
+                            int32_t use_normalized, int32_t kind, double x_min, double x_max,
+                            int64_t nx, double alpha, int64_t nt, int32_t n_threads, double* out4,
+                            int64_t* out_dims, int32_t* status) {
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+  std::vector<PricingParams> ps;
+  for (int64_t i = 0; i < n; ++i) {
+    auto p = make_params(S[i], K[i], T[i], sigma[i], r[i], q[i], is_put[i]);
+    if (curve_n[i] > 0) {
+      std::vector<TenorPoint> pts;
+      for (int64_t j = 0; j < curve_n[i]; ++j)
+        pts.push_back(TenorPoint{curve_t[curve_off[i] + j], curve_ld[curve_off[i] + j]});
+      auto c = YieldCurve::from_points(std::move(pts));
+      if (!c) return 1;
+      p.rate = *c;
+    }
+    for (int64_t j = 0; j < div_n[i]; ++j)
+      p.discrete_dividends.push_back(Dividend{div_t[div_off[i] + j], div_amt[div_off[i] + j]});
+    ps.push_back(std::move(p));
+  }
+  std::optional<PDEGridSpec> custom;
+  if (kind == 2 || kind == 3) {
+    auto spec = kind == 3 ? GridSpec<double>::uniform(x_min, x_max, static_cast<size_t>(nx))
+                          : GridSpec<double>::sinh_spaced(x_min, x_max, static_cast<size_t>(nx), alpha);
+    if (!spec) return 1;
+    custom = PDEGridSpec{PDEGridConfig{*spec, static_cast<size_t>(nt), {}}};
+  } else if (kind == 1) {
+    GridAccuracyParams acc;
+    acc.min_spatial_points = static_cast<size_t>(nx);
+    acc.max_spatial_points = static_cast<size_t>(nx);
+    custom = PDEGridSpec{acc};
+  }
+  BatchAmericanOptionSolver solver;
+  solver.set_use_normalized(use_normalized != 0);
+  auto res = solver.solve_batch(ps, true, nullptr, custom);
+  for (int64_t i = 0; i < n; ++i) {
+    const auto& ri = res.results[static_cast<size_t>(i)];
+    if (!ri) { status[i] = 5; continue; }
+    status[i] = 0;
+    out4[4 * i + 0] = ri->value();
+    out4[4 * i + 1] = ri->delta();
+    out4[4 * i + 2] = ri->gamma();
+    out4[4 * i + 3] = ri->theta();
+    out_dims[2 * i + 0] = static_cast<int64_t>(ri->grid()->n_space());
+    out_dims[2 * i + 1] = static_cast<int64_t>(ri->grid()->time().n_steps());
+  }
+  return 0;
+}
+
 }  // extern "C"

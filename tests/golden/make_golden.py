@@ -245,6 +245,7 @@ def main():
     golden_interp_iv(lib)
     golden_shared(lib)
     golden_tv(lib)
+    golden_shared_tv(lib)
 
 
 def table_axes(nm, ntau, ns, nr):
@@ -562,6 +563,73 @@ def golden_tv(lib):
         kw[f"{name}_dims"] = dims
         kw[f"{name}_rannacher"] = np.int32(rann)
     save("tv.npz", **kw)
+
+
+def shared_tv_batch(lib, rows, use_normalized, grid=(0, 0.0, 0.0, 0, 0.0, 0)):
+    n = len(rows)
+    col = lambda k, d=0.0: np.ascontiguousarray([r.get(k, d) for r in rows], dtype=np.float64)
+    curves = [np.asarray(r.get("curve") or np.zeros((0, 2)), np.float64).reshape(-1, 2) for r in rows]
+    divs = [np.asarray(r.get("divs") or np.zeros((0, 2)), np.float64).reshape(-1, 2) for r in rows]
+    def flat(blocks):
+        cnt = np.array([b.shape[0] for b in blocks], np.int64)
+        off = np.concatenate([[0], np.cumsum(cnt)[:-1]]).astype(np.int64)
+        allp = np.concatenate(blocks + [np.zeros((1, 2))])
+        return off, cnt, np.ascontiguousarray(allp[:, 0]), np.ascontiguousarray(allp[:, 1])
+    co, cn, ct, cl = flat(curves)
+    do, dn, dt, da = flat(divs)
+    put = np.ascontiguousarray([r["put"] for r in rows], dtype=np.int32)
+    out = np.full(4 * n, np.nan)
+    dims = np.zeros(2 * n, np.int64)
+    st = np.zeros(n, np.int32)
+    kind, x_min, x_max, nx, alpha, nt = grid
+    args = [col("S"), col("K"), col("T"), col("sigma"), col("r"), col("q")]
+    rc = lib.ref_batch_shared_tv(ctypes.c_int64(n), *(P(a) for a in args), P(put), P(co), P(cn), P(ct), P(cl),
+                                 P(do), P(dn), P(dt), P(da), ctypes.c_int32(use_normalized), ctypes.c_int32(kind),
+                                 ctypes.c_double(x_min), ctypes.c_double(x_max), ctypes.c_int64(nx),
+                                 ctypes.c_double(alpha), ctypes.c_int64(nt), ctypes.c_int32(8), P(out), P(dims),
+                                 P(st))
+    assert rc == 0
+    return out.reshape(n, 4), dims.reshape(n, 2), st
+
+
+def golden_shared_tv(lib):
+    """solve_batch(use_shared_grid = true) with yield curves (normalized
+    chains grouped by curve) and discrete dividends (regular shared grid
+    with per-option mandatory times)."""
+    rng = np.random.default_rng(61)
+    chain = []
+    for ci, c in enumerate(["up", "down", "up"]):
+        for K in rng.uniform(88.0, 114.0, 8):
+            chain.append({"S": 100.0, "K": float(K), "T": [1.0, 0.5, 1.0][ci], "sigma": [0.2, 0.3, 0.2][ci],
+                          "r": 0.0, "q": 0.01, "put": 1, "curve": TV_CURVES[c]})
+    chain.append({"S": 100.0, "K": 100.0, "T": 1.0, "sigma": 0.2, "r": 0.03, "q": 0.01, "put": 1})
+    divs = []
+    for i in range(40):
+        T = float(rng.uniform(0.4, 1.5))
+        r = {"S": 100.0, "K": float(rng.uniform(85, 115)), "T": T, "sigma": float(rng.uniform(0.15, 0.4)),
+             "r": 0.03, "q": 0.0, "put": int(i % 4 != 3)}
+        if i % 3 == 0:
+            r["divs"] = [(0.5 * T, 1.5)]
+        elif i % 3 == 1:
+            r["divs"] = [(0.3 * T, 1.0), (0.7 * T, 1.0)]
+            r["curve"] = TV_CURVES["up"]
+        divs.append(r)
+    cases = {
+        "chain_curve": (chain, 1, (0, 0.0, 0.0, 0, 0.0, 0)),
+        "chain_curve_sinh": (chain, 1, (2, -2.5, 2.5, 161, 2.0, 250)),
+        "divs": (divs, 1, (0, 0.0, 0.0, 0, 0.0, 0)),
+        "divs_uniform": (divs, 1, (3, -3.0, 3.0, 181, 0.0, 300)),
+        "divs_fixed_n": (divs, 1, (1, 0.0, 0.0, 131, 0.0, 0)),
+    }
+    kw = {}
+    for name, (rows, un, grid) in cases.items():
+        out, dims, st = shared_tv_batch(lib, rows, un, grid)
+        assert (st == 0).all(), name
+        kw[f"{name}_rows"] = np.array([json.dumps(r) for r in rows])
+        kw[f"{name}_out"] = out
+        kw[f"{name}_dims"] = dims
+        kw[f"{name}_grid"] = np.array(grid, dtype=np.float64)
+    save("shared_tv.npz", **kw)
 
 
 if __name__ == "__main__":

@@ -112,3 +112,28 @@ def test_batch_solver_mirror(engine, pkg):
     # option serves every option (the regular route)
     res = solver.set_use_normalized(True).solve_batch(plist, custom_grid=pkg.PDEGridConfig(-2.5, 2.5, 181, 300, 2.0))
     assert solver.last_route == 0 and res.failed_count == 0
+
+
+# Yield curves and dividends on the shared routes (tests/golden/shared_tv.npz):
+# chains grouped by curve on the normalized route, dividend batches on the
+# regular shared grid with each option's dividend times as mandatory points.
+TV_CASES = {"chain_curve": 1, "chain_curve_sinh": 1, "divs": 0, "divs_uniform": 0, "divs_fixed_n": 0}
+
+
+@pytest.mark.parametrize("name", list(TV_CASES))
+def test_shared_grid_schedules_vs_reference(engine, pkg, name):
+    import json
+    g = golden("shared_tv.npz")
+    rows = [json.loads(str(s)) for s in g[f"{name}_rows"]]
+    p = pkg.pricing_array([r["S"] for r in rows], [r["K"] for r in rows], [r["T"] for r in rows],
+                          [r["sigma"] for r in rows], [r["r"] for r in rows], [r["q"] for r in rows],
+                          [r["put"] for r in rows])
+    keep = pkg.attach_schedules(p, [r.get("curve") for r in rows], [r.get("divs") for r in rows])
+    out, route = engine.price_shared_arrays(p, custom_grid(pkg, g[f"{name}_grid"]))
+    assert route == TV_CASES[name]
+    assert (out["status"] == 0).all()
+    dims = g[f"{name}_dims"]
+    assert (out["n_space"] == dims[:, 0]).all() and (out["n_time"] == dims[:, 1]).all()
+    dt = np.array([r["T"] for r in rows]) / dims[:, 1]
+    check(greeks(out), g[f"{name}_out"], 1e-13 * np.array([r["K"] for r in rows]) / dt)
+    del keep

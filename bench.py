@@ -260,6 +260,51 @@ def bench_greeks(pkg, eng, n=16384):
             "failed": int(np.count_nonzero(out["status"]))}
 
 
+def bench_schedules(pkg, eng, torch, stream, n, fp64_peak):
+    """Time-varying march: n puts and calls (config-0 distributions) on the
+    101 x 498 grid rule with a 7-point yield curve, then with the curve plus
+    two cash dividends per option (mandatory time points, two spline
+    shifts).  Resident batches, device time of two runs."""
+    rng = np.random.default_rng(5)
+    T = rng.uniform(0.1, 2.0, n)
+    params = pkg.pricing_array(np.full(n, 100.0), rng.uniform(80, 120, n), T, rng.uniform(0.1, 0.5, n), 0.0,
+                               rng.uniform(0.0, 0.04, n), (np.arange(n) % 2 == 0).astype(np.int32))
+    tenors = [0.25, 0.5, 1.0, 2.0, 3.0, 5.0]
+    zeros = [0.02, 0.025, 0.03, 0.035, 0.038, 0.04]
+    curve = [(0.0, 0.0)] + [(t, -z * t) for t, z in zip(tenors, zeros)]
+    grid = pkg.grid_array(1, pkg.GRID_FIXED_N, NX, NT)
+    out = {}
+    for name, divs in (("yield_curve", None), ("curve_and_dividends",
+                                               [[(0.3 * t, 1.0), (0.7 * t, 1.0)] for t in T])):
+        p = params.copy()
+        keep = pkg.attach_schedules(p, [curve] * n, divs)
+        b = eng.batch(p, grid)
+        del keep
+        b.run()
+        torch.cuda.synchronize()
+        b.timings(reset=True)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(2):
+            b.run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        res = b.results()
+        kt = b.timings()
+        algo = eng.stats()["algo_flops"]
+        out[name] = {
+            "workload": f"{n} puts/calls, 101 points, 498 steps (+ dividend points), 7-point curve"
+                        + (", 2 cash dividends each" if divs else ""),
+            "value": 2 * n / t, "unit": "options/s", "failed": int(np.count_nonzero(res["status"])),
+            "march_ms": kt["march_ms"],
+            "fp64_frac": algo / (kt["march_ms"] / 1e3) / 1e12 / fp64_peak if fp64_peak else None,
+            "mean_steps": float(np.mean(res["n_time"]))}
+        b.close()
+    return out
+
+
 TABLE_AXES = (np.linspace(np.log(0.7), np.log(1.3), 50), np.linspace(0.02, 2.0, 30),
               np.linspace(0.05, 0.8, 20), np.linspace(0.0, 0.08, 10))
 
@@ -541,6 +586,8 @@ def main():
             "march_ms": kt2["march_ms"], "fp64_frac": algo2 / (kt2["march_ms"] / 1e3) / 1e12 / fp64_peak}
         b2.close()
 
+    if not args.no_extra and rank == 0:
+        extra["schedules"] = bench_schedules(pkg, eng, torch, stream, n, fp64_peak)
     if not args.no_iv and rank == 0:
         extra["iv_brent"] = bench_iv(pkg, eng, args.iv_quotes)
     if not args.no_iv and rank == 0:

@@ -14,9 +14,16 @@
  * failed count), and no exception crosses the boundary.  Every batch call is
  * synchronous with respect to the caller's host buffers.
  *
- * Scope (the reference's hot path): constant rate and continuous dividend
- * yield.  Yield curves and discrete dividends are rejected per slot with
- * MANGO_ERR_VALIDATION and a message naming the unsupported feature.
+ * Rates and dividends: the American-pricing batch calls
+ * (mango_gpu_price_american_batch, _batch_shared, mango_gpu_batch_create)
+ * accept the reference's yield curves (tenor_points, validated as
+ * YieldCurve::from_points does) and discrete dividends (validated as
+ * validate_pricing_params does) and march those options on a kernel whose
+ * stage matrices follow r(t), the mandatory dividend times and the dividend
+ * shift.  The other entry points (implied volatility, Greeks, table sweep,
+ * the no-allocation batch) take constant rates and continuous dividend
+ * yields only and reject the rest per slot with MANGO_ERR_VALIDATION and a
+ * message naming the unsupported feature.
  */
 #ifndef MANGO_GPU_H
 #define MANGO_GPU_H

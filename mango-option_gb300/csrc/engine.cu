@@ -215,10 +215,13 @@ std::string resolve(const MangoPricingParams& p, const MangoGpuGrid& g, Resolved
       if (!(vol > 0.0) || !std::isfinite(vol)) return "grid: sizing volatility must be > 0";
       Accuracy a = def;
       a.min_points = a.max_points = g.n_space;
-      int64_t nt_auto = 0;
-      estimate_grid(p.spot, p.strike, p.maturity, vol, a, &r->spec, &nt_auto, scratch);
-      // n_time 0: the estimate's own step count (GridAccuracyParams alone)
-      r->nt = g.n_time > 0 ? g.n_time : nt_auto;
+      if (g.n_time > 0) {
+        estimate_spec(p.spot, p.strike, p.maturity, vol, a, &r->spec);
+        r->nt = g.n_time;
+      } else {
+        // n_time 0: the estimate's own step count (GridAccuracyParams alone)
+        estimate_grid(p.spot, p.strike, p.maturity, vol, a, &r->spec, &r->nt, scratch);
+      }
       break;
     }
     case MANGO_GPU_GRID_SINH:

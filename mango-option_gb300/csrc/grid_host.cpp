@@ -132,17 +132,23 @@ void generate_grid(const GridSpec& s, double* x) {
       }
       double total = 0.0;
       for (int k = 0; k < s.n_clusters; ++k) total += s.c_weight[k];
+      // The per-cluster terms do not depend on the point: computed once
+      // (same expressions, same values).
+      double cw[4], cc[4], cshc[4], ceta[4], coff[4];
+      for (int k = 0; k < s.n_clusters; ++k) {
+        const double c = s.c_alpha[k], center = s.c_center[k];
+        cw[k] = s.c_weight[k] / total;
+        cc[k] = c;
+        cshc[k] = std::sinh(c / 2.0);
+        ceta[k] = (center - lo) / range;
+        coff[k] = center - (lo + hi) / 2.0;
+      }
       for (int64_t i = 0; i < n; ++i) {
         const double eta = static_cast<double>(i) / nm1;
         double acc = 0.0;
         for (int k = 0; k < s.n_clusters; ++k) {
-          const double c = s.c_alpha[k], center = s.c_center[k];
-          const double w = s.c_weight[k] / total;
-          const double shc = std::sinh(c / 2.0);
-          const double eta_c = (center - lo) / range;
-          const double st = std::sinh(c * (eta - eta_c)) / shc;
-          const double off = center - (lo + hi) / 2.0;
-          acc += w * (lo + range * ((1.0 + st) / 2.0) + off);
+          const double st = std::sinh(cc[k] * (eta - ceta[k])) / cshc[k];
+          acc += cw[k] * (lo + range * ((1.0 + st) / 2.0) + coff[k]);
         }
         x[i] = acc;
       }
@@ -150,6 +156,44 @@ void generate_grid(const GridSpec& s, double* x) {
       return;
     }
   }
+}
+
+void estimate_spec(double spot, double strike, double maturity, double sigma,
+                   const Accuracy& acc, GridSpec* spec) {
+  // The spatial half of estimate_grid below (no trial grid, no step count).
+  const double sst = sigma * std::sqrt(maturity);
+  const double x0 = std::log(spot / strike);
+  const double lo = x0 - acc.n_sigma * sst;
+  const double hi = x0 + acc.n_sigma * sst;
+  const double dx_target = sigma * std::sqrt(acc.tol);
+  int64_t nx = static_cast<int64_t>(std::ceil((hi - lo) / dx_target));
+  if (nx < acc.min_points) nx = acc.min_points;
+  if (nx > acc.max_points) nx = acc.max_points;
+  if (nx % 2 == 0) ++nx;
+  GridSpec s;
+  s.n = nx;
+  s.x_min = lo;
+  s.x_max = hi;
+  s.n_clusters = 1;
+  s.c_center[0] = x0;
+  s.c_alpha[0] = acc.alpha;
+  s.c_weight[0] = 0.5;
+  if (0.0 >= lo && 0.0 <= hi) {
+    s.c_center[1] = 0.0;
+    s.c_alpha[1] = acc.alpha;
+    s.c_weight[1] = 1.0;
+    s.n_clusters = 2;
+  }
+  bool ok = nx >= 2 && lo < hi;
+  for (int k = 0; k < s.n_clusters && ok; ++k)
+    ok = s.c_alpha[k] > 0 && s.c_weight[k] > 0 && s.c_center[k] >= lo && s.c_center[k] <= hi;
+  if (ok) {
+    s.type = GridSpec::MultiSinh;
+    merge_clusters(&s);
+  } else {
+    s = sinh_spec(lo, hi, nx, acc.alpha);
+  }
+  *spec = s;
 }
 
 void estimate_grid(double spot, double strike, double maturity, double sigma,

@@ -49,6 +49,11 @@ void estimate_grid(double spot, double strike, double maturity, double sigma,
                    const Accuracy& acc, GridSpec* spec, int64_t* n_time,
                    std::vector<double>* scratch);
 
+// The spatial GridSpec of estimate_grid alone, for callers that give the
+// step count themselves.
+void estimate_spec(double spot, double strike, double maturity, double sigma,
+                   const Accuracy& acc, GridSpec* spec);
+
 // Same, with caller-provided scratch of `cap` doubles (no heap use); a grid
 // larger than cap is not generated and *n_time is left at 0.
 void estimate_grid(double spot, double strike, double maturity, double sigma,

@@ -216,13 +216,51 @@ __device__ void tv_setup(Lane& L) {
 
 enum StageKind { kEuler = 0, kTrap = 1, kBdf2 = 2 };
 
+// Inputs of forward-sweep row i: the grid-only band parts, psi and the
+// stage's state (u_prev at row i + 1 for kEuler / kTrap, u* and u_prev at
+// row i for kBdf2).
+struct FwdRow {
+  double d2m, d2i, d2p, qm, qi, qp, psi, s0, s1;
+};
+template <int KIND>
+__device__ __forceinline__ FwdRow fwd_load(const TileView& V, int i) {
+  const double* r = V.rp(i);
+  FwdRow o;
+  o.d2m = r[T_D2M * kTile];
+  o.d2i = r[T_D2I * kTile];
+  o.d2p = r[T_D2P * kTile];
+  o.qm = r[T_QM * kTile];
+  o.qi = r[T_QI * kTile];
+  o.qp = r[T_QP * kTile];
+  o.psi = r[A_PSI * kTile];
+  if (KIND != kBdf2) {
+    o.s0 = V.rp(i + 1)[A_G * kTile];
+    o.s1 = 0.0;
+  } else {
+    o.s0 = r[A_G * kTile];
+    o.s1 = r[A_U * kTile];
+  }
+  return o;
+}
+struct BwdRow {
+  double cp, d, psi;
+};
+__device__ __forceinline__ BwdRow bwd_load(const TileView& V, int i) {
+  const double* r = V.rp(i);
+  return BwdRow{r[A_CP * kTile], r[A_D * kTile], r[A_PSI * kTile]};
+}
+
 // One implicit stage (solve_implicit_stage_projected) at time t_impl with
 // weight w, ending in A_G.
 //   kEuler: rhs = guess = u_prev, u_prev <- u first (A_G copied to A_U);
 //   kTrap:  rhs = u_prev + w L(u_prev) with L at rate r_expl, guess = u_prev,
 //           u_prev <- u first;
 //   kBdf2:  rhs = alpha u* + beta u_prev (u* in A_G), guess = u*.
-// Returns false on a pivot below the reference's singularity tolerance.
+// L(u_prev) is applied in band form, the Jacobian entries at r_expl (the
+// same operator as the reference's centred differences, summed in another
+// order).  Both sweeps read their rows two ahead of the row being solved, so
+// the serial recurrences overlap the loads.  Returns false on a pivot below
+// the reference's singularity tolerance.
 template <int KIND>
 __device__ bool tv_stage(const Lane& L, double t_impl, double w, double r_expl, double alpha,
                          double beta) {
@@ -231,30 +269,35 @@ __device__ bool tv_stage(const Lane& L, double t_impl, double w, double r_expl, 
   const double r_impl = L.rate(t_impl);
   const double b = r_impl - L.q - L.hss;  // first_derivative_coeff(t)
   const double c = -r_impl;               // -discount_rate(t)
-  const double drift_e = r_expl - L.q - L.hss;
+  const double be = r_expl - L.q - L.hss;
+  const double ce = -r_expl;
   const double bcl = L.bcl, bcr = L.bcr(t_impl);
   const bool lockable = L.psi_max > 0.0;
   // row 0: Dirichlet identity row, rhs = boundary value
   double cp = 0.0 / 1.0;
   double dp = bcl / 1.0;
-  double ul = 0.0, uc = 0.0, ur = 0.0;
+  double ul = 0.0, uc = 0.0;
   if (KIND != kBdf2) {
     ul = V.at(A_G, 0);
     uc = V.at(A_G, 1);
     V.at(A_U, 0) = ul;
     V.at(A_U, 1) = uc;
   }
-  for (int i = 1; i < n - 1; ++i) {
-    const double* r = V.rp(i);
+  const int last = n - 2;  // last interior row
+  FwdRow f0 = fwd_load<KIND>(V, 1);
+  FwdRow f1 = last >= 2 ? fwd_load<KIND>(V, 2) : f0;
+  for (int i = 1; i <= last; ++i) {
+    const FwdRow f2 = i + 2 <= last ? fwd_load<KIND>(V, i + 2) : f1;
     double rhs, guess;
     if (KIND != kBdf2) {
-      ur = V.at(A_G, i + 1);
+      const double ur = f0.s0;
       V.at(A_U, i + 1) = ur;
       guess = uc;
       if (KIND == kTrap) {
-        double d1, d2;
-        cdiff(L, i, ul, uc, ur, &d1, &d2);
-        const double lu = L.hss * d2 + drift_e * d1 - r_expl * uc;
+        const double el = f0.d2m + (-be) * f0.qm;
+        const double ed = f0.d2i + be * f0.qi + ce;
+        const double eu = f0.d2p + be * f0.qp;
+        const double lu = fma(el, ul, fma(ed, uc, eu * ur));
         rhs = fma(w, lu, uc);
       } else {
         rhs = uc;
@@ -262,17 +305,16 @@ __device__ bool tv_stage(const Lane& L, double t_impl, double w, double r_expl, 
       ul = uc;
       uc = ur;
     } else {
-      const double g = V.at(A_G, i);
-      guess = g;
-      rhs = fma(alpha, g, beta * V.at(A_U, i));
+      guess = f0.s0;
+      rhs = fma(alpha, f0.s0, beta * f0.s1);
     }
-    const double jl = r[T_D2M * kTile] + (-b) * r[T_QM * kTile];
-    const double jd = r[T_D2I * kTile] + b * r[T_QI * kTile] + c;
-    const double ju = r[T_D2P * kTile] + b * r[T_QP * kTile];
+    const double jl = f0.d2m + (-b) * f0.qm;
+    const double jd = f0.d2i + b * f0.qi + c;
+    const double ju = f0.d2p + b * f0.qp;
     double lo = -w * jl, dg = 1.0 - w * jd, up = -w * ju;
-    const double psi = r[A_PSI * kTile];
+    const double psi = f0.psi;
     if (lockable && psi > L.thr && guess - psi < 1e-8) {
-      const double lpsi = L.hss * r[T_D2PSI * kTile] + b * r[T_D1PSI * kTile] - r_impl * psi;
+      const double lpsi = L.hss * V.at(T_D2PSI, i) + b * V.at(T_D1PSI, i) - r_impl * psi;
       if (lpsi < 0.0) {
         lo = 0.0;
         dg = 1.0;
@@ -287,14 +329,21 @@ __device__ bool tv_stage(const Lane& L, double t_impl, double w, double r_expl, 
     dp = fma(-lo, dp, rhs) * inv;
     V.at(A_CP, i) = cp;
     V.at(A_D, i) = dp;
+    f0 = f1;
+    f1 = f2;
   }
   // row n-1: Dirichlet identity row (lower entry 0)
   const double dlast = fma(-0.0, dp, bcr) / fma(-0.0, cp, 1.0);
   double sol = dmax_ref(dlast, V.at(A_PSI, n - 1));
   V.at(A_G, n - 1) = sol;
-  for (int i = n - 2; i >= 1; --i) {
-    sol = dmax_ref(fma(-V.at(A_CP, i), sol, V.at(A_D, i)), V.at(A_PSI, i));
+  BwdRow g0 = bwd_load(V, last);
+  BwdRow g1 = last >= 2 ? bwd_load(V, last - 1) : g0;
+  for (int i = last; i >= 1; --i) {
+    const BwdRow g2 = i - 2 >= 1 ? bwd_load(V, i - 2) : g1;
+    sol = dmax_ref(fma(-g0.cp, sol, g0.d), g0.psi);
     V.at(A_G, i) = sol;
+    g0 = g1;
+    g1 = g2;
   }
   // row 0 (c'_0 = 0, d'_0 = bcl), then the boundary values again
   V.at(A_G, 0) = bcl;

@@ -57,9 +57,9 @@ void HostBuf::release() {
   cap = 0;
 }
 
-void parallel_for(int64_t n, const std::function<void(int64_t)>& f) {
+void parallel_for(int64_t n, const std::function<void(int64_t)>& f, int64_t grain) {
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const int64_t per = 512;
+  const int64_t per = std::max<int64_t>(1, grain);
   const int64_t nth = std::min<int64_t>(hw, (n + per - 1) / per);
   if (nth <= 1) {
     for (int64_t i = 0; i < n; ++i) f(i);
@@ -287,7 +287,8 @@ void destroy_batch(MangoGpuBatch* b) {
 // Validate, resolve grids, sort/tile, pack and upload.
 MangoGpuBatch* create_batch(MangoGpuContext* ctx, const MangoPricingParams* params, int64_t n,
                             const MangoGpuGrid* grids, uint64_t grid_stride,
-                            const MangoGpuTrbdf2* trbdf2) {
+                            const MangoGpuTrbdf2* trbdf2, MangoGpuBatch* reuse,
+                            cudaStream_t stream) {
   auto t0 = Clock::now();
   std::vector<Resolved> res(static_cast<size_t>(n));
   std::vector<std::string> msgs(static_cast<size_t>(n));
@@ -308,7 +309,8 @@ MangoGpuBatch* create_batch(MangoGpuContext* ctx, const MangoPricingParams* para
     }
   });
   const double resolve_ms = ms_since(t0);
-  MangoGpuBatch* b = create_batch_resolved(ctx, params, std::move(res), std::move(msgs), trbdf2);
+  MangoGpuBatch* b =
+      create_batch_resolved(ctx, params, std::move(res), std::move(msgs), trbdf2, reuse, stream);
   b->host_prep_ms += resolve_ms;
   return b;
 }
@@ -316,17 +318,31 @@ MangoGpuBatch* create_batch(MangoGpuContext* ctx, const MangoPricingParams* para
 MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingParams* params,
                                      std::vector<Resolved> resolved,
                                      std::vector<std::string> messages,
-                                     const MangoGpuTrbdf2* trbdf2) {
+                                     const MangoGpuTrbdf2* trbdf2, MangoGpuBatch* reuse,
+                                     cudaStream_t stream) {
   auto t0 = Clock::now();
   const int64_t n = static_cast<int64_t>(resolved.size());
-  std::unique_ptr<MangoGpuBatch, void (*)(MangoGpuBatch*)> b(new MangoGpuBatch(), destroy_batch);
+  auto keep = [](MangoGpuBatch*) {};
+  std::unique_ptr<MangoGpuBatch, void (*)(MangoGpuBatch*)> b(
+      reuse ? reuse : new MangoGpuBatch(), reuse ? static_cast<void (*)(MangoGpuBatch*)>(keep)
+                                                 : destroy_batch);
   b->ctx = ctx;
+  b->stream = stream ? stream : ctx->stream;
   b->n = n;
   b->mc = make_const(trbdf2);
   b->res = std::move(resolved);
   b->msgs = std::move(messages);
   b->msgs.resize(static_cast<size_t>(n));
-  for (auto& e : b->ev) check(cudaEventCreate(&e), "cudaEventCreate");
+  b->order.clear();
+  b->ntiles = 0;
+  b->algo_flops = 0;
+  b->h2d_bytes = 0;
+  b->host_prep_ms = 0;
+  b->tv_tile0 = 0;
+  b->ran = false;
+  b->runs = 0;
+  for (auto& e : b->ev)
+    if (!e) check(cudaEventCreate(&e), "cudaEventCreate");
   // Sort accepted options by (n_space, n_time) descending, so that the
   // largest tiles are dequeued first and a tile's lanes share their row
   // and step counts; then by option type and normalised moneyness
@@ -334,25 +350,59 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
   // similar rows and leave the cached factorisation together (lanes on the
   // off-cache path at different rows serialise a warp).
   std::vector<int32_t>& order = b->order;
-  std::vector<double> mkey(static_cast<size_t>(n), 0.0);
-  for (int64_t i = 0; i < n; ++i) {
-    if (b->res[i].status != 0) continue;
-    order.push_back(static_cast<int32_t>(i));
-    const MangoPricingParams& p = params[b->res[i].orig];
+  struct SortKey {
+    int64_t n, nt;
+    double mk;
+    int32_t tv, type, idx, pad;
+  };
+  std::vector<int32_t> valid;
+  valid.reserve(static_cast<size_t>(n));
+  for (int64_t i = 0; i < n; ++i)
+    if (b->res[i].status == 0) valid.push_back(static_cast<int32_t>(i));
+  const int64_t nv = static_cast<int64_t>(valid.size());
+  std::vector<SortKey> keys(static_cast<size_t>(nv));
+  parallel_for(nv, [&](int64_t j) {
+    const int32_t i = valid[j];
+    const Resolved& r = b->res[i];
+    const MangoPricingParams& p = params[r.orig];
     const double k = std::log(p.spot / p.strike) / (p.volatility * std::sqrt(p.maturity));
-    mkey[i] = std::isfinite(k) ? k : 0.0;
+    keys[j] = SortKey{r.spec.n, r.nt, std::isfinite(k) ? k : 0.0, r.tv ? 1 : 0, p.option_type, i, 0};
+  }, 4096);
+  auto before = [](const SortKey& a, const SortKey& c) {
+    if (a.tv != c.tv) return a.tv < c.tv;  // time-varying options last
+    if (a.n != c.n) return a.n > c.n;
+    if (a.nt != c.nt) return a.nt > c.nt;
+    if (a.type != c.type) return a.type < c.type;
+    if (a.mk != c.mk) return a.mk < c.mk;
+    return a.idx < c.idx;
+  };
+  {
+    // Parallel sort: sorted runs on all host cores, then pairwise merges.
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    int64_t parts = std::min<int64_t>(hw, std::max<int64_t>(1, nv / 4096));
+    std::vector<int64_t> cut(static_cast<size_t>(parts) + 1);
+    for (int64_t q = 0; q <= parts; ++q) cut[q] = nv * q / parts;
+    parallel_for(parts, [&](int64_t q) {
+      std::sort(keys.begin() + cut[q], keys.begin() + cut[q + 1], before);
+    }, 1);
+    std::vector<SortKey> tmp(keys.size());
+    while (parts > 1) {
+      const int64_t pairs = (parts + 1) / 2;
+      std::vector<int64_t> ncut(static_cast<size_t>(pairs) + 1);
+      parallel_for(pairs, [&](int64_t q) {
+        const int64_t a = cut[2 * q], mid = cut[std::min<int64_t>(2 * q + 1, parts)],
+                      e = cut[std::min<int64_t>(2 * q + 2, parts)];
+        std::merge(keys.begin() + a, keys.begin() + mid, keys.begin() + mid, keys.begin() + e,
+                   tmp.begin() + a, before);
+      }, 1);
+      for (int64_t q = 0; q <= pairs; ++q) ncut[q] = cut[std::min<int64_t>(2 * q, parts)];
+      keys.swap(tmp);
+      cut.swap(ncut);
+      parts = pairs;
+    }
   }
-  std::sort(order.begin(), order.end(), [&](int32_t a, int32_t c) {
-    const Resolved& ra = b->res[a];
-    const Resolved& rc = b->res[c];
-    if (ra.tv != rc.tv) return rc.tv;  // time-varying options last
-    if (ra.spec.n != rc.spec.n) return ra.spec.n > rc.spec.n;
-    if (ra.nt != rc.nt) return ra.nt > rc.nt;
-    const int pa = params[ra.orig].option_type, pc = params[rc.orig].option_type;
-    if (pa != pc) return pa < pc;
-    if (mkey[a] != mkey[c]) return mkey[a] < mkey[c];
-    return a < c;
-  });
+  order.resize(static_cast<size_t>(nv));
+  for (int64_t j = 0; j < nv; ++j) order[j] = keys[j].idx;
   const int64_t m = static_cast<int64_t>(order.size());
   const int32_t ntiles = static_cast<int32_t>((m + kTile - 1) / kTile);
   b->ntiles = ntiles;
@@ -389,7 +439,7 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
 
   OptDev* opts = static_cast<OptDev*>(b->h_opts.get(sizeof(OptDev) * std::max<int64_t>(m, 1)));
   double* xs = static_cast<double*>(b->h_xs.get(sizeof(double) * std::max<int64_t>(xoff, 1)));
-  parallel_for(ntiles, [&](int64_t t) {
+  parallel_for(ntiles, [&](int64_t t) {  // 32 grids per item: a small grain
     const TileDev& td = tiles[t];
     std::vector<double> x;
     for (int l = 0; l < kTile; ++l) {
@@ -420,7 +470,7 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
       o.is_put = put ? 1 : 0;
       o.orig = r.orig;
     }
-  });
+  }, 8);
   // Time-varying options: per-option data, time points, curves, events.
   int64_t nc = 0;
   while (nc < m && !b->res[order[nc]].tv) ++nc;
@@ -491,7 +541,7 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
   b->host_prep_ms = ms_since(t0);
 
   if (m > 0) {
-    cudaStream_t st = ctx->stream;
+    cudaStream_t st = b->stream;
     b->d_pool.get(sizeof(double) * off);
     double* d_xs = static_cast<double*>(b->d_xs.get(sizeof(double) * xoff));
     b->d_flags.get(static_cast<size_t>(foff));
@@ -531,7 +581,7 @@ void run_batch(MangoGpuBatch* b) {
   const int64_t m = static_cast<int64_t>(b->order.size());
   b->ran = true;
   if (m == 0) return;
-  cudaStream_t st = ctx->stream;
+  cudaStream_t st = b->stream;
   const int ntiles = b->ntiles;
   const int threads = ntiles * kTile;
   const TileDev* d_tiles = b->d_tiles.as<TileDev>();
@@ -596,7 +646,7 @@ uint64_t fetch_batch(MangoGpuBatch* b, MangoGpuAmericanOut* out, std::string* fi
     if (o.status != 0 && first_msg->empty()) *first_msg = b->msgs[i];
   }
   if (m > 0) {
-    cudaStream_t st = ctx->stream;
+    cudaStream_t st = b->stream;
     double* h_out4 = static_cast<double*>(b->h_out4.get(sizeof(double) * 4 * m));
     int32_t* h_status = static_cast<int32_t*>(b->h_status.get(sizeof(int32_t) * m));
     check(cudaMemcpyAsync(h_out4, b->d_out4.p, sizeof(double) * 4 * m, cudaMemcpyDeviceToHost, st),
@@ -665,6 +715,7 @@ MangoStatus mango_gpu_context_create(int32_t device, MangoGpuContext** out, Mang
     ctx->num_sms = prop.multiProcessorCount;
     check(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking), "stream");
     ctx->stream = ctx->own_stream;
+    for (auto& a : ctx->aux) check(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking), "stream");
     int bps = 0;
     check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, march_kernel, 128, 0), "occupancy");
     ctx->march_blocks_per_sm = std::max(1, bps);
@@ -672,6 +723,9 @@ MangoStatus mango_gpu_context_create(int32_t device, MangoGpuContext** out, Mang
     return MANGO_OK;
   } catch (const std::exception& e) {
     if (ctx && ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    if (ctx)
+      for (auto& a : ctx->aux)
+        if (a) cudaStreamDestroy(a);
     delete ctx;
     set_err(err, MANGO_ERR_SOLVER, e.what());
     return MANGO_ERR_SOLVER;
@@ -682,6 +736,12 @@ void mango_gpu_context_destroy(MangoGpuContext* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->scratch) destroy_batch(ctx->scratch);
+  for (int c = 0; c < 2; ++c) {
+    if (ctx->aux[c]) cudaStreamSynchronize(ctx->aux[c]);
+    if (ctx->chunk[c]) destroy_batch(ctx->chunk[c]);
+    if (ctx->aux[c]) cudaStreamDestroy(ctx->aux[c]);
+  }
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
 }
@@ -756,7 +816,7 @@ MangoStatus mango_gpu_batch_results(MangoGpuBatch* b, MangoGpuAmericanOut* out,
 void mango_gpu_batch_destroy(MangoGpuBatch* b) {
   if (!b) return;
   cudaSetDevice(b->ctx->device);
-  cudaStreamSynchronize(b->ctx->stream);
+  cudaStreamSynchronize(b->stream);
   destroy_batch(b);
 }
 
@@ -768,7 +828,7 @@ MangoStatus mango_gpu_batch_timings(MangoGpuBatch* b, int32_t reset, double* pre
     return MANGO_ERR_VALIDATION;
   }
   try {
-    check(cudaStreamSynchronize(b->ctx->stream), "stream synchronize");
+    check(cudaStreamSynchronize(b->stream), "stream synchronize");
     const int64_t k = std::min<int64_t>(b->runs, MangoGpuBatch::kMaxTimedRuns);
     double acc[3] = {0, 0, 0};
     for (int64_t r = 0; r < k; ++r)
@@ -799,15 +859,83 @@ MangoStatus mango_gpu_price_american_batch(MangoGpuContext* ctx, const MangoPric
     set_err(err, MANGO_ERR_VALIDATION, "null context, params or out");
     return MANGO_ERR_VALIDATION;
   }
+  if (n > (1ull << 30)) {
+    set_err(err, MANGO_ERR_VALIDATION, "batch above 2^30 options");
+    return MANGO_ERR_VALIDATION;
+  }
   auto t0 = Clock::now();
-  MangoGpuBatch* b = nullptr;
-  MangoStatus st = mango_gpu_batch_create(ctx, params, n, grids, grid_stride, trbdf2, &b, err);
-  if (st != MANGO_OK) return st;
-  st = mango_gpu_batch_run(b, err);
-  if (st == MANGO_OK) st = mango_gpu_batch_results(b, out, out_failed, err);
-  mango_gpu_batch_destroy(b);
-  ctx->stats.total_ms = ms_since(t0);
-  return st;
+  try {
+    check(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const int64_t nn = static_cast<int64_t>(n);
+    // Large batches: k chunks alternating over two streams and two reused
+    // batches; chunk c is prepared on the host while chunk c-1 runs, and
+    // chunk c-2's results are collected before its buffers are refilled.
+    // Chunks keep at least kChunkMin options, so each march still has
+    // several tiles per resident warp (a smaller chunk cannot fill the GPU).
+    constexpr int64_t kChunkMin = 65536;
+    const int k = static_cast<int>(std::min<int64_t>(4, std::max<int64_t>(1, nn / kChunkMin)));
+    if (k > 1) {
+      cudaEvent_t start = nullptr;
+      check(cudaEventCreateWithFlags(&start, cudaEventDisableTiming), "event");
+      check(cudaEventRecord(start, ctx->stream), "event");
+      for (auto a : ctx->aux) {
+        check(cudaStreamSynchronize(a), "stream synchronize");
+        check(cudaStreamWaitEvent(a, start, 0), "stream wait");
+      }
+      cudaEventDestroy(start);
+      Stats acc{};
+      uint64_t failed = 0;
+      std::string first;
+      std::vector<int64_t> off(static_cast<size_t>(k) + 1);
+      for (int c = 0; c <= k; ++c) off[c] = nn * c / k;
+      auto collect = [&](int c) {
+        failed += fetch_batch(ctx->chunk[c % 2], out + off[c], &first);
+        const Stats& S = ctx->stats;
+        acc.host_prep_ms += S.host_prep_ms;
+        acc.h2d_ms += S.h2d_ms;
+        acc.prep_ms += S.prep_ms;
+        acc.march_ms += S.march_ms;
+        acc.outputs_ms += S.outputs_ms;
+        acc.d2h_ms += S.d2h_ms;
+        acc.options += S.options;
+        acc.tiles += S.tiles;
+        acc.kernel_launches += S.kernel_launches;
+        acc.algo_flops += S.algo_flops;
+        acc.h2d_bytes += S.h2d_bytes;
+        acc.d2h_bytes += S.d2h_bytes;
+      };
+      for (int c = 0; c < k; ++c) {
+        if (c >= 2) collect(c - 2);
+        const MangoGpuGrid* g = grids ? grids + (grid_stride ? off[c] : 0) : nullptr;
+        ctx->chunk[c % 2] = create_batch(ctx, params + off[c], off[c + 1] - off[c], g, grid_stride,
+                                         trbdf2, ctx->chunk[c % 2], ctx->aux[c % 2]);
+        run_batch(ctx->chunk[c % 2]);
+      }
+      for (int c = std::max(0, k - 2); c < k; ++c) collect(c);
+      acc.total_ms = ms_since(t0);
+      ctx->stats = acc;
+      if (out_failed) *out_failed = failed;
+      if (failed && err) set_err(err, MANGO_OK, first.empty() ? "solver failure" : first);
+      return MANGO_OK;
+    }
+    // The context's scratch batch: its device and pinned host buffers are
+    // reused (grow-only) by the next call, once no copy of an earlier call
+    // (one that failed midway) can still touch them.
+    if (ctx->scratch) check(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    MangoGpuBatch* b = create_batch(ctx, params, static_cast<int64_t>(n), grids, grid_stride,
+                                    trbdf2, ctx->scratch);
+    ctx->scratch = b;
+    run_batch(b);
+    std::string first;
+    const uint64_t failed = fetch_batch(b, out, &first);
+    if (out_failed) *out_failed = failed;
+    if (failed && err) set_err(err, MANGO_OK, first.empty() ? "solver failure" : first);
+    ctx->stats.total_ms = ms_since(t0);
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
 }
 
 MangoStatus mango_gpu_fp64_probe(MangoGpuContext* ctx, double* tflops, MangoError* err) {

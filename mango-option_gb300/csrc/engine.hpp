@@ -74,8 +74,8 @@ void explicit_time_domain(double maturity, int64_t n_time, const std::vector<dou
 std::string resolve(const MangoPricingParams& p, const MangoGpuGrid& g, Resolved* r,
                     std::vector<double>* scratch);
 
-// Run f(i) for i in [0, n) on all host cores.
-void parallel_for(int64_t n, const std::function<void(int64_t)>& f);
+// Run f(i) for i in [0, n) on all host cores, at least grain items per thread.
+void parallel_for(int64_t n, const std::function<void(int64_t)>& f, int64_t grain = 512);
 
 void set_err(MangoError* err, int32_t code, const std::string& msg);
 
@@ -86,15 +86,20 @@ struct MangoGpuBatch;
 namespace mgpu {
 MarchConst make_const(const MangoGpuTrbdf2* trbdf2);
 // Validate, resolve grids, sort/tile, pack and upload (batch pipeline).
+// reuse: an existing batch whose buffers are refilled (grow-only) instead
+// of a new one.
 MangoGpuBatch* create_batch(MangoGpuContext* ctx, const MangoPricingParams* params, int64_t n,
                             const MangoGpuGrid* grids, uint64_t grid_stride,
-                            const MangoGpuTrbdf2* trbdf2);
+                            const MangoGpuTrbdf2* trbdf2, MangoGpuBatch* reuse = nullptr,
+                            cudaStream_t stream = nullptr);
 // Same pipeline from already validated and resolved options (res[i].orig
 // indexes params; status != 0 entries stay off the device).
 MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingParams* params,
                                      std::vector<Resolved> resolved,
                                      std::vector<std::string> messages,
-                                     const MangoGpuTrbdf2* trbdf2);
+                                     const MangoGpuTrbdf2* trbdf2,
+                                     MangoGpuBatch* reuse = nullptr,
+                                     cudaStream_t stream = nullptr);
 void destroy_batch(MangoGpuBatch* b);
 // Enqueue setup, march and outputs (with timing events).
 void run_batch(MangoGpuBatch* b);
@@ -135,10 +140,18 @@ struct MangoGpuContext {
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;  // own_stream or a caller's stream
   mgpu::Stats stats;
+  // Buffers of the one-shot batch call, kept for the next call (device
+  // allocation and host page locking would otherwise be paid every call).
+  MangoGpuBatch* scratch = nullptr;
+  // Large one-shot batches run as chunks on two streams, so that the host
+  // preparation of a chunk overlaps the device work of the one before.
+  cudaStream_t aux[2] = {nullptr, nullptr};
+  MangoGpuBatch* chunk[2] = {nullptr, nullptr};
 };
 
 struct MangoGpuBatch {
   MangoGpuContext* ctx = nullptr;
+  cudaStream_t stream = nullptr;          // all of this batch's device work
   int64_t n = 0;                          // caller's slot count
   std::vector<mgpu::Resolved> res;        // per slot
   std::vector<std::string> msgs;          // per slot validation message

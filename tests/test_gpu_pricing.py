@@ -121,3 +121,23 @@ def test_american_option_price_single(pkg):
     assert abs(res.delta() - -0.422923644193511) < 1e-9
     batch = pkg.BatchAmericanOptionSolver().solve_batch([p, p])
     assert batch.failed_count == 0 and batch.results[1].value() == res.value()
+
+
+@pytest.mark.parametrize("n", [131072, 270000])
+def test_chunked_batch_matches_resident_batch(engine, pkg, n):
+    """Batches of 131,072 options or more run as 2 to 4 chunks on two
+    streams; every option equals its price from one resident (unchunked)
+    batch."""
+    rng = np.random.default_rng(n)
+    p = pkg.pricing_array(100.0, rng.uniform(80, 120, n), rng.uniform(0.1, 2.0, n), rng.uniform(0.1, 0.5, n),
+                          rng.uniform(0.0, 0.08, n), rng.uniform(0.0, 0.04, n), (np.arange(n) % 3 != 0))
+    grid = pkg.grid_array(1, pkg.GRID_FIXED_N, 51, 60)
+    out = engine.price_arrays(p, grid)
+    b = engine.batch(p, grid)
+    b.run()
+    ref = b.results()
+    b.close()
+    assert (out["status"] == 0).all() and (ref["status"] == 0).all()
+    check(greeks(out), greeks(ref), rtol=1e-13, atol=1e-14)
+    again = engine.price_arrays(p, grid)  # buffers reused
+    assert np.array_equal(again["value"], out["value"])

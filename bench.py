@@ -465,7 +465,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--options", type=int, default=N_OPTIONS)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--no-extra", action="store_true", help="skip the uneven-grid side measurement")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the uneven-grid and schedule side measurements")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-grid side measurement")
     ap.add_argument("--no-iv", action="store_true", help="skip the batched-IV side measurement")
     ap.add_argument("--iv-quotes", type=int, default=262144)
     ap.add_argument("--no-table", action="store_true", help="skip the table sweep / query side measurement")
@@ -563,7 +565,7 @@ def main():
                 "algo_flops_per_launch": algo, "hbm_streaming": hbm}
 
     extra = {}
-    if not args.no_extra and rank == 0:
+    if not args.no_extra and not args.no_uneven and rank == 0:
         p2, g2, _ = make_workload(pkg, n, seed=77, uneven=True)
         b2 = eng.batch(p2, g2)
         b2.run()

@@ -114,6 +114,7 @@ struct Lane {
   double hss, q;
   double u_dx2, u_hdx;  // uniform-grid centred-difference weights
   double psi_max, thr;
+  int clo, chi;         // interior rows with psi > thr (lock candidates): [clo, chi]
   double bcl;           // left boundary value (time invariant)
   double exp_xr;        // e^{x_{n-1}}
   double T, r_const;
@@ -182,6 +183,16 @@ __device__ void tv_setup(Lane& L) {
   }
   L.psi_max = psi_max;
   L.thr = 0.95 * psi_max;
+  // Lock condition 1 (psi > 0.95 max psi) does not change in time: the
+  // stages test the other two only on rows where it holds.
+  L.clo = 0x7fffffff;
+  L.chi = -1;
+  if (psi_max > 0.0)
+    for (int i = 1; i < n - 1; ++i)
+      if (V.at(A_PSI, i) > L.thr) {
+        L.clo = min(L.clo, i);
+        L.chi = i;
+      }
   const double a = L.hss;
   for (int i = 1; i < n - 1; ++i) {
     const double xl = L.x(i - 1), xi = L.x(i), xr = L.x(i + 1);
@@ -215,6 +226,15 @@ __device__ void tv_setup(Lane& L) {
 }
 
 enum StageKind { kEuler = 0, kTrap = 1, kBdf2 = 2 };
+
+// std::max(v, psi) for a payoff psi >= +0, by integer compare (no FP64
+// instruction): non-negative doubles order like their bit patterns and a
+// negative v loses.  Differs from the reference only for v = -0, psi = +0
+// (+0 instead of -0, the same number).
+__device__ __forceinline__ double pmax(double v, double psi) {
+  const long long vb = __double_as_longlong(v), pb = __double_as_longlong(psi);
+  return __longlong_as_double(vb > pb ? vb : pb);
+}
 
 // Inputs of forward-sweep row i: the grid-only band parts, psi and the
 // stage's state (u_prev at row i + 1 for kEuler / kTrap, u* and u_prev at
@@ -272,7 +292,6 @@ __device__ bool tv_stage(const Lane& L, double t_impl, double w, double r_expl, 
   const double be = r_expl - L.q - L.hss;
   const double ce = -r_expl;
   const double bcl = L.bcl, bcr = L.bcr(t_impl);
-  const bool lockable = L.psi_max > 0.0;
   // row 0: Dirichlet identity row, rhs = boundary value
   double cp = 0.0 / 1.0;
   double dp = bcl / 1.0;
@@ -313,7 +332,7 @@ __device__ bool tv_stage(const Lane& L, double t_impl, double w, double r_expl, 
     const double ju = f0.d2p + b * f0.qp;
     double lo = -w * jl, dg = 1.0 - w * jd, up = -w * ju;
     const double psi = f0.psi;
-    if (lockable && psi > L.thr && guess - psi < 1e-8) {
+    if (i >= L.clo && i <= L.chi && psi > L.thr && guess - psi < 1e-8) {
       const double lpsi = L.hss * V.at(T_D2PSI, i) + b * V.at(T_D1PSI, i) - r_impl * psi;
       if (lpsi < 0.0) {
         lo = 0.0;
@@ -334,13 +353,13 @@ __device__ bool tv_stage(const Lane& L, double t_impl, double w, double r_expl, 
   }
   // row n-1: Dirichlet identity row (lower entry 0)
   const double dlast = fma(-0.0, dp, bcr) / fma(-0.0, cp, 1.0);
-  double sol = dmax_ref(dlast, V.at(A_PSI, n - 1));
+  double sol = pmax(dlast, V.at(A_PSI, n - 1));
   V.at(A_G, n - 1) = sol;
   BwdRow g0 = bwd_load(V, last);
   BwdRow g1 = last >= 2 ? bwd_load(V, last - 1) : g0;
   for (int i = last; i >= 1; --i) {
     const BwdRow g2 = i - 2 >= 1 ? bwd_load(V, i - 2) : g1;
-    sol = dmax_ref(fma(-g0.cp, sol, g0.d), g0.psi);
+    sol = pmax(fma(-g0.cp, sol, g0.d), g0.psi);
     V.at(A_G, i) = sol;
     g0 = g1;
     g1 = g2;

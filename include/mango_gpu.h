@@ -318,6 +318,19 @@ MangoStatus mango_gpu_bspline4d_eval_device(MangoGpuBSpline4D* surface, const do
 /* The packed knot vectors (axis 0..3, sizes[d] + 4 each), for inspection. */
 MangoStatus mango_gpu_bspline4d_knots(const MangoGpuBSpline4D* surface, double* out, uint64_t cap,
                                       uint64_t* n_out);
+/* The surface's data for serialisation (BSplineND grid(d) / coefficients(),
+ * src/option/table/serialization/extract_segments.hpp:38-58): sizes[4], the
+ * packed axes (sum of sizes doubles; NULL to skip) and the coefficients in
+ * row-major order (product of sizes doubles, copied from the device; NULL to
+ * skip). */
+MangoStatus mango_gpu_bspline4d_export(const MangoGpuBSpline4D* surface, int64_t* sizes,
+                                       double* grids, uint64_t grid_cap, double* coeffs,
+                                       uint64_t coeff_cap, MangoError* err);
+
+/* CRC64::update (src/support/crc64.hpp): reflected ECMA-182 polynomial
+ * 0xC96C5795D7870F42 over n bytes from crc (0 to start), no final
+ * inversion; the checksum of the Parquet price-table format.  Host only. */
+uint64_t mango_gpu_crc64_update(uint64_t crc, const void* data, uint64_t n);
 
 /* Separable collocation fit: BSplineNDSeparable<double,4>::fit
  * (src/math/bspline/bspline_nd_separable.hpp:153-384) with

@@ -173,6 +173,11 @@ def library() -> ctypes.CDLL:
         lib.mango_gpu_bspline4d_eval_device.restype = ctypes.c_int32
         lib.mango_gpu_bspline4d_knots.argtypes = [_P, _P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
         lib.mango_gpu_bspline4d_knots.restype = ctypes.c_int32
+        lib.mango_gpu_bspline4d_export.argtypes = [_P, _P, _P, ctypes.c_uint64, _P, ctypes.c_uint64,
+                                                   ctypes.POINTER(MangoError)]
+        lib.mango_gpu_bspline4d_export.restype = ctypes.c_int32
+        lib.mango_gpu_crc64_update.argtypes = [ctypes.c_uint64, ctypes.c_char_p, ctypes.c_uint64]
+        lib.mango_gpu_crc64_update.restype = ctypes.c_uint64
         lib.mango_gpu_bspline4d_fit.argtypes = [_P, _P, _P, _P, ctypes.c_double, _P,
                                                 ctypes.POINTER(MangoGpuFitStats), ctypes.POINTER(MangoError)]
         lib.mango_gpu_bspline4d_fit.restype = ctypes.c_int32
@@ -808,6 +813,23 @@ class GpuPriceTable:
         self.validate(params)
         return float(self.price_arrays(_to_array([params]))[0])
 
+    def spline_knots(self) -> np.ndarray:
+        """The spline's packed clamped knots (n_d + 4 per axis)."""
+        s = library().mango_gpu_price_table_spline(self._t)
+        n = ctypes.c_uint64()
+        library().mango_gpu_bspline4d_knots(s, None, 0, ctypes.byref(n))
+        out = np.zeros(n.value)
+        library().mango_gpu_bspline4d_knots(s, _ptr(out), n.value, ctypes.byref(n))
+        return out
+
+    def to_data(self) -> "PriceTableData":
+        """to_data: the reference's PriceTableData of this table."""
+        return to_data(self)
+
+    def save(self, path, compression: str = "zstd") -> None:
+        """write_parquet(to_data(table), path): the reference's Parquet file."""
+        write_parquet(to_data(self), path, compression)
+
     def spline_eval(self, queries: np.ndarray) -> np.ndarray:
         q = np.ascontiguousarray(queries, dtype=np.float64).reshape(-1, 4)
         out = np.zeros(q.shape[0])
@@ -1212,3 +1234,11 @@ class IVSolver:
             raise r
         return r
 
+
+from .persistence import (PriceTableData, PriceTableSegment, SerializationError,  # noqa: E402
+                          from_data, read_parquet, to_data, write_parquet)
+
+
+def load_price_table(path, engine: Optional[Engine] = None) -> "GpuPriceTable":
+    """read_parquet + from_data: a saved bspline_4d table on the device."""
+    return from_data(read_parquet(path), engine)

@@ -111,6 +111,7 @@ MangoGpuBSpline4D* new_surface(MangoGpuContext* ctx, const double* grids, const 
   try {
     s->ctx = ctx;
     bspline_tables(grids, sizes, &s->dims, &tab, &s->knots);
+    s->grids.assign(grids, grids + (sizes[0] + sizes[1] + sizes[2] + sizes[3]));
     cudaStream_t st = ctx->stream;
     double* dt = static_cast<double*>(s->d_tables.get(sizeof(double) * tab.size()));
     check(cudaMemcpyAsync(dt, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, st), "H2D");
@@ -237,6 +238,42 @@ MangoStatus mango_gpu_bspline4d_knots(const MangoGpuBSpline4D* s, double* out, u
   *n_out = s->knots.size();
   if (out && cap >= s->knots.size()) std::memcpy(out, s->knots.data(), sizeof(double) * s->knots.size());
   return MANGO_OK;
+}
+
+MangoStatus mango_gpu_bspline4d_export(const MangoGpuBSpline4D* s, int64_t* sizes, double* grids,
+                                       uint64_t grid_cap, double* coeffs, uint64_t coeff_cap,
+                                       MangoError* err) {
+  if (!s || !sizes) {
+    set_err(err, MANGO_ERR_VALIDATION, "null surface or sizes");
+    return MANGO_ERR_VALIDATION;
+  }
+  uint64_t total = 1;
+  for (int d = 0; d < 4; ++d) {
+    sizes[d] = s->dims.n[d];
+    total *= static_cast<uint64_t>(s->dims.n[d]);
+  }
+  try {
+    if (grids) {
+      if (grid_cap < s->grids.size()) {
+        set_err(err, MANGO_ERR_VALIDATION, "grid buffer too small");
+        return MANGO_ERR_VALIDATION;
+      }
+      std::memcpy(grids, s->grids.data(), sizeof(double) * s->grids.size());
+    }
+    if (coeffs) {
+      if (coeff_cap < total) {
+        set_err(err, MANGO_ERR_VALIDATION, "coefficient buffer too small");
+        return MANGO_ERR_VALIDATION;
+      }
+      check(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+      check(cudaStreamSynchronize(s->ctx->stream), "sync");
+      check(cudaMemcpy(coeffs, s->d_coeffs.p, sizeof(double) * total, cudaMemcpyDeviceToHost), "D2H");
+    }
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
 }
 
 }  // extern "C"

@@ -158,5 +158,6 @@ struct MangoGpuBSpline4D {
   mgpu::BSplineDims dims{};
   mgpu::DevBuf d_tables, d_coeffs, d_q, d_out;
   std::vector<double> knots;  // packed, for inspection
+  std::vector<double> grids;  // packed axes, for export
   int blocks = 0;
 };

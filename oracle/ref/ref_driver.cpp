@@ -11,6 +11,7 @@
 // PDEGridConfig{spec, nt} (src/option/grid_spec_types.hpp:55-59).
 #include "mango/option/american_option.hpp"
 #include "mango/option/yield_curve.hpp"
+#include "mango/support/crc64.hpp"
 #include "mango/option/american_option_batch.hpp"
 #include "mango/option/iv_solver.hpp"
 #include "mango/option/grid_spec_types.hpp"
@@ -618,6 +619,12 @@ int32_t ref_batch_shared_tv(int64_t n, const double* S, const double* K, const d
     out_dims[2 * i + 1] = static_cast<int64_t>(ri->grid()->time().n_steps());
   }
   return 0;
+}
+
+
+// CRC64::update of the reference (src/support/crc64.cpp).
+uint64_t ref_crc64_update(uint64_t crc, const uint8_t* data, uint64_t n) {
+  return CRC64::update(crc, data, static_cast<size_t>(n));
 }
 
 }  // extern "C"

@@ -166,3 +166,30 @@ def test_make_price_table_mirror(engine, pkg):
     direct = pkg.american_option_price(p).value()
     assert abs(t.price(p) - direct) < 0.02 * direct
     t.close()
+
+
+def test_table_data_round_trip(engine, pkg):
+    """to_data / from_data (the reference's PriceTableData for bspline_4d):
+    a built table exported and reconstructed prices identically; knots that
+    are not the grids' clamped knots and bounds off the grids are refused."""
+    grid = pkg.PDEGridConfig(-3.0, 3.0, 101, 200)
+    table, _ = engine.price_table_build(*TABLE_AXES, K_ref=100.0, dividend_yield=0.01, option_type=1, grid=grid)
+    d = table.to_data()
+    assert d.surface_type == "bspline_4d" and len(d.segments) == 1
+    s = d.segments[0]
+    assert s.num_pts == [a.size for a in TABLE_AXES] and s.K_ref == 100.0
+    for a, g, k in zip(TABLE_AXES, s.grids, s.knots):
+        assert np.array_equal(a, g) and np.array_equal(k, fit_oracle.clamped_knots(a))
+    t2 = pkg.from_data(d, engine)
+    p = records(pkg, np.stack([np.full(64, 100.0), 100.0 / np.exp(np.linspace(-0.3, 0.2, 64)),
+                               np.full(64, 0.8), np.full(64, 0.25), np.full(64, 0.03)], 1), 1, 0.01)
+    assert np.array_equal(table.price_arrays(p), t2.price_arrays(p))
+    s.knots[2] = s.knots[2] + 1e-9
+    with pytest.raises(pkg.SerializationError):
+        pkg.from_data(d, engine)
+    s.knots[2] = s.knots[2] - 1e-9
+    d.bounds_sigma_max = 0.7
+    with pytest.raises(pkg.SerializationError):
+        pkg.from_data(d, engine)
+    table.close()
+    t2.close()

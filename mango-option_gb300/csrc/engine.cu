@@ -872,7 +872,7 @@ MangoStatus mango_gpu_price_american_batch(MangoGpuContext* ctx, const MangoPric
     // chunk c-2's results are collected before its buffers are refilled.
     // Chunks keep at least kChunkMin options, so each march still has
     // several tiles per resident warp (a smaller chunk cannot fill the GPU).
-    constexpr int64_t kChunkMin = 65536;
+    constexpr int64_t kChunkMin = 32768;
     const int k = static_cast<int>(std::min<int64_t>(4, std::max<int64_t>(1, nn / kChunkMin)));
     if (k > 1) {
       cudaEvent_t start = nullptr;

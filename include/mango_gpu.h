@@ -187,8 +187,8 @@ void mango_gpu_context_destroy(MangoGpuContext* ctx);
  * Returns MANGO_OK unless the call itself could not run (bad pointers, CUDA
  * failure), in which case err says why and no slot is meaningful.
  * The call is synchronous.  Its device and pinned host buffers stay in the
- * context for the next call; batches of 131,072 options or more run as 2 to
- * 4 chunks (at least 65,536 options each) on two internal streams, ordered
+ * context for the next call; batches of 65,536 options or more run as 2 to
+ * 4 chunks (at least 32,768 options each) on two internal streams, ordered
  * after the context's stream, so that the host preparation of a chunk
  * overlaps the device work of the one before. */
 MangoStatus mango_gpu_price_american_batch(MangoGpuContext* ctx,

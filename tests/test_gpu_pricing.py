@@ -123,9 +123,9 @@ def test_american_option_price_single(pkg):
     assert batch.failed_count == 0 and batch.results[1].value() == res.value()
 
 
-@pytest.mark.parametrize("n", [131072, 270000])
+@pytest.mark.parametrize("n", [70000, 270000])
 def test_chunked_batch_matches_resident_batch(engine, pkg, n):
-    """Batches of 131,072 options or more run as 2 to 4 chunks on two
+    """Batches of 65,536 options or more run as 2 to 4 chunks on two
     streams; every option equals its price from one resident (unchunked)
     batch."""
     rng = np.random.default_rng(n)

@@ -9,6 +9,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <thread>
@@ -606,7 +607,14 @@ void run_batch(MangoGpuBatch* b) {
   check(cudaEventRecord(b->ev[3], st), "event");
   check(cudaEventRecord(b->run_ev[slot + 1], st), "event");
   const int warps_per_block = 4;
-  const int blocks = std::max(1, std::min<int>(ctx->num_sms * ctx->march_blocks_per_sm,
+  int bps = ctx->march_blocks_per_sm;
+  // MANGO_GPU_MARCH_BLOCKS_PER_SM: resident march blocks per SM (1 to the
+  // occupancy limit), for launch-shape sweeps.
+  if (const char* e = std::getenv("MANGO_GPU_MARCH_BLOCKS_PER_SM")) {
+    const int v = std::atoi(e);
+    if (v >= 1) bps = std::min(bps, v);
+  }
+  const int blocks = std::max(1, std::min<int>(ctx->num_sms * bps,
                                                (ntiles + warps_per_block - 1) / warps_per_block));
   march_kernel<<<blocks, 32 * warps_per_block, 0, st>>>(d_tiles, ntiles, d_opts, d_pool, d_flags,
                                                         d_mode, d_status, b->d_queue.as<int>(),

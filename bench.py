@@ -466,6 +466,7 @@ def main():
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the uneven-grid and schedule side measurements")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-grid side measurement")
+    ap.add_argument("--no-schedules", action="store_true", help="skip the yield-curve / dividend measurement")
     ap.add_argument("--no-iv", action="store_true", help="skip the batched-IV side measurement")
     ap.add_argument("--iv-quotes", type=int, default=262144)
     ap.add_argument("--no-table", action="store_true", help="skip the table sweep / query side measurement")
@@ -586,7 +587,7 @@ def main():
             "march_ms": kt2["march_ms"], "fp64_frac": algo2 / (kt2["march_ms"] / 1e3) / 1e12 / fp64_peak}
         b2.close()
 
-    if not args.no_extra and rank == 0:
+    if not args.no_extra and not args.no_schedules and rank == 0:
         extra["schedules"] = bench_schedules(pkg, eng, torch, stream, n, fp64_peak)
     if not args.no_iv and rank == 0:
         extra["iv_brent"] = bench_iv(pkg, eng, args.iv_quotes)

@@ -344,12 +344,14 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
   b->runs = 0;
   for (auto& e : b->ev)
     if (!e) check(cudaEventCreate(&e), "cudaEventCreate");
-  // Sort accepted options by (n_space, n_time) descending, so that the
-  // largest tiles are dequeued first and a tile's lanes share their row
-  // and step counts; then by option type and normalised moneyness
-  // ln(S/K) / (sigma sqrt(T)), so that a tile's lanes meet the obstacle at
-  // similar rows and leave the cached factorisation together (lanes on the
-  // off-cache path at different rows serialise a warp).
+  // Sort accepted options by n_space descending (the largest tiles are
+  // dequeued first and a tile's lanes share their row count), then by
+  // option type (puts and calls lock at opposite ends of the grid, so a
+  // mixed tile would test the lock on every row), then by n_time
+  // descending and normalised moneyness ln(S/K) / (sigma sqrt(T)), so that
+  // a tile's lanes meet the obstacle at similar rows and leave the cached
+  // factorisation together (lanes on the off-cache path at different rows
+  // serialise a warp).
   std::vector<int32_t>& order = b->order;
   struct SortKey {
     int64_t n, nt;
@@ -372,8 +374,8 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
   auto before = [](const SortKey& a, const SortKey& c) {
     if (a.tv != c.tv) return a.tv < c.tv;  // time-varying options last
     if (a.n != c.n) return a.n > c.n;
-    if (a.nt != c.nt) return a.nt > c.nt;
     if (a.type != c.type) return a.type < c.type;
+    if (a.nt != c.nt) return a.nt > c.nt;
     if (a.mk != c.mk) return a.mk < c.mk;
     return a.idx < c.idx;
   };

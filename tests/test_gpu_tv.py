@@ -121,3 +121,29 @@ def test_tv_mirror(engine, pkg):
     want = g["auto_out"][6]
     for x in res.results:
         assert abs(x.value() - want[0]) <= RTOL * abs(want[0])
+
+
+def test_tv_in_chunked_batch(engine, pkg):
+    """A one-shot batch large enough to run in chunks, with time-varying
+    options in every chunk: each option equals its price from one resident
+    (unchunked) batch."""
+    n = 70000
+    rng = np.random.default_rng(12)
+    p = pkg.pricing_array(100.0, rng.uniform(85, 115, n), rng.uniform(0.2, 1.5, n), rng.uniform(0.15, 0.4, n),
+                          0.03, 0.0, (np.arange(n) % 2 == 0))
+    curve = [(0.0, 0.0), (0.5, -0.012), (1.0, -0.027), (2.0, -0.06)]
+    tv = np.arange(n) % 7 == 0
+    keep = pkg.attach_schedules(p, [curve if t else None for t in tv],
+                                [[(0.4 * T, 1.0)] if t else None for t, T in zip(tv, p["maturity"])])
+    grid = pkg.grid_array(1, pkg.GRID_FIXED_N, 51, 60)
+    out = engine.price_arrays(p, grid)
+    b = engine.batch(p, grid)
+    b.run()
+    ref = b.results()
+    b.close()
+    assert (out["status"] == 0).all() and (ref["status"] == 0).all()
+    got = np.stack([out["value"], out["delta"], out["gamma"], out["theta"]], 1)
+    want = np.stack([ref["value"], ref["delta"], ref["gamma"], ref["theta"]], 1)
+    assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
+    assert (out["n_time"][tv] != 60).any()  # dividend points were added
+    del keep

@@ -344,19 +344,19 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
   b->runs = 0;
   for (auto& e : b->ev)
     if (!e) check(cudaEventCreate(&e), "cudaEventCreate");
-  // Sort accepted options by n_space descending (the largest tiles are
-  // dequeued first and a tile's lanes share their row count), then by
-  // option type (puts and calls lock at opposite ends of the grid, so a
-  // mixed tile would test the lock on every row), then by n_time
-  // descending and normalised moneyness ln(S/K) / (sigma sqrt(T)), so that
-  // a tile's lanes meet the obstacle at similar rows and leave the cached
-  // factorisation together (lanes on the off-cache path at different rows
-  // serialise a warp).
+  // Sort accepted options by n_space bucket descending (the largest tiles
+  // are dequeued first and a tile's lanes have nearly the same row count),
+  // then by option type (puts and calls lock at opposite ends of the grid,
+  // so a mixed tile would test the lock on every row), then by n_time and
+  // n_space descending and normalised moneyness ln(S/K) / (sigma sqrt(T)),
+  // so that a tile's lanes meet the obstacle at similar rows and leave the
+  // cached factorisation together (lanes on the off-cache path at different
+  // rows serialise a warp).
   std::vector<int32_t>& order = b->order;
   struct SortKey {
     int64_t n, nt;
     double mk;
-    int32_t tv, type, idx, pad;
+    int32_t tv, type, idx, nb;
   };
   std::vector<int32_t> valid;
   valid.reserve(static_cast<size_t>(n));
@@ -369,13 +369,19 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
     const Resolved& r = b->res[i];
     const MangoPricingParams& p = params[r.orig];
     const double k = std::log(p.spot / p.strike) / (p.volatility * std::sqrt(p.maturity));
-    keys[j] = SortKey{r.spec.n, r.nt, std::isfinite(k) ? k : 0.0, r.tv ? 1 : 0, p.option_type, i, 0};
+    // n_space in buckets 4 % wide: a tile then gathers options of nearly the
+    // same width, so the buckets hold enough options to keep the step
+    // counts of a tile close as well.
+    const int32_t nb = static_cast<int32_t>(std::floor(std::log(static_cast<double>(r.spec.n)) /
+                                                       std::log(1.04)));
+    keys[j] = SortKey{r.spec.n, r.nt, std::isfinite(k) ? k : 0.0, r.tv ? 1 : 0, p.option_type, i, nb};
   }, 4096);
   auto before = [](const SortKey& a, const SortKey& c) {
     if (a.tv != c.tv) return a.tv < c.tv;  // time-varying options last
-    if (a.n != c.n) return a.n > c.n;
+    if (a.nb != c.nb) return a.nb > c.nb;
     if (a.type != c.type) return a.type < c.type;
     if (a.nt != c.nt) return a.nt > c.nt;
+    if (a.n != c.n) return a.n > c.n;
     if (a.mk != c.mk) return a.mk < c.mk;
     return a.idx < c.idx;
   };

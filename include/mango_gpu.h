@@ -186,8 +186,8 @@ void mango_gpu_context_destroy(MangoGpuContext* ctx);
  * out: n slots.  *out_failed (nullable) = slots whose status != MANGO_OK.
  * Returns MANGO_OK unless the call itself could not run (bad pointers, CUDA
  * failure), in which case err says why and no slot is meaningful.
- * The call is synchronous.  Its device and pinned host buffers stay in the
- * context for the next call; batches of 65,536 options or more run as 2 to
+ * The call is synchronous.  Its device and pinned host buffers (up to 4 GB
+ * of device state per batch) stay in the context for the next call; batches of 65,536 options or more run as 2 to
  * 4 chunks (at least 32,768 options each) on two internal streams, ordered
  * after the context's stream, so that the host preparation of a chunk
  * overlaps the device work of the one before. */

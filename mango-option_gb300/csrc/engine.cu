@@ -866,6 +866,18 @@ MangoStatus mango_gpu_batch_timings(MangoGpuBatch* b, int32_t reset, double* pre
   }
 }
 
+namespace {
+// A kept batch whose device state exceeds this is freed after the call:
+// the reuse saves allocation time, not worth holding a huge batch's memory.
+constexpr size_t kKeepBytes = size_t(4) << 30;
+void release_if_large(MangoGpuBatch*& b) {
+  if (b && b->d_pool.cap > kKeepBytes) {
+    destroy_batch(b);
+    b = nullptr;
+  }
+}
+}  // namespace
+
 MangoStatus mango_gpu_price_american_batch(MangoGpuContext* ctx, const MangoPricingParams* params,
                                            uint64_t n, const MangoGpuGrid* grids,
                                            uint64_t grid_stride, const MangoGpuTrbdf2* trbdf2,
@@ -928,6 +940,7 @@ MangoStatus mango_gpu_price_american_batch(MangoGpuContext* ctx, const MangoPric
         run_batch(ctx->chunk[c % 2]);
       }
       for (int c = std::max(0, k - 2); c < k; ++c) collect(c);
+      for (auto& cb : ctx->chunk) release_if_large(cb);
       acc.total_ms = ms_since(t0);
       ctx->stats = acc;
       if (out_failed) *out_failed = failed;
@@ -944,6 +957,7 @@ MangoStatus mango_gpu_price_american_batch(MangoGpuContext* ctx, const MangoPric
     run_batch(b);
     std::string first;
     const uint64_t failed = fetch_batch(b, out, &first);
+    release_if_large(ctx->scratch);
     if (out_failed) *out_failed = failed;
     if (failed && err) set_err(err, MANGO_OK, first.empty() ? "solver failure" : first);
     ctx->stats.total_ms = ms_since(t0);

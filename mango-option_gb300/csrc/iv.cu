@@ -430,8 +430,8 @@ int32_t iv_query_status(const MangoIvQuery& q, std::string* msg) {
   };
   if (q.option_type != MANGO_PUT && q.option_type != MANGO_CALL)
     return bad(MANGO_ERR_VALIDATION, "invalid option type");
-  if (q.n_tenor_points != 0) return bad(MANGO_ERR_VALIDATION, "yield curves are not supported by the GPU engine");
-  if (q.n_dividends != 0) return bad(MANGO_ERR_VALIDATION, "discrete dividends are not supported by the GPU engine");
+  if (q.n_tenor_points != 0) return bad(MANGO_ERR_VALIDATION, "yield curves are not supported by the FDM IV entry point");
+  if (q.n_dividends != 0) return bad(MANGO_ERR_VALIDATION, "discrete dividends are not supported by the FDM IV entry point");
   if (!std::isfinite(q.dividend_yield)) return bad(MANGO_ERR_VALIDATION, "dividend_yield must be finite");
   if (!std::isfinite(q.rate_const)) return bad(MANGO_ERR_VALIDATION, "rate must be finite");
   if (!(q.spot > 0.0) || !std::isfinite(q.spot)) return bad(MANGO_ERR_VALIDATION, "invalid spot");

@@ -99,8 +99,8 @@ const char* validate_params(const MangoPricingParams& p) {
   if (p.dividend_yield < 0.0 || !std::isfinite(p.dividend_yield)) return "invalid dividend yield";
   if (!(p.volatility > 0.0) || !std::isfinite(p.volatility)) return "invalid volatility";
   if (p.option_type != MANGO_PUT && p.option_type != MANGO_CALL) return "invalid option type";
-  if (p.n_tenor_points != 0) return "yield curves are not supported by the GPU engine";
-  if (p.n_dividends != 0) return "discrete dividends are not supported by the GPU engine";
+  if (p.n_tenor_points != 0) return "yield curves are not supported by the no-allocation entry point";
+  if (p.n_dividends != 0) return "discrete dividends are not supported by the no-allocation entry point";
   return nullptr;
 }
 

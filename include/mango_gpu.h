@@ -16,14 +16,15 @@
  *
  * Rates and dividends: the American-pricing batch calls
  * (mango_gpu_price_american_batch, _batch_shared, mango_gpu_batch_create)
- * accept the reference's yield curves (tenor_points, validated as
- * YieldCurve::from_points does) and discrete dividends (validated as
- * validate_pricing_params does) and march those options on a kernel whose
- * stage matrices follow r(t), the mandatory dividend times and the dividend
- * shift.  The other entry points (implied volatility, Greeks, table sweep,
- * the no-allocation batch) take constant rates and continuous dividend
- * yields only and reject the rest per slot with MANGO_ERR_VALIDATION and a
- * message naming the unsupported feature.
+ * and the FDM implied-volatility calls accept the reference's yield curves
+ * (tenor_points, validated as YieldCurve::from_points does) and discrete
+ * dividends (validated as validate_pricing_params / validate_iv_query do)
+ * and march those options on a kernel whose stage matrices follow r(t), the
+ * mandatory dividend times and the dividend shift.  The other entry points
+ * (Greeks, table sweep, table queries, the no-allocation batch) take
+ * constant rates and continuous dividend yields only and reject the rest per
+ * slot with MANGO_ERR_VALIDATION and a message naming the unsupported
+ * feature.
  */
 #ifndef MANGO_GPU_H
 #define MANGO_GPU_H

@@ -77,6 +77,41 @@ void parallel_for(int64_t n, const std::function<void(int64_t)>& f, int64_t grai
   for (auto& x : th) x.join();
 }
 
+std::string schedule_error(const MangoTenorPoint* tenor_points, uint64_t n_tenor_points,
+                           const MangoDividend* dividends, uint64_t n_dividends, double maturity) {
+  if (n_tenor_points != 0) {
+    // build_rate + YieldCurve::from_points (src/ffi/mango_c_api.cpp:44-64,
+    // src/option/yield_curve.hpp): sorted by tenor, the first at t = 0 with
+    // log discount 0, tenors strictly increasing.  Non-finite entries are
+    // rejected too.
+    if (!tenor_points) return "tenor_points is null but n_tenor_points > 0";
+    std::vector<MangoTenorPoint> pts(tenor_points, tenor_points + n_tenor_points);
+    for (const auto& t : pts)
+      if (!std::isfinite(t.tenor) || !std::isfinite(t.log_discount))
+        return "invalid yield curve: non-finite tenor point";
+    std::sort(pts.begin(), pts.end(),
+              [](const MangoTenorPoint& a, const MangoTenorPoint& b) { return a.tenor < b.tenor; });
+    if (pts[0].tenor != 0.0) return "invalid yield curve: First point must have t=0";
+    if (std::abs(pts[0].log_discount) > 1e-10)
+      return "invalid yield curve: log_discount at t=0 must be 0";
+    for (size_t i = 1; i < pts.size(); ++i)
+      if (pts[i].tenor <= pts[i - 1].tenor + 1e-10)
+        return "invalid yield curve: Tenors must be strictly increasing";
+  }
+  if (n_dividends != 0) {
+    // build_dividends + validate_pricing_params / validate_iv_query
+    // (src/option/option_spec.cpp:89-110, 131-153)
+    if (!dividends) return "dividends is null but n_dividends > 0";
+    for (uint64_t i = 0; i < n_dividends; ++i) {
+      const MangoDividend& d = dividends[i];
+      if (d.calendar_time < 0.0 || d.calendar_time > maturity) return "invalid dividend time";
+      if (d.amount < 0.0) return "invalid dividend amount";
+      if (!std::isfinite(d.calendar_time) || !std::isfinite(d.amount)) return "invalid dividend";
+    }
+  }
+  return {};
+}
+
 std::string validate(const MangoPricingParams& p, bool allow_tv) {
   // validate_pricing_params (src/option/option_spec.cpp:8-40, 117-157)
   if (!(p.spot > 0.0) || !std::isfinite(p.spot)) return "invalid spot";
@@ -91,35 +126,7 @@ std::string validate(const MangoPricingParams& p, bool allow_tv) {
     if (p.n_dividends != 0) return "discrete dividends are not supported by this entry point";
     return {};
   }
-  if (p.n_tenor_points != 0) {
-    // build_rate + YieldCurve::from_points (src/ffi/mango_c_api.cpp:44-64,
-    // src/option/yield_curve.hpp): sorted by tenor, the first at t = 0 with
-    // log discount 0, tenors strictly increasing.  Non-finite entries are
-    // rejected too.
-    if (!p.tenor_points) return "tenor_points is null but n_tenor_points > 0";
-    std::vector<MangoTenorPoint> pts(p.tenor_points, p.tenor_points + p.n_tenor_points);
-    for (const auto& t : pts)
-      if (!std::isfinite(t.tenor) || !std::isfinite(t.log_discount))
-        return "invalid yield curve: non-finite tenor point";
-    std::sort(pts.begin(), pts.end(),
-              [](const MangoTenorPoint& a, const MangoTenorPoint& b) { return a.tenor < b.tenor; });
-    if (pts[0].tenor != 0.0) return "invalid yield curve: First point must have t=0";
-    if (std::abs(pts[0].log_discount) > 1e-10)
-      return "invalid yield curve: log_discount at t=0 must be 0";
-    for (size_t i = 1; i < pts.size(); ++i)
-      if (pts[i].tenor <= pts[i - 1].tenor + 1e-10)
-        return "invalid yield curve: Tenors must be strictly increasing";
-  }
-  if (p.n_dividends != 0) {
-    if (!p.dividends) return "dividends is null but n_dividends > 0";
-    for (uint64_t i = 0; i < p.n_dividends; ++i) {
-      const MangoDividend& d = p.dividends[i];
-      if (d.calendar_time < 0.0 || d.calendar_time > p.maturity) return "invalid dividend time";
-      if (d.amount < 0.0) return "invalid dividend amount";
-      if (!std::isfinite(d.calendar_time) || !std::isfinite(d.amount)) return "invalid dividend";
-    }
-  }
-  return {};
+  return schedule_error(p.tenor_points, p.n_tenor_points, p.dividends, p.n_dividends, p.maturity);
 }
 
 bool time_varying(const MangoPricingParams& p) {

@@ -62,6 +62,11 @@ struct Stats {
 
 // Validation (validate_pricing_params plus the engine's scope) and grid
 // resolution; empty string when the option is accepted.
+// Yield-curve and dividend checks (YieldCurve::from_points, build_rate,
+// build_dividends, the dividend rules of validate_pricing_params); empty
+// when accepted.
+std::string schedule_error(const MangoTenorPoint* tenor_points, uint64_t n_tenor_points,
+                           const MangoDividend* dividends, uint64_t n_dividends, double maturity);
 // allow_tv: accept yield curves and discrete dividends (the pricing batch
 // entry points); otherwise they are rejected with a message.
 std::string validate(const MangoPricingParams& p, bool allow_tv = false);

@@ -414,6 +414,16 @@ __global__ void iv_gather_kernel(int mw, const int32_t* __restrict__ map,
   active_w[k] = 1;
 }
 
+// Schedule data of the working set's time-varying slots: slot j takes the
+// per-option data of its quote (batch sorted index map[j], whose data sit
+// at map[j] - tv_first_b); time points, curves and events stay in the
+// batch's arrays.
+__global__ void iv_gather_tv_kernel(int n, const int32_t* __restrict__ map, int tv_first_b,
+                                    const TvDev* __restrict__ src, TvDev* __restrict__ dst) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) dst[j] = src[map[j] - tv_first_b];
+}
+
 // Status of an IV query before any solve, as the reference C ABI reports
 // it: build_iv_query (src/ffi/mango_c_api.cpp:168-203) rejects a bad option
 // type and non-finite rate or dividend yield with MANGO_ERR_VALIDATION; then
@@ -430,10 +440,19 @@ int32_t iv_query_status(const MangoIvQuery& q, std::string* msg) {
   };
   if (q.option_type != MANGO_PUT && q.option_type != MANGO_CALL)
     return bad(MANGO_ERR_VALIDATION, "invalid option type");
-  if (q.n_tenor_points != 0) return bad(MANGO_ERR_VALIDATION, "yield curves are not supported by the FDM IV entry point");
-  if (q.n_dividends != 0) return bad(MANGO_ERR_VALIDATION, "discrete dividends are not supported by the FDM IV entry point");
+  {
+    // build_rate / build_dividends, and the dividend rules of
+    // validate_iv_query (src/option/option_spec.cpp:89-110)
+    const std::string m = schedule_error(q.tenor_points, q.n_tenor_points, q.dividends, q.n_dividends,
+                                         q.maturity);
+    if (!m.empty()) {
+      *msg = m;
+      return MANGO_ERR_VALIDATION;
+    }
+  }
   if (!std::isfinite(q.dividend_yield)) return bad(MANGO_ERR_VALIDATION, "dividend_yield must be finite");
-  if (!std::isfinite(q.rate_const)) return bad(MANGO_ERR_VALIDATION, "rate must be finite");
+  if (q.n_tenor_points == 0 && !std::isfinite(q.rate_const))
+    return bad(MANGO_ERR_VALIDATION, "rate must be finite");
   if (!(q.spot > 0.0) || !std::isfinite(q.spot)) return bad(MANGO_ERR_VALIDATION, "invalid spot");
   if (!(q.strike > 0.0) || !std::isfinite(q.strike)) return bad(MANGO_ERR_VALIDATION, "invalid strike");
   if (!(q.maturity > 0.0) || !std::isfinite(q.maturity))
@@ -468,11 +487,14 @@ struct WorkSet {
   std::vector<int32_t> map_h, pt_h, qlist_h, qbase_h;
   std::vector<TileDev> tiles_h;
   DevBuf d_tiles, d_opts, d_xs, d_map, d_pt, d_qlist, d_qbase, d_sigma, d_active, d_pool, d_flags,
-      d_mode, d_status, d_out4;
+      d_mode, d_status, d_out4, d_tv;
+  // First slot of a time-varying quote (slots follow the batch order, where
+  // those quotes come last), or INT32_MAX.
+  int32_t tv_first = 0x7fffffff;
 
   ~WorkSet() {
     for (DevBuf* d : {&d_tiles, &d_opts, &d_xs, &d_map, &d_pt, &d_qlist, &d_qbase, &d_sigma,
-                      &d_active, &d_pool, &d_flags, &d_mode, &d_status, &d_out4})
+                      &d_active, &d_pool, &d_flags, &d_mode, &d_status, &d_out4, &d_tv})
       d->release();
   }
 
@@ -549,6 +571,19 @@ struct WorkSet {
         b->d_opts.as<OptDev>(), b->d_xs.as<double>(), d_tiles.as<TileDev>(), d_opts.as<OptDev>(),
         d_xs.as<double>(), next_sig, d_sigma.as<double>(), d_active.as<int32_t>());
     check(cudaGetLastError(), "iv_gather launch");
+    tv_first = 0x7fffffff;
+    for (int64_t k = 0; k < mw; ++k)
+      if (map_h[k] >= b->mc.tv_first) {
+        tv_first = static_cast<int32_t>(k);
+        break;
+      }
+    if (tv_first < mw) {
+      const int64_t ntv = mw - tv_first;
+      iv_gather_tv_kernel<<<static_cast<int>((ntv + 255) / 256), 256, 0, st>>>(
+          static_cast<int>(ntv), d_map.as<int32_t>() + tv_first, b->mc.tv_first,
+          b->d_tv.as<TvDev>(), static_cast<TvDev*>(d_tv.get(sizeof(TvDev) * ntv)));
+      check(cudaGetLastError(), "iv_gather_tv launch");
+    }
   }
 };
 
@@ -597,6 +632,10 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
       p.maturity = q.maturity;
       p.dividend_yield = q.dividend_yield;
       p.rate_const = q.rate_const;
+      p.tenor_points = q.tenor_points;
+      p.n_tenor_points = q.n_tenor_points;
+      p.dividends = q.dividends;
+      p.n_dividends = q.n_dividends;
       p.option_type = q.option_type;
       p.volatility = 0.2;  // placeholder; every evaluation overrides it
       vstatus[i] = iv_query_status(q, &vmsg[i]);
@@ -704,6 +743,7 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
         mc.value_only = 1;
         mc.sigma = w.d_sigma.as<double>();
         mc.active = w.d_active.as<int32_t>();
+        mc.tv_first = w.tv_first;
         const int ntiles = w.ntiles, threads = ntiles * kTile;
         const int blocks =
             std::max(1, std::min<int>(ctx->num_sms * ctx->march_blocks_per_sm, (ntiles + 3) / 4));
@@ -719,6 +759,15 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
         march_kernel<<<blocks, 128, 0, st>>>(tiles, ntiles, wopts, w.d_pool.as<double>(),
                                              w.d_flags.as<uint8_t>(), w.d_mode.as<int32_t>(),
                                              w.d_status.as<int32_t>(), b->d_queue.as<int>(), mc);
+        if (w.tv_first < w.mw) {
+          const int t0 = w.tv_first / kTile;
+          const int tvb = std::max(1, std::min<int>(ctx->num_sms * 8, (ntiles - t0 + 3) / 4));
+          march_tv_kernel<<<tvb, 128, 0, st>>>(tiles, t0, ntiles, wopts, w.d_tv.as<TvDev>(),
+                                               b->d_tv_tp.as<double>(), b->d_tv_curve.as<double>(),
+                                               b->d_tv_ev.as<double>(), xs, w.d_pool.as<double>(),
+                                               w.d_mode.as<int32_t>(), w.d_status.as<int32_t>(), mc);
+          ++launches;
+        }
         outputs_kernel<<<(threads + 127) / 128, 128, 0, st>>>(
             tiles, ntiles, wopts, xs, w.d_pool.as<double>(), w.d_mode.as<int32_t>(),
             w.d_status.as<int32_t>(), mc, w.d_out4.as<double>());

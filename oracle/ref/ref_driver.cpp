@@ -627,4 +627,67 @@ uint64_t ref_crc64_update(uint64_t crc, const uint8_t* data, uint64_t n) {
   return CRC64::update(crc, data, static_cast<size_t>(n));
 }
 
+
+// IVSolver::solve for quotes with yield curves and/or discrete dividends
+// (schedules as in ref_price_tv).  The grid: estimate_pde_grid of the quote
+// at grid_sigma with min == max == nx (dividends included, so the lower
+// bound is widened as for the option), as PDEGridConfig{spec, nt}; the
+// solver adds the dividend times (iv_solver.cpp:82-96).
+int32_t ref_iv_batch_tv(int64_t n, const double* S, const double* K, const double* T,
+                        const double* r, const double* q, const int32_t* is_put,
+                        const double* price, const double* grid_sigma, const int64_t* nx,
+                        const int64_t* nt, const int64_t* curve_off, const int64_t* curve_n,
+                        const double* curve_t, const double* curve_ld, const int64_t* div_off,
+                        const int64_t* div_n, const double* div_t, const double* div_amt,
+                        int32_t n_threads, double* out3, int32_t* status) {
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t i = 0; i < n; ++i) {
+    IVQuery query;
+    query.spot = S[i];
+    query.strike = K[i];
+    query.maturity = T[i];
+    query.rate = r[i];
+    query.dividend_yield = q[i];
+    query.option_type = is_put[i] ? OptionType::PUT : OptionType::CALL;
+    query.market_price = price[i];
+    auto p = make_params(S[i], K[i], T[i], grid_sigma[i], r[i], q[i], is_put[i]);
+    if (curve_n[i] > 0) {
+      std::vector<TenorPoint> pts;
+      for (int64_t j = 0; j < curve_n[i]; ++j)
+        pts.push_back(TenorPoint{curve_t[curve_off[i] + j], curve_ld[curve_off[i] + j]});
+      auto c = YieldCurve::from_points(std::move(pts));
+      if (!c) { status[i] = 1; continue; }
+      query.rate = *c;
+      p.rate = *c;
+    }
+    for (int64_t j = 0; j < div_n[i]; ++j) {
+      const Dividend d{div_t[div_off[i] + j], div_amt[div_off[i] + j]};
+      query.discrete_dividends.push_back(d);
+      p.discrete_dividends.push_back(d);
+    }
+    GridAccuracyParams acc;
+    acc.min_spatial_points = static_cast<size_t>(nx[i]);
+    acc.max_spatial_points = static_cast<size_t>(nx[i]);
+    auto [spec, td] = estimate_pde_grid(p, acc);
+    (void)td;
+    IVSolverConfig cfg;
+    cfg.grid = PDEGridConfig{spec, static_cast<size_t>(nt[i]), {}};
+    IVSolver solver(cfg);
+    auto res = solver.solve(query);
+    if (!res) {
+      status[i] = 10 + static_cast<int32_t>(res.error().code);
+      out3[3 * i + 0] = NAN;
+      out3[3 * i + 1] = static_cast<double>(res.error().iterations);
+      out3[3 * i + 2] = res.error().final_error;
+      continue;
+    }
+    status[i] = 0;
+    out3[3 * i + 0] = res->implied_vol;
+    out3[3 * i + 1] = static_cast<double>(res->iterations);
+    out3[3 * i + 2] = res->final_error;
+  }
+  return 0;
+}
+
 }  // extern "C"

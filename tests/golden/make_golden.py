@@ -246,6 +246,7 @@ def main():
     golden_shared(lib)
     golden_tv(lib)
     golden_shared_tv(lib)
+    golden_iv_tv(lib)
 
 
 def table_axes(nm, ntau, ns, nr):
@@ -630,6 +631,42 @@ def golden_shared_tv(lib):
         kw[f"{name}_dims"] = dims
         kw[f"{name}_grid"] = np.array(grid, dtype=np.float64)
     save("shared_tv.npz", **kw)
+
+
+def golden_iv_tv(lib):
+    """IVSolver::solve with yield curves and dividends: market prices from
+    the reference's own solver at the true volatility, implied vols on a
+    grid sized at 0.3 (PDEGridConfig, dividend times added by the solver)."""
+    rows = tv_rows(71, 96, [1])
+    rng = np.random.default_rng(72)
+    for r in rows:
+        r["nx"], r["nt"] = 101, 200
+        r["sigma"] = float(rng.uniform(0.12, 0.6))
+    out, dims, st = tv_batch(lib, rows, 1)
+    assert (st == 0).all()
+    price = np.ascontiguousarray(out[:, 0])
+    n = len(rows)
+    col = lambda k: np.ascontiguousarray([r.get(k, 0.0) for r in rows], dtype=np.float64)
+    curves = [np.asarray(r.get("curve") or np.zeros((0, 2)), np.float64).reshape(-1, 2) for r in rows]
+    divs = [np.asarray(r.get("divs") or np.zeros((0, 2)), np.float64).reshape(-1, 2) for r in rows]
+    def flat(blocks):
+        cnt = np.array([b.shape[0] for b in blocks], np.int64)
+        off = np.concatenate([[0], np.cumsum(cnt)[:-1]]).astype(np.int64)
+        allp = np.concatenate(blocks + [np.zeros((1, 2))])
+        return off, cnt, np.ascontiguousarray(allp[:, 0]), np.ascontiguousarray(allp[:, 1])
+    co, cn, ct, cl = flat(curves)
+    do, dn, dt, da = flat(divs)
+    put = np.ascontiguousarray([r["put"] for r in rows], dtype=np.int32)
+    gsig = np.full(n, 0.3)
+    nx = np.full(n, 101, np.int64)
+    nt = np.full(n, 200, np.int64)
+    o3 = np.full(3 * n, np.nan)
+    ist = np.zeros(n, np.int32)
+    lib.ref_iv_batch_tv(ctypes.c_int64(n), P(col("S")), P(col("K")), P(col("T")), P(col("r")), P(col("q")), P(put),
+                        P(price), P(gsig), P(nx), P(nt), P(co), P(cn), P(ct), P(cl), P(do), P(dn), P(dt), P(da),
+                        ctypes.c_int32(8), P(o3), P(ist))
+    save("iv_tv.npz", rows=np.array([json.dumps(r) for r in rows]), price=price, grid_sigma=gsig, nx=nx, nt=nt,
+         out=o3.reshape(n, 3), status=ist)
 
 
 if __name__ == "__main__":

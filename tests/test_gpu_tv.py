@@ -147,3 +147,35 @@ def test_tv_in_chunked_batch(engine, pkg):
     assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
     assert (out["n_time"][tv] != 60).any()  # dividend points were added
     del keep
+
+
+@pytest.mark.parametrize("method", ["brent", "secant"])
+def test_iv_with_schedules_vs_reference(engine, pkg, method):
+    """FDM implied volatility for quotes with yield curves and dividends
+    against the reference's IVSolver::solve (tests/golden/iv_tv.npz): grid
+    sized at 0.3 (PDEGridConfig), dividend times as mandatory points.  Brent
+    replays the reference's iterates: roots within 1e-8 and the same
+    iteration count (the time-varying march agrees with the reference to
+    ~1e-12, so a count may differ on a quote whose last step lands within
+    rounding of the tolerance: at most 2 of 96 allowed).  The secant method
+    stops elsewhere inside the same price tolerance, so its roots agree
+    within 1e-6 in volatility."""
+    g = golden("iv_tv.npz")
+    rows = [json.loads(str(s)) for s in g["rows"]]
+    n = len(rows)
+    q = pkg.query_array([r["S"] for r in rows], [r["K"] for r in rows], [r["T"] for r in rows],
+                        [r["r"] for r in rows], [r["q"] for r in rows], [r["put"] for r in rows], g["price"])
+    keep = pkg.attach_schedules(q, [r.get("curve") for r in rows], [r.get("divs") for r in rows])
+    grids = pkg.grid_array(n, pkg.GRID_FIXED_N_AT_VOL, 101, 200, alpha=g["grid_sigma"])
+    out = engine.solve_iv_arrays(q, grids, method=pkg.IV_BRENT if method == "brent" else pkg.IV_SECANT)
+    ok = g["status"] == 0
+    assert (out["status"][ok] == 0).all(), np.nonzero(out["status"][ok])[0][:8]
+    err = np.abs(out["implied_vol"][ok] - g["out"][ok, 0])
+    if method == "brent":
+        assert err.max() < 1e-8, err.max()
+        assert np.count_nonzero(out["iterations"][ok] != g["out"][ok, 1]) <= 2
+    else:
+        # another root finder stopping anywhere |V - P| < 1e-6: the roots
+        # agree to that price tolerance over vega (1e-6 in volatility here)
+        assert err.max() < 1e-6, err.max()
+    del keep

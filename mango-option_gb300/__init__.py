@@ -1150,14 +1150,16 @@ class BatchAmericanOptionSolver:
 
 @dataclasses.dataclass
 class IVQuery:
-    """Reference IVQuery (src/option/option_spec.hpp:208-228), constant rate."""
+    """Reference IVQuery (src/option/option_spec.hpp:208-228): rate is a
+    constant or a YieldCurve; discrete_dividends a list of Dividend."""
     spot: float = 0.0
     strike: float = 0.0
     maturity: float = 0.0
-    rate: float = 0.0
+    rate: object = 0.0
     dividend_yield: float = 0.0
     option_type: OptionType = OptionType.CALL
     market_price: float = 0.0
+    discrete_dividends: list = dataclasses.field(default_factory=list)
 
 
 @dataclasses.dataclass
@@ -1214,12 +1216,18 @@ class IVSolver:
 
     def solve_batch(self, queries) -> BatchIVResult:
         qs = list(queries)
+        curves = [q.rate if isinstance(q.rate, YieldCurve) else None for q in qs]
+        divs = [q.discrete_dividends or None for q in qs]
         arr = query_array([q.spot for q in qs], [q.strike for q in qs], [q.maturity for q in qs],
-                          [q.rate for q in qs], [q.dividend_yield for q in qs],
+                          [0.0 if c is not None else q.rate for c, q in zip(curves, qs)],
+                          [q.dividend_yield for q in qs],
                           [int(q.option_type == OptionType.PUT) for q in qs], [q.market_price for q in qs])
+        keep = attach_schedules(arr, curves if any(c is not None for c in curves) else None,
+                                divs if any(divs) else None)
         eng = self._engine or default_engine()
         out = eng.solve_iv_arrays(arr, self._grid(), self.config.brent_tol_abs, self.config.max_iter,
                                   self.config.method)
+        del keep
         res = []
         for row in out:
             if row["status"] == MANGO_OK:

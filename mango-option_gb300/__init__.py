@@ -875,6 +875,8 @@ class InterpolatedIVSolver:
 
     def solve_batch(self, queries) -> "BatchIVResult":
         qs = list(queries)
+        if any(isinstance(q.rate, YieldCurve) or getattr(q, "discrete_dividends", None) for q in qs):
+            raise ValueError("the interpolated IV solver takes constant rates and continuous dividend yields")
         arr = query_array([q.spot for q in qs], [q.strike for q in qs], [q.maturity for q in qs],
                           [q.rate for q in qs], [q.dividend_yield for q in qs],
                           [int(q.option_type == OptionType.PUT) for q in qs], [q.market_price for q in qs])

@@ -20,8 +20,9 @@
  * (tenor_points, validated as YieldCurve::from_points does) and discrete
  * dividends (validated as validate_pricing_params / validate_iv_query do)
  * and march those options on a kernel whose stage matrices follow r(t), the
- * mandatory dividend times and the dividend shift.  The other entry points
- * (Greeks, table sweep, table queries, the no-allocation batch) take
+ * mandatory dividend times and the dividend shift; so do the frozen-grid
+ * Greeks.  The other entry points (table sweep, table queries, the
+ * no-allocation batch) take
  * constant rates and continuous dividend yields only and reject the rest per
  * slot with MANGO_ERR_VALIDATION and a message naming the unsupported
  * feature.
@@ -451,8 +452,10 @@ MangoStatus mango_gpu_price_table_iv_batch_device(MangoGpuPriceTable* table,
  * priced on the unbumped option's grid (the grid of the reference's
  * estimate_pde_grid moves with volatility and strike, so derivatives through
  * it are discontinuous; this is the reference's bump-and-reprice definition
- * of these Greeks).  One device batch of 9 x n options.  No counterpart in
- * the reference ABI. */
+ * of these Greeks).  One device batch of 9 x n options.  Options with yield
+ * curves and discrete dividends are accepted; for a yield curve dV/drate is
+ * the derivative along a parallel shift of the zero rates (every log
+ * discount ln D(t) moves by -h t).  No counterpart in the reference ABI. */
 typedef struct {
   MangoGpuAmericanOut base;
   double vega;

@@ -7,7 +7,10 @@
 // once (resolve_grid, src/option/american_option.cpp:54-73) and the eight
 // bumped copies are priced on exactly that grid (the log-moneyness grid is
 // independent of the strike, so a strike bump only moves x = ln(S/K)), all in
-// one device batch.
+// one device batch.  Options with a yield curve or discrete dividends take
+// the time-varying march like their unbumped price; for a yield curve the
+// rate bump is a parallel shift of the continuously compounded zero rates
+// (every log discount ln D(t) moves by -h t).
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -38,7 +41,7 @@ extern "C" MangoStatus mango_gpu_price_american_greeks_batch(
     parallel_for(nn, [&](int64_t i) {
       thread_local std::vector<double> scratch;
       base[i].orig = static_cast<int32_t>(i);
-      std::string m = validate(params[i]);
+      std::string m = validate(params[i], true);
       if (m.empty()) {
         MangoGpuGrid g{};
         g.kind = MANGO_GPU_GRID_AUTO;
@@ -55,6 +58,8 @@ extern "C" MangoStatus mango_gpu_price_american_greeks_batch(
     std::vector<MangoPricingParams> pp(static_cast<size_t>(kCopies * nn));
     std::vector<Resolved> res(static_cast<size_t>(kCopies * nn));
     std::vector<double> step(static_cast<size_t>(4 * nn), 0.0);
+    // Shifted curves of the rate bumps, alive until the batch is packed.
+    std::vector<std::vector<MangoTenorPoint>> shifted(static_cast<size_t>(2 * nn));
     for (int64_t i = 0; i < nn; ++i) {
       const MangoPricingParams& p = params[i];
       const double hv = h * p.volatility;
@@ -70,7 +75,16 @@ extern "C" MangoStatus mango_gpu_price_american_greeks_batch(
         const double sgn = (c % 2 == 1) ? 1.0 : -1.0;
         switch ((c + 1) / 2) {
           case 1: q.volatility += sgn * hv; break;
-          case 2: q.rate_const += sgn * hr; break;
+          case 2:
+            if (q.n_tenor_points != 0 && base[i].status == 0) {
+              std::vector<MangoTenorPoint>& v = shifted[static_cast<size_t>((c - 3) * nn + i)];
+              v.assign(q.tenor_points, q.tenor_points + q.n_tenor_points);
+              for (auto& t : v) t.log_discount -= sgn * hr * t.tenor;
+              q.tenor_points = v.data();
+            } else {
+              q.rate_const += sgn * hr;
+            }
+            break;
           case 3: q.dividend_yield = std::max(0.0, q.dividend_yield + sgn * hq); break;
           case 4: q.strike += sgn * hk; break;
           default: break;

@@ -179,3 +179,41 @@ def test_iv_with_schedules_vs_reference(engine, pkg, method):
         # agree to that price tolerance over vega (1e-6 in volatility here)
         assert err.max() < 1e-6, err.max()
     del keep
+
+
+def test_greeks_with_schedules(engine, pkg):
+    """Frozen-grid sensitivities of options with a yield curve and
+    dividends equal central differences of the pricing path on the same
+    explicit grid: vega and dV/dK by bumped inputs, rho by a parallel shift
+    of the zero curve (ln D(t) - h t)."""
+    curve = np.array([(0.0, 0.0), (0.5, -0.012), (1.0, -0.027), (2.0, -0.06)])
+    n = 8
+    K = np.linspace(90, 110, n)
+    T = np.linspace(0.4, 1.6, n)
+    sig = np.full(n, 0.25)
+    put = (np.arange(n) % 2 == 0)
+    divs = [[(0.5 * t, 1.5)] for t in T]
+    grid = pkg.grid_array(1, pkg.GRID_SINH, 141, 300, -2.5, 2.5, 2.0)
+
+    def price(K_, sig_, curves):
+        p = pkg.pricing_array(100.0, K_, T, sig_, 0.0, 0.0, put)
+        keep = pkg.attach_schedules(p, curves, divs)
+        v = engine.price_arrays(p, grid)["value"]
+        del keep
+        return v
+
+    p = pkg.pricing_array(100.0, K, T, sig, 0.0, 0.0, put)
+    keep = pkg.attach_schedules(p, [curve] * n, divs)
+    g = engine.greeks_arrays(p, grid)
+    assert (g["status"] == 0).all()
+    h = 1e-5
+    hv, hr, hk = h * sig, h * 1e-2, h * K
+    vega = (price(K, sig + hv, [curve] * n) - price(K, sig - hv, [curve] * n)) / (2 * hv)
+    up = [np.column_stack([curve[:, 0], curve[:, 1] - hr * curve[:, 0]])] * n
+    dn = [np.column_stack([curve[:, 0], curve[:, 1] + hr * curve[:, 0]])] * n
+    rho = (price(K, sig, up) - price(K, sig, dn)) / (2 * hr)
+    dk = (price(K + hk, sig, [curve] * n) - price(K - hk, sig, [curve] * n)) / (2 * hk)
+    for got, want in ((g["vega"], vega), (g["rho"], rho), (g["dstrike"], dk)):
+        assert np.abs(got - want).max() <= 1e-9 * np.abs(want).max() + 1e-12
+    assert (g["rho"][put] < 0).all() and (g["rho"][~put] > 0).all()
+    del keep

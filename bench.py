@@ -243,7 +243,8 @@ def bench_iv(pkg, eng, n):
 
 
 def bench_greeks(pkg, eng, n=16384):
-    """Sensitivity workload: 16,384 American puts (config-0 distributions,
+    """Sensitivity workload: 16,384 American puts (spot 100, strike, maturity,
+    volatility, rate and dividend yield drawn as in the pricing workload,
     101 x 498 grid rule), value/delta/gamma/theta plus frozen-grid vega, rho,
     dividend rho and dV/dK (8 bumped copies each, one device batch)."""
     rng = np.random.default_rng(3)
@@ -261,7 +262,8 @@ def bench_greeks(pkg, eng, n=16384):
 
 
 def bench_schedules(pkg, eng, torch, stream, n, fp64_peak):
-    """Time-varying march: n puts and calls (config-0 distributions) on the
+    """Time-varying march: n puts and calls (the pricing workload's
+    distributions) on the
     101 x 498 grid rule with a 7-point yield curve, then with the curve plus
     two cash dividends per option (mandatory time points, two spline
     shifts).  Resident batches, device time of two runs."""

@@ -329,6 +329,33 @@ def bench_schedules(pkg, eng, torch, stream, n, fp64_peak):
     return out
 
 
+def bench_chain(pkg, eng, n):
+    """Shared-grid batch on the normalized-chain route: n American puts as
+    n/64 parameter groups (volatility, rate, yield, maturity) of 64 strikes
+    each, one S = K = 1 march per group, every strike read from it
+    (BatchAmericanOptionSolver::solve_batch with use_shared_grid)."""
+    rng = np.random.default_rng(9)
+    groups = max(1, n // 64)
+    per = n // groups
+    g_sig = rng.uniform(0.15, 0.45, groups)
+    g_r = rng.uniform(0.0, 0.06, groups)
+    g_q = rng.uniform(0.0, 0.03, groups)
+    g_T = rng.uniform(0.25, 1.5, groups)
+    # is_normalized_eligible tests the first option's grid (spacing <= 0.05)
+    g_sig[0], g_T[0] = 0.2, 1.0
+    K = np.tile(np.linspace(88.0, 112.0, per), groups)
+    rep = lambda a: np.repeat(a, per)
+    p = pkg.pricing_array(100.0, K, rep(g_T), rep(g_sig), rep(g_r), rep(g_q), 1)
+    eng.price_shared_arrays(p)
+    t0 = time.perf_counter()
+    out, route = eng.price_shared_arrays(p)
+    t = time.perf_counter() - t0
+    return {"workload": f"{p.size} American puts, {groups} groups of {per} strikes, estimated shared grid",
+            "value": p.size / t, "unit": "options/s (end to end through mango_gpu_price_american_batch_shared)",
+            "route": "normalized chain" if route == 1 else "regular shared grid",
+            "failed": int(np.count_nonzero(out["status"]))}
+
+
 TABLE_AXES = (np.linspace(np.log(0.7), np.log(1.3), 50), np.linspace(0.02, 2.0, 30),
               np.linspace(0.05, 0.8, 20), np.linspace(0.0, 0.08, 10))
 
@@ -613,6 +640,8 @@ def main():
 
     if not args.no_extra and not args.no_schedules and rank == 0:
         extra["schedules"] = bench_schedules(pkg, eng, torch, stream, n, fp64_peak)
+    if not args.no_extra and rank == 0:
+        extra["shared_chain"] = bench_chain(pkg, eng, n)
     if not args.no_iv and rank == 0:
         extra["iv_brent"] = bench_iv(pkg, eng, args.iv_quotes)
     if not args.no_iv and rank == 0:

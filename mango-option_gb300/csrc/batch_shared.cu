@@ -27,6 +27,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "engine.hpp"
@@ -221,22 +222,37 @@ extern "C" MangoStatus mango_gpu_price_american_batch_shared(
       };
       std::vector<Group> groups;
       std::vector<int32_t> gof(static_cast<size_t>(nn), -1);
+      // The first matching group, found without scanning every group: a
+      // group can only match if its volatility lies within 1e-10 of the
+      // option's, so groups are indexed by volatility in buckets 1e-10 wide
+      // and only the option's bucket and its neighbours (two either side, for
+      // the rounding of the bucket index) are tested; the smallest matching
+      // group index is the first match in creation order.
+      std::unordered_map<int64_t, std::vector<int32_t>> by_sigma;
+      auto bucket = [](double v) { return static_cast<int64_t>(std::floor(v / 1e-10)); };
       for (int64_t i = 0; i < nn; ++i) {
         if (!valid[i]) continue;
         const MangoPricingParams& p = params[i];
         int32_t found = -1;
-        for (size_t g = 0; g < groups.size(); ++g) {
-          const Group& G = groups[g];
-          if (std::fabs(G.sigma - p.volatility) < 1e-10 && same_rate(*G.rep, p) &&
-              std::fabs(G.q - p.dividend_yield) < 1e-10 && std::fabs(G.T - p.maturity) < 1e-10 &&
-              G.type == p.option_type) {
-            found = static_cast<int32_t>(g);
-            break;
+        const int64_t bk = bucket(p.volatility);
+        for (int64_t nb = bk - 2; nb <= bk + 2; ++nb) {
+          const auto it = by_sigma.find(nb);
+          if (it == by_sigma.end()) continue;
+          for (const int32_t g : it->second) {
+            if (found >= 0 && g >= found) break;  // lists are in creation order
+            const Group& G = groups[static_cast<size_t>(g)];
+            if (std::fabs(G.sigma - p.volatility) < 1e-10 && same_rate(*G.rep, p) &&
+                std::fabs(G.q - p.dividend_yield) < 1e-10 && std::fabs(G.T - p.maturity) < 1e-10 &&
+                G.type == p.option_type) {
+              found = g;
+              break;
+            }
           }
         }
         if (found < 0) {
           found = static_cast<int32_t>(groups.size());
           groups.push_back({p.volatility, p.dividend_yield, p.maturity, p.option_type, &p});
+          by_sigma[bk].push_back(found);
         }
         gof[i] = found;
       }

@@ -481,6 +481,15 @@ MangoStatus mango_gpu_batch_create(MangoGpuContext* ctx, const MangoPricingParam
                                    const MangoGpuTrbdf2* trbdf2, MangoGpuBatch** out,
                                    MangoError* err);
 MangoStatus mango_gpu_batch_run(MangoGpuBatch* batch, MangoError* err);
+/* AmericanOptionResult::value_at and the functionals at another spot, the
+ * batch counterpart of mango_american_value_at (src/ffi/mango_c_api.h:
+ * 148-149; american_option_result.cpp:29-45): for each j, the option in
+ * slot slots[j] of a batch that has run, read at spots[j] with its own
+ * strike: out4[4j..4j+3] = value, delta, gamma, theta (NaN for a slot that
+ * failed or never ran).  Waits for the batch's work. */
+MangoStatus mango_gpu_batch_value_at(MangoGpuBatch* batch, const uint64_t* slots,
+                                     const double* spots, uint64_t n, double* out4,
+                                     MangoError* err);
 MangoStatus mango_gpu_batch_results(MangoGpuBatch* batch, MangoGpuAmericanOut* out,
                                     uint64_t* out_failed, MangoError* err);
 void mango_gpu_batch_destroy(MangoGpuBatch* batch);

@@ -137,6 +137,8 @@ def library() -> ctypes.CDLL:
         lib.mango_gpu_batch_create.restype = ctypes.c_int32
         lib.mango_gpu_batch_run.argtypes = [_P, ctypes.POINTER(MangoError)]
         lib.mango_gpu_batch_run.restype = ctypes.c_int32
+        lib.mango_gpu_batch_value_at.argtypes = [_P, _P, _P, ctypes.c_uint64, _P, ctypes.POINTER(MangoError)]
+        lib.mango_gpu_batch_value_at.restype = ctypes.c_int32
         lib.mango_gpu_batch_results.argtypes = [_P, _P, ctypes.POINTER(ctypes.c_uint64),
                                                 ctypes.POINTER(MangoError)]
         lib.mango_gpu_batch_results.restype = ctypes.c_int32
@@ -980,6 +982,19 @@ class ResidentBatch:
         failed = ctypes.c_uint64()
         err = MangoError()
         if library().mango_gpu_batch_results(self._b, _ptr(out), ctypes.byref(failed), ctypes.byref(err)) != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+        return out
+
+    def value_at(self, slots, spots) -> np.ndarray:
+        """AmericanOptionResult::value_at (mango_american_value_at) and the
+        functionals at other spots: the option in slots[j] read at spots[j]
+        with its own strike; returns (n, 4) value, delta, gamma, theta."""
+        sl = np.ascontiguousarray(np.broadcast_to(np.asarray(slots, np.uint64), np.shape(spots)), np.uint64).ravel()
+        sp = np.ascontiguousarray(spots, dtype=np.float64).ravel()
+        out = np.zeros((sp.size, 4))
+        err = MangoError()
+        if library().mango_gpu_batch_value_at(self._b, _ptr(sl), _ptr(sp), sp.size, _ptr(out),
+                                              ctypes.byref(err)) != MANGO_OK:
             raise EngineError(err.message.decode(errors="replace"))
         return out
 

@@ -34,11 +34,6 @@
 
 namespace mgpu {
 
-__global__ void chain_outputs_kernel(int, const int32_t*, const double*, const double*,
-                                     const TileDev*, const OptDev*, const double*, double*,
-                                     const int32_t*, const int32_t*, MarchConst, double*, int,
-                                     double*);
-
 namespace {
 
 // BatchAmericanOptionSolver limits (src/option/american_option_batch.hpp:219-221).

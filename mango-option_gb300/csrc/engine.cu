@@ -836,6 +836,70 @@ MangoStatus mango_gpu_batch_results(MangoGpuBatch* b, MangoGpuAmericanOut* out,
   }
 }
 
+MangoStatus mango_gpu_batch_value_at(MangoGpuBatch* b, const uint64_t* slots, const double* spots,
+                                     uint64_t n, double* out4, MangoError* err) {
+  if (!b || (n > 0 && (!slots || !spots || !out4))) {
+    set_err(err, MANGO_ERR_VALIDATION, "null batch, slots, spots or out");
+    return MANGO_ERR_VALIDATION;
+  }
+  if (!b->ran) {
+    set_err(err, MANGO_ERR_VALIDATION, "mango_gpu_batch_run has not been called");
+    return MANGO_ERR_VALIDATION;
+  }
+  if (n == 0) return MANGO_OK;
+  if (n > (1ull << 30)) {
+    set_err(err, MANGO_ERR_VALIDATION, "above 2^30 points");
+    return MANGO_ERR_VALIDATION;
+  }
+  DevBuf d_grp, d_spot, d_strike, d_scratch, d_out;
+  auto release = [&]() {
+    for (DevBuf* d : {&d_grp, &d_spot, &d_strike, &d_scratch, &d_out}) d->release();
+  };
+  try {
+    check(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+    // slot -> sorted position (-1: the slot never reached the device)
+    std::vector<int32_t> pos(static_cast<size_t>(b->n), -1);
+    for (size_t s = 0; s < b->order.size(); ++s) pos[b->order[s]] = static_cast<int32_t>(s);
+    const OptDev* ho = b->h_opts.as<OptDev>();
+    const int64_t m = static_cast<int64_t>(n);
+    std::vector<int32_t> grp(static_cast<size_t>(m));
+    std::vector<double> strike(static_cast<size_t>(m));
+    int nmax = 3;
+    for (int64_t j = 0; j < m; ++j) {
+      if (slots[j] >= static_cast<uint64_t>(b->n)) {
+        set_err(err, MANGO_ERR_VALIDATION, "slot out of range");
+        return MANGO_ERR_VALIDATION;
+      }
+      const int32_t g = pos[slots[j]];
+      grp[j] = g;
+      strike[j] = g >= 0 ? ho[g].strike : 1.0;
+      if (g >= 0) nmax = std::max(nmax, ho[g].n);
+    }
+    cudaStream_t st = b->stream;
+    int32_t* dg = static_cast<int32_t*>(d_grp.get(sizeof(int32_t) * m));
+    double* ds = static_cast<double*>(d_spot.get(sizeof(double) * m));
+    double* dk = static_cast<double*>(d_strike.get(sizeof(double) * m));
+    double* dscr = static_cast<double*>(d_scratch.get(sizeof(double) * 2 * nmax * m));
+    double* dout = static_cast<double*>(d_out.get(sizeof(double) * 4 * m));
+    check(cudaMemcpyAsync(dg, grp.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, st), "H2D");
+    check(cudaMemcpyAsync(ds, spots, sizeof(double) * m, cudaMemcpyHostToDevice, st), "H2D");
+    check(cudaMemcpyAsync(dk, strike.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st), "H2D");
+    chain_outputs_kernel<<<static_cast<int>((m + 127) / 128), 128, 0, st>>>(
+        static_cast<int>(m), dg, ds, dk, b->d_tiles.as<TileDev>(), b->d_opts.as<OptDev>(),
+        b->d_xs.as<double>(), b->d_pool.as<double>(), b->d_mode.as<int32_t>(),
+        b->d_status.as<int32_t>(), b->mc, dscr, nmax, dout);
+    check(cudaGetLastError(), "value_at launch");
+    check(cudaMemcpyAsync(out4, dout, sizeof(double) * 4 * m, cudaMemcpyDeviceToHost, st), "D2H");
+    check(cudaStreamSynchronize(st), "stream synchronize");
+    release();
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    release();
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
 void mango_gpu_batch_destroy(MangoGpuBatch* b) {
   if (!b) return;
   cudaSetDevice(b->ctx->device);

@@ -132,6 +132,12 @@ __global__ void march_kernel(const TileDev*, int, const OptDev*, double*, const 
                              const int32_t*, int32_t*, int*, MarchConst);
 __global__ void outputs_kernel(const TileDev*, int, const OptDev*, const double*, double*,
                                const int32_t*, const int32_t*, MarchConst, double*);
+// Result functionals of sorted options grp[j] at spot[j] with strike[j]
+// (march.cu): the normalized chain's extraction, and value_at.
+__global__ void chain_outputs_kernel(int, const int32_t*, const double*, const double*,
+                                     const TileDev*, const OptDev*, const double*, double*,
+                                     const int32_t*, const int32_t*, MarchConst, double*, int,
+                                     double*);
 // Time-varying march (march_tv.cu).
 __global__ void march_tv_kernel(const TileDev*, int, int, const OptDev*, const TvDev*,
                                 const double*, const double*, const double*, const double*,

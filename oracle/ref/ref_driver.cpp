@@ -690,4 +690,26 @@ int32_t ref_iv_batch_tv(int64_t n, const double* S, const double* K, const doubl
   return 0;
 }
 
+
+// AmericanOptionResult::value_at (american_option_result.cpp:29-45) at
+// spot2[i] for options priced on the fixed-size grid rule (nx, nt).
+int32_t ref_value_at(int64_t n, const double* S, const double* K, const double* T,
+                     const double* sigma, const double* r, const double* q, const int32_t* is_put,
+                     const int64_t* nx, const int64_t* nt, const double* spot2, int32_t n_threads,
+                     double* out, int32_t* status) {
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t i = 0; i < n; ++i) {
+    auto p = make_params(S[i], K[i], T[i], sigma[i], r[i], q[i], is_put[i]);
+    auto grid = grid_for(p, nx[i], nt[i], 0.0);
+    auto solver = AmericanOptionSolver::create(p, grid);
+    if (!solver) { status[i] = 1; continue; }
+    auto res = solver->solve();
+    if (!res) { status[i] = 5; continue; }
+    status[i] = 0;
+    out[i] = res->value_at(spot2[i]);
+  }
+  return 0;
+}
+
 }  // extern "C"

@@ -247,6 +247,7 @@ def main():
     golden_tv(lib)
     golden_shared_tv(lib)
     golden_iv_tv(lib)
+    golden_value_at(lib)
 
 
 def table_axes(nm, ntau, ns, nr):
@@ -667,6 +668,24 @@ def golden_iv_tv(lib):
                         ctypes.c_int32(8), P(o3), P(ist))
     save("iv_tv.npz", rows=np.array([json.dumps(r) for r in rows]), price=price, grid_sigma=gsig, nx=nx, nt=nt,
          out=o3.reshape(n, 3), status=ist)
+
+
+def golden_value_at(lib):
+    """AmericanOptionResult::value_at at other spots, below, inside and
+    above each option's grid."""
+    S, K, T, sig, r, q, put = config0_inputs(64, 81, True)
+    rng = np.random.default_rng(82)
+    spot2 = rng.uniform(40.0, 160.0, 64)
+    spot2[:4] = [1e-3, 5.0, 1e4, 100.0]  # below / far below / above the grid, at the spot
+    nx = np.full(64, 101, np.int64)
+    nt = np.full(64, 498, np.int64)
+    out = np.zeros(64)
+    st = np.zeros(64, np.int32)
+    a = [np.ascontiguousarray(v, dtype=np.float64) for v in (S, K, T, sig, r, q)]
+    lib.ref_value_at(ctypes.c_int64(64), *(P(v) for v in a), P(np.ascontiguousarray(put, np.int32)), P(nx), P(nt),
+                     P(spot2), ctypes.c_int32(8), P(out), P(st))
+    assert (st == 0).all()
+    save("value_at.npz", S=S, K=K, T=T, sigma=sig, r=r, q=q, is_put=put, nx=nx, nt=nt, spot2=spot2, value=out)
 
 
 if __name__ == "__main__":

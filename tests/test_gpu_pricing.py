@@ -141,3 +141,20 @@ def test_chunked_batch_matches_resident_batch(engine, pkg, n):
     check(greeks(out), greeks(ref), rtol=1e-13, atol=1e-14)
     again = engine.price_arrays(p, grid)  # buffers reused
     assert np.array_equal(again["value"], out["value"])
+
+
+def test_value_at_vs_reference(engine, pkg):
+    """AmericanOptionResult::value_at at other spots (tests/golden/value_at.npz:
+    below, inside and above each grid), through the resident batch."""
+    g = golden("value_at.npz")
+    p = pkg.pricing_array(g["S"], g["K"], g["T"], g["sigma"], g["r"], g["q"], g["is_put"])
+    b = engine.batch(p, pkg.grid_array(len(g["S"]), pkg.GRID_FIXED_N, g["nx"], g["nt"]))
+    b.run()
+    res = b.results()
+    n = len(g["S"])
+    got = b.value_at(np.arange(n), g["spot2"])
+    want = g["value"]
+    assert np.abs(got[:, 0] - want).max() <= 1e-9 * np.abs(want).max()
+    own = b.value_at(np.arange(n), g["S"])  # at the option's own spot: the batch's results
+    check(own, greeks(res), rtol=1e-15, atol=0.0)
+    b.close()

@@ -420,6 +420,23 @@ MangoStatus mango_gpu_price_table_price_device(MangoGpuPriceTable* table,
 MangoStatus mango_gpu_price_table_vega(MangoGpuPriceTable* table, const MangoPricingParams* params,
                                        uint64_t n, double* out, MangoError* err);
 
+/* The table's delta, gamma, theta and rho for n records: the batch analogue
+ * of mango_price_table_delta / _gamma / _theta / _rho
+ * (src/ffi/mango_c_api.cpp:652-682, greek_call at 272-300).  Each record is
+ * validated first as AnyPriceTable::validate_pricing_params does
+ * (src/option/price_table_factory.cpp:700-745: positive finite inputs, the
+ * table's option type and dividend yield within 1e-10, every coordinate
+ * inside the table's axis ranges; constant rates only), then EEPLayer::greek
+ * / gamma (src/option/table/eep/eep_layer.hpp:33-76) over the analytic spline
+ * partials.  out4[4i .. 4i+3] = {delta, gamma, theta, rho}; a record that
+ * fails validation gets NaN there and MANGO_ERR_VALIDATION in status[i]
+ * (status may be NULL), and the call returns MANGO_ERR_VALIDATION with the
+ * count and the first failing index in err.  The other records are still
+ * computed. */
+MangoStatus mango_gpu_price_table_greeks(MangoGpuPriceTable* table, const MangoPricingParams* params,
+                                         uint64_t n, double* out4, int32_t* status,
+                                         MangoError* err);
+
 /* Interpolated implied volatility on the table:
  * InterpolatedIVSolver::solve_batch (src/option/interpolated_iv_solver.hpp:
  * 427-560), the batch analogue of mango_interp_iv_solve_batch

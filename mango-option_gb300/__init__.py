@@ -18,7 +18,7 @@ import ctypes
 import dataclasses
 import enum
 import pathlib
-from typing import Iterable, Optional, Sequence
+from typing import Iterable, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -211,6 +211,8 @@ def library() -> ctypes.CDLL:
         lib.mango_gpu_price_table_price_device.restype = ctypes.c_int32
         lib.mango_gpu_price_table_vega.argtypes = [_P, _P, ctypes.c_uint64, _P, ctypes.POINTER(MangoError)]
         lib.mango_gpu_price_table_vega.restype = ctypes.c_int32
+        lib.mango_gpu_price_table_greeks.argtypes = [_P, _P, ctypes.c_uint64, _P, _P, ctypes.POINTER(MangoError)]
+        lib.mango_gpu_price_table_greeks.restype = ctypes.c_int32
         lib.mango_gpu_price_table_iv_batch.argtypes = [_P, ctypes.POINTER(MangoInterpSolverConfig), _P,
                                                        ctypes.c_uint64, _P, ctypes.POINTER(ctypes.c_uint64),
                                                        ctypes.POINTER(MangoError)]
@@ -773,6 +775,40 @@ class GpuPriceTable:
     def vega(self, params: PricingParams) -> float:
         self.validate(params)
         return float(self.vega_arrays(_to_array([params]))[0])
+
+    def greeks_arrays(self, params: np.ndarray) -> Tuple[np.ndarray, np.ndarray]:
+        """delta, gamma, theta, rho (columns of an n x 4 array) and per-record
+        statuses for PRICING_DTYPE records (mango_gpu_price_table_greeks):
+        records that fail validation hold NaN and MANGO_ERR_VALIDATION."""
+        params = np.ascontiguousarray(params, dtype=PRICING_DTYPE)
+        out = np.zeros((params.size, 4))
+        status = np.zeros(params.size, dtype=np.int32)
+        err = MangoError()
+        rc = library().mango_gpu_price_table_greeks(self._t, _ptr(params), params.size, _ptr(out),
+                                                    _ptr(status), ctypes.byref(err))
+        if rc not in (MANGO_OK, MANGO_ERR_VALIDATION):
+            raise EngineError(err.message.decode(errors="replace"))
+        return out, status
+
+    def _greek(self, params: PricingParams, col: int) -> float:
+        """greek_call (mango_c_api.cpp:272-300): validate, then one Greek."""
+        self.validate(params)
+        out, status = self.greeks_arrays(_to_array([params]))
+        if status[0] != MANGO_OK:
+            raise ValueError("pricing params fail the table's validation")
+        return float(out[0, col])
+
+    def delta(self, params: PricingParams) -> float:
+        return self._greek(params, 0)
+
+    def gamma(self, params: PricingParams) -> float:
+        return self._greek(params, 1)
+
+    def theta(self, params: PricingParams) -> float:
+        return self._greek(params, 2)
+
+    def rho(self, params: PricingParams) -> float:
+        return self._greek(params, 3)
 
     def iv_arrays(self, queries: np.ndarray, config: Optional["InterpolatedIVSolverConfig"] = None) -> np.ndarray:
         """InterpolatedIVSolver::solve_batch (mango_gpu_price_table_iv_batch):

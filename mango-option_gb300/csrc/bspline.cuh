@@ -46,7 +46,10 @@ void bspline_tables(const double* grids, const int64_t* sizes, BSplineDims* D,
 // axis DAX (bspline_nd.hpp:168-199: the derivative basis
 // cubic_basis_derivative_nonuniform, bspline_basis.hpp:258-330, on that axis,
 // without the right-end special case); sm holds the packed tables.
-template <int DAX = -1>
+// DAX >= 0: the derivative basis of order ORD (1: cubic_basis_derivative_
+// nonuniform, 2: cubic_basis_second_derivative_nonuniform, bspline_basis.hpp:
+// 343-410) on that axis, the value basis on the others.
+template <int DAX = -1, int ORD = 1>
 __device__ __forceinline__ double bspline4d_eval_t(const BSplineDims& D, const double* sm,
                                                    const double* __restrict__ coeffs,
                                                    const double* xq) {
@@ -80,6 +83,20 @@ __device__ __forceinline__ double bspline4d_eval_t(const BSplineDims& D, const d
       i = min(max(lo - 1, 3), max_span);
     }
     span[d] = i;
+    if (d == DAX && ORD == 2) {
+      // degree-1 basis, its derivative quadratics, then the cubic's second
+      // derivative (zero-length knot spans give zero reciprocals)
+      const double n10 = (x - t[i]) * R1[i];
+      const double n11 = (t[i + 1] - x) * R1[i];
+      const double q0 = 2.0 * R2[i] * n10;
+      const double q1 = 2.0 * R2[i - 1] * n11 - 2.0 * R2[i] * n10;
+      const double q2 = 0.0 - 2.0 * R2[i - 1] * n11;
+      w[d][0] = 3.0 * R3[i] * q0;
+      w[d][1] = 3.0 * R3[i - 1] * q1 - 3.0 * R3[i] * q0;
+      w[d][2] = 3.0 * R3[i - 2] * q2 - 3.0 * R3[i - 1] * q1;
+      w[d][3] = 0.0 - 3.0 * R3[i - 2] * q2;
+      continue;
+    }
     if (d == DAX) {
       const double n10 = (x - t[i]) * R1[i];
       const double n11 = (t[i + 1] - x) * R1[i];

@@ -76,6 +76,38 @@ __device__ double european_vega(double S, double K, double tau, double sigma, do
   return S * exp(-q * tau) * sqrt(tau) * (0.3989422804014327 * exp(-0.5 * d1 * d1));
 }
 
+__device__ __forceinline__ double norm_pdf(double x) {
+  return 0.3989422804014327 * exp(-0.5 * x * x);  // european_option.hpp:24-27
+}
+
+// EuropeanOptionResult::delta/gamma/theta/rho (european_option.cpp:55-154)
+// with d1 = bs_d1, d2 = d1 - sigma sqrt(tau); g = {delta, gamma, theta, rho}.
+__device__ void european_greeks(double S, double K, double tau, double sigma, double r, double q,
+                                bool put, double g[4]) {
+  if (tau <= 0.0 || sigma <= 0.0) {
+    const double eq = exp(-q * tau);
+    g[0] = put ? (S < K ? -eq : 0.0) : (S > K ? eq : 0.0);
+    g[1] = g[2] = g[3] = 0.0;
+    return;
+  }
+  const double sqt = sqrt(tau);
+  const double d1 = (log(S / K) + (r - q + 0.5 * sigma * sigma) * tau) / (sigma * sqt);
+  const double d2 = d1 - sigma * sqt;
+  const double eq = exp(-q * tau), er = exp(-r * tau);
+  const double pdf = norm_pdf(d1);
+  g[1] = eq * pdf / (S * sigma * sqt);
+  const double common = -S * eq * pdf * sigma / (2.0 * sqt);
+  if (put) {
+    g[0] = -eq * norm_cdf(-d1);
+    g[2] = common + r * K * er * norm_cdf(-d2) - q * S * eq * norm_cdf(-d1);
+    g[3] = -K * tau * er * norm_cdf(-d2);
+  } else {
+    g[0] = eq * norm_cdf(d1);
+    g[2] = common - r * K * er * norm_cdf(d2) + q * S * eq * norm_cdf(d1);
+    g[3] = K * tau * er * norm_cdf(d2);
+  }
+}
+
 // eep_floor (eep_decomposer.hpp:21-29): debiased softplus with sharpness 100.
 __device__ double eep_floor(double e) {
   if (100.0 * e > 500.0) return e;
@@ -221,6 +253,59 @@ __global__ void surface_vega_kernel(BSplineDims D, const double* __restrict__ ta
                  ? __longlong_as_double(0x7ff8000000000000ll)
                  : table_vega(D, sm, coeffs, T, pk.spot, pk.strike, pk.maturity, pk.volatility,
                               pk.rate_const);
+  }
+}
+
+// AnyPriceTable::delta/gamma/theta/rho behind the C API's greek_call
+// (mango_c_api.cpp:272-300, 652-682): AnyPriceTable::validate_pricing_params
+// (price_table_factory.cpp:700-745) first, then EEPLayer::greek / gamma
+// (eep_layer.hpp:33-76) over TransformLeaf::greek / gamma
+// (transform_leaf.hpp:46-90) with StandardTransform4D's weights
+// (delta 1/S on axis 0, theta -1 on axis 1, rho 1 on axis 3) and
+// gamma = (f_xx - f_x) / S^2, each scaled by K / K_ref.  A record that fails
+// validation gets status MANGO_ERR_VALIDATION and NaN Greeks.
+__global__ void surface_greeks_kernel(BSplineDims D, const double* __restrict__ tables,
+                                      const double* __restrict__ coeffs, TableDev T,
+                                      const MangoPricingParams* __restrict__ p, int64_t n,
+                                      double* __restrict__ out4, int32_t* __restrict__ status) {
+  extern __shared__ double sm[];
+  for (int i = threadIdx.x; i < 4 * D.ktot; i += blockDim.x) sm[i] = tables[i];
+  __syncthreads();
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < n; k += stride) {
+    const MangoPricingParams pk = p[k];
+    const double S = pk.spot, K = pk.strike, tau = pk.maturity, sigma = pk.volatility,
+                 r = pk.rate_const;
+    const bool put = pk.option_type == MANGO_PUT;
+    const double x[4] = {log(S / K), tau, sigma, r};
+    const bool ok = (pk.option_type == MANGO_PUT || pk.option_type == MANGO_CALL) &&
+                    pk.n_tenor_points == 0 && S > 0.0 && isfinite(S) && K > 0.0 && isfinite(K) &&
+                    tau > 0.0 && isfinite(tau) && sigma > 0.0 && isfinite(sigma) && isfinite(r) &&
+                    isfinite(pk.dividend_yield) && put == (T.put != 0) &&
+                    fabs(pk.dividend_yield - T.q) <= 1e-10 && x[0] >= T.lo[0] && x[0] <= T.hi[0] &&
+                    tau >= T.lo[1] && tau <= T.hi[1] && sigma >= T.lo[2] && sigma <= T.hi[2] &&
+                    r >= T.lo[3] && r <= T.hi[3];
+    double g[4] = {nan, nan, nan, nan};
+    if (ok) {
+      double e[4] = {0.0, 0.0, 0.0, 0.0};
+      if (T.eep) european_greeks(S, K, tau, sigma, r, T.q, put, e);
+      const double raw = bspline4d_value(D, sm, coeffs, x);
+      if (raw > 0.0) {
+        const double fx = bspline4d_eval_t<0>(D, sm, coeffs, x);
+        const double fxx = bspline4d_eval_t<0, 2>(D, sm, coeffs, x);
+        const double ft = bspline4d_eval_t<1>(D, sm, coeffs, x);
+        const double fr = bspline4d_eval_t<3>(D, sm, coeffs, x);
+        g[0] = __dmul_rn(1.0 / S, fx) * K / T.K_ref + e[0];
+        g[1] = (fxx - fx) / (S * S) * K / T.K_ref + e[1];
+        g[2] = -ft * K / T.K_ref + e[2];
+        g[3] = fr * K / T.K_ref + e[3];
+      } else {
+        for (int j = 0; j < 4; ++j) g[j] = e[j];
+      }
+    }
+    for (int j = 0; j < 4; ++j) out4[4 * k + j] = g[j];
+    if (status) status[k] = ok ? MANGO_OK : MANGO_ERR_VALIDATION;
   }
 }
 
@@ -785,6 +870,52 @@ MangoStatus mango_gpu_price_table_vega(MangoGpuPriceTable* t, const MangoPricing
     check(cudaGetLastError(), "surface_vega_kernel launch");
     check(cudaMemcpyAsync(out, dout, sizeof(double) * n, cudaMemcpyDeviceToHost, st), "D2H");
     check(cudaStreamSynchronize(st), "stream synchronize");
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}
+
+MangoStatus mango_gpu_price_table_greeks(MangoGpuPriceTable* t, const MangoPricingParams* params,
+                                         uint64_t n, double* out4, int32_t* status,
+                                         MangoError* err) {
+  if (!t || (n > 0 && (!params || !out4))) {
+    set_err(err, MANGO_ERR_VALIDATION, "null argument");
+    return MANGO_ERR_VALIDATION;
+  }
+  if (n == 0) return MANGO_OK;
+  try {
+    MangoGpuBSpline4D* s = t->surface;
+    check(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    cudaStream_t st = s->ctx->stream;
+    const size_t pb = sizeof(MangoPricingParams) * n;
+    MangoPricingParams* dp = static_cast<MangoPricingParams*>(t->d_p.get(pb));
+    // Greeks (4n doubles) then the statuses (n int32) in one buffer.
+    char* dbuf = static_cast<char*>(t->d_out.get(sizeof(double) * 4 * n + sizeof(int32_t) * n));
+    double* dout = reinterpret_cast<double*>(dbuf);
+    int32_t* dst = reinterpret_cast<int32_t*>(dbuf + sizeof(double) * 4 * n);
+    check(cudaMemcpyAsync(dp, params, pb, cudaMemcpyHostToDevice, st), "H2D");
+    const int blocks = static_cast<int>(std::min<int64_t>(s->blocks, static_cast<int64_t>((n + 255) / 256)));
+    surface_greeks_kernel<<<blocks, 256, sizeof(double) * 4 * s->dims.ktot, st>>>(
+        s->dims, s->d_tables.as<double>(), s->d_coeffs.as<double>(), table_dev(t), dp,
+        static_cast<int64_t>(n), dout, dst);
+    check(cudaGetLastError(), "surface_greeks_kernel launch");
+    check(cudaMemcpyAsync(out4, dout, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st), "D2H");
+    std::vector<int32_t> hs(n);
+    check(cudaMemcpyAsync(hs.data(), dst, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st), "D2H");
+    check(cudaStreamSynchronize(st), "stream synchronize");
+    uint64_t bad = 0, first = 0;
+    for (uint64_t i = 0; i < n; ++i)
+      if (hs[i] != MANGO_OK && bad++ == 0) first = i;
+    if (status) std::memcpy(status, hs.data(), sizeof(int32_t) * n);
+    if (bad) {
+      const std::string msg = std::to_string(bad) + " record(s) failed validation (type, dividend "
+                              "yield, positivity or table range), first at index " +
+                              std::to_string(first);
+      set_err(err, MANGO_ERR_VALIDATION, msg.c_str());
+      return MANGO_ERR_VALIDATION;
+    }
     return MANGO_OK;
   } catch (const std::exception& e) {
     set_err(err, MANGO_ERR_SOLVER, e.what());

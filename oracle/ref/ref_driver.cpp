@@ -712,4 +712,42 @@ int32_t ref_value_at(int64_t n, const double* S, const double* K, const double* 
   return 0;
 }
 
+
+// The standard table's delta, gamma, theta and rho (PriceTable over
+// EEPLayer<TransformLeaf>: eep_layer.hpp:33-76, transform_leaf.hpp:46-90),
+// p n x 5 {spot, strike, tau, sigma, rate}; out n x 4; status 0 or 1 + the
+// GreekError code.
+int32_t ref_surface_greeks(const int64_t* sizes, const double* grids, const double* coeffs,
+                           double K_ref, double q, int32_t is_put, const double* p, int64_t n,
+                           double* out, int32_t* status) {
+  std::array<std::vector<double>, 4> g, k;
+  size_t off = 0, total = 1;
+  for (int d = 0; d < 4; ++d) {
+    g[d].assign(grids + off, grids + off + sizes[d]);
+    off += static_cast<size_t>(sizes[d]);
+    k[d] = clamped_knots_cubic(g[d]);
+    total *= static_cast<size_t>(sizes[d]);
+  }
+  std::vector<double> c(coeffs, coeffs + total);
+  auto sp = BSplineND<double, 4>::create(g, k, std::move(c));
+  if (!sp) return 1;
+  auto shared = std::make_shared<const BSplineND<double, 4>>(std::move(sp.value()));
+  auto table = make_bspline_surface(shared, K_ref, q, is_put ? OptionType::PUT : OptionType::CALL);
+  if (!table) return 2;
+  for (int64_t i = 0; i < n; ++i) {
+    PricingParams pp = make_params(p[5 * i], p[5 * i + 1], p[5 * i + 2], p[5 * i + 3], p[5 * i + 4], q, is_put);
+    auto d = table->delta(pp);
+    auto ga = table->gamma(pp);
+    auto th = table->theta(pp);
+    auto rh = table->rho(pp);
+    if (!d || !ga || !th || !rh) { status[i] = 1; continue; }
+    status[i] = 0;
+    out[4 * i + 0] = *d;
+    out[4 * i + 1] = *ga;
+    out[4 * i + 2] = *th;
+    out[4 * i + 3] = *rh;
+  }
+  return 0;
+}
+
 }  // extern "C"

@@ -248,6 +248,7 @@ def main():
     golden_shared_tv(lib)
     golden_iv_tv(lib)
     golden_value_at(lib)
+    golden_table_greeks(lib)
 
 
 def table_axes(nm, ntau, ns, nr):
@@ -688,5 +689,40 @@ def golden_value_at(lib):
     save("value_at.npz", S=S, K=K, T=T, sigma=sig, r=r, q=q, is_put=put, nx=nx, nt=nt, spot2=spot2, value=out)
 
 
+def golden_table_greeks(lib):
+    """The standard table's delta / gamma / theta / rho (PriceTable over
+    EEPLayer<TransformLeaf>) on interp_iv.npz's coefficients, as a put table
+    with q = 0 (the one the coefficients were fitted for), a put table with
+    q = 0.02 and a call table with q = 0.01 (the same spline reused, so the
+    European terms with a dividend yield are exercised)."""
+    g = np.load(HERE / "interp_iv.npz")
+    sizes, grids, coeffs = g["sizes"], g["grids"], g["coeffs"]
+    axes = np.split(grids, np.cumsum(sizes)[:-1])
+    rng = np.random.default_rng(57)
+    n = 512
+    m = rng.uniform(axes[0][0], axes[0][-1], n)
+    p = np.stack([np.full(n, 100.0), 100.0 / np.exp(m), rng.uniform(axes[1][0], axes[1][-1], n),
+                  rng.uniform(axes[2][0], axes[2][-1], n), rng.uniform(axes[3][0], axes[3][-1], n)], 1)
+    # the axis ends and a deep out-of-the-money corner (spline value <= 0)
+    p[0] = [100.0, 100.0 / np.exp(axes[0][0]), axes[1][0], axes[2][0], axes[3][0]]
+    p[1] = [100.0, 100.0 / np.exp(axes[0][-1]), axes[1][-1], axes[2][-1], axes[3][-1]]
+    p[2] = [100.0, 100.0 / np.exp(axes[0][-1]), axes[1][0], axes[2][0], axes[3][-1]]
+    p = np.ascontiguousarray(p)
+    kw = {}
+    for name, q, put in (("put", 0.0, 1), ("put_q", 0.02, 1), ("call_q", 0.01, 0)):
+        out = np.zeros(4 * n)
+        st = np.zeros(n, np.int32)
+        assert lib.ref_surface_greeks(P(sizes), P(grids), P(coeffs), ctypes.c_double(100.0), ctypes.c_double(q),
+                                      ctypes.c_int32(put), P(p), ctypes.c_int64(n), P(out), P(st)) == 0
+        assert (st == 0).all()
+        kw[f"{name}_greeks"] = out.reshape(n, 4)
+    save("table_greeks.npz", sizes=sizes, grids=grids, coeffs=coeffs, params=p, **kw)
+
+
 if __name__ == "__main__":
-    sys.exit(main())
+    if len(sys.argv) > 1:  # regenerate the named fixtures only
+        _l = _lib()
+        for _name in sys.argv[1:]:
+            globals()[f"golden_{_name}"](_l)
+    else:
+        sys.exit(main())

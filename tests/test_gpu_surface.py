@@ -193,3 +193,50 @@ def test_table_data_round_trip(engine, pkg):
         pkg.from_data(d, engine)
     table.close()
     t2.close()
+
+
+@pytest.mark.parametrize("name,q,put", [("put", 0.0, 1), ("put_q", 0.02, 1), ("call_q", 0.01, 0)])
+def test_table_greeks_vs_reference(engine, pkg, name, q, put):
+    """delta / gamma / theta / rho of the standard table (EEPLayer over
+    TransformLeaf with analytic spline partials) against the reference's
+    PriceTable on the same coefficients (tests/golden/table_greeks.npz).
+    Bar: 1e-11 of each Greek's largest magnitude (the reference divides by
+    knot spans where the kernel multiplies by their reciprocals)."""
+    g = golden("table_greeks.npz")
+    t = engine.price_table_create(axes_of(g), g["coeffs"], 100.0, q, put, eep=True)
+    out, status = t.greeks_arrays(records(pkg, g["params"], put, q))
+    assert (status == 0).all()
+    ref = g[f"{name}_greeks"]
+    for j in range(4):
+        scale = np.abs(ref[:, j]).max()
+        assert np.abs(out[:, j] - ref[:, j]).max() <= 1e-11 * scale + 1e-13, (name, j)
+    # the single-record mirror of mango_price_table_delta etc.
+    p0 = pkg.PricingParams(spot=100.0, strike=float(g["params"][5, 1]), maturity=float(g["params"][5, 2]),
+                           volatility=float(g["params"][5, 3]), rate=float(g["params"][5, 4]),
+                           dividend_yield=q, option_type=pkg.OptionType(put))
+    for j, f in enumerate((t.delta, t.gamma, t.theta, t.rho)):
+        assert f(p0) == out[5, j]
+
+
+def test_table_greeks_validation(engine, pkg):
+    """Records failing AnyPriceTable::validate_pricing_params get NaN and
+    MANGO_ERR_VALIDATION; the rest of the batch is still computed."""
+    g = golden("table_greeks.npz")
+    t = engine.price_table_create(axes_of(g), g["coeffs"], 100.0, 0.0, 1, eep=True)
+    p = g["params"][:8].copy()
+    recs = records(pkg, p, 1, 0.0)
+    recs["maturity"][1] = 5.0          # outside the maturity axis
+    recs["option_type"][2] = 0         # call on a put table
+    recs["dividend_yield"][3] = 0.01   # yield mismatch
+    recs["volatility"][4] = -0.2       # not positive
+    recs["strike"][5] = 10.0           # log-moneyness outside the axis
+    out, status = t.greeks_arrays(recs)
+    bad = [1, 2, 3, 4, 5]
+    assert (status[bad] == pkg.MANGO_ERR_VALIDATION).all()
+    assert np.isnan(out[bad]).all()
+    good = [0, 6, 7]
+    assert (status[good] == 0).all()
+    assert np.abs(out[good] - g["put_greeks"][good]).max() <= 1e-11 * np.abs(g["put_greeks"]).max()
+    with pytest.raises(ValueError):
+        t.delta(pkg.PricingParams(spot=100.0, strike=100.0, maturity=5.0, volatility=0.2, rate=0.02,
+                                  dividend_yield=0.0, option_type=pkg.OptionType.PUT))

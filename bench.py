@@ -259,6 +259,21 @@ def bench_greeks(pkg, eng, n=16384):
     return {"workload": f"{n} American puts, 101x498, value+delta+gamma+theta+vega+rho+dq+dK "
                         "(central differences on the frozen grid, 9 prices per option)",
             "value": n / t, "unit": "options with full Greeks/s (end to end)", "seconds": t,
+            "failed": int(np.count_nonzero(out["status"])),
+            "tangent": bench_tangent(pkg, eng, params, grid)}
+
+
+def bench_tangent(pkg, eng, params, grid):
+    """The same 16,384 puts through the forward-mode march
+    (mango_gpu_price_american_tangent_batch): value, delta and the exact
+    discrete dV/dvolatility, dV/drate, dV/ddividend_yield, dV/dK in one pass."""
+    eng.tangent_arrays(params, grid)
+    t0 = time.perf_counter()
+    out = eng.tangent_arrays(params, grid)
+    t = time.perf_counter() - t0
+    return {"workload": f"{params.size} American puts, 101x498, value+delta+exact discrete vega/rho/dq/dK "
+                        "(forward-mode march, 3 tangents)",
+            "value": params.size / t, "unit": "options with sensitivities/s (end to end)", "seconds": t,
             "failed": int(np.count_nonzero(out["status"]))}
 
 

@@ -486,6 +486,24 @@ MangoStatus mango_gpu_price_american_greeks_batch(MangoGpuContext* ctx,
                                                   double h_rel, MangoGpuGreeksOut* out,
                                                   uint64_t* out_failed, MangoError* err);
 
+/* Exact discrete sensitivities in one pass: the march of each option's own
+ * grid (the reference's plain method with the Rannacher start, as
+ * solve_american_option; constant rates and continuous dividends only)
+ * differentiated in forward mode with respect to volatility, rate and
+ * dividend yield, the active obstacle set frozen; dV/dK from the final
+ * spline on the strike-independent grid.  These are the derivatives of the
+ * discrete price that the central differences of
+ * mango_gpu_price_american_greeks_batch approximate on the same grid.
+ * Fills value, delta, vega, rho, dividend_rho, dstrike, status, n_space and
+ * n_time; gamma and theta are NaN (mango_gpu_price_american_batch gives
+ * them).  Returns MANGO_ERR_VALIDATION only when every option failed; per
+ * option statuses otherwise. */
+MangoStatus mango_gpu_price_american_tangent_batch(MangoGpuContext* ctx,
+                                                   const MangoPricingParams* params, uint64_t n,
+                                                   const MangoGpuGrid* grids, uint64_t grid_stride,
+                                                   MangoGpuGreeksOut* out, uint64_t* out_failed,
+                                                   MangoError* err);
+
 /* Resident batch: the same pipeline as mango_gpu_price_american_batch split
  * so that inputs can stay in device memory across runs (repeat pricing of a
  * book, IV iterations, benchmarking).  _create validates, resolves grids and

@@ -224,6 +224,10 @@ def library() -> ctypes.CDLL:
             _P, _P, ctypes.c_uint64, _P, ctypes.c_uint64, ctypes.c_double, _P,
             ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(MangoError)]
         lib.mango_gpu_price_american_greeks_batch.restype = ctypes.c_int32
+        lib.mango_gpu_price_american_tangent_batch.argtypes = [
+            _P, _P, ctypes.c_uint64, _P, ctypes.c_uint64, _P, ctypes.POINTER(ctypes.c_uint64),
+            ctypes.POINTER(MangoError)]
+        lib.mango_gpu_price_american_tangent_batch.restype = ctypes.c_int32
         lib.mango_gpu_build_info.argtypes = []
         lib.mango_gpu_build_info.restype = ctypes.c_char_p
         _lib = lib
@@ -645,6 +649,26 @@ class Engine:
         st = library().mango_gpu_price_american_greeks_batch(self._ctx, _ptr(params), n, _ptr(grids), stride,
                                                              h_rel, _ptr(out), ctypes.byref(failed),
                                                              ctypes.byref(err))
+        if st != MANGO_OK:
+            raise EngineError(err.message.decode(errors="replace"))
+        return out
+
+    def tangent_arrays(self, params: np.ndarray, grids: Optional[np.ndarray] = None) -> np.ndarray:
+        """Value, delta and the exact discrete dV/dvolatility, dV/drate,
+        dV/ddividend_yield, dV/dK of the march in one forward-mode pass
+        (mango_gpu_price_american_tangent_batch); GREEKS_DTYPE records with
+        gamma and theta NaN."""
+        params = np.ascontiguousarray(params, dtype=PRICING_DTYPE)
+        n = params.size
+        stride = 0
+        if grids is not None:
+            grids = np.ascontiguousarray(grids, dtype=GRID_DTYPE)
+            stride = 1 if (grids.size == n and n != 1) else 0
+        out = np.zeros(n, dtype=GREEKS_DTYPE)
+        failed = ctypes.c_uint64()
+        err = MangoError()
+        st = library().mango_gpu_price_american_tangent_batch(self._ctx, _ptr(params), n, _ptr(grids), stride,
+                                                              _ptr(out), ctypes.byref(failed), ctypes.byref(err))
         if st != MANGO_OK:
             raise EngineError(err.message.decode(errors="replace"))
         return out

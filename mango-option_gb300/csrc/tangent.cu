@@ -1,0 +1,573 @@
+// tangent.cu -- exact discrete sensitivities of the American march by
+// forward-mode (tangent-linear) differentiation.
+//
+// The primal is the reference's plain method on one option's own grid:
+// PDESolver::solve with the Rannacher start and TR-BDF2 stages
+// (src/pde/internal/pde_solver.hpp:114-178, 342-447), each stage
+// solve_implicit_stage_projected (pde_solver.hpp:525-729: boundary values,
+// the deep-ITM lock, solve_thomas_projected, src/math/thomas_solver.hpp:
+// 321-420), the Black-Scholes operator (spatial_operator.hpp:74-163,
+// black_scholes_pde.hpp:72-76) and AmericanOptionResult's value and delta
+// (src/option/american_option_result.cpp:25-60, natural CubicSpline,
+// src/math/cubic_spline_solver.hpp:74-230).  Beside it the kernel carries
+// three tangents, d/dsigma, d/drate and d/ddividend_yield, through every
+// operation of that algorithm: the operator's coefficients
+// a = sigma^2/2, b = r - q - a, c = -r are linear in the stencils, the
+// Thomas forward sweep is differentiated row by row (denominator, reciprocal,
+// modified upper band and right-hand side), and the projected back
+// substitution x_i = max(y_i, psi_i) passes the tangent of y_i where the
+// obstacle is inactive and 0 where it binds (the active set and the lock rows
+// of the primal, frozen).  The result is the derivative of the discrete
+// price the march computes, the quantity that central differences on the
+// same frozen grid approximate, in one pass; d/dstrike follows from the final
+// spline alone because the log-moneyness grid does not depend on the strike.
+//
+// GB300 layout: one thread per option; options in tiles of 32 with every
+// per-option vector interleaved by lane (element i of array a of the
+// tile's option `lane` at ((a * nmax + i) * 32 + lane)), so a warp's loads
+// and stores of the same row coalesce into 256-byte transactions.  The
+// work is FP64 and L2/HBM streaming; no tensor cores.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "engine.hpp"
+
+namespace mgpu {
+namespace {
+
+constexpr int kTan = 3;  // sigma, rate, dividend yield
+// Interleaved per-option arrays.
+enum : int {
+  TA_X = 0, TA_PSI, TA_U, TA_UP, TA_RHS, TA_CP, TA_DP,
+  TA_TU,                    // + j
+  TA_TUP = TA_TU + kTan,     // + j
+  TA_TRHS = TA_TUP + kTan,   // + j
+  TA_TCP = TA_TRHS + kTan,   // + j
+  TA_TDP = TA_TCP + kTan,    // + j
+  // time-invariant row coefficients, filled once per option:
+  TA_JL = TA_TDP + kTan, TA_JD, TA_JU,           // assemble_jacobian's rows
+  TA_G2M, TA_G2I, TA_G2P, TA_G1M, TA_G1I, TA_G1P,  // their d/da and d/db
+  TA_LI, TA_RI, TA_CI, TA_WL, TA_WR,              // CenteredDifference factors
+  TA_COUNT
+};
+
+struct TanOpt {
+  double S, K, T, sigma, r, q;
+  int64_t x_off;
+  int32_t n, nt, put, pad;
+};
+
+struct TanOut {
+  double value, delta, dsigma, drate, ddiv, dstrike;
+  int32_t status, pad;
+};
+
+struct View {
+  double* base;
+  int nmax;
+  __device__ __forceinline__ double& operator()(int a, int i) const {
+    return base[(static_cast<size_t>(a) * nmax + i) * 32];
+  }
+};
+
+// Per-parameter derivatives of (a, b, c).
+struct Coef {
+  double a, b, c;
+  double da[kTan], db[kTan], dc[kTan];
+};
+
+__device__ __forceinline__ void stencil(const View& v, int arr, int i, double& d2, double& d1) {
+  const double um = v(arr, i - 1), u0 = v(arr, i), up = v(arr, i + 1);
+  const double li = v(TA_LI, i), ri = v(TA_RI, i);
+  const double fwd = (up - u0) * ri, bwd = (u0 - um) * li;
+  d2 = (fwd - bwd) * v(TA_CI, i);
+  d1 = v(TA_WL, i) * (u0 - um) * li + v(TA_WR, i) * (up - u0) * ri;
+}
+
+// assemble_jacobian's row coefficients (spatial_operator.hpp:123-163) for
+// operator coefficients (a, b, c).
+__device__ __forceinline__ void jac_row(double dxl, double dxr, double a, double b, double c,
+                                        double& jl, double& jd, double& ju) {
+  const double dxa = (dxl + dxr) / 2.0;
+  const double d1d = dxl + dxr;
+  jl = a / (dxl * dxa) + (-b * dxr / (dxl * d1d));
+  jd = (-a * (1.0 / dxl + 1.0 / dxr) / dxa) + b * (dxr - dxl) / (dxl * dxr) + c;
+  ju = a / (dxr * dxa) + b * dxl / (dxr * d1d);
+}
+
+__device__ __forceinline__ double bc_right(bool put, double xr, double r, double t) {
+  return put ? 0.0 : exp(xr) - exp(-r * t);
+}
+
+// One projected implicit stage with its tangents: on entry U holds the
+// guess, RHS / TRHS_j the right-hand sides; on exit U / TU_j the solution.
+__device__ bool tan_stage(const View& v, int n, bool put, const Coef& C, double psi_max,
+                          double t, double w) {
+  const double xl = v(TA_X, 0), xr = v(TA_X, n - 1);
+  const double bl = put ? fmax(1.0 - exp(xl), 0.0) : 0.0;
+  const double br = bc_right(put, xr, -C.c, t);
+  const double dbr_dr = put ? 0.0 : t * exp(C.c * t);  // d/dr of -exp(-r t)
+  v(TA_U, 0) = bl;
+  v(TA_U, n - 1) = br;
+  const double thr = 0.95 * psi_max;
+  // row 0: identity, rhs = left boundary value
+  double cp = 0.0, dp = bl;
+  double tcp[kTan] = {0.0, 0.0, 0.0}, tdp[kTan] = {0.0, 0.0, 0.0};
+  v(TA_CP, 0) = cp;
+  v(TA_DP, 0) = dp;
+#pragma unroll
+  for (int j = 0; j < kTan; ++j) {
+    v(TA_TCP + j, 0) = 0.0;
+    v(TA_TDP + j, 0) = 0.0;
+  }
+  for (int i = 1; i < n - 1; ++i) {
+    const double ps = v(TA_PSI, i);
+    double lo, di, up, rhs = v(TA_RHS, i);
+    double tlo[kTan], tdi[kTan], tup[kTan], trhs[kTan];
+    bool lock = false;
+    if (psi_max > 0.0 && ps > thr && v(TA_U, i) - ps < 1e-8) {
+      double d2, d1;
+      stencil(v, TA_PSI, i, d2, d1);
+      lock = C.a * d2 + C.b * d1 + C.c * ps < 0.0;
+    }
+    if (lock) {
+      lo = 0.0;
+      di = 1.0;
+      up = 0.0;
+      rhs = ps;
+#pragma unroll
+      for (int j = 0; j < kTan; ++j) tlo[j] = tdi[j] = tup[j] = trhs[j] = 0.0;
+    } else {
+      lo = -w * v(TA_JL, i);
+      di = 1.0 - w * v(TA_JD, i);
+      up = -w * v(TA_JU, i);
+      const double g2m = v(TA_G2M, i), g2i = v(TA_G2I, i), g2p = v(TA_G2P, i);
+      const double g1m = v(TA_G1M, i), g1i = v(TA_G1I, i), g1p = v(TA_G1P, i);
+#pragma unroll
+      for (int j = 0; j < kTan; ++j) {
+        const double tjl = C.da[j] * g2m + C.db[j] * g1m;
+        const double tjd = C.da[j] * g2i + C.db[j] * g1i + C.dc[j];
+        const double tju = C.da[j] * g2p + C.db[j] * g1p;
+        tlo[j] = -w * tjl;
+        tdi[j] = -w * tjd;
+        tup[j] = -w * tju;
+        trhs[j] = v(TA_TRHS + j, i);
+      }
+    }
+    const double denom = fma(-lo, cp, di);
+    if (fabs(denom) < 1e-15) return false;
+    const double inv = 1.0 / denom;
+    const double num = fma(-lo, dp, rhs);
+    const double ncp = up * inv, ndp = num * inv;
+#pragma unroll
+    for (int j = 0; j < kTan; ++j) {
+      const double tden = tdi[j] - tlo[j] * cp - lo * tcp[j];
+      const double tinv = -inv * inv * tden;
+      const double tnum = trhs[j] - tlo[j] * dp - lo * tdp[j];
+      tcp[j] = tup[j] * inv + up * tinv;
+      tdp[j] = tnum * inv + num * tinv;
+      v(TA_TCP + j, i) = tcp[j];
+      v(TA_TDP + j, i) = tdp[j];
+    }
+    cp = ncp;
+    dp = ndp;
+    v(TA_CP, i) = cp;
+    v(TA_DP, i) = dp;
+  }
+  // row n-1: identity, rhs = right boundary value
+  const double dpl = br;
+  const double tdpl[kTan] = {0.0, dbr_dr, 0.0};
+  // projected back substitution
+  double x = fmax(dpl, v(TA_PSI, n - 1));
+  double tx[kTan];
+  const bool act_l = dpl < v(TA_PSI, n - 1);
+#pragma unroll
+  for (int j = 0; j < kTan; ++j) tx[j] = act_l ? 0.0 : tdpl[j];
+  for (int i = n - 2; i >= 0; --i) {
+    const double c = v(TA_CP, i), d = v(TA_DP, i), ps = v(TA_PSI, i);
+    const double unc = fma(-c, x, d);
+    const bool act = unc < ps;
+#pragma unroll
+    for (int j = 0; j < kTan; ++j) {
+      tx[j] = act ? 0.0 : v(TA_TDP + j, i) - v(TA_TCP + j, i) * x - c * tx[j];
+      v(TA_TU + j, i) = tx[j];
+    }
+    x = act ? ps : unc;
+    v(TA_U, i) = x;
+  }
+  // boundary values again
+  v(TA_U, 0) = bl;
+  v(TA_U, n - 1) = br;
+#pragma unroll
+  for (int j = 0; j < kTan; ++j) {
+    v(TA_TU + j, 0) = 0.0;
+    v(TA_TU + j, n - 1) = tdpl[j];
+  }
+  return true;
+}
+
+// Natural cubic spline of array y on X at xs (CubicSpline::build / eval /
+// eval_derivative); uses TA_RHS, TA_CP, TA_DP as scratch.
+__device__ bool spline_at(const View& v, int n, int y, double xs, double& val, double& der) {
+  const int m = n - 2;
+  auto h = [&](int k) { return v(TA_X, k + 1) - v(TA_X, k); };
+  // tridiagonal system for the interior second-derivative coefficients
+  double cp = 0.0, dp = 0.0;
+  for (int i = 0; i < m; ++i) {
+    const int k = i + 1;
+    const double td = 2.0 * (h(k - 1) + h(k));
+    const double tl = h(k - 1), tu = h(k);
+    const double sr = (v(y, k + 1) - v(y, k)) / h(k);
+    const double sl = (v(y, k) - v(y, k - 1)) / h(k - 1);
+    const double tr = 3.0 * (sr - sl);
+    if (i == 0) {
+      if (fabs(td) < 1e-15) return false;
+      cp = tu / td;
+      dp = tr / td;
+    } else if (i < m - 1) {
+      const double denom = fma(-tl, cp, td);
+      if (fabs(denom) < 1e-15) return false;
+      const double inv = 1.0 / denom;
+      dp = fma(-tl, dp, tr) * inv;
+      cp = tu * inv;
+    } else {
+      const double denom = fma(-tl, cp, td);
+      if (fabs(denom) < 1e-15) return false;
+      dp = fma(-tl, dp, tr) / denom;
+    }
+    v(TA_CP, i) = cp;
+    v(TA_DP, i) = dp;
+  }
+  // c[0] = c[n-1] = 0, c[i+1] = solution i
+  v(TA_RHS, 0) = 0.0;
+  v(TA_RHS, n - 1) = 0.0;
+  double s = v(TA_DP, m - 1);
+  v(TA_RHS, m) = s;
+  for (int i = m - 1; i > 0; --i) {
+    s = fma(-v(TA_CP, i - 1), s, v(TA_DP, i - 1));
+    v(TA_RHS, i) = s;
+  }
+  // find_interval (lower_bound semantics)
+  int idx;
+  if (xs <= v(TA_X, 0)) {
+    idx = 0;
+  } else if (xs >= v(TA_X, n - 1)) {
+    idx = n - 2;
+  } else {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+      const int mid = lo + (hi - lo) / 2;
+      if (v(TA_X, mid) < xs) lo = mid + 1; else hi = mid;
+    }
+    idx = lo;
+    if (idx > 0 && (idx == n || v(TA_X, idx) > xs)) --idx;
+    idx = min(idx, n - 2);
+  }
+  const double hi_ = h(idx);
+  const double c0 = v(TA_RHS, idx), c1 = v(TA_RHS, idx + 1);
+  const double a = v(y, idx);
+  const double b = (v(y, idx + 1) - a) / hi_ - hi_ * (2.0 * c0 + c1) / 3.0;
+  const double d = (c1 - c0) / (3.0 * hi_);
+  const double dx = xs - v(TA_X, idx);
+  val = a + b * dx + c0 * (dx * dx) + d * (dx * dx * dx);
+  der = b + 2.0 * c0 * dx + 3.0 * d * (dx * dx);
+  return true;
+}
+
+__global__ void __launch_bounds__(128) tangent_march_kernel(const TanOpt* __restrict__ opts, int n_opts,
+                                                            const double* __restrict__ xs_all,
+                                                            double* __restrict__ ws, int nmax,
+                                                            TanOut* __restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_opts) return;
+  const TanOpt o = opts[k];
+  TanOut res{};
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  res.value = res.delta = res.dsigma = res.drate = res.ddiv = res.dstrike = nan;
+  if (o.n < 3 || o.n > nmax || o.nt < 1) {
+    res.status = MANGO_ERR_VALIDATION;
+    out[k] = res;
+    return;
+  }
+  View v{ws + static_cast<size_t>(k / 32) * TA_COUNT * nmax * 32 + (k % 32), nmax};
+  const int n = o.n;
+  const bool put = o.put != 0;
+  Coef C;
+  C.a = 0.5 * o.sigma * o.sigma;
+  C.b = o.r - o.q - C.a;
+  C.c = -o.r;
+  // j = 0: sigma, 1: rate, 2: dividend yield
+  C.da[0] = o.sigma; C.db[0] = -o.sigma; C.dc[0] = 0.0;
+  C.da[1] = 0.0;     C.db[1] = 1.0;      C.dc[1] = -1.0;
+  C.da[2] = 0.0;     C.db[2] = -1.0;     C.dc[2] = 0.0;
+  double psi_max = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double x = xs_all[o.x_off + i];
+    v(TA_X, i) = x;
+    const double ps = put ? fmax(1.0 - exp(x), 0.0) : fmax(exp(x) - 1.0, 0.0);
+    v(TA_PSI, i) = ps;
+    psi_max = i == 0 ? ps : fmax(psi_max, ps);
+  }
+  for (int i = 1; i < n - 1; ++i) {
+    const double dxl = v(TA_X, i) - v(TA_X, i - 1);
+    const double dxr = v(TA_X, i + 1) - v(TA_X, i);
+    double jl, jd, ju;
+    jac_row(dxl, dxr, C.a, C.b, C.c, jl, jd, ju);
+    v(TA_JL, i) = jl;
+    v(TA_JD, i) = jd;
+    v(TA_JU, i) = ju;
+    jac_row(dxl, dxr, 1.0, 0.0, 0.0, jl, jd, ju);
+    v(TA_G2M, i) = jl;
+    v(TA_G2I, i) = jd;
+    v(TA_G2P, i) = ju;
+    jac_row(dxl, dxr, 0.0, 1.0, 0.0, jl, jd, ju);
+    v(TA_G1M, i) = jl;
+    v(TA_G1I, i) = jd;
+    v(TA_G1P, i) = ju;
+    v(TA_LI, i) = 1.0 / dxl;
+    v(TA_RI, i) = 1.0 / dxr;
+    v(TA_CI, i) = 1.0 / (0.5 * (dxl + dxr));
+    v(TA_WL, i) = dxr / (dxl + dxr);
+    v(TA_WR, i) = dxl / (dxl + dxr);
+  }
+  // initialize: payoff, boundary values at t = 0, obstacle
+  const double bl0 = put ? fmax(1.0 - exp(v(TA_X, 0)), 0.0) : 0.0;
+  const double br0 = bc_right(put, v(TA_X, n - 1), o.r, 0.0);
+  for (int i = 0; i < n; ++i) {
+    double u = v(TA_PSI, i);
+    if (i == 0) u = bl0;
+    if (i == n - 1) u = br0;
+    v(TA_U, i) = fmax(u, v(TA_PSI, i));
+#pragma unroll
+    for (int j = 0; j < kTan; ++j) v(TA_TU + j, i) = 0.0;
+  }
+  const double dt = o.T / static_cast<double>(o.nt);
+  const double gamma = 2.0 - sqrt(2.0);
+  bool ok = true;
+  // Rannacher start: two implicit-Euler half steps
+  {
+    const double half = 0.5 * dt;
+    for (int hs = 0; hs < 2 && ok; ++hs) {
+      for (int i = 0; i < n; ++i) {
+        v(TA_RHS, i) = v(TA_U, i);
+#pragma unroll
+        for (int j = 0; j < kTan; ++j) v(TA_TRHS + j, i) = v(TA_TU + j, i);
+      }
+      ok = tan_stage(v, n, put, C, psi_max, hs == 0 ? half : dt, half);
+    }
+  }
+  double t = dt;
+  const double w1 = gamma * dt / 2.0;
+  const double omg = 1.0 - gamma, tmg = 2.0 - gamma, den = gamma * tmg;
+  const double alpha = 1.0 / den, beta = -(omg * omg) / den;
+  const double w2 = (1.0 - gamma) * dt / (2.0 - gamma);
+  for (int step = 1; ok && step < o.nt; ++step) {
+    const double t_next = static_cast<double>(step + 1) * dt;
+    // stage 1: rhs = u + w1 L(u), guess u
+    for (int i = 0; i < n; ++i) {
+      const double u = v(TA_U, i);
+      v(TA_UP, i) = u;
+      double lu = 0.0, tl[kTan] = {0.0, 0.0, 0.0};
+      if (i > 0 && i < n - 1) {
+        double d2, d1;
+        stencil(v, TA_U, i, d2, d1);
+        lu = C.a * d2 + C.b * d1 + C.c * u;
+#pragma unroll
+        for (int j = 0; j < kTan; ++j) {
+          double e2, e1;
+          stencil(v, TA_TU + j, i, e2, e1);
+          tl[j] = C.da[j] * d2 + C.db[j] * d1 + C.dc[j] * u + C.a * e2 + C.b * e1 +
+                  C.c * v(TA_TU + j, i);
+        }
+      }
+      v(TA_RHS, i) = fma(w1, lu, u);
+#pragma unroll
+      for (int j = 0; j < kTan; ++j) v(TA_TRHS + j, i) = w1 * tl[j] + v(TA_TU + j, i);
+    }
+#pragma unroll
+    for (int j = 0; j < kTan; ++j)
+      for (int i = 0; i < n; ++i) v(TA_TUP + j, i) = v(TA_TU + j, i);
+    ok = tan_stage(v, n, put, C, psi_max, t + gamma * dt, w1);
+    if (!ok) break;
+    // stage 2: rhs = alpha u* + beta u_prev, guess u*
+    for (int i = 0; i < n; ++i) {
+      v(TA_RHS, i) = fma(alpha, v(TA_U, i), beta * v(TA_UP, i));
+#pragma unroll
+      for (int j = 0; j < kTan; ++j)
+        v(TA_TRHS + j, i) = alpha * v(TA_TU + j, i) + beta * v(TA_TUP + j, i);
+    }
+    ok = tan_stage(v, n, put, C, psi_max, t_next, w2);
+    t = t_next;
+  }
+  if (!ok) {
+    res.status = MANGO_ERR_SOLVER;
+    out[k] = res;
+    return;
+  }
+  // AmericanOptionResult::value_at / delta and the tangents' splines
+  const double xs = log(o.S / o.K);
+  double s, sd;
+  if (!spline_at(v, n, TA_U, xs, s, sd)) {
+    res.status = MANGO_ERR_SOLVER;
+    out[k] = res;
+    return;
+  }
+  double tv[kTan];
+  for (int j = 0; j < kTan; ++j) {
+    double tvj, tdj;
+    if (!spline_at(v, n, TA_TU + j, xs, tvj, tdj)) {
+      res.status = MANGO_ERR_SOLVER;
+      out[k] = res;
+      return;
+    }
+    tv[j] = tvj;
+  }
+  double value, dK;
+  if (xs <= v(TA_X, 0) || xs >= v(TA_X, n - 1)) {
+    const int e = xs <= v(TA_X, 0) ? 0 : n - 1;
+    value = v(TA_U, e) * o.K;
+    for (int j = 0; j < kTan; ++j) tv[j] = v(TA_TU + j, e);
+    dK = v(TA_U, e);
+  } else {
+    const bool pos = 0.0 < s;
+    value = (pos ? s : 0.0) * o.K;
+    for (int j = 0; j < kTan; ++j) tv[j] = pos ? tv[j] : 0.0;
+    dK = pos ? s - sd : 0.0;
+  }
+  res.value = value;
+  res.delta = sd * (o.K / o.S);
+  res.dsigma = tv[0] * o.K;
+  res.drate = tv[1] * o.K;
+  res.ddiv = tv[2] * o.K;
+  res.dstrike = dK;
+  res.status = MANGO_OK;
+  out[k] = res;
+}
+
+}  // namespace
+}  // namespace mgpu
+
+using namespace mgpu;
+
+extern "C" MangoStatus mango_gpu_price_american_tangent_batch(
+    MangoGpuContext* ctx, const MangoPricingParams* params, uint64_t n, const MangoGpuGrid* grids,
+    uint64_t grid_stride, MangoGpuGreeksOut* out, uint64_t* out_failed, MangoError* err) {
+  if (!ctx || (n > 0 && (!params || !out))) {
+    set_err(err, MANGO_ERR_VALIDATION, "null context, params or out");
+    return MANGO_ERR_VALIDATION;
+  }
+  if (n > (1ull << 26)) {
+    set_err(err, MANGO_ERR_VALIDATION, "batch above 2^26 options");
+    return MANGO_ERR_VALIDATION;
+  }
+  if (out_failed) *out_failed = 0;
+  if (n == 0) return MANGO_OK;
+  DevBuf d_opts, d_x, d_ws, d_out;
+  try {
+    check(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    const int64_t nn = static_cast<int64_t>(n);
+    std::vector<Resolved> res(static_cast<size_t>(nn));
+    std::vector<std::string> msg(static_cast<size_t>(nn));
+    parallel_for(nn, [&](int64_t i) {
+      thread_local std::vector<double> scratch;
+      std::string m = validate(params[i], false);
+      if (m.empty()) {
+        MangoGpuGrid g{};
+        g.kind = MANGO_GPU_GRID_AUTO;
+        if (grids) g = grids[grid_stride ? i : 0];
+        m = resolve(params[i], g, &res[i], &scratch);
+      }
+      if (!m.empty()) {
+        res[i].status = MANGO_ERR_VALIDATION;
+        msg[i] = m;
+      }
+    });
+    std::vector<TanOpt> opts(static_cast<size_t>(nn));
+    std::vector<int64_t> xoff(static_cast<size_t>(nn) + 1, 0);
+    int nmax = 3;
+    for (int64_t i = 0; i < nn; ++i) {
+      const int64_t np = res[i].status == 0 ? res[i].spec.n : 0;
+      xoff[i + 1] = xoff[i] + np;
+      nmax = std::max<int>(nmax, static_cast<int>(np));
+    }
+    std::vector<double> xs(static_cast<size_t>(std::max<int64_t>(xoff[nn], 1)));
+    parallel_for(nn, [&](int64_t i) {
+      const MangoPricingParams& p = params[i];
+      TanOpt& o = opts[i];
+      o.S = p.spot; o.K = p.strike; o.T = p.maturity; o.sigma = p.volatility;
+      o.r = p.rate_const; o.q = p.dividend_yield;
+      o.put = p.option_type == MANGO_PUT ? 1 : 0;
+      o.x_off = xoff[i];
+      if (res[i].status == 0) {
+        generate_grid(res[i].spec, xs.data() + xoff[i]);
+        o.n = static_cast<int32_t>(res[i].spec.n);
+        o.nt = static_cast<int32_t>(res[i].nt);
+      } else {
+        o.n = 0;  // rejected on the device as invalid, overwritten below
+        o.nt = 0;
+      }
+    }, 64);
+    d_opts.get(sizeof(TanOpt) * n);
+    d_x.get(sizeof(double) * xs.size());
+    d_out.get(sizeof(TanOut) * n);
+    check(cudaMemcpyAsync(d_opts.p, opts.data(), sizeof(TanOpt) * n, cudaMemcpyHostToDevice, st), "H2D");
+    check(cudaMemcpyAsync(d_x.p, xs.data(), sizeof(double) * xs.size(), cudaMemcpyHostToDevice, st), "H2D");
+    // workspace chunks of at most 4 GiB
+    const size_t per_tile = static_cast<size_t>(TA_COUNT) * nmax * 32 * sizeof(double);
+    const int64_t tiles_per_chunk = std::max<int64_t>(1, static_cast<int64_t>((size_t{4} << 30) / per_tile));
+    const int64_t ntiles = (nn + 31) / 32;
+    const int64_t chunk_tiles = std::min(ntiles, tiles_per_chunk);
+    d_ws.get(per_tile * static_cast<size_t>(chunk_tiles));
+    for (int64_t t0 = 0; t0 < ntiles; t0 += chunk_tiles) {
+      const int64_t o0 = t0 * 32;
+      const int cnt = static_cast<int>(std::min<int64_t>(nn - o0, chunk_tiles * 32));
+      tangent_march_kernel<<<(cnt + 127) / 128, 128, 0, st>>>(
+          d_opts.as<TanOpt>() + o0, cnt, d_x.as<double>(), d_ws.as<double>(), nmax,
+          d_out.as<TanOut>() + o0);
+      check(cudaGetLastError(), "tangent_march_kernel launch");
+    }
+    std::vector<TanOut> ho(static_cast<size_t>(nn));
+    check(cudaMemcpyAsync(ho.data(), d_out.p, sizeof(TanOut) * n, cudaMemcpyDeviceToHost, st), "D2H");
+    check(cudaStreamSynchronize(st), "stream synchronize");
+    uint64_t failed = 0;
+    std::string first;
+    const double nan = std::nan("");
+    for (int64_t i = 0; i < nn; ++i) {
+      MangoGpuGreeksOut& g = out[i];
+      MangoGpuAmericanOut& b = g.base;
+      const TanOut& h = ho[i];
+      g = MangoGpuGreeksOut{};
+      b.status = res[i].status != 0 ? res[i].status : h.status;
+      b.n_space = static_cast<int32_t>(res[i].spec.n);
+      b.n_time = static_cast<int32_t>(res[i].nt);
+      b.gamma = b.theta = nan;
+      if (b.status != MANGO_OK) {
+        b.value = b.delta = g.vega = g.rho = g.dividend_rho = g.dstrike = nan;
+        if (failed++ == 0) first = msg[i].empty() ? "solver failure" : msg[i];
+        continue;
+      }
+      b.value = h.value;
+      b.delta = h.delta;
+      g.vega = h.dsigma;
+      g.rho = h.drate;
+      g.dividend_rho = h.ddiv;
+      g.dstrike = h.dstrike;
+    }
+    if (out_failed) *out_failed = failed;
+    d_opts.release(); d_x.release(); d_ws.release(); d_out.release();
+    if (failed == n) {
+      set_err(err, MANGO_ERR_VALIDATION, "every option failed: " + first);
+      return MANGO_ERR_VALIDATION;
+    }
+    return MANGO_OK;
+  } catch (const std::exception& e) {
+    d_opts.release(); d_x.release(); d_ws.release(); d_out.release();
+    set_err(err, MANGO_ERR_SOLVER, e.what());
+    return MANGO_ERR_SOLVER;
+  }
+}

@@ -1,0 +1,72 @@
+"""Forward-mode (tangent-linear) sensitivities of the march
+(mango_gpu_price_american_tangent_batch) against central differences of
+the pricing kernel on the same frozen grid (mango_gpu_price_american_greeks_
+batch), plus the value against the pricing batch.
+
+The discrete price is piecewise smooth in each parameter: a node of the
+obstacle's active set (or a deep-ITM lock row) flips at some time step when
+the parameter moves far enough, and a central difference whose bump
+straddles such a flip differs from the exact derivative at the point.  As
+the bump shrinks from 1e-5 to 1e-7 relative the differences converge onto
+the tangent, so each sensitivity is compared with the closest of the
+differences at 1e-5, 1e-6 and 1e-7 (until the smallest bump's rounding
+error dominates).
+
+Bars: value 1e-11 relative to the pricing batch (same algorithm, different
+kernel: rounding only); delta 1e-9; sensitivities on 101 x 498 grids 2e-6
+relative + 1e-6 absolute for 99% of the options and 1e-3 relative for all,
+with a median relative error at h = 1e-5 below 1e-7; on the automatic grids
+(up to 5000 steps, so more flips per bump) 2e-5 relative + 1e-5 absolute for
+95% of the options."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def inputs(pkg, n, seed, mixed):
+    rng = np.random.default_rng(seed)
+    S = np.full(n, 100.0)
+    K = rng.uniform(80, 120, n)
+    T = rng.uniform(0.1, 2.0, n)
+    sig = rng.uniform(0.1, 0.5, n)
+    r = rng.uniform(0.0, 0.08, n)
+    q = rng.uniform(0.0, 0.04, n)
+    put = (np.arange(n) % 2 == 0).astype(np.int32) if mixed else np.ones(n, np.int32)
+    return pkg.pricing_array(S, K, T, sig, r, q, put)
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_tangent_vs_central_differences(engine, pkg, mixed):
+    params = inputs(pkg, 512, 7 + mixed, mixed)
+    grid = pkg.grid_array(1, pkg.GRID_FIXED_N, 101, 498)
+    tan = engine.tangent_arrays(params, grid)
+    fds = [engine.greeks_arrays(params, grid, h) for h in (1e-5, 1e-6, 1e-7)]
+    fd = fds[0]
+    assert (tan["status"] == 0).all()
+    assert (tan["n_space"] == fd["n_space"]).all() and (tan["n_time"] == fd["n_time"]).all()
+    v = fd["value"]
+    assert np.abs(tan["value"] - v).max() <= 1e-11 * np.abs(v).max()
+    assert np.abs(tan["delta"] - fd["delta"]).max() <= 1e-9
+    for k in ("vega", "rho", "dividend_rho", "dstrike"):
+        err = np.min([np.abs(tan[k] - f[k]) for f in fds], axis=0)
+        bar = 2e-6 * np.abs(fd[k]) + 1e-6
+        assert (err <= bar).mean() >= 0.99, (k, err.max())
+        assert (err <= 1e-3 * np.abs(fd[k]) + 1e-6).all(), (k, err.max())
+        assert np.median(np.abs(tan[k] - fd[k]) / (np.abs(fd[k]) + 1e-12)) <= 1e-7, k
+    assert np.isnan(tan["gamma"]).all() and np.isnan(tan["theta"]).all()
+
+
+def test_tangent_auto_grid_and_validation(engine, pkg):
+    params = inputs(pkg, 64, 3, True)
+    params["volatility"][5] = -0.1          # invalid
+    tan = engine.tangent_arrays(params)
+    fd = engine.greeks_arrays(params, None, 1e-5)
+    ok = np.arange(64) != 5
+    assert tan["status"][5] == pkg.MANGO_ERR_VALIDATION and np.isnan(tan["vega"][5])
+    assert (tan["status"][ok] == 0).all()
+    assert np.abs(tan["value"][ok] - fd["value"][ok]).max() <= 1e-11 * np.abs(fd["value"][ok]).max()
+    fd7 = engine.greeks_arrays(params, None, 1e-7)
+    for k in ("vega", "rho", "dividend_rho", "dstrike"):
+        err = np.minimum(np.abs(tan[k][ok] - fd[k][ok]), np.abs(tan[k][ok] - fd7[k][ok]))
+        assert (err <= 2e-5 * np.abs(fd[k][ok]) + 1e-5).mean() >= 0.95, (k, err.max())

@@ -22,11 +22,17 @@
 // same frozen grid approximate, in one pass; d/dstrike follows from the final
 // spline alone because the log-moneyness grid does not depend on the strike.
 //
-// GB300 layout: one thread per option; options in tiles of 32 with every
-// per-option vector interleaved by lane (element i of array a of the
-// tile's option `lane` at ((a * nmax + i) * 32 + lane)), so a warp's loads
-// and stores of the same row coalesce into 256-byte transactions.  The
-// work is FP64 and L2/HBM streaming; no tensor cores.
+// GB300 layout: three threads per option, each marching the primal with one
+// tangent (sigma, rate or dividend yield): the primal is recomputed three
+// times, but a thread's chain of dependent row updates is half as long and
+// three times as many warps hide the memory latency of a batch of ~16k
+// options.  Threads in tiles of 32 with every per-thread vector interleaved
+// by lane (element i of array a of lane `lane` at ((a * nmax + i) * 32 +
+// lane)), so a warp's loads and stores of the same row coalesce.  The
+// time-invariant row coefficients (Jacobian rows and their parameter
+// derivatives, stencil factors) are computed once per thread, so no FP64
+// divide remains in the time loop.  FP64 and L2/HBM streaming; no tensor
+// cores.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -39,7 +45,10 @@
 namespace mgpu {
 namespace {
 
-constexpr int kTan = 3;  // sigma, rate, dividend yield
+// One tangent per thread: three threads per option carry the primal and the
+// derivative along sigma, rate and dividend yield respectively.
+constexpr int kTan = 1;
+constexpr int kDirs = 3;
 // Interleaved per-option arrays.
 enum : int {
   TA_X = 0, TA_PSI, TA_U, TA_UP, TA_RHS, TA_CP, TA_DP,
@@ -78,6 +87,7 @@ struct View {
 struct Coef {
   double a, b, c;
   double da[kTan], db[kTan], dc[kTan];
+  double dbc;  // 1 for the rate direction (the call's right boundary moves)
 };
 
 __device__ __forceinline__ void stencil(const View& v, int arr, int i, double& d2, double& d1) {
@@ -116,7 +126,7 @@ __device__ bool tan_stage(const View& v, int n, bool put, const Coef& C, double 
   const double thr = 0.95 * psi_max;
   // row 0: identity, rhs = left boundary value
   double cp = 0.0, dp = bl;
-  double tcp[kTan] = {0.0, 0.0, 0.0}, tdp[kTan] = {0.0, 0.0, 0.0};
+  double tcp[kTan] = {0.0}, tdp[kTan] = {0.0};
   v(TA_CP, 0) = cp;
   v(TA_DP, 0) = dp;
 #pragma unroll
@@ -180,7 +190,7 @@ __device__ bool tan_stage(const View& v, int n, bool put, const Coef& C, double 
   }
   // row n-1: identity, rhs = right boundary value
   const double dpl = br;
-  const double tdpl[kTan] = {0.0, dbr_dr, 0.0};
+  const double tdpl[kTan] = {C.dbc * dbr_dr};
   // projected back substitution
   double x = fmax(dpl, v(TA_PSI, n - 1));
   double tx[kTan];
@@ -283,8 +293,9 @@ __global__ void __launch_bounds__(128) tangent_march_kernel(const TanOpt* __rest
                                                             double* __restrict__ ws, int nmax,
                                                             TanOut* __restrict__ out) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n_opts) return;
-  const TanOpt o = opts[k];
+  if (k >= n_opts * kDirs) return;
+  const int dir = k % kDirs;
+  const TanOpt o = opts[k / kDirs];
   TanOut res{};
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
   res.value = res.delta = res.dsigma = res.drate = res.ddiv = res.dstrike = nan;
@@ -300,10 +311,12 @@ __global__ void __launch_bounds__(128) tangent_march_kernel(const TanOpt* __rest
   C.a = 0.5 * o.sigma * o.sigma;
   C.b = o.r - o.q - C.a;
   C.c = -o.r;
-  // j = 0: sigma, 1: rate, 2: dividend yield
-  C.da[0] = o.sigma; C.db[0] = -o.sigma; C.dc[0] = 0.0;
-  C.da[1] = 0.0;     C.db[1] = 1.0;      C.dc[1] = -1.0;
-  C.da[2] = 0.0;     C.db[2] = -1.0;     C.dc[2] = 0.0;
+  // direction 0: sigma (da = sigma, db = -sigma), 1: rate (db = 1, dc = -1),
+  // 2: dividend yield (db = -1)
+  C.da[0] = dir == 0 ? o.sigma : 0.0;
+  C.db[0] = dir == 0 ? -o.sigma : (dir == 1 ? 1.0 : -1.0);
+  C.dc[0] = dir == 1 ? -1.0 : 0.0;
+  C.dbc = dir == 1 ? 1.0 : 0.0;
   double psi_max = 0.0;
   for (int i = 0; i < n; ++i) {
     const double x = xs_all[o.x_off + i];
@@ -371,7 +384,7 @@ __global__ void __launch_bounds__(128) tangent_march_kernel(const TanOpt* __rest
     for (int i = 0; i < n; ++i) {
       const double u = v(TA_U, i);
       v(TA_UP, i) = u;
-      double lu = 0.0, tl[kTan] = {0.0, 0.0, 0.0};
+      double lu = 0.0, tl[kTan] = {0.0};
       if (i > 0 && i < n - 1) {
         double d2, d1;
         stencil(v, TA_U, i, d2, d1);
@@ -416,33 +429,28 @@ __global__ void __launch_bounds__(128) tangent_march_kernel(const TanOpt* __rest
     out[k] = res;
     return;
   }
-  double tv[kTan];
-  for (int j = 0; j < kTan; ++j) {
-    double tvj, tdj;
-    if (!spline_at(v, n, TA_TU + j, xs, tvj, tdj)) {
-      res.status = MANGO_ERR_SOLVER;
-      out[k] = res;
-      return;
-    }
-    tv[j] = tvj;
+  double tv, tdj;
+  if (!spline_at(v, n, TA_TU, xs, tv, tdj)) {
+    res.status = MANGO_ERR_SOLVER;
+    out[k] = res;
+    return;
   }
   double value, dK;
   if (xs <= v(TA_X, 0) || xs >= v(TA_X, n - 1)) {
     const int e = xs <= v(TA_X, 0) ? 0 : n - 1;
     value = v(TA_U, e) * o.K;
-    for (int j = 0; j < kTan; ++j) tv[j] = v(TA_TU + j, e);
+    tv = v(TA_TU, e);
     dK = v(TA_U, e);
   } else {
     const bool pos = 0.0 < s;
     value = (pos ? s : 0.0) * o.K;
-    for (int j = 0; j < kTan; ++j) tv[j] = pos ? tv[j] : 0.0;
+    tv = pos ? tv : 0.0;
     dK = pos ? s - sd : 0.0;
   }
+  // each thread reports the primal and its own direction in dsigma
   res.value = value;
   res.delta = sd * (o.K / o.S);
-  res.dsigma = tv[0] * o.K;
-  res.drate = tv[1] * o.K;
-  res.ddiv = tv[2] * o.K;
+  res.dsigma = tv * o.K;
   res.dstrike = dK;
   res.status = MANGO_OK;
   out[k] = res;
@@ -514,25 +522,27 @@ extern "C" MangoStatus mango_gpu_price_american_tangent_batch(
     }, 64);
     d_opts.get(sizeof(TanOpt) * n);
     d_x.get(sizeof(double) * xs.size());
-    d_out.get(sizeof(TanOut) * n);
+    d_out.get(sizeof(TanOut) * n * kDirs);
     check(cudaMemcpyAsync(d_opts.p, opts.data(), sizeof(TanOpt) * n, cudaMemcpyHostToDevice, st), "H2D");
     check(cudaMemcpyAsync(d_x.p, xs.data(), sizeof(double) * xs.size(), cudaMemcpyHostToDevice, st), "H2D");
     // workspace chunks of at most 4 GiB
     const size_t per_tile = static_cast<size_t>(TA_COUNT) * nmax * 32 * sizeof(double);
     const int64_t tiles_per_chunk = std::max<int64_t>(1, static_cast<int64_t>((size_t{4} << 30) / per_tile));
-    const int64_t ntiles = (nn + 31) / 32;
+    const int64_t ntiles = (nn * kDirs + 31) / 32;
     const int64_t chunk_tiles = std::min(ntiles, tiles_per_chunk);
     d_ws.get(per_tile * static_cast<size_t>(chunk_tiles));
-    for (int64_t t0 = 0; t0 < ntiles; t0 += chunk_tiles) {
-      const int64_t o0 = t0 * 32;
-      const int cnt = static_cast<int>(std::min<int64_t>(nn - o0, chunk_tiles * 32));
-      tangent_march_kernel<<<(cnt + 127) / 128, 128, 0, st>>>(
+    // options per chunk: their kDirs threads fill at most chunk_tiles tiles
+    const int64_t per_chunk = chunk_tiles * 32 / kDirs;
+    for (int64_t o0 = 0; o0 < nn; o0 += per_chunk) {
+      const int cnt = static_cast<int>(std::min<int64_t>(nn - o0, per_chunk));
+      tangent_march_kernel<<<(cnt * kDirs + 127) / 128, 128, 0, st>>>(
           d_opts.as<TanOpt>() + o0, cnt, d_x.as<double>(), d_ws.as<double>(), nmax,
-          d_out.as<TanOut>() + o0);
+          d_out.as<TanOut>() + o0 * kDirs);
       check(cudaGetLastError(), "tangent_march_kernel launch");
     }
-    std::vector<TanOut> ho(static_cast<size_t>(nn));
-    check(cudaMemcpyAsync(ho.data(), d_out.p, sizeof(TanOut) * n, cudaMemcpyDeviceToHost, st), "D2H");
+    std::vector<TanOut> ho(static_cast<size_t>(nn) * kDirs);
+    check(cudaMemcpyAsync(ho.data(), d_out.p, sizeof(TanOut) * n * kDirs, cudaMemcpyDeviceToHost, st),
+          "D2H");
     check(cudaStreamSynchronize(st), "stream synchronize");
     uint64_t failed = 0;
     std::string first;
@@ -540,9 +550,12 @@ extern "C" MangoStatus mango_gpu_price_american_tangent_batch(
     for (int64_t i = 0; i < nn; ++i) {
       MangoGpuGreeksOut& g = out[i];
       MangoGpuAmericanOut& b = g.base;
-      const TanOut& h = ho[i];
+      const TanOut& h = ho[kDirs * i];
+      const TanOut& hr = ho[kDirs * i + 1];
+      const TanOut& hq = ho[kDirs * i + 2];
       g = MangoGpuGreeksOut{};
-      b.status = res[i].status != 0 ? res[i].status : h.status;
+      b.status = res[i].status != 0 ? res[i].status
+                                    : (h.status != 0 ? h.status : (hr.status != 0 ? hr.status : hq.status));
       b.n_space = static_cast<int32_t>(res[i].spec.n);
       b.n_time = static_cast<int32_t>(res[i].nt);
       b.gamma = b.theta = nan;
@@ -554,8 +567,8 @@ extern "C" MangoStatus mango_gpu_price_american_tangent_batch(
       b.value = h.value;
       b.delta = h.delta;
       g.vega = h.dsigma;
-      g.rho = h.drate;
-      g.dividend_rho = h.ddiv;
+      g.rho = hr.dsigma;
+      g.dividend_rho = hq.dsigma;
       g.dstrike = h.dstrike;
     }
     if (out_failed) *out_failed = failed;

@@ -51,15 +51,16 @@ constexpr int kTan = 1;
 constexpr int kDirs = 3;
 // Interleaved per-option arrays.
 enum : int {
-  TA_X = 0, TA_PSI, TA_U, TA_UP, TA_RHS, TA_CP, TA_DP,
+  // TA_U: u at the step start, TA_US: the TR-BDF2 stage-1 solution
+  TA_X = 0, TA_PSI, TA_U, TA_US, TA_RHS, TA_CP, TA_DP,
   TA_TU,                    // + j
-  TA_TUP = TA_TU + kTan,     // + j
-  TA_TRHS = TA_TUP + kTan,   // + j
+  TA_TUS = TA_TU + kTan,     // + j
+  TA_TRHS = TA_TUS + kTan,   // + j
   TA_TCP = TA_TRHS + kTan,   // + j
   TA_TDP = TA_TCP + kTan,    // + j
   // time-invariant row coefficients, filled once per option:
   TA_JL = TA_TDP + kTan, TA_JD, TA_JU,           // assemble_jacobian's rows
-  TA_G2M, TA_G2I, TA_G2P, TA_G1M, TA_G1I, TA_G1P,  // their d/da and d/db
+  TA_TJL, TA_TJD, TA_TJU,                        // their derivative along the direction
   TA_LI, TA_RI, TA_CI, TA_WL, TA_WR,              // CenteredDifference factors
   TA_COUNT
 };
@@ -113,16 +114,16 @@ __device__ __forceinline__ double bc_right(bool put, double xr, double r, double
   return put ? 0.0 : exp(xr) - exp(-r * t);
 }
 
-// One projected implicit stage with its tangents: on entry U holds the
-// guess, RHS / TRHS_j the right-hand sides; on exit U / TU_j the solution.
+// One projected implicit stage with its tangents: array g holds the guess
+// (read by the deep-ITM lock test only), RHS / TRHS_j the right-hand sides;
+// the solution goes to array o and its tangents to to + j (o may be g: every
+// read of g precedes the back substitution).
 __device__ bool tan_stage(const View& v, int n, bool put, const Coef& C, double psi_max,
-                          double t, double w) {
+                          double t, double w, int g, int o, int to) {
   const double xl = v(TA_X, 0), xr = v(TA_X, n - 1);
   const double bl = put ? fmax(1.0 - exp(xl), 0.0) : 0.0;
   const double br = bc_right(put, xr, -C.c, t);
   const double dbr_dr = put ? 0.0 : t * exp(C.c * t);  // d/dr of -exp(-r t)
-  v(TA_U, 0) = bl;
-  v(TA_U, n - 1) = br;
   const double thr = 0.95 * psi_max;
   // row 0: identity, rhs = left boundary value
   double cp = 0.0, dp = bl;
@@ -139,7 +140,7 @@ __device__ bool tan_stage(const View& v, int n, bool put, const Coef& C, double 
     double lo, di, up, rhs = v(TA_RHS, i);
     double tlo[kTan], tdi[kTan], tup[kTan], trhs[kTan];
     bool lock = false;
-    if (psi_max > 0.0 && ps > thr && v(TA_U, i) - ps < 1e-8) {
+    if (psi_max > 0.0 && ps > thr && v(g, i) - ps < 1e-8) {
       double d2, d1;
       stencil(v, TA_PSI, i, d2, d1);
       lock = C.a * d2 + C.b * d1 + C.c * ps < 0.0;
@@ -155,16 +156,11 @@ __device__ bool tan_stage(const View& v, int n, bool put, const Coef& C, double 
       lo = -w * v(TA_JL, i);
       di = 1.0 - w * v(TA_JD, i);
       up = -w * v(TA_JU, i);
-      const double g2m = v(TA_G2M, i), g2i = v(TA_G2I, i), g2p = v(TA_G2P, i);
-      const double g1m = v(TA_G1M, i), g1i = v(TA_G1I, i), g1p = v(TA_G1P, i);
 #pragma unroll
       for (int j = 0; j < kTan; ++j) {
-        const double tjl = C.da[j] * g2m + C.db[j] * g1m;
-        const double tjd = C.da[j] * g2i + C.db[j] * g1i + C.dc[j];
-        const double tju = C.da[j] * g2p + C.db[j] * g1p;
-        tlo[j] = -w * tjl;
-        tdi[j] = -w * tjd;
-        tup[j] = -w * tju;
+        tlo[j] = -w * v(TA_TJL, i);
+        tdi[j] = -w * v(TA_TJD, i);
+        tup[j] = -w * v(TA_TJU, i);
         trhs[j] = v(TA_TRHS + j, i);
       }
     }
@@ -204,18 +200,18 @@ __device__ bool tan_stage(const View& v, int n, bool put, const Coef& C, double 
 #pragma unroll
     for (int j = 0; j < kTan; ++j) {
       tx[j] = act ? 0.0 : v(TA_TDP + j, i) - v(TA_TCP + j, i) * x - c * tx[j];
-      v(TA_TU + j, i) = tx[j];
+      v(to + j, i) = tx[j];
     }
     x = act ? ps : unc;
-    v(TA_U, i) = x;
+    v(o, i) = x;
   }
   // boundary values again
-  v(TA_U, 0) = bl;
-  v(TA_U, n - 1) = br;
+  v(o, 0) = bl;
+  v(o, n - 1) = br;
 #pragma unroll
   for (int j = 0; j < kTan; ++j) {
-    v(TA_TU + j, 0) = 0.0;
-    v(TA_TU + j, n - 1) = tdpl[j];
+    v(to + j, 0) = 0.0;
+    v(to + j, n - 1) = tdpl[j];
   }
   return true;
 }
@@ -333,14 +329,11 @@ __global__ void __launch_bounds__(128) tangent_march_kernel(const TanOpt* __rest
     v(TA_JL, i) = jl;
     v(TA_JD, i) = jd;
     v(TA_JU, i) = ju;
-    jac_row(dxl, dxr, 1.0, 0.0, 0.0, jl, jd, ju);
-    v(TA_G2M, i) = jl;
-    v(TA_G2I, i) = jd;
-    v(TA_G2P, i) = ju;
-    jac_row(dxl, dxr, 0.0, 1.0, 0.0, jl, jd, ju);
-    v(TA_G1M, i) = jl;
-    v(TA_G1I, i) = jd;
-    v(TA_G1P, i) = ju;
+    // the rows are linear in (a, b, c): the same formula on (da, db, dc)
+    jac_row(dxl, dxr, C.da[0], C.db[0], C.dc[0], jl, jd, ju);
+    v(TA_TJL, i) = jl;
+    v(TA_TJD, i) = jd;
+    v(TA_TJU, i) = ju;
     v(TA_LI, i) = 1.0 / dxl;
     v(TA_RI, i) = 1.0 / dxr;
     v(TA_CI, i) = 1.0 / (0.5 * (dxl + dxr));
@@ -370,7 +363,7 @@ __global__ void __launch_bounds__(128) tangent_march_kernel(const TanOpt* __rest
 #pragma unroll
         for (int j = 0; j < kTan; ++j) v(TA_TRHS + j, i) = v(TA_TU + j, i);
       }
-      ok = tan_stage(v, n, put, C, psi_max, hs == 0 ? half : dt, half);
+      ok = tan_stage(v, n, put, C, psi_max, hs == 0 ? half : dt, half, TA_U, TA_U, TA_TU);
     }
   }
   double t = dt;
@@ -380,40 +373,39 @@ __global__ void __launch_bounds__(128) tangent_march_kernel(const TanOpt* __rest
   const double w2 = (1.0 - gamma) * dt / (2.0 - gamma);
   for (int step = 1; ok && step < o.nt; ++step) {
     const double t_next = static_cast<double>(step + 1) * dt;
-    // stage 1: rhs = u + w1 L(u), guess u
+    // stage 1: rhs = u + w1 L(u), guess u, solution into US (u stays in U)
     for (int i = 0; i < n; ++i) {
       const double u = v(TA_U, i);
-      v(TA_UP, i) = u;
       double lu = 0.0, tl[kTan] = {0.0};
       if (i > 0 && i < n - 1) {
-        double d2, d1;
-        stencil(v, TA_U, i, d2, d1);
+        const double li = v(TA_LI, i), ri = v(TA_RI, i), ci = v(TA_CI, i);
+        const double wl = v(TA_WL, i), wr = v(TA_WR, i);
+        const double um = v(TA_U, i - 1), upl = v(TA_U, i + 1);
+        const double d2 = ((upl - u) * ri - (u - um) * li) * ci;
+        const double d1 = wl * (u - um) * li + wr * (upl - u) * ri;
         lu = C.a * d2 + C.b * d1 + C.c * u;
 #pragma unroll
         for (int j = 0; j < kTan; ++j) {
-          double e2, e1;
-          stencil(v, TA_TU + j, i, e2, e1);
-          tl[j] = C.da[j] * d2 + C.db[j] * d1 + C.dc[j] * u + C.a * e2 + C.b * e1 +
-                  C.c * v(TA_TU + j, i);
+          const double tm = v(TA_TU + j, i - 1), t0 = v(TA_TU + j, i), tp = v(TA_TU + j, i + 1);
+          const double e2 = ((tp - t0) * ri - (t0 - tm) * li) * ci;
+          const double e1 = wl * (t0 - tm) * li + wr * (tp - t0) * ri;
+          tl[j] = C.da[j] * d2 + C.db[j] * d1 + C.dc[j] * u + C.a * e2 + C.b * e1 + C.c * t0;
         }
       }
       v(TA_RHS, i) = fma(w1, lu, u);
 #pragma unroll
       for (int j = 0; j < kTan; ++j) v(TA_TRHS + j, i) = w1 * tl[j] + v(TA_TU + j, i);
     }
-#pragma unroll
-    for (int j = 0; j < kTan; ++j)
-      for (int i = 0; i < n; ++i) v(TA_TUP + j, i) = v(TA_TU + j, i);
-    ok = tan_stage(v, n, put, C, psi_max, t + gamma * dt, w1);
+    ok = tan_stage(v, n, put, C, psi_max, t + gamma * dt, w1, TA_U, TA_US, TA_TUS);
     if (!ok) break;
-    // stage 2: rhs = alpha u* + beta u_prev, guess u*
+    // stage 2: rhs = alpha u* + beta u, guess u*, solution into U
     for (int i = 0; i < n; ++i) {
-      v(TA_RHS, i) = fma(alpha, v(TA_U, i), beta * v(TA_UP, i));
+      v(TA_RHS, i) = fma(alpha, v(TA_US, i), beta * v(TA_U, i));
 #pragma unroll
       for (int j = 0; j < kTan; ++j)
-        v(TA_TRHS + j, i) = alpha * v(TA_TU + j, i) + beta * v(TA_TUP + j, i);
+        v(TA_TRHS + j, i) = alpha * v(TA_TUS + j, i) + beta * v(TA_TU + j, i);
     }
-    ok = tan_stage(v, n, put, C, psi_max, t_next, w2);
+    ok = tan_stage(v, n, put, C, psi_max, t_next, w2, TA_US, TA_U, TA_TU);
     t = t_next;
   }
   if (!ok) {

@@ -135,12 +135,33 @@ __device__ bool tan_stage(const View& v, int n, bool put, const Coef& C, double 
     v(TA_TCP + j, 0) = 0.0;
     v(TA_TDP + j, 0) = 0.0;
   }
+  // Row inputs are loaded one row ahead: none of the arrays read here is
+  // written by this sweep, so the next row's loads overlap this row's work.
+  struct RowIn {
+    double ps, rhs, gv, jl, jd, ju, tjl, tjd, tju, trhs;
+  };
+  auto load_row = [&](int i) {
+    RowIn r;
+    r.ps = v(TA_PSI, i);
+    r.rhs = v(TA_RHS, i);
+    r.gv = v(g, i);
+    r.jl = v(TA_JL, i);
+    r.jd = v(TA_JD, i);
+    r.ju = v(TA_JU, i);
+    r.tjl = v(TA_TJL, i);
+    r.tjd = v(TA_TJD, i);
+    r.tju = v(TA_TJU, i);
+    r.trhs = v(TA_TRHS, i);
+    return r;
+  };
+  RowIn nx = load_row(1);
   for (int i = 1; i < n - 1; ++i) {
-    const double ps = v(TA_PSI, i);
-    double lo, di, up, rhs = v(TA_RHS, i);
-    double tlo[kTan], tdi[kTan], tup[kTan], trhs[kTan];
+    const RowIn cu = nx;
+    if (i + 1 < n - 1) nx = load_row(i + 1);
+    const double ps = cu.ps;
+    double lo, di, up, rhs, tlo, tdi, tup, trhs;
     bool lock = false;
-    if (psi_max > 0.0 && ps > thr && v(g, i) - ps < 1e-8) {
+    if (psi_max > 0.0 && ps > thr && cu.gv - ps < 1e-8) {
       double d2, d1;
       stencil(v, TA_PSI, i, d2, d1);
       lock = C.a * d2 + C.b * d1 + C.c * ps < 0.0;
@@ -150,35 +171,29 @@ __device__ bool tan_stage(const View& v, int n, bool put, const Coef& C, double 
       di = 1.0;
       up = 0.0;
       rhs = ps;
-#pragma unroll
-      for (int j = 0; j < kTan; ++j) tlo[j] = tdi[j] = tup[j] = trhs[j] = 0.0;
+      tlo = tdi = tup = trhs = 0.0;
     } else {
-      lo = -w * v(TA_JL, i);
-      di = 1.0 - w * v(TA_JD, i);
-      up = -w * v(TA_JU, i);
-#pragma unroll
-      for (int j = 0; j < kTan; ++j) {
-        tlo[j] = -w * v(TA_TJL, i);
-        tdi[j] = -w * v(TA_TJD, i);
-        tup[j] = -w * v(TA_TJU, i);
-        trhs[j] = v(TA_TRHS + j, i);
-      }
+      lo = -w * cu.jl;
+      di = 1.0 - w * cu.jd;
+      up = -w * cu.ju;
+      rhs = cu.rhs;
+      tlo = -w * cu.tjl;
+      tdi = -w * cu.tjd;
+      tup = -w * cu.tju;
+      trhs = cu.trhs;
     }
     const double denom = fma(-lo, cp, di);
     if (fabs(denom) < 1e-15) return false;
     const double inv = 1.0 / denom;
     const double num = fma(-lo, dp, rhs);
     const double ncp = up * inv, ndp = num * inv;
-#pragma unroll
-    for (int j = 0; j < kTan; ++j) {
-      const double tden = tdi[j] - tlo[j] * cp - lo * tcp[j];
-      const double tinv = -inv * inv * tden;
-      const double tnum = trhs[j] - tlo[j] * dp - lo * tdp[j];
-      tcp[j] = tup[j] * inv + up * tinv;
-      tdp[j] = tnum * inv + num * tinv;
-      v(TA_TCP + j, i) = tcp[j];
-      v(TA_TDP + j, i) = tdp[j];
-    }
+    const double tden = tdi - tlo * cp - lo * tcp[0];
+    const double tinv = -inv * inv * tden;
+    const double tnum = trhs - tlo * dp - lo * tdp[0];
+    tcp[0] = tup * inv + up * tinv;
+    tdp[0] = tnum * inv + num * tinv;
+    v(TA_TCP, i) = tcp[0];
+    v(TA_TDP, i) = tdp[0];
     cp = ncp;
     dp = ndp;
     v(TA_CP, i) = cp;
@@ -193,15 +208,21 @@ __device__ bool tan_stage(const View& v, int n, bool put, const Coef& C, double 
   const bool act_l = dpl < v(TA_PSI, n - 1);
 #pragma unroll
   for (int j = 0; j < kTan; ++j) tx[j] = act_l ? 0.0 : tdpl[j];
+  double nc = v(TA_CP, n - 2), nd = v(TA_DP, n - 2), nps = v(TA_PSI, n - 2);
+  double ntd = v(TA_TDP, n - 2), ntc = v(TA_TCP, n - 2);
   for (int i = n - 2; i >= 0; --i) {
-    const double c = v(TA_CP, i), d = v(TA_DP, i), ps = v(TA_PSI, i);
+    const double c = nc, d = nd, ps = nps, td = ntd, tc = ntc;
+    if (i > 0) {  // next row's inputs (this sweep writes only o and to)
+      nc = v(TA_CP, i - 1);
+      nd = v(TA_DP, i - 1);
+      nps = v(TA_PSI, i - 1);
+      ntd = v(TA_TDP, i - 1);
+      ntc = v(TA_TCP, i - 1);
+    }
     const double unc = fma(-c, x, d);
     const bool act = unc < ps;
-#pragma unroll
-    for (int j = 0; j < kTan; ++j) {
-      tx[j] = act ? 0.0 : v(TA_TDP + j, i) - v(TA_TCP + j, i) * x - c * tx[j];
-      v(to + j, i) = tx[j];
-    }
+    tx[0] = act ? 0.0 : td - tc * x - c * tx[0];
+    v(to, i) = tx[0];
     x = act ? ps : unc;
     v(o, i) = x;
   }

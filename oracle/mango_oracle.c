@@ -1018,3 +1018,252 @@ int32_t mo_bspline4d_eval(const int64_t* sizes, const double* grids, const doubl
   for (int d = 0; d < 4; ++d) free(knots[d]);
   return 0;
 }
+
+/* ------------------------------------------------------------- tangent -- */
+
+/* Tangent bands of assemble_jacobian for operator coefficients (a, b, c):
+ * the rows are linear in them, so these are d(A)/d(theta) for
+ * (a, b, c) = (da, db, dc); boundary rows are constant (zero). */
+static void tangent_bands(const double* g, int64_t n, double a, double b, double c, double w,
+                          double* lower, double* diag, double* upper) {
+  for (int64_t i = 1; i < n - 1; ++i) {
+    const double dxl = g[i] - g[i - 1];
+    const double dxr = g[i + 1] - g[i];
+    const double dxa = (dxl + dxr) / 2.0;
+    const double d1d = dxl + dxr;
+    const double jl = a / (dxl * dxa) + (-b * dxr / (dxl * d1d));
+    const double jd = (-a * (1.0 / dxl + 1.0 / dxr) / dxa) + b * (dxr - dxl) / (dxl * dxr) + c;
+    const double ju = a / (dxr * dxa) + b * dxl / (dxr * d1d);
+    lower[i - 1] = -w * jl;
+    diag[i] = -w * jd;
+    upper[i] = -w * ju;
+  }
+  diag[0] = 0.0;
+  upper[0] = 0.0;
+  diag[n - 1] = 0.0;
+  lower[n - 2] = 0.0;
+}
+
+typedef struct {
+  march_t m;
+  op_t dop[3];                       /* the operator along each direction */
+  double dbc[3];                     /* 1 where the right boundary moves (rate) */
+  double *tl[3], *td[3], *tu[3], *trhs[3], *tcp[3], *tdp[3], *tw[3];
+} tmarch_t;
+
+/* One projected stage with tangents: u / tv[j] guess in, solution out. */
+static int tangent_stage(tmarch_t* T, double t, double w, double* u, double** tv,
+                         const double* rhs_in, double* const* trhs_in) {
+  march_t* m = &T->m;
+  const int64_t n = m->n;
+  apply_bc(m, u, t);
+  op_jacobian(&m->op, w, m->lower, m->diag, m->upper);
+  memcpy(m->rhs, rhs_in, sizeof(double) * (size_t)n);
+  m->rhs[0] = bc_left(m, t);
+  m->rhs[n - 1] = bc_right(m, t);
+  const double dbr = m->is_put ? 0.0 : t * exp(-m->r * t);
+  for (int j = 0; j < 3; ++j) {
+    tangent_bands(m->x, n, T->dop[j].hss, T->dop[j].r - T->dop[j].q - T->dop[j].hss, -T->dop[j].r, w,
+                  T->tl[j], T->td[j], T->tu[j]);
+    memcpy(T->trhs[j], trhs_in[j], sizeof(double) * (size_t)n);
+    T->trhs[j][0] = 0.0;
+    T->trhs[j][n - 1] = T->dbc[j] * dbr;
+  }
+  const double* psi = m->psi;
+  double psi_max = psi[0];
+  for (int64_t i = 1; i < n; ++i) if (psi_max < psi[i]) psi_max = psi[i];
+  if (psi_max > 0.0) {
+    const double thr = 0.95 * psi_max;
+    op_apply(&m->op, psi, m->lpsi, m->d2u, m->du);
+    for (int64_t i = 1; i < n - 1; ++i) {
+      if (psi[i] > thr && u[i] - psi[i] < 1e-8 && m->lpsi[i] < 0.0) {
+        m->lower[i - 1] = 0.0;
+        m->diag[i] = 1.0;
+        m->upper[i] = 0.0;
+        m->rhs[i] = psi[i];
+        for (int j = 0; j < 3; ++j) {
+          T->tl[j][i - 1] = 0.0;
+          T->td[j][i] = 0.0;
+          T->tu[j][i] = 0.0;
+          T->trhs[j][i] = 0.0;
+        }
+      }
+    }
+  }
+  /* projected Thomas and its tangent */
+  double* cp = m->ws;
+  double* dp = m->ws + n;
+  const double* lo = m->lower;
+  const double* di = m->diag;
+  const double* up = m->upper;
+  const double* r = m->rhs;
+  if (fabs(di[0]) < 1e-15) return 5;
+  cp[0] = up[0] / di[0];
+  dp[0] = r[0] / di[0];
+  for (int j = 0; j < 3; ++j) {
+    T->tcp[j][0] = (T->tu[j][0] - cp[0] * T->td[j][0]) / di[0];
+    T->tdp[j][0] = (T->trhs[j][0] - dp[0] * T->td[j][0]) / di[0];
+  }
+  for (int64_t i = 1; i < n; ++i) {
+    const double denom = fma(-lo[i - 1], cp[i - 1], di[i]);
+    if (fabs(denom) < 1e-15) return 5;
+    const double num = fma(-lo[i - 1], dp[i - 1], r[i]);
+    for (int j = 0; j < 3; ++j) {
+      const double tden = T->td[j][i] - T->tl[j][i - 1] * cp[i - 1] - lo[i - 1] * T->tcp[j][i - 1];
+      const double tnum = T->trhs[j][i] - T->tl[j][i - 1] * dp[i - 1] - lo[i - 1] * T->tdp[j][i - 1];
+      T->tdp[j][i] = (tnum - num / denom * tden) / denom;
+      if (i < n - 1) T->tcp[j][i] = (T->tu[j][i] - up[i] / denom * tden) / denom;
+    }
+    if (i < n - 1) {
+      const double inv = 1.0 / denom;
+      cp[i] = up[i] * inv;
+      dp[i] = num * inv;
+    } else {
+      dp[i] = num / denom;
+    }
+  }
+  double x = dmax(dp[n - 1], psi[n - 1]);
+  for (int j = 0; j < 3; ++j) tv[j][n - 1] = dp[n - 1] < psi[n - 1] ? 0.0 : T->tdp[j][n - 1];
+  u[n - 1] = x;
+  for (int64_t i = n - 1; i > 0; --i) {
+    const double unc = fma(-cp[i - 1], u[i], dp[i - 1]);
+    const int act = unc < psi[i - 1];
+    for (int j = 0; j < 3; ++j)
+      tv[j][i - 1] = act ? 0.0 : T->tdp[j][i - 1] - T->tcp[j][i - 1] * u[i] - cp[i - 1] * tv[j][i];
+    u[i - 1] = dmax(unc, psi[i - 1]);
+  }
+  apply_bc(m, u, t);
+  for (int j = 0; j < 3; ++j) {
+    tv[j][0] = 0.0;
+    tv[j][n - 1] = T->dbc[j] * dbr;
+  }
+  return 0;
+}
+
+int32_t mo_price_tangent_on_grid(double spot, double strike, double maturity, double sigma,
+                                 double rate, double q, int32_t is_put, const double* x,
+                                 int64_t n, int64_t nt, double* out6) {
+  if (!(spot > 0.0) || !isfinite(spot) || !(strike > 0.0) || !isfinite(strike) ||
+      !(maturity > 0.0) || !isfinite(maturity) || !isfinite(rate) || q < 0.0 ||
+      !isfinite(q) || !(sigma > 0.0) || !isfinite(sigma) || n < 3 || nt < 1)
+    return 1;
+  tmarch_t T;
+  memset(&T, 0, sizeof(T));
+  march_t* m = &T.m;
+  m->is_put = is_put;
+  m->r = rate;
+  m->x = x;
+  m->n = n;
+  if (op_init(&m->op, x, n, sigma, rate, q)) return 2;
+  /* direction operators: (a, b, c) -> (da, db, dc) with b = r - q - a, c = -r */
+  const double da[3] = {sigma, 0.0, 0.0}, db[3] = {-sigma, 1.0, -1.0}, dc[3] = {0.0, -1.0, 0.0};
+  for (int j = 0; j < 3; ++j) {
+    T.dop[j] = m->op;
+    T.dop[j].hss = da[j];
+    T.dop[j].r = -dc[j];
+    T.dop[j].q = -dc[j] - da[j] - db[j];
+    T.dbc[j] = j == 1 ? 1.0 : 0.0;
+  }
+  const size_t nn = (size_t)n;
+  double* mem = (double*)calloc(nn * (14 + 3 * 9 + 1), sizeof(double));
+  if (!mem) { op_free(&m->op); return 2; }
+  m->psi = mem;
+  m->lower = mem + n;
+  m->diag = mem + 2 * n;
+  m->upper = mem + 3 * n;
+  m->rhs = mem + 4 * n;
+  m->lpsi = mem + 5 * n;
+  m->ws = mem + 6 * n;
+  m->lu = mem + 8 * n;
+  m->d2u = mem + 9 * n;
+  m->du = mem + 10 * n;
+  double* u = mem + 11 * n;
+  double* up = mem + 12 * n;
+  double* rhs = mem + 13 * n;
+  double* base = mem + 14 * n;
+  double *tv[3], *tvp[3], *trhs[3];
+  for (int j = 0; j < 3; ++j) {
+    double* b = base + (size_t)j * 9 * nn;
+    T.tl[j] = b; T.td[j] = b + n; T.tu[j] = b + 2 * n; T.trhs[j] = b + 3 * n;
+    T.tcp[j] = b + 4 * n; T.tdp[j] = b + 5 * n;
+    tv[j] = b + 6 * n; tvp[j] = b + 7 * n; trhs[j] = b + 8 * n;
+  }
+  double* tmp = base + 27 * nn;
+  for (int64_t i = 0; i < n; ++i)
+    m->psi[i] = is_put ? dmax(1.0 - exp(x[i]), 0.0) : dmax(exp(x[i]) - 1.0, 0.0);
+  for (int64_t i = 0; i < n; ++i) u[i] = m->psi[i];
+  apply_bc(m, u, 0.0);
+  for (int64_t i = 0; i < n; ++i) u[i] = dmax(u[i], m->psi[i]);
+  const double dt = maturity / (double)nt;
+  const double gamma = 2.0 - sqrt(2.0);
+  int rc = 0;
+  const double half = 0.5 * dt;
+  for (int hs = 0; hs < 2 && !rc; ++hs) {
+    memcpy(rhs, u, sizeof(double) * nn);
+    for (int j = 0; j < 3; ++j) memcpy(trhs[j], tv[j], sizeof(double) * nn);
+    rc = tangent_stage(&T, hs == 0 ? half : dt, half, u, tv, rhs, trhs);
+  }
+  double t = dt;
+  for (int64_t step = 1; !rc && step < nt; ++step) {
+    const double t_next = (double)(step + 1) * dt;
+    memcpy(up, u, sizeof(double) * nn);
+    for (int j = 0; j < 3; ++j) memcpy(tvp[j], tv[j], sizeof(double) * nn);
+    const double w1 = gamma * dt / 2.0;
+    op_apply(&m->op, up, m->lu, m->d2u, m->du);
+    for (int64_t i = 0; i < n; ++i) rhs[i] = fma(w1, m->lu[i], up[i]);
+    for (int j = 0; j < 3; ++j) {
+      op_apply(&T.dop[j], up, tmp, m->d2u, m->du);           /* dL(u) */
+      op_apply(&m->op, tvp[j], m->lu, m->d2u, m->du);         /* L(du) */
+      for (int64_t i = 0; i < n; ++i) trhs[j][i] = w1 * (tmp[i] + m->lu[i]) + tvp[j][i];
+    }
+    rc = tangent_stage(&T, t + gamma * dt, w1, u, tv, rhs, trhs);
+    if (rc) break;
+    const double omg = 1.0 - gamma, tmg = 2.0 - gamma, den = gamma * tmg;
+    const double alpha = 1.0 / den, beta = -(omg * omg) / den;
+    const double w2 = (1.0 - gamma) * dt / (2.0 - gamma);
+    for (int64_t i = 0; i < n; ++i) rhs[i] = fma(alpha, u[i], beta * up[i]);
+    for (int j = 0; j < 3; ++j)
+      for (int64_t i = 0; i < n; ++i) trhs[j][i] = alpha * tv[j][i] + beta * tvp[j][i];
+    rc = tangent_stage(&T, t_next, w2, u, tv, rhs, trhs);
+    t = t_next;
+  }
+  if (!rc) {
+    const double xs = log(spot / strike);
+    spline_t sp;
+    if (spline_build(&sp, x, u, n)) rc = 5;
+    if (!rc) {
+      const double s = spline_eval(&sp, xs), sd = spline_deriv(&sp, xs);
+      double tvv[3];
+      for (int j = 0; j < 3 && !rc; ++j) {
+        spline_t st;
+        if (spline_build(&st, x, tv[j], n)) rc = 5;
+        else tvv[j] = spline_eval(&st, xs);
+        spline_free(&st);
+      }
+      if (!rc) {
+        double value, dK;
+        if (xs <= x[0] || xs >= x[n - 1]) {
+          const int64_t e = xs <= x[0] ? 0 : n - 1;
+          value = u[e] * strike;
+          for (int j = 0; j < 3; ++j) tvv[j] = tv[j][e];
+          dK = u[e];
+        } else {
+          const int pos = 0.0 < s;
+          value = (pos ? s : 0.0) * strike;
+          for (int j = 0; j < 3; ++j) tvv[j] = pos ? tvv[j] : 0.0;
+          dK = pos ? s - sd : 0.0;
+        }
+        out6[0] = value;
+        out6[1] = sd * (strike / spot);
+        out6[2] = tvv[0] * strike;
+        out6[3] = tvv[1] * strike;
+        out6[4] = tvv[2] * strike;
+        out6[5] = dK;
+      }
+    }
+    spline_free(&sp);
+  }
+  free(mem);
+  op_free(&m->op);
+  return rc;
+}

@@ -63,6 +63,16 @@ int32_t mo_price_on_grid(double spot, double strike, double maturity, double sig
                          const double* x, int64_t nx, int64_t nt, int32_t rannacher,
                          double* out4, double* u_final, double* u_prev);
 
+/* Forward-mode derivative of mo_price_on_grid (Rannacher start) along
+ * volatility, rate and dividend yield, the primal's active obstacle set and
+ * deep-ITM lock rows frozen; dV/dK from the final spline on the
+ * strike-independent grid.  out6 = {value, delta, dV/dsigma, dV/drate,
+ * dV/dq, dV/dK}.  The checker of the GPU tangent march.  Returns as
+ * mo_price_on_grid. */
+int32_t mo_price_tangent_on_grid(double spot, double strike, double maturity, double sigma,
+                                 double rate, double dividend_yield, int32_t is_put,
+                                 const double* x, int64_t nx, int64_t nt, double* out6);
+
 /* Batch over options, each with its own grid rule (nx > 0: estimate_pde_grid
  * with min = max = nx, and nt steps; nx == 0: default auto grid).  OpenMP over
  * options when compiled with -fopenmp, n_threads <= 0 means all.

@@ -70,6 +70,15 @@ def price_on_grid(S, K, T, sigma, r, q, is_put, x, nt, rannacher=1):
     return rc, out, u, up
 
 
+def price_tangent_on_grid(S, K, T, sigma, r, q, is_put, x, nt):
+    """mo_price_tangent_on_grid: {value, delta, dV/dsigma, dV/drate, dV/dq, dV/dK}."""
+    x = np.ascontiguousarray(x, np.float64)
+    out = np.full(6, np.nan)
+    rc = lib().mo_price_tangent_on_grid(c(S), c(K), c(T), c(sigma), c(r), c(q), ctypes.c_int32(int(is_put)),
+                                        P(x), ctypes.c_int64(x.size), ctypes.c_int64(int(nt)), P(out))
+    return rc, out
+
+
 def grid(S, K, T, sigma, nx=0):
     acc = Accuracy()
     lib().mo_default_accuracy(ctypes.byref(acc))

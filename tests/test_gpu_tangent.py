@@ -70,3 +70,24 @@ def test_tangent_auto_grid_and_validation(engine, pkg):
     for k in ("vega", "rho", "dividend_rho", "dstrike"):
         err = np.minimum(np.abs(tan[k][ok] - fd[k][ok]), np.abs(tan[k][ok] - fd7[k][ok]))
         assert (err <= 2e-5 * np.abs(fd[k][ok]) + 1e-5).mean() >= 0.95, (k, err.max())
+
+
+def test_tangent_vs_oracle_tangent(engine, pkg, oracle):
+    """The GPU march and the oracle's restatement of the same forward-mode
+    derivative on the same 101 x 498 grids.  Bars: value 1e-11, the
+    sensitivities 1e-8 relative + 1e-9 (rounding of the precomputed row
+    coefficients against the per-stage ones, through 998 stages)."""
+    params = inputs(pkg, 24, 21, True)
+    grid = pkg.grid_array(1, pkg.GRID_FIXED_N, 101, 498)
+    tan = engine.tangent_arrays(params, grid)
+    assert (tan["status"] == 0).all()
+    for i in range(params.size):
+        x, _ = pkg.resolve_grid(params[i:i + 1], pkg.FixedGrid(101, 498))
+        p = params[i]
+        rc, t6 = oracle.price_tangent_on_grid(p["spot"], p["strike"], p["maturity"], p["volatility"],
+                                              p["rate_const"], p["dividend_yield"], p["option_type"], x, 498)
+        assert rc == 0
+        assert abs(tan["value"][i] - t6[0]) <= 1e-11 * abs(t6[0]) + 1e-13, i
+        assert abs(tan["delta"][i] - t6[1]) <= 1e-9, i
+        for col, k in ((2, "vega"), (3, "rho"), (4, "dividend_rho"), (5, "dstrike")):
+            assert abs(tan[k][i] - t6[col]) <= 1e-8 * abs(t6[col]) + 1e-9, (i, k, tan[k][i], t6[col])

@@ -455,6 +455,22 @@ def bench_table(pkg, eng, torch, stream, nq, fp64_peak):
         "value": nrec / t_price, "unit": "prices/s (device-resident)",
         "e2e": {"value": nrec / t_price_e2e, "unit": "prices/s", "h2d_bytes_per_step": int(recs.nbytes),
                 "d2h_bytes_per_step": int(host_vals.nbytes)}}
+    # delta / gamma / theta / rho on the table (mango_gpu_price_table_greeks),
+    # end to end from host records; in-range records so every status is 0.
+    ng = min(nrec, 1_000_000)
+    grng = np.random.default_rng(13)
+    gp = pkg.pricing_array(np.full(ng, 100.0), 100.0 / np.exp(grng.uniform(-0.3, 0.2, ng)),
+                           grng.uniform(0.1, 1.9, ng), grng.uniform(0.1, 0.7, ng), grng.uniform(0.005, 0.075, ng),
+                           0.0, 1)
+    table.greeks_arrays(gp)
+    t0 = time.perf_counter()
+    g4, gst = table.greeks_arrays(gp)
+    t_g = time.perf_counter() - t0
+    query["table_greeks"] = {
+        "workload": f"{ng} American put delta/gamma/theta/rho from the 50x30x20x10 EEP table "
+                    "(analytic spline partials + closed-form European Greeks)",
+        "value": ng / t_g, "unit": "records with 4 Greeks/s (end to end)",
+        "failed": int(np.count_nonzero(gst))}
     # Interpolated IV on the table (InterpolatedIVSolver::solve_batch): quotes
     # priced from the table at seeded vols, solved back on the device.
     niv = min(nq, 1_000_000)

@@ -29,10 +29,11 @@
 // options.  Threads in tiles of 32 with every per-thread vector interleaved
 // by lane (element i of array a of lane `lane` at ((a * nmax + i) * 32 +
 // lane)), so a warp's loads and stores of the same row coalesce.  The
-// time-invariant row coefficients (Jacobian rows and their parameter
-// derivatives, stencil factors) are computed once per thread, so no FP64
-// divide remains in the time loop.  FP64 and L2/HBM streaming; no tensor
-// cores.
+// time-invariant row coefficients (Jacobian rows, their derivative along the
+// thread's direction, stencil factors) are computed once per thread, so the
+// only FP64 divide left in the time loop is the Thomas reciprocal of each
+// row.  Bound by FP64 issue and HBM streaming of the per-thread state; no
+// tensor cores.
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -26,7 +26,8 @@
 // tangent (sigma, rate or dividend yield): the primal is recomputed three
 // times, but a thread's chain of dependent row updates is half as long and
 // three times as many warps hide the memory latency of a batch of ~16k
-// options.  Threads in tiles of 32 with every per-thread vector interleaved
+// options.  A warp holds one direction of 32 consecutive options.  Threads
+// in tiles of 32 (one per warp) with every per-thread vector interleaved
 // by lane (element i of array a of lane `lane` at ((a * nmax + i) * 32 +
 // lane)), so a warp's loads and stores of the same row coalesce.  The
 // time-invariant row coefficients (Jacobian rows, their derivative along the
@@ -310,19 +311,23 @@ __global__ void __launch_bounds__(128) tangent_march_kernel(const TanOpt* __rest
                                                             const double* __restrict__ xs_all,
                                                             double* __restrict__ ws, int nmax,
                                                             TanOut* __restrict__ out) {
+  // warp w holds direction w % kDirs of options (w / kDirs) * 32 + lane
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n_opts * kDirs) return;
-  const int dir = k % kDirs;
-  const TanOpt o = opts[k / kDirs];
+  const int w = k / 32, lane = k % 32;
+  const int dir = w % kDirs;
+  const int oi = (w / kDirs) * 32 + lane;
+  if (oi >= n_opts) return;
+  const int ko = oi * kDirs + dir;  // result slot
+  const TanOpt o = opts[oi];
   TanOut res{};
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
   res.value = res.delta = res.dsigma = res.drate = res.ddiv = res.dstrike = nan;
   if (o.n < 3 || o.n > nmax || o.nt < 1) {
     res.status = MANGO_ERR_VALIDATION;
-    out[k] = res;
+    out[ko] = res;
     return;
   }
-  View v{ws + static_cast<size_t>(k / 32) * TA_COUNT * nmax * 32 + (k % 32), nmax};
+  View v{ws + static_cast<size_t>(w) * TA_COUNT * nmax * 32 + lane, nmax};
   const int n = o.n;
   const bool put = o.put != 0;
   Coef C;
@@ -432,7 +437,7 @@ __global__ void __launch_bounds__(128) tangent_march_kernel(const TanOpt* __rest
   }
   if (!ok) {
     res.status = MANGO_ERR_SOLVER;
-    out[k] = res;
+    out[ko] = res;
     return;
   }
   // AmericanOptionResult::value_at / delta and the tangents' splines
@@ -440,13 +445,13 @@ __global__ void __launch_bounds__(128) tangent_march_kernel(const TanOpt* __rest
   double s, sd;
   if (!spline_at(v, n, TA_U, xs, s, sd)) {
     res.status = MANGO_ERR_SOLVER;
-    out[k] = res;
+    out[ko] = res;
     return;
   }
   double tv, tdj;
   if (!spline_at(v, n, TA_TU, xs, tv, tdj)) {
     res.status = MANGO_ERR_SOLVER;
-    out[k] = res;
+    out[ko] = res;
     return;
   }
   double value, dK;
@@ -467,7 +472,7 @@ __global__ void __launch_bounds__(128) tangent_march_kernel(const TanOpt* __rest
   res.dsigma = tv * o.K;
   res.dstrike = dK;
   res.status = MANGO_OK;
-  out[k] = res;
+  out[ko] = res;
 }
 
 }  // namespace
@@ -542,14 +547,15 @@ extern "C" MangoStatus mango_gpu_price_american_tangent_batch(
     // workspace chunks of at most 4 GiB
     const size_t per_tile = static_cast<size_t>(TA_COUNT) * nmax * 32 * sizeof(double);
     const int64_t tiles_per_chunk = std::max<int64_t>(1, static_cast<int64_t>((size_t{4} << 30) / per_tile));
-    const int64_t ntiles = (nn * kDirs + 31) / 32;
-    const int64_t chunk_tiles = std::min(ntiles, tiles_per_chunk);
+    const int64_t ntiles = (nn + 31) / 32 * kDirs;
+    const int64_t chunk_tiles = std::min(ntiles, std::max<int64_t>(tiles_per_chunk, kDirs));
     d_ws.get(per_tile * static_cast<size_t>(chunk_tiles));
     // options per chunk: their kDirs threads fill at most chunk_tiles tiles
-    const int64_t per_chunk = chunk_tiles * 32 / kDirs;
+    const int64_t per_chunk = std::max<int64_t>(1, chunk_tiles / kDirs) * 32;
     for (int64_t o0 = 0; o0 < nn; o0 += per_chunk) {
       const int cnt = static_cast<int>(std::min<int64_t>(nn - o0, per_chunk));
-      tangent_march_kernel<<<(cnt * kDirs + 127) / 128, 128, 0, st>>>(
+      const int threads = (cnt + 31) / 32 * 32 * kDirs;
+      tangent_march_kernel<<<(threads + 127) / 128, 128, 0, st>>>(
           d_opts.as<TanOpt>() + o0, cnt, d_x.as<double>(), d_ws.as<double>(), nmax,
           d_out.as<TanOut>() + o0 * kDirs);
       check(cudaGetLastError(), "tangent_march_kernel launch");

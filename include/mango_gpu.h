@@ -238,14 +238,14 @@ MangoStatus mango_gpu_price_american_batch_shared(MangoGpuContext* ctx,
  * pricing.  config NULL or zero fields => brent_tol_abs 1e-6, max_iter 100.
  * Slot status: MANGO_OK, _VALIDATION, _ARBITRAGE (price outside
  * [intrinsic, upper bound]), _BRACKETING, _NO_CONVERGENCE, _SOLVER.  Each
- * Brent evaluation re-prices the quotes still iterating on the device; the
- * launch sequence of one evaluation is a CUDA graph replayed per iteration,
- * and the quotes still iterating are re-packed into full tiles as others
- * finish.  After the call, mango_gpu_last_stats reports options = quote
- * evaluations (marches), tiles = evaluations (graph replays), algo_flops =
- * their work, march_ms = device time of the evaluations, prep_ms = host
- * time of the re-packing, host_prep_ms = validation and grid generation,
- * total_ms = the whole call. */
+ * evaluation re-prices the quotes still iterating on the device: the host
+ * re-packs their trial points into full tiles (finished quotes leave the
+ * working set), then one gather, setup, march, outputs and root-finder step
+ * launch run on the context's stream.  After the call, mango_gpu_last_stats
+ * reports options = quote evaluations (marches), tiles = evaluations (rounds
+ * of those launches), algo_flops = their work, march_ms = device time of the
+ * evaluations, prep_ms = host time of the re-packing, host_prep_ms =
+ * validation and grid generation, total_ms = the whole call. */
 MangoStatus mango_gpu_solve_iv_batch(MangoGpuContext* ctx, const MangoIvQuery* queries,
                                      uint64_t n, const MangoGpuGrid* grids, uint64_t grid_stride,
                                      const MangoIvConfig* config, MangoIvBatchSlot* out,
@@ -558,7 +558,9 @@ MangoStatus mango_gpu_fp64_probe(MangoGpuContext* ctx, double* tflops, MangoErro
  * the array's address (make it outside any stream capture).  Calls share
  * the array: GPU work of overlapping calls races, so keep them on one stream
  * or synchronise between them.  stream may be NULL (legacy default stream).
- * No counterpart in the reference ABI. */
+ * The calling thread's current device is restored before the call returns.
+ * A call rejected or failed as a whole still fills every slot (NaN results,
+ * the call's status).  No counterpart in the reference ABI. */
 MangoStatus mango_gpu_price_american_batch_noalloc(int32_t device, void* stream,
                                                    const MangoPricingParams* params, uint64_t n,
                                                    const MangoGpuGrid* grids, uint64_t grid_stride,

@@ -87,11 +87,22 @@ def build_oracle(force: bool = False) -> pathlib.Path:
     return ORACLE_LIB
 
 
+def reference_dir() -> pathlib.Path | None:
+    """The reference tree: $MANGO_REFERENCE_DIR, else a checkout named
+    `reference` beside this repository; None when neither exists (the GPU
+    host never has it)."""
+    env = os.environ.get("MANGO_REFERENCE_DIR")
+    for cand in ([pathlib.Path(env)] if env else []) + [ROOT.parent / "reference"]:
+        if (cand / "src" / "option" / "american_option.cpp").exists():
+            return cand
+    return None
+
+
 def build_reference_oracle() -> pathlib.Path | None:
     """Compile the reference's own sources into oracle/_ref when the
-    reference tree is present (never on the GPU host)."""
-    ref = pathlib.Path(os.environ.get("MANGO_REFERENCE_DIR", "/root/reference"))
-    if not (ref / "src" / "option" / "american_option.cpp").exists():
+    reference tree is present."""
+    ref = reference_dir()
+    if ref is None:
         return None
     _run(["make", "-s", "-C", str(ORACLE_DIR / "ref"), f"REF={ref}", "-j8"])
     return ORACLE_DIR / "_ref" / "libmango_ref.so"

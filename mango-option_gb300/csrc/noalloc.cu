@@ -18,7 +18,9 @@
 //
 // Set-up: the first call on a device (with that device current) looks up
 // the array's device address with cudaGetSymbolAddress; make that first call
-// outside any stream capture.  Every call shares the array and the static
+// outside any stream capture.  The calling thread's current device is the
+// same after the call as before it.  A call that fails as a whole (a limit,
+// a CUDA error) still writes every slot: NaN results and the call's status.  Every call shares the array and the static
 // host staging buffers: calls are serialised on the host by a mutex, but two
 // calls whose GPU work overlaps (different streams) race on the array, so
 // order them on one stream or synchronise between them.  Whatever must start
@@ -110,18 +112,24 @@ const char* resolve_grid(const MangoPricingParams& p, const MangoGpuGrid& g, Gri
   const Accuracy def = default_accuracy();
   switch (g.kind) {
     case MANGO_GPU_GRID_AUTO:
-    case MANGO_GPU_GRID_FIXED_N: {
+    case MANGO_GPU_GRID_FIXED_N:
+    case MANGO_GPU_GRID_FIXED_N_AT_VOL: {
       Accuracy a = def;
-      if (g.kind == MANGO_GPU_GRID_FIXED_N) {
+      const bool pinned = g.kind != MANGO_GPU_GRID_AUTO;
+      if (pinned) {
         if (g.n_space < 3 || g.n_time < 0) return "grid: n_space >= 3 and n_time >= 0 required";
         if (g.n_space > kMaxSpace) return "grid: n_space above the no-allocation limit";
         a.min_points = a.max_points = g.n_space;
       }
+      // FIXED_N_AT_VOL sizes the grid at the volatility in g.alpha instead
+      // of the option's own, as the allocating batch does.
+      const double vol = g.kind == MANGO_GPU_GRID_FIXED_N_AT_VOL ? g.alpha : p.volatility;
+      if (!(vol > 0.0) || !std::isfinite(vol)) return "grid: sizing volatility must be > 0";
       int64_t nt_auto = 0;
-      estimate_grid(p.spot, p.strike, p.maturity, p.volatility, a, spec, &nt_auto,
-                    g_host.scratch, static_cast<int64_t>(sizeof(g_host.scratch) / sizeof(double)));
+      estimate_grid(p.spot, p.strike, p.maturity, vol, a, spec, &nt_auto, g_host.scratch,
+                    static_cast<int64_t>(sizeof(g_host.scratch) / sizeof(double)));
       if (spec->n > kMaxSpace) return "grid: n_space above the no-allocation limit";
-      *nt = (g.kind == MANGO_GPU_GRID_FIXED_N && g.n_time > 0) ? g.n_time : nt_auto;
+      *nt = (pinned && g.n_time > 0) ? g.n_time : nt_auto;
       break;
     }
     case MANGO_GPU_GRID_SINH:
@@ -160,6 +168,30 @@ bool cuda_ok(cudaError_t e, const char* what, MangoError* err) {
   return false;
 }
 
+// Every slot NaN with one status: a call that fails as a whole never leaves
+// the caller's slots holding stale results.
+void fail_all(MangoGpuAmericanOut* out, uint64_t n, int32_t status, uint64_t* out_failed) {
+  for (uint64_t i = 0; i < n; ++i) {
+    MangoGpuAmericanOut& o = out[i];
+    o.value = o.delta = o.gamma = o.theta = NAN;
+    o.status = status;
+    o.n_space = o.n_time = 0;
+    o.reserved = 0;
+  }
+  if (out_failed) *out_failed = n;
+}
+
+// Restores the calling thread's current device on every return path.
+struct DeviceGuard {
+  int prev = -1;
+  DeviceGuard() {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
 }  // namespace noalloc
 }  // namespace mgpu
 
@@ -177,26 +209,33 @@ extern "C" MangoStatus mango_gpu_price_american_batch_noalloc(
   if (n > static_cast<uint64_t>(kMaxOptions)) {
     set_err(err, MANGO_ERR_VALIDATION,
             "no-allocation entry point: more than 4096 options in one call");
+    fail_all(out, n, MANGO_ERR_VALIDATION, out_failed);
     return MANGO_ERR_VALIDATION;
   }
   if (device < 0 || device >= kMaxDevices) {
     set_err(err, MANGO_ERR_VALIDATION, "invalid device index");
+    fail_all(out, n, MANGO_ERR_VALIDATION, out_failed);
     return MANGO_ERR_VALIDATION;
   }
   std::lock_guard<std::mutex> lock(g_mutex);
-  if (!cuda_ok(cudaSetDevice(device), "cudaSetDevice", err)) return MANGO_ERR_SOLVER;
+  const DeviceGuard device_guard;
+  auto cuda_fail = [&]() {
+    fail_all(out, n, MANGO_ERR_SOLVER, out_failed);
+    return MANGO_ERR_SOLVER;
+  };
+  if (!cuda_ok(cudaSetDevice(device), "cudaSetDevice", err)) return cuda_fail();
   // Once per device, with that device current: the array's device address.
   if (!g_scratch_ptr[device]) {
     void* ptr = nullptr;
     if (!cuda_ok(cudaGetSymbolAddress(&ptr, g_scratch), "cudaGetSymbolAddress", err))
-      return MANGO_ERR_SOLVER;
+      return cuda_fail();
     int sms = 0, bps = 0;
     if (!cuda_ok(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device),
                  "cudaDeviceGetAttribute", err))
-      return MANGO_ERR_SOLVER;
+      return cuda_fail();
     if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, march_kernel, 128, 0),
                  "occupancy", err))
-      return MANGO_ERR_SOLVER;
+      return cuda_fail();
     g_num_sms[device] = sms;
     g_blocks_per_sm[device] = std::max(1, bps);
     g_scratch_ptr[device] = ptr;
@@ -255,6 +294,7 @@ extern "C" MangoStatus mango_gpu_price_american_batch_noalloc(
   if (rows > kMaxRows) {
     set_err(err, MANGO_ERR_VALIDATION,
             "no-allocation entry point: batch needs more than 131072 grid rows");
+    fail_all(out, n, MANGO_ERR_VALIDATION, out_failed);
     return MANGO_ERR_VALIDATION;
   }
   for (int32_t t = 0; t < ntiles; ++t) {
@@ -307,7 +347,7 @@ extern "C" MangoStatus mango_gpu_price_american_batch_noalloc(
                                  cudaMemcpyHostToDevice, st),
                  "H2D tiles", err) ||
         !cuda_ok(cudaMemsetAsync(d_queue, 0, sizeof(int32_t) * 4, st), "clear queue", err))
-      return MANGO_ERR_SOLVER;
+      return cuda_fail();
     const int threads = ntiles * kTile;
     prep_kernel<<<(threads + 127) / 128, 128, 0, st>>>(d_tiles, ntiles, d_opts, d_xs, d_pool,
                                                        d_flags, d_mode, mc);
@@ -325,7 +365,7 @@ extern "C" MangoStatus mango_gpu_price_american_batch_noalloc(
                                  cudaMemcpyDeviceToHost, st),
                  "D2H status", err) ||
         !cuda_ok(cudaStreamSynchronize(st), "stream synchronize", err))
-      return MANGO_ERR_SOLVER;
+      return cuda_fail();
   }
 
   uint64_t failed = 0;

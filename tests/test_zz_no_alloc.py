@@ -78,9 +78,44 @@ def test_noalloc_rejects_requests_beyond_its_limits(pkg):
     st, _, _, msg = _call(pkg, f, params, grids)
     assert st == pkg.MANGO_ERR_VALIDATION and "4096" in msg
     big = pkg.grid_array(64, pkg.GRID_FIXED_N, 3001, 10)
-    st, _, _, msg = _call(pkg, f, params[:64].copy(), big)
+    st, out, failed, msg = _call(pkg, f, params[:64].copy(), big)
     assert st == pkg.MANGO_ERR_VALIDATION and "131072" in msg
+    # a call refused as a whole still fills every slot
+    assert failed == 64 and (out["status"] == pkg.MANGO_ERR_VALIDATION).all()
+    assert np.isnan(out["value"]).all() and (out["n_space"] == 0).all()
     # per-slot validation still works inside the limits
     p = pkg.pricing_array([100.0, -5.0], [100.0, 100.0], 1.0, 0.2, 0.05, 0.0, 1)
     st, out, failed, _ = _call(pkg, f, p, pkg.grid_array(2, pkg.GRID_FIXED_N, 101, 50))
     assert st == 0 and failed == 1 and out["status"].tolist() == [0, 1]
+
+
+def test_noalloc_grid_sized_at_a_given_volatility(pkg):
+    """MANGO_GPU_GRID_FIXED_N_AT_VOL (the grid an IV caller fixes) gives the
+    allocating entry point's results."""
+    f = _noalloc(pkg)
+    params, _ = _workload(pkg, 96, 12)
+    grids = pkg.grid_array(96, pkg.GRID_FIXED_N_AT_VOL, 101, 200, alpha=np.linspace(0.1, 0.6, 96))
+    with pkg.Engine(0) as eng:
+        want = eng.price_arrays(params, grids)
+    st, got, failed, msg = _call(pkg, f, params, grids)
+    assert st == 0 and failed == 0, msg
+    assert (got["n_space"] == want["n_space"]).all() and (got["n_time"] == want["n_time"]).all()
+    for k in ("value", "delta", "gamma", "theta"):
+        assert np.allclose(got[k], want[k], rtol=RTOL, atol=ATOL), k
+
+
+def test_noalloc_allocates_no_device_memory(pkg):
+    """Once the first call has set up the array, calls of different sizes
+    leave the device's free memory unchanged."""
+    torch = pytest.importorskip("torch")
+    f = _noalloc(pkg)
+    params, grids = _workload(pkg, 512, 7)
+    assert _call(pkg, f, params, grids)[0] == 0  # set-up call
+    torch.cuda.mem_get_info(0)
+    free0, _ = torch.cuda.mem_get_info(0)
+    for n, seed in ((512, 8), (64, 9), (300, 10), (1, 11)):
+        p, g = _workload(pkg, n, seed)
+        st, _, failed, msg = _call(pkg, f, p, g)
+        assert st == 0 and failed == 0, msg
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0

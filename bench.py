@@ -211,34 +211,81 @@ def make_iv_workload(pkg, n, seed=4242):
     return S, K, T, r, q, vt, put, grids
 
 
+VEGA_FLOOR = 1e-4  # the reference InterpolatedIVSolver's default vega_threshold
+
+
 def bench_iv(pkg, eng, n):
+    """Batched IV (262,144 quotes): the reference's Brent, the secant and
+    Newton on the exact discrete vega, end to end through
+    mango_gpu_solve_iv_batch_method.  The quotes are priced at their true vol
+    with the forward-mode march (which also gives the discrete vega at the true
+    vol) on each quote's 101 x 498 grid sized at that vol -- the grid the
+    synthetic generator used; inverting on the generator's grid makes the
+    round trip exact, so |sigma - sigma_true| measures the root finder alone.
+    (A caller without the true vol sizes every grid at some other fixed vol;
+    the solver's accuracy on its own discrete objective is the same.)
+
+    Accuracy per arm, over the quotes outside two named classes, each counted:
+    validation/arbitrage statuses (the price is not a valid American price
+    for the quote, e.g. below intrinsic after rounding), and a discrete vega
+    at the true vol below VEGA_FLOOR (the volatility barely moves the price,
+    so it is not determined to 1e-6 by a price; the reference's
+    InterpolatedIVSolver rejects such quotes for the same reason).  A quote
+    outside 1e-6 whose returned vol re-prices to the quote (another root of
+    a non-monotone objective) is counted separately."""
     S, K, T, r, q, vt, put, grids = make_iv_workload(pkg, n)
-    px = eng.price_arrays(pkg.pricing_array(S, K, T, vt, r, q, put), grids)
-    quotes = pkg.query_array(S, K, T, r, q, put, px["value"])
+    truth = eng.tangent_arrays(pkg.pricing_array(S, K, T, vt, r, q, put), grids, vega_only=True)
+    px = truth["value"]
+    quotes = pkg.query_array(S, K, T, r, q, put, px)
+    low_vega = np.abs(truth["vega"]) < VEGA_FLOOR
     res = {"workload": f"{n} American quotes (3/4 puts), true vol~U[0.05,0.8], K/S~U[0.8,1.2], "
-                       f"T~U[0.02,2], 101x498 per-quote grids, prices from the forward solver"}
-    for name, method in (("brent", pkg.IV_BRENT), ("secant", pkg.IV_SECANT)):
+                       f"T~U[0.02,2], 101x498 per-quote grids sized at the true vol (the generator's "
+                       f"grid), prices from the forward solver",
+           "vega_floor": VEGA_FLOOR}
+    arms = (("brent", pkg.IV_BRENT, "Brent, the reference iterate sequence"),
+            ("secant", pkg.IV_SECANT, "secant from the Black-Scholes IV, Brent fallback"),
+            ("newton", pkg.IV_NEWTON, "Newton on the exact discrete vega (coarse grid, then own grid), "
+                                      "Brent fallback"))
+    for name, method, desc in arms:
+        eng.solve_iv_arrays(quotes[:4096], grids[:4096], method=method)  # warm the buffers
         t0 = time.perf_counter()
         out = eng.solve_iv_arrays(quotes, grids, method=method)
         t = time.perf_counter() - t0
         st = eng.stats()
+        invalid = np.isin(out["status"], (pkg.MANGO_ERR_VALIDATION, pkg.MANGO_ERR_ARBITRAGE))
+        eligible = ~invalid & ~low_vega
         ok = out["status"] == 0
-        err = np.abs(out["implied_vol"][ok] - vt[ok])
+        err = np.abs(out["implied_vol"] - vt)
+        within = eligible & ok & (err <= 1e-6)
+        miss = eligible & ~within
+        other_root = np.zeros(n, bool)
+        if miss.any():
+            idx = np.nonzero(miss & ok)[0]
+            if idx.size:
+                sel = lambda a: np.asarray(a)[idx]
+                v = eng.price_arrays(pkg.pricing_array(sel(S), sel(K), sel(T), out["implied_vol"][idx], sel(r),
+                                                       sel(q), sel(put)), grids[idx])["value"]
+                other_root[idx] = np.abs(v - px[idx]) <= 1e-9 * np.maximum(px[idx], 1.0)
         codes, counts = np.unique(out["status"], return_counts=True)
         res[name] = {
-            "method": ("Brent, the reference iterate sequence" if method == pkg.IV_BRENT else
-                       "secant from the Black-Scholes IV, Brent fallback"),
-            "value": n / t, "unit": "IV/s (end to end through mango_gpu_solve_iv_batch_method)",
-            "seconds": t, "status_counts": {int(c): int(k) for c, k in zip(codes, counts)},
+            "method": desc, "value": n / t,
+            "unit": "IV/s (end to end through mango_gpu_solve_iv_batch_method)", "seconds": t,
+            "status_counts": {int(c): int(k) for c, k in zip(codes, counts)},
             "iterations_mean": float(out["iterations"][ok].mean()) if ok.any() else None,
-            "max_abs_vol_error": float(err.max()) if ok.any() else None,
-            "frac_within_1e-6_vol": float(np.mean(err <= 1e-6)) if ok.any() else None,
-            "quote_marches": int(st["options"]), "evaluations": int(st["tiles"]),
-            "kernel_launches": int(st["kernel_launches"]),
+            "excluded_invalid": int(invalid.sum()), "excluded_low_vega": int((~invalid & low_vega).sum()),
+            "eligible": int(eligible.sum()),
+            "frac_within_1e-6_vol": float(within.sum() / max(eligible.sum(), 1)),
+            "misses": int(miss.sum()), "misses_at_another_root": int(other_root.sum()),
+            "max_abs_vol_error_eligible": float(err[eligible & ok].max()) if (eligible & ok).any() else None,
+            "quote_evaluations": int(st["options"]),
+            "evaluations_by_grid": {"coarse_tangent": int(st["iv_evals"][0]),
+                                    "own_tangent": int(st["iv_evals"][1]), "own": int(st["iv_evals"][2])},
+            "rounds": int(st["tiles"]), "kernel_launches": int(st["kernel_launches"]),
             "breakdown_ms": {"host_prep": round(st["host_prep_ms"], 2), "repack": round(st["prep_ms"], 2),
                              "evaluations_device": round(st["march_ms"], 2), "total": round(st["total_ms"], 2)}}
-    res["value"] = res["secant"]["value"]
-    res["unit"] = res["secant"]["unit"]
+    res["value"] = res["newton"]["value"]
+    res["unit"] = res["newton"]["unit"]
+    res["speedup_newton_vs_brent"] = res["newton"]["value"] / res["brent"]["value"]
     res["speedup_secant_vs_brent"] = res["secant"]["value"] / res["brent"]["value"]
     return res
 
@@ -675,7 +722,7 @@ def main():
     if not args.no_extra and rank == 0:
         extra["shared_chain"] = bench_chain(pkg, eng, n)
     if not args.no_iv and rank == 0:
-        extra["iv_brent"] = bench_iv(pkg, eng, args.iv_quotes)
+        extra["iv"] = bench_iv(pkg, eng, args.iv_quotes)
     if not args.no_iv and rank == 0:
         extra["greeks"] = bench_greeks(pkg, eng)
     if not args.no_table and rank == 0:

@@ -254,7 +254,8 @@ MangoStatus mango_gpu_solve_iv_batch(MangoGpuContext* ctx, const MangoIvQuery* q
 /* Root finders for mango_gpu_solve_iv_batch_method. */
 enum {
   MANGO_GPU_IV_BRENT = 0,   /* the reference's Brent, iterate for iterate */
-  MANGO_GPU_IV_SECANT = 1   /* safeguarded secant, Brent fallback (below) */
+  MANGO_GPU_IV_SECANT = 1,  /* safeguarded secant, Brent fallback (below) */
+  MANGO_GPU_IV_NEWTON = 2   /* Newton on the exact discrete vega (below) */
 };
 
 /* mango_gpu_solve_iv_batch with a choice of root finder.  MANGO_GPU_IV_BRENT
@@ -270,7 +271,25 @@ enum {
  * |V - P| < brent_tol_abs inside it, the quote is reported settled at that
  * point.  Converged roots of the two methods differ by at most about
  * 2 brent_tol_abs / vega.  iterations = evaluations for secant-settled
- * quotes, Brent's count otherwise.  No counterpart in the reference ABI. */
+ * quotes, Brent's count otherwise.
+ *
+ * MANGO_GPU_IV_NEWTON prices each evaluation with the forward-mode march
+ * (the exact derivative of the discrete price along the volatility, as
+ * mango_gpu_price_american_vega_batch), so every evaluation yields V and
+ * dV/dsigma.  Newton runs first on a coarse grid of the quote's grid kind
+ * (half the space points, a quarter of the steps) from the Black-Scholes
+ * implied volatility, then on the quote's own grid with the coarse curvature
+ * d(vega)/d(sigma) as a second-order correction.  A step on the own grid of
+ * at most 1e-3 whose second-order correction is at most 5e-8 is taken and the
+ * quote settles one step beyond its last evaluation (a volatility-space
+ * stop: the error left is a fraction of that correction); where the vega is
+ * small the reference's test |V - P| < brent_tol_abs also settles it.  A quote
+ * whose vega is not positive, whose step leaves the bracket seen so far, or
+ * that has not settled after 6 evaluations on its own grid is solved from
+ * scratch by Brent (statuses are Brent's).  Quotes with yield curves or
+ * discrete dividends use the secant path.  iterations = coarse plus own-grid
+ * evaluations for Newton-settled quotes; final_error = |V - P| at the last
+ * evaluated point.  No counterpart in the reference ABI. */
 MangoStatus mango_gpu_solve_iv_batch_method(MangoGpuContext* ctx, const MangoIvQuery* queries,
                                             uint64_t n, const MangoGpuGrid* grids,
                                             uint64_t grid_stride, const MangoIvConfig* config,
@@ -504,6 +523,16 @@ MangoStatus mango_gpu_price_american_tangent_batch(MangoGpuContext* ctx,
                                                    MangoGpuGreeksOut* out, uint64_t* out_failed,
                                                    MangoError* err);
 
+/* mango_gpu_price_american_tangent_batch along volatility alone: value,
+ * delta, vega and dstrike (rho and dividend_rho NaN) at about a third of the
+ * tangent work; the derivative a Newton step on the implied volatility
+ * needs.  No counterpart in the reference ABI. */
+MangoStatus mango_gpu_price_american_vega_batch(MangoGpuContext* ctx,
+                                                const MangoPricingParams* params, uint64_t n,
+                                                const MangoGpuGrid* grids, uint64_t grid_stride,
+                                                MangoGpuGreeksOut* out, uint64_t* out_failed,
+                                                MangoError* err);
+
 /* Resident batch: the same pipeline as mango_gpu_price_american_batch split
  * so that inputs can stay in device memory across runs (repeat pricing of a
  * book, IV iterations, benchmarking).  _create validates, resolves grids and
@@ -595,6 +624,10 @@ typedef struct {
   int64_t options;
   int64_t tiles;
   int64_t kernel_launches;
+  /* FDM IV: quote evaluations on the coarse grids with the volatility
+   * tangent, on the quotes' own grids with it, and on the own grids without
+   * it (MANGO_GPU_IV_NEWTON uses all three; the other methods the last). */
+  int64_t iv_evals[3];
 } MangoGpuStats;
 MangoStatus mango_gpu_last_stats(const MangoGpuContext* ctx, MangoGpuStats* out);
 

@@ -41,6 +41,7 @@ GRID_FIXED_N_AT_VOL = 4
 # Root finders of mango_gpu_solve_iv_batch_method.
 IV_BRENT = 0
 IV_SECANT = 1
+IV_NEWTON = 2
 
 # C layouts (include/mango_gpu.h); sizes are asserted there and in tests.
 PRICING_DTYPE = np.dtype([
@@ -85,7 +86,8 @@ class MangoGpuStats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_double) for k in (
         "host_prep_ms", "h2d_ms", "prep_ms", "march_ms", "outputs_ms", "d2h_ms", "total_ms",
         "algo_flops", "h2d_bytes", "d2h_bytes")] + [
-        ("options", ctypes.c_int64), ("tiles", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
+        ("options", ctypes.c_int64), ("tiles", ctypes.c_int64), ("kernel_launches", ctypes.c_int64),
+        ("iv_evals", ctypes.c_int64 * 3)]
 
 
 class MangoInterpSolverConfig(ctypes.Structure):
@@ -228,6 +230,9 @@ def library() -> ctypes.CDLL:
             _P, _P, ctypes.c_uint64, _P, ctypes.c_uint64, _P, ctypes.POINTER(ctypes.c_uint64),
             ctypes.POINTER(MangoError)]
         lib.mango_gpu_price_american_tangent_batch.restype = ctypes.c_int32
+        lib.mango_gpu_price_american_vega_batch.argtypes = \
+            lib.mango_gpu_price_american_tangent_batch.argtypes
+        lib.mango_gpu_price_american_vega_batch.restype = ctypes.c_int32
         lib.mango_gpu_build_info.argtypes = []
         lib.mango_gpu_build_info.restype = ctypes.c_char_p
         _lib = lib
@@ -523,7 +528,7 @@ class Engine:
         """Batched FDM implied volatility (mango_gpu_solve_iv_batch_method).
         queries: IVQUERY_DTYPE; grids: GRID_DTYPE (length 1 or len(queries)),
         each a volatility-independent grid; method IV_BRENT (the reference's
-        Brent) or IV_SECANT.  Returns IVSLOT_DTYPE records."""
+        Brent), IV_SECANT or IV_NEWTON (Newton on the exact discrete vega).  Returns IVSLOT_DTYPE records."""
         queries = np.ascontiguousarray(queries, dtype=IVQUERY_DTYPE)
         grids = np.ascontiguousarray(grids, dtype=GRID_DTYPE)
         n = queries.size
@@ -653,11 +658,13 @@ class Engine:
             raise EngineError(err.message.decode(errors="replace"))
         return out
 
-    def tangent_arrays(self, params: np.ndarray, grids: Optional[np.ndarray] = None) -> np.ndarray:
+    def tangent_arrays(self, params: np.ndarray, grids: Optional[np.ndarray] = None,
+                       vega_only: bool = False) -> np.ndarray:
         """Value, delta and the exact discrete dV/dvolatility, dV/drate,
         dV/ddividend_yield, dV/dK of the march in one forward-mode pass
         (mango_gpu_price_american_tangent_batch); GREEKS_DTYPE records with
-        gamma and theta NaN."""
+        gamma and theta NaN.  vega_only: the volatility direction alone
+        (mango_gpu_price_american_vega_batch; rho and dividend_rho NaN)."""
         params = np.ascontiguousarray(params, dtype=PRICING_DTYPE)
         n = params.size
         stride = 0
@@ -667,8 +674,10 @@ class Engine:
         out = np.zeros(n, dtype=GREEKS_DTYPE)
         failed = ctypes.c_uint64()
         err = MangoError()
-        st = library().mango_gpu_price_american_tangent_batch(self._ctx, _ptr(params), n, _ptr(grids), stride,
-                                                              _ptr(out), ctypes.byref(failed), ctypes.byref(err))
+        fn = (library().mango_gpu_price_american_vega_batch if vega_only
+              else library().mango_gpu_price_american_tangent_batch)
+        st = fn(self._ctx, _ptr(params), n, _ptr(grids), stride, _ptr(out), ctypes.byref(failed),
+                ctypes.byref(err))
         if st != MANGO_OK:
             raise EngineError(err.message.decode(errors="replace"))
         return out
@@ -692,7 +701,9 @@ class Engine:
     def stats(self) -> dict:
         s = MangoGpuStats()
         library().mango_gpu_last_stats(self._ctx, ctypes.byref(s))
-        return {k: getattr(s, k) for k, _ in MangoGpuStats._fields_}
+        d = {k: getattr(s, k) for k, _ in MangoGpuStats._fields_}
+        d["iv_evals"] = list(d["iv_evals"])
+        return d
 
 
 class BSpline4D:
@@ -1270,7 +1281,7 @@ class IVSolverConfig:
     grid_vol: float = 0.0
     brent_tol_abs: float = 1e-6
     max_iter: int = 100
-    method: int = 0  # IV_BRENT (the reference's root finder) or IV_SECANT
+    method: int = 0  # IV_BRENT (the reference's root finder), IV_SECANT or IV_NEWTON
 
 
 class IVSolver:

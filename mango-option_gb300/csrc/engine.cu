@@ -1126,6 +1126,7 @@ MangoStatus mango_gpu_last_stats(const MangoGpuContext* ctx, MangoGpuStats* out)
   out->options = s.options;
   out->tiles = s.tiles;
   out->kernel_launches = s.kernel_launches;
+  for (int j = 0; j < 3; ++j) out->iv_evals[j] = s.iv_evals[j];
   return MANGO_OK;
 }
 

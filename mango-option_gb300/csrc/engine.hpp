@@ -58,6 +58,9 @@ struct Stats {
   int64_t options = 0, tiles = 0, kernel_launches = 0;
   double algo_flops = 0;
   double h2d_bytes = 0, d2h_bytes = 0;
+  // FDM IV: quote evaluations on coarse grids with the volatility tangent,
+  // on the own grids with it, and on the own grids without it
+  int64_t iv_evals[3] = {0, 0, 0};
 };
 
 // Validation (validate_pricing_params plus the engine's scope) and grid

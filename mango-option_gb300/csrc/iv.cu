@@ -50,6 +50,7 @@
 
 #include "brent.cuh"
 #include "engine.hpp"
+#include "march_tan.cuh"
 
 namespace mgpu {
 
@@ -64,6 +65,9 @@ constexpr int kFastMaxBracketEvals = 60;
 constexpr int kMaxPts = 32;
 // IVSolver::solve_brent lower bracket (iv_solver.cpp:150).
 constexpr double kVolLower = 0.01;
+// Volatility-space tolerance of quotes the Newton path hands to the
+// k-section finder: a sign-change bracket this narrow settles them.
+constexpr double kVolTol = 1e-7;
 
 // Fast root-finder state of one quote.  Until a sign change of f has been
 // seen, [lo, hi] steers the search assuming f rises with the volatility;
@@ -79,19 +83,71 @@ struct FastDev {
   double e0, e1;   // f at Brent's bracket ends 0.01 and upper, when evaluated
   double guess;    // Black-Scholes implied volatility of the price
   double width;    // bracket width before the last evaluation
+  double ftol;     // > 0: settle on |f| < ftol or a bracket narrower than kVolTol
+                   // (a quote Newton handed over); 0: the call's price tolerance
   int32_t iter;    // evaluations consumed
   int32_t seen;
   int32_t ends;    // bit 0: f(0.01) evaluated; bit 1: f(upper) evaluated
   int32_t has_br;
 };
 
+// Safeguarded Newton on the exact discrete vega, started on a coarse grid.
+//   level 0: kCoarseEvals Newton steps on a coarse grid of the same kind
+//            (2/5 of the space points, an eighth of the time steps) from the
+//            Black-Scholes implied volatility; the coarse vegas give the
+//            curvature d(vega)/d(sigma);
+//   level 1: Newton on the quote's own grid with the exact vega and that
+//            curvature as a second-order correction, then value-only steps
+//            along the secant slope, inside the bracket seen so far.
+struct NewtonDev {
+  double x;        // point evaluated this round
+  double lo, hi;   // f(lo) < 0 < f(hi) where seen, else the Brent bracket ends
+  double flo, fhi; // f there (seen bits)
+  double kc;       // curvature estimate d(vega)/d(sigma)
+  double xp, vp;   // previous point on this level and its vega
+  double x0;       // starting point (Black-Scholes implied volatility)
+  double xb, fb;   // own-grid point with the smallest |f|
+  double x1, v1;   // last own-grid point with the exact vega, and that vega
+  double fp;       // f at xp (own grid)
+  int32_t has_v1;
+  int32_t level;   // 0 coarse, 1 own grid
+  int32_t it;      // evaluations on this level
+  int32_t total;   // evaluations overall
+  int32_t has_prev;
+  int32_t seen;    // bit 0: f(lo) < 0 evaluated, bit 1: f(hi) > 0 evaluated
+};
+
 // Per-quote root-finder state.
 struct IvDev {
   BrentDev br;
   FastDev fs;
-  int32_t mode;  // 0 fast, 1 Brent, 2 finished
+  NewtonDev nw;
+  int32_t mode;  // 0 fast, 1 Brent, 2 finished, 3 Newton
   int32_t pad;
 };
+
+// Newton schedule: coarse evaluations at most, the coarse step at which the
+// coarse level has converged, evaluations on the quote's own grid before a
+// hand-over to Brent, and the acceptance test of a step on the own grid
+// (|step| and the size of its second-order correction; the error left after
+// the corrected step is a fraction of that correction).
+constexpr int kCoarseEvals = 2;
+constexpr int kFineEvals = 3;
+constexpr double kAcceptStep = 1e-3;
+constexpr double kAcceptCorr = 2e-7;
+// The third-order term of a step d is about |d|^3 / (6 sigma^2) times a
+// moneyness factor; a step is taken only while that stays below
+// kAcceptCubic (|d| <= (6 kAcceptCubic sigma^2 / 20)^(1/3)).
+constexpr double kAcceptCubic = 1e-7;
+// A step from an estimated slope (evaluations without the tangent) is taken
+// when it is at most kAcceptStepEst and the disagreement of the two slope
+// estimates (secant through the last two values; last exact vega carried
+// along the curvature) moves it by at most kAcceptCorr.
+constexpr double kAcceptStepEst = 1e-4;
+// Below this vega (per unit volatility, relative to max(1, price)) the
+// objective is flat: the volatility is not determined by the price, and the
+// reference's price test |V - P| < tol settles the quote.
+constexpr double kFlatVega = 1e-7;
 
 // Final result of one quote.
 struct IvOut {
@@ -188,7 +244,9 @@ __device__ int fast_consume(FastDev& s, const double* sig, const double* f, int 
       s.seen |= 2;
     }
   }
-  if (fabs(s.fa) < tol) return kFastSettled;
+  const double ptol = s.ftol > 0.0 ? s.ftol : tol;
+  const double btol = s.ftol > 0.0 ? kVolTol : tol;
+  if (fabs(s.fa) < ptol) return kFastSettled;
   if (!s.has_br && s.seen == 3) {
     s.has_br = 1;
     if (s.lo < s.hi) {
@@ -224,7 +282,7 @@ __device__ int fast_consume(FastDev& s, const double* sig, const double* f, int 
     }
     s.bl = xl;
     s.fl = fl;
-    if (s.br - s.bl < tol) return kFastSettled;
+    if (s.br - s.bl < btol) return kFastSettled;
   } else if (s.ends == 3) {
     return kFastBracket;
   }
@@ -292,21 +350,173 @@ __device__ __forceinline__ double objective(const double* out4, const int32_t* m
   return mstatus[k] == kStatusOk ? out4[4 * static_cast<size_t>(k)] - price : qnan();
 }
 
+// Working sets of an evaluation round: the coarse grids and the quotes' own
+// grids with the volatility tangent (Newton), and the quotes' own grids
+// without it (Brent, the secant, time-varying quotes).
+constexpr int32_t kLevelCoarse = 0, kLevelFine = 1, kLevelPlain = 2;
+
+// Newton on f = V - P at s.x, with v = dV/dsigma when the evaluation carried
+// the tangent (has_v).  Coarse level: exactly kCoarseEvals evaluations (all
+// quotes reach their own grid in the same round), the curvature from the
+// last two.  Own grid: the first evaluation carries the exact vega; later
+// ones are value-only and use the slope of the secant through the last two
+// values, corrected to the new point with the curvature.  Returns 0 to go on
+// (s.x is the next point, *level its working set), 1 when settled at *root,
+// 2 to hand the quote over.
+__device__ int newton_consume(NewtonDev& s, double f, double v, bool has_v, double upper,
+                              double tol, double* root, int32_t* level) {
+  s.total += 1;
+  s.it += 1;
+  const double x = s.x;
+  if (s.level == 0) {
+    // Every quote spends exactly kCoarseEvals evaluations here, so that all
+    // reach their own grid in the same round; a failed or flat coarse
+    // evaluation restarts from the initial guess.
+    const bool good = isfinite(f) && isfinite(v) && v > 0.0;
+    if (good) {
+      if (s.has_prev && x != s.xp) s.kc = (v - s.vp) / (x - s.xp);
+      s.xp = x;
+      s.vp = v;
+      s.has_prev = 1;
+      s.x = fmin(fmax(x - f / v, kVolLower), upper);
+    } else {
+      s.x = s.x0;
+    }
+    if (s.it >= kCoarseEvals) {
+      s.level = 1;  // the curvature estimate carries over
+      s.it = 0;
+      s.has_prev = 0;
+      *level = kLevelFine;
+    } else {
+      *level = kLevelCoarse;
+    }
+    return 0;
+  }
+  if (!isfinite(f) || (has_v && !isfinite(v))) return 2;
+  if (f < 0.0 && (!(s.seen & 1) || x > s.lo)) {
+    s.lo = x;
+    s.flo = f;
+    s.seen |= 1;
+  } else if (f > 0.0 && (!(s.seen & 2) || x < s.hi)) {
+    s.hi = x;
+    s.fhi = f;
+    s.seen |= 2;
+  }
+  if (!(fabs(f) >= fabs(s.fb))) {
+    s.xb = x;
+    s.fb = f;
+  }
+  if (f == 0.0) {
+    *root = x;
+    return 1;
+  }
+  double slope, slope_err = 0.0;
+  if (has_v) {
+    slope = v;
+    s.x1 = x;
+    s.v1 = v;
+    s.has_v1 = 1;
+  } else if (s.has_prev && x != s.xp) {
+    slope = (f - s.fp) / (x - s.xp) + 0.5 * s.kc * (x - s.xp);
+    slope_err = s.has_v1 ? fabs(slope - (s.v1 + s.kc * (x - s.x1))) : fabs(slope);
+  } else if (s.has_v1) {
+    slope = s.v1 + s.kc * (x - s.x1);
+    slope_err = fabs(slope);
+  } else {
+    return 2;
+  }
+  s.xp = x;
+  s.fp = f;
+  s.has_prev = 1;
+  const double flat = kFlatVega * fmax(1.0, fabs(f) + fabs(s.fb));
+  if (!(slope > flat)) {
+    if (fabs(f) < tol) {  // flat objective: the reference's stopping test
+      *root = x;
+      return 1;
+    }
+    return 2;
+  }
+  const double d = -f / slope;
+  // second-order step on f + slope d + kc d^2 / 2 = 0 (fixed point, where
+  // the correction is small against the step)
+  double dh = d;
+  if (fabs(s.kc * d / slope) < 0.5)
+    for (int k = 0; k < 3; ++k) dh = -(f + 0.5 * s.kc * dh * dh) / slope;
+  const double xn = x + dh;
+  const double cubic_max = cbrt(0.3 * kAcceptCubic * x * x);
+  const bool ok = has_v ? fabs(d) <= fmin(kAcceptStep, cubic_max)
+                        : fabs(d) <= fmin(kAcceptStepEst, cubic_max) &&
+                              fabs(d) * slope_err <= kAcceptCorr * slope;
+  if (ok && fabs(dh - d) <= kAcceptCorr && xn >= kVolLower && xn <= upper) {
+    *root = xn;
+    return 1;
+  }
+  if (s.it >= kFineEvals || (s.seen == 3 && !(s.lo < s.hi))) return 2;
+  s.x = (xn > s.lo && xn < s.hi) ? xn : 0.5 * (s.lo + s.hi);
+  *level = kLevelPlain;  // value-only from here on
+  return 0;
+}
+
+// Hand a quote Newton did not settle to the secant / k-section finder on
+// the plain working set, seeded with what Newton learned: the bracket ends it
+// evaluated and its best point.
+__device__ void newton_to_fast(const NewtonDev& n, FastDev& s, double upper) {
+  s = FastDev{};
+  s.lo = (n.seen & 1) ? n.lo : kVolLower;
+  s.hi = (n.seen & 2) ? n.hi : upper;
+  s.flo = n.flo;
+  s.fhi = n.fhi;
+  s.seen = n.seen;
+  s.xa = n.xb;
+  s.fa = isfinite(n.fb) ? n.fb : pinf();
+  s.xb = qnan();
+  s.fb = pinf();
+  s.e0 = s.e1 = qnan();
+  s.guess = isfinite(n.xb) ? n.xb : n.x0;
+  s.iter = 1;  // the first proposal uses the best point, not the guess
+  s.ftol = n.has_v1 && n.v1 > 0.0 ? kVolTol * n.v1 : kVolTol;
+  if (s.seen == 3) {
+    s.has_br = 1;
+    if (s.lo < s.hi) {
+      s.bl = s.lo, s.fl = s.flo, s.br = s.hi, s.fr = s.fhi;
+    } else {
+      s.bl = s.hi, s.fl = s.fhi, s.br = s.lo, s.fr = s.flo;
+    }
+  }
+}
+
 }  // namespace
 
 // First trial points of every sorted quote: the Black-Scholes implied vol
 // and up to k - 1 more (fast), or the lower bracket 0.01 (Brent).
-__global__ void iv_init_kernel(int m, int32_t method, int k, const OptDev* __restrict__ opts,
-                               const double* __restrict__ mat, const double* __restrict__ price,
-                               const double* __restrict__ upper, IvDev* __restrict__ S,
-                               IvOut* __restrict__ R, double* __restrict__ next_sig,
-                               int32_t* __restrict__ npts) {
+__global__ void iv_init_kernel(int m, int32_t method, int k, int tv_first,
+                               const OptDev* __restrict__ opts, const double* __restrict__ mat,
+                               const double* __restrict__ price, const double* __restrict__ upper,
+                               IvDev* __restrict__ S, IvOut* __restrict__ R,
+                               double* __restrict__ next_sig, int32_t* __restrict__ npts,
+                               int32_t* __restrict__ lev) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= m) return;
   R[q] = IvOut{qnan(), qnan(), 0, kIvNumerical};
   IvDev st{};
   double* pts = next_sig + static_cast<size_t>(q) * kMaxPts;
-  if (method == MANGO_GPU_IV_SECANT) {
+  lev[q] = kLevelPlain;
+  if (method == MANGO_GPU_IV_NEWTON && q < tv_first) {
+    const OptDev o = opts[q];
+    NewtonDev& s = st.nw;
+    s.lo = kVolLower;
+    s.hi = upper[q];
+    s.x0 = european_iv_guess(o.is_put != 0, o.spot, o.strike, mat[q], o.r, o.q, price[q], s.lo,
+                             s.hi);
+    s.x = s.x0;
+    s.xb = qnan();
+    s.fb = pinf();
+    s.x1 = s.v1 = s.fp = qnan();
+    st.mode = 3;
+    pts[0] = s.x;
+    npts[q] = 1;
+    lev[q] = kLevelCoarse;
+  } else if (method == MANGO_GPU_IV_SECANT || method == MANGO_GPU_IV_NEWTON) {
     const OptDev o = opts[q];
     FastDev& s = st.fs;
     s.lo = kVolLower;
@@ -337,7 +547,7 @@ __global__ void iv_step_kernel(int nq, const int32_t* __restrict__ qlist,
                                const double* __restrict__ out4, const int32_t* __restrict__ mstatus,
                                const double* __restrict__ sigma_w, const double* __restrict__ price,
                                double* __restrict__ next_sig, int32_t* __restrict__ npts, double tol,
-                               int max_iter, int trace) {
+                               int max_iter, int trace, int has_vega, int32_t* __restrict__ lev) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nq) return;
   const int q = qlist[i];
@@ -373,6 +583,26 @@ __global__ void iv_step_kernel(int nq, const int32_t* __restrict__ qlist,
       pts[0] = st.br.a;
       next_n = 1;
     }
+  } else if (st.mode == 3) {
+    const double f = objective(out4, mstatus, base, P);
+    const double v = (has_vega && mstatus[base] == kStatusOk)
+                         ? out4[4 * static_cast<size_t>(base) + 3] : qnan();
+    double root = qnan();
+    int32_t level = kLevelFine;
+    const int r = newton_consume(st.nw, f, v, has_vega != 0, upper[q], tol, &root, &level);
+    if (r == 0) {
+      pts[0] = st.nw.x;
+      next_n = 1;
+      lev[q] = level;
+    } else if (r == 1) {
+      R[q] = IvOut{root, fabs(f), st.nw.total, kIvOk};
+      st.mode = 2;
+    } else {
+      newton_to_fast(st.nw, st.fs, upper[q]);
+      st.mode = 0;
+      next_n = fast_propose(st.fs, opts[q], mat[q], upper[q], k, pts);
+      lev[q] = kLevelPlain;
+    }
   } else if (st.mode == 1) {
     double next = 0.0;
     if (brent_consume(st.br, objective(out4, mstatus, base, P), tol, max_iter, &next)) {
@@ -391,6 +621,7 @@ __global__ void iv_step_kernel(int nq, const int32_t* __restrict__ qlist,
 // sorted quotes [32 t, 32 t + 32)): slot k prices quote map[k] at its trial
 // point pt[k].
 __global__ void iv_gather_kernel(int mw, const int32_t* __restrict__ map,
+                                 const int32_t* __restrict__ src_map,
                                  const int32_t* __restrict__ pt,
                                  const TileDev* __restrict__ src_tiles,
                                  const OptDev* __restrict__ src_opts,
@@ -402,11 +633,12 @@ __global__ void iv_gather_kernel(int mw, const int32_t* __restrict__ map,
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= mw) return;
   const int q = map[k];
-  const OptDev o = src_opts[q];
+  const int qs = src_map ? src_map[k] : q;  // the quote's index in the source batch
+  const OptDev o = src_opts[qs];
   dst_opts[k] = o;
-  const TileDev ts = src_tiles[q / kTile];
+  const TileDev ts = src_tiles[qs / kTile];
   const TileDev td = dst_tiles[k / kTile];
-  const double* src = src_xs + ts.xoff + (q % kTile);
+  const double* src = src_xs + ts.xoff + (qs % kTile);
   double* dst = dst_xs + td.xoff + (k % kTile);
   for (int i = 0; i < td.nx; ++i)
     dst[static_cast<size_t>(i) * kTile] = src[static_cast<size_t>(min(i, o.n - 1)) * kTile];
@@ -477,24 +709,33 @@ double ms_since(Clock::time_point t0) {
 }
 
 // The trial points of one evaluation packed into tiles of 32 (sorted
-// order), with the device buffers their marches use.
+// order), with the device buffers their marches use.  Quotes are indexed by
+// their position in the batch b; their grids and parameters come from the
+// batch src (b itself, or the coarse-grid batch of the Newton method, where
+// smap maps b's sorted index to src's).  A tangent working set also carries
+// the volatility tangent (march_tan.cu).
 struct WorkSet {
   MangoGpuBatch* b = nullptr;
+  MangoGpuBatch* src = nullptr;
+  const std::vector<int32_t>* smap = nullptr;
+  bool tangent = false;
   cudaStream_t st = nullptr;
   int64_t mw = 0;  // slots
   int32_t ntiles = 0;
   int64_t nq = 0;  // quotes
-  std::vector<int32_t> map_h, pt_h, qlist_h, qbase_h;
+  int64_t pool_doubles = 0;
+  std::vector<int32_t> map_h, src_h, pt_h, qlist_h, qbase_h;
   std::vector<TileDev> tiles_h;
-  DevBuf d_tiles, d_opts, d_xs, d_map, d_pt, d_qlist, d_qbase, d_sigma, d_active, d_pool, d_flags,
-      d_mode, d_status, d_out4, d_tv;
+  DevBuf d_tiles, d_opts, d_xs, d_map, d_src, d_pt, d_qlist, d_qbase, d_sigma, d_active, d_pool,
+      d_flags, d_mode, d_status, d_out4, d_tv, d_tpool;
   // First slot of a time-varying quote (slots follow the batch order, where
   // those quotes come last), or INT32_MAX.
   int32_t tv_first = 0x7fffffff;
 
   ~WorkSet() {
-    for (DevBuf* d : {&d_tiles, &d_opts, &d_xs, &d_map, &d_pt, &d_qlist, &d_qbase, &d_sigma,
-                      &d_active, &d_pool, &d_flags, &d_mode, &d_status, &d_out4, &d_tv})
+    for (DevBuf* d : {&d_tiles, &d_opts, &d_xs, &d_map, &d_src, &d_pt, &d_qlist, &d_qbase,
+                      &d_sigma, &d_active, &d_pool, &d_flags, &d_mode, &d_status, &d_out4, &d_tv,
+                      &d_tpool})
       d->release();
   }
 
@@ -502,6 +743,7 @@ struct WorkSet {
   // host arrays must stay untouched until the stream has passed the copies.
   void pack(const std::vector<int32_t>& active, const int32_t* npts, const double* next_sig) {
     map_h.clear();
+    src_h.clear();
     pt_h.clear();
     qlist_h.clear();
     qbase_h.clear();
@@ -510,8 +752,10 @@ struct WorkSet {
       if (c <= 0) continue;
       qlist_h.push_back(q);
       qbase_h.push_back(static_cast<int32_t>(map_h.size()));
+      const int32_t qs = smap ? (*smap)[q] : q;
       for (int j = 0; j < c; ++j) {
         map_h.push_back(q);
+        src_h.push_back(qs);
         pt_h.push_back(j);
       }
     }
@@ -521,7 +765,7 @@ struct WorkSet {
     if (mw > (1LL << 31) - 1) throw CudaError("IV working set above 2^31 points");
     ntiles = static_cast<int32_t>((mw + kTile - 1) / kTile);
     tiles_h.assign(static_cast<size_t>(ntiles), TileDev{});
-    const OptDev* ho = b->h_opts.as<OptDev>();
+    const OptDev* ho = src->h_opts.as<OptDev>();
     int64_t off = 0, xoff = 0, foff = 0;
     for (int32_t t = 0; t < ntiles; ++t) {
       TileDev& td = tiles_h[t];
@@ -529,7 +773,7 @@ struct WorkSet {
       td.count = static_cast<int32_t>(std::min<int64_t>(kTile, mw - td.first));
       int32_t nx = 0, nt = 0;
       for (int l = 0; l < td.count; ++l) {
-        const OptDev& o = ho[map_h[td.first + l]];
+        const OptDev& o = ho[src_h[td.first + l]];
         nx = std::max(nx, o.n);
         nt = std::max(nt, o.nt);
       }
@@ -542,12 +786,17 @@ struct WorkSet {
       xoff += static_cast<int64_t>(nx) * kTile;
       foff += static_cast<int64_t>(nx) * kTile;
     }
+    pool_doubles = off;
     check(cudaMemcpyAsync(d_tiles.get(sizeof(TileDev) * ntiles), tiles_h.data(),
                           sizeof(TileDev) * ntiles, cudaMemcpyHostToDevice, st),
           "H2D working tiles");
     check(cudaMemcpyAsync(d_map.get(sizeof(int32_t) * mw), map_h.data(), sizeof(int32_t) * mw,
                           cudaMemcpyHostToDevice, st),
           "H2D working map");
+    if (smap)
+      check(cudaMemcpyAsync(d_src.get(sizeof(int32_t) * mw), src_h.data(), sizeof(int32_t) * mw,
+                            cudaMemcpyHostToDevice, st),
+            "H2D working source map");
     check(cudaMemcpyAsync(d_pt.get(sizeof(int32_t) * mw), pt_h.data(), sizeof(int32_t) * mw,
                           cudaMemcpyHostToDevice, st),
           "H2D working points");
@@ -566,12 +815,15 @@ struct WorkSet {
     d_mode.get(sizeof(int32_t) * mw);
     d_status.get(sizeof(int32_t) * mw);
     d_out4.get(sizeof(double) * 4 * mw);
+    if (tangent) d_tpool.get(sizeof(double) * static_cast<size_t>(tan_pool_doubles(1, off)));
     iv_gather_kernel<<<static_cast<int>((mw + 255) / 256), 256, 0, st>>>(
-        static_cast<int>(mw), d_map.as<int32_t>(), d_pt.as<int32_t>(), b->d_tiles.as<TileDev>(),
-        b->d_opts.as<OptDev>(), b->d_xs.as<double>(), d_tiles.as<TileDev>(), d_opts.as<OptDev>(),
-        d_xs.as<double>(), next_sig, d_sigma.as<double>(), d_active.as<int32_t>());
+        static_cast<int>(mw), d_map.as<int32_t>(), smap ? d_src.as<int32_t>() : nullptr,
+        d_pt.as<int32_t>(), src->d_tiles.as<TileDev>(), src->d_opts.as<OptDev>(),
+        src->d_xs.as<double>(), d_tiles.as<TileDev>(), d_opts.as<OptDev>(), d_xs.as<double>(),
+        next_sig, d_sigma.as<double>(), d_active.as<int32_t>());
     check(cudaGetLastError(), "iv_gather launch");
     tv_first = 0x7fffffff;
+    if (smap) return;  // the coarse batch holds no time-varying quote
     for (int64_t k = 0; k < mw; ++k)
       if (map_h[k] >= b->mc.tv_first) {
         tv_first = static_cast<int32_t>(k);
@@ -599,7 +851,8 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
             "IV needs a fixed grid per quote (MANGO_GPU_GRID_FIXED_N_AT_VOL, _SINH or _UNIFORM)");
     return MANGO_ERR_VALIDATION;
   }
-  if (method != MANGO_GPU_IV_BRENT && method != MANGO_GPU_IV_SECANT) {
+  if (method != MANGO_GPU_IV_BRENT && method != MANGO_GPU_IV_SECANT &&
+      method != MANGO_GPU_IV_NEWTON) {
     set_err(err, MANGO_ERR_VALIDATION, "unknown IV method");
     return MANGO_ERR_VALIDATION;
   }
@@ -612,6 +865,7 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
   const char* trace_env = std::getenv("MANGO_GPU_IV_TRACE");
   const bool trace = trace_env && trace_env[0] == '1';
   MangoGpuBatch* b = nullptr;
+  MangoGpuBatch* bc = nullptr;  // Newton: the coarse grids
   const auto t_start = Clock::now();
   try {
     check(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -656,10 +910,34 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
     // The batch's own march buffers are not used: every evaluation runs on
     // a packed working set.
     for (DevBuf* d : {&b->d_pool, &b->d_flags, &b->d_mode, &b->d_status, &b->d_out4}) d->release();
-    const double host_prep_ms = b->host_prep_ms;
+    double host_prep_ms = b->host_prep_ms;
     const int64_t m = static_cast<int64_t>(b->order.size());
+    // Newton: the same quotes on coarse grids of the same kind (2/5 of the
+    // space points, an eighth of the steps; an estimated step count stays
+    // estimated), and the map from b's sorted order to bc's.
+    std::vector<int32_t> cmap;
+    if (method == MANGO_GPU_IV_NEWTON && m > 0) {
+      std::vector<MangoPricingParams> pc(pp);
+      std::vector<MangoGpuGrid> gc(static_cast<size_t>(nn));
+      for (int64_t i = 0; i < nn; ++i) {
+        MangoGpuGrid g = grids[grid_stride ? i : 0];
+        g.n_space = std::max<int64_t>(21, (2 * g.n_space / 5) | 1);
+        if (g.n_time > 0) g.n_time = std::max<int64_t>(16, g.n_time / 8);
+        gc[i] = g;
+        if (vstatus[i] != MANGO_OK || time_varying(pp[i])) pc[i].spot = -1.0;
+      }
+      bc = create_batch(ctx, pc.data(), nn, gc.data(), 1, nullptr);
+      for (DevBuf* d : {&bc->d_pool, &bc->d_flags, &bc->d_mode, &bc->d_status, &bc->d_out4})
+        d->release();
+      host_prep_ms += bc->host_prep_ms;
+      std::vector<int32_t> pos(static_cast<size_t>(nn), -1);
+      for (size_t s2 = 0; s2 < bc->order.size(); ++s2) pos[bc->order[s2]] = static_cast<int32_t>(s2);
+      cmap.assign(static_cast<size_t>(m), -1);
+      for (int64_t s2 = 0; s2 < m; ++s2) cmap[s2] = pos[b->order[s2]];
+    }
     std::vector<IvOut> hr(static_cast<size_t>(m));
     int64_t launches = 0, evaluations = 0;
+    int64_t level_evals[3] = {0, 0, 0};
     double slot_evals = 0, eval_ms = 0, pack_ms = 0;
     if (m > 0) {
       cudaStream_t st = ctx->stream;
@@ -671,21 +949,24 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
         px[s] = q.market_price;
         mat[s] = q.maturity;
       }
-      DevBuf d_state, d_res, d_next, d_npts, d_hi, d_px, d_mat;
-      HostBuf h_npts;
+      DevBuf d_state, d_res, d_next, d_npts, d_hi, d_px, d_mat, d_lev;
+      HostBuf h_npts, h_lev;
       struct Release {
         std::vector<DevBuf*> d;
-        HostBuf* h;
+        std::vector<HostBuf*> h;
         ~Release() {
           for (DevBuf* x : d) x->release();
-          h->release();
+          for (HostBuf* x : h) x->release();
         }
-      } release{{&d_state, &d_res, &d_next, &d_npts, &d_hi, &d_px, &d_mat}, &h_npts};
+      } release{{&d_state, &d_res, &d_next, &d_npts, &d_hi, &d_px, &d_mat, &d_lev},
+                {&h_npts, &h_lev}};
       IvDev* S = static_cast<IvDev*>(d_state.get(sizeof(IvDev) * m));
       IvOut* R = static_cast<IvOut*>(d_res.get(sizeof(IvOut) * m));
       double* next_sig = static_cast<double*>(d_next.get(sizeof(double) * kMaxPts * m));
       int32_t* npts = static_cast<int32_t*>(d_npts.get(sizeof(int32_t) * m));
       int32_t* hnpts = static_cast<int32_t*>(h_npts.get(sizeof(int32_t) * m));
+      int32_t* lev = static_cast<int32_t*>(d_lev.get(sizeof(int32_t) * m));
+      int32_t* hlev = static_cast<int32_t*>(h_lev.get(sizeof(int32_t) * m));
       double* dhi = static_cast<double*>(d_hi.get(sizeof(double) * m));
       double* dpx = static_cast<double*>(d_px.get(sizeof(double) * m));
       double* dmat = static_cast<double*>(d_mat.get(sizeof(double) * m));
@@ -704,13 +985,14 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
       const int64_t wave =
           static_cast<int64_t>(ctx->num_sms) * ctx->march_blocks_per_sm * 4 * kTile;
       auto points_for = [&](int64_t quotes) {
-        if (method != MANGO_GPU_IV_SECANT) return 1;
+        if (method == MANGO_GPU_IV_BRENT) return 1;
         return static_cast<int>(
             std::max<int64_t>(1, std::min<int64_t>(kMaxPts, wave / std::max<int64_t>(quotes, 1))));
       };
-      iv_init_kernel<<<grid_of(m), tb, 0, st>>>(static_cast<int>(m), method, points_for(m),
-                                                b->d_opts.as<OptDev>(), dmat, dpx, dhi, S, R,
-                                                next_sig, npts);
+      iv_init_kernel<<<grid_of(m), tb, 0, st>>>(
+          static_cast<int>(m), method, points_for(m),
+          static_cast<int>(std::min<int64_t>(b->mc.tv_first, m)), b->d_opts.as<OptDev>(), dmat,
+          dpx, dhi, S, R, next_sig, npts, lev);
       check(cudaGetLastError(), "iv_init launch");
       ++launches;
       cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -722,75 +1004,120 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
         }
       } events{ev};
       for (cudaEvent_t& e : ev) check(cudaEventCreate(&e), "cudaEventCreate");
-      WorkSet w;
-      w.b = b;
-      w.st = st;
+      // Working sets by level: coarse grids with the volatility tangent
+      // (Newton), the own grids with it (Newton, and Brent after a Newton
+      // hand-over), the own grids without it (Brent, the secant).
+      WorkSet ws[3];
+      for (int L = 0; L < 3; ++L) {
+        ws[L].b = b;
+        ws[L].src = (L == kLevelCoarse) ? bc : b;
+        ws[L].smap = (L == kLevelCoarse) ? &cmap : nullptr;
+        ws[L].tangent = L != kLevelPlain;
+        ws[L].st = st;
+      }
       std::vector<int32_t> active(static_cast<size_t>(m));
       std::iota(active.begin(), active.end(), 0);
-      // Fast evaluations, then Brent's two bracket ends and max_iter steps.
-      const int max_evals = (method == MANGO_GPU_IV_SECANT ? kFastMaxBracketEvals : 0) + max_iter + 3;
+      std::vector<int32_t> lists[3];
+      double level_slot_evals[3] = {0.0, 0.0, 0.0};
+      // Fast or Newton evaluations, then Brent's two bracket ends and max_iter steps.
+      const int max_evals =
+          (method == MANGO_GPU_IV_BRENT ? 0 : kFastMaxBracketEvals + kCoarseEvals) + max_iter + 3;
       for (int e = 0; e < max_evals; ++e) {
         check(cudaMemcpyAsync(hnpts, npts, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, st),
               "D2H points");
+        check(cudaMemcpyAsync(hlev, lev, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, st),
+              "D2H levels");
         check(cudaStreamSynchronize(st), "stream synchronize");
         const auto tp = Clock::now();
-        w.pack(active, hnpts, next_sig);
+        for (auto& l : lists) l.clear();
+        std::vector<int32_t> still;
+        still.reserve(active.size());
+        for (int32_t q : active)
+          if (hnpts[q] > 0) {
+            still.push_back(q);
+            lists[std::min(std::max(hlev[q], 0), 2)].push_back(q);
+          }
+        active.swap(still);
+        int64_t nq_all = 0;
+        for (int L = 0; L < 3; ++L) {
+          ws[L].pack(lists[L], hnpts, next_sig);
+          nq_all += ws[L].nq;
+        }
         pack_ms += ms_since(tp);
-        if (w.nq == 0) break;
-        active = w.qlist_h;
-        const int k_next = points_for(w.nq);
-        MarchConst mc = b->mc;
-        mc.value_only = 1;
-        mc.sigma = w.d_sigma.as<double>();
-        mc.active = w.d_active.as<int32_t>();
-        mc.tv_first = w.tv_first;
-        const int ntiles = w.ntiles, threads = ntiles * kTile;
-        const int blocks =
-            std::max(1, std::min<int>(ctx->num_sms * ctx->march_blocks_per_sm, (ntiles + 3) / 4));
-        const TileDev* tiles = w.d_tiles.as<TileDev>();
-        const OptDev* wopts = w.d_opts.as<OptDev>();
-        const double* xs = w.d_xs.as<double>();
+        if (nq_all == 0) break;
+        const int k_next = points_for(nq_all);
         check(cudaMemsetAsync(b->d_queue.p, 0, sizeof(int) * 4, st), "memset queue");
         check(cudaEventRecord(ev[0], st), "event");
-        prep_kernel<<<(threads + 127) / 128, 128, 0, st>>>(tiles, ntiles, wopts, xs,
-                                                           w.d_pool.as<double>(),
-                                                           w.d_flags.as<uint8_t>(),
-                                                           w.d_mode.as<int32_t>(), mc);
-        march_kernel<<<blocks, 128, 0, st>>>(tiles, ntiles, wopts, w.d_pool.as<double>(),
-                                             w.d_flags.as<uint8_t>(), w.d_mode.as<int32_t>(),
-                                             w.d_status.as<int32_t>(), b->d_queue.as<int>(), mc);
-        if (w.tv_first < w.mw) {
-          const int t0 = w.tv_first / kTile;
-          const int tvb = std::max(1, std::min<int>(ctx->num_sms * 8, (ntiles - t0 + 3) / 4));
-          march_tv_kernel<<<tvb, 128, 0, st>>>(tiles, t0, ntiles, wopts, w.d_tv.as<TvDev>(),
-                                               b->d_tv_tp.as<double>(), b->d_tv_curve.as<double>(),
-                                               b->d_tv_ev.as<double>(), xs, w.d_pool.as<double>(),
-                                               w.d_mode.as<int32_t>(), w.d_status.as<int32_t>(), mc);
-          ++launches;
+        for (int L = 0; L < 3; ++L) {
+          WorkSet& w = ws[L];
+          if (w.mw == 0) continue;
+          MarchConst mc = w.src->mc;
+          mc.value_only = 1;
+          mc.sigma = w.d_sigma.as<double>();
+          mc.active = w.d_active.as<int32_t>();
+          mc.tv_first = w.tv_first;
+          const int ntiles = w.ntiles, threads = ntiles * kTile;
+          const TileDev* tiles = w.d_tiles.as<TileDev>();
+          const OptDev* wopts = w.d_opts.as<OptDev>();
+          const double* xs = w.d_xs.as<double>();
+          int* queue = b->d_queue.as<int>() + L;
+          if (w.tangent) {
+            TanConst tc{};
+            tc.dirs[0] = kDirSigma;
+            tan_launch(1, st, ctx->num_sms, tiles, ntiles, wopts, xs, w.d_pool.as<double>(),
+                       w.d_tpool.as<double>(), w.d_flags.as<uint8_t>(), w.d_mode.as<int32_t>(),
+                       w.d_status.as<int32_t>(), queue, tc, mc, w.d_out4.as<double>());
+            launches += 5;  // gather, prep, tangent prep, march, outputs
+          } else {
+            const int blocks = std::max(
+                1, std::min<int>(ctx->num_sms * ctx->march_blocks_per_sm, (ntiles + 3) / 4));
+            prep_kernel<<<(threads + 127) / 128, 128, 0, st>>>(tiles, ntiles, wopts, xs,
+                                                               w.d_pool.as<double>(),
+                                                               w.d_flags.as<uint8_t>(),
+                                                               w.d_mode.as<int32_t>(), mc);
+            march_kernel<<<blocks, 128, 0, st>>>(tiles, ntiles, wopts, w.d_pool.as<double>(),
+                                                 w.d_flags.as<uint8_t>(), w.d_mode.as<int32_t>(),
+                                                 w.d_status.as<int32_t>(), queue, mc);
+            if (w.tv_first < w.mw) {
+              const int t0 = w.tv_first / kTile;
+              const int tvb = std::max(1, std::min<int>(ctx->num_sms * 8, (ntiles - t0 + 3) / 4));
+              march_tv_kernel<<<tvb, 128, 0, st>>>(
+                  tiles, t0, ntiles, wopts, w.d_tv.as<TvDev>(), b->d_tv_tp.as<double>(),
+                  b->d_tv_curve.as<double>(), b->d_tv_ev.as<double>(), xs, w.d_pool.as<double>(),
+                  w.d_mode.as<int32_t>(), w.d_status.as<int32_t>(), mc);
+              ++launches;
+            }
+            outputs_kernel<<<(threads + 127) / 128, 128, 0, st>>>(
+                tiles, ntiles, wopts, xs, w.d_pool.as<double>(), w.d_mode.as<int32_t>(),
+                w.d_status.as<int32_t>(), mc, w.d_out4.as<double>());
+            launches += 4;  // gather, prep, march, outputs
+          }
+          iv_step_kernel<<<grid_of(w.nq), tb, 0, st>>>(
+              static_cast<int>(w.nq), w.d_qlist.as<int32_t>(), w.d_qbase.as<int32_t>(), k_next, S,
+              R, b->d_opts.as<OptDev>(), dmat, dhi, w.d_out4.as<double>(),
+              w.d_status.as<int32_t>(), w.d_sigma.as<double>(), dpx, next_sig, npts, tol,
+              max_iter, trace ? 1 : 0, w.tangent ? 1 : 0, lev);
+          check(cudaGetLastError(), "iv evaluation launch");
+          launches += 1;
+          level_slot_evals[L] += static_cast<double>(w.mw);
+          slot_evals += static_cast<double>(w.mw);
         }
-        outputs_kernel<<<(threads + 127) / 128, 128, 0, st>>>(
-            tiles, ntiles, wopts, xs, w.d_pool.as<double>(), w.d_mode.as<int32_t>(),
-            w.d_status.as<int32_t>(), mc, w.d_out4.as<double>());
-        iv_step_kernel<<<grid_of(w.nq), tb, 0, st>>>(
-            static_cast<int>(w.nq), w.d_qlist.as<int32_t>(), w.d_qbase.as<int32_t>(), k_next, S, R,
-            b->d_opts.as<OptDev>(), dmat, dhi, w.d_out4.as<double>(), w.d_status.as<int32_t>(),
-            w.d_sigma.as<double>(), dpx, next_sig, npts, tol, max_iter, trace ? 1 : 0);
-        check(cudaGetLastError(), "iv evaluation launch");
         check(cudaEventRecord(ev[1], st), "event");
         check(cudaStreamSynchronize(st), "stream synchronize");
         float ms = 0.f;
         check(cudaEventElapsedTime(&ms, ev[0], ev[1]), "event time");
         eval_ms += ms;
-        launches += 5;  // gather, prep, march, outputs, step
         evaluations += 1;
-        slot_evals += static_cast<double>(w.mw);
         if (trace)
           std::fprintf(stderr,
-                       "iv evaluation %d: %lld quotes, %lld points in %d tiles, next %d per quote, "
-                       "%.3f ms\n",
-                       e, static_cast<long long>(w.nq), static_cast<long long>(w.mw), w.ntiles, k_next,
+                       "iv evaluation %d: quotes coarse %lld / own+tangent %lld / own %lld, "
+                       "points %lld / %lld / %lld, next %d per quote, %.3f ms\n",
+                       e, static_cast<long long>(ws[0].nq), static_cast<long long>(ws[1].nq),
+                       static_cast<long long>(ws[2].nq), static_cast<long long>(ws[0].mw),
+                       static_cast<long long>(ws[1].mw), static_cast<long long>(ws[2].mw), k_next,
                        ms);
       }
+      for (int L = 0; L < 3; ++L) level_evals[L] = static_cast<int64_t>(level_slot_evals[L]);
       check(cudaMemcpyAsync(hr.data(), R, sizeof(IvOut) * m, cudaMemcpyDeviceToHost, st), "D2H results");
       check(cudaStreamSynchronize(st), "stream synchronize");
     }
@@ -826,14 +1153,17 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
     ctx->stats.total_ms = ms_since(t_start);
     ctx->stats.kernel_launches = launches;
     ctx->stats.options = static_cast<int64_t>(slot_evals);
+    for (int L = 0; L < 3; ++L) ctx->stats.iv_evals[L] = level_evals[L];
     ctx->stats.tiles = evaluations;
     ctx->stats.algo_flops = m > 0 ? b->algo_flops * slot_evals / static_cast<double>(m) : 0.0;
     if (out_failed) *out_failed = failed;
     if (failed && err) set_err(err, MANGO_OK, first.empty() ? "root finding failed" : first);
     destroy_batch(b);
+    if (bc) destroy_batch(bc);
     return MANGO_OK;
   } catch (const std::exception& e) {
     if (b) destroy_batch(b);
+    if (bc) destroy_batch(bc);
     set_err(err, MANGO_ERR_SOLVER, e.what());
     return MANGO_ERR_SOLVER;
   }

@@ -1,0 +1,87 @@
+"""GPU FDM implied volatility by Newton on the exact discrete vega
+(MANGO_GPU_IV_NEWTON).
+
+Every evaluation prices the quote with the forward-mode march, so it yields
+V and dV/dsigma of the discrete price; Newton runs on a coarse grid first and
+then on the quote's own grid, and stops in volatility space: the returned
+root is one corrected Newton step beyond the last evaluation.  Bars:
+
+* against the reference's own Brent roots (iv.npz, produced by the
+  reference IVSolver): |sigma_newton - sigma_brent| <= tol / vega + 3e-7
+  (Brent stops within tol / vega of the exact root, Newton within 3e-7),
+  and within 1e-6 of the volatility the quote was priced at;
+* round trip on 2,048 quotes drawn like the batched-IV workload (true vol
+  U[0.05, 0.8], K/S U[0.8, 1.2], T U[0.02, 2]) priced at their true vol on the
+  101 x 498 grid sized at that vol: every quote whose discrete vega at the
+  true vol is at least 1e-4 (the reference InterpolatedIVSolver's default
+  vega_threshold) settles within 1e-6 of the true vol, except where the
+  objective has a second root (V(sigma) = P re-priced at the returned root,
+  to 1e-9 relative) -- at most 0.2 % of them on this sample;
+* statuses: settled quotes are MANGO_OK; quotes Newton hands over are
+  solved by Brent, so every status is one Brent can return.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+
+
+def per_quote_grid(pkg, vol, nx=101, nt=498):
+    return pkg.grid_array(len(vol), pkg.GRID_FIXED_N_AT_VOL, nx, nt, alpha=vol)
+
+
+def test_newton_vs_reference_golden(engine, pkg):
+    g = golden("iv.npz")
+    q = pkg.query_array(g["S"], g["K"], g["T"], g["r"], g["q"], g["is_put"], g["price"])
+    grids = per_quote_grid(pkg, g["true_vol"])
+    out = engine.solve_iv_arrays(q, grids, method=pkg.IV_NEWTON)
+    st = engine.stats()
+    assert st["iv_evals"][0] > 0 and st["iv_evals"][1] > 0
+    assert (out["status"] == 0).all()
+    sig = out["implied_vol"]
+    p = pkg.pricing_array(g["S"], g["K"], g["T"], sig, g["r"], g["q"], g["is_put"])
+    vega = np.abs(engine.tangent_arrays(p, grids, vega_only=True)["vega"])
+    # Brent's root is within tol / vega of the exact root of the discrete
+    # objective, Newton's within its volatility-space stop (2e-7 plus the
+    # third-order bound)
+    d = np.abs(sig - g["out"][:, 0])
+    assert (d <= TOL / vega + 3e-7).all(), f"worst {d.max():.3e}"
+    assert np.abs(sig - g["true_vol"]).max() < 1e-6
+
+
+def test_newton_round_trip_config_sample(engine, pkg):
+    rng = np.random.default_rng(4243)
+    n = 2048
+    S = np.full(n, 100.0)
+    K = S * rng.uniform(0.8, 1.2, n)
+    T = rng.uniform(0.02, 2.0, n)
+    r = rng.uniform(0.0, 0.08, n)
+    q = rng.uniform(0.0, 0.04, n)
+    vt = rng.uniform(0.05, 0.8, n)
+    put = (np.arange(n) % 4 != 3).astype(np.int32)
+    grids = per_quote_grid(pkg, vt)
+    truth = engine.tangent_arrays(pkg.pricing_array(S, K, T, vt, r, q, put), grids, vega_only=True)
+    assert (truth["status"] == 0).all()
+    quotes = pkg.query_array(S, K, T, r, q, put, truth["value"])
+    out = engine.solve_iv_arrays(quotes, grids, method=pkg.IV_NEWTON)
+    st = engine.stats()
+    valid = out["status"] != pkg.MANGO_ERR_VALIDATION
+    valid &= out["status"] != pkg.MANGO_ERR_ARBITRAGE
+    assert np.isin(out["status"][valid], (0, pkg.MANGO_ERR_BRACKETING, pkg.MANGO_ERR_NO_CONVERGENCE)).all()
+    keep = valid & (np.abs(truth["vega"]) >= 1e-4)
+    assert (out["status"][keep] == 0).all()
+    err = np.abs(out["implied_vol"] - vt)
+    miss = keep & ~(err <= 1e-6)
+    if miss.any():
+        # a miss must be another root of the discrete objective
+        sel = lambda a: np.asarray(a)[miss]
+        v = engine.price_arrays(pkg.pricing_array(sel(S), sel(K), sel(T), out["implied_vol"][miss], sel(r),
+                                                  sel(q), sel(put)), grids[miss])["value"]
+        assert np.abs(v - sel(truth["value"])).max() <= 1e-9 * sel(truth["value"]).max() + TOL
+    assert miss.sum() <= 0.002 * keep.sum() + 1, (miss.sum(), keep.sum())
+    # Newton-settled quotes need few evaluations on their own grid
+    assert st["iv_evals"][1] <= 2.5 * keep.sum()

@@ -80,7 +80,8 @@ def test_tangent_vs_oracle_tangent(engine, pkg, oracle):
     params = inputs(pkg, 24, 21, True)
     grid = pkg.grid_array(1, pkg.GRID_FIXED_N, 101, 498)
     tan = engine.tangent_arrays(params, grid)
-    assert (tan["status"] == 0).all()
+    one = engine.tangent_arrays(params, grid, vega_only=True)
+    assert (tan["status"] == 0).all() and (one["status"] == 0).all()
     for i in range(params.size):
         x, _ = pkg.resolve_grid(params[i:i + 1], pkg.FixedGrid(101, 498))
         p = params[i]
@@ -91,3 +92,21 @@ def test_tangent_vs_oracle_tangent(engine, pkg, oracle):
         assert abs(tan["delta"][i] - t6[1]) <= 1e-9, i
         for col, k in ((2, "vega"), (3, "rho"), (4, "dividend_rho"), (5, "dstrike")):
             assert abs(tan[k][i] - t6[col]) <= 1e-8 * abs(t6[col]) + 1e-9, (i, k, tan[k][i], t6[col])
+        assert abs(one["vega"][i] - t6[2]) <= 1e-8 * abs(t6[2]) + 1e-9, (i, one["vega"][i], t6[2])
+
+
+def test_vega_batch_matches_three_direction_tangent(engine, pkg):
+    """mango_gpu_price_american_vega_batch carries the volatility tangent
+    alone: its value and delta equal the three-direction march's bit for bit
+    (the same primal), its vega and dV/dK to 1e-10 relative (the same
+    formulas, compiled with another contraction order)."""
+    params = inputs(pkg, 256, 5, True)
+    for grid in (pkg.grid_array(1, pkg.GRID_FIXED_N, 101, 498), None):
+        full = engine.tangent_arrays(params, grid)
+        one = engine.tangent_arrays(params, grid, vega_only=True)
+        assert (one["status"] == 0).all() and (full["status"] == 0).all()
+        for k in ("value", "delta"):
+            assert (one[k] == full[k]).all(), k
+        for k in ("vega", "dstrike"):
+            assert np.allclose(one[k], full[k], rtol=1e-10, atol=1e-12), (k, np.abs(one[k] - full[k]).max())
+        assert np.isnan(one["rho"]).all() and np.isnan(one["dividend_rho"]).all()

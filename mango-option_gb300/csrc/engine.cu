@@ -4,6 +4,7 @@
 // caught at the boundary (mango_c_api.cpp:354-360), per-slot status for batch
 // calls (mango_c_api.cpp:523-576).
 #include "engine.hpp"
+#include "wmarch.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -281,7 +282,7 @@ void destroy_batch(MangoGpuBatch* b) {
   if (!b) return;
   for (mgpu::DevBuf* d : {&b->d_pool, &b->d_xs, &b->d_flags, &b->d_opts, &b->d_tiles, &b->d_mode,
                           &b->d_status, &b->d_out4, &b->d_queue, &b->d_tv, &b->d_tv_tp,
-                          &b->d_tv_curve, &b->d_tv_ev})
+                          &b->d_tv_curve, &b->d_tv_ev, &b->d_wt, &b->d_tile_warp})
     d->release();
   for (mgpu::HostBuf* h : {&b->h_xs, &b->h_opts, &b->h_tiles, &b->h_out4, &b->h_status})
     h->release();
@@ -347,6 +348,8 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
   b->h2d_bytes = 0;
   b->host_prep_ms = 0;
   b->tv_tile0 = 0;
+  b->wplan_ready = false;
+  b->nwt = 0;
   b->ran = false;
   b->runs = 0;
   for (auto& e : b->ev)
@@ -621,6 +624,24 @@ void run_batch(MangoGpuBatch* b) {
   check(cudaGetLastError(), "prep_kernel launch");
   check(cudaEventRecord(b->ev[3], st), "event");
   check(cudaEventRecord(b->run_ev[slot + 1], st), "event");
+  if (!b->wplan_ready) {
+    const int tv0 = b->mc.tv_first < m ? b->tv_tile0 : ntiles;
+    const WarpPlan plan = plan_warp_tiles(b->h_tiles.as<TileDev>(), ntiles, tv0, ctx->num_sms);
+    b->nwt = static_cast<int32_t>(plan.tiles.size());
+    b->wR = plan.R;
+    if (b->nwt > 0) {
+      // pageable sources: staged before the calls return
+      check(cudaMemcpyAsync(b->d_wt.get(sizeof(int32_t) * b->nwt), plan.tiles.data(),
+                            sizeof(int32_t) * b->nwt, cudaMemcpyHostToDevice, st),
+            "H2D warp tiles");
+      check(cudaMemcpyAsync(b->d_tile_warp.get(static_cast<size_t>(ntiles)), plan.flag.data(),
+                            static_cast<size_t>(ntiles), cudaMemcpyHostToDevice, st),
+            "H2D warp flags");
+    }
+    b->wplan_ready = true;
+  }
+  MarchConst mc = b->mc;
+  mc.tile_warp = b->nwt > 0 ? b->d_tile_warp.as<uint8_t>() : nullptr;
   const int warps_per_block = 4;
   int bps = ctx->march_blocks_per_sm;
   // MANGO_GPU_MARCH_BLOCKS_PER_SM: resident march blocks per SM (1 to the
@@ -631,10 +652,13 @@ void run_batch(MangoGpuBatch* b) {
   }
   const int blocks = std::max(1, std::min<int>(ctx->num_sms * bps,
                                                (ntiles + warps_per_block - 1) / warps_per_block));
-  march_kernel<<<blocks, 32 * warps_per_block, 0, st>>>(d_tiles, ntiles, d_opts, d_pool, d_flags,
-                                                        d_mode, d_status, b->d_queue.as<int>(),
-                                                        b->mc);
+  if (b->nwt < ntiles)
+    march_kernel<<<blocks, 32 * warps_per_block, 0, st>>>(d_tiles, ntiles, d_opts, d_pool,
+                                                          d_flags, d_mode, d_status,
+                                                          b->d_queue.as<int>(), mc);
   check(cudaGetLastError(), "march_kernel launch");
+  wmarch_launch(st, ctx->num_sms, d_tiles, b->d_wt.as<int32_t>(), b->nwt, d_opts, d_pool, d_flags,
+                d_mode, d_status, b->d_queue.as<int>() + 1, mc, b->wR);
   if (b->mc.tv_first < m) {
     const int tv_tiles = ntiles - b->tv_tile0;
     const int tv_blocks = std::max(1, std::min<int>(ctx->num_sms * 8, (tv_tiles + 3) / 4));
@@ -702,7 +726,9 @@ uint64_t fetch_batch(MangoGpuBatch* b, MangoGpuAmericanOut* out, std::string* fi
   S.algo_flops = b->algo_flops;
   S.h2d_bytes = b->h2d_bytes;
   S.host_prep_ms = b->host_prep_ms;
-  S.kernel_launches = m > 0 ? (b->mc.tv_first < m ? 4 : 3) : 0;
+  S.kernel_launches = m > 0 ? (2 + (b->nwt < b->ntiles ? 1 : 0) + (b->nwt > 0 ? 1 : 0) +
+                               (b->mc.tv_first < m ? 1 : 0))
+                            : 0;
   return failed;
 }
 

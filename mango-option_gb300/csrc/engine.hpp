@@ -180,6 +180,10 @@ struct MangoGpuBatch {
   // explicit time points, yield-curve pairs, dividend-event pairs.
   mgpu::DevBuf d_tv, d_tv_tp, d_tv_curve, d_tv_ev;
   int32_t tv_tile0 = 0;  // first tile holding a time-varying option
+  // Tiles marched one warp per option (wmarch.cu), planned on the first run.
+  bool wplan_ready = false;
+  int32_t nwt = 0, wR = 0;
+  mgpu::DevBuf d_wt, d_tile_warp;
   mgpu::HostBuf h_xs, h_opts, h_tiles, h_out4, h_status;
   cudaEvent_t ev[8] = {};
   bool ran = false;

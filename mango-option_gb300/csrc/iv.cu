@@ -51,6 +51,7 @@
 #include "brent.cuh"
 #include "engine.hpp"
 #include "march_tan.cuh"
+#include "wmarch.cuh"
 
 namespace mgpu {
 
@@ -727,7 +728,7 @@ struct WorkSet {
   std::vector<int32_t> map_h, src_h, pt_h, qlist_h, qbase_h;
   std::vector<TileDev> tiles_h;
   DevBuf d_tiles, d_opts, d_xs, d_map, d_src, d_pt, d_qlist, d_qbase, d_sigma, d_active, d_pool,
-      d_flags, d_mode, d_status, d_out4, d_tv, d_tpool;
+      d_flags, d_mode, d_status, d_out4, d_tv, d_tpool, d_wt, d_twarp;
   // First slot of a time-varying quote (slots follow the batch order, where
   // those quotes come last), or INT32_MAX.
   int32_t tv_first = 0x7fffffff;
@@ -735,7 +736,7 @@ struct WorkSet {
   ~WorkSet() {
     for (DevBuf* d : {&d_tiles, &d_opts, &d_xs, &d_map, &d_src, &d_pt, &d_qlist, &d_qbase,
                       &d_sigma, &d_active, &d_pool, &d_flags, &d_mode, &d_status, &d_out4, &d_tv,
-                      &d_tpool})
+                      &d_tpool, &d_wt, &d_twarp})
       d->release();
   }
 
@@ -1071,13 +1072,31 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
           } else {
             const int blocks = std::max(
                 1, std::min<int>(ctx->num_sms * ctx->march_blocks_per_sm, (ntiles + 3) / 4));
+            // few points left: one warp per option (wmarch.cu)
+            const WarpPlan plan = plan_warp_tiles(
+                w.tiles_h.data(), ntiles, w.tv_first < w.mw ? w.tv_first / kTile : ntiles,
+                ctx->num_sms);
+            const int nwt = static_cast<int>(plan.tiles.size());
+            if (nwt > 0) {
+              check(cudaMemcpyAsync(w.d_wt.get(sizeof(int32_t) * nwt), plan.tiles.data(),
+                                    sizeof(int32_t) * nwt, cudaMemcpyHostToDevice, st),
+                    "H2D warp tiles");
+              check(cudaMemcpyAsync(w.d_twarp.get(static_cast<size_t>(ntiles)), plan.flag.data(),
+                                    static_cast<size_t>(ntiles), cudaMemcpyHostToDevice, st),
+                    "H2D warp flags");
+              mc.tile_warp = w.d_twarp.as<uint8_t>();
+            }
             prep_kernel<<<(threads + 127) / 128, 128, 0, st>>>(tiles, ntiles, wopts, xs,
                                                                w.d_pool.as<double>(),
                                                                w.d_flags.as<uint8_t>(),
                                                                w.d_mode.as<int32_t>(), mc);
-            march_kernel<<<blocks, 128, 0, st>>>(tiles, ntiles, wopts, w.d_pool.as<double>(),
-                                                 w.d_flags.as<uint8_t>(), w.d_mode.as<int32_t>(),
-                                                 w.d_status.as<int32_t>(), queue, mc);
+            if (nwt < ntiles)
+              march_kernel<<<blocks, 128, 0, st>>>(tiles, ntiles, wopts, w.d_pool.as<double>(),
+                                                   w.d_flags.as<uint8_t>(), w.d_mode.as<int32_t>(),
+                                                   w.d_status.as<int32_t>(), queue, mc);
+            wmarch_launch(st, ctx->num_sms, tiles, w.d_wt.as<int32_t>(), nwt, wopts,
+                          w.d_pool.as<double>(), w.d_flags.as<uint8_t>(), w.d_mode.as<int32_t>(),
+                          w.d_status.as<int32_t>(), b->d_queue.as<int>() + 3, mc, plan.R);
             if (w.tv_first < w.mw) {
               const int t0 = w.tv_first / kTile;
               const int tvb = std::max(1, std::min<int>(ctx->num_sms * 8, (ntiles - t0 + 3) / 4));

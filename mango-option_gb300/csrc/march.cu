@@ -422,6 +422,7 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
     if (lane == 0) t = atomicAdd(queue, 1);
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= ntiles) break;
+    if (mc.tile_warp && mc.tile_warp[t]) continue;  // marched one warp per option
     const TileDev td = tiles[t];
     const int k = td.first + lane;
     const bool active = lane < td.count && (!mc.active || mc.active[k]) && k < mc.tv_first;

@@ -83,6 +83,9 @@ struct MarchConst {
   // Sorted index of the first option on the time-varying march
   // (march_tv.cu); options from here on are skipped by prep and march.
   int32_t tv_first = 0x7fffffff;
+  // Per tile, nonzero: the tile's options are marched one warp per option
+  // (wmarch.cu) and march_kernel skips it; null: every tile on march_kernel.
+  const uint8_t* tile_warp = nullptr;
 };
 
 // Per-option data of the time-varying march, indexed by sorted index minus

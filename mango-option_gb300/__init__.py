@@ -1173,6 +1173,52 @@ def american_option_price(params: PricingParams, grid=None) -> AmericanOptionRes
     return AmericanOptionResult(out[0], params)
 
 
+def american_option_price_autograd(spot, strike, maturity, volatility, rate, dividend_yield, is_put,
+                                   grid=None, engine: Optional[Engine] = None):
+    """Differentiable American prices for torch: the values of a batch of
+    options (mango_gpu_price_american_tangent_batch), with gradients with
+    respect to volatility, rate, dividend_yield and strike from the exact
+    discrete derivatives of the march (the same grid; the active obstacle
+    set frozen).  Arguments are scalars or 1-D tensors / arrays broadcast to
+    one length; any of volatility, rate, dividend_yield and strike may be a
+    tensor that requires grad.  The result is a float64 tensor on the device
+    of the first tensor argument.  A failed option raises SolverError.
+
+    This is the torch counterpart of the reference's american_option_price
+    binding (src/python/mango_bindings.cpp:580) for a batch, with backward
+    grad_output * [dV/dsigma, dV/dr, dV/dq, dV/dK]."""
+    import torch
+
+    class _AmericanPrice(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, sig, r, q, k, S, T, put):
+            eng = engine or default_engine()
+            host = [np.ascontiguousarray(t.detach().cpu().numpy(), np.float64) for t in (S, k, T, sig, r, q)]
+            params = pricing_array(*host, np.ascontiguousarray(put.detach().cpu().numpy(), np.int32))
+            out = eng.tangent_arrays(params, _grid_entry(grid) if not isinstance(grid, np.ndarray) else grid)
+            bad = np.nonzero(out["status"] != MANGO_OK)[0]
+            if bad.size:
+                raise SolverError(int(out["status"][bad[0]]))
+            dev = sig.device
+            ctx.save_for_backward(*(torch.from_numpy(np.ascontiguousarray(out[f])).to(dev)
+                                    for f in ("vega", "rho", "dividend_rho", "dstrike")))
+            return torch.from_numpy(np.ascontiguousarray(out["value"])).to(dev)
+
+        @staticmethod
+        def backward(ctx, g):
+            vega, rho, drho, dk = ctx.saved_tensors
+            return g * vega, g * rho, g * drho, g * dk, None, None, None
+
+    args = [spot, strike, maturity, volatility, rate, dividend_yield, is_put]
+    dev = next((a.device for a in args if isinstance(a, torch.Tensor)), torch.device("cpu"))
+    ts = [a if isinstance(a, torch.Tensor) else torch.as_tensor(np.asarray(a, np.float64), device=dev)
+          for a in args]
+    n = max(t.numel() for t in ts)
+    S, K, T, sig, r, q, put = (t.to(torch.float64).reshape(-1).expand(n) if t.numel() == 1
+                               else t.to(torch.float64).reshape(-1) for t in ts)
+    return _AmericanPrice.apply(sig, r, q, K, S, T, put)
+
+
 @dataclasses.dataclass
 class BatchAmericanOptionResult:
     results: list

@@ -167,6 +167,41 @@ int32_t ref_price_solution(double S, double K, double T, double sigma, double r,
   return 0;
 }
 
+// Prices on a frozen grid: the spatial GridSpec comes from the grid rule
+// (estimate_pde_grid pinned to nx points) for the base option (gS, gK, gT,
+// gsigma), then every option i is solved on PDEGridConfig{that spec, nt[i]}
+// with its own parameters.  Central differences of these prices are the
+// reference's frozen-grid sensitivities (the auto grid moves with the
+// volatility and the strike, so differences through it jump).
+int32_t ref_price_frozen(int64_t n, const double* S, const double* K, const double* T,
+                         const double* sigma, const double* r, const double* q,
+                         const int32_t* is_put, const double* gS, const double* gK,
+                         const double* gT, const double* gsigma, const int64_t* nx,
+                         const int64_t* nt, int32_t n_threads, double* out4, int32_t* status) {
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t i = 0; i < n; ++i) {
+    auto pg = make_params(gS[i], gK[i], gT[i], gsigma[i], r[i], q[i], is_put[i]);
+    GridAccuracyParams acc;
+    acc.min_spatial_points = static_cast<size_t>(nx[i]);
+    acc.max_spatial_points = static_cast<size_t>(nx[i]);
+    auto [spec, td] = estimate_pde_grid(pg, acc);
+    (void)td;
+    std::optional<PDEGridSpec> grid = PDEGridSpec{PDEGridConfig{spec, static_cast<size_t>(nt[i]), {}}};
+    auto p = make_params(S[i], K[i], T[i], sigma[i], r[i], q[i], is_put[i]);
+    auto solver = AmericanOptionSolver::create(p, grid);
+    if (!solver) { status[i] = 1; continue; }
+    auto res = solver->solve();
+    if (!res) { status[i] = 5; continue; }
+    status[i] = 0;
+    out4[4 * i + 0] = res->value();
+    out4[4 * i + 1] = res->delta();
+    out4[4 * i + 2] = res->gamma();
+    out4[4 * i + 3] = res->theta();
+  }
+  return 0;
+}
+
 // Grid only (estimate_pde_grid + GridSpec::generate), for the host grid code.
 int32_t ref_make_grid(double S, double K, double T, double sigma, int64_t nx,
                       int64_t cap, double* x_out, int64_t* n_out, int64_t* nt_out) {

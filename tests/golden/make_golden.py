@@ -56,7 +56,14 @@ REF_SO = ROOT / "oracle" / "_ref" / "libmango_ref.so"
 
 
 def _lib():
-    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle" / "ref"), "-j8"], check=True)
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_b", ROOT / "mango-option_gb300" / "build.py")
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    ref = b.reference_dir()
+    if ref is None:
+        sys.exit("the reference tree is needed (MANGO_REFERENCE_DIR or a checkout beside the repository)")
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle" / "ref"), f"REF={ref}", "-j8"], check=True)
     return ctypes.CDLL(str(REF_SO))
 
 
@@ -241,6 +248,9 @@ def main():
 
     golden_bspline(lib)
     golden_table(lib)
+    golden_table_full(lib)
+    golden_iv_config4(lib)
+    golden_greeks_fd(lib)
     golden_surface(lib)
     golden_interp_iv(lib)
     golden_shared(lib)
@@ -717,6 +727,85 @@ def golden_table_greeks(lib):
         assert (st == 0).all()
         kw[f"{name}_greeks"] = out.reshape(n, 4)
     save("table_greeks.npz", sizes=sizes, grids=grids, coeffs=coeffs, params=p, **kw)
+
+
+def golden_table_full(lib):
+    """The table-build workload's sweep at full size: 50 x 30 x 20 x 10 axes,
+    200 (vol, rate) slices, the explicit 201 x 1000 grid (the reference's
+    per-slice fallback route)."""
+    axes = table_axes(50, 30, 20, 10)
+    alpha = 2.0 * np.arcsinh(5.0 / np.sqrt(2.0))
+    nm, nt, ns, nr = (a.size for a in axes)
+    out = np.zeros(nm * nt * ns * nr)
+    dims = np.zeros(2 * ns * nr, np.int64)
+    rc = lib.ref_table_sweep(P(axes[0]), ctypes.c_int64(nm), P(axes[1]), ctypes.c_int64(nt), P(axes[2]),
+                             ctypes.c_int64(ns), P(axes[3]), ctypes.c_int64(nr), ctypes.c_double(100.0),
+                             ctypes.c_double(0.0), ctypes.c_int32(1), ctypes.c_int32(1),
+                             ctypes.c_double(-3.0), ctypes.c_double(3.0), ctypes.c_int64(201),
+                             ctypes.c_double(alpha), ctypes.c_int64(1000), P(out), P(dims))
+    assert rc == 0
+    save("table_full.npz", m=axes[0], tau=axes[1], sigma=axes[2], r=axes[3], alpha=np.array(alpha),
+         tensor=out.reshape(nm, nt, ns, nr), dims=dims.reshape(ns * nr, 2))
+
+
+def golden_iv_config4(lib):
+    """4,096 quotes of the batched-IV workload's distributions (true vol
+    U[0.05, 0.8], K/S U[0.8, 1.2], T U[0.02, 2], r U[0, 0.08], q U[0, 0.04],
+    3 in 4 puts), priced by the reference at the true vol on the 101 x 498
+    grid rule sized at that vol, and inverted by the reference's IVSolver
+    (Brent) on the same grid."""
+    rng = np.random.default_rng(4244)
+    n = 4096
+    S = np.full(n, 100.0)
+    K = S * rng.uniform(0.8, 1.2, n)
+    T = rng.uniform(0.02, 2.0, n)
+    r = rng.uniform(0.0, 0.08, n)
+    q = rng.uniform(0.0, 0.04, n)
+    vt = rng.uniform(0.05, 0.8, n)
+    put = (np.arange(n) % 4 != 3).astype(np.int32)
+    nx = np.full(n, 101)
+    nt = np.full(n, 498)
+    out, _, pst = price(lib, S, K, T, vt, r, q, put, nx, nt)
+    assert (pst == 0).all()
+    px = out[:, 0].copy()
+    o3 = np.full(3 * n, np.nan)
+    st = np.zeros(n, np.int32)
+    f = [np.ascontiguousarray(a, dtype=np.float64) for a in (S, K, T, r, q)]
+    lib.ref_iv_batch(ctypes.c_int64(n), *(P(a) for a in f), P(put), P(px), P(vt),
+                     P(np.ascontiguousarray(nx, np.int64)), P(np.ascontiguousarray(nt, np.int64)),
+                     ctypes.c_int32(0), P(o3), P(st))
+    save("iv_config4.npz", S=S, K=K, T=T, r=r, q=q, is_put=put, price=px, true_vol=vt, nx=nx, nt=nt,
+         out=o3.reshape(n, 3), status=st)
+
+
+def golden_greeks_fd(lib):
+    """1,024 American puts of the differentiation workload (config-0
+    distributions, 101 x 498 grid rule): the reference's prices at the
+    option and at the eight bumped parameter sets of a central difference
+    (h = 1e-5: sigma h, max(|r|, 1e-2) h, max(q, 1e-2) h clipped at q = 0,
+    K h), all on the option's own frozen grid."""
+    n = 1024
+    S, K, T, sig, r, q, put = config0_inputs(n, 3, False)
+    h = 1e-5
+    hs, hr = sig * h, np.maximum(np.abs(r), 1e-2) * h
+    hq, hk = np.maximum(q, 1e-2) * h, K * h
+    qdn = np.maximum(q - hq, 0.0)
+    sets = [(sig, r, q, K), (sig + hs, r, q, K), (sig - hs, r, q, K), (sig, r + hr, q, K), (sig, r - hr, q, K),
+            (sig, r, q + hq, K), (sig, r, qdn, K), (sig, r, q, K + hk), (sig, r, q, K - hk)]
+    vals = np.zeros((9, n))
+    nx = np.full(n, 101, np.int64)
+    nt = np.full(n, 498, np.int64)
+    for j, (s_, r_, q_, k_) in enumerate(sets):
+        out = np.zeros(4 * n)
+        st = np.zeros(n, np.int32)
+        f = [np.ascontiguousarray(a, dtype=np.float64) for a in (S, k_, T, s_, r_, q_, S, K, T, sig)]
+        lib.ref_price_frozen(ctypes.c_int64(n), *(P(a) for a in f[:6]), P(put), *(P(a) for a in f[6:]),
+                             P(nx), P(nt), ctypes.c_int32(0), P(out), P(st))
+        assert (st == 0).all()
+        vals[j] = out.reshape(n, 4)[:, 0]
+    fd = {"vega": (vals[1] - vals[2]) / (2 * hs), "rho": (vals[3] - vals[4]) / (2 * hr),
+          "dividend_rho": (vals[5] - vals[6]) / (q + hq - qdn), "dstrike": (vals[7] - vals[8]) / (2 * hk)}
+    save("greeks_fd.npz", S=S, K=K, T=T, sigma=sig, r=r, q=q, is_put=put, h=np.array(h), prices=vals, **fd)
 
 
 if __name__ == "__main__":

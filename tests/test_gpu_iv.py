@@ -44,9 +44,10 @@ def test_iv_vs_oracle_sample(engine, pkg, oracle):
     ok = (st == 0)
     assert (out["status"][ok] == 0).all()
     # Same Brent path: identical iteration counts; final residuals |f(b)| equal
-    # up to price rounding noise (they are 1e-9..1e-12 dollars themselves).
+    # up to price rounding noise (the march's last bits depend on the order
+    # of its recurrences: one lane per option or one warp per option).
     assert (out["iterations"][ok] == ref[ok, 1]).all()
-    assert np.abs(out["final_error"][ok] - ref[ok, 2]).max() < 1e-10
+    assert np.abs(out["final_error"][ok] - ref[ok, 2]).max() < 1e-9
     # Vols within 1e-8, except where the quote is ill-conditioned: Brent
     # stops at |f| < 1e-6 in price units, so a rounding-level price
     # difference dp moves the root by dp / vega.  Allow 1e-11 dollars.
@@ -89,3 +90,35 @@ def test_iv_solver_mirror(pkg):
                                    option_type=pkg.OptionType.PUT, market_price=float(px["value"][0])))
     assert abs(res.implied_vol - 0.25) < 1e-6
     assert p.volatility == 0.25
+
+
+# IVErrorCode (src/support/error_types.hpp:116-135) + 10 in the fixture ->
+# the status the C ABI reports (map_iv_error, src/ffi/mango_c_api.cpp:124-141)
+REF_STATUS = {0: 0, 13: 1, 14: 2, 18: 3, 19: 4}
+
+
+def test_iv_config4_sample_vs_reference_brent(engine, pkg):
+    """4,096 quotes of the batched-IV workload (true vol U[0.05, 0.8], K/S
+    U[0.8, 1.2], T U[0.02, 2]) priced and inverted by the reference's
+    IVSolver on each quote's 101 x 498 grid: identical statuses and Brent
+    iteration counts, roots within 1e-8 (plus 1e-11 / vega for the
+    ill-conditioned quotes, as against the oracle)."""
+    g = golden("iv_config4.npz")
+    q = pkg.query_array(g["S"], g["K"], g["T"], g["r"], g["q"], g["is_put"], g["price"])
+    grids = per_quote_grid(pkg, g["true_vol"])
+    out = engine.solve_iv_arrays(q, grids)
+    want = np.array([REF_STATUS[int(s)] for s in g["status"]])
+    diff = out["status"] != want
+    # a quote whose price sits within rounding of the objective's value at a
+    # bracket end can flip between solved and not bracketed; nothing else
+    assert np.isin(out["status"][diff], (0, 4)).all() and np.isin(want[diff], (0, 4)).all(), \
+        list(zip(np.nonzero(diff)[0][:8], out["status"][diff][:8], want[diff][:8]))
+    assert diff.sum() <= 4, diff.sum()
+    ok = (want == 0) & ~diff
+    assert (out["iterations"][ok] == g["out"][ok, 1]).all()
+    sig = out["implied_vol"]
+    p = pkg.pricing_array(g["S"], g["K"], g["T"], np.where(ok, sig, 0.2), g["r"], g["q"], g["is_put"])
+    vega = np.abs(engine.tangent_arrays(p, grids, vega_only=True)["vega"])
+    d = np.abs(sig - g["out"][:, 0])
+    allowed = 1e-8 + 1e-11 / np.maximum(vega, 1e-12)
+    assert (d[ok] <= allowed[ok]).all(), f"worst {d[ok].max():.3e}"

@@ -85,3 +85,36 @@ def test_newton_round_trip_config_sample(engine, pkg):
     assert miss.sum() <= 0.002 * keep.sum() + 1, (miss.sum(), keep.sum())
     # Newton-settled quotes need few evaluations on their own grid
     assert st["iv_evals"][1] <= 2.5 * keep.sum()
+
+
+REF_STATUS = {0: 0, 13: 1, 14: 2, 18: 3, 19: 4}
+
+
+def test_newton_config4_sample_vs_reference(engine, pkg):
+    """The 4,096 reference quotes of iv_config4.npz (the reference IVSolver's
+    Brent roots on each quote's 101 x 498 grid).  Validation and arbitrage
+    statuses are the reference's; every quote the reference solves is solved;
+    a quote Brent cannot bracket may still be settled.  Roots: within
+    tol / vega + 3e-7 of the reference's for at least 99.5 % of the solved
+    quotes, and every other one re-prices to within tol of its quote (a root
+    of the same objective where it is flat or not monotone)."""
+    g = golden("iv_config4.npz")
+    q = pkg.query_array(g["S"], g["K"], g["T"], g["r"], g["q"], g["is_put"], g["price"])
+    grids = per_quote_grid(pkg, g["true_vol"])
+    out = engine.solve_iv_arrays(q, grids, method=pkg.IV_NEWTON)
+    want = np.array([REF_STATUS[int(s)] for s in g["status"]])
+    invalid = np.isin(want, (1, 2))
+    assert (out["status"][invalid] == want[invalid]).all()
+    ok = want == 0
+    assert (out["status"][ok] == 0).all()
+    brk = want == 4
+    assert np.isin(out["status"][brk], (0, 4)).all()
+    sig = out["implied_vol"]
+    p = pkg.pricing_array(g["S"], g["K"], g["T"], np.where(ok, sig, 0.2), g["r"], g["q"], g["is_put"])
+    t = engine.tangent_arrays(p, grids, vega_only=True)
+    vega = np.abs(t["vega"])
+    d = np.abs(sig - g["out"][:, 0])
+    close = d <= TOL / np.maximum(vega, 1e-12) + 3e-7
+    assert close[ok].mean() >= 0.995, close[ok].mean()
+    far = ok & ~close
+    assert (np.abs(t["value"][far] - g["price"][far]) < TOL).all()

@@ -1,8 +1,9 @@
 """GPU price-table sweep and 4D B-spline query against the reference.
 
 Table: PriceTableBuilderND<4> sweep + extraction on reduced axes, explicit
-201 x 1000 grid (the per-slice fallback route) and the default accuracy route;
-bar 1e-9 relative on the normalized prices, identical per-slice grids.
+201 x 1000 grid (the per-slice fallback route) and the default accuracy route,
+and the full 50 x 30 x 20 x 10 sweep of the table-build workload; bar 1e-9
+relative on the normalized prices, identical per-slice grids.
 Query: BSplineND<double,4>::eval on the 50x30x20x10 axes; bar 1e-12 relative
 (plus 1e-14 of the largest coefficient for results near zero), knots exact."""
 import numpy as np
@@ -25,23 +26,19 @@ def test_table_sweep_vs_reference(engine, pkg, route):
     assert not bad.any(), f"max abs diff {np.abs(tensor - want).max():.3e}"
 
 
-def test_table_sweep_full_axes_properties(engine, pkg):
-    """Config-2 shape (50 x 30 x 20 x 10, 200 slices on the explicit 201 x 1000
-    grid): no failures, finite values near [intrinsic, 1].  The reference
-    resamples snapshots with an unclamped cubic spline (which can dip slightly
-    below intrinsic near the payoff kink) and, for the lowest volatilities,
-    evaluates it just outside the slice's PDE domain, so no monotonicity in
-    volatility is asserted; the reduced-axes test above pins the values."""
-    m = np.linspace(np.log(0.7), np.log(1.3), 50)
-    tau = np.linspace(0.02, 2.0, 30)
-    sig = np.linspace(0.05, 0.8, 20)
-    r = np.linspace(0.0, 0.08, 10)
-    tensor, dims, failed = engine.price_table_sweep(m, tau, sig, r, 100.0, 0.0, 1,
+def test_table_sweep_full_axes_vs_reference(engine, pkg):
+    """The table-build workload's sweep at full size (50 x 30 x 20 x 10 axes,
+    200 slices on the explicit 201 x 1000 grid, the reference's per-slice
+    fallback route) against the reference's own tensor (table_full.npz):
+    identical per-slice grids, every entry within 1e-9 relative (+1e-12)."""
+    g = golden("table_full.npz")
+    tensor, dims, failed = engine.price_table_sweep(g["m"], g["tau"], g["sigma"], g["r"], 100.0, 0.0, 1,
                                                     pkg.PDEGridConfig(-3.0, 3.0, 201, 1000))
-    assert failed == 0 and np.isfinite(tensor).all()
-    assert (dims[:, 0] == 201).all() and dims[:, 1].max() == 1000
-    intrinsic = np.maximum(1.0 - np.exp(m), 0.0)[:, None, None, None]
-    assert (tensor >= intrinsic - 5e-3).all() and (tensor <= 1.0).all()
+    assert failed == 0
+    assert (dims == g["dims"]).all()
+    want = g["tensor"]
+    bad = np.abs(tensor - want) > 1e-9 * np.abs(want) + 1e-12
+    assert not bad.any(), f"{bad.sum()} entries; max abs diff {np.abs(tensor - want).max():.3e}"
 
 
 def test_bspline_query_vs_reference(engine, pkg):

@@ -68,7 +68,9 @@ def test_layouts_auto_grids(engine, pkg, monkeypatch, layout):
 
 def test_warp_matches_thread_layout(engine, pkg, monkeypatch):
     """512 puts and calls on uneven grids (51..401 points, 100..600 steps):
-    the two layouts agree to 1e-11 relative."""
+    the two layouts agree to 1e-11 relative on value, delta and gamma;
+    theta, a one-step difference over dt, amplifies that rounding by 1/dt
+    and agrees to 1e-9."""
     rng = np.random.default_rng(99)
     n = 512
     p = pkg.pricing_array(np.full(n, 100.0), rng.uniform(70, 130, n), rng.uniform(0.05, 2.0, n),
@@ -80,4 +82,6 @@ def test_warp_matches_thread_layout(engine, pkg, monkeypatch):
         monkeypatch.setenv("MANGO_GPU_WARP_MARCH", layout)
         outs[layout] = engine.price_arrays(p, grid)
         assert (outs[layout]["status"] == 0).all()
-    check(greeks(outs["1"]), greeks(outs["0"]), rtol=1e-11, atol=1e-13)
+    a, b = greeks(outs["1"]), greeks(outs["0"])
+    check(a[:, :3], b[:, :3], rtol=1e-11, atol=1e-13)
+    check(a[:, 3], b[:, 3], rtol=1e-9, atol=1e-11)

@@ -143,3 +143,46 @@ def test_oracle_bspline_vs_reference(oracle):
                                           ctypes.c_int64(q.shape[0]), oracle.P(out)) == 0
     bound = 1e-12 * np.abs(g["out"]) + 1e-14 * np.abs(coeffs).max()
     assert (np.abs(out - g["out"]) <= bound).all()
+
+
+def test_oracle_iv_config4_sample(oracle):
+    """256 quotes of iv_config4.npz: the oracle's Brent finds the reference's
+    roots with the same iteration counts, and fails where it fails."""
+    g = golden("iv_config4.npz")
+    sel = np.arange(0, 4096, 16)
+    out, st = oracle.iv_batch(*(g[k][sel] for k in ("S", "K", "T", "r", "q", "is_put", "price", "true_vol",
+                                                     "nx", "nt")))
+    ok = g["status"][sel] == 0
+    assert ((st == 0) == ok).all()
+    assert np.abs(out[ok, 0] - g["out"][sel][ok, 0]).max() < 1e-9
+    assert (out[ok, 1] == g["out"][sel][ok, 1]).all()
+
+
+def test_oracle_frozen_grid_prices(oracle):
+    """The reference's bumped prices of greeks_fd.npz on each option's frozen
+    grid, for 16 options: the oracle on the same grid agrees to 1e-10."""
+    import ctypes
+
+    from oracle_lib import Accuracy, P, Spec, lib
+
+    g = golden("greeks_fd.npz")
+    h = float(g["h"])
+    for i in range(0, 1024, 64):
+        S, K, T, s, r, q = (float(g[k][i]) for k in ("S", "K", "T", "sigma", "r", "q"))
+        acc = Accuracy()
+        lib().mo_default_accuracy(ctypes.byref(acc))
+        acc.min_spatial_points = acc.max_spatial_points = 101
+        spec = Spec()
+        nt = ctypes.c_int64()
+        c = ctypes.c_double
+        lib().mo_estimate_grid(c(S), c(K), c(T), c(s), ctypes.byref(acc), ctypes.byref(spec), ctypes.byref(nt))
+        x = np.zeros(spec.n_points)
+        lib().mo_generate_grid(ctypes.byref(spec), P(x))
+        hs, hr, hq, hk = s * h, max(abs(r), 1e-2) * h, max(q, 1e-2) * h, K * h
+        sets = [(s, r, q, K), (s + hs, r, q, K), (s - hs, r, q, K), (s, r + hr, q, K), (s, r - hr, q, K),
+                (s, r, q + hq, K), (s, r, max(q - hq, 0.0), K), (s, r, q, K + hk), (s, r, q, K - hk)]
+        for j, (s_, r_, q_, k_) in enumerate(sets):
+            rc, out, _, _ = oracle.price_on_grid(S, k_, T, s_, r_, q_, 1, x, 498)
+            assert rc == 0
+            want = g["prices"][j, i]
+            assert abs(out[0] - want) <= 1e-10 * abs(want) + 1e-12, (i, j, out[0], want)

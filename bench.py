@@ -169,6 +169,15 @@ def load_oracle():
     return ctypes.CDLL(str(b.build_oracle())), "port", "mo_price_batch"
 
 
+def load_port():
+    """The C restatement of the reference's path (oracle/), built in place."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_b", ROOT / "mango-option_gb300" / "build.py")
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    return ctypes.CDLL(str(b.build_oracle()))
+
+
 def cpu_price(lib, fn, cols, nx, nt, threads):
     S, K, T, sig, r, q, put = (np.ascontiguousarray(c) for c in cols)
     n = len(S)
@@ -193,6 +202,110 @@ def cpu_sample(lib, fn, cols, threads, target_s=2.0):
             break
         m = min(len(cols[0]), m * 4)
     return m / t, m, t
+
+
+def _cpu_threads():
+    return os.cpu_count() or 1
+
+
+def _P(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def cpu_uneven(lib, n=None, target_s=2.0):
+    """The uneven-grid workload on the CPU restatement (OpenMP, all host
+    cores): options of the 65,536-option batch's distributions, N_x ~
+    U{51..401}, N_t ~ U{100..1000}, growing samples until ~target_s."""
+    threads = _cpu_threads()
+    m = 64
+    while True:
+        rng = np.random.default_rng(77)
+        S = np.full(m, 100.0)
+        K, T, sig = rng.uniform(80, 120, m), rng.uniform(0.1, 2.0, m), rng.uniform(0.1, 0.5, m)
+        r, q = rng.uniform(0.0, 0.08, m), rng.uniform(0.0, 0.04, m)
+        put = (np.arange(m) % 2 == 0).astype(np.int32)
+        nx = rng.integers(51, 402, m).astype(np.int64)
+        nt = rng.integers(100, 1001, m).astype(np.int64)
+        out = np.zeros(4 * m)
+        st = np.zeros(m, np.int32)
+        t0 = time.perf_counter()
+        lib.mo_price_batch(ctypes.c_int64(m), *(_P(np.ascontiguousarray(a)) for a in (S, K, T, sig, r, q)), _P(put),
+                           _P(nx), _P(nt), ctypes.c_int32(1), ctypes.c_int32(threads), _P(out), None, _P(st))
+        t = time.perf_counter() - t0
+        if t > target_s / 4 or m >= 16384:
+            break
+        m *= 4
+    return {"value": m / t, "unit": "options/s", "cores": threads, "kind": "port",
+            "sample": f"{m} options of the uneven-grid distributions, {t:.2f} s on {threads} threads"}
+
+
+def cpu_iv(lib, pkg, target_s=2.0):
+    """Brent FDM IV (the reference's IVSolver restated) on quotes of the
+    batched-IV distributions, OpenMP over quotes on all host cores."""
+    threads = _cpu_threads()
+    m = 32
+    while True:
+        S, K, T, r, q, vt, put, _ = make_iv_workload(pkg, m, seed=4245)
+        out4 = np.zeros(4 * m)
+        dims = np.zeros(2 * m, np.int64)
+        pst = np.zeros(m, np.int32)
+        nx = np.full(m, NX, np.int64)
+        ntv = np.full(m, NT, np.int64)
+        f = [np.ascontiguousarray(a, np.float64) for a in (S, K, T, vt, r, q)]
+        lib.mo_price_batch(ctypes.c_int64(m), *(_P(a) for a in f), _P(put), _P(nx), _P(ntv), ctypes.c_int32(1),
+                           ctypes.c_int32(threads), _P(out4), _P(dims), _P(pst))
+        px = np.ascontiguousarray(out4.reshape(m, 4)[:, 0])
+        o3 = np.zeros(3 * m)
+        st = np.zeros(m, np.int32)
+        g = [np.ascontiguousarray(a, np.float64) for a in (S, K, T, r, q)]
+        t0 = time.perf_counter()
+        lib.mo_iv_batch(ctypes.c_int64(m), *(_P(a) for a in g), _P(put), _P(px), _P(np.ascontiguousarray(vt)),
+                        _P(nx), _P(ntv), ctypes.c_int32(threads), _P(o3), _P(st))
+        t = time.perf_counter() - t0
+        if t > target_s / 4 or m >= 8192:
+            break
+        m *= 4
+    return {"value": m / t, "unit": "IV/s", "cores": threads, "kind": "port",
+            "sample": f"{m} quotes of the batched-IV distributions, Brent on 101x498, {t:.2f} s on {threads} threads"}
+
+
+def cpu_sweep(lib, slices=16):
+    """The table sweep's PDE solves on the CPU restatement, on one core as the
+    reference routes them (its per-slice fallback solves the (vol, rate) groups
+    one after the other): `slices` of the 200 (vol, rate) solves at
+    S = K = 100, T = 2 on 201 points x 1000 steps (the explicit grid's sizes,
+    an upper bound of the per-slice grids), scaled to solves/s."""
+    sig = np.repeat(TABLE_AXES[2], TABLE_AXES[3].size)[:: 200 // slices][:slices]
+    rr = np.tile(TABLE_AXES[3], TABLE_AXES[2].size)[:: 200 // slices][:slices]
+    m = sig.size
+    out = np.zeros(4 * m)
+    st = np.zeros(m, np.int32)
+    t0 = time.perf_counter()
+    lib.mo_price_batch(ctypes.c_int64(m), _P(np.full(m, 100.0)), _P(np.full(m, 100.0)), _P(np.full(m, 2.0)),
+                       _P(np.ascontiguousarray(sig)), _P(np.ascontiguousarray(rr)), _P(np.zeros(m)),
+                       _P(np.ones(m, np.int32)), _P(np.full(m, 201, np.int64)), _P(np.full(m, 1000, np.int64)),
+                       ctypes.c_int32(1), ctypes.c_int32(1), _P(out), None, _P(st))
+    t = time.perf_counter() - t0
+    return {"value": m / t, "unit": "PDE solves/s", "cores": 1, "kind": "port",
+            "sample": f"{m} of the 200 (vol, rate) solves at 201x1000, {t:.2f} s on 1 thread "
+                      "(the reference solves the slices serially)"}
+
+
+def cpu_query(lib, nq=2_000_000):
+    """BSplineND<double,4>::eval restated, OpenMP over queries on all host
+    cores, on the same table and query distribution."""
+    threads = _cpu_threads()
+    sizes = np.array([a.size for a in TABLE_AXES], np.int64)
+    grids = np.ascontiguousarray(np.concatenate(TABLE_AXES))
+    coeffs = np.random.default_rng(2025).standard_normal(int(np.prod(sizes)))
+    rng = np.random.default_rng(7)
+    q = np.ascontiguousarray(np.stack([rng.uniform(a[0], a[-1], nq) for a in TABLE_AXES], 1))
+    out = np.zeros(nq)
+    t0 = time.perf_counter()
+    lib.mo_bspline4d_eval(_P(sizes), _P(grids), _P(coeffs), _P(q), ctypes.c_int64(nq), _P(out))
+    t = time.perf_counter() - t0
+    return {"value": nq / t, "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": f"{nq} queries, {t:.2f} s on {threads} threads"}
 
 
 def make_iv_workload(pkg, n, seed=4242):
@@ -279,6 +392,8 @@ def bench_iv(pkg, eng, n):
             "eligible": int(eligible.sum()),
             "frac_within_1e-6_vol": float(within.sum() / max(eligible.sum(), 1)),
             "misses": int((miss & ~other_root).sum()), "flat_or_non_monotone": int(other_root.sum()),
+            "misses_settled_by_newton": int((miss & ~other_root & (out["has_vega"] == 1)).sum()),
+            "settled_by_newton": int(((out["has_vega"] == 1) & ok).sum()),
             "frac_within_1e-6_vol_excluding_flat": float(within.sum() / max((eligible & ~other_root).sum(), 1)),
             "max_abs_vol_error_eligible": float(err[eligible & ok].max()) if (eligible & ok).any() else None,
             "quote_evaluations": int(st["options"]),
@@ -733,6 +848,18 @@ def main():
         extra["table_sweep"], extra["bspline_query"] = bench_table(pkg, eng, torch, stream,
                                                                    args.queries, fp64_peak)
 
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        # CPU baselines of the side workloads (the reference's paths restated,
+        # bounded samples, after every GPU measurement)
+        port = load_port()
+        if "uneven_grids" in extra:
+            extra["uneven_grids"]["cpu_baseline"] = cpu_uneven(port)
+        if "iv" in extra:
+            extra["iv"]["cpu_baseline"] = cpu_iv(port, pkg)
+        if "table_sweep" in extra:
+            extra["table_sweep"]["cpu_baseline"] = cpu_sweep(port)
+        if "bspline_query" in extra:
+            extra["bspline_query"]["cpu_baseline"] = cpu_query(port)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         lib, kind, fn = load_oracle()

@@ -289,7 +289,9 @@ enum {
  * scratch by Brent (statuses are Brent's).  Quotes with yield curves or
  * discrete dividends use the secant path.  iterations = coarse plus own-grid
  * evaluations for Newton-settled quotes; final_error = |V - P| at the last
- * evaluated point.  No counterpart in the reference ABI. */
+ * evaluated point; has_vega = 1 and vega = dV/dsigma at the root (the exact
+ * discrete vega of the last tangent evaluation, carried to the root along the
+ * curvature) for Newton-settled quotes.  No counterpart in the reference ABI. */
 MangoStatus mango_gpu_solve_iv_batch_method(MangoGpuContext* ctx, const MangoIvQuery* queries,
                                             uint64_t n, const MangoGpuGrid* grids,
                                             uint64_t grid_stride, const MangoIvConfig* config,

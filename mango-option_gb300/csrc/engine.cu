@@ -290,6 +290,12 @@ void destroy_batch(MangoGpuBatch* b) {
     if (e) cudaEventDestroy(e);
   for (auto& e : b->run_ev)
     if (e) cudaEventDestroy(e);
+  for (auto& e : b->wev)
+    if (e) cudaEventDestroy(e);
+  if (b->wstream) {
+    cudaStreamSynchronize(b->wstream);
+    cudaStreamDestroy(b->wstream);
+  }
   delete b;
 }
 
@@ -629,6 +635,8 @@ void run_batch(MangoGpuBatch* b) {
     const WarpPlan plan = plan_warp_tiles(b->h_tiles.as<TileDev>(), ntiles, tv0, ctx->num_sms);
     b->nwt = static_cast<int32_t>(plan.tiles.size());
     b->wR = plan.R;
+    b->wblocks = plan.blocks;
+    b->wconcurrent = plan.concurrent;
     if (b->nwt > 0) {
       // pageable sources: staged before the calls return
       check(cudaMemcpyAsync(b->d_wt.get(sizeof(int32_t) * b->nwt), plan.tiles.data(),
@@ -652,13 +660,29 @@ void run_batch(MangoGpuBatch* b) {
   }
   const int blocks = std::max(1, std::min<int>(ctx->num_sms * bps,
                                                (ntiles + warps_per_block - 1) / warps_per_block));
+  if (b->wconcurrent) {
+    // the long poles on their own stream, launched first so that their
+    // blocks are resident beside the persistent thread march
+    if (!b->wstream) {
+      check(cudaStreamCreateWithFlags(&b->wstream, cudaStreamNonBlocking), "stream");
+      for (auto& e : b->wev) check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+    }
+    check(cudaEventRecord(b->wev[0], st), "event");
+    check(cudaStreamWaitEvent(b->wstream, b->wev[0], 0), "stream wait");
+    wmarch_launch(b->wstream, ctx->num_sms, d_tiles, b->d_wt.as<int32_t>(), b->nwt, d_opts, d_pool,
+                  d_flags, d_mode, d_status, b->d_queue.as<int>() + 1, mc, b->wR, b->wblocks);
+    check(cudaEventRecord(b->wev[1], b->wstream), "event");
+  }
   if (b->nwt < ntiles)
     march_kernel<<<blocks, 32 * warps_per_block, 0, st>>>(d_tiles, ntiles, d_opts, d_pool,
                                                           d_flags, d_mode, d_status,
                                                           b->d_queue.as<int>(), mc);
   check(cudaGetLastError(), "march_kernel launch");
-  wmarch_launch(st, ctx->num_sms, d_tiles, b->d_wt.as<int32_t>(), b->nwt, d_opts, d_pool, d_flags,
-                d_mode, d_status, b->d_queue.as<int>() + 1, mc, b->wR);
+  if (b->wconcurrent)
+    check(cudaStreamWaitEvent(st, b->wev[1], 0), "stream wait");
+  else
+    wmarch_launch(st, ctx->num_sms, d_tiles, b->d_wt.as<int32_t>(), b->nwt, d_opts, d_pool,
+                  d_flags, d_mode, d_status, b->d_queue.as<int>() + 1, mc, b->wR, b->wblocks);
   if (b->mc.tv_first < m) {
     const int tv_tiles = ntiles - b->tv_tile0;
     const int tv_blocks = std::max(1, std::min<int>(ctx->num_sms * 8, (tv_tiles + 3) / 4));

@@ -182,7 +182,10 @@ struct MangoGpuBatch {
   int32_t tv_tile0 = 0;  // first tile holding a time-varying option
   // Tiles marched one warp per option (wmarch.cu), planned on the first run.
   bool wplan_ready = false;
-  int32_t nwt = 0, wR = 0;
+  int32_t nwt = 0, wR = 0, wblocks = 0;
+  bool wconcurrent = false;             // warp march beside the thread march
+  cudaStream_t wstream = nullptr;       // its stream, created on first use
+  cudaEvent_t wev[2] = {nullptr, nullptr};
   mgpu::DevBuf d_wt, d_tile_warp;
   mgpu::HostBuf h_xs, h_opts, h_tiles, h_out4, h_status;
   cudaEvent_t ev[8] = {};

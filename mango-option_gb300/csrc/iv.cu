@@ -110,7 +110,9 @@ struct NewtonDev {
   double xb, fb;   // own-grid point with the smallest |f|
   double x1, v1;   // last own-grid point with the exact vega, and that vega
   double fp;       // f at xp (own grid)
+  double xpp, fpp; // the own-grid point before xp
   int32_t has_v1;
+  int32_t has_pp;
   int32_t level;   // 0 coarse, 1 own grid
   int32_t it;      // evaluations on this level
   int32_t total;   // evaluations overall
@@ -133,7 +135,7 @@ struct IvDev {
 // (|step| and the size of its second-order correction; the error left after
 // the corrected step is a fraction of that correction).
 constexpr int kCoarseEvals = 2;
-constexpr int kFineEvals = 3;
+constexpr int kFineEvals = 4;
 constexpr double kAcceptStep = 1e-3;
 constexpr double kAcceptCorr = 2e-7;
 // The third-order term of a step d is about |d|^3 / (6 sigma^2) times a
@@ -154,6 +156,7 @@ constexpr double kFlatVega = 1e-7;
 struct IvOut {
   double root, ferr;
   int32_t iter, code;
+  double vega;  // Newton-settled quotes: the exact discrete vega carried to the root; else NaN
 };
 
 namespace {
@@ -418,13 +421,29 @@ __device__ int newton_consume(NewtonDev& s, double f, double v, bool has_v, doub
     s.v1 = v;
     s.has_v1 = 1;
   } else if (s.has_prev && x != s.xp) {
-    slope = (f - s.fp) / (x - s.xp) + 0.5 * s.kc * (x - s.xp);
-    slope_err = s.has_v1 ? fabs(slope - (s.v1 + s.kc * (x - s.x1))) : fabs(slope);
+    // The curvature of the parabola through the own-grid data replaces the
+    // coarse one: through (x1, f1, v1) and (x, f) after the exact-vega
+    // evaluation, through the last three values after that.  The slope is the
+    // secant's, carried to x; its uncertainty is half the change of the
+    // curvature estimate times the secant's span.
+    const double sec = (f - s.fp) / (x - s.xp);
+    const double kc_old = s.kc;
+    if (s.has_v1 && s.xp == s.x1)
+      s.kc = 2.0 * (sec - s.v1) / (x - s.x1);
+    else if (s.has_pp && x != s.xpp)
+      s.kc = 2.0 * (sec - (s.fp - s.fpp) / (s.xp - s.xpp)) / (x - s.xpp);
+    slope = sec + 0.5 * s.kc * (x - s.xp);
+    slope_err = 0.5 * fabs(s.kc - kc_old) * fabs(x - s.xp);
   } else if (s.has_v1) {
     slope = s.v1 + s.kc * (x - s.x1);
     slope_err = fabs(slope);
   } else {
     return 2;
+  }
+  if (s.has_prev) {
+    s.xpp = s.xp;
+    s.fpp = s.fp;
+    s.has_pp = 1;
   }
   s.xp = x;
   s.fp = f;
@@ -498,7 +517,7 @@ __global__ void iv_init_kernel(int m, int32_t method, int k, int tv_first,
                                int32_t* __restrict__ lev) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= m) return;
-  R[q] = IvOut{qnan(), qnan(), 0, kIvNumerical};
+  R[q] = IvOut{qnan(), qnan(), 0, kIvNumerical, qnan()};
   IvDev st{};
   double* pts = next_sig + static_cast<size_t>(q) * kMaxPts;
   lev[q] = kLevelPlain;
@@ -568,10 +587,10 @@ __global__ void iv_step_kernel(int nq, const int32_t* __restrict__ qlist,
     if (r == kFastGo) {
       next_n = fast_propose(st.fs, opts[q], mat[q], upper[q], k, pts);
     } else if (r == kFastSettled) {
-      R[q] = IvOut{st.fs.xa, fabs(st.fs.fa), st.fs.iter, kIvOk};
+      R[q] = IvOut{st.fs.xa, fabs(st.fs.fa), st.fs.iter, kIvOk, qnan()};
       st.mode = 2;
     } else if (r == kFastBracket) {
-      R[q] = IvOut{qnan(), fmin(fabs(st.fs.e0), fabs(st.fs.e1)), 0, kIvBracket};
+      R[q] = IvOut{qnan(), fmin(fabs(st.fs.e0), fabs(st.fs.e1)), 0, kIvBracket, qnan()};
       st.mode = 2;
     } else {
       if (trace)
@@ -596,7 +615,8 @@ __global__ void iv_step_kernel(int nq, const int32_t* __restrict__ qlist,
       next_n = 1;
       lev[q] = level;
     } else if (r == 1) {
-      R[q] = IvOut{root, fabs(f), st.nw.total, kIvOk};
+      R[q] = IvOut{root, fabs(f), st.nw.total, kIvOk,
+                   st.nw.has_v1 ? st.nw.v1 + st.nw.kc * (root - st.nw.x1) : qnan()};
       st.mode = 2;
     } else {
       newton_to_fast(st.nw, st.fs, upper[q]);
@@ -610,7 +630,7 @@ __global__ void iv_step_kernel(int nq, const int32_t* __restrict__ qlist,
       pts[0] = next;
       next_n = 1;
     } else {
-      R[q] = IvOut{st.br.root, st.br.ferr, st.br.iter, st.br.code};
+      R[q] = IvOut{st.br.root, st.br.ferr, st.br.iter, st.br.code, qnan()};
       st.mode = 2;
     }
   }
@@ -1160,8 +1180,8 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
       o.success.implied_vol = r.code == kIvOk ? r.root : NAN;
       o.success.iterations = static_cast<uint64_t>(r.iter);
       o.success.final_error = r.ferr;
-      o.success.vega = 0.0;
-      o.success.has_vega = 0;
+      o.success.has_vega = r.code == kIvOk && std::isfinite(r.vega) ? 1 : 0;
+      o.success.vega = o.success.has_vega ? r.vega : 0.0;
       o.success.used_rate_approximation = 0;
     }
     for (int64_t i = 0; i < nn; ++i) failed += out[i].status != MANGO_OK;

@@ -62,6 +62,9 @@ enum WArray : int {
 // Row modes of a stage, per row (bytes after the double arrays).
 constexpr unsigned char kRowCached = 0, kRowLocked = 1, kRowOff = 2;
 constexpr double kBig = 1e300;  // "no bound" of a clamp map
+// Options of a large uneven batch that may go to the warp march beside the
+// thread march (two warp blocks per SM, a few options each).
+constexpr int64_t kLongWarpOptions = 1216;
 
 struct WView {
   double* s;
@@ -475,14 +478,15 @@ void wmarch_opt_in() {
 
 void wmarch_launch(void* stream, int num_sms, const TileDev* tiles, const int32_t* wt, int nwt,
                    const OptDev* opts, double* pool, const uint8_t* flags, const int32_t* mode,
-                   int32_t* status, int* queue, const MarchConst& mc, int R) {
+                   int32_t* status, int* queue, const MarchConst& mc, int R, int max_blocks) {
   if (nwt <= 0) return;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const size_t smem = wmarch_smem_bytes(R);
   wmarch_opt_in();
   int bps = 0;
   check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, wmarch_kernel, 32, smem), "occupancy");
-  const int blocks = std::max(1, std::min(num_sms * std::max(bps, 1), nwt * kTile));
+  int blocks = std::max(1, std::min(num_sms * std::max(bps, 1), nwt * kTile));
+  if (max_blocks > 0) blocks = std::min(blocks, max_blocks);
   wmarch_kernel<<<blocks, 32, smem, st>>>(tiles, wt, nwt, opts, pool, flags, mode, status, queue,
                                           mc, R);
   check(cudaGetLastError(), "wmarch_kernel launch");
@@ -511,13 +515,43 @@ WarpPlan plan_warp_tiles(const TileDev* tiles, int ntiles, int tv_tile0, int num
                                                       wmarch_smem_bytes(R)),
         "occupancy");
   const int64_t wave = static_cast<int64_t>(num_sms) * std::max(bps, 1);
-  if (force != 1 && options > wave) return plan;
+  if (force == 1 || options <= wave) {
+    for (int t = 0; t < last; ++t)
+      if (wmarch_rows_per_lane(tiles[t].nx) <= rmax) {
+        plan.tiles.push_back(t);
+        plan.flag[t] = 1;
+      }
+    plan.R = R;
+    return plan;
+  }
+  // A large batch: only the long poles, when the tile costs (rows x steps of
+  // the tile's widest and longest lane) are uneven.
+  int64_t cap = kLongWarpOptions;
+  if (const char* e = std::getenv("MANGO_GPU_WARP_LONG")) cap = std::atoll(e);
+  if (cap <= 0) return plan;
+  std::vector<std::pair<double, int>> cost;
+  double sum = 0.0;
+  for (int t = 0; t < last; ++t) {
+    const double c = static_cast<double>(tiles[t].nx) * tiles[t].nt;
+    sum += c;
+    if (wmarch_rows_per_lane(tiles[t].nx) <= rmax) cost.push_back({c, t});
+  }
+  const double mean = sum / std::max(last, 1);
+  std::sort(cost.begin(), cost.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+  int64_t taken = 0;
+  int Rw = 1;
+  for (const auto& [c, t] : cost) {
+    if (c <= 2.0 * mean || taken + tiles[t].count > cap) break;
+    plan.flag[t] = 1;
+    taken += tiles[t].count;
+    Rw = std::max(Rw, wmarch_rows_per_lane(tiles[t].nx));
+  }
+  if (taken == 0) return plan;
   for (int t = 0; t < last; ++t)
-    if (wmarch_rows_per_lane(tiles[t].nx) <= rmax) {
-      plan.tiles.push_back(t);
-      plan.flag[t] = 1;
-    }
-  plan.R = R;
+    if (plan.flag[t]) plan.tiles.push_back(t);
+  plan.R = Rw;
+  plan.concurrent = true;
+  plan.blocks = 2 * num_sms;
   return plan;
 }
 

@@ -20,7 +20,8 @@ int wmarch_max_rows();
 // the widest option of those tiles.
 void wmarch_launch(void* stream, int num_sms, const TileDev* tiles, const int32_t* wt, int nwt,
                    const OptDev* opts, double* pool, const uint8_t* flags, const int32_t* mode,
-                   int32_t* status, int* queue, const MarchConst& mc, int R);
+                   int32_t* status, int* queue, const MarchConst& mc, int R,
+                   int max_blocks = 0);
 
 // Which tiles of a packed set march one warp per option.  The options of the
 // tiles [0, ntiles) except the time-varying ones (from tile tv_tile0) are
@@ -28,12 +29,19 @@ void wmarch_launch(void* stream, int num_sms, const TileDev* tiles, const int32_
 // candidate options fit in one wave of resident warps (the last evaluations
 // of a batched IV, a table sweep, small batches), every candidate tile goes
 // to the warp march; otherwise the thread march keeps them (a full batch
-// keeps every lane busy with its cheaper per-row work).  MANGO_GPU_WARP_MARCH
-// = 0 / 1 forces the thread / warp layout for the candidates.
+// keeps every lane busy with its cheaper per-row work), except the longest
+// tiles of a batch whose tiles differ widely in cost (uneven grids): a
+// thread-march warp needs n x n_time dependent row updates for its tile, so
+// the tiles of more than twice the mean cost, up to kLongWarpOptions options,
+// go to the warp march, which runs beside the thread march on two blocks per
+// SM (concurrent = true).  MANGO_GPU_WARP_MARCH = 0 / 1 forces the thread /
+// warp layout for the candidates.
 struct WarpPlan {
   std::vector<int32_t> tiles;  // warp tiles, ascending
   std::vector<uint8_t> flag;   // per tile: 1 = warp
   int R = 0;                   // rows per lane of the widest warp option
+  bool concurrent = false;     // a subset beside the thread march
+  int blocks = 0;              // warp-march blocks (0: by occupancy)
 };
 WarpPlan plan_warp_tiles(const TileDev* tiles, int ntiles, int tv_tile0, int num_sms);
 

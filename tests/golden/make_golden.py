@@ -782,30 +782,35 @@ def golden_greeks_fd(lib):
     """1,024 American puts of the differentiation workload (config-0
     distributions, 101 x 498 grid rule): the reference's prices at the
     option and at the eight bumped parameter sets of a central difference
-    (h = 1e-5: sigma h, max(|r|, 1e-2) h, max(q, 1e-2) h clipped at q = 0,
-    K h), all on the option's own frozen grid."""
+    for h = 1e-5, 1e-6 and 1e-7 (sigma h, max(|r|, 1e-2) h, max(q, 1e-2) h
+    clipped at q = 0, K h), all on the option's own frozen grid; and the
+    differences themselves, per h."""
     n = 1024
     S, K, T, sig, r, q, put = config0_inputs(n, 3, False)
-    h = 1e-5
-    hs, hr = sig * h, np.maximum(np.abs(r), 1e-2) * h
-    hq, hk = np.maximum(q, 1e-2) * h, K * h
-    qdn = np.maximum(q - hq, 0.0)
-    sets = [(sig, r, q, K), (sig + hs, r, q, K), (sig - hs, r, q, K), (sig, r + hr, q, K), (sig, r - hr, q, K),
-            (sig, r, q + hq, K), (sig, r, qdn, K), (sig, r, q, K + hk), (sig, r, q, K - hk)]
-    vals = np.zeros((9, n))
     nx = np.full(n, 101, np.int64)
     nt = np.full(n, 498, np.int64)
-    for j, (s_, r_, q_, k_) in enumerate(sets):
+
+    def prices(s_, r_, q_, k_):
         out = np.zeros(4 * n)
         st = np.zeros(n, np.int32)
         f = [np.ascontiguousarray(a, dtype=np.float64) for a in (S, k_, T, s_, r_, q_, S, K, T, sig)]
         lib.ref_price_frozen(ctypes.c_int64(n), *(P(a) for a in f[:6]), P(put), *(P(a) for a in f[6:]),
                              P(nx), P(nt), ctypes.c_int32(0), P(out), P(st))
         assert (st == 0).all()
-        vals[j] = out.reshape(n, 4)[:, 0]
-    fd = {"vega": (vals[1] - vals[2]) / (2 * hs), "rho": (vals[3] - vals[4]) / (2 * hr),
-          "dividend_rho": (vals[5] - vals[6]) / (q + hq - qdn), "dstrike": (vals[7] - vals[8]) / (2 * hk)}
-    save("greeks_fd.npz", S=S, K=K, T=T, sigma=sig, r=r, q=q, is_put=put, h=np.array(h), prices=vals, **fd)
+        return out.reshape(n, 4)[:, 0]
+
+    base = prices(sig, r, q, K)
+    hs_all = np.array([1e-5, 1e-6, 1e-7])
+    kw = {k: np.zeros((3, n)) for k in ("vega", "rho", "dividend_rho", "dstrike")}
+    for j, h in enumerate(hs_all):
+        hs, hr = sig * h, np.maximum(np.abs(r), 1e-2) * h
+        hq, hk = np.maximum(q, 1e-2) * h, K * h
+        qdn = np.maximum(q - hq, 0.0)
+        kw["vega"][j] = (prices(sig + hs, r, q, K) - prices(sig - hs, r, q, K)) / (2 * hs)
+        kw["rho"][j] = (prices(sig, r + hr, q, K) - prices(sig, r - hr, q, K)) / (2 * hr)
+        kw["dividend_rho"][j] = (prices(sig, r, q + hq, K) - prices(sig, r, qdn, K)) / (q + hq - qdn)
+        kw["dstrike"][j] = (prices(sig, r, q, K + hk) - prices(sig, r, q, K - hk)) / (2 * hk)
+    save("greeks_fd.npz", S=S, K=K, T=T, sigma=sig, r=r, q=q, is_put=put, h=hs_all, value=base, **kw)
 
 
 if __name__ == "__main__":

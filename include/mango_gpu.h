@@ -399,13 +399,33 @@ MangoStatus mango_gpu_price_table_create(MangoGpuContext* ctx, const double* gri
  * src/option/table/eep/eep_decomposer.hpp:60-80: entry = softplus floor of
  * K_ref V - European), then the fit (tolerance as for
  * mango_gpu_bspline4d_fit).  A build with failed PDE slices is refused
- * (MANGO_ERR_SOLVER; the reference repairs them from neighbours). */
+ * (MANGO_ERR_SOLVER), as the reference's strict default max_failure_rate = 0
+ * refuses it; mango_gpu_price_table_build_ex takes the rate and repairs. */
 MangoStatus mango_gpu_price_table_build(
     MangoGpuContext* ctx, const double* moneyness, uint64_t n_moneyness, const double* maturity,
     uint64_t n_maturity, const double* volatility, uint64_t n_volatility, const double* rate,
     uint64_t n_rate, double K_ref, double dividend_yield, MangoOptionType option_type,
     const MangoGpuGrid* grid, int32_t eep, double tolerance, MangoGpuPriceTable** out,
     MangoGpuFitStats* stats, uint64_t* out_failed_slices, MangoError* err);
+/* mango_gpu_price_table_build with PriceTableBuilderND<4>'s failure handling
+ * (src/option/table/bspline/bspline_builder.cpp:95-101, 773-959):
+ * max_failure_rate in [0, 1] (PriceTableConfig, bspline_builder.hpp:101; 0 =
+ * strict, the reference's default) bounds the fraction of (volatility, rate)
+ * slices whose PDE solve failed; below it the swept tensor is repaired before
+ * the EEP step and the fit -- maturities where a slice's resampling failed
+ * are interpolated along tau, whole failed slices are copied from the
+ * nearest valid slice in (volatility, rate) index distance -- and above it
+ * the build fails (MANGO_ERR_SOLVER).  out_repaired (nullable, 2 entries):
+ * whole slices and single maturity points repaired.
+ * mango_gpu_price_table_build is this call with max_failure_rate = 0.  No
+ * counterpart in the reference ABI. */
+MangoStatus mango_gpu_price_table_build_ex(
+    MangoGpuContext* ctx, const double* moneyness, uint64_t n_moneyness, const double* maturity,
+    uint64_t n_maturity, const double* volatility, uint64_t n_volatility, const double* rate,
+    uint64_t n_rate, double K_ref, double dividend_yield, MangoOptionType option_type,
+    const MangoGpuGrid* grid, int32_t eep, double tolerance, double max_failure_rate,
+    MangoGpuPriceTable** out, MangoGpuFitStats* stats, uint64_t* out_failed_slices,
+    uint64_t* out_repaired, MangoError* err);
 void mango_gpu_price_table_destroy(MangoGpuPriceTable* table);
 /* The EEP step alone (the TensorTransformFn of the standard build,
  * eep_decompose with AnalyticalEEP over BSplineTensorAccessor,

@@ -195,6 +195,11 @@ def library() -> ctypes.CDLL:
             ctypes.POINTER(_P), ctypes.POINTER(MangoGpuFitStats), ctypes.POINTER(ctypes.c_uint64),
             ctypes.POINTER(MangoError)]
         lib.mango_gpu_price_table_build.restype = ctypes.c_int32
+        lib.mango_gpu_price_table_build_ex.argtypes = \
+            lib.mango_gpu_price_table_build.argtypes[:15] + [ctypes.c_double] + \
+            lib.mango_gpu_price_table_build.argtypes[15:18] + [_P] + \
+            lib.mango_gpu_price_table_build.argtypes[18:]
+        lib.mango_gpu_price_table_build_ex.restype = ctypes.c_int32
         lib.mango_gpu_eep_decompose.argtypes = [_P, _P, ctypes.c_uint64, _P, ctypes.c_uint64, _P, ctypes.c_uint64,
                                                 _P, ctypes.c_uint64, ctypes.c_double, ctypes.c_double,
                                                 ctypes.c_int32, _P, ctypes.POINTER(MangoError)]
@@ -618,24 +623,30 @@ class Engine:
 
     def price_table_build(self, moneyness, maturity, volatility, rate, K_ref: float = 100.0,
                           dividend_yield: float = 0.0, option_type: int = 1, grid=None, eep: bool = True,
-                          tolerance: float = 0.0):
-        """PriceTableBuilderND<4>::build on the device (mango_gpu_price_table_build):
-        sweep, EEP decomposition, fit.  moneyness is log-moneyness.  Returns
-        (GpuPriceTable, fit diagnostics)."""
+                          tolerance: float = 0.0, max_failure_rate: float = 0.0):
+        """PriceTableBuilderND<4>::build on the device (mango_gpu_price_table_build_ex):
+        sweep, failure check and repair (max_failure_rate as PriceTableConfig's,
+        0 = strict), EEP decomposition, fit.  moneyness is log-moneyness.
+        Returns (GpuPriceTable, fit diagnostics with the failed and repaired
+        counts)."""
         axes = [np.ascontiguousarray(a, dtype=np.float64) for a in (moneyness, maturity, volatility, rate)]
         g = None if grid is None else _grid_entry(grid)
         h = _P()
         stats = MangoGpuFitStats()
         failed = ctypes.c_uint64()
+        repaired = (ctypes.c_uint64 * 2)()
         err = MangoError()
-        st = library().mango_gpu_price_table_build(
+        st = library().mango_gpu_price_table_build_ex(
             self._ctx, _ptr(axes[0]), axes[0].size, _ptr(axes[1]), axes[1].size, _ptr(axes[2]), axes[2].size,
             _ptr(axes[3]), axes[3].size, K_ref, dividend_yield, int(option_type), _ptr(g), int(bool(eep)),
-            tolerance, ctypes.byref(h), ctypes.byref(stats), ctypes.byref(failed), ctypes.byref(err))
+            tolerance, float(max_failure_rate), ctypes.byref(h), ctypes.byref(stats), ctypes.byref(failed),
+            repaired, ctypes.byref(err))
         if st != MANGO_OK:
             raise EngineError(err.message.decode(errors="replace"))
         info = _fit_stats(stats)
         info["failed_pde_slices"] = int(failed.value)
+        info["repaired_slices"] = int(repaired[0])
+        info["repaired_points"] = int(repaired[1])
         return GpuPriceTable(self, h), info
 
     def greeks_arrays(self, params: np.ndarray, grids: Optional[np.ndarray] = None,

@@ -30,6 +30,8 @@
 // table build (sweep -> EEP -> fit -> surface) never leaves the device.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -607,13 +609,169 @@ MangoStatus mango_gpu_price_table_create(MangoGpuContext* ctx, const double* gri
   return MANGO_OK;
 }
 
+}  // extern "C"
+
+namespace mgpu {
+namespace {
+
+// PriceTableBuilderND<4>'s failure handling on the swept tensor
+// [m][tau][sigma][r] (host copy), as the reference runs it after the sweep
+// (src/option/table/bspline/bspline_builder.cpp:95-101, 773-959).  A slice
+// (sigma, r) whose every entry is NaN failed as a whole (its PDE solve, or
+// the spline resampling at every maturity); a slice with NaN at some
+// maturities failed there only.  Those maturities are interpolated linearly
+// along tau from the nearest valid maturities of the same slice (or copied
+// from the one valid side); whole slices are copied from the nearest valid
+// (sigma, r) slice in Manhattan distance, searched dist = 1, 2, ... with
+// dsigma from -dist to dist and the rate offset's sign -, + (a repaired slice
+// then counts as a donor).  The reference visits whole-slice failures in a
+// hash set's order; here they go in ascending (sigma, r) order.
+// Returns the whole slices and the (slice, maturity) points repaired; throws
+// when a slice has no valid neighbour.
+std::pair<uint64_t, uint64_t> repair_tensor(std::vector<double>& ten, int64_t nm, int64_t nt,
+                                            int64_t ns, int64_t nr) {
+  auto at = [&](int64_t i, int64_t j, int64_t s, int64_t r) -> double& {
+    return ten[((i * nt + j) * ns + s) * nr + r];
+  };
+  const int64_t nslice = ns * nr;
+  std::vector<char> full(static_cast<size_t>(nslice), 0);
+  std::vector<std::vector<int64_t>> partial(static_cast<size_t>(nslice));
+  for (int64_t s = 0; s < ns; ++s)
+    for (int64_t r = 0; r < nr; ++r) {
+      int64_t bad = 0;
+      for (int64_t j = 0; j < nt; ++j) {
+        bool nanj = false;
+        for (int64_t i = 0; i < nm && !nanj; ++i) nanj = std::isnan(at(i, j, s, r));
+        if (nanj) {
+          partial[s * nr + r].push_back(j);
+          ++bad;
+        }
+      }
+      if (bad == nt) full[s * nr + r] = 1;
+    }
+  uint64_t points = 0;
+  for (int64_t k = 0; k < nslice; ++k) {
+    if (full[k] || partial[k].empty()) continue;
+    const int64_t s = k / nr, r = k % nr;
+    for (int64_t j : partial[k]) {
+      int64_t before = -1, after = -1;
+      for (int64_t q = j; q-- > 0;)
+        if (!std::isnan(at(0, q, s, r))) {
+          before = q;
+          break;
+        }
+      for (int64_t q = j + 1; q < nt; ++q)
+        if (!std::isnan(at(0, q, s, r))) {
+          after = q;
+          break;
+        }
+      for (int64_t i = 0; i < nm; ++i) {
+        if (before >= 0 && after >= 0) {
+          const double w = static_cast<double>(j - before) / static_cast<double>(after - before);
+          at(i, j, s, r) = (1.0 - w) * at(i, before, s, r) + w * at(i, after, s, r);
+        } else {
+          at(i, j, s, r) = at(i, before >= 0 ? before : after, s, r);
+        }
+      }
+      ++points;
+    }
+  }
+  std::vector<char> valid(static_cast<size_t>(nslice));
+  for (int64_t k = 0; k < nslice; ++k) valid[k] = !full[k];
+  uint64_t slices = 0;
+  for (int64_t k = 0; k < nslice; ++k) {
+    if (!full[k]) continue;
+    const int64_t s = k / nr, r = k % nr;
+    int64_t ds_found = -1, dr_found = -1;
+    for (int64_t dist = 1; dist <= (ns - 1) + (nr - 1) && ds_found < 0; ++dist)
+      for (int64_t dsg = -dist; dsg <= dist && ds_found < 0; ++dsg) {
+        const int64_t drr = dist - (dsg < 0 ? -dsg : dsg);
+        for (int sign : {-1, 1}) {
+          const int64_t s2 = s + dsg, r2 = r + sign * drr;
+          if (s2 >= 0 && s2 < ns && r2 >= 0 && r2 < nr && valid[s2 * nr + r2]) {
+            ds_found = s2;
+            dr_found = r2;
+            break;
+          }
+        }
+      }
+    if (ds_found < 0)
+      throw std::runtime_error("failed-slice repair: slice " + std::to_string(k) +
+                               " has no valid neighbour");
+    for (int64_t i = 0; i < nm; ++i)
+      for (int64_t j = 0; j < nt; ++j) at(i, j, s, r) = at(i, j, ds_found, dr_found);
+    valid[k] = 1;
+    ++slices;
+  }
+  return {slices, points};
+}
+
+// Test hook, host side: MANGO_GPU_TABLE_FAIL="k,k:j,..." reports slice k
+// (flat sigma * n_rate + r) as failed as a whole, or at maturity j only, as
+// if its solve or its resampling had failed; the repair then runs on it.
+// Nothing on the device is altered.
+uint64_t inject_table_failures(std::vector<double>& ten, int64_t nm, int64_t nt, int64_t ns,
+                               int64_t nr) {
+  const char* e = std::getenv("MANGO_GPU_TABLE_FAIL");
+  if (!e || !*e) return 0;
+  uint64_t whole = 0;
+  std::string spec(e);
+  size_t pos = 0;
+  while (pos < spec.size()) {
+    size_t end = spec.find(',', pos);
+    if (end == std::string::npos) end = spec.size();
+    const std::string item = spec.substr(pos, end - pos);
+    pos = end + 1;
+    if (item.empty()) continue;
+    const size_t colon = item.find(':');
+    const int64_t k = std::stoll(item.substr(0, colon));
+    if (k < 0 || k >= ns * nr) continue;
+    const int64_t s = k / nr, r = k % nr;
+    const double nan = std::nan("");
+    if (colon == std::string::npos) {
+      for (int64_t i = 0; i < nm; ++i)
+        for (int64_t j = 0; j < nt; ++j) ten[((i * nt + j) * ns + s) * nr + r] = nan;
+      ++whole;
+    } else {
+      const int64_t j = std::stoll(item.substr(colon + 1));
+      if (j < 0 || j >= nt) continue;
+      for (int64_t i = 0; i < nm; ++i) ten[((i * nt + j) * ns + s) * nr + r] = nan;
+    }
+  }
+  return whole;
+}
+
+}  // namespace
+}  // namespace mgpu
+
+extern "C" {
+
 MangoStatus mango_gpu_price_table_build(
     MangoGpuContext* ctx, const double* moneyness, uint64_t nm, const double* maturity,
     uint64_t ntau, const double* volatility, uint64_t nsig, const double* rate, uint64_t nr,
     double K_ref, double dividend_yield, MangoOptionType option_type, const MangoGpuGrid* grid,
     int32_t eep, double tolerance, MangoGpuPriceTable** out, MangoGpuFitStats* stats,
     uint64_t* out_failed_slices, MangoError* err) {
+  return mango_gpu_price_table_build_ex(ctx, moneyness, nm, maturity, ntau, volatility, nsig, rate,
+                                        nr, K_ref, dividend_yield, option_type, grid, eep,
+                                        tolerance, 0.0, out, stats, out_failed_slices, nullptr,
+                                        err);
+}
+
+MangoStatus mango_gpu_price_table_build_ex(
+    MangoGpuContext* ctx, const double* moneyness, uint64_t nm, const double* maturity,
+    uint64_t ntau, const double* volatility, uint64_t nsig, const double* rate, uint64_t nr,
+    double K_ref, double dividend_yield, MangoOptionType option_type, const MangoGpuGrid* grid,
+    int32_t eep, double tolerance, double max_failure_rate, MangoGpuPriceTable** out,
+    MangoGpuFitStats* stats, uint64_t* out_failed_slices, uint64_t* out_repaired,
+    MangoError* err) {
   if (out) *out = nullptr;
+  if (out_repaired) out_repaired[0] = out_repaired[1] = 0;
+  if (!(max_failure_rate >= 0.0 && max_failure_rate <= 1.0)) {
+    // PriceTableConfig validation (bspline_builder.hpp:108-111)
+    set_err(err, MANGO_ERR_VALIDATION, "max_failure_rate must be in [0.0, 1.0]");
+    return MANGO_ERR_VALIDATION;
+  }
   std::string bad = check_table_args(moneyness, nm, maturity, ntau, volatility, nsig, rate, nr,
                                      K_ref, dividend_yield, option_type);
   if (bad.empty() && (!ctx || !out)) bad = "null argument";
@@ -654,10 +812,45 @@ MangoStatus mango_gpu_price_table_build(
     const uint64_t failed = table_sweep_device(ctx, moneyness, nm, maturity, ntau, volatility, nsig,
                                                rate, nr, K_ref, dividend_yield, option_type, grid,
                                                a, nullptr);
-    if (out_failed_slices) *out_failed_slices = failed;
-    if (failed > 0)
-      throw std::runtime_error(std::to_string(failed) +
-                               " PDE slices failed (failed-slice repair is not supported)");
+    // Failure rate and repair (bspline_builder.cpp:95-101, 773-959) on a
+    // host copy of the tensor (nm x ntau x nsig x nr doubles, a few MB); it
+    // goes back to the device only when some entry was NaN (a failed solve
+    // or resampling, or the host-side test hook) and has been repaired.
+    {
+      std::vector<double> ten(static_cast<size_t>(total));
+      check(cudaMemcpyAsync(ten.data(), a, sizeof(double) * total, cudaMemcpyDeviceToHost, st),
+            "D2H tensor");
+      check(cudaStreamSynchronize(st), "stream synchronize");
+      const uint64_t injected = inject_table_failures(ten, static_cast<int64_t>(nm),
+                                                      static_cast<int64_t>(ntau),
+                                                      static_cast<int64_t>(nsig),
+                                                      static_cast<int64_t>(nr));
+      const uint64_t pde_failed = failed + injected;
+      if (out_failed_slices) *out_failed_slices = pde_failed;
+      const double rate_failed =
+          static_cast<double>(pde_failed) / static_cast<double>(nsig * nr);
+      if (rate_failed > max_failure_rate)
+        throw std::runtime_error(std::to_string(pde_failed) + " of " +
+                                 std::to_string(nsig * nr) +
+                                 " PDE slices failed, above max_failure_rate");
+      bool any_nan = false;
+      for (double v : ten)
+        if (std::isnan(v)) {
+          any_nan = true;
+          break;
+        }
+      if (any_nan) {
+        const auto rep = repair_tensor(ten, static_cast<int64_t>(nm), static_cast<int64_t>(ntau),
+                                       static_cast<int64_t>(nsig), static_cast<int64_t>(nr));
+        if (out_repaired) {
+          out_repaired[0] = rep.first;
+          out_repaired[1] = rep.second;
+        }
+        check(cudaMemcpyAsync(a, ten.data(), sizeof(double) * total, cudaMemcpyHostToDevice, st),
+              "H2D repaired tensor");
+        check(cudaStreamSynchronize(st), "stream synchronize");
+      }
+    }
     // Step 3: EEP decomposition.
     if (t->eep) {
       double* ax = static_cast<double*>(dax.get(sizeof(double) * grids.size()));

@@ -137,6 +137,49 @@ def test_table_build_vs_restated_pipeline(engine, pkg, oracle):
     table.close()
 
 
+def test_table_build_failure_rate_and_repair(engine, pkg, oracle, monkeypatch):
+    """PriceTableBuilderND<4>'s failure handling (bspline_builder.cpp:95-101,
+    773-959) driven by the host-side hook MANGO_GPU_TABLE_FAIL, which reports
+    slice 5 (sigma 1, r 1) failed as a whole and slice 17 (sigma 4, r 1) at
+    maturity 3 only.  max_failure_rate 0 (strict, the reference's default)
+    and 0.03 refuse the build (1 of 20 slices = 0.05); 0.05 builds it after
+    the repair: the whole slice becomes a copy of its nearest valid neighbour
+    in the search order (dsigma -1 first: sigma 0, r 1), the failed maturity
+    the index-weighted interpolation of maturities 2 and 4.  The repaired
+    table equals the restated pipeline run on the tensor repaired the same
+    way."""
+    grid = pkg.PDEGridConfig(-3.0, 3.0, 101, 200)
+    args = (*TABLE_AXES, 100.0, 0.0, 1, grid)
+    with pytest.raises(pkg.EngineError, match="max_failure_rate"):
+        engine.price_table_build(*args, max_failure_rate=1.5)
+    monkeypatch.setenv("MANGO_GPU_TABLE_FAIL", "5,17:3")
+    for rate in (0.0, 0.03):
+        with pytest.raises(pkg.EngineError, match="above max_failure_rate"):
+            engine.price_table_build(*args, max_failure_rate=rate)
+    table, info = engine.price_table_build(*args, max_failure_rate=0.05)
+    assert info["failed_pde_slices"] == 1
+    assert info["repaired_slices"] == 1 and info["repaired_points"] == 1
+    monkeypatch.delenv("MANGO_GPU_TABLE_FAIL")
+    tensor, _, failed = engine.price_table_sweep(*args)
+    assert failed == 0
+    rep = tensor.copy()
+    rep[:, :, 1, 1] = tensor[:, :, 0, 1]
+    rep[:, 3, 4, 1] = 0.5 * (tensor[:, 2, 4, 1] + tensor[:, 4, 4, 1])
+    coeffs = fit_oracle.fit4d(TABLE_AXES, fit_oracle.eep_decompose(TABLE_AXES, rep, 100.0, 0.0, True))
+    rng = np.random.default_rng(17)
+    n = 512
+    p = np.stack([np.full(n, 100.0), 100.0 / np.exp(rng.uniform(TABLE_AXES[0][0], TABLE_AXES[0][-1], n)),
+                  rng.uniform(0.05, 1.5, n), rng.uniform(0.1, 0.6, n), rng.uniform(0.0, 0.06, n)], 1)
+    got = table.price_arrays(records(pkg, p, 1, 0.0))
+    ref = oracle.surface_price(TABLE_AXES, coeffs, p, 100.0, 0.0, 1)
+    assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max()
+    clean, info = engine.price_table_build(*args)
+    assert info["repaired_slices"] == 0 and info["repaired_points"] == 0
+    assert np.abs(clean.price_arrays(records(pkg, p, 1, 0.0)) - got).max() > 1e-6
+    table.close()
+    clean.close()
+
+
 def test_table_build_interpolates_at_nodes(engine, pkg):
     """At the table's nodes the surface returns the PDE price it was built
     from, through the EEP floor: K/K_ref (eep_floor(K_ref u - E) + E), with

@@ -64,3 +64,4 @@ def test_bspline_linear_reproduction(engine, pkg):
     corners = np.array([[a[0] if (k >> d) & 1 == 0 else a[-1] for d, a in enumerate(axes)] for k in range(16)])
     want = np.array([C[tuple(0 if (k >> d) & 1 == 0 else len(axes[d]) - 1 for d in range(4))] for k in range(16)])
     assert np.allclose(surf.eval(corners), want, rtol=0, atol=1e-10)
+

@@ -499,6 +499,17 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
   // Time-varying options: per-option data, time points, curves, events.
   int64_t nc = 0;
   while (nc < m && !b->res[order[nc]].tv) ++nc;
+  // Test hook MANGO_GPU_SINGULAR_PIVOT=<caller index>: that option (when it
+  // is on the constant-coefficient march) gets a zero first pivot, so its
+  // slot comes back MANGO_ERR_SOLVER as after a singular Thomas solve
+  // (thomas_solver.hpp:386-388).  Nothing else changes.
+  b->mc.singular_pivot = -1;
+  if (const char* e = std::getenv("MANGO_GPU_SINGULAR_PIVOT"))
+    if (*e) {
+      const long long want = std::atoll(e);
+      for (int64_t k = 0; k < nc; ++k)
+        if (b->res[order[k]].orig == want) b->mc.singular_pivot = static_cast<int32_t>(k);
+    }
   std::vector<TvDev> tvh;
   std::vector<double> tph, curveh, evh;
   if (nc < m) {

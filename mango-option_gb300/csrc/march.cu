@@ -139,8 +139,11 @@ __global__ void prep_kernel(const TileDev* __restrict__ tiles, int ntiles,
     const double jl = d2m + d1m;
     const double jd = d2i + d1i + (-rate);
     const double ju = d2p + d1p;
-    const double l1 = -w1 * jl, dg1 = 1.0 - w1 * jd, u1 = -w1 * ju;
-    const double l2 = -w2 * jl, dg2 = 1.0 - w2 * jd, u2 = -w2 * ju;
+    // Row 1 follows the Dirichlet row 0 (c'_0 = 0): a zero diagonal there
+    // is a zero pivot (the singular-pivot test hook).
+    const bool zero_pivot = (k == mc.singular_pivot && i == 1);
+    const double l1 = -w1 * jl, dg1 = zero_pivot ? 0.0 : 1.0 - w1 * jd, u1 = -w1 * ju;
+    const double l2 = -w2 * jl, dg2 = zero_pivot ? 0.0 : 1.0 - w2 * jd, u2 = -w2 * ju;
     r[A_L1 * kTile] = l1;
     r[A_D1 * kTile] = dg1;
     r[A_U1 * kTile] = u1;
@@ -148,7 +151,7 @@ __global__ void prep_kernel(const TileDev* __restrict__ tiles, int ntiles,
     r[A_D2 * kTile] = dg2;
     r[A_U2 * kTile] = u2;
     r[A_LR * kTile] = -wr * jl;
-    r[A_DR * kTile] = 1.0 - wr * jd;
+    r[A_DR * kTile] = zero_pivot ? 0.0 : 1.0 - wr * jd;
     r[A_UR * kTile] = -wr * ju;
 
     // Cached factorisations (the thomas_solver.hpp:382-395 recurrence).

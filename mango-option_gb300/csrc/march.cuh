@@ -86,6 +86,11 @@ struct MarchConst {
   // Per tile, nonzero: the tile's options are marched one warp per option
   // (wmarch.cu) and march_kernel skips it; null: every tile on march_kernel.
   const uint8_t* tile_warp = nullptr;
+  // Test hook (set by the host from MANGO_GPU_SINGULAR_PIVOT): sorted index
+  // of the one option whose row-1 diagonals prep_kernel zeroes, so that its
+  // first pivot is exactly 0 and the solve reports kStatusSolver as a
+  // singular Thomas pivot does; -1 = none.
+  int32_t singular_pivot = -1;
 };
 
 // Per-option data of the time-varying march, indexed by sorted index minus

@@ -158,3 +158,31 @@ def test_value_at_vs_reference(engine, pkg):
     own = b.value_at(np.arange(n), g["S"])  # at the option's own spot: the batch's results
     check(own, greeks(res), rtol=1e-15, atol=0.0)
     b.close()
+
+
+@pytest.mark.parametrize("warp", ["0", "1"])
+def test_singular_pivot_reports_solver_error(engine, pkg, monkeypatch, warp):
+    """A singular Thomas pivot (thomas_solver.hpp:386-388) fails that option
+    alone with MANGO_ERR_SOLVER and NaN results, on the thread march and on
+    the warp march.  The pivot is made singular by the host-side hook
+    MANGO_GPU_SINGULAR_PIVOT (row 1's diagonals zeroed in the coefficients
+    of caller slot 5); the other slots keep their results bit for bit."""
+    g = golden("pricing_mixed.npz")
+    grid = pkg.grid_array(1, pkg.GRID_FIXED_N, 101, 498)
+    monkeypatch.setenv("MANGO_GPU_WARP_MARCH", warp)
+    clean = run(engine, pkg, g, grid)
+    assert (clean["status"] == 0).all()
+    monkeypatch.setenv("MANGO_GPU_SINGULAR_PIVOT", "5")
+    out = run(engine, pkg, g, grid)
+    assert out["status"][5] == pkg.MANGO_ERR_SOLVER
+    assert np.isnan(greeks(out)[5]).all()
+    keep = np.arange(len(out)) != 5
+    assert (out["status"][keep] == 0).all()
+    assert np.array_equal(greeks(out)[keep], greeks(clean)[keep])
+    p = pkg.PricingParams(spot=float(g["S"][5]), strike=float(g["K"][5]), maturity=float(g["T"][5]),
+                          rate=float(g["r"][5]), dividend_yield=float(g["q"][5]),
+                          option_type=pkg.OptionType.PUT if g["is_put"][5] else pkg.OptionType.CALL,
+                          volatility=float(g["sigma"][5]))
+    monkeypatch.setenv("MANGO_GPU_SINGULAR_PIVOT", "0")
+    with pytest.raises(pkg.SolverError):
+        pkg.american_option_price(p)

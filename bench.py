@@ -329,7 +329,8 @@ VEGA_FLOOR = 1e-4  # the reference InterpolatedIVSolver's default vega_threshold
 
 def bench_iv(pkg, eng, n):
     """Batched IV (262,144 quotes): the reference's Brent, the secant and
-    Newton on the exact discrete vega, end to end through
+    Newton (coarse-grid Newton on the exact discrete vega, then the secant on
+    the own grid), end to end through
     mango_gpu_solve_iv_batch_method.  The quotes are priced at their true vol
     with the forward-mode march (which also gives the discrete vega at the true
     vol) on each quote's 101 x 498 grid sized at that vol -- the grid the
@@ -360,8 +361,8 @@ def bench_iv(pkg, eng, n):
            "vega_floor": VEGA_FLOOR}
     arms = (("brent", pkg.IV_BRENT, "Brent, the reference iterate sequence"),
             ("secant", pkg.IV_SECANT, "secant from the Black-Scholes IV, Brent fallback"),
-            ("newton", pkg.IV_NEWTON, "Newton on the exact discrete vega (coarse grid, then own grid), "
-                                      "Brent fallback"))
+            ("newton", pkg.IV_NEWTON, "Newton on the exact discrete vega of a coarse grid, then the secant "
+                                      "on the own grid (3e-6 secant stop), k-section and Brent fallback"))
     for name, method, desc in arms:
         eng.solve_iv_arrays(quotes[:4096], grids[:4096], method=method)  # warm the buffers
         t0 = time.perf_counter()
@@ -397,8 +398,7 @@ def bench_iv(pkg, eng, n):
             "frac_within_1e-6_vol_excluding_flat": float(within.sum() / max((eligible & ~other_root).sum(), 1)),
             "max_abs_vol_error_eligible": float(err[eligible & ok].max()) if (eligible & ok).any() else None,
             "quote_evaluations": int(st["options"]),
-            "evaluations_by_grid": {"coarse_tangent": int(st["iv_evals"][0]),
-                                    "own_tangent": int(st["iv_evals"][1]), "own": int(st["iv_evals"][2])},
+            "evaluations_by_grid": {"coarse_tangent": int(st["iv_evals"][0]), "own": int(st["iv_evals"][1])},
             "rounds": int(st["tiles"]), "kernel_launches": int(st["kernel_launches"]),
             "breakdown_ms": {"host_prep": round(st["host_prep_ms"], 2), "repack": round(st["prep_ms"], 2),
                              "evaluations_device": round(st["march_ms"], 2), "total": round(st["total_ms"], 2)}}
@@ -551,10 +551,14 @@ def bench_table(pkg, eng, torch, stream, nq, fp64_peak):
     t0 = time.perf_counter()
     tensor, dims, failed = eng.price_table_sweep(*TABLE_AXES, 100.0, 0.0, 1, grid)
     t_sweep = time.perf_counter() - t0
+    st = eng.stats()
     sweep = {"workload": "PriceTableBuilderND<4> sweep+extraction, 50x30x20x10 axes, 200 PDE solves, "
                          "explicit 201x1000 grid (per-slice fallback grids)",
              "seconds": t_sweep, "value": 200 / t_sweep, "unit": "PDE solves/s (end to end)",
-             "failed": int(failed), "max_n_time": int(dims[:, 1].max())}
+             "failed": int(failed), "max_n_time": int(dims[:, 1].max()),
+             "breakdown_ms": {k: round(float(st[k]), 3) for k in
+                              ("host_prep_ms", "h2d_ms", "prep_ms", "march_ms", "outputs_ms", "d2h_ms")
+                              if k in st}}
     sizes = [a.size for a in TABLE_AXES]
     coeffs = np.random.default_rng(2025).standard_normal(int(np.prod(sizes)))
     surf = eng.bspline4d(TABLE_AXES, coeffs)

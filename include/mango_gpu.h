@@ -255,7 +255,7 @@ MangoStatus mango_gpu_solve_iv_batch(MangoGpuContext* ctx, const MangoIvQuery* q
 enum {
   MANGO_GPU_IV_BRENT = 0,   /* the reference's Brent, iterate for iterate */
   MANGO_GPU_IV_SECANT = 1,  /* safeguarded secant, Brent fallback (below) */
-  MANGO_GPU_IV_NEWTON = 2   /* Newton on the exact discrete vega (below) */
+  MANGO_GPU_IV_NEWTON = 2   /* coarse-grid Newton, own-grid secant (below) */
 };
 
 /* mango_gpu_solve_iv_batch with a choice of root finder.  MANGO_GPU_IV_BRENT
@@ -273,25 +273,28 @@ enum {
  * 2 brent_tol_abs / vega.  iterations = evaluations for secant-settled
  * quotes, Brent's count otherwise.
  *
- * MANGO_GPU_IV_NEWTON prices each evaluation with the forward-mode march
- * (the exact derivative of the discrete price along the volatility, as
- * mango_gpu_price_american_vega_batch), so every evaluation yields V and
- * dV/dsigma.  Newton runs first on a coarse grid of the quote's grid kind
- * (half the space points, a quarter of the steps) from the Black-Scholes
- * implied volatility, then on the quote's own grid with the coarse curvature
- * d(vega)/d(sigma) as a second-order correction.  A step on the own grid of
- * at most 1e-3 whose second-order correction is at most 5e-8 is taken and the
- * quote settles one step beyond its last evaluation (a volatility-space
- * stop: the error left is a fraction of that correction); where the vega is
- * small the reference's test |V - P| < brent_tol_abs also settles it.  A quote
- * whose vega is not positive, whose step leaves the bracket seen so far, or
- * that has not settled after 6 evaluations on its own grid is solved from
- * scratch by Brent (statuses are Brent's).  Quotes with yield curves or
- * discrete dividends use the secant path.  iterations = coarse plus own-grid
+ * MANGO_GPU_IV_NEWTON starts on a coarse grid of the quote's grid kind (2/5
+ * of the space points, an eighth of the time steps): two Newton steps from
+ * the Black-Scholes implied volatility with the exact discrete vega of that
+ * grid (the forward-mode march of mango_gpu_price_american_vega_batch), whose
+ * two vegas also give the curvature d(vega)/d(sigma).  On the quote's own
+ * grid it then evaluates prices only: one step from the coarse root along the
+ * coarse vega and curvature, then secant steps corrected by the curvature of
+ * the last three values, kept inside the bracket seen so far.  The quote
+ * settles when the secant step through its last two own-grid values is at
+ * most 3e-6 in volatility, at that step's end (a volatility-space stop: the
+ * error left is that step times the relative change of the slope over it),
+ * or, where the objective is flat, on the reference's test |V - P| <
+ * brent_tol_abs.  A quote not settled after 4 own-grid evaluations, or whose
+ * slope is not positive, goes on with the k-section finder of
+ * MANGO_GPU_IV_SECANT inside what Newton has bracketed (settling at |V - P|
+ * below 1e-7 times the slope, or a bracket narrower than 1e-7), then Brent
+ * from scratch as that finder does.  Quotes with yield curves or discrete
+ * dividends use the secant path.  iterations = coarse plus own-grid
  * evaluations for Newton-settled quotes; final_error = |V - P| at the last
- * evaluated point; has_vega = 1 and vega = dV/dsigma at the root (the exact
- * discrete vega of the last tangent evaluation, carried to the root along the
- * curvature) for Newton-settled quotes.  No counterpart in the reference ABI. */
+ * evaluated point; has_vega = 1 and vega = the slope of that last secant
+ * (dV/dsigma of the discrete objective over the last step) for quotes settled
+ * by the secant stop.  No counterpart in the reference ABI. */
 MangoStatus mango_gpu_solve_iv_batch_method(MangoGpuContext* ctx, const MangoIvQuery* queries,
                                             uint64_t n, const MangoGpuGrid* grids,
                                             uint64_t grid_stride, const MangoIvConfig* config,
@@ -647,9 +650,8 @@ typedef struct {
   int64_t tiles;
   int64_t kernel_launches;
   /* FDM IV: quote evaluations on the coarse grids with the volatility
-   * tangent, on the quotes' own grids with it, and on the own grids without
-   * it (MANGO_GPU_IV_NEWTON uses all three; the other methods the last). */
-  int64_t iv_evals[3];
+   * tangent (MANGO_GPU_IV_NEWTON only) and on the quotes' own grids. */
+  int64_t iv_evals[2];
 } MangoGpuStats;
 MangoStatus mango_gpu_last_stats(const MangoGpuContext* ctx, MangoGpuStats* out);
 

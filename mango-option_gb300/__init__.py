@@ -87,7 +87,7 @@ class MangoGpuStats(ctypes.Structure):
         "host_prep_ms", "h2d_ms", "prep_ms", "march_ms", "outputs_ms", "d2h_ms", "total_ms",
         "algo_flops", "h2d_bytes", "d2h_bytes")] + [
         ("options", ctypes.c_int64), ("tiles", ctypes.c_int64), ("kernel_launches", ctypes.c_int64),
-        ("iv_evals", ctypes.c_int64 * 3)]
+        ("iv_evals", ctypes.c_int64 * 2)]
 
 
 class MangoInterpSolverConfig(ctypes.Structure):

@@ -92,26 +92,30 @@ struct FastDev {
   int32_t has_br;
 };
 
-// Safeguarded Newton on the exact discrete vega, started on a coarse grid.
-//   level 0: kCoarseEvals Newton steps on a coarse grid of the same kind
-//            (2/5 of the space points, an eighth of the time steps) from the
-//            Black-Scholes implied volatility; the coarse vegas give the
-//            curvature d(vega)/d(sigma);
-//   level 1: Newton on the quote's own grid with the exact vega and that
-//            curvature as a second-order correction, then value-only steps
-//            along the secant slope, inside the bracket seen so far.
+// Newton on a coarse grid, then the secant on the quote's own grid.
+//   level 0: kCoarseEvals Newton steps with the exact discrete vega (the
+//            volatility tangent of the march) on a coarse grid of the same
+//            kind (2/5 of the space points, an eighth of the time steps)
+//            from the Black-Scholes implied volatility; the two vegas give
+//            the curvature d(vega)/d(sigma);
+//   level 1: value-only evaluations on the quote's own grid: a first step
+//            from the coarse root with the coarse vega (and its curvature),
+//            then secant steps, corrected by the curvature of the parabola
+//            through the last three values.  A quote settles once the
+//            secant step through its last two own-grid values is at most
+//            kSecantAccept, at that step's end point.
 struct NewtonDev {
   double x;        // point evaluated this round
   double lo, hi;   // f(lo) < 0 < f(hi) where seen, else the Brent bracket ends
   double flo, fhi; // f there (seen bits)
-  double kc;       // curvature estimate d(vega)/d(sigma)
-  double xp, vp;   // previous point on this level and its vega
+  double kc;       // coarse curvature estimate d(vega)/d(sigma)
+  double xp, vp;   // previous point on this level; its vega on the coarse level
   double x0;       // starting point (Black-Scholes implied volatility)
   double xb, fb;   // own-grid point with the smallest |f|
-  double x1, v1;   // last own-grid point with the exact vega, and that vega
+  double vs;       // coarse vega carried to the first own-grid point
+  double sec;      // slope of the secant through the last two own-grid values
   double fp;       // f at xp (own grid)
   double xpp, fpp; // the own-grid point before xp
-  int32_t has_v1;
   int32_t has_pp;
   int32_t level;   // 0 coarse, 1 own grid
   int32_t it;      // evaluations on this level
@@ -129,24 +133,17 @@ struct IvDev {
   int32_t pad;
 };
 
-// Newton schedule: coarse evaluations at most, the coarse step at which the
-// coarse level has converged, evaluations on the quote's own grid before a
-// hand-over to Brent, and the acceptance test of a step on the own grid
-// (|step| and the size of its second-order correction; the error left after
-// the corrected step is a fraction of that correction).
+// Newton schedule: evaluations on the coarse grid, evaluations on the
+// quote's own grid before a hand-over to the k-section finder, and the
+// acceptance test on the own grid.  A secant step of at most kSecantAccept
+// through two own-grid values leaves an error of that step times the
+// relative change of the slope over it: below 1e-7 in volatility even where
+// the discrete objective's slope jumps by a few per cent as grid rows enter
+// or leave the exercise region.  Larger unverified steps (a Newton step from
+// a single evaluation) were measured to miss by up to 2e-6 across such jumps.
 constexpr int kCoarseEvals = 2;
-constexpr int kFineEvals = 4;
-constexpr double kAcceptStep = 1e-3;
-constexpr double kAcceptCorr = 2e-7;
-// The third-order term of a step d is about |d|^3 / (6 sigma^2) times a
-// moneyness factor; a step is taken only while that stays below
-// kAcceptCubic (|d| <= (6 kAcceptCubic sigma^2 / 20)^(1/3)).
-constexpr double kAcceptCubic = 1e-7;
-// A step from an estimated slope (evaluations without the tangent) is taken
-// when it is at most kAcceptStepEst and the disagreement of the two slope
-// estimates (secant through the last two values; last exact vega carried
-// along the curvature) moves it by at most kAcceptCorr.
-constexpr double kAcceptStepEst = 1e-4;
+constexpr int kOwnEvals = 4;
+constexpr double kSecantAccept = 3e-6;
 // Below this vega (per unit volatility, relative to max(1, price)) the
 // objective is flat: the volatility is not determined by the price, and the
 // reference's price test |V - P| < tol settles the quote.
@@ -156,7 +153,7 @@ constexpr double kFlatVega = 1e-7;
 struct IvOut {
   double root, ferr;
   int32_t iter, code;
-  double vega;  // Newton-settled quotes: the exact discrete vega carried to the root; else NaN
+  double vega;  // Newton-settled quotes: the slope of the last own-grid secant; else NaN
 };
 
 namespace {
@@ -354,28 +351,25 @@ __device__ __forceinline__ double objective(const double* out4, const int32_t* m
   return mstatus[k] == kStatusOk ? out4[4 * static_cast<size_t>(k)] - price : qnan();
 }
 
-// Working sets of an evaluation round: the coarse grids and the quotes' own
-// grids with the volatility tangent (Newton), and the quotes' own grids
-// without it (Brent, the secant, time-varying quotes).
-constexpr int32_t kLevelCoarse = 0, kLevelFine = 1, kLevelPlain = 2;
+// Working sets of an evaluation round: the coarse grids with the volatility
+// tangent (Newton's first evaluations) and the quotes' own grids without it
+// (Newton's later evaluations, Brent, the secant, time-varying quotes).
+constexpr int32_t kLevelCoarse = 0, kLevelPlain = 1, kLevels = 2;
 
-// Newton on f = V - P at s.x, with v = dV/dsigma when the evaluation carried
-// the tangent (has_v).  Coarse level: exactly kCoarseEvals evaluations (all
-// quotes reach their own grid in the same round), the curvature from the
-// last two.  Own grid: the first evaluation carries the exact vega; later
-// ones are value-only and use the slope of the secant through the last two
-// values, corrected to the new point with the curvature.  Returns 0 to go on
-// (s.x is the next point, *level its working set), 1 when settled at *root,
+// Newton on f = V - P at s.x; v = dV/dsigma on the coarse level (the
+// evaluation carried the tangent).  Coarse level: exactly kCoarseEvals
+// evaluations (all quotes reach their own grid in the same round), the
+// curvature from the last two.  Own grid: value-only steps as described at
+// NewtonDev.  Returns 0 to go on (s.x is the next point, *level its working
+// set), 1 when settled at *root (*vega: the last secant's slope, or NaN),
 // 2 to hand the quote over.
-__device__ int newton_consume(NewtonDev& s, double f, double v, bool has_v, double upper,
-                              double tol, double* root, int32_t* level) {
+__device__ int newton_consume(NewtonDev& s, double f, double v, double upper, double tol,
+                              double* root, double* vega, int32_t* level) {
   s.total += 1;
   s.it += 1;
   const double x = s.x;
+  *vega = qnan();
   if (s.level == 0) {
-    // Every quote spends exactly kCoarseEvals evaluations here, so that all
-    // reach their own grid in the same round; a failed or flat coarse
-    // evaluation restarts from the initial guess.
     const bool good = isfinite(f) && isfinite(v) && v > 0.0;
     if (good) {
       if (s.has_prev && x != s.xp) s.kc = (v - s.vp) / (x - s.xp);
@@ -387,16 +381,16 @@ __device__ int newton_consume(NewtonDev& s, double f, double v, bool has_v, doub
       s.x = s.x0;
     }
     if (s.it >= kCoarseEvals) {
-      s.level = 1;  // the curvature estimate carries over
+      s.vs = s.has_prev ? s.vp + s.kc * (s.x - s.xp) : qnan();
+      s.level = 1;
       s.it = 0;
       s.has_prev = 0;
-      *level = kLevelFine;
-    } else {
-      *level = kLevelCoarse;
     }
+    *level = s.level == 0 ? kLevelCoarse : kLevelPlain;
     return 0;
   }
-  if (!isfinite(f) || (has_v && !isfinite(v))) return 2;
+  *level = kLevelPlain;
+  if (!isfinite(f)) return 2;
   if (f < 0.0 && (!(s.seen & 1) || x > s.lo)) {
     s.lo = x;
     s.flo = f;
@@ -412,34 +406,39 @@ __device__ int newton_consume(NewtonDev& s, double f, double v, bool has_v, doub
   }
   if (f == 0.0) {
     *root = x;
+    *vega = s.sec;
     return 1;
   }
-  double slope, slope_err = 0.0;
-  if (has_v) {
-    slope = v;
-    s.x1 = x;
-    s.v1 = v;
-    s.has_v1 = 1;
-  } else if (s.has_prev && x != s.xp) {
-    // The curvature of the parabola through the own-grid data replaces the
-    // coarse one: through (x1, f1, v1) and (x, f) after the exact-vega
-    // evaluation, through the last three values after that.  The slope is the
-    // secant's, carried to x; its uncertainty is half the change of the
-    // curvature estimate times the secant's span.
-    const double sec = (f - s.fp) / (x - s.xp);
-    const double kc_old = s.kc;
-    if (s.has_v1 && s.xp == s.x1)
-      s.kc = 2.0 * (sec - s.v1) / (x - s.x1);
-    else if (s.has_pp && x != s.xpp)
-      s.kc = 2.0 * (sec - (s.fp - s.fpp) / (s.xp - s.xpp)) / (x - s.xpp);
-    slope = sec + 0.5 * s.kc * (x - s.xp);
-    slope_err = 0.5 * fabs(s.kc - kc_old) * fabs(x - s.xp);
-  } else if (s.has_v1) {
-    slope = s.v1 + s.kc * (x - s.x1);
-    slope_err = fabs(slope);
+  double slope, kk = s.kc;
+  if (!s.has_prev) {
+    slope = s.vs;  // first own-grid point: the coarse vega carried there
+    if (!(slope > 0.0)) return 2;
   } else {
-    return 2;
+    if (x == s.xp) return 2;
+    const double sec = (f - s.fp) / (x - s.xp);
+    s.sec = sec;
+    const double flat = kFlatVega * fmax(1.0, fabs(f) + fabs(s.fb));
+    if (!(sec > flat)) {
+      if (fabs(f) < tol) {  // flat objective: the reference's stopping test
+        *root = x;
+        return 1;
+      }
+      return 2;
+    }
+    const double d = -f / sec;
+    const double xs = x + d;
+    if (fabs(d) <= kSecantAccept && xs >= kVolLower && xs <= upper) {
+      *root = xs;
+      *vega = sec;
+      return 1;
+    }
+    // the parabola through the last three values; with two, the coarse
+    // curvature
+    if (s.has_pp && x != s.xpp) kk = 2.0 * (sec - (s.fp - s.fpp) / (s.xp - s.xpp)) / (x - s.xpp);
+    slope = sec + 0.5 * kk * (x - s.xp);
+    if (!(slope > 0.0)) return 2;
   }
+  if (s.it >= kOwnEvals || (s.seen == 3 && !(s.lo < s.hi))) return 2;
   if (s.has_prev) {
     s.xpp = s.xp;
     s.fpp = s.fp;
@@ -448,32 +447,15 @@ __device__ int newton_consume(NewtonDev& s, double f, double v, bool has_v, doub
   s.xp = x;
   s.fp = f;
   s.has_prev = 1;
-  const double flat = kFlatVega * fmax(1.0, fabs(f) + fabs(s.fb));
-  if (!(slope > flat)) {
-    if (fabs(f) < tol) {  // flat objective: the reference's stopping test
-      *root = x;
-      return 1;
-    }
-    return 2;
-  }
-  const double d = -f / slope;
-  // second-order step on f + slope d + kc d^2 / 2 = 0 (fixed point, where
+  // second-order step on f + slope d + kk d^2 / 2 = 0 (fixed point, where
   // the correction is small against the step)
+  const double d = -f / slope;
   double dh = d;
-  if (fabs(s.kc * d / slope) < 0.5)
-    for (int k = 0; k < 3; ++k) dh = -(f + 0.5 * s.kc * dh * dh) / slope;
-  const double xn = x + dh;
-  const double cubic_max = cbrt(0.3 * kAcceptCubic * x * x);
-  const bool ok = has_v ? fabs(d) <= fmin(kAcceptStep, cubic_max)
-                        : fabs(d) <= fmin(kAcceptStepEst, cubic_max) &&
-                              fabs(d) * slope_err <= kAcceptCorr * slope;
-  if (ok && fabs(dh - d) <= kAcceptCorr && xn >= kVolLower && xn <= upper) {
-    *root = xn;
-    return 1;
-  }
-  if (s.it >= kFineEvals || (s.seen == 3 && !(s.lo < s.hi))) return 2;
-  s.x = (xn > s.lo && xn < s.hi) ? xn : 0.5 * (s.lo + s.hi);
-  *level = kLevelPlain;  // value-only from here on
+  if (fabs(kk * d / slope) < 0.5)
+    for (int k = 0; k < 3; ++k) dh = -(f + 0.5 * kk * dh * dh) / slope;
+  double xn = fmin(fmax(x + dh, kVolLower), upper);
+  if (s.seen == 3 && !(xn > s.lo && xn < s.hi)) xn = 0.5 * (s.lo + s.hi);
+  s.x = xn;
   return 0;
 }
 
@@ -494,7 +476,9 @@ __device__ void newton_to_fast(const NewtonDev& n, FastDev& s, double upper) {
   s.e0 = s.e1 = qnan();
   s.guess = isfinite(n.xb) ? n.xb : n.x0;
   s.iter = 1;  // the first proposal uses the best point, not the guess
-  s.ftol = n.has_v1 && n.v1 > 0.0 ? kVolTol * n.v1 : kVolTol;
+  // settle at |f| < 1e-7 vol times the best slope known
+  const double slope = n.sec > 0.0 ? n.sec : (n.vs > 0.0 ? n.vs : 1.0);
+  s.ftol = kVolTol * slope;
   if (s.seen == 3) {
     s.has_br = 1;
     if (s.lo < s.hi) {
@@ -531,7 +515,7 @@ __global__ void iv_init_kernel(int m, int32_t method, int k, int tv_first,
     s.x = s.x0;
     s.xb = qnan();
     s.fb = pinf();
-    s.x1 = s.v1 = s.fp = qnan();
+    s.vs = s.sec = s.fp = qnan();
     st.mode = 3;
     pts[0] = s.x;
     npts[q] = 1;
@@ -607,16 +591,15 @@ __global__ void iv_step_kernel(int nq, const int32_t* __restrict__ qlist,
     const double f = objective(out4, mstatus, base, P);
     const double v = (has_vega && mstatus[base] == kStatusOk)
                          ? out4[4 * static_cast<size_t>(base) + 3] : qnan();
-    double root = qnan();
-    int32_t level = kLevelFine;
-    const int r = newton_consume(st.nw, f, v, has_vega != 0, upper[q], tol, &root, &level);
+    double root = qnan(), vega = qnan();
+    int32_t level = kLevelPlain;
+    const int r = newton_consume(st.nw, f, v, upper[q], tol, &root, &vega, &level);
     if (r == 0) {
       pts[0] = st.nw.x;
       next_n = 1;
       lev[q] = level;
     } else if (r == 1) {
-      R[q] = IvOut{root, fabs(f), st.nw.total, kIvOk,
-                   st.nw.has_v1 ? st.nw.v1 + st.nw.kc * (root - st.nw.x1) : qnan()};
+      R[q] = IvOut{root, fabs(f), st.nw.total, kIvOk, vega};
       st.mode = 2;
     } else {
       newton_to_fast(st.nw, st.fs, upper[q]);
@@ -958,7 +941,7 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
     }
     std::vector<IvOut> hr(static_cast<size_t>(m));
     int64_t launches = 0, evaluations = 0;
-    int64_t level_evals[3] = {0, 0, 0};
+    int64_t level_evals[kLevels] = {0, 0};
     double slot_evals = 0, eval_ms = 0, pack_ms = 0;
     if (m > 0) {
       cudaStream_t st = ctx->stream;
@@ -1026,20 +1009,19 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
       } events{ev};
       for (cudaEvent_t& e : ev) check(cudaEventCreate(&e), "cudaEventCreate");
       // Working sets by level: coarse grids with the volatility tangent
-      // (Newton), the own grids with it (Newton, and Brent after a Newton
-      // hand-over), the own grids without it (Brent, the secant).
-      WorkSet ws[3];
-      for (int L = 0; L < 3; ++L) {
+      // (Newton's first evaluations), the own grids without it.
+      WorkSet ws[kLevels];
+      for (int L = 0; L < kLevels; ++L) {
         ws[L].b = b;
         ws[L].src = (L == kLevelCoarse) ? bc : b;
         ws[L].smap = (L == kLevelCoarse) ? &cmap : nullptr;
-        ws[L].tangent = L != kLevelPlain;
+        ws[L].tangent = L == kLevelCoarse;
         ws[L].st = st;
       }
       std::vector<int32_t> active(static_cast<size_t>(m));
       std::iota(active.begin(), active.end(), 0);
-      std::vector<int32_t> lists[3];
-      double level_slot_evals[3] = {0.0, 0.0, 0.0};
+      std::vector<int32_t> lists[kLevels];
+      double level_slot_evals[kLevels] = {0.0, 0.0};
       // Fast or Newton evaluations, then Brent's two bracket ends and max_iter steps.
       const int max_evals =
           (method == MANGO_GPU_IV_BRENT ? 0 : kFastMaxBracketEvals + kCoarseEvals) + max_iter + 3;
@@ -1056,11 +1038,11 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
         for (int32_t q : active)
           if (hnpts[q] > 0) {
             still.push_back(q);
-            lists[std::min(std::max(hlev[q], 0), 2)].push_back(q);
+            lists[std::min(std::max(hlev[q], 0), kLevels - 1)].push_back(q);
           }
         active.swap(still);
         int64_t nq_all = 0;
-        for (int L = 0; L < 3; ++L) {
+        for (int L = 0; L < kLevels; ++L) {
           ws[L].pack(lists[L], hnpts, next_sig);
           nq_all += ws[L].nq;
         }
@@ -1069,7 +1051,7 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
         const int k_next = points_for(nq_all);
         check(cudaMemsetAsync(b->d_queue.p, 0, sizeof(int) * 4, st), "memset queue");
         check(cudaEventRecord(ev[0], st), "event");
-        for (int L = 0; L < 3; ++L) {
+        for (int L = 0; L < kLevels; ++L) {
           WorkSet& w = ws[L];
           if (w.mw == 0) continue;
           MarchConst mc = w.src->mc;
@@ -1156,7 +1138,7 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
                        static_cast<long long>(ws[1].mw), static_cast<long long>(ws[2].mw), k_next,
                        ms);
       }
-      for (int L = 0; L < 3; ++L) level_evals[L] = static_cast<int64_t>(level_slot_evals[L]);
+      for (int L = 0; L < kLevels; ++L) level_evals[L] = static_cast<int64_t>(level_slot_evals[L]);
       check(cudaMemcpyAsync(hr.data(), R, sizeof(IvOut) * m, cudaMemcpyDeviceToHost, st), "D2H results");
       check(cudaStreamSynchronize(st), "stream synchronize");
     }
@@ -1192,7 +1174,7 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
     ctx->stats.total_ms = ms_since(t_start);
     ctx->stats.kernel_launches = launches;
     ctx->stats.options = static_cast<int64_t>(slot_evals);
-    for (int L = 0; L < 3; ++L) ctx->stats.iv_evals[L] = level_evals[L];
+    for (int L = 0; L < kLevels; ++L) ctx->stats.iv_evals[L] = level_evals[L];
     ctx->stats.tiles = evaluations;
     ctx->stats.algo_flops = m > 0 ? b->algo_flops * slot_evals / static_cast<double>(m) : 0.0;
     if (out_failed) *out_failed = failed;

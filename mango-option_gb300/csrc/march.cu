@@ -195,12 +195,36 @@ enum StageKind { kRannacher = 0, kStage1 = 1, kStage2 = 2 };
 // it was read.
 constexpr int kRing = 4;                        // rows in flight
 constexpr int kRingSlots = kRing + 1;           // the slot refilled was read one row earlier
-constexpr int kRingArrays = 5;
+constexpr int kRingArrays = 4;
 constexpr int kRingSlot = kRingArrays * kTile;  // doubles per slot
+
+// L2 eviction priorities.  The time-invariant row arrays are re-read once
+// per step, after every resident tile has streamed its own (far more than
+// L2), so they are marked evict-first; d' is read back by the same sweep's
+// back substitution, with every resident tile's d' together about 63 MB at
+// 101 rows, so it is marked evict-last and is meant to stay in L2.
+struct L2Pol {
+  uint64_t first, last;
+};
+__device__ __forceinline__ L2Pol l2_policies() {
+  L2Pol p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p.first));
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p.last));
+  return p;
+}
 
 __device__ __forceinline__ void cp_async8(double* sdst, const double* gsrc) {
   const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(sdst));
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async8(double* sdst, const double* gsrc, uint64_t pol) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(sdst));
+  asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gsrc),
+               "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ void st_hint(double* g, double v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;\n" ::"l"(g), "d"(v), "l"(pol) : "memory");
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 // Wait until the oldest of the kRing groups in flight has landed.
@@ -208,36 +232,42 @@ __device__ __forceinline__ void cp_wait_oldest() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(kRing - 1) : "memory");
 }
 
-// Forward-sweep inputs of row i into ring slot i % kRingSlots.
+// Forward-sweep inputs of row i into ring slot i % kRingSlots.  The cached
+// stage-1 row uses -l/pivot for both u_{i-1} and d'_{i-1} (the explicit
+// operator's lower weight equals the Jacobian's), and the stage-2 row takes
+// beta/alpha times the alpha weight for u^n, so neither E1L nor B2H streams.
+//   stage 1: E1D, E1U, N1H, u_{i+1};  stage 2: A2H, N2H, g_i, u_i;
+//   Rannacher: slot 2 = u_prev.
 template <int K>
-__device__ __forceinline__ void issue_fwd(const TileView& V, double* R, int a_in, int i) {
+__device__ __forceinline__ void issue_fwd(const TileView& V, double* R, int a_in, int i,
+                                          const L2Pol& pol) {
   double* s = R + (i % kRingSlots) * kRingSlot;
   const double* p = V.rp(i);
   if (K == kStage1) {
-    cp_async8(s, p + A_E1L * kTile);
-    cp_async8(s + kTile, p + A_E1D * kTile);
-    cp_async8(s + 2 * kTile, p + A_E1U * kTile);
-    cp_async8(s + 3 * kTile, p + A_N1H * kTile);
-    cp_async8(s + 4 * kTile, V.rp(i + 1) + A_U * kTile);
+    cp_async8(s, p + A_E1D * kTile, pol.first);
+    cp_async8(s + kTile, p + A_E1U * kTile, pol.first);
+    cp_async8(s + 2 * kTile, p + A_N1H * kTile, pol.first);
+    cp_async8(s + 3 * kTile, V.rp(i + 1) + A_U * kTile);
   } else if (K == kStage2) {
-    cp_async8(s, p + A_A2H * kTile);
-    cp_async8(s + kTile, p + A_B2H * kTile);
-    cp_async8(s + 2 * kTile, p + A_N2H * kTile);
-    cp_async8(s + 3 * kTile, p + A_G * kTile);  // guess u^{n+gamma}
-    cp_async8(s + 4 * kTile, p + A_U * kTile);  // u^n
+    cp_async8(s, p + A_A2H * kTile, pol.first);
+    cp_async8(s + kTile, p + A_N2H * kTile, pol.first);
+    cp_async8(s + 2 * kTile, p + A_G * kTile);  // guess u^{n+gamma}
+    cp_async8(s + 3 * kTile, p + A_U * kTile);  // u^n
   } else {
-    cp_async8(s + 3 * kTile, p + a_in * kTile);  // rhs = guess = u_prev
+    cp_async8(s + 2 * kTile, p + a_in * kTile);  // rhs = guess = u_prev
   }
 }
 
-// Back-substitution inputs of row i into ring slot i % kRingSlots.
+// Back-substitution inputs of row i into ring slot i % kRingSlots: -c', the
+// obstacle where it is positive (rows [plo, phi]; 0 elsewhere), d'.
 template <int K>
-__device__ __forceinline__ void issue_bwd(const TileView& V, double* R, int i) {
+__device__ __forceinline__ void issue_bwd(const TileView& V, double* R, int i, int plo, int phi,
+                                          const L2Pol& pol) {
   double* s = R + (i % kRingSlots) * kRingSlot;
   const double* p = V.rp(i);
-  cp_async8(s, p + (K == kStage2 ? A_NC2 : A_NC1) * kTile);
-  cp_async8(s + kTile, p + A_PSI * kTile);
-  cp_async8(s + 2 * kTile, p + A_D * kTile);
+  cp_async8(s, p + (K == kStage2 ? A_NC2 : A_NC1) * kTile, pol.first);
+  if (i >= plo && i <= phi) cp_async8(s + kTile, p + A_PSI * kTile, pol.first);
+  cp_async8(s + 2 * kTile, p + A_D * kTile, pol.last);
 }
 
 // Result of a forward-sweep row solved off the cached factorisation.
@@ -305,9 +335,11 @@ template <int K>
 __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
                                       const uint8_t* __restrict__ F, bool nocache, double bcl,
                                       double bcr, double alpha, double beta, int a_in, int a_out,
-                                      int32_t st, int flo, int fhi, double* R) {
+                                      int32_t st, int flo, int fhi, int plo, int phi, double* R) {
   const int last = V.NX - 2;  // last interior row of the tile
   const bool always_fresh = (K == kRannacher) || nocache;
+  const L2Pol pol = l2_policies();
+  const double beta_alpha = beta / alpha;
   R += threadIdx.x & (kTile - 1);  // this lane's column of the ring
   // The previous sweeps' global writes of this lane come before the async
   // copies that read them.
@@ -325,7 +357,7 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
   }
   const int stop = live ? min(last, n - 2) : 0;
   for (int j = 1; j <= kRing; ++j) {
-    if (j <= stop) issue_fwd<K>(V, R, a_in, j);
+    if (j <= stop) issue_fwd<K>(V, R, a_in, j, pol);
     cp_commit();
   }
   // The lock test (pde_solver.hpp:635-680) only runs on the tile's
@@ -335,15 +367,14 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
   auto row = [&](int i, auto may_lock) {
     cp_wait_oldest();
     const double* s = R + (i % kRingSlots) * kRingSlot;
-    double ra = 0.0, rb = 0.0, rc, rnl = 0.0, rv = 0.0;
+    double ra = 0.0, rnl = 0.0, rv = 0.0;
     if (K != kRannacher) {
-      ra = s[0];
-      rb = s[kTile];
-      rnl = s[(K == kStage1 ? 3 : 2) * kTile];
-      rv = s[4 * kTile];
+      ra = s[0];  // stage 1: E1D; stage 2: A2H
+      rnl = s[(K == kStage1 ? 2 : 1) * kTile];
+      rv = s[3 * kTile];
     }
-    rc = s[(K == kStage1 ? 2 : 3) * kTile];
-    if (i + kRing <= stop) issue_fwd<K>(V, R, a_in, i + kRing);
+    const double rc = s[(K == kStage1 ? 1 : 2) * kTile];  // stage 1: E1U; else the guess
+    if (i + kRing <= stop) issue_fwd<K>(V, R, a_in, i + kRing, pol);
     cp_commit();
     const double g = (K == kStage1) ? u0 : rc;
     bool lock = false;
@@ -355,9 +386,9 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
     double dcur;
     if (!lock && !fresh) {
       if (K == kStage1)
-        dcur = fma(rnl, dprev, fma(ra, um, fma(rb, u0, rc * rv)));
+        dcur = fma(rnl, dprev + um, fma(ra, u0, rc * rv));
       else
-        dcur = fma(rnl, dprev, fma(ra, g, rb * rv));
+        dcur = fma(rnl, dprev, ra * fma(beta_alpha, rv, g));
     } else {
       const SlowOut so = slow_row<K>(V, i, lock, psi_i, um, u0, rv, g, alpha, beta, dprev, cprev,
                                      always_fresh, lo, hi);
@@ -368,7 +399,7 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
       hi = so.hi;
       if (so.singular) st = kStatusSolver;
     }
-    V.at(A_D, i) = dcur;
+    st_hint(&V.at(A_D, i), dcur, pol.last);
     dprev = dcur;
     if (K == kStage1) {
       um = u0;
@@ -386,14 +417,15 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
   double xnext = dmax_ref(bcr, V.at(A_PSI, n - 1));
   const int top = n - 2;  // this lane's first row going down
   for (int j = 0; j < kRing; ++j) {
-    if (top - j >= 1) issue_bwd<K>(V, R, top - j);
+    if (top - j >= 1) issue_bwd<K>(V, R, top - j, plo, phi, pol);
     cp_commit();
   }
   for (int i = top; i >= 1; --i) {
     cp_wait_oldest();
     const double* s = R + (i % kRingSlots) * kRingSlot;
-    const double rnc = s[0], rpsi = s[kTile], rd = s[2 * kTile];
-    if (i - kRing >= 1) issue_bwd<K>(V, R, i - kRing);
+    const double rnc = s[0], rd = s[2 * kTile];
+    const double rpsi = (i >= plo && i <= phi) ? s[kTile] : 0.0;
+    if (i - kRing >= 1) issue_bwd<K>(V, R, i - kRing, plo, phi, pol);
     cp_commit();
     const double nc = (i >= lo && i <= hi) ? V.at(A_CP, i) : rnc;
     const double xv = proj_max(fma(nc, xnext, rd), rpsi);
@@ -412,7 +444,32 @@ __device__ __forceinline__ double right_bc(const OptDev& o, double t) {
 
 }  // namespace
 
-// Persistent march: each warp pulls tiles (largest first) from the queue.
+// Next tile for the calling lane's warp from the per-sub-partition lists
+// (MarchConst::nbins > 0): its own list first, then the others in turn;
+// -1 once every list is exhausted.  At most nbins list probes.
+__device__ int take_binned(const MarchConst& mc) {
+  unsigned smid, wslot;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+  asm volatile("mov.u32 %0, %%warpid;" : "=r"(wslot));
+  const int nsm = mc.nbins / 4;
+  const int home = static_cast<int>(smid % static_cast<unsigned>(nsm)) * 4 + static_cast<int>(wslot & 3u);
+  volatile const int* cnt = mc.bin_cnt;
+  for (int j = 0; j < mc.nbins; ++j) {
+    if (cnt[mc.nbins] >= mc.nbin_tiles) return -1;
+    const int b = home + j < mc.nbins ? home + j : home + j - mc.nbins;
+    const int size = mc.bin_off[b + 1] - mc.bin_off[b];
+    if (cnt[b] >= size) continue;
+    const int k = atomicAdd(&mc.bin_cnt[b], 1);
+    if (k < size) {
+      atomicAdd(&mc.bin_cnt[mc.nbins], 1);
+      return mc.bin_tiles[mc.bin_off[b] + k];
+    }
+  }
+  return -1;
+}
+
+// Persistent march: each warp pulls tiles (largest first) from the queue,
+// or from its sub-partition's list (take_binned).
 __global__ void __launch_bounds__(128, 4) march_kernel(
     const TileDev* __restrict__ tiles, int ntiles, const OptDev* __restrict__ opts,
     double* __restrict__ pool, const uint8_t* __restrict__ flags,
@@ -422,9 +479,9 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
   __shared__ double ring[4][kRingSlots * kRingSlot];  // one ring per warp (128 threads)
   for (;;) {
     int t = 0;
-    if (lane == 0) t = atomicAdd(queue, 1);
+    if (lane == 0) t = mc.nbins > 0 ? take_binned(mc) : atomicAdd(queue, 1);
     t = __shfl_sync(0xffffffffu, t, 0);
-    if (t >= ntiles) break;
+    if (t < 0 || t >= ntiles) break;
     if (mc.tile_warp && mc.tile_warp[t]) continue;  // marched one warp per option
     const TileDev td = tiles[t];
     const int k = td.first + lane;
@@ -451,6 +508,14 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
       }
     flo = __reduce_min_sync(0xffffffffu, flo);
     fhi = __reduce_max_sync(0xffffffffu, fhi);
+    // Interior rows where this lane's obstacle is positive (one contiguous
+    // block: the payoff is monotone in x); elsewhere it is exactly 0.
+    int plo = INT_MAX, phi = -1;
+    for (int i = 1; i < n - 1; ++i)
+      if (V.at(A_PSI, i) > 0.0) {
+        plo = min(plo, i);
+        phi = i;
+      }
     int32_t st = kStatusOk;
     const double dt = o.dt;
     // Snapshot taps: copy the state after the listed steps.
@@ -476,9 +541,9 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
       const double t_mid = 0.0 + 0.5 * dt;
       const double t_next = 0.0 + dt;
       st = stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_mid),
-                             mc.alpha, mc.beta, A_U, A_G, st, flo, fhi, R);
+                             mc.alpha, mc.beta, A_U, A_G, st, flo, fhi, plo, phi, R);
       st = stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_next),
-                             mc.alpha, mc.beta, A_G, A_U, st, flo, fhi, R);
+                             mc.alpha, mc.beta, A_G, A_U, st, flo, fhi, plo, phi, R);
       step = 1;
       if (active && nt >= 1) record(1, A_U);
     }
@@ -490,9 +555,9 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
       const double tn = static_cast<double>(step + 1) * dt;
       const bool last = (step == nt - 1);
       st = stage<kStage1>(live, n, V, F, nocache, o.bc_left, right_bc(o, t1), mc.alpha,
-                          mc.beta, A_U, A_G, st, flo, fhi, R);
+                          mc.beta, A_U, A_G, st, flo, fhi, plo, phi, R);
       st = stage<kStage2>(live, n, V, F, nocache, o.bc_left, right_bc(o, tn), mc.alpha,
-                          mc.beta, A_G, last ? A_G : A_U, st, flo, fhi, R);
+                          mc.beta, A_G, last ? A_G : A_U, st, flo, fhi, plo, phi, R);
       if (live && sc) record(step + 1, last ? A_G : A_U);
     }
     if (active) status[k] = st;

@@ -1,24 +1,25 @@
-"""GPU FDM implied volatility by Newton on the exact discrete vega
-(MANGO_GPU_IV_NEWTON).
+"""GPU FDM implied volatility by MANGO_GPU_IV_NEWTON: two Newton steps on a
+coarse grid with the exact discrete vega, then value-only secant steps on
+the quote's own grid, settling once the secant step through the last two
+own-grid values is at most 3e-6 (at that step's end).  Bars:
 
-Every evaluation prices the quote with the forward-mode march, so it yields
-V and dV/dsigma of the discrete price; Newton runs on a coarse grid first and
-then on the quote's own grid, and stops in volatility space: the returned
-root is one corrected Newton step beyond the last evaluation.  Bars:
-
-* against the reference's own Brent roots (iv.npz, produced by the
-  reference IVSolver): |sigma_newton - sigma_brent| <= tol / vega + 3e-7
-  (Brent stops within tol / vega of the exact root, Newton within 3e-7),
-  and within 1e-6 of the volatility the quote was priced at;
+* against the reference's own Brent roots (iv.npz and the 4,096 quotes of
+  iv_config4.npz, produced by the reference IVSolver):
+  |sigma_newton - sigma_brent| <= 2 tol / vega + 1e-7 (Brent stops where
+  |V - P| < tol, within tol / vega of the exact root; the secant stop and
+  the k-section fallback leave at most 1e-7 in volatility), except where the
+  objective is flat or has a second root: the returned vol then re-prices
+  to within tol;
 * round trip on 2,048 quotes drawn like the batched-IV workload (true vol
   U[0.05, 0.8], K/S U[0.8, 1.2], T U[0.02, 2]) priced at their true vol on the
   101 x 498 grid sized at that vol: every quote whose discrete vega at the
   true vol is at least 1e-4 (the reference InterpolatedIVSolver's default
   vega_threshold) settles within 1e-6 of the true vol, except where the
   objective has a second root (V(sigma) = P re-priced at the returned root,
-  to 1e-9 relative) -- at most 0.2 % of them on this sample;
+  to tol) -- at most 0.2 % of them on this sample;
 * statuses: settled quotes are MANGO_OK; quotes Newton hands over are
-  solved by Brent, so every status is one Brent can return.
+  solved by the k-section finder or Brent, so every status is one Brent can
+  return.
 """
 import numpy as np
 import pytest
@@ -46,10 +47,9 @@ def test_newton_vs_reference_golden(engine, pkg):
     p = pkg.pricing_array(g["S"], g["K"], g["T"], sig, g["r"], g["q"], g["is_put"])
     vega = np.abs(engine.tangent_arrays(p, grids, vega_only=True)["vega"])
     # Brent's root is within tol / vega of the exact root of the discrete
-    # objective, Newton's within its volatility-space stop (2e-7 plus the
-    # third-order bound)
+    # objective, Newton's within its volatility-space stop
     d = np.abs(sig - g["out"][:, 0])
-    assert (d <= TOL / vega + 3e-7).all(), f"worst {d.max():.3e}"
+    assert (d <= 2 * TOL / vega + 1e-7).all(), f"worst {d.max():.3e}"
     assert np.abs(sig - g["true_vol"]).max() < 1e-6
 
 
@@ -81,10 +81,12 @@ def test_newton_round_trip_config_sample(engine, pkg):
         sel = lambda a: np.asarray(a)[miss]
         v = engine.price_arrays(pkg.pricing_array(sel(S), sel(K), sel(T), out["implied_vol"][miss], sel(r),
                                                   sel(q), sel(put)), grids[miss])["value"]
-        assert np.abs(v - sel(truth["value"])).max() <= 1e-9 * sel(truth["value"]).max() + TOL
+        assert np.abs(v - sel(truth["value"])).max() <= TOL
     assert miss.sum() <= 0.002 * keep.sum() + 1, (miss.sum(), keep.sum())
-    # Newton-settled quotes need few evaluations on their own grid
-    assert st["iv_evals"][1] <= 2.5 * keep.sum()
+    # two coarse evaluations per quote, few on the own grid (the k-section
+    # fallback's rounds price several points per quote)
+    assert st["iv_evals"][0] <= 2 * len(S)
+    assert st["iv_evals"][1] <= 3 * len(S), st["iv_evals"]
 
 
 REF_STATUS = {0: 0, 13: 1, 14: 2, 18: 3, 19: 4}
@@ -95,10 +97,11 @@ def test_newton_config4_sample_vs_reference(engine, pkg):
     Brent roots on each quote's 101 x 498 grid).  Validation and arbitrage
     statuses are the reference's; every quote the reference solves is solved;
     a quote Brent cannot bracket may still be settled.  Roots: within
-    tol / vega + 3e-7 of the reference's for at least 99.5 % of the solved
-    quotes; the others either lie where the objective is flat or not
-    monotone (|V(sigma_newton) - P| below half of what the vega implies over
-    the distance) or count as misses, at most 0.3 % of the solved quotes."""
+    2 tol / vega + 1e-7 of the reference's; the rest (at most 0.5 %) are
+    roots themselves, |V(sigma_newton) - P| <= tol, where the objective is
+    flat or not monotone.  Quotes settled by the secant stop report the
+    secant's slope, the discrete vega at the root to 1 % where the
+    objective's slope does not jump within the last step (99 % of them)."""
     g = golden("iv_config4.npz")
     q = pkg.query_array(g["S"], g["K"], g["T"], g["r"], g["q"], g["is_put"], g["price"])
     grids = per_quote_grid(pkg, g["true_vol"])
@@ -115,12 +118,12 @@ def test_newton_config4_sample_vs_reference(engine, pkg):
     t = engine.tangent_arrays(p, grids, vega_only=True)
     vega = np.abs(t["vega"])
     d = np.abs(sig - g["out"][:, 0])
-    close = d <= TOL / np.maximum(vega, 1e-12) + 3e-7
-    assert close[ok].mean() >= 0.995, close[ok].mean()
+    close = d <= 2 * TOL / np.maximum(vega, 1e-12) + 1e-7
     far = ok & ~close
-    flat = np.abs(t["value"] - g["price"]) < 0.5 * vega * d
-    miss = far & ~flat
-    assert miss.sum() <= 0.003 * ok.sum(), (miss.sum(), ok.sum())
-    # Newton-settled quotes report the vega at the root
+    assert far.sum() <= 0.005 * ok.sum(), (far.sum(), ok.sum())
+    resid = np.abs(t["value"] - g["price"])
+    assert (resid[far] <= TOL).all(), resid[far].max()
     nw = ok & (out["has_vega"] == 1)
-    assert nw.mean() > 0.9 and np.allclose(out["vega"][nw], t["vega"][nw], rtol=1e-2, atol=1e-3)
+    assert nw.mean() > 0.9
+    good = np.isclose(out["vega"][nw], t["vega"][nw], rtol=1e-2, atol=1e-6)
+    assert good.mean() >= 0.99, good.mean()

@@ -59,7 +59,7 @@ struct Stats {
   double algo_flops = 0;
   double h2d_bytes = 0, d2h_bytes = 0;
   // FDM IV: quote evaluations on coarse grids with the volatility tangent,
-  // on the own grids with it, and on the own grids without it
+  // and on the own grids
   int64_t iv_evals[2] = {0, 0};
 };
 

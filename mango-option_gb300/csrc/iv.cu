@@ -245,8 +245,13 @@ __device__ int fast_consume(FastDev& s, const double* sig, const double* f, int 
       s.seen |= 2;
     }
   }
-  const double ptol = s.ftol > 0.0 ? s.ftol : tol;
+  double ptol = s.ftol > 0.0 ? s.ftol : tol;
   const double btol = s.ftol > 0.0 ? kVolTol : tol;
+  if (s.ftol > 0.0 && s.has_br && s.fr > s.fl) {
+    // a Newton hand-over settles within kVolTol along the bracket's own
+    // slope when that is the smaller one
+    ptol = fmin(ptol, kVolTol * (s.fr - s.fl) / (s.br - s.bl));
+  }
   if (fabs(s.fa) < ptol) return kFastSettled;
   if (!s.has_br && s.seen == 3) {
     s.has_br = 1;
@@ -476,8 +481,10 @@ __device__ void newton_to_fast(const NewtonDev& n, FastDev& s, double upper) {
   s.e0 = s.e1 = qnan();
   s.guess = isfinite(n.xb) ? n.xb : n.x0;
   s.iter = 1;  // the first proposal uses the best point, not the guess
-  // settle at |f| < 1e-7 vol times the best slope known
-  const double slope = n.sec > 0.0 ? n.sec : (n.vs > 0.0 ? n.vs : 1.0);
+  // settle at |f| < 1e-7 vol times the slope: the own grid's last secant,
+  // else the smaller of the coarse vega and the vega floor 1e-4 (a quote
+  // whose slope is unknown settles on its bracket instead)
+  const double slope = n.sec > 0.0 ? n.sec : (n.vs > 0.0 ? fmin(n.vs, 1e-4) : 1e-4);
   s.ftol = kVolTol * slope;
   if (s.seen == 3) {
     s.has_br = 1;

@@ -384,8 +384,21 @@ uint64_t table_sweep_device(MangoGpuContext* ctx, const double* moneyness, uint6
       check(cudaGetLastError(), "resample_kernel launch");
       std::vector<int32_t> hst(static_cast<size_t>(m));
       check(cudaMemcpyAsync(hst.data(), b->d_status.p, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, st), "D2H");
+      check(cudaEventRecord(b->ev[6], st), "event");
       check(cudaStreamSynchronize(st), "stream synchronize");
       for (int64_t k = 0; k < m; ++k) failed += hst[k] != kStatusOk;
+      // the call's stats: host preparation, setup, march (with snapshots),
+      // then the value-only outputs and the resampling together
+      Stats& S = ctx->stats;
+      S = Stats{};
+      float a = 0;
+      S.host_prep_ms = b->host_prep_ms;
+      if (cudaEventElapsedTime(&a, b->ev[2], b->ev[3]) == cudaSuccess) S.prep_ms = a;
+      if (cudaEventElapsedTime(&a, b->ev[3], b->ev[4]) == cudaSuccess) S.march_ms = a;
+      if (cudaEventElapsedTime(&a, b->ev[4], b->ev[6]) == cudaSuccess) S.outputs_ms = a;
+      cudaGetLastError();
+      S.options = m;
+      S.tiles = b->ntiles;
       for (DevBuf* d : {&d_sidx, &d_sbegin, &d_scount, &d_soff, &d_snaps, &d_slice, &d_m, &d_scratch})
         d->release();
     }

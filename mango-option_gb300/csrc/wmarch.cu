@@ -101,6 +101,20 @@ __device__ __forceinline__ double apply(const Clamp& c, double x) {
   return fmin(fmax(fma(c.b, x, c.a), c.lo), c.hi);
 }
 
+// x -> max(b x + a, lo) with b >= 0: the back-substitution maps whenever
+// every -c' of the stage is non-negative (the usual case: the implicit
+// matrix is an M-matrix, so its upper factor has non-positive c').  Closed
+// under composition without an upper bound, at half the arithmetic.
+struct Mono {
+  double b, a, lo;
+};
+__device__ __forceinline__ Mono compose(const Mono& o, const Mono& f) {
+  return Mono{o.b * f.b, fma(o.b, f.a, o.a), fmax(fma(o.b, f.lo, o.a), o.lo)};
+}
+__device__ __forceinline__ double apply(const Mono& c, double x) {
+  return fmax(fma(c.b, x, c.a), c.lo);
+}
+
 __device__ __forceinline__ double shfl_up_d(double v, int d) {
   return __shfl_up_sync(0xffffffffu, v, d);
 }
@@ -251,10 +265,23 @@ __device__ int32_t wstage(const WView& W, const TileView& P, int n, bool nocache
     a = rhs * inv;
     m = -l * inv;
   };
+  // the multiplier of a row map again, without its constant term
+  auto row_m = [&](int r) {
+    const int i = lane * R + r;
+    if (i == 0) return 0.0;
+    if (i > n - 2) return 1.0;
+    const unsigned char md = W.md[r * 32 + lane];
+    if (md == kRowLocked) return 0.0;
+    if (md == kRowCached) return W.atl(K == kStage1 ? W_N1H : W_N2H, r, lane);
+    const double l = K == kStage1 ? W.atl(W_L1, r, lane)
+                                  : (K == kStage2 ? W.atl(W_L2, r, lane) : P.at(A_LR, i));
+    return -l * W.atl(W_MI, r, lane);
+  };
   double A = 0.0, M = 1.0;
   for (int r = 0; r < R; ++r) {
     double a, m;
     row_map(r, a, m);
+    W.atl(W_D, r, lane) = a;  // the constant term, reused below
     A = fma(m, A, a);
     M = m * M;
   }
@@ -267,9 +294,7 @@ __device__ int32_t wstage(const WView& W, const TileView& P, int n, bool nocache
   }
   double dprev = shfl_up_d(A, 1);  // d' at the top row of the lane below
   for (int r = 0; r < R; ++r) {
-    double a, m;
-    row_map(r, a, m);
-    const double d = fma(m, dprev, a);
+    const double d = fma(row_m(r), dprev, W.atl(W_D, r, lane));
     W.atl(W_D, r, lane) = d;
     dprev = d;
   }
@@ -287,20 +312,42 @@ __device__ int32_t wstage(const WView& W, const TileView& P, int n, bool nocache
     if (i == n - 1) return Clamp{0.0, bcr, W.atl(W_PSI, r, lane), kBig};
     return Clamp{row_nc(r), W.atl(W_D, r, lane), W.atl(W_PSI, r, lane), kBig};
   };
-  Clamp C{1.0, 0.0, -kBig, kBig};
-  for (int r = R - 1; r >= 0; --r) C = compose(back_map(r), C);
-  for (int off = 1; off < 32; off <<= 1) {
-    Clamp o;
-    o.b = shfl_down_d(C.b, off);
-    o.a = shfl_down_d(C.a, off);
-    o.lo = shfl_down_d(C.lo, off);
-    o.hi = shfl_down_d(C.hi, off);
-    if (lane + off < 32) C = compose(C, o);
-  }
   // every suffix that reaches row n-1 holds its constant map: its value is x
   // at the lane's lowest row, and the lane above supplies the input of this
   // lane's top row
-  double xnext = shfl_down_d(apply(C, 0.0), 1);
+  bool nonneg = true;
+  for (int r = 0; r < R; ++r) {
+    const int i = lane * R + r;
+    if (i >= 1 && i <= n - 2) nonneg = nonneg && !(row_nc(r) < 0.0);
+  }
+  double xnext;
+  if (__all_sync(0xffffffffu, nonneg)) {
+    Mono C{1.0, 0.0, -kBig};
+    for (int r = R - 1; r >= 0; --r) {
+      const Clamp m = back_map(r);
+      C = compose(Mono{m.b, m.a, m.lo}, C);
+    }
+    for (int off = 1; off < 32; off <<= 1) {
+      Mono o;
+      o.b = shfl_down_d(C.b, off);
+      o.a = shfl_down_d(C.a, off);
+      o.lo = shfl_down_d(C.lo, off);
+      if (lane + off < 32) C = compose(C, o);
+    }
+    xnext = shfl_down_d(apply(C, 0.0), 1);
+  } else {
+    Clamp C{1.0, 0.0, -kBig, kBig};
+    for (int r = R - 1; r >= 0; --r) C = compose(back_map(r), C);
+    for (int off = 1; off < 32; off <<= 1) {
+      Clamp o;
+      o.b = shfl_down_d(C.b, off);
+      o.a = shfl_down_d(C.a, off);
+      o.lo = shfl_down_d(C.lo, off);
+      o.hi = shfl_down_d(C.hi, off);
+      if (lane + off < 32) C = compose(C, o);
+    }
+    xnext = shfl_down_d(apply(C, 0.0), 1);
+  }
   for (int r = R - 1; r >= 0; --r) {
     const int i = lane * R + r;
     if (i >= n) continue;
@@ -515,7 +562,26 @@ WarpPlan plan_warp_tiles(const TileDev* tiles, int ntiles, int tv_tile0, int num
                                                       wmarch_smem_bytes(R)),
         "occupancy");
   const int64_t wave = static_cast<int64_t>(num_sms) * std::max(bps, 1);
-  if (force == 1 || options <= wave) {
+  // Cost model of the two layouts for the candidate tiles, in microseconds,
+  // from measurements on GB300 (101 x 498 and 201 x 1000 grids, 200 to
+  // 65,536 options, both layouts forced): the warp march takes about
+  // kWarpStepUs + kWarpStepUsPerR * R per time step and wave of resident
+  // warps; the thread march about kThreadRowUs per row and step for a tile
+  // whose warp has its sub-partition to itself, or, once the tiles crowd the
+  // sub-partitions, kThreadRowTileUs per row, step and tile overall.
+  constexpr double kWarpStepUs = 10.8, kWarpStepUsPerR = 3.47;
+  constexpr double kThreadRowUs = 1.0, kThreadRowTileUs = 0.93e-3;
+  int rows = 0, steps = 0;
+  for (int t = 0; t < last; ++t)
+    if (wmarch_rows_per_lane(tiles[t].nx) <= rmax) {
+      rows = std::max(rows, tiles[t].nx);
+      steps = std::max(steps, tiles[t].nt);
+    }
+  const double waves = static_cast<double>((options + wave - 1) / wave);
+  const double warp_us = steps * (kWarpStepUs + kWarpStepUsPerR * R) * waves;
+  const double thread_us =
+      steps * std::max(rows * kThreadRowUs, static_cast<double>(last) * rows * kThreadRowTileUs);
+  if (force == 1 || warp_us < thread_us) {
     for (int t = 0; t < last; ++t)
       if (wmarch_rows_per_lane(tiles[t].nx) <= rmax) {
         plan.tiles.push_back(t);

@@ -25,11 +25,12 @@ void wmarch_launch(void* stream, int num_sms, const TileDev* tiles, const int32_
 
 // Which tiles of a packed set march one warp per option.  The options of the
 // tiles [0, ntiles) except the time-varying ones (from tile tv_tile0) are
-// candidates when their grid fits a warp's shared memory.  When all
-// candidate options fit in one wave of resident warps (the last evaluations
-// of a batched IV, a table sweep, small batches), every candidate tile goes
-// to the warp march; otherwise the thread march keeps them (a full batch
-// keeps every lane busy with its cheaper per-row work), except the longest
+// candidates when their grid fits a warp's shared memory.  When a measured
+// cost model says the warp march finishes them sooner (the last evaluations
+// of a batched IV, a table sweep, batches up to a few waves of resident
+// warps), every candidate tile goes to the warp march; otherwise the thread
+// march keeps them (a full batch keeps every lane busy with its cheaper
+// per-row work), except the longest
 // tiles of a batch whose tiles differ widely in cost (uneven grids): a
 // thread-march warp needs n x n_time dependent row updates for its tile, so
 // the tiles of more than twice the mean cost, up to kLongWarpOptions options,

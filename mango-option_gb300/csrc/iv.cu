@@ -1138,12 +1138,12 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
         evaluations += 1;
         if (trace)
           std::fprintf(stderr,
-                       "iv evaluation %d: quotes coarse %lld / own+tangent %lld / own %lld, "
-                       "points %lld / %lld / %lld, next %d per quote, %.3f ms\n",
-                       e, static_cast<long long>(ws[0].nq), static_cast<long long>(ws[1].nq),
-                       static_cast<long long>(ws[2].nq), static_cast<long long>(ws[0].mw),
-                       static_cast<long long>(ws[1].mw), static_cast<long long>(ws[2].mw), k_next,
-                       ms);
+                       "iv evaluation %d: quotes coarse %lld / own %lld, points %lld / %lld, "
+                       "next %d per quote, %.3f ms\n",
+                       e, static_cast<long long>(ws[kLevelCoarse].nq),
+                       static_cast<long long>(ws[kLevelPlain].nq),
+                       static_cast<long long>(ws[kLevelCoarse].mw),
+                       static_cast<long long>(ws[kLevelPlain].mw), k_next, ms);
       }
       for (int L = 0; L < kLevels; ++L) level_evals[L] = static_cast<int64_t>(level_slot_evals[L]);
       check(cudaMemcpyAsync(hr.data(), R, sizeof(IvOut) * m, cudaMemcpyDeviceToHost, st), "D2H results");

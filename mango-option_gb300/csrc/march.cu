@@ -193,7 +193,7 @@ enum StageKind { kRannacher = 0, kStage1 = 1, kStage2 = 2 };
 // serial recurrences never wait on HBM.  Ring layout [slot][array][lane],
 // at most kRingArrays arrays per row; a row's slot is refilled one row after
 // it was read.
-constexpr int kRing = 4;                        // rows in flight
+constexpr int kRing = 6;                        // rows in flight
 constexpr int kRingSlots = kRing + 1;           // the slot refilled was read one row earlier
 constexpr int kRingArrays = 4;
 constexpr int kRingSlot = kRingArrays * kTile;  // doubles per slot

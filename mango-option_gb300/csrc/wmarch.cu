@@ -162,8 +162,9 @@ __device__ int32_t wstage(const WView& W, const TileView& P, int n, bool nocache
       int i = always_fresh ? 1 : first_lock;
       double cprev = 0.0;  // c'_{i-1}: zero after a locked or Dirichlet row
       bool fresh = always_fresh;
-      for (; i <= n - 2; ++i) {
-        unsigned char& m = W.mode(i);
+      int ri = i % R, li = i / R;  // row i at [ri][li], advanced without division
+      for (; i <= n - 2; ++i, ri = (ri + 1 == R) ? 0 : ri + 1, li += (ri == 0) ? 1 : 0) {
+        unsigned char& m = W.md[ri * 32 + li];
         if (m == kRowLocked) {
           cprev = 0.0;
           fresh = true;
@@ -180,22 +181,22 @@ __device__ int32_t wstage(const WView& W, const TileView& P, int n, bool nocache
           up = P.at(A_UR, i);
           nc_cached = 0.0;
         } else if (K == kStage1) {
-          l = W.at(W_L1, i);
-          dg = W.at(W_D1, i);
-          up = W.at(W_U1, i);
-          nc_cached = W.at(W_NC1, i);
+          l = W.atl(W_L1, ri, li);
+          dg = W.atl(W_D1, ri, li);
+          up = W.atl(W_U1, ri, li);
+          nc_cached = W.atl(W_NC1, ri, li);
         } else {
-          l = W.at(W_L2, i);
-          dg = W.at(W_D2, i);
-          up = W.at(W_U2, i);
-          nc_cached = W.at(W_NC2, i);
+          l = W.atl(W_L2, ri, li);
+          dg = W.atl(W_D2, ri, li);
+          up = W.atl(W_U2, ri, li);
+          nc_cached = W.atl(W_NC2, ri, li);
         }
         const double denom = fma(-l, cprev, dg);
         if (fabs(denom) < 1e-15) st = kStatusSolver;
         const double inv = 1.0 / denom;
         const double c = up * inv;
-        W.at(W_MC, i) = -c;
-        W.at(W_MI, i) = inv;
+        W.atl(W_MC, ri, li) = -c;
+        W.atl(W_MI, ri, li) = inv;
         m = kRowOff;
         fresh = always_fresh || __double_as_longlong(-c) != __double_as_longlong(nc_cached);
         cprev = c;
@@ -226,9 +227,10 @@ __device__ int32_t wstage(const WView& W, const TileView& P, int n, bool nocache
     }
     double um = 0.0, u0 = 0.0, up = 0.0, g = 0.0, v = 0.0;
     if (K == kStage1) {
-      um = W.at(W_U, i - 1);
+      // neighbours: the lane's own adjacent rows, or the next lane's edge
+      um = r > 0 ? W.atl(W_U, r - 1, lane) : W.atl(W_U, R - 1, lane - 1);
       u0 = W.atl(W_U, r, lane);
-      up = W.at(W_U, i + 1);
+      up = r + 1 < R ? W.atl(W_U, r + 1, lane) : W.atl(W_U, 0, lane + 1);
     } else if (K == kStage2) {
       g = W.atl(W_G, r, lane);
       v = W.atl(W_U, r, lane);

@@ -708,6 +708,55 @@ def run_reference(args, ws, rank):
     return 0
 
 
+def bench_layouts(pkg, eng, torch):
+    """The engine's layout choice (thread-per-option or warp-per-option march,
+    plan_warp_tiles) against both layouts forced with MANGO_GPU_WARP_MARCH, on
+    the pricing workload at several batch sizes, the uneven batch, and the
+    table sweep.  Device march time of the batch's run after a warm-up run;
+    the table sweep end to end.  One JSON line per workload."""
+    def batch_ms(p, g):
+        b = eng.batch(p, g)
+        b.run()
+        torch.cuda.synchronize()
+        b.timings(reset=True)
+        for _ in range(3):
+            b.run()
+        torch.cuda.synchronize()
+        ms = b.timings()["march_ms"]
+        b.close()
+        return ms
+
+    def sweep_ms():
+        grid = pkg.PDEGridConfig(-3.0, 3.0, 201, 1000)
+        eng.price_table_sweep(*TABLE_AXES, 100.0, 0.0, 1, grid)
+        t0 = time.perf_counter()
+        for _ in range(3):
+            eng.price_table_sweep(*TABLE_AXES, 100.0, 0.0, 1, grid)
+        return (time.perf_counter() - t0) / 3 * 1e3
+
+    work = []
+    for n in (65536, 8192, 4096, 512):
+        p, g, _ = make_workload(pkg, n)
+        work.append((f"{n} options, 101x498", lambda p=p, g=g: batch_ms(p, g)))
+    p, g, _ = make_workload(pkg, 200)
+    work.append(("200 options, 201x1000", lambda p=p: batch_ms(p, pkg.grid_array(1, pkg.GRID_FIXED_N, 201, 1000))))
+    p, g, _ = make_workload(pkg, 65536, seed=77, uneven=True)
+    work.append(("65536 options, N_x~U{51..401}, N_t~U{100..1000}", lambda p=p, g=g: batch_ms(p, g)))
+    work.append(("table sweep, 200 solves at 201x1000 (end to end)", sweep_ms))
+    for name, fn in work:
+        row = {}
+        for label, val in (("auto", None), ("thread", "0"), ("warp", "1")):
+            if val is None:
+                os.environ.pop("MANGO_GPU_WARP_MARCH", None)
+            else:
+                os.environ["MANGO_GPU_WARP_MARCH"] = val
+            row[label] = round(fn(), 3)
+        os.environ.pop("MANGO_GPU_WARP_MARCH", None)
+        best = min(("thread", "warp"), key=lambda k: row[k])
+        print(json.dumps({"workload": name, "ms": row, "faster": best,
+                          "auto_within_3pct_of_faster": row["auto"] <= 1.03 * row[best]}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -724,6 +773,8 @@ def main():
     ap.add_argument("--iv-quotes", type=int, default=262144)
     ap.add_argument("--no-table", action="store_true", help="skip the table sweep / query side measurement")
     ap.add_argument("--queries", type=int, default=10_000_000)
+    ap.add_argument("--layouts", action="store_true",
+                    help="only compare the engine's thread/warp march choice with both layouts forced")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
@@ -743,6 +794,8 @@ def main():
     torch.cuda.set_stream(stream)
     assert stream.cuda_stream != 0
     eng.set_stream(stream.cuda_stream)
+    if args.layouts:
+        return bench_layouts(pkg, eng, torch)
     fp64_peak = eng.fp64_probe()
 
     n = args.options

@@ -863,11 +863,28 @@ def main():
         hbm = {"traffic_gbs": traffic / march_s / 1e9, "peak_gbs": hbm_peak,
                "frac": (traffic / march_s / 1e9 / hbm_peak) if hbm_peak else None,
                "note": "per-option working state (21 KB) re-streamed every step; 1.4 GB >> L2"}
+    # FP64 pipe: the kernel's FP64 warp instructions per warp row-step
+    # (ncu sm__inst_executed_pipe_fp64.sum of a captured launch) times this
+    # launch's row-steps, per second, against the probe's DFMA issue rate
+    # (TFLOP/s / 2 flops / 32 lanes): the pipe fraction beside the
+    # algorithmic one.
+    pipe = None
+    pf = ROOT / "profiles" / "march_kernel_fp64.json"
+    if pf.exists():
+        try:
+            per = json.loads(pf.read_text())["fp64_warp_inst_per_warp_row_step"]
+            inst = per * n * (NT - 1) * (NX - 2) / 32.0
+            probe_inst = fp64_peak * 1e12 / 2.0 / 32.0
+            pipe = {"fp64_warp_inst_per_warp_row_step": per, "achieved_ginst_s": inst / march_s / 1e9,
+                    "probe_ginst_s": probe_inst / 1e9, "frac": inst / march_s / probe_inst,
+                    "source": "profiles/march_kernel_fp64.json"}
+        except Exception:
+            pipe = None
     roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp64_peak, "traffic": traffic,
                 "peak_source": "measured live: mango_gpu_fp64_probe (independent DFMA chains, all SMs)",
                 "kernel": "march_kernel", "kernel_ms": kt["march_ms"],
-                "algo_flops_per_launch": algo, "hbm_streaming": hbm}
+                "algo_flops_per_launch": algo, "fp64_pipe": pipe, "hbm_streaming": hbm}
 
     extra = {}
     if not args.no_extra and not args.no_uneven and rank == 0:

@@ -66,17 +66,15 @@ constexpr double kBig = 1e300;  // "no bound" of a clamp map
 // thread march (two warp blocks per SM, a few options each).
 constexpr int64_t kLongWarpOptions = 1216;
 
+// R rows per lane, a compile-time constant: every row loop unrolls and
+// every shared-memory address is a constant offset from the lane's column.
+template <int R>
 struct WView {
   double* s;
   unsigned char* md;  // row modes [r][lane]
-  int R;
-  __device__ __forceinline__ double& at(int a, int i) const {
-    return s[(static_cast<size_t>(a) * R + (i % R)) * 32 + i / R];
-  }
   __device__ __forceinline__ double& atl(int a, int r, int lane) const {
-    return s[(static_cast<size_t>(a) * R + r) * 32 + lane];
+    return s[(a * R + r) * 32 + lane];
   }
-  __device__ __forceinline__ unsigned char& mode(int i) const { return md[(i % R) * 32 + i / R]; }
 };
 
 // x -> min(max(b x + a, lo), hi)
@@ -129,12 +127,11 @@ enum StageKind { kRannacher = 0, kStage1 = 1, kStage2 = 2 };
 //   kStage1:    rhs = u + w1 L(u) of u^n (W_U), guess u^n, writes W_G;
 //   kStage2:    rhs = alpha g + beta u^n (g = W_G), guess g, writes a_out.
 // P: the option's rows in the tile pool (Rannacher bands); returns the status.
-template <int K>
-__device__ int32_t wstage(const WView& W, const TileView& P, int n, bool nocache, int flo,
+template <int K, int R>
+__device__ int32_t wstage(const WView<R>& W, const TileView& P, int n, bool nocache, int flo,
                           int fhi, double bcl, double bcr, double alpha, double beta, int a_in,
                           int a_out, int32_t st) {
   const int lane = threadIdx.x & 31;
-  const int R = W.R;
   const bool always_fresh = (K == kRannacher) || nocache;
   const int a_guess = (K == kStage1) ? W_U : a_in;
   // ---- lock test per row (pde_solver.hpp:635-680), rows [flo, fhi]
@@ -376,16 +373,15 @@ __device__ __forceinline__ double right_bc(const OptDev& o, double t) {
 }  // namespace
 
 // Persistent: each warp takes options (warp tiles wt[0..nwt) x 32 lanes) from
-// the queue; R = rows per lane of the launch's widest option.
-__global__ void __launch_bounds__(32) wmarch_kernel(
-    const TileDev* __restrict__ tiles, const int32_t* __restrict__ wt, int nwt,
+// the queue; R = rows per lane, at least that of the launch's widest option.
+template <int R>
+__device__ __forceinline__ void wmarch_body(
+    double* wsm, const TileDev* __restrict__ tiles, const int32_t* __restrict__ wt, int nwt,
     const OptDev* __restrict__ opts, double* __restrict__ pool, const uint8_t* __restrict__ flags,
     const int32_t* __restrict__ mode, int32_t* __restrict__ status, int* __restrict__ queue,
-    MarchConst mc, int R) {
-  extern __shared__ double wsm[];
+    const MarchConst& mc) {
   const int lane = threadIdx.x & 31;
-  const WView W{wsm, reinterpret_cast<unsigned char*>(wsm + static_cast<size_t>(kWArrays) * R * 32),
-                R};
+  const WView<R> W{wsm, reinterpret_cast<unsigned char*>(wsm + static_cast<size_t>(kWArrays) * R * 32)};
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(queue, 1);
@@ -466,9 +462,9 @@ __global__ void __launch_bounds__(32) wmarch_kernel(
     if (mc.rannacher) {
       const double t_mid = 0.0 + 0.5 * dt;
       const double t_next = 0.0 + dt;
-      st = wstage<kRannacher>(W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, t_mid), mc.alpha,
+      st = wstage<kRannacher, R>(W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, t_mid), mc.alpha,
                               mc.beta, W_U, W_G, st);
-      st = wstage<kRannacher>(W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, t_next),
+      st = wstage<kRannacher, R>(W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, t_next),
                               mc.alpha, mc.beta, W_G, W_U, st);
       step = 1;
       if (o.nt >= 1) record(1, W_U);
@@ -478,9 +474,9 @@ __global__ void __launch_bounds__(32) wmarch_kernel(
       const double t1 = tt + mc.gamma * dt;
       const double tn = static_cast<double>(step + 1) * dt;
       const bool last = (step == o.nt - 1);
-      st = wstage<kStage1>(W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, t1), mc.alpha,
+      st = wstage<kStage1, R>(W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, t1), mc.alpha,
                            mc.beta, W_U, W_G, st);
-      st = wstage<kStage2>(W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, tn), mc.alpha,
+      st = wstage<kStage2, R>(W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, tn), mc.alpha,
                            mc.beta, W_G, last ? W_G : W_U, st);
       if (sc) record(step + 1, last ? W_G : W_U);
     }
@@ -497,30 +493,62 @@ __global__ void __launch_bounds__(32) wmarch_kernel(
   }
 }
 
+// Concrete kernels, one per row count (a __global__ template is not used).
+#define MGPU_WMARCH_KERNEL(RT)                                                                   \
+  __global__ void __launch_bounds__(32) wmarch_kernel_##RT(                                     \
+      const TileDev* __restrict__ tiles, const int32_t* __restrict__ wt, int nwt,               \
+      const OptDev* __restrict__ opts, double* __restrict__ pool,                               \
+      const uint8_t* __restrict__ flags, const int32_t* __restrict__ mode,                      \
+      int32_t* __restrict__ status, int* __restrict__ queue, MarchConst mc) {                   \
+    extern __shared__ double wsm[];                                                             \
+    wmarch_body<RT>(wsm, tiles, wt, nwt, opts, pool, flags, mode, status, queue, mc);           \
+  }
+MGPU_WMARCH_KERNEL(1)
+MGPU_WMARCH_KERNEL(2)
+MGPU_WMARCH_KERNEL(4)
+MGPU_WMARCH_KERNEL(8)
+MGPU_WMARCH_KERNEL(16)
+MGPU_WMARCH_KERNEL(32)
+#undef MGPU_WMARCH_KERNEL
+
 // ------------------------------------------------------------------- host --
 
 size_t wmarch_smem_bytes(int R) {
   return sizeof(double) * static_cast<size_t>(kWArrays) * R * 32 + static_cast<size_t>(R) * 32;
 }
 
-int wmarch_rows_per_lane(int n) { return (n + 31) / 32; }
-
-int wmarch_max_rows() {
-  // rows per lane that fit one warp's shared memory (227 KB per block)
+int wmarch_rows_per_lane(int n) {
+  // the instantiated row counts: 1, 2, 4, 8, 16, 32 rows per lane
   int R = 1;
-  while (wmarch_smem_bytes(R + 1) <= 227 * 1024) ++R;
+  while (R * 32 < n) R *= 2;
   return R;
 }
 
+int wmarch_max_rows() { return 32; }
+
 namespace {
-// Opt the kernel in to the largest dynamic shared memory once per process
-// (the attribute applies on every device the kernel runs on).
+using WmarchFn = void (*)(const TileDev*, const int32_t*, int, const OptDev*, double*,
+                          const uint8_t*, const int32_t*, int32_t*, int*, MarchConst);
+WmarchFn wmarch_kernel_for(int R) {
+  switch (R) {
+    case 1: return wmarch_kernel_1;
+    case 2: return wmarch_kernel_2;
+    case 4: return wmarch_kernel_4;
+    case 8: return wmarch_kernel_8;
+    case 16: return wmarch_kernel_16;
+    default: return wmarch_kernel_32;
+  }
+}
+// Opt each kernel in to its dynamic shared memory once per process (the
+// attribute applies on every device the kernel runs on).
 void wmarch_opt_in() {
   static bool done = false;
   if (done) return;
-  check(cudaFuncSetAttribute(wmarch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(wmarch_smem_bytes(wmarch_max_rows()))),
-        "wmarch smem attribute");
+  for (int R = 1; R <= 32; R *= 2)
+    check(cudaFuncSetAttribute(reinterpret_cast<const void*>(wmarch_kernel_for(R)),
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(wmarch_smem_bytes(R))),
+          "wmarch smem attribute");
   done = true;
 }
 }  // namespace
@@ -532,12 +560,12 @@ void wmarch_launch(void* stream, int num_sms, const TileDev* tiles, const int32_
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const size_t smem = wmarch_smem_bytes(R);
   wmarch_opt_in();
+  const WmarchFn fn = wmarch_kernel_for(R);
   int bps = 0;
-  check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, wmarch_kernel, 32, smem), "occupancy");
+  check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, 32, smem), "occupancy");
   int blocks = std::max(1, std::min(num_sms * std::max(bps, 1), nwt * kTile));
   if (max_blocks > 0) blocks = std::min(blocks, max_blocks);
-  wmarch_kernel<<<blocks, 32, smem, st>>>(tiles, wt, nwt, opts, pool, flags, mode, status, queue,
-                                          mc, R);
+  fn<<<blocks, 32, smem, st>>>(tiles, wt, nwt, opts, pool, flags, mode, status, queue, mc);
   check(cudaGetLastError(), "wmarch_kernel launch");
 }
 
@@ -560,7 +588,7 @@ WarpPlan plan_warp_tiles(const TileDev* tiles, int ntiles, int tv_tile0, int num
   if (options == 0) return plan;
   wmarch_opt_in();
   int bps = 0;
-  check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, wmarch_kernel, 32,
+  check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, wmarch_kernel_for(R), 32,
                                                       wmarch_smem_bytes(R)),
         "occupancy");
   const int64_t wave = static_cast<int64_t>(num_sms) * std::max(bps, 1);

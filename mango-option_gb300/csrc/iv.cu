@@ -360,6 +360,8 @@ __device__ __forceinline__ double objective(const double* out4, const int32_t* m
 // tangent (Newton's first evaluations) and the quotes' own grids without it
 // (Newton's later evaluations, Brent, the secant, time-varying quotes).
 constexpr int32_t kLevelCoarse = 0, kLevelPlain = 1, kLevels = 2;
+// Quotes left at or below which a round re-orders its working set.
+constexpr int64_t kTailQuotes = 65536;
 
 // Newton on f = V - P at s.x; v = dV/dsigma on the coarse level (the
 // evaluation carried the tangent).  Coarse level: exactly kCoarseEvals
@@ -961,7 +963,7 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
         mat[s] = q.maturity;
       }
       DevBuf d_state, d_res, d_next, d_npts, d_hi, d_px, d_mat, d_lev;
-      HostBuf h_npts, h_lev;
+      HostBuf h_npts, h_lev, h_sig1;
       struct Release {
         std::vector<DevBuf*> d;
         std::vector<HostBuf*> h;
@@ -970,7 +972,7 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
           for (HostBuf* x : h) x->release();
         }
       } release{{&d_state, &d_res, &d_next, &d_npts, &d_hi, &d_px, &d_mat, &d_lev},
-                {&h_npts, &h_lev}};
+                {&h_npts, &h_lev, &h_sig1}};
       IvDev* S = static_cast<IvDev*>(d_state.get(sizeof(IvDev) * m));
       IvOut* R = static_cast<IvOut*>(d_res.get(sizeof(IvOut) * m));
       double* next_sig = static_cast<double*>(d_next.get(sizeof(double) * kMaxPts * m));
@@ -978,6 +980,7 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
       int32_t* hnpts = static_cast<int32_t*>(h_npts.get(sizeof(int32_t) * m));
       int32_t* lev = static_cast<int32_t*>(d_lev.get(sizeof(int32_t) * m));
       int32_t* hlev = static_cast<int32_t*>(h_lev.get(sizeof(int32_t) * m));
+      double* hsig1 = static_cast<double*>(h_sig1.get(sizeof(double) * m));
       double* dhi = static_cast<double*>(d_hi.get(sizeof(double) * m));
       double* dpx = static_cast<double*>(d_px.get(sizeof(double) * m));
       double* dmat = static_cast<double*>(d_mat.get(sizeof(double) * m));
@@ -1037,6 +1040,13 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
               "D2H points");
         check(cudaMemcpyAsync(hlev, lev, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, st),
               "D2H levels");
+        // Few quotes left (the tail): their first trial points too, to order
+        // the working set below.
+        const bool tail = static_cast<int64_t>(active.size()) <= kTailQuotes;
+        if (tail)
+          check(cudaMemcpy2DAsync(hsig1, sizeof(double), next_sig, sizeof(double) * kMaxPts,
+                                  sizeof(double), static_cast<size_t>(m), cudaMemcpyDeviceToHost, st),
+                "D2H trial points");
         check(cudaStreamSynchronize(st), "stream synchronize");
         const auto tp = Clock::now();
         for (auto& l : lists) l.clear();
@@ -1048,6 +1058,24 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
             lists[std::min(std::max(hlev[q], 0), kLevels - 1)].push_back(q);
           }
         active.swap(still);
+        if (tail) {
+          // The tail's quotes are a sparse, scattered subset whose trial
+          // volatilities differ from the ones the batch was sorted by: order
+          // them again by type and ln(S/K) / (sigma sqrt(T)) at their next
+          // trial point, so that the lanes of a tile meet the obstacle at
+          // similar rows (as the pricing batch's sort arranges).
+          const OptDev* ho = b->h_opts.as<OptDev>();
+          auto key = [&](int32_t q) {
+            const double sg = hsig1[q] > 0.0 ? hsig1[q] : 0.2;
+            return std::log(ho[q].spot / ho[q].strike) / (sg * std::sqrt(mat[q]));
+          };
+          for (auto& l : lists)
+            std::sort(l.begin(), l.end(), [&](int32_t a, int32_t c) {
+              if (ho[a].is_put != ho[c].is_put) return ho[a].is_put < ho[c].is_put;
+              const double ka = key(a), kc = key(c);
+              return ka != kc ? ka < kc : a < c;
+            });
+        }
         int64_t nq_all = 0;
         for (int L = 0; L < kLevels; ++L) {
           ws[L].pack(lists[L], hnpts, next_sig);

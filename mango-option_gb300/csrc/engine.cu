@@ -12,11 +12,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <functional>
 #include <memory>
-#include <queue>
 #include <thread>
-#include <utility>
 
 namespace mgpu {
 
@@ -285,8 +282,7 @@ void destroy_batch(MangoGpuBatch* b) {
   if (!b) return;
   for (mgpu::DevBuf* d : {&b->d_pool, &b->d_xs, &b->d_flags, &b->d_opts, &b->d_tiles, &b->d_mode,
                           &b->d_status, &b->d_out4, &b->d_queue, &b->d_tv, &b->d_tv_tp,
-                          &b->d_tv_curve, &b->d_tv_ev, &b->d_wt, &b->d_tile_warp, &b->d_bins,
-                          &b->d_bin_cnt})
+                          &b->d_tv_curve, &b->d_tv_ev, &b->d_wt, &b->d_tile_warp})
     d->release();
   for (mgpu::HostBuf* h : {&b->h_xs, &b->h_opts, &b->h_tiles, &b->h_out4, &b->h_status})
     h->release();
@@ -360,8 +356,6 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
   b->tv_tile0 = 0;
   b->wplan_ready = false;
   b->nwt = 0;
-  b->nbins = 0;
-  b->nbin_tiles = 0;
   b->ran = false;
   b->runs = 0;
   for (auto& e : b->ev)
@@ -663,62 +657,10 @@ void run_batch(MangoGpuBatch* b) {
                             static_cast<size_t>(ntiles), cudaMemcpyHostToDevice, st),
             "H2D warp flags");
     }
-    // The thread march's tiles over the SM sub-partitions, longest first to
-    // the least-loaded list (cost: rows x steps of the tile's widest and
-    // longest lane).  A warp's FP64 issue is shared with the other warps of
-    // its sub-partition, so a tile's march time is set by its list's total,
-    // not by a single queue's order: balanced lists keep the longest tiles of
-    // an uneven batch from running four to a sub-partition at the end.
-    const int nbins = 4 * ctx->num_sms;
-    std::vector<int32_t> mt;
-    for (int t = 0; t < tv0; ++t)
-      if (b->nwt == 0 || !plan.flag[t]) mt.push_back(t);
-    b->nbins = 0;
-    if (static_cast<int64_t>(mt.size()) >= 2 * static_cast<int64_t>(nbins)) {
-      const TileDev* th = b->h_tiles.as<TileDev>();
-      auto cost = [&](int32_t t) {
-        return static_cast<double>(std::max(th[t].nx - 2, 1)) * static_cast<double>(th[t].nt);
-      };
-      std::stable_sort(mt.begin(), mt.end(), [&](int32_t a, int32_t c) { return cost(a) > cost(c); });
-      std::vector<std::vector<int32_t>> lists(static_cast<size_t>(nbins));
-      using Load = std::pair<double, int>;
-      std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
-      for (int j = 0; j < nbins; ++j) heap.push({0.0, j});
-      for (int32_t t : mt) {
-        Load l = heap.top();
-        heap.pop();
-        lists[static_cast<size_t>(l.second)].push_back(t);
-        l.first += cost(t);
-        heap.push(l);
-      }
-      std::vector<int32_t> packed(static_cast<size_t>(nbins) + 1 + mt.size());
-      int32_t off = 0;
-      for (int j = 0; j < nbins; ++j) {
-        packed[static_cast<size_t>(j)] = off;
-        for (int32_t t : lists[static_cast<size_t>(j)])
-          packed[static_cast<size_t>(nbins) + 1 + static_cast<size_t>(off++)] = t;
-      }
-      packed[static_cast<size_t>(nbins)] = off;
-      check(cudaMemcpyAsync(b->d_bins.get(sizeof(int32_t) * packed.size()), packed.data(),
-                            sizeof(int32_t) * packed.size(), cudaMemcpyHostToDevice, st),
-            "H2D tile lists");  // pageable source: staged before the call returns
-      b->d_bin_cnt.get(sizeof(int) * (static_cast<size_t>(nbins) + 1));
-      b->nbins = nbins;
-      b->nbin_tiles = off;
-    }
     b->wplan_ready = true;
   }
   MarchConst mc = b->mc;
   mc.tile_warp = b->nwt > 0 ? b->d_tile_warp.as<uint8_t>() : nullptr;
-  if (b->nbins > 0) {
-    check(cudaMemsetAsync(b->d_bin_cnt.p, 0, sizeof(int) * (static_cast<size_t>(b->nbins) + 1), st),
-          "memset tile lists");
-    mc.bin_off = b->d_bins.as<int32_t>();
-    mc.bin_tiles = mc.bin_off + b->nbins + 1;
-    mc.bin_cnt = b->d_bin_cnt.as<int>();
-    mc.nbins = b->nbins;
-    mc.nbin_tiles = b->nbin_tiles;
-  }
   const int warps_per_block = 4;
   int bps = ctx->march_blocks_per_sm;
   // MANGO_GPU_MARCH_BLOCKS_PER_SM: resident march blocks per SM (1 to the

@@ -187,10 +187,6 @@ struct MangoGpuBatch {
   cudaStream_t wstream = nullptr;       // its stream, created on first use
   cudaEvent_t wev[2] = {nullptr, nullptr};
   mgpu::DevBuf d_wt, d_tile_warp;
-  // Thread-march tiles balanced over the SM sub-partitions (planned with the
-  // warp tiles): list offsets then tiles, and the list counters.
-  int32_t nbins = 0, nbin_tiles = 0;
-  mgpu::DevBuf d_bins, d_bin_cnt;
   mgpu::HostBuf h_xs, h_opts, h_tiles, h_out4, h_status;
   cudaEvent_t ev[8] = {};
   bool ran = false;

@@ -444,32 +444,7 @@ __device__ __forceinline__ double right_bc(const OptDev& o, double t) {
 
 }  // namespace
 
-// Next tile for the calling lane's warp from the per-sub-partition lists
-// (MarchConst::nbins > 0): its own list first, then the others in turn;
-// -1 once every list is exhausted.  At most nbins list probes.
-__device__ int take_binned(const MarchConst& mc) {
-  unsigned smid, wslot;
-  asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
-  asm volatile("mov.u32 %0, %%warpid;" : "=r"(wslot));
-  const int nsm = mc.nbins / 4;
-  const int home = static_cast<int>(smid % static_cast<unsigned>(nsm)) * 4 + static_cast<int>(wslot & 3u);
-  volatile const int* cnt = mc.bin_cnt;
-  for (int j = 0; j < mc.nbins; ++j) {
-    if (cnt[mc.nbins] >= mc.nbin_tiles) return -1;
-    const int b = home + j < mc.nbins ? home + j : home + j - mc.nbins;
-    const int size = mc.bin_off[b + 1] - mc.bin_off[b];
-    if (cnt[b] >= size) continue;
-    const int k = atomicAdd(&mc.bin_cnt[b], 1);
-    if (k < size) {
-      atomicAdd(&mc.bin_cnt[mc.nbins], 1);
-      return mc.bin_tiles[mc.bin_off[b] + k];
-    }
-  }
-  return -1;
-}
-
-// Persistent march: each warp pulls tiles (largest first) from the queue,
-// or from its sub-partition's list (take_binned).
+// Persistent march: each warp pulls tiles (largest first) from the queue.
 __global__ void __launch_bounds__(128, 4) march_kernel(
     const TileDev* __restrict__ tiles, int ntiles, const OptDev* __restrict__ opts,
     double* __restrict__ pool, const uint8_t* __restrict__ flags,
@@ -479,9 +454,9 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
   __shared__ double ring[4][kRingSlots * kRingSlot];  // one ring per warp (128 threads)
   for (;;) {
     int t = 0;
-    if (lane == 0) t = mc.nbins > 0 ? take_binned(mc) : atomicAdd(queue, 1);
+    if (lane == 0) t = atomicAdd(queue, 1);
     t = __shfl_sync(0xffffffffu, t, 0);
-    if (t < 0 || t >= ntiles) break;
+    if (t >= ntiles) break;
     if (mc.tile_warp && mc.tile_warp[t]) continue;  // marched one warp per option
     const TileDev td = tiles[t];
     const int k = td.first + lane;

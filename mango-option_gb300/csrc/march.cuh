@@ -91,16 +91,6 @@ struct MarchConst {
   // first pivot is exactly 0 and the solve reports kStatusSolver as a
   // singular Thomas pivot does; -1 = none.
   int32_t singular_pivot = -1;
-  // Per-SM-sub-partition tile lists, or nbins = 0: every warp pulls from one
-  // queue.  List b is bin_tiles[bin_off[b] .. bin_off[b + 1]); a warp takes
-  // from the list of its own sub-partition ((SM id, warp slot mod 4)) first,
-  // then from the others.  bin_cnt: nbins list counters, then at [nbins]
-  // the tiles taken overall (nbin_tiles in all); zero before the launch.
-  const int32_t* bin_off = nullptr;
-  const int32_t* bin_tiles = nullptr;
-  int* bin_cnt = nullptr;
-  int32_t nbins = 0;
-  int32_t nbin_tiles = 0;
 };
 
 // Per-option data of the time-varying march, indexed by sorted index minus

@@ -274,32 +274,57 @@ __device__ __forceinline__ void issue_bwd(const TileView& V, double* R, int i, i
 struct SlowOut {
   double d;      // d'_i
   double c;      // c'_i of this row (0 for a locked row)
-  int lo, hi;    // rows held in A_CP
+  int lo, hi;    // rows held in the stage's -c' array
   bool fresh;    // next row is still off the cache
   bool singular; // |pivot| < 1e-15 (thomas_solver.hpp:386-388)
 };
 
+// Rows off the cache of one stage kind, kept from the last sweep: the factor
+// run that restarted after row L (a locked row, or the Dirichlet row 0 of an
+// option without a usable cache) is stored for rows (L, H] in the stage's
+// -c' and inverse-pivot arrays.  The run depends on L and the stage matrix
+// only, so the next sweep that restarts after the same row takes the stored
+// factors instead of dividing again; the deep-ITM lock block of a put keeps
+// its end row for many steps.  L = -2: nothing stored.
+struct RunMemo {
+  int L = -2, H = -2;
+};
+
 // A forward-sweep row off the cached factorisation: a locked row (identity
 // with rhs psi) or a row whose factor is recomputed exactly as the reference
-// does (thomas_solver.hpp:382-395).  Records the row's own -c' in A_CP and
-// keeps [lo, hi] contiguous.  All state travels by value so the caller keeps
-// it in registers.
+// does (thomas_solver.hpp:382-395), or taken from the memo when the current
+// run restarted after the memo's row.  Records the row's own -c' and keeps
+// [lo, hi] contiguous.  run_l: the row the current run restarted after.  All
+// state travels by value so the caller keeps it in registers.
 template <int K>
 __device__ __forceinline__ SlowOut slow_row(const TileView V, int i, bool lock, double psi_i,
                                          double um, double u0, double v, double g,
                                          double alpha, double beta, double dprev,
-                                         double cprev, bool always_fresh, int lo, int hi) {
+                                         double cprev, bool always_fresh, int lo, int hi,
+                                         int run_l, RunMemo& memo) {
   constexpr int aL = (K == kRannacher) ? A_LR : (K == kStage1 ? A_L1 : A_L2);
   constexpr int aDg = (K == kRannacher) ? A_DR : (K == kStage1 ? A_D1 : A_D2);
   constexpr int aU = (K == kRannacher) ? A_UR : (K == kStage1 ? A_U1 : A_U2);
   constexpr int aNC = (K == kStage2) ? A_NC2 : A_NC1;
+  constexpr int aCP = (K == kStage2) ? A_CP2 : A_CP;
+  constexpr int aIP = (K == kStage2) ? A_IP2 : A_IP1;
+  constexpr bool kMemo = (K != kRannacher);
   double* p = V.rp(i);
   SlowOut o;
   o.singular = false;
+  // Rows between the previous off-cache row and this one keep their cached
+  // value in the -c' array so that [lo, hi] is valid for the back
+  // substitution; a memo whose rows they overwrite ends before them.
+  if (hi >= 0 && i > hi + 1) {
+    for (int q = hi + 1; q < i; ++q) V.at(aCP, q) = V.at(aNC, q);
+    if (kMemo && max(hi + 1, memo.L + 1) <= min(i - 1, memo.H)) memo.H = max(hi, memo.L);
+  }
   if (lock) {
     o.d = psi_i;  // identity row with rhs psi: c' = 0, d' = psi
     o.c = 0.0;
     o.fresh = true;
+    p[aCP * kTile] = -0.0;
+    if (kMemo && i > memo.L && i <= memo.H) memo.H = i - 1;
   } else {
     double rhs;
     if (K == kStage1)
@@ -309,18 +334,31 @@ __device__ __forceinline__ SlowOut slow_row(const TileView V, int i, bool lock, 
     else
       rhs = g;
     const double l = p[aL * kTile];
-    const double denom = fma(-l, cprev, p[aDg * kTile]);
-    o.singular = fabs(denom) < 1e-15;
-    const double inv = 1.0 / denom;
-    o.c = p[aU * kTile] * inv;
-    o.d = fma(-l, dprev, rhs) * inv;
+    if (kMemo && run_l == memo.L && i <= memo.H) {
+      const double negc = p[aCP * kTile];  // stored by the memo's run
+      o.c = -negc;
+      o.d = fma(-l, dprev, rhs) * p[aIP * kTile];
+    } else {
+      const double denom = fma(-l, cprev, p[aDg * kTile]);
+      o.singular = fabs(denom) < 1e-15;
+      const double inv = 1.0 / denom;
+      o.c = p[aU * kTile] * inv;
+      o.d = fma(-l, dprev, rhs) * inv;
+      p[aCP * kTile] = -o.c;
+      if (kMemo) {
+        p[aIP * kTile] = inv;
+        if (run_l == memo.L && i == memo.H + 1) {
+          memo.H = i;  // the memo's run goes on
+        } else if (i == run_l + 1) {
+          memo.L = run_l;  // a new run starts here: it becomes the memo
+          memo.H = i;
+        } else if (i > memo.L && i <= memo.H) {
+          memo.H = i - 1;  // this run overwrote the memo's rows from i on
+        }
+      }
+    }
     o.fresh = always_fresh || !same_bits(-o.c, p[aNC * kTile]);
   }
-  // Rows between the previous off-cache row and this one keep their cached
-  // value in A_CP so that [lo, hi] is valid for the back substitution.
-  if (hi >= 0 && i > hi + 1)
-    for (int q = hi + 1; q < i; ++q) V.at(A_CP, q) = V.at(aNC, q);
-  p[A_CP * kTile] = -o.c;
   o.lo = lo == INT_MAX ? i : lo;
   o.hi = i;
   return o;
@@ -335,7 +373,8 @@ template <int K>
 __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
                                       const uint8_t* __restrict__ F, bool nocache, double bcl,
                                       double bcr, double alpha, double beta, int a_in, int a_out,
-                                      int32_t st, int flo, int fhi, int plo, int phi, double* R) {
+                                      int32_t st, int flo, int fhi, int plo, int phi, double* R,
+                                      RunMemo& memo) {
   const int last = V.NX - 2;  // last interior row of the tile
   const bool always_fresh = (K == kRannacher) || nocache;
   const L2Pol pol = l2_policies();
@@ -349,7 +388,8 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
   double dprev = bcl;  // d'_0 = rhs_0 / 1 on the Dirichlet row
   double cprev = 0.0;  // recomputed c'_{i-1}; valid whenever `fresh`
   bool fresh = always_fresh;
-  int lo = INT_MAX, hi = -1;  // rows [lo, hi] take -c' from A_CP
+  int lo = INT_MAX, hi = -1;  // rows [lo, hi] take -c' from the stage's array
+  int run_l = always_fresh ? 0 : -1;  // the row the current off-cache run restarted after
   double um = 0.0, u0 = 0.0;
   if (K == kStage1 && live) {
     um = V.at(A_U, 0);
@@ -391,7 +431,8 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
         dcur = fma(rnl, dprev, ra * fma(beta_alpha, rv, g));
     } else {
       const SlowOut so = slow_row<K>(V, i, lock, psi_i, um, u0, rv, g, alpha, beta, dprev, cprev,
-                                     always_fresh, lo, hi);
+                                     always_fresh, lo, hi, run_l, memo);
+      if (lock) run_l = i;
       dcur = so.d;
       cprev = so.c;
       fresh = so.fresh;
@@ -427,7 +468,7 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
     const double rpsi = (i >= plo && i <= phi) ? s[kTile] : 0.0;
     if (i - kRing >= 1) issue_bwd<K>(V, R, i - kRing, plo, phi, pol);
     cp_commit();
-    const double nc = (i >= lo && i <= hi) ? V.at(A_CP, i) : rnc;
+    const double nc = (i >= lo && i <= hi) ? V.at(K == kStage2 ? A_CP2 : A_CP, i) : rnc;
     const double xv = proj_max(fma(nc, xnext, rd), rpsi);
     V.at(a_out, i) = xv;
     xnext = xv;
@@ -493,6 +534,7 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
       }
     int32_t st = kStatusOk;
     const double dt = o.dt;
+    RunMemo memo1, memo2, memo_r;  // stage 1, stage 2; the Rannacher stages keep none
     // Snapshot taps: copy the state after the listed steps.
     int sp = 0, sc = 0;
     const int32_t* sidx = nullptr;
@@ -516,9 +558,9 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
       const double t_mid = 0.0 + 0.5 * dt;
       const double t_next = 0.0 + dt;
       st = stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_mid),
-                             mc.alpha, mc.beta, A_U, A_G, st, flo, fhi, plo, phi, R);
+                             mc.alpha, mc.beta, A_U, A_G, st, flo, fhi, plo, phi, R, memo_r);
       st = stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_next),
-                             mc.alpha, mc.beta, A_G, A_U, st, flo, fhi, plo, phi, R);
+                             mc.alpha, mc.beta, A_G, A_U, st, flo, fhi, plo, phi, R, memo_r);
       step = 1;
       if (active && nt >= 1) record(1, A_U);
     }
@@ -530,9 +572,9 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
       const double tn = static_cast<double>(step + 1) * dt;
       const bool last = (step == nt - 1);
       st = stage<kStage1>(live, n, V, F, nocache, o.bc_left, right_bc(o, t1), mc.alpha,
-                          mc.beta, A_U, A_G, st, flo, fhi, plo, phi, R);
+                          mc.beta, A_U, A_G, st, flo, fhi, plo, phi, R, memo1);
       st = stage<kStage2>(live, n, V, F, nocache, o.bc_left, right_bc(o, tn), mc.alpha,
-                          mc.beta, A_G, last ? A_G : A_U, st, flo, fhi, plo, phi, R);
+                          mc.beta, A_G, last ? A_G : A_U, st, flo, fhi, plo, phi, R, memo2);
       if (live && sc) record(step + 1, last ? A_G : A_U);
     }
     if (active) status[k] = st;

@@ -29,7 +29,10 @@ enum TileArray : int {
   A_U,        // state u^n
   A_G,        // state u^{n+gamma} (and the final u)
   A_D,        // Thomas d' scratch
-  A_CP,       // Thomas c' of rows solved off the cache
+  A_CP,       // Thomas -c' of rows solved off the cache (stage 1, Rannacher)
+  A_CP2,      // the same for stage 2
+  A_IP1,      // inverse pivot of stage-1 rows solved off the cache
+  A_IP2,      // the same for stage 2
   A_E1L0,     // unscaled stage-1 stencil (rows off the cache)
   A_E1D0,
   A_E1U0,

@@ -55,7 +55,8 @@ enum WArray : int {
   W_A2H, W_B2H, W_N2H, W_NC2,         // stage 2 cached row factors
   W_L1, W_D1, W_U1, W_L2, W_D2, W_U2, // stage matrix bands (rows off the cache)
   W_U, W_G, W_D,                      // state u^n, u^{n+gamma}, Thomas d'
-  W_MC, W_MI,                         // -c' and 1 / pivot of rows off the cache
+  W_MC, W_MI,                         // -c' and 1 / pivot of rows off the cache (stage 1)
+  W_MC2, W_MI2,                       //   the same for stage 2
   W_FL,                               // lock-candidate flag (0 / 1)
   kWArrays
 };
@@ -75,6 +76,13 @@ struct WView {
   __device__ __forceinline__ double& atl(int a, int r, int lane) const {
     return s[(a * R + r) * 32 + lane];
   }
+};
+
+// The factor run of one stage kind that restarted after row L, kept in the
+// stage's -c' / inverse-pivot arrays for rows (L, H] (lane 0's walk): a walk
+// that restarts after the same row takes them instead of dividing again.
+struct RunMemo {
+  int L = -2, H = -2;
 };
 
 // x -> min(max(b x + a, lo), hi)
@@ -128,7 +136,7 @@ enum StageKind { kRannacher = 0, kStage1 = 1, kStage2 = 2 };
 //   kStage2:    rhs = alpha g + beta u^n (g = W_G), guess g, writes a_out.
 // P: the option's rows in the tile pool (Rannacher bands); returns the status.
 template <int K, int R>
-__device__ int32_t wstage(const WView<R>& W, const TileView& P, int n, bool nocache, int flo,
+__device__ int32_t wstage(RunMemo& memo, const WView<R>& W, const TileView& P, int n, bool nocache, int flo,
                           int fhi, double bcl, double bcr, double alpha, double beta, int a_in,
                           int a_out, int32_t st) {
   const int lane = threadIdx.x & 31;
@@ -156,15 +164,19 @@ __device__ int32_t wstage(const WView<R>& W, const TileView& P, int n, bool noca
   // is bit-identical to the cached one after the last locked row.
   if (always_fresh || last_lock >= 0) {
     if (lane == 0) {
+      constexpr int aMC = (K == kStage2) ? W_MC2 : W_MC, aMI = (K == kStage2) ? W_MI2 : W_MI;
+      constexpr bool kMemo = (K != kRannacher);
       int i = always_fresh ? 1 : first_lock;
       double cprev = 0.0;  // c'_{i-1}: zero after a locked or Dirichlet row
       bool fresh = always_fresh;
+      int run_l = always_fresh ? 0 : -1;  // the row the current run restarted after
       int ri = i % R, li = i / R;  // row i at [ri][li], advanced without division
       for (; i <= n - 2; ++i, ri = (ri + 1 == R) ? 0 : ri + 1, li += (ri == 0) ? 1 : 0) {
         unsigned char& m = W.md[ri * 32 + li];
         if (m == kRowLocked) {
           cprev = 0.0;
           fresh = true;
+          run_l = i;
           continue;
         }
         if (!fresh) {
@@ -188,12 +200,27 @@ __device__ int32_t wstage(const WView<R>& W, const TileView& P, int n, bool noca
           up = W.atl(W_U2, ri, li);
           nc_cached = W.atl(W_NC2, ri, li);
         }
-        const double denom = fma(-l, cprev, dg);
-        if (fabs(denom) < 1e-15) st = kStatusSolver;
-        const double inv = 1.0 / denom;
-        const double c = up * inv;
-        W.atl(W_MC, ri, li) = -c;
-        W.atl(W_MI, ri, li) = inv;
+        double c;
+        if (kMemo && run_l == memo.L && i <= memo.H) {
+          c = -W.atl(aMC, ri, li);  // stored by the memo's run, with its inverse pivot
+        } else {
+          const double denom = fma(-l, cprev, dg);
+          if (fabs(denom) < 1e-15) st = kStatusSolver;
+          const double inv = 1.0 / denom;
+          c = up * inv;
+          W.atl(aMC, ri, li) = -c;
+          W.atl(aMI, ri, li) = inv;
+          if (kMemo) {
+            if (run_l == memo.L && i == memo.H + 1) {
+              memo.H = i;
+            } else if (i == run_l + 1) {
+              memo.L = run_l;
+              memo.H = i;
+            } else if (i > memo.L && i <= memo.H) {
+              memo.H = i - 1;
+            }
+          }
+        }
         m = kRowOff;
         fresh = always_fresh || __double_as_longlong(-c) != __double_as_longlong(nc_cached);
         cprev = c;
@@ -260,7 +287,7 @@ __device__ int32_t wstage(const WView<R>& W, const TileView& P, int n, bool noca
       rhs = g;
       l = P.at(A_LR, i);
     }
-    const double inv = W.atl(W_MI, r, lane);
+    const double inv = W.atl(K == kStage2 ? W_MI2 : W_MI, r, lane);
     a = rhs * inv;
     m = -l * inv;
   };
@@ -274,7 +301,7 @@ __device__ int32_t wstage(const WView<R>& W, const TileView& P, int n, bool noca
     if (md == kRowCached) return W.atl(K == kStage1 ? W_N1H : W_N2H, r, lane);
     const double l = K == kStage1 ? W.atl(W_L1, r, lane)
                                   : (K == kStage2 ? W.atl(W_L2, r, lane) : P.at(A_LR, i));
-    return -l * W.atl(W_MI, r, lane);
+    return -l * W.atl(K == kStage2 ? W_MI2 : W_MI, r, lane);
   };
   double A = 0.0, M = 1.0;
   for (int r = 0; r < R; ++r) {
@@ -303,7 +330,7 @@ __device__ int32_t wstage(const WView<R>& W, const TileView& P, int n, bool noca
   auto row_nc = [&](int r) {
     const unsigned char md = W.md[r * 32 + lane];
     return md == kRowCached ? W.atl(K == kStage2 ? W_NC2 : W_NC1, r, lane)
-                            : (md == kRowOff ? W.atl(W_MC, r, lane) : 0.0);
+                            : (md == kRowOff ? W.atl(K == kStage2 ? W_MC2 : W_MC, r, lane) : 0.0);
   };
   auto back_map = [&](int r) {
     const int i = lane * R + r;
@@ -440,6 +467,7 @@ __device__ __forceinline__ void wmarch_body(
     __syncwarp();
     int32_t st = kStatusOk;
     const double dt = o.dt;
+    RunMemo memo1, memo2, memo_r;  // stage 1, stage 2; the Rannacher stages keep none
     int sp = 0, sc = 0;
     const int32_t* sidx = nullptr;
     double* sout = nullptr;
@@ -462,9 +490,9 @@ __device__ __forceinline__ void wmarch_body(
     if (mc.rannacher) {
       const double t_mid = 0.0 + 0.5 * dt;
       const double t_next = 0.0 + dt;
-      st = wstage<kRannacher, R>(W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, t_mid), mc.alpha,
+      st = wstage<kRannacher, R>(memo_r, W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, t_mid), mc.alpha,
                               mc.beta, W_U, W_G, st);
-      st = wstage<kRannacher, R>(W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, t_next),
+      st = wstage<kRannacher, R>(memo_r, W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, t_next),
                               mc.alpha, mc.beta, W_G, W_U, st);
       step = 1;
       if (o.nt >= 1) record(1, W_U);
@@ -474,9 +502,9 @@ __device__ __forceinline__ void wmarch_body(
       const double t1 = tt + mc.gamma * dt;
       const double tn = static_cast<double>(step + 1) * dt;
       const bool last = (step == o.nt - 1);
-      st = wstage<kStage1, R>(W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, t1), mc.alpha,
+      st = wstage<kStage1, R>(memo1, W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, t1), mc.alpha,
                            mc.beta, W_U, W_G, st);
-      st = wstage<kStage2, R>(W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, tn), mc.alpha,
+      st = wstage<kStage2, R>(memo2, W, P, n, nocache, flo, fhi, o.bc_left, right_bc(o, tn), mc.alpha,
                            mc.beta, W_G, last ? W_G : W_U, st);
       if (sc) record(step + 1, last ? W_G : W_U);
     }

@@ -604,7 +604,7 @@ MangoStatus mango_gpu_fp64_probe(MangoGpuContext* ctx, double* tflops, MangoErro
  * example code running under an allocator that owns the whole GPU, or with a
  * fixed memory budget).  Same inputs, outputs and per-slot semantics as
  * mango_gpu_price_american_batch, but no context is needed and nothing is
- * allocated: the work runs in one static device array of about 28 MB that
+ * allocated: the work runs in one static device array of about 32 MB that
  * every GPU loading this library holds until the process exits.  Limits: at
  * most 4096 options per call and at most 131072 grid rows (sum over
  * 32-option tiles of 32 x the tile's largest n_space); larger requests are

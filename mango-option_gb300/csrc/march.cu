@@ -270,6 +270,39 @@ __device__ __forceinline__ void issue_bwd(const TileView& V, double* R, int i, i
   cp_async8(s + 2 * kTile, p + A_D * kTile, pol.last);
 }
 
+// Rows off the cache read their bands, their explicit stencil (stage 1) and
+// the memo's factors straight from the tile pool, outside the ring; while a
+// run is off the cache the sweep prefetches them kSlowAhead rows ahead so
+// that a long run (a trial volatility far above the grid's, whose factor
+// never re-converges) does not wait on DRAM row by row.
+constexpr int kSlowAhead = 4;
+__device__ __forceinline__ void prefetch_l1(const double* p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+template <int K>
+__device__ __forceinline__ void prefetch_slow(const TileView& V, int i) {
+  const double* p = V.rp(i);
+  if (K == kRannacher) {
+    prefetch_l1(p + A_LR * kTile);
+    prefetch_l1(p + A_DR * kTile);
+    prefetch_l1(p + A_UR * kTile);
+    return;
+  }
+  constexpr int aL = K == kStage1 ? A_L1 : A_L2, aDg = K == kStage1 ? A_D1 : A_D2,
+                aU = K == kStage1 ? A_U1 : A_U2, aCP = K == kStage1 ? A_CP : A_CP2,
+                aIP = K == kStage1 ? A_IP1 : A_IP2;
+  prefetch_l1(p + aL * kTile);
+  prefetch_l1(p + aDg * kTile);
+  prefetch_l1(p + aU * kTile);
+  prefetch_l1(p + aCP * kTile);
+  prefetch_l1(p + aIP * kTile);
+  if (K == kStage1) {
+    prefetch_l1(p + A_E1L0 * kTile);
+    prefetch_l1(p + A_E1D0 * kTile);
+    prefetch_l1(p + A_E1U0 * kTile);
+  }
+}
+
 // Result of a forward-sweep row solved off the cached factorisation.
 struct SlowOut {
   double d;      // d'_i
@@ -439,6 +472,7 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
       lo = so.lo;
       hi = so.hi;
       if (so.singular) st = kStatusSolver;
+      if (fresh && i + kSlowAhead <= stop) prefetch_slow<K>(V, i + kSlowAhead);
     }
     st_hint(&V.at(A_D, i), dcur, pol.last);
     dprev = dcur;

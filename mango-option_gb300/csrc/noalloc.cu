@@ -10,7 +10,7 @@
 // the process exits.  It calls no cudaMalloc/cudaFree/cudaMallocAsync and no
 // allocating library routine.
 //
-// Limits (the array is sized for them, ~28 MB of device memory per GPU):
+// Limits (the array is sized for them, ~32 MB of device memory per GPU):
 //   at most kNoAllocMaxOptions options per call, and at most
 //   kNoAllocMaxRows grid rows in total, counted as the sum over 32-option
 //   tiles (options sorted by grid size) of 32 x the tile's largest n_space.

@@ -83,6 +83,7 @@ struct WView {
 // that restarts after the same row takes them instead of dividing again.
 struct RunMemo {
   int L = -2, H = -2;
+  int done = 0;  // the run ended in (L, H]: it re-converged at H or reached row n - 2
 };
 
 // x -> min(max(b x + a, lo), hi)
@@ -143,7 +144,7 @@ __device__ int32_t wstage(RunMemo& memo, const WView<R>& W, const TileView& P, i
   const bool always_fresh = (K == kRannacher) || nocache;
   const int a_guess = (K == kStage1) ? W_U : a_in;
   // ---- lock test per row (pde_solver.hpp:635-680), rows [flo, fhi]
-  int last_lock = -1, first_lock = INT_MAX;
+  int last_lock = -1, first_lock = INT_MAX, nlock = 0;
   for (int r = 0; r < R; ++r) {
     const int i = lane * R + r;
     bool lock = false;
@@ -153,23 +154,44 @@ __device__ int32_t wstage(RunMemo& memo, const WView<R>& W, const TileView& P, i
     if (lock) {
       last_lock = i;
       first_lock = min(first_lock, i);
+      ++nlock;
     }
   }
   last_lock = __reduce_max_sync(0xffffffffu, last_lock);
   first_lock = __reduce_min_sync(0xffffffffu, first_lock);
+  nlock = __reduce_add_sync(0xffffffffu, nlock);
+  const bool one_block = last_lock >= 0 && nlock == last_lock - first_lock + 1;
+  // lane 0 keeps the memo; every lane reads it
+  memo.L = __shfl_sync(0xffffffffu, memo.L, 0);
+  memo.H = __shfl_sync(0xffffffffu, memo.H, 0);
+  memo.done = __shfl_sync(0xffffffffu, memo.done, 0);
   __syncwarp();
+  // One lock block ending where the memo's complete run restarted: the rows
+  // off the cache are exactly the memo's, so every lane marks its own and
+  // nothing is walked.
+  const bool memo_run = K != kRannacher && !always_fresh && one_block && memo.done &&
+                        memo.L == last_lock;
+  if (memo_run) {
+    for (int r = 0; r < R; ++r) {
+      const int i = lane * R + r;
+      if (i > memo.L && i <= memo.H) W.md[r * 32 + lane] = kRowOff;
+    }
+    __syncwarp();
+  }
   // ---- rows off the cache: one lane walks them in order, as the serial
   // sweep does, from the first locked row (every row for the Rannacher
   // stages and an option without a usable cache) until the recomputed c'
   // is bit-identical to the cached one after the last locked row.
-  if (always_fresh || last_lock >= 0) {
+  if (!memo_run && (always_fresh || last_lock >= 0)) {
     if (lane == 0) {
       constexpr int aMC = (K == kStage2) ? W_MC2 : W_MC, aMI = (K == kStage2) ? W_MI2 : W_MI;
       constexpr bool kMemo = (K != kRannacher);
-      int i = always_fresh ? 1 : first_lock;
+      // one lock block: its rows before the last need no visit
+      int i = always_fresh ? 1 : (one_block ? last_lock : first_lock);
       double cprev = 0.0;  // c'_{i-1}: zero after a locked or Dirichlet row
       bool fresh = always_fresh;
       int run_l = always_fresh ? 0 : -1;  // the row the current run restarted after
+      int last_off = -1;                  // the last row put off the cache
       int ri = i % R, li = i / R;  // row i at [ri][li], advanced without division
       for (; i <= n - 2; ++i, ri = (ri + 1 == R) ? 0 : ri + 1, li += (ri == 0) ? 1 : 0) {
         unsigned char& m = W.md[ri * 32 + li];
@@ -224,7 +246,11 @@ __device__ int32_t wstage(RunMemo& memo, const WView<R>& W, const TileView& P, i
         m = kRowOff;
         fresh = always_fresh || __double_as_longlong(-c) != __double_as_longlong(nc_cached);
         cprev = c;
+        last_off = i;
       }
+      // the memo's run is complete when it is the last run and holds its
+      // last row (re-convergence, or row n - 2)
+      if (kMemo) memo.done = (run_l == memo.L && memo.H == last_off) ? 1 : 0;
     }
     st = __shfl_sync(0xffffffffu, st, 0);
     __syncwarp();

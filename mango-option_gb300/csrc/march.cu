@@ -195,7 +195,7 @@ enum StageKind { kRannacher = 0, kStage1 = 1, kStage2 = 2 };
 // it was read.
 constexpr int kRing = 6;                        // rows in flight
 constexpr int kRingSlots = kRing + 1;           // the slot refilled was read one row earlier
-constexpr int kRingArrays = 4;
+constexpr int kRingArrays = 5;
 constexpr int kRingSlot = kRingArrays * kTile;  // doubles per slot
 
 // L2 eviction priorities.  The time-invariant row arrays are re-read once
@@ -237,12 +237,14 @@ __device__ __forceinline__ void cp_wait_oldest() {
 // operator's lower weight equals the Jacobian's), and the stage-2 row takes
 // beta/alpha times the alpha weight for u^n, so neither E1L nor B2H streams.
 //   stage 1: E1D, E1U, N1H, u_{i+1};  stage 2: A2H, N2H, g_i, u_i;
-//   Rannacher: slot 2 = u_prev.
+//   Rannacher: slot 2 = u_prev;  all: slot 4 = psi on the tile's
+//   lock-candidate rows [flo, fhi] (the lock test's obstacle).
 template <int K>
 __device__ __forceinline__ void issue_fwd(const TileView& V, double* R, int a_in, int i,
-                                          const L2Pol& pol) {
+                                          const L2Pol& pol, int flo, int fhi) {
   double* s = R + (i % kRingSlots) * kRingSlot;
   const double* p = V.rp(i);
+  if (i >= flo && i <= fhi) cp_async8(s + 4 * kTile, p + A_PSI * kTile, pol.first);
   if (K == kStage1) {
     cp_async8(s, p + A_E1D * kTile, pol.first);
     cp_async8(s + kTile, p + A_E1U * kTile, pol.first);
@@ -407,7 +409,7 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
                                       const uint8_t* __restrict__ F, bool nocache, double bcl,
                                       double bcr, double alpha, double beta, int a_in, int a_out,
                                       int32_t st, int flo, int fhi, int plo, int phi, double* R,
-                                      RunMemo& memo) {
+                                      RunMemo& memo, int cflo, int cfhi, bool cexact) {
   const int last = V.NX - 2;  // last interior row of the tile
   const bool always_fresh = (K == kRannacher) || nocache;
   const L2Pol pol = l2_policies();
@@ -430,7 +432,7 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
   }
   const int stop = live ? min(last, n - 2) : 0;
   for (int j = 1; j <= kRing; ++j) {
-    if (j <= stop) issue_fwd<K>(V, R, a_in, j, pol);
+    if (j <= stop) issue_fwd<K>(V, R, a_in, j, pol, flo, fhi);
     cp_commit();
   }
   // The lock test (pde_solver.hpp:635-680) only runs on the tile's
@@ -447,13 +449,14 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
       rv = s[3 * kTile];
     }
     const double rc = s[(K == kStage1 ? 1 : 2) * kTile];  // stage 1: E1U; else the guess
-    if (i + kRing <= stop) issue_fwd<K>(V, R, a_in, i + kRing, pol);
+    if (i + kRing <= stop) issue_fwd<K>(V, R, a_in, i + kRing, pol, flo, fhi);
     cp_commit();
     const double g = (K == kStage1) ? u0 : rc;
     bool lock = false;
     double psi_i = 0.0;
-    if (decltype(may_lock)::value && ROW(F, i)) {
-      psi_i = V.at(A_PSI, i);
+    // this lane's candidate rows: its own contiguous block, else the flags
+    if (decltype(may_lock)::value && (cexact ? (i >= cflo && i <= cfhi) : ROW(F, i) != 0)) {
+      psi_i = s[4 * kTile];
       lock = (g - psi_i < 1e-8);
     }
     double dcur;
@@ -549,13 +552,17 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
     const TileView V{pool + td.off + lane, td.nx};
     const uint8_t* F = flags + td.foff + lane;
     double* R = ring[threadIdx.x / kTile];
-    // Lock-candidate rows of the tile: union over its lanes.
-    int flo = INT_MAX, fhi = -1;
+    // Lock-candidate rows: this lane's (one contiguous block when cexact),
+    // and the tile's union over its lanes.
+    int flo = INT_MAX, fhi = -1, ncand = 0;
     for (int i = 1; i < n - 1; ++i)
       if (ROW(F, i)) {
         flo = min(flo, i);
         fhi = i;
+        ++ncand;
       }
+    const int cflo = flo, cfhi = fhi;
+    const bool cexact = ncand == 0 || ncand == cfhi - cflo + 1;
     flo = __reduce_min_sync(0xffffffffu, flo);
     fhi = __reduce_max_sync(0xffffffffu, fhi);
     // Interior rows where this lane's obstacle is positive (one contiguous
@@ -592,9 +599,9 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
       const double t_mid = 0.0 + 0.5 * dt;
       const double t_next = 0.0 + dt;
       st = stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_mid),
-                             mc.alpha, mc.beta, A_U, A_G, st, flo, fhi, plo, phi, R, memo_r);
+                             mc.alpha, mc.beta, A_U, A_G, st, flo, fhi, plo, phi, R, memo_r, cflo, cfhi, cexact);
       st = stage<kRannacher>(active, n, V, F, nocache, o.bc_left, right_bc(o, t_next),
-                             mc.alpha, mc.beta, A_G, A_U, st, flo, fhi, plo, phi, R, memo_r);
+                             mc.alpha, mc.beta, A_G, A_U, st, flo, fhi, plo, phi, R, memo_r, cflo, cfhi, cexact);
       step = 1;
       if (active && nt >= 1) record(1, A_U);
     }
@@ -606,9 +613,9 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
       const double tn = static_cast<double>(step + 1) * dt;
       const bool last = (step == nt - 1);
       st = stage<kStage1>(live, n, V, F, nocache, o.bc_left, right_bc(o, t1), mc.alpha,
-                          mc.beta, A_U, A_G, st, flo, fhi, plo, phi, R, memo1);
+                          mc.beta, A_U, A_G, st, flo, fhi, plo, phi, R, memo1, cflo, cfhi, cexact);
       st = stage<kStage2>(live, n, V, F, nocache, o.bc_left, right_bc(o, tn), mc.alpha,
-                          mc.beta, A_G, last ? A_G : A_U, st, flo, fhi, plo, phi, R, memo2);
+                          mc.beta, A_G, last ? A_G : A_U, st, flo, fhi, plo, phi, R, memo2, cflo, cfhi, cexact);
       if (live && sc) record(step + 1, last ? A_G : A_U);
     }
     if (active) status[k] = st;

@@ -181,7 +181,8 @@ template <int ND>
 struct TanRing {
   static constexpr int kAhead = ND == 1 ? 4 : 2;   // rows in flight
   static constexpr int kSlots = kAhead + 1;        // a slot is refilled one row after it was read
-  static constexpr int kArrays = 5 + 5 * ND;       // per row: primal 5, per direction 5
+  static constexpr int kArrays = 6 + 5 * ND;       // per row: primal 5, per direction 5, psi
+  static constexpr int kPsi = 5 + 5 * ND;          // the lock test's obstacle
   static constexpr int kSlot = kArrays * kTile;    // doubles per slot
   static constexpr int kWarp = kSlots * kSlot;     // doubles per warp
 };
@@ -210,10 +211,11 @@ struct TanVec {
 // then per direction its four row-factor derivatives and its state.
 template <int K, int ND>
 __device__ __forceinline__ void issue_fwd_t(const TileView& V, const TanView<ND>& W, double* R,
-                                            int a_in, int t_in, int i) {
+                                            int a_in, int t_in, int i, int flo, int fhi) {
   using RG = TanRing<ND>;
   double* s = R + (i % RG::kSlots) * RG::kSlot;
   const double* p = V.rp(i);
+  if (i >= flo && i <= fhi) cp_async8(s + RG::kPsi * kTile, p + A_PSI * kTile);
   if (K == kStage1) {
     cp_async8(s, p + A_E1L * kTile);
     cp_async8(s + kTile, p + A_E1D * kTile);
@@ -281,7 +283,8 @@ __device__ __noinline__ int32_t stage_t(bool live, int n, const TileView V, cons
                                         const uint8_t* __restrict__ F, bool nocache, double bcl,
                                         double bcr, TanVec<ND> tbcr, double alpha, double beta,
                                         double wst, int a_in, int a_out, int t_in, int t_out,
-                                        int32_t st, int flo, int fhi, double* R) {
+                                        int32_t st, int flo, int fhi, double* R, int cflo,
+                                        int cfhi, bool cexact) {
   using RG = TanRing<ND>;
   constexpr int aL = (K == kRannacher) ? A_LR : (K == kStage1 ? A_L1 : A_L2);
   constexpr int aDg = (K == kRannacher) ? A_DR : (K == kStage1 ? A_D1 : A_D2);
@@ -312,7 +315,7 @@ __device__ __noinline__ int32_t stage_t(bool live, int n, const TileView V, cons
   }
   const int stop = live ? min(last, n - 2) : 0;
   for (int j = 1; j <= RG::kAhead; ++j) {
-    if (j <= stop) issue_fwd_t<K, ND>(V, W, R, a_in, t_in, j);
+    if (j <= stop) issue_fwd_t<K, ND>(V, W, R, a_in, t_in, j, flo, fhi);
     cp_commit();
   }
   auto row = [&](int i, auto may_lock) {
@@ -336,13 +339,14 @@ __device__ __noinline__ int32_t stage_t(bool live, int n, const TileView V, cons
       qn[j] = q[3 * kTile];
       qv[j] = q[4 * kTile];
     }
-    if (i + RG::kAhead <= stop) issue_fwd_t<K, ND>(V, W, R, a_in, t_in, i + RG::kAhead);
+    if (i + RG::kAhead <= stop) issue_fwd_t<K, ND>(V, W, R, a_in, t_in, i + RG::kAhead, flo, fhi);
     cp_commit();
     const double g = (K == kStage1) ? u0 : rc;
     bool lock = false;
     double psi_i = 0.0;
-    if (decltype(may_lock)::value && ROW(F, i)) {
-      psi_i = V.at(A_PSI, i);
+    // this lane's candidate rows: its own contiguous block, else the flags
+    if (decltype(may_lock)::value && (cexact ? (i >= cflo && i <= cfhi) : ROW(F, i) != 0)) {
+      psi_i = s[RG::kPsi * kTile];
       lock = (g - psi_i < 1e-8);
     }
     double dcur, tdcur[ND];
@@ -540,12 +544,15 @@ __device__ __forceinline__ void march_tan_body(
     const TanView<ND> W{tpool + tan_off<ND>(td) + lane};
     const uint8_t* F = flags + td.foff + lane;
     double* R = ring[threadIdx.x / kTile];
-    int flo = INT_MAX, fhi = -1;
+    int flo = INT_MAX, fhi = -1, ncand = 0;
     for (int i = 1; i < n - 1; ++i)
       if (ROW(F, i)) {
         flo = min(flo, i);
         fhi = i;
+        ++ncand;
       }
+    const int cflo = flo, cfhi = fhi;
+    const bool cexact = ncand == 0 || ncand == cfhi - cflo + 1;
     flo = __reduce_min_sync(0xffffffffu, flo);
     fhi = __reduce_max_sync(0xffffffffu, fhi);
     int32_t st = kStatusOk;
@@ -572,10 +579,12 @@ __device__ __forceinline__ void march_tan_body(
       const double t_next = 0.0 + dt;
       double bcr = bc_r(t_mid, &tb);
       st = stage_t<kRannacher, ND>(active, n, V, W, F, nocache, o.bc_left, bcr, tb, mc.alpha,
-                                   mc.beta, wr, A_U, A_G, T_U, T_G, st, flo, fhi, R);
+                                   mc.beta, wr, A_U, A_G, T_U, T_G, st, flo, fhi, R, cflo, cfhi,
+                                   cexact);
       bcr = bc_r(t_next, &tb);
       st = stage_t<kRannacher, ND>(active, n, V, W, F, nocache, o.bc_left, bcr, tb, mc.alpha,
-                                   mc.beta, wr, A_G, A_U, T_G, T_U, st, flo, fhi, R);
+                                   mc.beta, wr, A_G, A_U, T_G, T_U, st, flo, fhi, R, cflo, cfhi,
+                                   cexact);
       step = 1;
     }
     for (; step < td.nt; ++step) {
@@ -586,10 +595,11 @@ __device__ __forceinline__ void march_tan_body(
       const bool last = (step == nt - 1);
       double bcr = bc_r(t1, &tb);
       st = stage_t<kStage1, ND>(live, n, V, W, F, nocache, o.bc_left, bcr, tb, mc.alpha, mc.beta,
-                                w1, A_U, A_G, T_U, T_G, st, flo, fhi, R);
+                                w1, A_U, A_G, T_U, T_G, st, flo, fhi, R, cflo, cfhi, cexact);
       bcr = bc_r(tn, &tb);
       st = stage_t<kStage2, ND>(live, n, V, W, F, nocache, o.bc_left, bcr, tb, mc.alpha, mc.beta,
-                                w2, A_G, last ? A_G : A_U, T_G, last ? T_G : T_U, st, flo, fhi, R);
+                                w2, A_G, last ? A_G : A_U, T_G, last ? T_G : T_U, st, flo, fhi, R,
+                                cflo, cfhi, cexact);
     }
     if (active) status[k] = st;
   }

@@ -9,7 +9,7 @@ Workload (one "step" = one pass of the hot path over the batch):
   min = max = 101, PDEGridConfig n_time = 498).  Synthetic data.
 
   value : options/s with the batch resident in device memory (setup +
-          march + outputs kernels per step; ~1.4 GB of per-option state,
+          march + outputs kernels per step; ~1.5 GB of per-option state,
           far above the 129 MB L2, so no flush is needed between steps).
   e2e   : options/s through the C ABI call mango_gpu_price_american_batch
           with host arrays: validation, grid generation, H2D, kernels, D2H.
@@ -862,7 +862,7 @@ def main():
         hbm_peak = measured_hbm_gbs()
         hbm = {"traffic_gbs": traffic / march_s / 1e9, "peak_gbs": hbm_peak,
                "frac": (traffic / march_s / 1e9 / hbm_peak) if hbm_peak else None,
-               "note": "per-option working state (21 KB) re-streamed every step; 1.4 GB >> L2"}
+               "note": "per-option working state (23 KB) re-streamed every step; 1.5 GB >> L2"}
     # FP64 pipe: the kernel's FP64 warp instructions per warp row-step
     # (ncu sm__inst_executed_pipe_fp64.sum of a captured launch) times this
     # launch's row-steps, per second, against the probe's DFMA issue rate
@@ -949,7 +949,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"{n} American puts/calls (50/50), 101x498 sinh grid rule, FP64",
                        "options": n, "n_space": NX, "n_time": NT, "parallelism": f"replicas x{ws}",
-                       "l2": "no flush: per-step device state ~1.4 GB >> 129 MB L2"},
+                       "l2": "no flush: per-step device state ~1.5 GB >> 129 MB L2"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": 3 * args.steps,
             "kernel_ms_per_step": {k: round(kt[k], 4) for k in ("prep_ms", "march_ms", "outputs_ms")},

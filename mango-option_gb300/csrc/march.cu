@@ -260,14 +260,19 @@ __device__ __forceinline__ void issue_fwd(const TileView& V, double* R, int a_in
   }
 }
 
-// Back-substitution inputs of row i into ring slot i % kRingSlots: -c', the
-// obstacle where it is positive (rows [plo, phi]; 0 elsewhere), d'.
+// Back-substitution inputs of row i into ring slot i % kRingSlots: -c' (the
+// cached factor, or this sweep's own for the rows [lo, hi] it solved off the
+// cache), the obstacle where it is positive (rows [plo, phi]; 0 elsewhere),
+// d'.
 template <int K>
 __device__ __forceinline__ void issue_bwd(const TileView& V, double* R, int i, int plo, int phi,
-                                          const L2Pol& pol) {
+                                          const L2Pol& pol, int lo, int hi) {
   double* s = R + (i % kRingSlots) * kRingSlot;
   const double* p = V.rp(i);
-  cp_async8(s, p + (K == kStage2 ? A_NC2 : A_NC1) * kTile, pol.first);
+  if (i >= lo && i <= hi)
+    cp_async8(s, p + (K == kStage2 ? A_CP2 : A_CP) * kTile);
+  else
+    cp_async8(s, p + (K == kStage2 ? A_NC2 : A_NC1) * kTile, pol.first);
   if (i >= plo && i <= phi) cp_async8(s + kTile, p + A_PSI * kTile, pol.first);
   cp_async8(s + 2 * kTile, p + A_D * kTile, pol.last);
 }
@@ -495,7 +500,7 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
   double xnext = dmax_ref(bcr, V.at(A_PSI, n - 1));
   const int top = n - 2;  // this lane's first row going down
   for (int j = 0; j < kRing; ++j) {
-    if (top - j >= 1) issue_bwd<K>(V, R, top - j, plo, phi, pol);
+    if (top - j >= 1) issue_bwd<K>(V, R, top - j, plo, phi, pol, lo, hi);
     cp_commit();
   }
   for (int i = top; i >= 1; --i) {
@@ -503,9 +508,9 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
     const double* s = R + (i % kRingSlots) * kRingSlot;
     const double rnc = s[0], rd = s[2 * kTile];
     const double rpsi = (i >= plo && i <= phi) ? s[kTile] : 0.0;
-    if (i - kRing >= 1) issue_bwd<K>(V, R, i - kRing, plo, phi, pol);
+    if (i - kRing >= 1) issue_bwd<K>(V, R, i - kRing, plo, phi, pol, lo, hi);
     cp_commit();
-    const double nc = (i >= lo && i <= hi) ? V.at(K == kStage2 ? A_CP2 : A_CP, i) : rnc;
+    const double nc = rnc;  // the ring holds the right -c' for this row
     const double xv = proj_max(fma(nc, xnext, rd), rpsi);
     V.at(a_out, i) = xv;
     xnext = xv;

@@ -254,19 +254,22 @@ __device__ __forceinline__ void issue_fwd_t(const TileView& V, const TanView<ND>
 }
 
 // Back-substitution inputs of row i: -c', psi, d', then per direction the
-// cached -c' derivative and the tangent d'.
+// -c' derivative and the tangent d'.  For the rows [lo, hi] this sweep solved
+// off the cache, -c' and its derivatives are the sweep's own (A_CP, T_CP)
+// rather than the cached ones.
 template <int K, int ND>
 __device__ __forceinline__ void issue_bwd_t(const TileView& V, const TanView<ND>& W, double* R,
-                                            int i) {
+                                            int i, int lo, int hi) {
   using RG = TanRing<ND>;
   double* s = R + (i % RG::kSlots) * RG::kSlot;
   const double* p = V.rp(i);
-  cp_async8(s, p + (K == kStage2 ? A_NC2 : A_NC1) * kTile);
+  const bool off = i >= lo && i <= hi;
+  cp_async8(s, p + (off ? A_CP : (K == kStage2 ? A_NC2 : A_NC1)) * kTile);
   cp_async8(s + kTile, p + A_PSI * kTile);
   cp_async8(s + 2 * kTile, p + A_D * kTile);
 #pragma unroll
   for (int j = 0; j < ND; ++j) {
-    cp_async8(s + (3 + 2 * j) * kTile, &W.at(j, K == kStage2 ? T_NC2 : T_NC1, i));
+    cp_async8(s + (3 + 2 * j) * kTile, &W.at(j, off ? T_CP : (K == kStage2 ? T_NC2 : T_NC1), i));
     cp_async8(s + (4 + 2 * j) * kTile, &W.at(j, T_D, i));
   }
 }
@@ -471,7 +474,7 @@ __device__ __noinline__ int32_t stage_t(bool live, int n, const TileView V, cons
   for (int j = 0; j < ND; ++j) txnext[j] = bcr < psi_last ? 0.0 : tbcr.v[j];
   const int top = n - 2;
   for (int j = 0; j < RG::kAhead; ++j) {
-    if (top - j >= 1) issue_bwd_t<K, ND>(V, W, R, top - j);
+    if (top - j >= 1) issue_bwd_t<K, ND>(V, W, R, top - j, lo, hi);
     cp_commit();
   }
   for (int i = top; i >= 1; --i) {
@@ -484,16 +487,15 @@ __device__ __noinline__ int32_t stage_t(bool live, int n, const TileView V, cons
       rtnc[j] = s[(3 + 2 * j) * kTile];
       rtd[j] = s[(4 + 2 * j) * kTile];
     }
-    if (i - RG::kAhead >= 1) issue_bwd_t<K, ND>(V, W, R, i - RG::kAhead);
+    if (i - RG::kAhead >= 1) issue_bwd_t<K, ND>(V, W, R, i - RG::kAhead, lo, hi);
     cp_commit();
-    const bool off = i >= lo && i <= hi;
-    const double nc = off ? V.at(A_CP, i) : rnc;
+    const double nc = rnc;  // the ring holds the right -c' (and derivatives) for this row
     const double unc = fma(nc, xnext, rd);
     const bool act = binds(unc, rpsi);
     const double xv = act ? rpsi : unc;
 #pragma unroll
     for (int j = 0; j < ND; ++j) {
-      const double tnc = off ? W.at(j, T_CP, i) : rtnc[j];
+      const double tnc = rtnc[j];
       const double tx = act ? 0.0 : fma(nc, txnext[j], fma(tnc, xnext, rtd[j]));
       W.at(j, t_out, i) = tx;
       txnext[j] = tx;

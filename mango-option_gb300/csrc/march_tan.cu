@@ -792,16 +792,26 @@ MangoStatus tan_batch(MangoGpuContext* ctx, const MangoPricingParams* params, ui
   if (n == 0) return MANGO_OK;
   MangoGpuBatch* b = nullptr;
   DevBuf d_tpool, d_tout;
+  // the split three-direction march: two more primal pools, three tangent
+  // pools and outputs, per extra direction its flags, modes and statuses
+  DevBuf d_split[2], d_split_t[3], d_split_o[3], d_split_aux[2][3];
+  cudaEvent_t split_ev[2] = {nullptr, nullptr};
   struct Release {
     MangoGpuBatch** b;
-    DevBuf* t;
-    DevBuf* o;
+    std::vector<DevBuf*> bufs;
+    cudaEvent_t* ev;
     ~Release() {
       if (*b) destroy_batch(*b);
-      t->release();
-      o->release();
+      for (DevBuf* x : bufs) x->release();
+      for (int j = 0; j < 2; ++j)
+        if (ev[j]) cudaEventDestroy(ev[j]);
     }
-  } release{&b, &d_tpool, &d_tout};
+  } release{&b,
+            {&d_tpool, &d_tout, &d_split[0], &d_split[1], &d_split_t[0], &d_split_t[1],
+             &d_split_t[2], &d_split_o[0], &d_split_o[1], &d_split_o[2], &d_split_aux[0][0],
+             &d_split_aux[0][1], &d_split_aux[0][2], &d_split_aux[1][0], &d_split_aux[1][1],
+             &d_split_aux[1][2]},
+            split_ev};
   try {
     check(cudaSetDevice(ctx->device), "cudaSetDevice");
     const int64_t nn = static_cast<int64_t>(n);
@@ -825,6 +835,7 @@ MangoStatus tan_batch(MangoGpuContext* ctx, const MangoPricingParams* params, ui
       }
     });
     b = create_batch_resolved(ctx, params, std::move(res), std::move(msg), nullptr);
+    for (auto& e : split_ev) check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
     const int64_t m = static_cast<int64_t>(b->order.size());
     const int S = tan_out_stride(nd);
     std::vector<double> hout(static_cast<size_t>(m) * S);
@@ -842,18 +853,80 @@ MangoStatus tan_batch(MangoGpuContext* ctx, const MangoPricingParams* params, ui
       tc.dirs[2] = kDirDividend;
       check(cudaMemsetAsync(b->d_queue.p, 0, sizeof(int) * 4, st), "memset queue");
       check(cudaEventRecord(b->ev[2], st), "event");
-      tan_launch(nd, st, ctx->num_sms, b->d_tiles.as<TileDev>(), b->ntiles,
-                 b->d_opts.as<OptDev>(), b->d_xs.as<double>(), b->d_pool.as<double>(), tpool,
-                 b->d_flags.as<uint8_t>(), b->d_mode.as<int32_t>(), b->d_status.as<int32_t>(),
-                 b->d_queue.as<int>(), tc, b->mc, dout);
-      check(cudaEventRecord(b->ev[4], st), "event");
-      check(cudaMemcpyAsync(hout.data(), dout, sizeof(double) * hout.size(),
-                            cudaMemcpyDeviceToHost, st),
-            "D2H tangent results");
-      check(cudaMemcpyAsync(hst.data(), b->d_status.p, sizeof(int32_t) * m,
-                            cudaMemcpyDeviceToHost, st),
-            "D2H status");
-      check(cudaStreamSynchronize(st), "stream synchronize");
+      // A batch whose three single-direction marches still fit one wave of
+      // resident warps runs them side by side on three streams, each with its
+      // own primal pool: the FP64 work grows by a third (the primal is
+      // marched three times), but three times as many warps share the SM
+      // sub-partitions of a launch that one warp per tile leaves
+      // latency-bound (16,384 options: 512 tiles for 608 sub-partitions).
+      const int wave1 = ctx->num_sms * tan_blocks_per_sm<1>() * 2;
+      if (nd == 3 && 3 * b->ntiles <= wave1) {
+        check(cudaEventRecord(b->ev[3], st), "event");
+        cudaStream_t sd[3] = {st, ctx->aux[0], ctx->aux[1]};
+        const size_t pool_bytes = sizeof(double) * static_cast<size_t>(pool_doubles);
+        double* pools[3] = {b->d_pool.as<double>(), static_cast<double*>(d_split[0].get(pool_bytes)),
+                            static_cast<double*>(d_split[1].get(pool_bytes))};
+        const size_t t1 = sizeof(double) * static_cast<size_t>(tan_pool_doubles(1, pool_doubles));
+        const size_t nflags = b->d_flags.cap;
+        const size_t o1 = sizeof(double) * static_cast<size_t>(m) * tan_out_stride(1);
+        for (int d = 0; d < 3; ++d) {
+          if (d > 0) check(cudaStreamWaitEvent(sd[d], b->ev[3], 0), "stream wait");
+          TanConst td{};
+          td.dirs[0] = tc.dirs[d];
+          uint8_t* fl = d == 0 ? b->d_flags.as<uint8_t>()
+                               : static_cast<uint8_t*>(d_split_aux[d - 1][0].get(nflags));
+          int32_t* md = d == 0 ? b->d_mode.as<int32_t>()
+                               : static_cast<int32_t*>(d_split_aux[d - 1][1].get(sizeof(int32_t) * m));
+          int32_t* sts = d == 0 ? b->d_status.as<int32_t>()
+                                : static_cast<int32_t*>(d_split_aux[d - 1][2].get(sizeof(int32_t) * m));
+          tan_launch(1, sd[d], ctx->num_sms, b->d_tiles.as<TileDev>(), b->ntiles,
+                     b->d_opts.as<OptDev>(), b->d_xs.as<double>(), pools[d],
+                     static_cast<double*>(d_split_t[d].get(t1)), fl, md, sts,
+                     b->d_queue.as<int>() + d, td, b->mc,
+                     static_cast<double*>(d_split_o[d].get(o1)));
+          if (d > 0) {
+            check(cudaEventRecord(split_ev[d - 1], sd[d]), "event");
+            check(cudaStreamWaitEvent(st, split_ev[d - 1], 0), "stream wait");
+          }
+        }
+        check(cudaEventRecord(b->ev[4], st), "event");
+        std::vector<double> h1(static_cast<size_t>(m) * tan_out_stride(1));
+        std::vector<int32_t> hs(static_cast<size_t>(m));
+        for (int d = 0; d < 3; ++d) {
+          check(cudaMemcpyAsync(h1.data(), d_split_o[d].p, o1, cudaMemcpyDeviceToHost, st),
+                "D2H tangent results");
+          const void* src = d == 0 ? b->d_status.p : d_split_aux[d - 1][2].p;
+          check(cudaMemcpyAsync(hs.data(), src, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, st),
+                "D2H status");
+          check(cudaStreamSynchronize(st), "stream synchronize");
+          for (int64_t k = 0; k < m; ++k) {
+            const double* h = h1.data() + static_cast<size_t>(k) * tan_out_stride(1);
+            double* o = hout.data() + static_cast<size_t>(k) * S;
+            if (d == 0) {
+              o[0] = h[0];  // value, delta, dV/dK from the volatility march
+              o[1] = h[1];
+              o[2] = h[2];
+              hst[k] = hs[k];
+            } else if (hst[k] == kStatusOk) {
+              hst[k] = hs[k];
+            }
+            o[3 + d] = h[3];
+          }
+        }
+      } else {
+        tan_launch(nd, st, ctx->num_sms, b->d_tiles.as<TileDev>(), b->ntiles,
+                   b->d_opts.as<OptDev>(), b->d_xs.as<double>(), b->d_pool.as<double>(), tpool,
+                   b->d_flags.as<uint8_t>(), b->d_mode.as<int32_t>(), b->d_status.as<int32_t>(),
+                   b->d_queue.as<int>(), tc, b->mc, dout);
+        check(cudaEventRecord(b->ev[4], st), "event");
+        check(cudaMemcpyAsync(hout.data(), dout, sizeof(double) * hout.size(),
+                              cudaMemcpyDeviceToHost, st),
+              "D2H tangent results");
+        check(cudaMemcpyAsync(hst.data(), b->d_status.p, sizeof(int32_t) * m,
+                              cudaMemcpyDeviceToHost, st),
+              "D2H status");
+        check(cudaStreamSynchronize(st), "stream synchronize");
+      }
     }
     const double nan = std::nan("");
     uint64_t failed = 0;
@@ -892,7 +965,7 @@ MangoStatus tan_batch(MangoGpuContext* ctx, const MangoPricingParams* params, ui
     S2.options = nn;
     S2.tiles = b->ntiles;
     S2.host_prep_ms = b->host_prep_ms;
-    S2.kernel_launches = m > 0 ? 4 : 0;
+    S2.kernel_launches = m > 0 ? (nd == 3 && 3 * b->ntiles <= ctx->num_sms * tan_blocks_per_sm<1>() * 2 ? 12 : 4) : 0;
     if (out_failed) *out_failed = failed;
     if (failed == n) {
       set_err(err, MANGO_ERR_VALIDATION, "every option failed: " + first);

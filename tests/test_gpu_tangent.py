@@ -137,3 +137,20 @@ def test_tangent_vs_reference_frozen_grid_differences(engine, pkg):
     fd = engine.greeks_arrays(params, grid, 1e-5)
     for k in ("vega", "rho", "dividend_rho", "dstrike"):
         assert np.allclose(fd[k], g[k][0], rtol=1e-5, atol=1e-6), (k, np.abs(fd[k] - g[k][0]).max())
+
+
+def test_large_batch_single_launch_matches_split_marches(engine, pkg):
+    """A three-direction batch small enough to fit one wave runs as three
+    single-direction marches side by side; a large one (40,000 options) as
+    one three-direction march.  Both are the same differentiation of the
+    same march: the first 512 options agree to rounding (value and delta
+    1e-12 relative, the sensitivities 1e-10)."""
+    params = inputs(pkg, 40000, 11, True)
+    grid = pkg.grid_array(1, pkg.GRID_FIXED_N, 101, 498)
+    big = engine.tangent_arrays(params, grid)
+    small = engine.tangent_arrays(params[:512], grid)
+    assert (big["status"] == 0).all() and (small["status"] == 0).all()
+    for k in ("value", "delta"):
+        assert np.allclose(big[k][:512], small[k], rtol=1e-12, atol=1e-14), k
+    for k in ("vega", "rho", "dividend_rho", "dstrike"):
+        assert np.allclose(big[k][:512], small[k], rtol=1e-10, atol=1e-12), (k, np.abs(big[k][:512] - small[k]).max())

@@ -12,8 +12,11 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <memory>
+#include <queue>
 #include <thread>
+#include <utility>
 
 namespace mgpu {
 
@@ -282,7 +285,8 @@ void destroy_batch(MangoGpuBatch* b) {
   if (!b) return;
   for (mgpu::DevBuf* d : {&b->d_pool, &b->d_xs, &b->d_flags, &b->d_opts, &b->d_tiles, &b->d_mode,
                           &b->d_status, &b->d_out4, &b->d_queue, &b->d_tv, &b->d_tv_tp,
-                          &b->d_tv_curve, &b->d_tv_ev, &b->d_wt, &b->d_tile_warp})
+                          &b->d_tv_curve, &b->d_tv_ev, &b->d_wt, &b->d_tile_warp, &b->d_bins,
+                          &b->d_bin_cnt, &b->d_tile_done})
     d->release();
   for (mgpu::HostBuf* h : {&b->h_xs, &b->h_opts, &b->h_tiles, &b->h_out4, &b->h_status})
     h->release();
@@ -356,6 +360,7 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
   b->tv_tile0 = 0;
   b->wplan_ready = false;
   b->nwt = 0;
+  b->nbins = 0;
   b->ran = false;
   b->runs = 0;
   for (auto& e : b->ev)
@@ -611,6 +616,44 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
   return b.release();
 }
 
+namespace {
+
+__global__ void smid_probe_kernel(int* seen, int cap) {
+  unsigned smid;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+  if (threadIdx.x == 0 && smid < static_cast<unsigned>(cap)) seen[smid] = 1;
+}
+
+// The dense SM index of every %smid value, from a launch of eight blocks per
+// SM; left unset (nsmid = 0) unless exactly num_sms distinct ids were seen.
+void probe_sm_index(MangoGpuContext* ctx, cudaStream_t st) {
+  ctx->sm_probed = true;
+  constexpr int kCap = 1024;
+  DevBuf d;
+  int* seen = static_cast<int*>(d.get(sizeof(int) * kCap));
+  check(cudaMemsetAsync(seen, 0, sizeof(int) * kCap, st), "memset smid probe");
+  smid_probe_kernel<<<ctx->num_sms * 8, 32, 0, st>>>(seen, kCap);
+  check(cudaGetLastError(), "smid probe launch");
+  std::vector<int> h(kCap);
+  check(cudaMemcpyAsync(h.data(), seen, sizeof(int) * kCap, cudaMemcpyDeviceToHost, st), "D2H");
+  check(cudaStreamSynchronize(st), "stream synchronize");
+  d.release();
+  std::vector<int32_t> index(kCap, -1);
+  int count = 0, top = 0;
+  for (int i = 0; i < kCap; ++i)
+    if (h[i]) {
+      index[i] = count++;
+      top = i + 1;
+    }
+  if (count != ctx->num_sms) return;
+  check(cudaMemcpyAsync(ctx->d_sm_index.get(sizeof(int32_t) * top), index.data(),
+                        sizeof(int32_t) * top, cudaMemcpyHostToDevice, st),
+        "H2D SM index");  // pageable source: staged before the call returns
+  ctx->nsmid = top;
+}
+
+}  // namespace
+
 // Enqueue setup, march and outputs for a created batch.
 void run_batch(MangoGpuBatch* b) {
   MangoGpuContext* ctx = b->ctx;
@@ -657,6 +700,63 @@ void run_batch(MangoGpuBatch* b) {
                             static_cast<size_t>(ntiles), cudaMemcpyHostToDevice, st),
             "H2D warp flags");
     }
+    // Uneven batches (the costliest tile above 1.5x the mean; cost: rows x
+    // steps of the tile's widest and longest lane): the thread march's tiles
+    // go to one list per SM sub-partition, longest first to the least-loaded
+    // list.  A warp's FP64 issue is shared with the other warps of its
+    // sub-partition, and every warp of a 65,536-option batch holds one tile
+    // for the whole launch, so which tiles share a sub-partition sets the
+    // launch's length; the lists give the costliest tiles a sub-partition to
+    // themselves.  MANGO_GPU_BINS=0 turns this off.
+    b->nbins = 0;
+    bool bins_on = true;
+    if (const char* e = std::getenv("MANGO_GPU_BINS")) bins_on = std::atoi(e) != 0;
+    const int nbins = 4 * ctx->num_sms;
+    std::vector<int32_t> mt;
+    for (int t = 0; t < tv0; ++t)
+      if (b->nwt == 0 || !plan.flag[t]) mt.push_back(t);
+    const TileDev* th = b->h_tiles.as<TileDev>();
+    auto cost = [&](int32_t t) {
+      return static_cast<double>(std::max(th[t].nx - 2, 1)) * static_cast<double>(th[t].nt);
+    };
+    double csum = 0.0, cmax = 0.0;
+    for (int32_t t : mt) {
+      csum += cost(t);
+      cmax = std::max(cmax, cost(t));
+    }
+    const bool uneven = !mt.empty() && cmax > 1.5 * csum / static_cast<double>(mt.size());
+    if (bins_on && uneven && static_cast<int64_t>(mt.size()) >= nbins) {
+      if (!ctx->sm_probed) probe_sm_index(ctx, st);
+      if (ctx->nsmid > 0) {
+        std::stable_sort(mt.begin(), mt.end(),
+                         [&](int32_t a, int32_t c) { return cost(a) > cost(c); });
+        std::vector<std::vector<int32_t>> lists(static_cast<size_t>(nbins));
+        using Load = std::pair<double, int>;
+        std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
+        for (int j = 0; j < nbins; ++j) heap.push({0.0, j});
+        for (int32_t t : mt) {
+          Load l = heap.top();
+          heap.pop();
+          lists[static_cast<size_t>(l.second)].push_back(t);
+          l.first += cost(t);
+          heap.push(l);
+        }
+        std::vector<int32_t> packed(static_cast<size_t>(nbins) + 1 + mt.size());
+        int32_t off = 0;
+        for (int j = 0; j < nbins; ++j) {
+          packed[static_cast<size_t>(j)] = off;
+          for (int32_t t : lists[static_cast<size_t>(j)])
+            packed[static_cast<size_t>(nbins) + 1 + static_cast<size_t>(off++)] = t;
+        }
+        packed[static_cast<size_t>(nbins)] = off;
+        check(cudaMemcpyAsync(b->d_bins.get(sizeof(int32_t) * packed.size()), packed.data(),
+                              sizeof(int32_t) * packed.size(), cudaMemcpyHostToDevice, st),
+              "H2D tile lists");  // pageable source: staged before the call returns
+        b->d_bin_cnt.get(sizeof(int) * static_cast<size_t>(nbins));
+        b->d_tile_done.get(static_cast<size_t>(ntiles));
+        b->nbins = nbins;
+      }
+    }
     b->wplan_ready = true;
   }
   MarchConst mc = b->mc;
@@ -683,6 +783,24 @@ void run_batch(MangoGpuBatch* b) {
     wmarch_launch(b->wstream, ctx->num_sms, d_tiles, b->d_wt.as<int32_t>(), b->nwt, d_opts, d_pool,
                   d_flags, d_mode, d_status, b->d_queue.as<int>() + 1, mc, b->wR, b->wblocks);
     check(cudaEventRecord(b->wev[1], b->wstream), "event");
+  }
+  if (b->nwt < ntiles && b->nbins > 0) {
+    // the binned launch, then one over the queue for any tile left untaken
+    check(cudaMemsetAsync(b->d_bin_cnt.p, 0, sizeof(int) * static_cast<size_t>(b->nbins), st),
+          "memset tile lists");
+    check(cudaMemsetAsync(b->d_tile_done.p, 0, static_cast<size_t>(ntiles), st), "memset taken");
+    MarchConst mb = mc;
+    mb.bin_off = b->d_bins.as<int32_t>();
+    mb.bin_tiles = mb.bin_off + b->nbins + 1;
+    mb.bin_cnt = b->d_bin_cnt.as<int>();
+    mb.sm_index = ctx->d_sm_index.as<int32_t>();
+    mb.nsmid = ctx->nsmid;
+    mb.nbins = b->nbins;
+    mb.tile_done = b->d_tile_done.as<uint8_t>();
+    march_kernel<<<ctx->num_sms * bps, 32 * warps_per_block, 0, st>>>(
+        d_tiles, ntiles, d_opts, d_pool, d_flags, d_mode, d_status, b->d_queue.as<int>(), mb);
+    check(cudaGetLastError(), "march_kernel launch");
+    mc.tile_done = b->d_tile_done.as<uint8_t>();
   }
   if (b->nwt < ntiles)
     march_kernel<<<blocks, 32 * warps_per_block, 0, st>>>(d_tiles, ntiles, d_opts, d_pool,
@@ -762,6 +880,7 @@ uint64_t fetch_batch(MangoGpuBatch* b, MangoGpuAmericanOut* out, std::string* fi
   S.h2d_bytes = b->h2d_bytes;
   S.host_prep_ms = b->host_prep_ms;
   S.kernel_launches = m > 0 ? (2 + (b->nwt < b->ntiles ? 1 : 0) + (b->nwt > 0 ? 1 : 0) +
+                               (b->nbins > 0 && b->nwt < b->ntiles ? 1 : 0) +
                                (b->mc.tv_first < m ? 1 : 0))
                             : 0;
   return failed;
@@ -827,6 +946,7 @@ void mango_gpu_context_destroy(MangoGpuContext* ctx) {
     if (ctx->aux[c]) cudaStreamDestroy(ctx->aux[c]);
   }
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  ctx->d_sm_index.release();
   delete ctx;
 }
 

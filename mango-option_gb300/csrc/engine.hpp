@@ -161,6 +161,12 @@ struct MangoGpuContext {
   // preparation of a chunk overlaps the device work of the one before.
   cudaStream_t aux[2] = {nullptr, nullptr};
   MangoGpuBatch* chunk[2] = {nullptr, nullptr};
+  // %smid -> dense SM index (-1: not an SM of this device), probed on first
+  // use by a binned launch; nsmid = 0 until then, or when the probe did not
+  // see every SM.
+  mgpu::DevBuf d_sm_index;
+  int nsmid = 0;
+  bool sm_probed = false;
 };
 
 struct MangoGpuBatch {
@@ -187,6 +193,11 @@ struct MangoGpuBatch {
   cudaStream_t wstream = nullptr;       // its stream, created on first use
   cudaEvent_t wev[2] = {nullptr, nullptr};
   mgpu::DevBuf d_wt, d_tile_warp;
+  // Thread-march tiles of an uneven batch assigned to SM sub-partitions
+  // (planned with the warp tiles): list offsets then tiles, the list
+  // counters, and the per-tile taken flags of the binned launch.
+  int32_t nbins = 0;
+  mgpu::DevBuf d_bins, d_bin_cnt, d_tile_done;
   mgpu::HostBuf h_xs, h_opts, h_tiles, h_out4, h_status;
   cudaEvent_t ev[8] = {};
   bool ran = false;

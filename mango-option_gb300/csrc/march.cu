@@ -535,11 +535,31 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
     MarchConst mc) {
   const int lane = threadIdx.x & (kTile - 1);
   __shared__ double ring[4][kRingSlots * kRingSlot];  // one ring per warp (128 threads)
+  int my_bin = -1;  // this warp's tile list in a binned launch
+  if (mc.nbins > 0) {
+    unsigned smid, wslot;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    asm volatile("mov.u32 %0, %%warpid;" : "=r"(wslot));
+    const int sm = smid < static_cast<unsigned>(mc.nsmid) ? mc.sm_index[smid] : -1;
+    if (sm >= 0 && sm * 4 + 3 < mc.nbins) my_bin = sm * 4 + static_cast<int>(wslot & 3u);
+  }
   for (;;) {
     int t = 0;
-    if (lane == 0) t = atomicAdd(queue, 1);
+    if (lane == 0) {
+      if (mc.nbins > 0) {
+        t = -1;
+        if (my_bin >= 0) {
+          const int k = atomicAdd(&mc.bin_cnt[my_bin], 1);
+          if (k < mc.bin_off[my_bin + 1] - mc.bin_off[my_bin]) t = mc.bin_tiles[mc.bin_off[my_bin] + k];
+        }
+        if (t >= 0) mc.tile_done[t] = 1;
+      } else {
+        t = atomicAdd(queue, 1);
+      }
+    }
     t = __shfl_sync(0xffffffffu, t, 0);
-    if (t >= ntiles) break;
+    if (t < 0 || t >= ntiles) break;
+    if (mc.nbins == 0 && mc.tile_done && mc.tile_done[t]) continue;  // taken by the binned launch
     if (mc.tile_warp && mc.tile_warp[t]) continue;  // marched one warp per option
     const TileDev td = tiles[t];
     const int k = td.first + lane;

@@ -94,6 +94,18 @@ struct MarchConst {
   // first pivot is exactly 0 and the solve reports kStatusSolver as a
   // singular Thomas pivot does; -1 = none.
   int32_t singular_pivot = -1;
+  // Tiles assigned to SM sub-partitions (uneven batches), or nbins = 0.  A
+  // warp of the binned launch takes the tiles of list (SM index x 4 + warp
+  // slot mod 4) in order, marks each in tile_done, and leaves when its list
+  // is empty; a second launch (tile_done set, nbins = 0) marches whatever
+  // tile no warp took.
+  const int32_t* bin_off = nullptr;   // nbins + 1 offsets into bin_tiles
+  const int32_t* bin_tiles = nullptr;
+  int* bin_cnt = nullptr;             // per list, tiles taken so far
+  const int32_t* sm_index = nullptr;  // %smid -> dense SM index, -1: none
+  int32_t nsmid = 0;                  // entries of sm_index
+  int32_t nbins = 0;
+  uint8_t* tile_done = nullptr;
 };
 
 // Per-option data of the time-varying march, indexed by sorted index minus

@@ -85,3 +85,26 @@ def test_warp_matches_thread_layout(engine, pkg, monkeypatch):
     a, b = greeks(outs["1"]), greeks(outs["0"])
     check(a[:, :3], b[:, :3], rtol=1e-11, atol=1e-13)
     check(a[:, 3], b[:, 3], rtol=1e-9, atol=1e-11)
+
+
+def test_uneven_batch_binned_equals_single_queue(engine, pkg, monkeypatch):
+    """An uneven batch (N_x ~ U{51..401}, N_t ~ U{100..1000}; 24,576 options,
+    768 tiles) has its thread-march tiles assigned to SM sub-partitions, then
+    a second launch marches anything left.  Which warp marches a tile changes
+    nothing: results equal the single-queue launch (MANGO_GPU_BINS=0) bit for
+    bit, with and without the warp march for the long poles."""
+    n = 24576
+    rng = np.random.default_rng(31)
+    p = pkg.pricing_array(np.full(n, 100.0), rng.uniform(80, 120, n), rng.uniform(0.1, 2.0, n),
+                          rng.uniform(0.1, 0.5, n), rng.uniform(0.0, 0.08, n),
+                          rng.uniform(0.0, 0.04, n), (np.arange(n) % 2 == 0).astype(np.int32))
+    g = pkg.grid_array(n, pkg.GRID_FIXED_N, rng.integers(51, 402, n), rng.integers(100, 1001, n))
+    for long_poles in ("0", "1216"):
+        monkeypatch.setenv("MANGO_GPU_WARP_LONG", long_poles)
+        monkeypatch.setenv("MANGO_GPU_BINS", "1")
+        binned = engine.price_arrays(p, g)
+        monkeypatch.setenv("MANGO_GPU_BINS", "0")
+        queue = engine.price_arrays(p, g)
+        assert (binned["status"] == 0).all() and (queue["status"] == 0).all()
+        for k in ("value", "delta", "gamma", "theta"):
+            assert np.array_equal(binned[k], queue[k]), (long_poles, k)

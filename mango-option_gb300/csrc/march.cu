@@ -466,8 +466,8 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
     }
     double dcur;
     if (!lock && !fresh) {
-      if (K == kStage1)
-        dcur = fma(rnl, dprev + um, fma(ra, u0, rc * rv));
+      if (K == kStage1)  // d'_{i-1} enters last: one FP64 operation on the serial chain
+        dcur = fma(rnl, dprev, fma(rnl, um, fma(ra, u0, rc * rv)));
       else
         dcur = fma(rnl, dprev, ra * fma(beta_alpha, rv, g));
     } else {

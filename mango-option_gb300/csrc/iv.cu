@@ -1109,10 +1109,14 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
           } else {
             const int blocks = std::max(
                 1, std::min<int>(ctx->num_sms * ctx->march_blocks_per_sm, (ntiles + 3) / 4));
-            // few points left: one warp per option (wmarch.cu)
+            // few points left: one warp per option (wmarch.cu).  A tail
+            // round's thread march was measured at about twice the time of a
+            // pricing batch of its size (trial volatilities far from the
+            // grid's slow some lanes, and a tile waits for its slowest), so
+            // its estimate counts double.
             const WarpPlan plan = plan_warp_tiles(
                 w.tiles_h.data(), ntiles, w.tv_first < w.mw ? w.tv_first / kTile : ntiles,
-                ctx->num_sms);
+                ctx->num_sms, static_cast<int64_t>(active.size()) <= kTailQuotes ? 2.0 : 1.0);
             const int nwt = static_cast<int>(plan.tiles.size());
             if (nwt > 0) {
               check(cudaMemcpyAsync(w.d_wt.get(sizeof(int32_t) * nwt), plan.tiles.data(),

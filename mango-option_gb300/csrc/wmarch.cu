@@ -623,7 +623,8 @@ void wmarch_launch(void* stream, int num_sms, const TileDev* tiles, const int32_
   check(cudaGetLastError(), "wmarch_kernel launch");
 }
 
-WarpPlan plan_warp_tiles(const TileDev* tiles, int ntiles, int tv_tile0, int num_sms) {
+WarpPlan plan_warp_tiles(const TileDev* tiles, int ntiles, int tv_tile0, int num_sms,
+                         double thread_scale) {
   WarpPlan plan;
   plan.flag.assign(static_cast<size_t>(std::max(ntiles, 0)), 0);
   int force = -1;
@@ -663,8 +664,8 @@ WarpPlan plan_warp_tiles(const TileDev* tiles, int ntiles, int tv_tile0, int num
     }
   const double waves = static_cast<double>((options + wave - 1) / wave);
   const double warp_us = steps * (kWarpStepUs + kWarpStepUsPerR * R) * waves;
-  const double thread_us =
-      steps * std::max(rows * kThreadRowUs, static_cast<double>(last) * rows * kThreadRowTileUs);
+  const double thread_us = thread_scale * steps *
+                           std::max(rows * kThreadRowUs, static_cast<double>(last) * rows * kThreadRowTileUs);
   if (force == 1 || warp_us < thread_us) {
     for (int t = 0; t < last; ++t)
       if (wmarch_rows_per_lane(tiles[t].nx) <= rmax) {

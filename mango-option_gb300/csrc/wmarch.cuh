@@ -44,6 +44,10 @@ struct WarpPlan {
   bool concurrent = false;     // a subset beside the thread march
   int blocks = 0;              // warp-march blocks (0: by occupancy)
 };
-WarpPlan plan_warp_tiles(const TileDev* tiles, int ntiles, int tv_tile0, int num_sms);
+// thread_scale multiplies the thread march's estimate: 1 for a batch sorted
+// by the pricing pipeline, more for working sets whose lanes march slower
+// than the model's (the tail of a batched IV).
+WarpPlan plan_warp_tiles(const TileDev* tiles, int ntiles, int tv_tile0, int num_sms,
+                         double thread_scale = 1.0);
 
 }  // namespace mgpu

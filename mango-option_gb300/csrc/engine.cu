@@ -945,6 +945,8 @@ void mango_gpu_context_destroy(MangoGpuContext* ctx) {
     if (ctx->chunk[c]) destroy_batch(ctx->chunk[c]);
     if (ctx->aux[c]) cudaStreamDestroy(ctx->aux[c]);
   }
+  if (ctx->table_batch) destroy_batch(ctx->table_batch);
+  for (auto& d : ctx->table_buf) d.release();
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   ctx->d_sm_index.release();
   delete ctx;

@@ -167,6 +167,11 @@ struct MangoGpuContext {
   mgpu::DevBuf d_sm_index;
   int nsmid = 0;
   bool sm_probed = false;
+  // The price-table sweep's batch and snapshot buffers, kept for the next
+  // sweep (a table build calls it once; a caller sweeping repeatedly would
+  // otherwise pay some twenty device allocations per call).
+  MangoGpuBatch* table_batch = nullptr;
+  mgpu::DevBuf table_buf[8];
 };
 
 struct MangoGpuBatch {

@@ -215,13 +215,19 @@ uint64_t table_sweep_device(MangoGpuContext* ctx, const double* moneyness, uint6
                             uint64_t nsig, const double* rate, uint64_t nr, double K_ref,
                             double dividend_yield, MangoOptionType option_type,
                             const MangoGpuGrid* grid, double* dten, int64_t* slice_dims) {
+  // The batch is the context's, refilled call after call; an exception
+  // leaves it in an unknown state, so it is dropped then.
   MangoGpuBatch* b = nullptr;
   struct Guard {
+    MangoGpuContext* ctx;
     MangoGpuBatch** b;
+    bool ok = false;
     ~Guard() {
-      if (*b) destroy_batch(*b);
+      if (ok || !*b) return;
+      destroy_batch(*b);
+      if (ctx->table_batch == *b) ctx->table_batch = nullptr;
     }
-  } guard{&b};
+  } guard{ctx, &b};
   {
     check(cudaSetDevice(ctx->device), "cudaSetDevice");
     const double T = maturity[ntau - 1];
@@ -317,7 +323,9 @@ uint64_t table_sweep_device(MangoGpuContext* ctx, const double* moneyness, uint6
       if (spec[s].n < 3 || nts[s] < 1) res[s].status = MANGO_ERR_VALIDATION;
     }
     b = create_batch_resolved(ctx, pp.data(), std::move(res),
-                              std::vector<std::string>(static_cast<size_t>(ns)), nullptr);
+                              std::vector<std::string>(static_cast<size_t>(ns)), nullptr,
+                              ctx->table_batch);
+    ctx->table_batch = b;
     const int64_t m = static_cast<int64_t>(b->order.size());
     // Snapshot indices per slice: convert_times_to_indices (grid.hpp:627-700),
     // uniform time points, sorted and de-duplicated.
@@ -351,7 +359,14 @@ uint64_t table_sweep_device(MangoGpuContext* ctx, const double* moneyness, uint6
     uint64_t failed = 0;
     if (m > 0) {
       cudaStream_t st = ctx->stream;
-      DevBuf d_sidx, d_sbegin, d_scount, d_soff, d_snaps, d_slice, d_m, d_scratch;
+      DevBuf& d_sidx = ctx->table_buf[0];
+      DevBuf& d_sbegin = ctx->table_buf[1];
+      DevBuf& d_scount = ctx->table_buf[2];
+      DevBuf& d_soff = ctx->table_buf[3];
+      DevBuf& d_snaps = ctx->table_buf[4];
+      DevBuf& d_slice = ctx->table_buf[5];
+      DevBuf& d_m = ctx->table_buf[6];
+      DevBuf& d_scratch = ctx->table_buf[7];
       int32_t* dsidx = static_cast<int32_t*>(d_sidx.get(sizeof(int32_t) * std::max<size_t>(sidx.size(), 1)));
       int32_t* dsb = static_cast<int32_t*>(d_sbegin.get(sizeof(int32_t) * m));
       int32_t* dsc = static_cast<int32_t*>(d_scount.get(sizeof(int32_t) * m));
@@ -399,8 +414,6 @@ uint64_t table_sweep_device(MangoGpuContext* ctx, const double* moneyness, uint6
       cudaGetLastError();
       S.options = m;
       S.tiles = b->ntiles;
-      for (DevBuf* d : {&d_sidx, &d_sbegin, &d_scount, &d_soff, &d_snaps, &d_slice, &d_m, &d_scratch})
-        d->release();
     }
     if (m == 0)  // no slice reached the device: every tensor entry is NaN
       check(cudaMemsetAsync(dten, 0xFF, sizeof(double) * nm * ntau * nsig * nr, ctx->stream),
@@ -411,6 +424,7 @@ uint64_t table_sweep_device(MangoGpuContext* ctx, const double* moneyness, uint6
         slice_dims[2 * s] = b->res[s].status == 0 ? b->res[s].spec.n : -1;
         slice_dims[2 * s + 1] = b->res[s].status == 0 ? b->res[s].nt : -1;
       }
+    guard.ok = true;
     return failed;
   }
 }

@@ -88,9 +88,16 @@ __global__ void prep_kernel(const TileDev* __restrict__ tiles, int ntiles,
   int32_t md = uniform ? 2 : 0;
   double cp1 = 0.0, cp2 = 0.0;  // cached factor recurrences; row 0: c'_0 = 0/1
   for (int i = 0; i < td.nx; ++i) F[static_cast<size_t>(i) * kTile] = 0;
+  // Spacing reciprocals, shared by the explicit operator and the Jacobian:
+  // 1/dx_{i-1/2} carries over from the previous row's 1/dx_{i+1/2}, so a row
+  // takes three divisions besides its two pivots (the reference's formulas
+  // divide eleven times; the products here differ from them by rounding).
+  double li = 1.0 / (x(1) - x(0));
   for (int i = 1; i < n - 1; ++i) {
     const double xl = x(i - 1), xi = x(i), xr = x(i + 1);
     const double pl = V.at(A_PSI, i - 1), pi = V.at(A_PSI, i), pr = V.at(A_PSI, i + 1);
+    const double dl = xi - xl, dr = xr - xi;  // grid.hpp:552-565
+    const double ri = 1.0 / dr, ci = 1.0 / (0.5 * (dl + dr)), si = 1.0 / (dl + dr);
     // Explicit operator L(u)_i = A u_{i-1} + Bc u_i + C u_{i+1}; L(psi)_i in
     // the reference's apply order for the lock test's sign.
     double A, Bc, C, lpsi;
@@ -102,10 +109,7 @@ __global__ void prep_kernel(const TileDev* __restrict__ tiles, int ntiles,
       const double d1 = (pr - pl) * u_hdx;
       lpsi = hss * d2 + drift * d1 - rate * pi;
     } else {
-      const double dl = xi - xl, dr = xr - xi;  // grid.hpp:552-565
-      const double dc = 0.5 * (dl + dr);
-      const double li = 1.0 / dl, ri = 1.0 / dr, ci = 1.0 / dc;
-      const double wl = dr / (dl + dr), wrr = dl / (dl + dr);
+      const double wl = dr * si, wrr = dl * si;
       A = hss * (li * ci) - drift * (wl * li);
       Bc = -hss * ((ri + li) * ci) + drift * (wl * li - wrr * ri) - rate;
       C = hss * (ri * ci) + drift * (wrr * ri);
@@ -125,17 +129,16 @@ __global__ void prep_kernel(const TileDev* __restrict__ tiles, int ntiles,
     r[A_E1D0 * kTile] = ed;
     r[A_E1U0 * kTile] = eu;
 
-    // assemble_jacobian (spatial_operator.hpp:123-163).
+    // assemble_jacobian (spatial_operator.hpp:123-163): hss / (dxl dxa),
+    // -hss (1/dxl + 1/dxr) / dxa, hss / (dxr dxa), -b dxr / (dxl (dxl + dxr)),
+    // b (dxr - dxl) / (dxl dxr), b dxl / (dxr (dxl + dxr)).
     const double b_coef = rate - o.q - hss;
-    const double dxl = xi - xl, dxr = xr - xi;
-    const double dxa = (dxl + dxr) / 2.0;
-    const double d2m = hss / (dxl * dxa);
-    const double d2i = -hss * (1.0 / dxl + 1.0 / dxr) / dxa;
-    const double d2p = hss / (dxr * dxa);
-    const double d1d = dxl + dxr;
-    const double d1m = -b_coef * dxr / (dxl * d1d);
-    const double d1i = b_coef * (dxr - dxl) / (dxl * dxr);
-    const double d1p = b_coef * dxl / (dxr * d1d);
+    const double d2m = hss * (li * ci);
+    const double d2i = -hss * ((li + ri) * ci);
+    const double d2p = hss * (ri * ci);
+    const double d1m = -b_coef * (dr * (li * si));
+    const double d1i = b_coef * ((dr - dl) * (li * ri));
+    const double d1p = b_coef * (dl * (ri * si));
     const double jl = d2m + d1m;
     const double jd = d2i + d1i + (-rate);
     const double ju = d2p + d1p;
@@ -170,6 +173,7 @@ __global__ void prep_kernel(const TileDev* __restrict__ tiles, int ntiles,
     r[A_A2H * kTile] = mc.alpha * inv2;
     r[A_B2H * kTile] = mc.beta * inv2;
     r[A_N2H * kTile] = -(l2 * inv2);
+    li = ri;
   }
   mode[k] = md;
 

@@ -129,8 +129,6 @@ uint64_t table_sweep_device(MangoGpuContext* ctx, const double* moneyness, uint6
                             double dividend_yield, MangoOptionType option_type,
                             const MangoGpuGrid* grid, double* dten, int64_t* slice_dims);
 // Kernels (march.cu).
-__global__ void grid_kernel(const TileDev*, const GridDev*, double*);
-__global__ void grid_finish_kernel(const TileDev*, int, const GridDev*, double*, OptDev*);
 __global__ void prep_kernel(const TileDev*, int, const OptDev*, const double*, double*, uint8_t*,
                             int32_t*, MarchConst);
 __global__ void march_kernel(const TileDev*, int, const OptDev*, double*, const uint8_t*,
@@ -188,7 +186,7 @@ struct MangoGpuBatch {
   double algo_flops = 0;
   double h2d_bytes = 0;
   double host_prep_ms = 0;
-  mgpu::DevBuf d_pool, d_xs, d_grids, d_flags, d_opts, d_tiles, d_mode, d_status, d_out4, d_queue;
+  mgpu::DevBuf d_pool, d_xs, d_flags, d_opts, d_tiles, d_mode, d_status, d_out4, d_queue;
   // Time-varying options (sorted last, from mc.tv_first): per-option data,
   // explicit time points, yield-curve pairs, dividend-event pairs.
   mgpu::DevBuf d_tv, d_tv_tp, d_tv_curve, d_tv_ev;
@@ -205,7 +203,7 @@ struct MangoGpuBatch {
   // counters, and the per-tile taken flags of the binned launch.
   int32_t nbins = 0;
   mgpu::DevBuf d_bins, d_bin_cnt, d_tile_done;
-  mgpu::HostBuf h_grids, h_opts, h_tiles, h_out4, h_status;
+  mgpu::HostBuf h_xs, h_opts, h_tiles, h_out4, h_status;
   cudaEvent_t ev[8] = {};
   bool ran = false;
   // Per-run kernel timing: 4 events per run (before setup, after setup,

@@ -364,7 +364,9 @@ def bench_iv(pkg, eng, n):
             ("newton", pkg.IV_NEWTON, "Newton on the exact discrete vega of a coarse grid, then the secant "
                                       "on the own grid (3e-6 secant stop), k-section and Brent fallback"))
     for name, method, desc in arms:
-        eng.solve_iv_arrays(quotes[:4096], grids[:4096], method=method)  # warm the buffers
+        # warm the context's buffers with a solve of the same size (steady state of repeated
+        # batches; the first solve of a context also page-locks its staging and allocates)
+        eng.solve_iv_arrays(quotes, grids, method=method)
         t0 = time.perf_counter()
         out = eng.solve_iv_arrays(quotes, grids, method=method)
         t = time.perf_counter() - t0
@@ -387,6 +389,7 @@ def bench_iv(pkg, eng, n):
         res[name] = {
             "method": desc, "value": n / t,
             "unit": "IV/s (end to end through mango_gpu_solve_iv_batch_method)", "seconds": t,
+            "buffers": "warm: one solve of the same batch before the timed one",
             "status_counts": {int(c): int(k) for c, k in zip(codes, counts)},
             "iterations_mean": float(out["iterations"][ok].mean()) if ok.any() else None,
             "excluded_invalid": int(invalid.sum()), "excluded_low_vega": int((~invalid & low_vega).sum()),

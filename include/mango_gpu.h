@@ -288,8 +288,9 @@ enum {
  * brent_tol_abs.  A quote not settled after 4 own-grid evaluations, or whose
  * slope is not positive, goes on with the k-section finder of
  * MANGO_GPU_IV_SECANT inside what Newton has bracketed (settling at |V - P|
- * below 1e-7 times the slope, or a bracket narrower than 1e-7), then Brent
- * from scratch as that finder does.  Quotes with yield curves or discrete
+ * below 1e-7 times the slope, or a bracket narrower than 1e-7, or, where two
+ * points below brent_tol_abs show the objective flat, on the reference's
+ * test), then Brent from scratch as that finder does.  Quotes with yield curves or discrete
  * dividends use the secant path.  iterations = coarse plus own-grid
  * evaluations for Newton-settled quotes; final_error = |V - P| at the last
  * evaluated point; has_vega = 1 and vega = the slope of that last secant

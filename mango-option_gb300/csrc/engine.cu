@@ -583,14 +583,16 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
 
   if (m > 0) {
     cudaStream_t st = b->stream;
-    b->d_pool.get(sizeof(double) * off);
     double* d_xs = static_cast<double*>(b->d_xs.get(sizeof(double) * xoff));
-    b->d_flags.get(static_cast<size_t>(foff));
     OptDev* d_opts = static_cast<OptDev*>(b->d_opts.get(sizeof(OptDev) * m));
     TileDev* d_tiles = static_cast<TileDev*>(b->d_tiles.get(sizeof(TileDev) * ntiles));
-    b->d_mode.get(sizeof(int32_t) * m);
-    b->d_status.get(sizeof(int32_t) * m);
-    b->d_out4.get(sizeof(double) * 4 * m);
+    if (b->march_buffers) {
+      b->d_pool.get(sizeof(double) * off);
+      b->d_flags.get(static_cast<size_t>(foff));
+      b->d_mode.get(sizeof(int32_t) * m);
+      b->d_status.get(sizeof(int32_t) * m);
+      b->d_out4.get(sizeof(double) * 4 * m);
+    }
     b->d_queue.get(sizeof(int) * 4);
     check(cudaEventRecord(b->ev[0], st), "event");
     check(cudaMemcpyAsync(d_xs, xs, sizeof(double) * xoff, cudaMemcpyHostToDevice, st), "H2D grids");
@@ -947,6 +949,12 @@ void mango_gpu_context_destroy(MangoGpuContext* ctx) {
   }
   if (ctx->table_batch) destroy_batch(ctx->table_batch);
   for (auto& d : ctx->table_buf) d.release();
+  for (MangoGpuBatch* ib : ctx->iv_batch)
+    if (ib) destroy_batch(ib);
+  for (auto& d : ctx->iv_dev) d.release();
+  for (auto& h : ctx->iv_host) h.release();
+  for (auto& level : ctx->iv_ws)
+    for (auto& d : level) d.release();
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   ctx->d_sm_index.release();
   delete ctx;

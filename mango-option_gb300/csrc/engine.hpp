@@ -87,6 +87,10 @@ void parallel_for(int64_t n, const std::function<void(int64_t)>& f, int64_t grai
 
 void set_err(MangoError* err, int32_t code, const std::string& msg);
 
+// Device buffers of one FDM IV working set (iv.cu), kept per level in the
+// context between solves.
+constexpr int kIvWorkBufs = 19;
+
 }  // namespace mgpu
 
 struct MangoGpuBatch;
@@ -172,11 +176,25 @@ struct MangoGpuContext {
   // otherwise pay some twenty device allocations per call).
   MangoGpuBatch* table_batch = nullptr;
   mgpu::DevBuf table_buf[8];
+  // The FDM IV solver's state, kept for the next solve (a fresh solve of
+  // 262,144 quotes would otherwise page-lock some 300 MB of host staging
+  // and allocate and free several GB of device memory): its two batches
+  // (the own grids and Newton's coarse grids, created without march
+  // buffers), the per-quote device and pinned host arrays, and the device
+  // buffers of the working sets of each level.
+  MangoGpuBatch* iv_batch[2] = {nullptr, nullptr};
+  mgpu::DevBuf iv_dev[8];
+  mgpu::HostBuf iv_host[3];
+  mgpu::DevBuf iv_ws[2][mgpu::kIvWorkBufs];
 };
 
 struct MangoGpuBatch {
   MangoGpuContext* ctx = nullptr;
   cudaStream_t stream = nullptr;          // all of this batch's device work
+  // false: creation leaves the march's pool, flags, modes, statuses and
+  // outputs unallocated (the IV batches, whose evaluations march packed
+  // working sets of their own)
+  bool march_buffers = true;
   int64_t n = 0;                          // caller's slot count
   std::vector<mgpu::Resolved> res;        // per slot
   std::vector<std::string> msgs;          // per slot validation message

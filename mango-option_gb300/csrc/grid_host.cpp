@@ -5,8 +5,36 @@
 
 #include <cfloat>
 #include <cmath>
+#include <vector>
 
 namespace mgpu {
+
+namespace {
+
+// sinh(c (i / (n - 1) - 0.5)) / sinh(c / 2) for i in [0, n): the same for
+// every grid with this concentration and point count, so a batch of grids
+// that differ only in their bounds evaluates it once per host thread.  The
+// values are computed by the same expression, in the same order, as an
+// uncached evaluation: the grids stay bit for bit the same.
+const double* sinh_profile(double c, int64_t n) {
+  thread_local double cached_c = 0.0;
+  thread_local int64_t cached_n = -1;
+  thread_local std::vector<double> st;
+  if (cached_n != n || !(cached_c == c) || std::signbit(cached_c) != std::signbit(c)) {
+    const double nm1 = static_cast<double>(n - 1);
+    const double shc = std::sinh(c / 2.0);
+    st.resize(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) {
+      const double eta = static_cast<double>(i) / nm1;
+      st[static_cast<size_t>(i)] = std::sinh(c * (eta - 0.5)) / shc;
+    }
+    cached_c = c;
+    cached_n = n;
+  }
+  return st.data();
+}
+
+}  // namespace
 
 Accuracy default_accuracy() {
   Accuracy a;
@@ -98,13 +126,8 @@ void generate_grid(const GridSpec& s, double* x) {
       return;
     }
     case GridSpec::Sinh: {
-      const double c = s.concentration;
-      const double shc = std::sinh(c / 2.0);
-      for (int64_t i = 0; i < n; ++i) {
-        const double eta = static_cast<double>(i) / nm1;
-        const double st = std::sinh(c * (eta - 0.5)) / shc;
-        x[i] = lo + (hi - lo) * ((1.0 + st) / 2.0);
-      }
+      const double* st = sinh_profile(s.concentration, n);
+      for (int64_t i = 0; i < n; ++i) x[i] = lo + (hi - lo) * ((1.0 + st[i]) / 2.0);
       return;
     }
     case GridSpec::MultiSinh: {
@@ -114,11 +137,8 @@ void generate_grid(const GridSpec& s, double* x) {
         const double shc = std::sinh(c / 2.0);
         const double eta_c = (center - lo) / range;
         if (std::fabs(eta_c - 0.5) < 1e-10) {
-          for (int64_t i = 0; i < n; ++i) {
-            const double eta = static_cast<double>(i) / nm1;
-            const double st = std::sinh(c * (eta - 0.5)) / shc;
-            x[i] = lo + range * ((1.0 + st) / 2.0);
-          }
+          const double* st = sinh_profile(c, n);
+          for (int64_t i = 0; i < n; ++i) x[i] = lo + range * ((1.0 + st[i]) / 2.0);
         } else {
           const double off = center - (lo + hi) / 2.0;
           for (int64_t i = 0; i < n; ++i) {

@@ -39,6 +39,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -69,6 +70,9 @@ constexpr double kVolLower = 0.01;
 // Volatility-space tolerance of quotes the Newton path hands to the
 // k-section finder: a sign-change bracket this narrow settles them.
 constexpr double kVolTol = 1e-7;
+// A sign-change bracket at most this wide: its secant stands for the local
+// slope in the settle test of a Newton hand-over.
+constexpr double kNarrowBracket = 1e-3;
 
 // Fast root-finder state of one quote.  Until a sign change of f has been
 // seen, [lo, hi] steers the search assuming f rises with the volatility;
@@ -216,6 +220,24 @@ __device__ int fast_consume(FastDev& s, const double* sig, const double* f, int 
   s.width = s.has_br ? s.br - s.bl : s.hi - s.lo;
   for (int j = 0; j < n; ++j)
     if (!isfinite(f[j])) return kFastHandOver;
+  // A quote Newton handed over whose objective is flat within the call's
+  // tolerance: two points (of this round, or one of them the best point so
+  // far) with |f| < tol and a secant slope not above kFlatVega, where the
+  // volatility is not determined by the price (the spot node locked to the
+  // payoff over a range of volatilities).  It settles on the reference's
+  // test, as Newton's own flat stop does, at its best point.
+  bool flat = false;
+  if (s.ftol > 0.0) {
+    for (int j = 0; j < n && !flat; ++j) {
+      if (!(fabs(f[j]) < tol)) continue;
+      if (fabs(s.fa) < tol && sig[j] != s.xa &&
+          (f[j] - s.fa) / (sig[j] - s.xa) <= kFlatVega)
+        flat = true;
+      for (int l = j + 1; l < n && !flat; ++l)
+        if (fabs(f[l]) < tol && sig[l] != sig[j] && (f[l] - f[j]) / (sig[l] - sig[j]) <= kFlatVega)
+          flat = true;
+    }
+  }
   for (int j = 0; j < n; ++j) {
     const double x = sig[j], fj = f[j];
     if (fabs(fj) < fabs(s.fa)) {
@@ -249,10 +271,12 @@ __device__ int fast_consume(FastDev& s, const double* sig, const double* f, int 
   const double btol = s.ftol > 0.0 ? kVolTol : tol;
   if (s.ftol > 0.0 && s.has_br && s.fr > s.fl) {
     // a Newton hand-over settles within kVolTol along the bracket's own
-    // slope when that is the smaller one
-    ptol = fmin(ptol, kVolTol * (s.fr - s.fl) / (s.br - s.bl));
+    // slope: when that is the smaller one while the bracket is wide, and
+    // alone once it is narrower than kNarrowBracket
+    const double sb = kVolTol * (s.fr - s.fl) / (s.br - s.bl);
+    ptol = (s.br - s.bl <= kNarrowBracket) ? sb : fmin(ptol, sb);
   }
-  if (fabs(s.fa) < ptol) return kFastSettled;
+  if (fabs(s.fa) < ptol || flat) return kFastSettled;
   if (!s.has_br && s.seen == 3) {
     s.has_br = 1;
     if (s.lo < s.hi) {
@@ -342,8 +366,12 @@ __device__ int fast_propose(const FastDev& s, const OptDev& o, double T, double 
     const double x = (j & 1) ? c + off : c - off;
     if (inside(x)) add(x);
   }
+  // evenly over [lo, hi]; for a Newton hand-over whose bracket spans more
+  // than a factor 4, evenly in log volatility
+  const bool geometric = s.ftol > 0.0 && hi > 4.0 * lo;
   for (int j = 1; j <= spread; ++j) {
-    const double x = lo + (hi - lo) * static_cast<double>(j) / static_cast<double>(spread + 1);
+    const double t = static_cast<double>(j) / static_cast<double>(spread + 1);
+    const double x = geometric ? lo * pow(hi / lo, t) : lo + (hi - lo) * t;
     if (inside(x)) add(x);
   }
   return n;
@@ -577,6 +605,11 @@ __global__ void iv_step_kernel(int nq, const int32_t* __restrict__ qlist,
       fv[j] = objective(out4, mstatus, base + j, P);
     }
     const int r = fast_consume(st.fs, sg, fv, n, upper[q], tol);
+    if (trace && st.fs.ftol > 0.0)
+      printf("iv k-section orig=%d iter=%d r=%d n=%d br=%d [%.17g, %.17g] lo=%.17g hi=%.17g "
+             "seen=%d xa=%.17g fa=%.6e xb=%.17g fb=%.6e ftol=%.3e\n",
+             opts[q].orig, st.fs.iter, r, n, st.fs.has_br, st.fs.bl, st.fs.br, st.fs.lo, st.fs.hi,
+             st.fs.seen, st.fs.xa, st.fs.fa, st.fs.xb, st.fs.fb, st.fs.ftol);
     if (r == kFastGo) {
       next_n = fast_propose(st.fs, opts[q], mat[q], upper[q], k, pts);
     } else if (r == kFastSettled) {
@@ -611,6 +644,11 @@ __global__ void iv_step_kernel(int nq, const int32_t* __restrict__ qlist,
       R[q] = IvOut{root, fabs(f), st.nw.total, kIvOk, vega};
       st.mode = 2;
     } else {
+      if (trace)
+        printf("iv newton hand-over orig=%d total=%d x=%.17g f=%.6e seen=%d lo=%.17g hi=%.17g "
+               "flo=%.6e fhi=%.6e xb=%.17g fb=%.6e sec=%.6e vs=%.6e\n",
+               opts[q].orig, st.nw.total, st.nw.x, f, st.nw.seen, st.nw.lo, st.nw.hi, st.nw.flo,
+               st.nw.fhi, st.nw.xb, st.nw.fb, st.nw.sec, st.nw.vs);
       newton_to_fast(st.nw, st.fs, upper[q]);
       st.mode = 0;
       next_n = fast_propose(st.fs, opts[q], mat[q], upper[q], k, pts);
@@ -745,11 +783,28 @@ struct WorkSet {
   // those quotes come last), or INT32_MAX.
   int32_t tv_first = 0x7fffffff;
 
+  // The context's buffers this set uses for the solve (swapped in by
+  // borrow, back out on destruction), or null: released on destruction.
+  DevBuf* home = nullptr;
+
+  std::array<DevBuf*, kIvWorkBufs> bufs() {
+    return {&d_tiles, &d_opts, &d_xs, &d_map, &d_src, &d_pt, &d_qlist, &d_qbase, &d_sigma,
+            &d_active, &d_pool, &d_flags, &d_mode, &d_status, &d_out4, &d_tv, &d_tpool, &d_wt,
+            &d_twarp};
+  }
+  void borrow(DevBuf* h) {
+    home = h;
+    const auto l = bufs();
+    for (int i = 0; i < kIvWorkBufs; ++i) std::swap(*l[i], h[i]);
+  }
   ~WorkSet() {
-    for (DevBuf* d : {&d_tiles, &d_opts, &d_xs, &d_map, &d_src, &d_pt, &d_qlist, &d_qbase,
-                      &d_sigma, &d_active, &d_pool, &d_flags, &d_mode, &d_status, &d_out4, &d_tv,
-                      &d_tpool, &d_wt, &d_twarp})
-      d->release();
+    const auto l = bufs();
+    for (int i = 0; i < kIvWorkBufs; ++i) {
+      if (home)
+        std::swap(*l[i], home[i]);
+      else
+        l[i]->release();
+    }
   }
 
   // Slots for the quotes in `active` (ascending) with npts[q] > 0.  The
@@ -919,10 +974,15 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
       const double ratio = (q.market_price - intrinsic) / q.market_price;
       upper[i] = ratio > 0.5 ? 3.0 : (ratio > 0.2 ? 2.0 : 1.5);
     }
-    b = create_batch(ctx, pp.data(), nn, grids, grid_stride, nullptr);
-    // The batch's own march buffers are not used: every evaluation runs on
-    // a packed working set.
-    for (DevBuf* d : {&b->d_pool, &b->d_flags, &b->d_mode, &b->d_status, &b->d_out4}) d->release();
+    // The batches live in the context between solves.  Their own march
+    // buffers are never allocated: every evaluation runs on a packed
+    // working set.
+    for (MangoGpuBatch*& ib : ctx->iv_batch)
+      if (!ib) {
+        ib = new MangoGpuBatch();
+        ib->march_buffers = false;
+      }
+    b = create_batch(ctx, pp.data(), nn, grids, grid_stride, nullptr, ctx->iv_batch[0]);
     double host_prep_ms = b->host_prep_ms;
     const int64_t m = static_cast<int64_t>(b->order.size());
     // Newton: the same quotes on coarse grids of the same kind (2/5 of the
@@ -939,9 +999,7 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
         gc[i] = g;
         if (vstatus[i] != MANGO_OK || time_varying(pp[i])) pc[i].spot = -1.0;
       }
-      bc = create_batch(ctx, pc.data(), nn, gc.data(), 1, nullptr);
-      for (DevBuf* d : {&bc->d_pool, &bc->d_flags, &bc->d_mode, &bc->d_status, &bc->d_out4})
-        d->release();
+      bc = create_batch(ctx, pc.data(), nn, gc.data(), 1, nullptr, ctx->iv_batch[1]);
       host_prep_ms += bc->host_prep_ms;
       std::vector<int32_t> pos(static_cast<size_t>(nn), -1);
       for (size_t s2 = 0; s2 < bc->order.size(); ++s2) pos[bc->order[s2]] = static_cast<int32_t>(s2);
@@ -962,17 +1020,10 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
         px[s] = q.market_price;
         mat[s] = q.maturity;
       }
-      DevBuf d_state, d_res, d_next, d_npts, d_hi, d_px, d_mat, d_lev;
-      HostBuf h_npts, h_lev, h_sig1;
-      struct Release {
-        std::vector<DevBuf*> d;
-        std::vector<HostBuf*> h;
-        ~Release() {
-          for (DevBuf* x : d) x->release();
-          for (HostBuf* x : h) x->release();
-        }
-      } release{{&d_state, &d_res, &d_next, &d_npts, &d_hi, &d_px, &d_mat, &d_lev},
-                {&h_npts, &h_lev, &h_sig1}};
+      DevBuf &d_state = ctx->iv_dev[0], &d_res = ctx->iv_dev[1], &d_next = ctx->iv_dev[2],
+             &d_npts = ctx->iv_dev[3], &d_hi = ctx->iv_dev[4], &d_px = ctx->iv_dev[5],
+             &d_mat = ctx->iv_dev[6], &d_lev = ctx->iv_dev[7];
+      HostBuf &h_npts = ctx->iv_host[0], &h_lev = ctx->iv_host[1], &h_sig1 = ctx->iv_host[2];
       IvDev* S = static_cast<IvDev*>(d_state.get(sizeof(IvDev) * m));
       IvOut* R = static_cast<IvOut*>(d_res.get(sizeof(IvOut) * m));
       double* next_sig = static_cast<double*>(d_next.get(sizeof(double) * kMaxPts * m));
@@ -1022,6 +1073,7 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
       // (Newton's first evaluations), the own grids without it.
       WorkSet ws[kLevels];
       for (int L = 0; L < kLevels; ++L) {
+        ws[L].borrow(ctx->iv_ws[L]);
         ws[L].b = b;
         ws[L].src = (L == kLevelCoarse) ? bc : b;
         ws[L].smap = (L == kLevelCoarse) ? &cmap : nullptr;
@@ -1218,12 +1270,8 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
     ctx->stats.algo_flops = m > 0 ? b->algo_flops * slot_evals / static_cast<double>(m) : 0.0;
     if (out_failed) *out_failed = failed;
     if (failed && err) set_err(err, MANGO_OK, first.empty() ? "root finding failed" : first);
-    destroy_batch(b);
-    if (bc) destroy_batch(bc);
     return MANGO_OK;
   } catch (const std::exception& e) {
-    if (b) destroy_batch(b);
-    if (bc) destroy_batch(bc);
     set_err(err, MANGO_ERR_SOLVER, e.what());
     return MANGO_ERR_SOLVER;
   }

@@ -283,12 +283,12 @@ MarchConst make_const(const MangoGpuTrbdf2* trbdf2) {
 
 void destroy_batch(MangoGpuBatch* b) {
   if (!b) return;
-  for (mgpu::DevBuf* d : {&b->d_pool, &b->d_xs, &b->d_flags, &b->d_opts, &b->d_tiles, &b->d_mode,
+  for (mgpu::DevBuf* d : {&b->d_pool, &b->d_xs, &b->d_grids, &b->d_flags, &b->d_opts, &b->d_tiles, &b->d_mode,
                           &b->d_status, &b->d_out4, &b->d_queue, &b->d_tv, &b->d_tv_tp,
                           &b->d_tv_curve, &b->d_tv_ev, &b->d_wt, &b->d_tile_warp, &b->d_bins,
                           &b->d_bin_cnt, &b->d_tile_done})
     d->release();
-  for (mgpu::HostBuf* h : {&b->h_xs, &b->h_opts, &b->h_tiles, &b->h_out4, &b->h_status})
+  for (mgpu::HostBuf* h : {&b->h_xs, &b->h_grids, &b->h_opts, &b->h_tiles, &b->h_out4, &b->h_status})
     h->release();
   for (auto& e : b->ev)
     if (e) cudaEventDestroy(e);
@@ -468,30 +468,55 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
   b->algo_flops = flops;
 
   OptDev* opts = static_cast<OptDev*>(b->h_opts.get(sizeof(OptDev) * std::max<int64_t>(m, 1)));
-  double* xs = static_cast<double*>(b->h_xs.get(sizeof(double) * std::max<int64_t>(xoff, 1)));
+  const bool dev_grids = b->device_grids;
+  double* xs = dev_grids ? nullptr
+                         : static_cast<double*>(b->h_xs.get(sizeof(double) * std::max<int64_t>(xoff, 1)));
+  GridDev* gspec = dev_grids ? static_cast<GridDev*>(
+                                   b->h_grids.get(sizeof(GridDev) * std::max<int64_t>(m, 1)))
+                             : nullptr;
   parallel_for(ntiles, [&](int64_t t) {  // 32 grids per item: a small grain
     const TileDev& td = tiles[t];
     std::vector<double> x;
     for (int l = 0; l < kTile; ++l) {
-      double* dst = xs + td.xoff + l;
       if (l >= td.count) {
-        for (int i = 0; i < td.nx; ++i) dst[static_cast<size_t>(i) * kTile] = 0.0;
+        if (!dev_grids) {
+          double* dst = xs + td.xoff + l;
+          for (int i = 0; i < td.nx; ++i) dst[static_cast<size_t>(i) * kTile] = 0.0;
+        }
         continue;
       }
       const Resolved& r = b->res[order[td.first + l]];
       const MangoPricingParams& p = params[r.orig];
-      x.resize(static_cast<size_t>(r.spec.n));
-      generate_grid(r.spec, x.data());
-      for (int i = 0; i < td.nx; ++i)
-        dst[static_cast<size_t>(i) * kTile] = x[std::min<int64_t>(i, r.spec.n - 1)];
+      if (dev_grids) {
+        GridDev& g = gspec[td.first + l];
+        g = GridDev{};
+        g.type = r.spec.type;
+        g.n_clusters = r.spec.n_clusters;
+        g.n = static_cast<int32_t>(r.spec.n);
+        g.x_min = r.spec.x_min;
+        g.x_max = r.spec.x_max;
+        g.concentration = r.spec.concentration;
+        for (int c = 0; c < 4; ++c) {
+          g.c_center[c] = r.spec.c_center[c];
+          g.c_alpha[c] = r.spec.c_alpha[c];
+          g.c_weight[c] = r.spec.c_weight[c];
+        }
+      } else {
+        double* dst = xs + td.xoff + l;
+        x.resize(static_cast<size_t>(r.spec.n));
+        generate_grid(r.spec, x.data());
+        for (int i = 0; i < td.nx; ++i)
+          dst[static_cast<size_t>(i) * kTile] = x[std::min<int64_t>(i, r.spec.n - 1)];
+      }
       OptDev& o = opts[td.first + l];
       o.dt = (p.maturity - 0.0) / static_cast<double>(r.nt);  // TimeDomain::from_n_steps
       o.sigma = p.volatility;
       o.r = p.rate_const;
       o.q = p.dividend_yield;
       const bool put = p.option_type == MANGO_PUT;
-      o.bc_left = put ? std::max(1.0 - std::exp(x[0]), 0.0) : 0.0;  // american_option.cpp:192-197
-      o.exp_xr = std::exp(x[r.spec.n - 1]);
+      // american_option.cpp:192-197; with device grids, grid_finish_kernel
+      o.bc_left = dev_grids ? 0.0 : (put ? std::max(1.0 - std::exp(x[0]), 0.0) : 0.0);
+      o.exp_xr = dev_grids ? 0.0 : std::exp(x[r.spec.n - 1]);
       o.x_spot = std::log(p.spot / p.strike);
       o.spot = p.spot;
       o.strike = p.strike;
@@ -595,10 +620,24 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
     }
     b->d_queue.get(sizeof(int) * 4);
     check(cudaEventRecord(b->ev[0], st), "event");
-    check(cudaMemcpyAsync(d_xs, xs, sizeof(double) * xoff, cudaMemcpyHostToDevice, st), "H2D grids");
+    GridDev* d_grids =
+        dev_grids ? static_cast<GridDev*>(b->d_grids.get(sizeof(GridDev) * m)) : nullptr;
+    if (dev_grids)
+      check(cudaMemcpyAsync(d_grids, gspec, sizeof(GridDev) * m, cudaMemcpyHostToDevice, st),
+            "H2D grid specs");
+    else
+      check(cudaMemcpyAsync(d_xs, xs, sizeof(double) * xoff, cudaMemcpyHostToDevice, st),
+            "H2D grids");
     check(cudaMemcpyAsync(d_opts, opts, sizeof(OptDev) * m, cudaMemcpyHostToDevice, st), "H2D options");
     check(cudaMemcpyAsync(d_tiles, tiles, sizeof(TileDev) * ntiles, cudaMemcpyHostToDevice, st),
           "H2D tiles");
+    if (dev_grids) {
+      grid_kernel<<<ntiles, 256, 0, st>>>(d_tiles, d_grids, d_xs);
+      check(cudaGetLastError(), "grid_kernel launch");
+      grid_finish_kernel<<<(ntiles * kTile + 127) / 128, 128, 0, st>>>(d_tiles, ntiles, d_grids,
+                                                                      d_xs, d_opts);
+      check(cudaGetLastError(), "grid_finish_kernel launch");
+    }
     double tv_bytes = 0;
     if (!tvh.empty()) {
       auto up = [&](DevBuf& d, const void* src, size_t bytes) {
@@ -612,8 +651,9 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
       up(b->d_tv_ev, evh.data(), sizeof(double) * evh.size());
     }
     check(cudaEventRecord(b->ev[1], st), "event");
-    b->h2d_bytes = static_cast<double>(sizeof(double) * xoff + sizeof(OptDev) * m +
-                                       sizeof(TileDev) * ntiles) + tv_bytes;
+    b->h2d_bytes = static_cast<double>((dev_grids ? sizeof(GridDev) * m : sizeof(double) * xoff) +
+                                       sizeof(OptDev) * m + sizeof(TileDev) * ntiles) +
+                   tv_bytes;
   }
   return b.release();
 }

@@ -133,6 +133,8 @@ uint64_t table_sweep_device(MangoGpuContext* ctx, const double* moneyness, uint6
                             double dividend_yield, MangoOptionType option_type,
                             const MangoGpuGrid* grid, double* dten, int64_t* slice_dims);
 // Kernels (march.cu).
+__global__ void grid_kernel(const TileDev*, const GridDev*, double*);
+__global__ void grid_finish_kernel(const TileDev*, int, const GridDev*, double*, OptDev*);
 __global__ void prep_kernel(const TileDev*, int, const OptDev*, const double*, double*, uint8_t*,
                             int32_t*, MarchConst);
 __global__ void march_kernel(const TileDev*, int, const OptDev*, double*, const uint8_t*,
@@ -195,6 +197,12 @@ struct MangoGpuBatch {
   // outputs unallocated (the IV batches, whose evaluations march packed
   // working sets of their own)
   bool march_buffers = true;
+  // true: the grids are generated on the device from each option's spec
+  // (grid_kernel), within a few units in the last place of the host's
+  // generate_grid; for grids the reference never sees (the Newton IV
+  // method's coarse grids), where the host's sinh evaluations would be
+  // most of the preparation
+  bool device_grids = false;
   int64_t n = 0;                          // caller's slot count
   std::vector<mgpu::Resolved> res;        // per slot
   std::vector<std::string> msgs;          // per slot validation message
@@ -204,7 +212,7 @@ struct MangoGpuBatch {
   double algo_flops = 0;
   double h2d_bytes = 0;
   double host_prep_ms = 0;
-  mgpu::DevBuf d_pool, d_xs, d_flags, d_opts, d_tiles, d_mode, d_status, d_out4, d_queue;
+  mgpu::DevBuf d_pool, d_xs, d_grids, d_flags, d_opts, d_tiles, d_mode, d_status, d_out4, d_queue;
   // Time-varying options (sorted last, from mc.tv_first): per-option data,
   // explicit time points, yield-curve pairs, dividend-event pairs.
   mgpu::DevBuf d_tv, d_tv_tp, d_tv_curve, d_tv_ev;
@@ -221,7 +229,7 @@ struct MangoGpuBatch {
   // counters, and the per-tile taken flags of the binned launch.
   int32_t nbins = 0;
   mgpu::DevBuf d_bins, d_bin_cnt, d_tile_done;
-  mgpu::HostBuf h_xs, h_opts, h_tiles, h_out4, h_status;
+  mgpu::HostBuf h_xs, h_grids, h_opts, h_tiles, h_out4, h_status;
   cudaEvent_t ev[8] = {};
   bool ran = false;
   // Per-run kernel timing: 4 events per run (before setup, after setup,

@@ -356,8 +356,14 @@ __device__ int fast_propose(const FastDev& s, const OptDev& o, double T, double 
   }
   add(c);
   if (k >= 3 && !s.has_br) {
-    if (!(s.ends & 1)) add(kVolLower);
-    if (!(s.ends & 2)) add(upper);
+    // Brent's bracket ends (f at both, without a sign change, fails the
+    // quote as Brent fails it).  A Newton hand-over has seen one sign
+    // already: it tries the end that may show the other, and the far end
+    // only once that one has not (trial volatilities far above the grid's
+    // march slowly).
+    const bool nh = s.ftol > 0.0;
+    if (!(s.ends & 1) && (!nh || !(s.seen & 1) || (s.ends & 2))) add(kVolLower);
+    if (!(s.ends & 2) && (!nh || !(s.seen & 2) || (s.ends & 1))) add(upper);
   }
   const int rest = k - n;
   const int near = rest / 2, spread = rest - near;
@@ -982,6 +988,10 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
         ib = new MangoGpuBatch();
         ib->march_buffers = false;
       }
+    // Newton's coarse grids only steer the iteration (every root is
+    // settled on the quote's own grid), so they are generated on the
+    // device.
+    ctx->iv_batch[1]->device_grids = true;
     b = create_batch(ctx, pp.data(), nn, grids, grid_stride, nullptr, ctx->iv_batch[0]);
     double host_prep_ms = b->host_prep_ms;
     const int64_t m = static_cast<int64_t>(b->order.size());

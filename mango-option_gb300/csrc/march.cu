@@ -32,6 +32,120 @@
 
 namespace mgpu {
 
+// ---------------------------------------------------------------- grids --
+
+namespace {
+
+// Point i of a grid before generate_grid's monotone fix-up (the same
+// formulas, with the device's sinh / exp / log: within a few units in the
+// last place of the host's, so these grids serve where bit-for-bit
+// agreement with the reference's grids is not needed -- the coarse grids of
+// the Newton IV method).
+__device__ double grid_point(const GridDev& g, int i) {
+  const double lo = g.x_min, hi = g.x_max;
+  const double nm1 = static_cast<double>(g.n - 1);
+  const double eta = static_cast<double>(i) / nm1;
+  switch (g.type) {
+    case 0: {  // Uniform
+      const double dx = (hi - lo) / nm1;
+      return lo + static_cast<double>(i) * dx;
+    }
+    case 1: {  // Log
+      const double l0 = log(lo), l1 = log(hi);
+      return exp(l0 + static_cast<double>(i) * ((l1 - l0) / nm1));
+    }
+    case 2: {  // Sinh
+      const double c = g.concentration;
+      const double st = sinh(c * (eta - 0.5)) / sinh(c / 2.0);
+      return lo + (hi - lo) * ((1.0 + st) / 2.0);
+    }
+    default: {  // MultiSinh
+      const double range = hi - lo;
+      if (g.n_clusters == 1) {
+        const double c = g.c_alpha[0], center = g.c_center[0];
+        const double shc = sinh(c / 2.0);
+        const double eta_c = (center - lo) / range;
+        if (fabs(eta_c - 0.5) < 1e-10) {
+          const double st = sinh(c * (eta - 0.5)) / shc;
+          return lo + range * ((1.0 + st) / 2.0);
+        }
+        const double st = sinh(c * (eta - eta_c)) / shc;
+        return lo + range * ((1.0 + st) / 2.0) + (center - (lo + hi) / 2.0);
+      }
+      double total = 0.0;
+      for (int k = 0; k < g.n_clusters; ++k) total += g.c_weight[k];
+      double acc = 0.0;
+      for (int k = 0; k < g.n_clusters; ++k) {
+        const double c = g.c_alpha[k], center = g.c_center[k];
+        const double st = sinh(c * (eta - (center - lo) / range)) / sinh(c / 2.0);
+        acc += (g.c_weight[k] / total) * (lo + range * ((1.0 + st) / 2.0) + (center - (lo + hi) / 2.0));
+      }
+      return acc;
+    }
+  }
+}
+
+// generate_grid runs its monotone fix-up for the multi-cluster and the
+// off-centre single-cluster MultiSinh grids.
+__device__ bool grid_needs_monotone(const GridDev& g) {
+  if (g.type != 3) return false;
+  if (g.n_clusters != 1) return true;
+  return !(fabs((g.c_center[0] - g.x_min) / (g.x_max - g.x_min) - 0.5) < 1e-10);
+}
+
+}  // namespace
+
+// The tiles' grids, [row][lane] per tile: one block per tile, every
+// (row, lane) in parallel; rows past an option's n hold its last point.
+__global__ void grid_kernel(const TileDev* __restrict__ tiles, const GridDev* __restrict__ grids,
+                            double* __restrict__ xs) {
+  const TileDev td = tiles[blockIdx.x];
+  double* X = xs + td.xoff;
+  for (int e = threadIdx.x; e < td.nx * kTile; e += blockDim.x) {
+    const int i = e / kTile, l = e % kTile;
+    if (l >= td.count) {
+      X[e] = 0.0;
+      continue;
+    }
+    const GridDev g = grids[td.first + l];
+    const int n = g.n;
+    double v;
+    if (grid_needs_monotone(g) && (i == 0 || i >= n - 1))
+      v = i == 0 ? g.x_min : g.x_max;  // the fix-up pins both ends
+    else
+      v = grid_point(g, min(i, n - 1));
+    X[e] = v;
+  }
+}
+
+// Per option after grid_kernel: generate_grid's monotone fix-up where it
+// applies (a serial pass each way), then the option's boundary data from
+// its first and last points (american_option.cpp:192-197, 276-290).
+__global__ void grid_finish_kernel(const TileDev* __restrict__ tiles, int ntiles,
+                                   const GridDev* __restrict__ grids, double* __restrict__ xs,
+                                   OptDev* __restrict__ opts) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = gt / kTile, lane = gt % kTile;
+  if (t >= ntiles) return;
+  const TileDev td = tiles[t];
+  if (lane >= td.count) return;
+  const int k = td.first + lane;
+  const GridDev g = grids[k];
+  const int n = g.n;
+  double* X = xs + td.xoff + lane;
+  auto x = [&](int i) -> double& { return X[static_cast<size_t>(i) * kTile]; };
+  if (grid_needs_monotone(g) && n >= 2) {
+    const double lo = g.x_min, hi = g.x_max;
+    const double ms = (hi - lo) / static_cast<double>(static_cast<int64_t>(n) * 100);
+    for (int i = 1; i < n - 1; ++i)
+      if (x(i) <= x(i - 1) + ms) x(i) = x(i - 1) + ms;
+    for (int i = n - 2; i > 0; --i)
+      if (x(i) >= x(i + 1) - ms) x(i) = x(i + 1) - ms;
+  }
+  OptDev& o = opts[k];
+  o.bc_left = o.is_put ? dmax_ref(1.0 - exp(x(0)), 0.0) : 0.0;
+  o.exp_xr = exp(x(n - 1));
+}
 
 // ---------------------------------------------------------------- setup --
 // One lane per option.  Builds psi, the stencils, the three stage-matrix

@@ -56,6 +56,18 @@ struct OptDev {
   int32_t orig;     // index in the caller's array
 };
 
+// One option's grid (GridSpec of grid_host.hpp as plain data), generated on
+// the device by grid_kernel / grid_finish_kernel with generate_grid's
+// formulas (GridSpec::generate, src/pde/core/grid.hpp:364-498).
+struct GridDev {
+  int32_t type;        // GridSpec::Type
+  int32_t n_clusters;
+  int32_t n;
+  int32_t pad;
+  double x_min, x_max, concentration;
+  double c_center[4], c_alpha[4], c_weight[4];
+};
+
 struct TileDev {
   int64_t off;      // offset (doubles) of this tile's block in the pool
   int64_t xoff;     // offset (doubles) of this tile's grid in the grid array

@@ -350,7 +350,7 @@ __device__ __forceinline__ void cp_wait_oldest() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(kRing - 1) : "memory");
 }
 
-// Forward-sweep inputs of row i into ring slot i % kRingSlots.  The cached
+// Forward-sweep inputs of row i into its ring slot s (slot i % kRingSlots).  The cached
 // stage-1 row uses -l/pivot for both u_{i-1} and d'_{i-1} (the explicit
 // operator's lower weight equals the Jacobian's), and the stage-2 row takes
 // beta/alpha times the alpha weight for u^n, so neither E1L nor B2H streams.
@@ -358,9 +358,8 @@ __device__ __forceinline__ void cp_wait_oldest() {
 //   Rannacher: slot 2 = u_prev;  all: slot 4 = psi on the tile's
 //   lock-candidate rows [flo, fhi] (the lock test's obstacle).
 template <int K>
-__device__ __forceinline__ void issue_fwd(const TileView& V, double* R, int a_in, int i,
+__device__ __forceinline__ void issue_fwd(const TileView& V, double* s, int a_in, int i,
                                           const L2Pol& pol, int flo, int fhi) {
-  double* s = R + (i % kRingSlots) * kRingSlot;
   const double* p = V.rp(i);
   if (i >= flo && i <= fhi) cp_async8(s + 4 * kTile, p + A_PSI * kTile, pol.first);
   if (K == kStage1) {
@@ -378,14 +377,13 @@ __device__ __forceinline__ void issue_fwd(const TileView& V, double* R, int a_in
   }
 }
 
-// Back-substitution inputs of row i into ring slot i % kRingSlots: -c' (the
+// Back-substitution inputs of row i into its ring slot s (slot i % kRingSlots): -c' (the
 // cached factor, or this sweep's own for the rows [lo, hi] it solved off the
 // cache), the obstacle where it is positive (rows [plo, phi]; 0 elsewhere),
 // d'.
 template <int K>
-__device__ __forceinline__ void issue_bwd(const TileView& V, double* R, int i, int plo, int phi,
+__device__ __forceinline__ void issue_bwd(const TileView& V, double* s, int i, int plo, int phi,
                                           const L2Pol& pol, int lo, int hi) {
-  double* s = R + (i % kRingSlots) * kRingSlot;
   const double* p = V.rp(i);
   if (i >= lo && i <= hi)
     cp_async8(s, p + (K == kStage2 ? A_CP2 : A_CP) * kTile);
@@ -555,16 +553,22 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
   }
   const int stop = live ? min(last, n - 2) : 0;
   for (int j = 1; j <= kRing; ++j) {
-    if (j <= stop) issue_fwd<K>(V, R, a_in, j, pol, flo, fhi);
+    if (j <= stop) issue_fwd<K>(V, R + j * kRingSlot, a_in, j, pol, flo, fhi);
     cp_commit();
   }
+  // Ring slots of the row being solved and of the row being fetched (row
+  // i + kRing lands in the slot row i - 1 was read from), advanced by a
+  // pointer step per row rather than a modulo.
+  double* const r_last = R + kRing * kRingSlot;
+  double* s_rd = R + kRingSlot;  // row 1
+  double* s_wr = R;              // row 0's slot, never filled: row 1 + kRing's
   // The lock test (pde_solver.hpp:635-680) only runs on the tile's
   // lock-candidate rows [flo, fhi]: the union over its lanes of each lane's
   // contiguous candidate block.  Elsewhere a row cannot lock, so those
   // segments carry no test at all.
   auto row = [&](int i, auto may_lock) {
     cp_wait_oldest();
-    const double* s = R + (i % kRingSlots) * kRingSlot;
+    const double* s = s_rd;
     double ra = 0.0, rnl = 0.0, rv = 0.0;
     if (K != kRannacher) {
       ra = s[0];  // stage 1: E1D; stage 2: A2H
@@ -572,8 +576,10 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
       rv = s[3 * kTile];
     }
     const double rc = s[(K == kStage1 ? 1 : 2) * kTile];  // stage 1: E1U; else the guess
-    if (i + kRing <= stop) issue_fwd<K>(V, R, a_in, i + kRing, pol, flo, fhi);
+    if (i + kRing <= stop) issue_fwd<K>(V, s_wr, a_in, i + kRing, pol, flo, fhi);
     cp_commit();
+    s_wr = s_rd;
+    s_rd = (s_rd == r_last) ? R : s_rd + kRingSlot;
     const double g = (K == kStage1) ? u0 : rc;
     bool lock = false;
     double psi_i = 0.0;
@@ -618,16 +624,20 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
   double xnext = dmax_ref(bcr, V.at(A_PSI, n - 1));
   const int top = n - 2;  // this lane's first row going down
   for (int j = 0; j < kRing; ++j) {
-    if (top - j >= 1) issue_bwd<K>(V, R, top - j, plo, phi, pol, lo, hi);
+    if (top - j >= 1) issue_bwd<K>(V, R + ((top - j) % kRingSlots) * kRingSlot, top - j, plo, phi, pol, lo, hi);
     cp_commit();
   }
+  s_rd = R + (top % kRingSlots) * kRingSlot;            // row top
+  s_wr = R + ((top + 1) % kRingSlots) * kRingSlot;      // row top - kRing's
   for (int i = top; i >= 1; --i) {
     cp_wait_oldest();
-    const double* s = R + (i % kRingSlots) * kRingSlot;
+    const double* s = s_rd;
     const double rnc = s[0], rd = s[2 * kTile];
     const double rpsi = (i >= plo && i <= phi) ? s[kTile] : 0.0;
-    if (i - kRing >= 1) issue_bwd<K>(V, R, i - kRing, plo, phi, pol, lo, hi);
+    if (i - kRing >= 1) issue_bwd<K>(V, s_wr, i - kRing, plo, phi, pol, lo, hi);
     cp_commit();
+    s_wr = s_rd;
+    s_rd = (s_rd == R) ? r_last : s_rd - kRingSlot;
     const double nc = rnc;  // the ring holds the right -c' for this row
     const double xv = proj_max(fma(nc, xnext, rd), rpsi);
     V.at(a_out, i) = xv;

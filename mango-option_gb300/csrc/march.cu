@@ -341,6 +341,22 @@ __device__ __forceinline__ void cp_async8(double* sdst, const double* gsrc, uint
                "l"(pol)
                : "memory");
 }
+// The same copies to a shared-memory address (the rings are addressed as
+// 32-bit shared addresses, so that neither the copies nor the reads go
+// through generic addressing).
+__device__ __forceinline__ void cp_async8s(unsigned s, const double* gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async8s(unsigned s, const double* gsrc, uint64_t pol) {
+  asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gsrc),
+               "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ double lds(unsigned s) {
+  double v;
+  asm volatile("ld.shared.f64 %0, [%1];\n" : "=d"(v) : "r"(s) : "memory");
+  return v;
+}
 __device__ __forceinline__ void st_hint(double* g, double v, uint64_t pol) {
   asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;\n" ::"l"(g), "d"(v), "l"(pol) : "memory");
 }
@@ -358,22 +374,23 @@ __device__ __forceinline__ void cp_wait_oldest() {
 //   Rannacher: slot 2 = u_prev;  all: slot 4 = psi on the tile's
 //   lock-candidate rows [flo, fhi] (the lock test's obstacle).
 template <int K>
-__device__ __forceinline__ void issue_fwd(const TileView& V, double* s, int a_in, int i,
+__device__ __forceinline__ void issue_fwd(const TileView& V, unsigned s, int a_in, int i,
                                           const L2Pol& pol, int flo, int fhi) {
+  constexpr unsigned A = kTile * sizeof(double);  // bytes between a slot's arrays
   const double* p = V.rp(i);
-  if (i >= flo && i <= fhi) cp_async8(s + 4 * kTile, p + A_PSI * kTile, pol.first);
+  if (i >= flo && i <= fhi) cp_async8s(s + 4 * A, p + A_PSI * kTile, pol.first);
   if (K == kStage1) {
-    cp_async8(s, p + A_E1D * kTile, pol.first);
-    cp_async8(s + kTile, p + A_E1U * kTile, pol.first);
-    cp_async8(s + 2 * kTile, p + A_N1H * kTile, pol.first);
-    cp_async8(s + 3 * kTile, V.rp(i + 1) + A_U * kTile);
+    cp_async8s(s, p + A_E1D * kTile, pol.first);
+    cp_async8s(s + A, p + A_E1U * kTile, pol.first);
+    cp_async8s(s + 2 * A, p + A_N1H * kTile, pol.first);
+    cp_async8s(s + 3 * A, V.rp(i + 1) + A_U * kTile);
   } else if (K == kStage2) {
-    cp_async8(s, p + A_A2H * kTile, pol.first);
-    cp_async8(s + kTile, p + A_N2H * kTile, pol.first);
-    cp_async8(s + 2 * kTile, p + A_G * kTile);  // guess u^{n+gamma}
-    cp_async8(s + 3 * kTile, p + A_U * kTile);  // u^n
+    cp_async8s(s, p + A_A2H * kTile, pol.first);
+    cp_async8s(s + A, p + A_N2H * kTile, pol.first);
+    cp_async8s(s + 2 * A, p + A_G * kTile);  // guess u^{n+gamma}
+    cp_async8s(s + 3 * A, p + A_U * kTile);  // u^n
   } else {
-    cp_async8(s + 2 * kTile, p + a_in * kTile);  // rhs = guess = u_prev
+    cp_async8s(s + 2 * A, p + a_in * kTile);  // rhs = guess = u_prev
   }
 }
 
@@ -382,15 +399,16 @@ __device__ __forceinline__ void issue_fwd(const TileView& V, double* s, int a_in
 // cache), the obstacle where it is positive (rows [plo, phi]; 0 elsewhere),
 // d'.
 template <int K>
-__device__ __forceinline__ void issue_bwd(const TileView& V, double* s, int i, int plo, int phi,
+__device__ __forceinline__ void issue_bwd(const TileView& V, unsigned s, int i, int plo, int phi,
                                           const L2Pol& pol, int lo, int hi) {
+  constexpr unsigned A = kTile * sizeof(double);
   const double* p = V.rp(i);
   if (i >= lo && i <= hi)
-    cp_async8(s, p + (K == kStage2 ? A_CP2 : A_CP) * kTile);
+    cp_async8s(s, p + (K == kStage2 ? A_CP2 : A_CP) * kTile);
   else
-    cp_async8(s, p + (K == kStage2 ? A_NC2 : A_NC1) * kTile, pol.first);
-  if (i >= plo && i <= phi) cp_async8(s + kTile, p + A_PSI * kTile, pol.first);
-  cp_async8(s + 2 * kTile, p + A_D * kTile, pol.last);
+    cp_async8s(s, p + (K == kStage2 ? A_NC2 : A_NC1) * kTile, pol.first);
+  if (i >= plo && i <= phi) cp_async8s(s + A, p + A_PSI * kTile, pol.first);
+  cp_async8s(s + 2 * A, p + A_D * kTile, pol.last);
 }
 
 // Rows off the cache read their bands, their explicit stencil (stage 1) and
@@ -536,6 +554,10 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
   const L2Pol pol = l2_policies();
   const double beta_alpha = beta / alpha;
   R += threadIdx.x & (kTile - 1);  // this lane's column of the ring
+  // The ring as 32-bit shared addresses: rs (slot 0), kSlotB bytes per slot,
+  // kArrB bytes between a slot's arrays.
+  constexpr unsigned kSlotB = kRingSlot * sizeof(double), kArrB = kTile * sizeof(double);
+  const unsigned rs = static_cast<unsigned>(__cvta_generic_to_shared(R));
   // The previous sweeps' global writes of this lane come before the async
   // copies that read them.
   __threadfence_block();
@@ -553,39 +575,39 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
   }
   const int stop = live ? min(last, n - 2) : 0;
   for (int j = 1; j <= kRing; ++j) {
-    if (j <= stop) issue_fwd<K>(V, R + j * kRingSlot, a_in, j, pol, flo, fhi);
+    if (j <= stop) issue_fwd<K>(V, rs + j * kSlotB, a_in, j, pol, flo, fhi);
     cp_commit();
   }
   // Ring slots of the row being solved and of the row being fetched (row
   // i + kRing lands in the slot row i - 1 was read from), advanced by a
   // pointer step per row rather than a modulo.
-  double* const r_last = R + kRing * kRingSlot;
-  double* s_rd = R + kRingSlot;  // row 1
-  double* s_wr = R;              // row 0's slot, never filled: row 1 + kRing's
+  const unsigned r_last = rs + kRing * kSlotB;
+  unsigned s_rd = rs + kSlotB;  // row 1
+  unsigned s_wr = rs;           // row 0's slot, never filled: row 1 + kRing's
   // The lock test (pde_solver.hpp:635-680) only runs on the tile's
   // lock-candidate rows [flo, fhi]: the union over its lanes of each lane's
   // contiguous candidate block.  Elsewhere a row cannot lock, so those
   // segments carry no test at all.
   auto row = [&](int i, auto may_lock) {
     cp_wait_oldest();
-    const double* s = s_rd;
+    const unsigned s = s_rd;
     double ra = 0.0, rnl = 0.0, rv = 0.0;
     if (K != kRannacher) {
-      ra = s[0];  // stage 1: E1D; stage 2: A2H
-      rnl = s[(K == kStage1 ? 2 : 1) * kTile];
-      rv = s[3 * kTile];
+      ra = lds(s);  // stage 1: E1D; stage 2: A2H
+      rnl = lds(s + (K == kStage1 ? 2 : 1) * kArrB);
+      rv = lds(s + 3 * kArrB);
     }
-    const double rc = s[(K == kStage1 ? 1 : 2) * kTile];  // stage 1: E1U; else the guess
+    const double rc = lds(s + (K == kStage1 ? 1 : 2) * kArrB);  // stage 1: E1U; else the guess
     if (i + kRing <= stop) issue_fwd<K>(V, s_wr, a_in, i + kRing, pol, flo, fhi);
     cp_commit();
     s_wr = s_rd;
-    s_rd = (s_rd == r_last) ? R : s_rd + kRingSlot;
+    s_rd = (s_rd == r_last) ? rs : s_rd + kSlotB;
     const double g = (K == kStage1) ? u0 : rc;
     bool lock = false;
     double psi_i = 0.0;
     // this lane's candidate rows: its own contiguous block, else the flags
     if (decltype(may_lock)::value && (cexact ? (i >= cflo && i <= cfhi) : ROW(F, i) != 0)) {
-      psi_i = s[4 * kTile];
+      psi_i = lds(s + 4 * kArrB);
       lock = (g - psi_i < 1e-8);
     }
     double dcur;
@@ -624,20 +646,20 @@ __device__ __noinline__ int32_t stage(bool live, int n, const TileView V,
   double xnext = dmax_ref(bcr, V.at(A_PSI, n - 1));
   const int top = n - 2;  // this lane's first row going down
   for (int j = 0; j < kRing; ++j) {
-    if (top - j >= 1) issue_bwd<K>(V, R + ((top - j) % kRingSlots) * kRingSlot, top - j, plo, phi, pol, lo, hi);
+    if (top - j >= 1) issue_bwd<K>(V, rs + ((top - j) % kRingSlots) * kSlotB, top - j, plo, phi, pol, lo, hi);
     cp_commit();
   }
-  s_rd = R + (top % kRingSlots) * kRingSlot;            // row top
-  s_wr = R + ((top + 1) % kRingSlots) * kRingSlot;      // row top - kRing's
+  s_rd = rs + (top % kRingSlots) * kSlotB;          // row top
+  s_wr = rs + ((top + 1) % kRingSlots) * kSlotB;    // row top - kRing's
   for (int i = top; i >= 1; --i) {
     cp_wait_oldest();
-    const double* s = s_rd;
-    const double rnc = s[0], rd = s[2 * kTile];
-    const double rpsi = (i >= plo && i <= phi) ? s[kTile] : 0.0;
+    const unsigned s = s_rd;
+    const double rnc = lds(s), rd = lds(s + 2 * kArrB);
+    const double rpsi = (i >= plo && i <= phi) ? lds(s + kArrB) : 0.0;
     if (i - kRing >= 1) issue_bwd<K>(V, s_wr, i - kRing, plo, phi, pol, lo, hi);
     cp_commit();
     s_wr = s_rd;
-    s_rd = (s_rd == R) ? r_last : s_rd - kRingSlot;
+    s_rd = (s_rd == rs) ? r_last : s_rd - kSlotB;
     const double nc = rnc;  // the ring holds the right -c' for this row
     const double xv = proj_max(fma(nc, xnext, rd), rpsi);
     V.at(a_out, i) = xv;

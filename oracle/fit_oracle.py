@@ -11,10 +11,10 @@ product (mango-option_gb300/) never imports it.
 * fit4d: BSplineNDSeparable<double,4>::fit
   (src/math/bspline/bspline_nd_separable.hpp:153-384): axes 3, 2, 1, 0, each
   slice along the axis solved with the axis's collocation matrix.  The
-  reference solves with LAPACKE dgbtrf/dgbtrs (absent here); this restatement
-  uses numpy's dense LU solve, so coefficients agree to the conditioning of B
-  times the rounding unit, not bit for bit (parity at the LAPACK boundary is
-  unpinned).
+  reference solves with LAPACKE dgbtrf/dgbtrs; this restatement uses numpy's
+  dense LU solve, so coefficients agree to the conditioning of B times the
+  rounding unit, not bit for bit.  Pinned to the reference's own fit
+  (tests/golden/fit.npz) in tests/test_oracle_surface.py.
 * european_price / eep_floor / eep_decompose: EuropeanOptionResult::
   compute_price (src/option/european_option.cpp:25-51), eep_floor and
   eep_decompose (src/option/table/eep/eep_decomposer.hpp:21-80).

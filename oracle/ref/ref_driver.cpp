@@ -289,6 +289,34 @@ int32_t ref_bspline4d_eval(const int64_t* sizes, const double* grids, const doub
   return 0;
 }
 
+// Separable 4D collocation fit (BSplineNDSeparable<double,4>::create + fit,
+// src/math/bspline/bspline_nd_separable.hpp:127-230), with its LAPACKE calls
+// forwarded by lapacke_stubs.c.  values row-major [d0][d1][d2][d3] ->
+// coeffs; residual4 / cond4: the per-axis diagnostics.  Returns 0, or 1
+// when create or fit fails.
+int32_t ref_bspline4d_fit(const int64_t* sizes, const double* grids, const double* values,
+                          double tolerance, double* coeffs, double* residual4, double* cond4) {
+  std::array<std::vector<double>, 4> g;
+  size_t off = 0, total = 1;
+  for (int d = 0; d < 4; ++d) {
+    g[d].assign(grids + off, grids + off + sizes[d]);
+    off += static_cast<size_t>(sizes[d]);
+    total *= static_cast<size_t>(sizes[d]);
+  }
+  auto fitter = BSplineNDSeparable<double, 4>::create(g);
+  if (!fitter) return 1;
+  BSplineNDSeparableConfig<double> cfg;
+  cfg.tolerance = tolerance;
+  auto res = fitter->fit(std::vector<double>(values, values + total), cfg);
+  if (!res) return 1;
+  for (size_t i = 0; i < total; ++i) coeffs[i] = res->coefficients[i];
+  for (int d = 0; d < 4; ++d) {
+    residual4[d] = res->max_residual_per_axis[d];
+    cond4[d] = res->condition_per_axis[d];
+  }
+  return 0;
+}
+
 // Price-table PDE sweep + extraction (PriceTableBuilderND<4>::make_batch,
 // solve_batch, extract_tensor; src/option/table/bspline/bspline_builder.cpp:
 // 198-480).  grid_kind 0: GridAccuracyParams{}; 1: PDEGridConfig with

@@ -1,8 +1,7 @@
 /* Oracle build shim (test infrastructure only): LAPACKE is not installed
- * here.  The reference's table builder references three banded routines in
- * its fit stage; the oracle driver never runs the fit, so these declarations
- * only let the sweep and extraction translation unit compile, and
- * lapacke_stubs.c makes every call fail loudly. */
+ * here.  The reference's collocation fit calls three banded routines; these
+ * declarations let it compile, and lapacke_stubs.c forwards the calls to the
+ * library MANGO_REF_LAPACKE names (or fails loudly without one). */
 #pragma once
 #include <stdint.h>
 typedef int32_t lapack_int;

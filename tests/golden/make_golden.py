@@ -32,10 +32,19 @@ every output value):
                      coefficients: 2048 price queries (some outside the axes)
                      for a put and a call table; and eep_decompose
                      (AnalyticalEEP) of a seeded V/K_ref tensor on the same axes
+  fit.npz            BSplineNDSeparable<double,4>::fit (the reference's own
+                     collocation fit, its LAPACKE dgbtrf/dgbtrs/dgbcon calls
+                     forwarded to the LAPACK that scipy bundles, see
+                     oracle/ref/lapacke_stubs.c): on the full 50 x 30 x 20 x 10
+                     table axes, values from a stored seed (regenerated by the
+                     test) and 4096 of the 300,000 coefficients at stored
+                     indices; on the 12 x 8 x 6 x 5 surface axes, seeded values
+                     and every coefficient; per-axis residuals and condition
+                     estimates
   interp_iv.npz      a real EEP table: the reference's own sweep tensor on
                      12 x 6 x 5 x 4 axes (auto grid), its eep_decompose, fitted by the
-                     CPU restatement (oracle/fit_oracle.py; the reference's fit
-                     needs LAPACKE); on it the reference's vega at 1024 points
+                     CPU restatement (oracle/fit_oracle.py, within 4e-16 of the
+                     reference's own fit, fit.npz); on it the reference's vega at 1024 points
                      and InterpolatedIVSolver::solve_batch for 1024 quotes
                      (prices from the table at seeded vols, plus invalid,
                      out-of-range and mismatched quotes)
@@ -43,6 +52,7 @@ every output value):
 from __future__ import annotations
 
 import ctypes
+import os
 import json
 import pathlib
 import subprocess
@@ -259,6 +269,7 @@ def main():
     golden_iv_tv(lib)
     golden_value_at(lib)
     golden_table_greeks(lib)
+    golden_fit(lib)
 
 
 def table_axes(nm, ntau, ns, nr):
@@ -746,6 +757,56 @@ def golden_table_full(lib):
     assert rc == 0
     save("table_full.npz", m=axes[0], tau=axes[1], sigma=axes[2], r=axes[3], alpha=np.array(alpha),
          tensor=out.reshape(nm, nt, ns, nr), dims=dims.reshape(ns * nr, 2))
+
+
+def scipy_lapacke():
+    """The OpenBLAS that scipy bundles, which exports LAPACKE's banded
+    routines (with a scipy_ prefix): the reference's fit calls them through
+    oracle/ref/lapacke_stubs.c."""
+    import glob
+    import scipy
+    libs = glob.glob(str(pathlib.Path(scipy.__file__).parent.parent / "scipy.libs" / "libscipy_openblas*.so"))
+    if not libs:
+        sys.exit("no LAPACKE-providing library found for the reference's fit")
+    return libs[0]
+
+
+FIT_SEED = 2028
+
+
+def fit_table_values(sizes):
+    """Values of the full-axes fit case (regenerated by the tests from
+    FIT_SEED)."""
+    return np.random.default_rng(FIT_SEED).standard_normal(int(np.prod(sizes)))
+
+
+def golden_fit(lib):
+    """The reference's separable fit on the full table axes and on the
+    surface axes."""
+    os.environ["MANGO_REF_LAPACKE"] = scipy_lapacke()
+    lib.ref_bspline4d_fit.restype = ctypes.c_int32
+    res = {"table_seed": np.array(FIT_SEED)}
+    big = table_axes(50, 30, 20, 10)
+    small = table_axes(12, 8, 6, 5)
+    cases = (("table", big, fit_table_values([a.size for a in big])),
+             ("rand", small, np.random.default_rng(2027).standard_normal(12 * 8 * 6 * 5)))
+    for name, ax, vals in cases:
+        sizes = np.array([a.size for a in ax], np.int64)
+        grids = np.ascontiguousarray(np.concatenate(ax))
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        co = np.zeros_like(vals)
+        resid, cond = np.zeros(4), np.zeros(4)
+        rc = lib.ref_bspline4d_fit(P(sizes), P(grids), P(vals), ctypes.c_double(1e-6), P(co), P(resid), P(cond))
+        assert rc == 0, name
+        res.update({f"{name}_sizes": sizes, f"{name}_grids": grids, f"{name}_residual": resid,
+                    f"{name}_cond": cond})
+        if name == "table":
+            idx = np.sort(np.random.default_rng(FIT_SEED + 1).choice(vals.size, 4096, replace=False))
+            res.update({"table_idx": idx, "table_coeffs": co[idx], "table_coeff_sum": np.array(co.sum()),
+                        "table_coeff_absmax": np.array(np.abs(co).max())})
+        else:
+            res.update({f"{name}_values": vals, f"{name}_coeffs": co})
+    save("fit.npz", **res)
 
 
 def golden_iv_config4(lib):

@@ -4,9 +4,9 @@ reference's golden outputs (surface.npz) and the CPU restatement
 (oracle/fit_oracle.py, pinned in test_oracle_surface.py).
 
 Bars: prices 1e-12 relative against the reference on the same coefficients;
-EEP 1e-12 absolute; fit coefficients within cond(B) x 1e-14 of the dense
-restatement (LAPACK boundary, parity otherwise unpinned); cubic
-reproduction 1e-11."""
+EEP 1e-12 absolute; fit coefficients 1e-13 of the largest against the
+reference's own fit (fit.npz) and within cond(B) x 1e-14 of the dense
+restatement; cubic reproduction 1e-11."""
 import sys
 
 import numpy as np
@@ -85,6 +85,28 @@ def test_fit_vs_dense_restatement(engine):
     assert np.allclose(stats["condition"], conds, rtol=1e-9)
     bound = np.prod(conds) * 1e-14 * np.abs(ref).max()
     assert np.abs(coeffs - ref).max() <= bound, (np.abs(coeffs - ref).max(), bound)
+
+
+def test_fit_vs_reference_fit(engine):
+    """The device fit against the reference's BSplineNDSeparable<double,4>::fit
+    (fit.npz): every coefficient on the 12 x 8 x 6 x 5 surface axes, 4096
+    sampled coefficients and the sum of all on the full 50 x 30 x 20 x 10
+    table axes, at 1e-13 of the largest coefficient; per-axis condition
+    numbers against the reference's dgbcon estimates (rtol 1e-9)."""
+    g = golden("fit.npz")
+    axes = np.split(g["rand_grids"], np.cumsum(g["rand_sizes"])[:-1])
+    coeffs, stats = engine.bspline4d_fit(axes, g["rand_values"].reshape([a.size for a in axes]))
+    ref = g["rand_coeffs"]
+    assert np.abs(coeffs.ravel() - ref).max() <= 1e-13 * np.abs(ref).max()
+    assert np.allclose(stats["condition"], g["rand_cond"], rtol=1e-9)
+    axes = np.split(g["table_grids"], np.cumsum(g["table_sizes"])[:-1])
+    vals = np.random.default_rng(int(g["table_seed"])).standard_normal(int(np.prod(g["table_sizes"])))
+    coeffs, stats = engine.bspline4d_fit(axes, vals.reshape([a.size for a in axes]))
+    c = coeffs.ravel()
+    amax = float(g["table_coeff_absmax"])
+    assert np.abs(c[g["table_idx"]] - g["table_coeffs"]).max() <= 1e-13 * amax
+    assert abs(c.sum() - float(g["table_coeff_sum"])) <= 1e-13 * amax * c.size
+    assert np.allclose(stats["condition"], g["table_cond"], rtol=1e-9)
 
 
 def test_fit_failure_and_validation(engine, pkg):

@@ -105,7 +105,26 @@ def build_reference_oracle() -> pathlib.Path | None:
     if ref is None:
         return None
     _run(["make", "-s", "-C", str(ORACLE_DIR / "ref"), f"REF={ref}", "-j8"])
+    build_reference_parquet(ref)
     return ORACLE_DIR / "_ref" / "libmango_ref.so"
+
+
+def build_reference_parquet(ref: pathlib.Path) -> pathlib.Path | None:
+    """The reference's Parquet writer and reader, against the Arrow C++
+    libraries pyarrow bundles, when pyarrow is importable (its version's
+    library names must match the ones found)."""
+    try:
+        import pyarrow as pa
+    except ImportError:
+        return None
+    lib_dir = pa.get_library_dirs()[0]
+    sover = [p.name.split(".so.")[1] for p in pathlib.Path(lib_dir).glob("libparquet.so.*")
+             if p.name.split(".so.")[1].isdigit()]
+    if not sover:
+        return None
+    _run(["make", "-s", "-C", str(ORACLE_DIR / "ref"), f"REF={ref}", "parquet",
+          f"ARROW_INC={pa.get_include()}", f"ARROW_LIB={lib_dir}", f"ARROW_SOVER={sover[0]}"])
+    return ORACLE_DIR / "_ref" / "libmango_ref_parquet.so"
 
 
 if __name__ == "__main__":

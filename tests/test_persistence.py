@@ -1,10 +1,11 @@
 """Price-table persistence: the CRC64 against the reference's own
 src/support/crc64.cpp (compiled into the reference library), and the
-Parquet format of src/option/table/parquet/parquet_io.cpp on a file written
-and read back.  The container itself is unpinned: the reference's writer
-needs Arrow C++, which is not present, and the reference holds no sample
-files.  The device round trip (table -> file -> table) is in the GPU test at
-the end."""
+Parquet format of src/option/table/parquet/parquet_io.cpp: a file written
+and read back, and the reference's own writer and reader (compiled against
+the Arrow C++ libraries pyarrow bundles into oracle/_ref/
+libmango_ref_parquet.so, where the reference tree is present) reading the
+engine's files and writing files the engine reads.  The device round trip
+(table -> file -> table) is in the GPU test at the end."""
 import ctypes
 import sys
 
@@ -78,6 +79,75 @@ def test_parquet_round_trip_and_layout(pkg, tmp_path, compression):
     for g0, g1 in zip(s0.grids + s0.knots, s1.grids + s1.knots):
         assert np.array_equal(g0, g1)
     assert np.array_equal(s0.values, s1.values)
+
+
+def ref_parquet():
+    so = ROOT / "oracle" / "_ref" / "libmango_ref_parquet.so"
+    if not so.exists():
+        pytest.skip("the reference's Parquet writer is not built here")
+    lib = ctypes.CDLL(str(so))
+    lib.ref_parquet_write_bspline4d.restype = ctypes.c_int32
+    lib.ref_parquet_read.restype = ctypes.c_int32
+    return lib
+
+
+def P(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+COMPRESSION = {"none": 0, "snappy": 1, "zstd": 2}
+
+
+@pytest.mark.parametrize("compression", ["zstd", "snappy", "none"])
+def test_reference_reads_engine_file(pkg, tmp_path, compression):
+    """read_parquet of the reference accepts the engine's file (format
+    version, keys, column types, both checksum levels) and returns its
+    fields."""
+    lib = ref_parquet()
+    d = sample_data(pkg)
+    f = tmp_path / "engine.parquet"
+    pkg.write_parquet(d, f, compression)
+    kind = ctypes.create_string_buffer(64)
+    sc, b8, s4 = np.zeros(8), np.zeros(8), np.zeros(4, np.int64)
+    vals = np.zeros(d.segments[0].values.size)
+    assert lib.ref_parquet_read(str(f).encode(), kind, P(sc), P(b8), P(s4), P(vals), ctypes.c_int64(vals.size)) == 0
+    assert kind.value == b"bspline_4d"
+    assert list(sc) == [1.0, 0.01, 1.5, 20.0, 0.125, 1.0, 100.0, 4.0]
+    assert list(b8) == [-0.3, 0.3, 0.05, 1.5, 0.1, 0.6, 0.0, 0.06]
+    assert list(s4) == d.segments[0].num_pts
+    assert np.array_equal(vals, d.segments[0].values)
+
+
+@pytest.mark.parametrize("compression", ["zstd", "snappy", "none"])
+def test_engine_reads_reference_file(pkg, tmp_path, compression):
+    """The reference's write_parquet output is read by the engine with every
+    field and both checksums as written."""
+    lib = ref_parquet()
+    d = sample_data(pkg)
+    s = d.segments[0]
+    f = tmp_path / "reference.parquet"
+    sizes = np.array(s.num_pts, np.int64)
+    grids, knots = np.concatenate(s.grids), np.concatenate(s.knots)
+    b8 = np.array([d.bounds_m_min, d.bounds_m_max, d.bounds_tau_min, d.bounds_tau_max, d.bounds_sigma_min,
+                   d.bounds_sigma_max, d.bounds_rate_min, d.bounds_rate_max])
+    lo, hi = np.array(s.domain_lo, float), np.array(s.domain_hi, float)
+    rc = lib.ref_parquet_write_bspline4d(
+        str(f).encode(), P(sizes), P(grids), P(knots), P(np.ascontiguousarray(s.values)), ctypes.c_double(s.K_ref),
+        ctypes.c_int32(1), ctypes.c_double(d.dividend_yield), ctypes.c_double(d.maturity), P(b8), P(lo), P(hi),
+        ctypes.c_double(s.tau_start), ctypes.c_double(s.tau_end), ctypes.c_double(s.tau_min),
+        ctypes.c_double(s.tau_max), ctypes.c_int64(d.n_pde_solves), ctypes.c_double(d.precompute_time_seconds),
+        ctypes.c_int32(COMPRESSION[compression]))
+    assert rc == 0
+    back = pkg.read_parquet(f)
+    assert back.option_type == 1 and back.dividend_yield == 0.01 and back.maturity == 1.5
+    assert back.n_pde_solves == 20 and back.precompute_time_seconds == 0.125
+    assert (back.bounds_m_min, back.bounds_rate_max) == (-0.3, 0.06)
+    s1 = back.segments[0]
+    assert (s1.K_ref, s1.tau_start, s1.tau_end, s1.tau_min, s1.tau_max) == (100.0, 0.0, 1.5, 0.05, 1.5)
+    assert s1.interp_type == "bspline" and s1.ndim == 4 and list(s1.num_pts) == s.num_pts
+    for g0, g1 in zip(s.grids + s.knots, s1.grids + s1.knots):
+        assert np.array_equal(g0, g1)
+    assert np.array_equal(s.values, s1.values)
 
 
 def test_parquet_rejects_corruption(pkg, tmp_path):

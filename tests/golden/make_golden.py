@@ -43,8 +43,8 @@ every output value):
                      estimates
   interp_iv.npz      a real EEP table: the reference's own sweep tensor on
                      12 x 6 x 5 x 4 axes (auto grid), its eep_decompose, fitted by the
-                     CPU restatement (oracle/fit_oracle.py, within 4e-16 of the
-                     reference's own fit, fit.npz); on it the reference's vega at 1024 points
+                     reference's own fit (BSplineNDSeparable, see fit.npz); on it the
+                     reference's vega at 1024 points
                      and InterpolatedIVSolver::solve_batch for 1024 quotes
                      (prices from the table at seeded vols, plus invalid,
                      out-of-range and mismatched quotes)
@@ -369,9 +369,16 @@ def golden_interp_iv(lib):
                                ctypes.c_int64(ns), P(axes[3]), ctypes.c_int64(nr), ctypes.c_double(100.0),
                                ctypes.c_double(0.0), ctypes.c_int32(1), P(ten))
     assert rc == 0
-    coeffs = np.ascontiguousarray(fit_oracle.fit4d(axes, ten.reshape(nm, nt, ns, nr)).ravel())
     sizes = np.array([nm, nt, ns, nr], np.int64)
     grids = np.ascontiguousarray(np.concatenate(axes))
+    # the reference's own fit (BSplineNDSeparable<double,4>, LAPACKE forwarded)
+    os.environ["MANGO_REF_LAPACKE"] = scipy_lapacke()
+    lib.ref_bspline4d_fit.restype = ctypes.c_int32
+    coeffs = np.zeros_like(ten)
+    assert lib.ref_bspline4d_fit(P(sizes), P(grids), P(ten), ctypes.c_double(1e-6), P(coeffs), P(np.zeros(4)),
+                                 P(np.zeros(4))) == 0
+    dense = fit_oracle.fit4d(axes, ten.reshape(nm, nt, ns, nr)).ravel()
+    assert np.abs(coeffs - dense).max() <= 1e-13 * np.abs(coeffs).max()
     rng = np.random.default_rng(31)
     n = 1024
     # vega at random in-range points

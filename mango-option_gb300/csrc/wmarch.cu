@@ -64,8 +64,11 @@ enum WArray : int {
 constexpr unsigned char kRowCached = 0, kRowLocked = 1, kRowOff = 2;
 constexpr double kBig = 1e300;  // "no bound" of a clamp map
 // Options of a large uneven batch that may go to the warp march beside the
-// thread march (two warp blocks per SM, a few options each).
-constexpr int64_t kLongWarpOptions = 1216;
+// thread march (two warp blocks per SM, a few options each).  With the
+// thread march's tiles assigned to SM sub-partitions, caps of 0, 304, 456,
+// 608, 760, 912, 1216 and 2432 options measured 398, 360, 357, 355, 361,
+// 382, 407 and 527 ms per launch on the 65,536-option uneven batch.
+constexpr int64_t kLongWarpOptions = 608;
 
 // R rows per lane, a compile-time constant: every row loop unrolls and
 // every shared-memory address is a constant offset from the lane's column.

@@ -1175,10 +1175,15 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
             // round's thread march was measured at about twice the time of a
             // pricing batch of its size (trial volatilities far from the
             // grid's slow some lanes, and a tile waits for its slowest), so
-            // its estimate counts double.
+            // its estimate counts double (MANGO_GPU_IV_TAIL_SCALE: that
+            // factor, for sweeps).
+            double tail_scale = 2.0;
+            if (const char* e = std::getenv("MANGO_GPU_IV_TAIL_SCALE"))
+              if (std::atof(e) > 0.0) tail_scale = std::atof(e);
             const WarpPlan plan = plan_warp_tiles(
                 w.tiles_h.data(), ntiles, w.tv_first < w.mw ? w.tv_first / kTile : ntiles,
-                ctx->num_sms, static_cast<int64_t>(active.size()) <= kTailQuotes ? 2.0 : 1.0);
+                ctx->num_sms,
+                static_cast<int64_t>(active.size()) <= kTailQuotes ? tail_scale : 1.0);
             const int nwt = static_cast<int>(plan.tiles.size());
             if (nwt > 0) {
               check(cudaMemcpyAsync(w.d_wt.get(sizeof(int32_t) * nwt), plan.tiles.data(),

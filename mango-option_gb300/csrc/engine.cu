@@ -474,12 +474,15 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
   GridDev* gspec = dev_grids ? static_cast<GridDev*>(
                                    b->h_grids.get(sizeof(GridDev) * std::max<int64_t>(m, 1)))
                              : nullptr;
+  // Deferred grids: the points (and the boundary data taken from them) are
+  // filled later by fill_batch_grids and uploaded by upload_batch_grids.
+  const bool defer = b->defer_grids && !dev_grids;
   parallel_for(ntiles, [&](int64_t t) {  // 32 grids per item: a small grain
     const TileDev& td = tiles[t];
     std::vector<double> x;
     for (int l = 0; l < kTile; ++l) {
       if (l >= td.count) {
-        if (!dev_grids) {
+        if (!dev_grids && !defer) {
           double* dst = xs + td.xoff + l;
           for (int i = 0; i < td.nx; ++i) dst[static_cast<size_t>(i) * kTile] = 0.0;
         }
@@ -501,7 +504,7 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
           g.c_alpha[c] = r.spec.c_alpha[c];
           g.c_weight[c] = r.spec.c_weight[c];
         }
-      } else {
+      } else if (!defer) {
         double* dst = xs + td.xoff + l;
         x.resize(static_cast<size_t>(r.spec.n));
         generate_grid(r.spec, x.data());
@@ -514,9 +517,10 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
       o.r = p.rate_const;
       o.q = p.dividend_yield;
       const bool put = p.option_type == MANGO_PUT;
-      // american_option.cpp:192-197; with device grids, grid_finish_kernel
-      o.bc_left = dev_grids ? 0.0 : (put ? std::max(1.0 - std::exp(x[0]), 0.0) : 0.0);
-      o.exp_xr = dev_grids ? 0.0 : std::exp(x[r.spec.n - 1]);
+      // american_option.cpp:192-197; with device grids, grid_finish_kernel;
+      // deferred, fill_batch_grids
+      o.bc_left = (dev_grids || defer) ? 0.0 : (put ? std::max(1.0 - std::exp(x[0]), 0.0) : 0.0);
+      o.exp_xr = (dev_grids || defer) ? 0.0 : std::exp(x[r.spec.n - 1]);
       o.x_spot = std::log(p.spot / p.strike);
       o.spot = p.spot;
       o.strike = p.strike;
@@ -526,6 +530,8 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
       o.orig = r.orig;
     }
   }, 8);
+  b->grids_pending = defer;
+  b->grid_params = params;
   // Time-varying options: per-option data, time points, curves, events.
   int64_t nc = 0;
   while (nc < m && !b->res[order[nc]].tv) ++nc;
@@ -625,7 +631,7 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
     if (dev_grids)
       check(cudaMemcpyAsync(d_grids, gspec, sizeof(GridDev) * m, cudaMemcpyHostToDevice, st),
             "H2D grid specs");
-    else
+    else if (!defer)
       check(cudaMemcpyAsync(d_xs, xs, sizeof(double) * xoff, cudaMemcpyHostToDevice, st),
             "H2D grids");
     check(cudaMemcpyAsync(d_opts, opts, sizeof(OptDev) * m, cudaMemcpyHostToDevice, st), "H2D options");
@@ -656,6 +662,50 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
                    tv_bytes;
   }
   return b.release();
+}
+
+void fill_batch_grids(MangoGpuBatch* b) {
+  const MangoPricingParams* params = b->grid_params;
+  const std::vector<int32_t>& order = b->order;
+  const TileDev* tiles = b->h_tiles.as<TileDev>();
+  OptDev* opts = b->h_opts.as<OptDev>();
+  double* xs = b->h_xs.as<double>();
+  parallel_for(b->ntiles, [&](int64_t t) {
+    const TileDev& td = tiles[t];
+    std::vector<double> x;
+    for (int l = 0; l < kTile; ++l) {
+      double* dst = xs + td.xoff + l;
+      if (l >= td.count) {
+        for (int i = 0; i < td.nx; ++i) dst[static_cast<size_t>(i) * kTile] = 0.0;
+        continue;
+      }
+      const Resolved& r = b->res[order[td.first + l]];
+      const MangoPricingParams& p = params[r.orig];
+      x.resize(static_cast<size_t>(r.spec.n));
+      generate_grid(r.spec, x.data());
+      for (int i = 0; i < td.nx; ++i)
+        dst[static_cast<size_t>(i) * kTile] = x[std::min<int64_t>(i, r.spec.n - 1)];
+      OptDev& o = opts[td.first + l];
+      const bool put = p.option_type == MANGO_PUT;
+      o.bc_left = put ? std::max(1.0 - std::exp(x[0]), 0.0) : 0.0;  // american_option.cpp:192-197
+      o.exp_xr = std::exp(x[r.spec.n - 1]);
+    }
+  }, 8);
+}
+
+void upload_batch_grids(MangoGpuBatch* b) {
+  const int64_t m = static_cast<int64_t>(b->order.size());
+  if (m == 0) return;
+  const TileDev* tiles = b->h_tiles.as<TileDev>();
+  const TileDev& tl = tiles[b->ntiles - 1];
+  const int64_t xoff = tl.xoff + static_cast<int64_t>(tl.nx) * kTile;
+  check(cudaMemcpyAsync(b->d_xs.p, b->h_xs.p, sizeof(double) * xoff, cudaMemcpyHostToDevice,
+                        b->stream),
+        "H2D grids");
+  check(cudaMemcpyAsync(b->d_opts.p, b->h_opts.p, sizeof(OptDev) * m, cudaMemcpyHostToDevice,
+                        b->stream),
+        "H2D options");
+  b->grids_pending = false;
 }
 
 namespace {

@@ -113,6 +113,12 @@ MangoGpuBatch* create_batch_resolved(MangoGpuContext* ctx, const MangoPricingPar
                                      MangoGpuBatch* reuse = nullptr,
                                      cudaStream_t stream = nullptr);
 void destroy_batch(MangoGpuBatch* b);
+// Deferred grids (MangoGpuBatch::defer_grids): fill the pinned grid array
+// and the options' boundary data from the batch's params (host only, any
+// thread; the params array must still be alive), then copy both to the
+// device on the batch's stream.
+void fill_batch_grids(MangoGpuBatch* b);
+void upload_batch_grids(MangoGpuBatch* b);
 // Enqueue setup, march and outputs (with timing events).
 void run_batch(MangoGpuBatch* b);
 // Wait, copy results into caller slots, update the context stats.
@@ -203,6 +209,13 @@ struct MangoGpuBatch {
   // method's coarse grids), where the host's sinh evaluations would be
   // most of the preparation
   bool device_grids = false;
+  // true: creation leaves the grid points (and the boundary data taken from
+  // them) to fill_batch_grids, which may run on another host thread while
+  // the device works on something else, and upload_batch_grids (the Newton
+  // IV method's own grids, filled during its coarse rounds)
+  bool defer_grids = false;
+  bool grids_pending = false;              // deferred grids not yet uploaded
+  const MangoPricingParams* grid_params = nullptr;  // the params they come from
   int64_t n = 0;                          // caller's slot count
   std::vector<mgpu::Resolved> res;        // per slot
   std::vector<std::string> msgs;          // per slot validation message

@@ -45,8 +45,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "brent.cuh"
@@ -990,8 +992,11 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
       }
     // Newton's coarse grids only steer the iteration (every root is
     // settled on the quote's own grid), so they are generated on the
-    // device.
+    // device.  The own grids (host sinh, bit for bit the reference's) are
+    // first needed after the coarse rounds: Newton fills them on a host
+    // thread while those run.
     ctx->iv_batch[1]->device_grids = true;
+    ctx->iv_batch[0]->defer_grids = method == MANGO_GPU_IV_NEWTON;
     b = create_batch(ctx, pp.data(), nn, grids, grid_stride, nullptr, ctx->iv_batch[0]);
     double host_prep_ms = b->host_prep_ms;
     const int64_t m = static_cast<int64_t>(b->order.size());
@@ -1016,6 +1021,36 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
       cmap.assign(static_cast<size_t>(m), -1);
       for (int64_t s2 = 0; s2 < m; ++s2) cmap[s2] = pos[b->order[s2]];
     }
+    // Deferred own grids: the options' upload must have left the pinned
+    // buffer before the worker writes their boundary data into it.
+    std::thread grid_worker;
+    std::exception_ptr grid_err;
+    struct JoinGuard {
+      std::thread& t;
+      ~JoinGuard() {
+        if (t.joinable()) t.join();
+      }
+    } grid_guard{grid_worker};
+    bool grids_pending = b->grids_pending;
+    if (grids_pending) {
+      check(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+      grid_worker = std::thread([b, &grid_err] {
+        try {
+          fill_batch_grids(b);
+        } catch (...) {
+          grid_err = std::current_exception();
+        }
+      });
+    }
+    auto grids_ready = [&] {
+      if (!grids_pending) return;
+      const auto tw = Clock::now();
+      grid_worker.join();
+      if (grid_err) std::rethrow_exception(grid_err);
+      upload_batch_grids(b);
+      grids_pending = false;
+      host_prep_ms += ms_since(tw);
+    };
     std::vector<IvOut> hr(static_cast<size_t>(m));
     int64_t launches = 0, evaluations = 0;
     int64_t level_evals[kLevels] = {0, 0};
@@ -1138,6 +1173,7 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
               return ka != kc ? ka < kc : a < c;
             });
         }
+        if (!lists[kLevelPlain].empty()) grids_ready();
         int64_t nq_all = 0;
         for (int L = 0; L < kLevels; ++L) {
           ws[L].pack(lists[L], hnpts, next_sig);

@@ -127,3 +127,30 @@ def test_newton_config4_sample_vs_reference(engine, pkg):
     assert nw.mean() > 0.9
     good = np.isclose(out["vega"][nw], t["vega"][nw], rtol=1e-2, atol=1e-6)
     assert good.mean() >= 0.99, good.mean()
+
+
+def test_context_buffers_reused_across_solves(engine, pkg):
+    """The context keeps the IV batches, per-quote arrays and working sets
+    between solves (grow-only): a sequence of solves of different sizes and
+    methods on one context returns exactly what each solve returns on a fresh
+    context."""
+    rng = np.random.default_rng(4245)
+    n = 3072
+    S = np.full(n, 100.0)
+    K = S * rng.uniform(0.8, 1.2, n)
+    T = rng.uniform(0.02, 2.0, n)
+    r = rng.uniform(0.0, 0.08, n)
+    q = rng.uniform(0.0, 0.04, n)
+    vt = rng.uniform(0.05, 0.8, n)
+    put = (np.arange(n) % 4 != 3).astype(np.int32)
+    grids = per_quote_grid(pkg, vt)
+    px = engine.price_arrays(pkg.pricing_array(S, K, T, vt, r, q, put), grids)["value"]
+    quotes = pkg.query_array(S, K, T, r, q, put, px)
+    plan = ((pkg.IV_NEWTON, slice(0, 3072)), (pkg.IV_BRENT, slice(0, 512)), (pkg.IV_NEWTON, slice(1000, 2024)),
+            (pkg.IV_SECANT, slice(0, 3072)), (pkg.IV_NEWTON, slice(0, 256)))
+    seq = [engine.solve_iv_arrays(quotes[s], grids[s], method=m) for m, s in plan]
+    for (m, s), got in zip(plan, seq):
+        with pkg.Engine(0) as fresh:
+            want = fresh.solve_iv_arrays(quotes[s], grids[s], method=m)
+        for k in ("status", "implied_vol", "iterations", "vega"):
+            assert np.array_equal(got[k], want[k], equal_nan=True), (m, s, k)

@@ -149,7 +149,7 @@ def test_tv_in_chunked_batch(engine, pkg):
     del keep
 
 
-@pytest.mark.parametrize("method", ["brent", "secant"])
+@pytest.mark.parametrize("method", ["brent", "secant", "newton"])
 def test_iv_with_schedules_vs_reference(engine, pkg, method):
     """FDM implied volatility for quotes with yield curves and dividends
     against the reference's IVSolver::solve (tests/golden/iv_tv.npz): grid
@@ -159,7 +159,8 @@ def test_iv_with_schedules_vs_reference(engine, pkg, method):
     ~1e-12, so a count may differ on a quote whose last step lands within
     rounding of the tolerance: at most 2 of 96 allowed).  The secant method
     stops elsewhere inside the same price tolerance, so its roots agree
-    within 1e-6 in volatility."""
+    within 1e-6 in volatility; so do Newton's (its quotes with schedules take
+    the secant path, the others Newton's)."""
     g = golden("iv_tv.npz")
     rows = [json.loads(str(s)) for s in g["rows"]]
     n = len(rows)
@@ -167,7 +168,8 @@ def test_iv_with_schedules_vs_reference(engine, pkg, method):
                         [r["r"] for r in rows], [r["q"] for r in rows], [r["put"] for r in rows], g["price"])
     keep = pkg.attach_schedules(q, [r.get("curve") for r in rows], [r.get("divs") for r in rows])
     grids = pkg.grid_array(n, pkg.GRID_FIXED_N_AT_VOL, 101, 200, alpha=g["grid_sigma"])
-    out = engine.solve_iv_arrays(q, grids, method=pkg.IV_BRENT if method == "brent" else pkg.IV_SECANT)
+    out = engine.solve_iv_arrays(q, grids, method={"brent": pkg.IV_BRENT, "secant": pkg.IV_SECANT,
+                                                   "newton": pkg.IV_NEWTON}[method])
     ok = g["status"] == 0
     assert (out["status"][ok] == 0).all(), np.nonzero(out["status"][ok])[0][:8]
     err = np.abs(out["implied_vol"][ok] - g["out"][ok, 0])

@@ -332,7 +332,13 @@ __device__ int fast_propose(const FastDev& s, const OptDev& o, double T, double 
       if (fabs(pts[j] - x) <= 1e-14 * x) return;
     pts[n++] = x;
   };
-  const double lo = s.has_br ? s.bl : s.lo, hi = s.has_br ? s.br : s.hi;
+  const double lo = s.has_br ? s.bl : s.lo;
+  // A Newton hand-over that has only seen f < 0 searches upward in ranges
+  // of a factor 4 (trial volatilities far above the grid's march slowly, and
+  // its root is usually close): Brent's upper end only once the range
+  // reaches it.
+  const bool climb = s.ftol > 0.0 && !s.has_br && s.seen == 1;
+  const double hi = s.has_br ? s.br : (climb ? fmin(s.hi, 4.0 * s.lo) : s.hi);
   auto inside = [&](double x) { return x > lo && x < hi; };
   // centre: the secant through the two best points, a Black-Scholes-vega
   // Newton step from a lone point, or the starting guess; inside a
@@ -365,7 +371,7 @@ __device__ int fast_propose(const FastDev& s, const OptDev& o, double T, double 
     // march slowly).
     const bool nh = s.ftol > 0.0;
     if (!(s.ends & 1) && (!nh || !(s.seen & 1) || (s.ends & 2))) add(kVolLower);
-    if (!(s.ends & 2) && (!nh || !(s.seen & 2) || (s.ends & 1))) add(upper);
+    if (!(s.ends & 2) && (!nh || !(s.seen & 2) || (s.ends & 1)) && !(climb && hi < upper)) add(upper);
   }
   const int rest = k - n;
   const int near = rest / 2, spread = rest - near;

@@ -283,7 +283,7 @@ MarchConst make_const(const MangoGpuTrbdf2* trbdf2) {
 
 void destroy_batch(MangoGpuBatch* b) {
   if (!b) return;
-  for (mgpu::DevBuf* d : {&b->d_pool, &b->d_xs, &b->d_grids, &b->d_flags, &b->d_opts, &b->d_tiles, &b->d_mode,
+  for (mgpu::DevBuf* d : {&b->d_handoff, &b->d_pool, &b->d_xs, &b->d_grids, &b->d_flags, &b->d_opts, &b->d_tiles, &b->d_mode,
                           &b->d_status, &b->d_out4, &b->d_queue, &b->d_tv, &b->d_tv_tp,
                           &b->d_tv_curve, &b->d_tv_ev, &b->d_wt, &b->d_tile_warp, &b->d_bins,
                           &b->d_bin_cnt, &b->d_tile_done})
@@ -894,10 +894,26 @@ void run_batch(MangoGpuBatch* b) {
     check(cudaGetLastError(), "march_kernel launch");
     mc.tile_done = b->d_tile_done.as<uint8_t>();
   }
-  if (b->nwt < ntiles)
+  if (b->nwt < ntiles) {
+    MarchConst mh = mc;
+    // tile hand-off (march.cuh) on the plain queue launch without snapshots;
+    // MANGO_GPU_HANDOFF=0 turns it off
+    const char* he = std::getenv("MANGO_GPU_HANDOFF");
+    if (b->nbins == 0 && !mc.snap_idx && !(he && he[0] == '0')) {
+      const int cap = 4 * ntiles + 1024;
+      const size_t bytes = 16 + sizeof(unsigned long long) * static_cast<size_t>(cap) +
+                           static_cast<size_t>(ntiles);
+      char* h = static_cast<char*>(b->d_handoff.get(bytes));
+      check(cudaMemsetAsync(h, 0, bytes, st), "memset hand-off");
+      mh.ho_ctl = reinterpret_cast<int*>(h);
+      mh.ho_slot = reinterpret_cast<unsigned long long*>(h + 16);
+      mh.ho_moved = reinterpret_cast<uint8_t*>(h + 16 + sizeof(unsigned long long) * cap);
+      mh.ho_cap = cap;
+    }
     march_kernel<<<blocks, 32 * warps_per_block, 0, st>>>(d_tiles, ntiles, d_opts, d_pool,
                                                           d_flags, d_mode, d_status,
-                                                          b->d_queue.as<int>(), mc);
+                                                          b->d_queue.as<int>(), mh);
+  }
   check(cudaGetLastError(), "march_kernel launch");
   if (b->wconcurrent)
     check(cudaStreamWaitEvent(st, b->wev[1], 0), "stream wait");

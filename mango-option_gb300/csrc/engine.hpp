@@ -242,6 +242,7 @@ struct MangoGpuBatch {
   // counters, and the per-tile taken flags of the binned launch.
   int32_t nbins = 0;
   mgpu::DevBuf d_bins, d_bin_cnt, d_tile_done;
+  mgpu::DevBuf d_handoff;  // the thread march's tile hand-off state (march.cuh)
   mgpu::HostBuf h_xs, h_grids, h_opts, h_tiles, h_out4, h_status;
   cudaEvent_t ev[8] = {};
   bool ran = false;

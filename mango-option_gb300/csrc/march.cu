@@ -677,6 +677,45 @@ __device__ __forceinline__ double right_bc(const OptDev& o, double t) {
 
 }  // namespace
 
+// Tile hand-off (MarchConst::ho_ctl): slot values.
+constexpr unsigned long long kHoEmpty = 0, kHoSkip = 1, kHoAbandon = 2;
+constexpr int kHoSegment = 16;    // steps between a marching warp's checks
+constexpr int kHoMinLeft = 32;    // steps a tile must have left to move
+constexpr int kHoPolls = 1 << 22; // a waiting warp's polls (500 ns apart) before it leaves
+
+__device__ __forceinline__ unsigned long long ho_item(int t, int step) {
+  return (static_cast<unsigned long long>(t + 1) << 32) | static_cast<unsigned>(step);
+}
+
+// Lane 0 of a warp whose queue ran dry: a handed-off tile's item, or 0 when
+// every tile is finished (or the wait gave up; a claimed slot is released by
+// marking it abandoned, so that no tile is ever left in it).
+__device__ unsigned long long ho_take(const MarchConst& mc, int ntiles) {
+  volatile int* ctl = mc.ho_ctl;
+  volatile unsigned long long* slot = mc.ho_slot;
+  for (;;) {
+    const int s = atomicAdd(mc.ho_ctl, 1);
+    if (s >= mc.ho_cap) return 0;
+    for (int it = 0;; ++it) {
+      const unsigned long long v = slot[s];
+      if (v == kHoSkip) break;  // nobody came for this slot: claim another
+      if (v > kHoAbandon) {
+        __threadfence();
+        return v;
+      }
+      if (ctl[2] >= ntiles || it >= kHoPolls) {
+        const unsigned long long old = atomicCAS(&mc.ho_slot[s], kHoEmpty, kHoAbandon);
+        if (old > kHoAbandon) {
+          __threadfence();
+          return old;
+        }
+        return 0;
+      }
+      __nanosleep(500);
+    }
+  }
+}
+
 // Persistent march: each warp pulls tiles (largest first) from the queue.
 __global__ void __launch_bounds__(128, 4) march_kernel(
     const TileDev* __restrict__ tiles, int ntiles, const OptDev* __restrict__ opts,
@@ -693,8 +732,14 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
     const int sm = smid < static_cast<unsigned>(mc.nsmid) ? mc.sm_index[smid] : -1;
     if (sm >= 0 && sm * 4 + 3 < mc.nbins) my_bin = sm * 4 + static_cast<int>(wslot & 3u);
   }
+  const bool ho = mc.ho_ctl != nullptr;
+  bool queue_dry = false;
+  // a tile finished or skipped (hand-off launches count them)
+  auto ho_done = [&] {
+    if (ho && lane == 0) atomicAdd(&mc.ho_ctl[2], 1);
+  };
   for (;;) {
-    int t = 0;
+    int t = 0, step0 = 0;
     if (lane == 0) {
       if (mc.nbins > 0) {
         t = -1;
@@ -703,18 +748,37 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
           if (k < mc.bin_off[my_bin + 1] - mc.bin_off[my_bin]) t = mc.bin_tiles[mc.bin_off[my_bin] + k];
         }
         if (t >= 0) mc.tile_done[t] = 1;
-      } else {
+      } else if (!queue_dry) {
         t = atomicAdd(queue, 1);
+      } else {
+        t = ntiles;
+      }
+      if (ho && t >= ntiles) {
+        // the queue ran dry: wait for a tile another warp hands off
+        queue_dry = true;
+        const unsigned long long v = ho_take(mc, ntiles);
+        if (v != 0) {
+          t = static_cast<int>(v >> 32) - 1;
+          step0 = static_cast<int>(v & 0xffffffffu);
+        }
       }
     }
     t = __shfl_sync(0xffffffffu, t, 0);
+    step0 = __shfl_sync(0xffffffffu, step0, 0);
     if (t < 0 || t >= ntiles) break;
+    if (step0 > 0) __threadfence();  // the previous warp's state before this one's reads
     if (mc.nbins == 0 && mc.tile_done && mc.tile_done[t]) continue;  // taken by the binned launch
-    if (mc.tile_warp && mc.tile_warp[t]) continue;  // marched one warp per option
+    if (mc.tile_warp && mc.tile_warp[t]) {  // marched one warp per option
+      ho_done();
+      continue;
+    }
     const TileDev td = tiles[t];
     const int k = td.first + lane;
     const bool active = lane < td.count && (!mc.active || mc.active[k]) && k < mc.tv_first;
-    if (!__any_sync(0xffffffffu, active)) continue;
+    if (!__any_sync(0xffffffffu, active)) {
+      ho_done();
+      continue;
+    }
     OptDev o{};
     int32_t md = 0;
     if (active) {
@@ -766,9 +830,10 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
         ++sp;
       }
     };
-    if (active) record(0, A_U);
-    int step = 0;
-    if (mc.rannacher) {
+    if (step0 > 0 && active) st = status[k];  // carried over by the warp that handed the tile off
+    if (active && step0 == 0) record(0, A_U);
+    int step = step0;
+    if (mc.rannacher && step0 == 0) {
       // solve_rannacher_startup (pde_solver.hpp:413-447): two implicit Euler
       // half steps with coefficient dt/2 to t + dt/2 and t + dt.
       const double t_mid = 0.0 + 0.5 * dt;
@@ -780,7 +845,39 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
       step = 1;
       if (active && nt >= 1) record(1, A_U);
     }
+    bool moved = false;
     for (; step < td.nt; ++step) {
+      if (ho && step > step0 && (step - step0) % kHoSegment == 0 && td.nt - step >= kHoMinLeft) {
+        // a warp waits for work: hand it this tile's remaining steps
+        int hand = 0;
+        if (lane == 0 && !mc.ho_moved[t]) {
+          volatile int* ctl = mc.ho_ctl;
+          if (ctl[0] > ctl[1]) {
+            const int s = atomicAdd(&mc.ho_ctl[1], 1);
+            if (s < mc.ho_cap) {
+              if (s < ctl[0])
+                hand = s + 1;
+              else
+                atomicCAS(&mc.ho_slot[s], kHoEmpty, kHoSkip);
+            }
+          }
+        }
+        hand = __shfl_sync(0xffffffffu, hand, 0);
+        if (hand) {
+          if (active) status[k] = st;
+          __threadfence();
+          __syncwarp();
+          int ok = 0;
+          if (lane == 0) {
+            mc.ho_moved[t] = 1;
+            ok = atomicCAS(&mc.ho_slot[hand - 1], kHoEmpty, ho_item(t, step)) == kHoEmpty;
+          }
+          if (__shfl_sync(0xffffffffu, ok, 0)) {
+            moved = true;
+            break;
+          }
+        }
+      }
       const bool live = active && step < nt && st == kStatusOk;
       // Time points are i*dt (time_domain.hpp:120-128).
       const double t = static_cast<double>(step) * dt;
@@ -793,7 +890,9 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
                           mc.beta, A_G, last ? A_G : A_U, st, flo, fhi, plo, phi, R, memo2, cflo, cfhi, cexact);
       if (live && sc) record(step + 1, last ? A_G : A_U);
     }
+    if (moved) return;  // the tile goes on elsewhere; this warp leaves
     if (active) status[k] = st;
+    ho_done();
   }
 }
 

@@ -118,6 +118,18 @@ struct MarchConst {
   int32_t nsmid = 0;                  // entries of sm_index
   int32_t nbins = 0;
   uint8_t* tile_done = nullptr;
+  // Hand-off of a tile's remaining steps (non-binned thread-march launches
+  // without snapshots), or ho_ctl = null: a warp whose queue ran dry waits on
+  // a claimed slot (ho_ctl[0] counts the claims); a marching warp that sees a
+  // claim not yet served (ho_ctl[0] > ho_ctl[1]) takes a slot (ho_ctl[1]),
+  // stores its tile and next step there and leaves, so that the tiles of a
+  // sub-partition holding four warps end on one holding fewer.  ho_ctl[2]
+  // counts the tiles finished or skipped; waiting warps leave once it reaches
+  // ntiles.  A tile moves at most once (ho_moved).
+  int* ho_ctl = nullptr;
+  unsigned long long* ho_slot = nullptr;
+  uint8_t* ho_moved = nullptr;
+  int32_t ho_cap = 0;
 };
 
 // Per-option data of the time-varying march, indexed by sorted index minus

@@ -143,6 +143,28 @@ def test_chunked_batch_matches_resident_batch(engine, pkg, n):
     assert np.array_equal(again["value"], out["value"])
 
 
+def test_tile_handoff_does_not_change_results(engine, pkg, monkeypatch):
+    """The thread march hands a tile's remaining steps to a warp whose queue
+    ran dry (the tile's state is in device memory between steps): 65,536
+    options at 101 x 498, where the sub-partitions holding four warps hand
+    tiles to those that finished, price bit for bit as with the hand-off
+    off."""
+    rng = np.random.default_rng(77)
+    n = 65536
+    p = pkg.pricing_array(100.0, rng.uniform(80, 120, n), rng.uniform(0.1, 2.0, n), rng.uniform(0.1, 0.5, n),
+                          rng.uniform(0.0, 0.08, n), rng.uniform(0.0, 0.04, n), (np.arange(n) % 2 == 0))
+    grid = pkg.grid_array(1, pkg.GRID_FIXED_N, 101, 498)
+    res = {}
+    for ho in ("0", "1"):
+        monkeypatch.setenv("MANGO_GPU_HANDOFF", ho)
+        b = engine.batch(p, grid)
+        b.run()
+        res[ho] = b.results()
+        b.close()
+    for k in ("value", "delta", "gamma", "theta", "status"):
+        assert np.array_equal(res["0"][k], res["1"][k]), k
+
+
 def test_value_at_vs_reference(engine, pkg):
     """AmericanOptionResult::value_at at other spots (tests/golden/value_at.npz:
     below, inside and above each grid), through the resident batch."""

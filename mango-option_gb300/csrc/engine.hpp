@@ -89,7 +89,7 @@ void set_err(MangoError* err, int32_t code, const std::string& msg);
 
 // Device buffers of one FDM IV working set (iv.cu), kept per level in the
 // context between solves.
-constexpr int kIvWorkBufs = 19;
+constexpr int kIvWorkBufs = 20;
 
 }  // namespace mgpu
 

@@ -792,7 +792,7 @@ struct WorkSet {
   std::vector<int32_t> map_h, src_h, pt_h, qlist_h, qbase_h;
   std::vector<TileDev> tiles_h;
   DevBuf d_tiles, d_opts, d_xs, d_map, d_src, d_pt, d_qlist, d_qbase, d_sigma, d_active, d_pool,
-      d_flags, d_mode, d_status, d_out4, d_tv, d_tpool, d_wt, d_twarp;
+      d_flags, d_mode, d_status, d_out4, d_tv, d_tpool, d_wt, d_twarp, d_ho;
   // First slot of a time-varying quote (slots follow the batch order, where
   // those quotes come last), or INT32_MAX.
   int32_t tv_first = 0x7fffffff;
@@ -804,7 +804,7 @@ struct WorkSet {
   std::array<DevBuf*, kIvWorkBufs> bufs() {
     return {&d_tiles, &d_opts, &d_xs, &d_map, &d_src, &d_pt, &d_qlist, &d_qbase, &d_sigma,
             &d_active, &d_pool, &d_flags, &d_mode, &d_status, &d_out4, &d_tv, &d_tpool, &d_wt,
-            &d_twarp};
+            &d_twarp, &d_ho};
   }
   void borrow(DevBuf* h) {
     home = h;
@@ -1240,10 +1240,25 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
                                                                w.d_pool.as<double>(),
                                                                w.d_flags.as<uint8_t>(),
                                                                w.d_mode.as<int32_t>(), mc);
-            if (nwt < ntiles)
+            if (nwt < ntiles) {
+              // tile hand-off (march.cuh), as in the pricing batch's launch
+              MarchConst mh = mc;
+              const char* he = std::getenv("MANGO_GPU_HANDOFF");
+              if (!(he && he[0] == '0')) {
+                const int cap = 4 * ntiles + 1024;
+                const size_t bytes = 16 + sizeof(unsigned long long) * static_cast<size_t>(cap) +
+                                     static_cast<size_t>(ntiles);
+                char* h = static_cast<char*>(w.d_ho.get(bytes));
+                check(cudaMemsetAsync(h, 0, bytes, st), "memset hand-off");
+                mh.ho_ctl = reinterpret_cast<int*>(h);
+                mh.ho_slot = reinterpret_cast<unsigned long long*>(h + 16);
+                mh.ho_moved = reinterpret_cast<uint8_t*>(h + 16 + sizeof(unsigned long long) * cap);
+                mh.ho_cap = cap;
+              }
               march_kernel<<<blocks, 128, 0, st>>>(tiles, ntiles, wopts, w.d_pool.as<double>(),
                                                    w.d_flags.as<uint8_t>(), w.d_mode.as<int32_t>(),
-                                                   w.d_status.as<int32_t>(), queue, mc);
+                                                   w.d_status.as<int32_t>(), queue, mh);
+            }
             wmarch_launch(st, ctx->num_sms, tiles, w.d_wt.as<int32_t>(), nwt, wopts,
                           w.d_pool.as<double>(), w.d_flags.as<uint8_t>(), w.d_mode.as<int32_t>(),
                           w.d_status.as<int32_t>(), b->d_queue.as<int>() + 3, mc, plan.R);

@@ -681,7 +681,11 @@ __device__ __forceinline__ double right_bc(const OptDev& o, double t) {
 constexpr unsigned long long kHoEmpty = 0, kHoSkip = 1, kHoAbandon = 2;
 constexpr int kHoSegment = 16;    // steps between a marching warp's checks
 constexpr int kHoMinLeft = 32;    // steps a tile must have left to move
-constexpr int kHoPolls = 1 << 22; // a waiting warp's polls (500 ns apart) before it leaves
+// A waiting warp's polls (500 ns apart) before it leaves: about 8-16 ms, a
+// few hand-off checks of the marching warps; a warp that leaves frees its
+// block's resources for a launch queued behind this one (the chunks of a
+// large one-shot batch).
+constexpr int kHoPolls = 1 << 14;
 
 __device__ __forceinline__ unsigned long long ho_item(int t, int step) {
   return (static_cast<unsigned long long>(t + 1) << 32) | static_cast<unsigned>(step);

@@ -1254,6 +1254,7 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
                 mh.ho_slot = reinterpret_cast<unsigned long long*>(h + 16);
                 mh.ho_moved = reinterpret_cast<uint8_t*>(h + 16 + sizeof(unsigned long long) * cap);
                 mh.ho_cap = cap;
+                mh.ho_total = ntiles;
               }
               march_kernel<<<blocks, 128, 0, st>>>(tiles, ntiles, wopts, w.d_pool.as<double>(),
                                                    w.d_flags.as<uint8_t>(), w.d_mode.as<int32_t>(),

@@ -707,7 +707,7 @@ __device__ unsigned long long ho_take(const MarchConst& mc, int ntiles) {
         __threadfence();
         return v;
       }
-      if (ctl[2] >= ntiles || it >= kHoPolls) {
+      if (ctl[2] >= mc.ho_total || it >= kHoPolls) {
         const unsigned long long old = atomicCAS(&mc.ho_slot[s], kHoEmpty, kHoAbandon);
         if (old > kHoAbandon) {
           __threadfence();
@@ -757,7 +757,7 @@ __global__ void __launch_bounds__(128, 4) march_kernel(
       } else {
         t = ntiles;
       }
-      if (ho && t >= ntiles) {
+      if (ho && (t < 0 || t >= ntiles)) {
         // the queue ran dry: wait for a tile another warp hands off
         queue_dry = true;
         const unsigned long long v = ho_take(mc, ntiles);

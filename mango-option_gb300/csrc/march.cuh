@@ -130,6 +130,7 @@ struct MarchConst {
   unsigned long long* ho_slot = nullptr;
   uint8_t* ho_moved = nullptr;
   int32_t ho_cap = 0;
+  int32_t ho_total = 0;  // tiles this launch finishes or skips (its ntiles)
 };
 
 // Per-option data of the time-varying march, indexed by sorted index minus

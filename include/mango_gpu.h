@@ -285,7 +285,7 @@ enum {
  * most 3e-6 in volatility, at that step's end (a volatility-space stop: the
  * error left is that step times the relative change of the slope over it),
  * or, where the objective is flat, on the reference's test |V - P| <
- * brent_tol_abs.  A quote not settled after 4 own-grid evaluations, or whose
+ * brent_tol_abs.  A quote not settled after 6 own-grid evaluations, or whose
  * slope is not positive, goes on with the k-section finder of
  * MANGO_GPU_IV_SECANT inside what Newton has bracketed (settling at |V - P|
  * below 1e-7 times the slope, or a bracket narrower than 1e-7, or, where two

@@ -148,7 +148,7 @@ struct IvDev {
 // or leave the exercise region.  Larger unverified steps (a Newton step from
 // a single evaluation) were measured to miss by up to 2e-6 across such jumps.
 constexpr int kCoarseEvals = 2;
-constexpr int kOwnEvals = 4;
+constexpr int kOwnEvals = 6;
 constexpr double kSecantAccept = 3e-6;
 // Below this vega (per unit volatility, relative to max(1, price)) the
 // objective is flat: the volatility is not determined by the price, and the

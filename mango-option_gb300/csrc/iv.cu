@@ -1167,17 +1167,28 @@ MangoStatus solve_iv(MangoGpuContext* ctx, const MangoIvQuery* queries, uint64_t
           // them again by type and ln(S/K) / (sigma sqrt(T)) at their next
           // trial point, so that the lanes of a tile meet the obstacle at
           // similar rows (as the pricing batch's sort arranges).
+          // (keys computed once per quote, not per comparison)
           const OptDev* ho = b->h_opts.as<OptDev>();
-          auto key = [&](int32_t q) {
-            const double sg = hsig1[q] > 0.0 ? hsig1[q] : 0.2;
-            return std::log(ho[q].spot / ho[q].strike) / (sg * std::sqrt(mat[q]));
+          struct TailKey {
+            int32_t put;
+            double k;
+            int32_t q;
           };
-          for (auto& l : lists)
-            std::sort(l.begin(), l.end(), [&](int32_t a, int32_t c) {
-              if (ho[a].is_put != ho[c].is_put) return ho[a].is_put < ho[c].is_put;
-              const double ka = key(a), kc = key(c);
-              return ka != kc ? ka < kc : a < c;
+          std::vector<TailKey> keys;
+          for (auto& l : lists) {
+            keys.resize(l.size());
+            for (size_t j = 0; j < l.size(); ++j) {
+              const int32_t q = l[j];
+              const double sg = hsig1[q] > 0.0 ? hsig1[q] : 0.2;
+              keys[j] = TailKey{ho[q].is_put,
+                                std::log(ho[q].spot / ho[q].strike) / (sg * std::sqrt(mat[q])), q};
+            }
+            std::sort(keys.begin(), keys.end(), [](const TailKey& a, const TailKey& c) {
+              if (a.put != c.put) return a.put < c.put;
+              return a.k != c.k ? a.k < c.k : a.q < c.q;
             });
+            for (size_t j = 0; j < l.size(); ++j) l[j] = keys[j].q;
+          }
         }
         if (!lists[kLevelPlain].empty()) grids_ready();
         int64_t nq_all = 0;
